@@ -1,0 +1,166 @@
+/* stablercwa_gb300.h -- C ABI of the GB300 RCWA solve engine (libstablercwa_gb300.so).
+ *
+ * The engine is a drop-in for StableRCWA's solve path. Every entry point below names the
+ * StableRCWA interface it replaces (paths are relative to the StableRCWA project root).
+ *
+ * Conventions
+ *   - Plain C types only: pointers, sizes, doubles. Complex numbers are rcwa_complex, laid out as
+ *     two doubles {re, im} (the layout of std::complex<double> and cuDoubleComplex).
+ *   - Matrices are column-major (element (i, j) at [i + j*rows]), batches are contiguous.
+ *   - Return value of every call: RCWA_OK (0) or a negative RCWA_E* code. A negative code means the
+ *     call did no work (invalid argument, CUDA error); the message is read with rcwa_gpu_last_error.
+ *     Invalid input is rejected exactly where the reference throws std::invalid_argument
+ *     (include/stablercwa/rcwa1d.hpp:191-229).
+ *   - Numerical failures are per sample, never a call failure: the sample's R/T/DEr/DEt are NaN and
+ *     its status word says why, as the reference fills NaN on NumericalFailure
+ *     (include/stablercwa/rcwa1d.hpp:1064-1067, :810-816).
+ *   - Host-pointer calls copy inputs to the device and results back inside the call. *_dev calls take
+ *     device pointers and leave everything resident in device memory (inputs already in HBM).
+ *   - A context is internally synchronised: calls from several host threads serialise on it.
+ */
+#ifndef STABLERCWA_GB300_H
+#define STABLERCWA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RCWA_GB300_ABI_VERSION 1
+
+/* call status */
+#define RCWA_OK 0
+#define RCWA_EINVAL (-1)       /* invalid argument: the reference throws std::invalid_argument */
+#define RCWA_ECUDA (-2)        /* CUDA runtime error (no device, launch failure, ...) */
+#define RCWA_ENOMEM (-3)       /* device allocation failed */
+#define RCWA_EUNSUPPORTED (-4) /* option value the engine does not implement */
+
+/* per-sample status word */
+#define RCWA_SAMPLE_OK 0
+#define RCWA_SAMPLE_NUMERICAL 1      /* zero pivot / non-finite value: results are NaN */
+#define RCWA_SAMPLE_EIG_NOCONV 2     /* an eigensolve hit max_iter: results NaN, eig_info set */
+
+#define RCWA_TE 0
+#define RCWA_TM 1
+
+typedef struct rcwa_complex {
+    double re, im;
+} rcwa_complex;
+
+/* One layer (include/stablercwa/rcwa1d.hpp:80-106). homogeneous != 0: a uniform film of index n.
+ * Otherwise a grating: n_segments indices n_values[K] and K+1 strictly increasing edges spanning one
+ * period. fourier_method 0 = analytic coefficients (the reference default). */
+typedef struct rcwa_layer1d {
+    double d;
+    int homogeneous;
+    rcwa_complex n;
+    int n_segments;
+    const double* edges;
+    const rcwa_complex* n_values;
+    int fourier_method;
+    int fft_samples;
+} rcwa_layer1d;
+
+/* Top to bottom: incident medium nI, layers, exit medium nII (include/stablercwa/rcwa1d.hpp:109-114). */
+typedef struct rcwa_stack1d {
+    rcwa_complex nI;
+    rcwa_complex nII;
+    double period;
+    int n_layers;
+    const rcwa_layer1d* layers;
+} rcwa_stack1d;
+
+/* One sweep point (include/stablercwa/rcwa1d.hpp:139). */
+typedef struct rcwa_point1d {
+    double wavelength;
+    double theta_deg;
+} rcwa_point1d;
+
+/* Solve options (include/stablercwa/rcwa1d.hpp:116-137, include/stablercwa/eig_types.hpp:25-31).
+ * The engine implements eig = QR, linear = LU with partial pivoting and the homogeneous fast path;
+ * other values return RCWA_EUNSUPPORTED. rcwa_options_default fills the reference defaults. */
+typedef struct rcwa_options {
+    int eig_method;            /* 0 = QR (EigMethod::QR) */
+    int linear_solver;         /* 0 = LU with partial pivoting (LinearSolver::LUPartial) */
+    int homogeneous_fast_path; /* 1 (default) */
+    int diagnostics;           /* 1: fill max_eig_residual per sample */
+    int eig_max_iter;          /* 30 */
+    double eig_eps;            /* DBL_EPSILON */
+} rcwa_options;
+
+/* Batched 1-D results; every array is caller-allocated with n_points rows of n = 2M+1 orders
+ * (point p, order m at [p*n + m + M]) or n_points entries (include/stablercwa/rcwa1d.hpp:145-164).
+ * Optional arrays may be NULL. */
+typedef struct rcwa_result1d {
+    rcwa_complex* R;
+    rcwa_complex* T;
+    double* DEr;
+    double* DEt;
+    int* status;               /* RCWA_SAMPLE_* */
+    int* eig_info;             /* optional */
+    int* n_eig;                /* optional */
+    int* n_dense_solve;        /* optional */
+    double* max_eig_residual;  /* optional, filled when options.diagnostics */
+} rcwa_result1d;
+
+typedef struct rcwa_gpu_config {
+    int device;                /* CUDA device ordinal */
+    size_t workspace_limit;    /* bytes of device workspace the context may hold; 0 = 8 GiB */
+} rcwa_gpu_config;
+
+typedef struct rcwa_gpu_ctx rcwa_gpu_ctx;
+
+int rcwa_gpu_abi_version(void);
+void rcwa_options_default(rcwa_options* options);
+
+/* Context lifetime. No reference counterpart: the reference keeps no state between calls
+ * (include/stablercwa/rcwa1d.hpp:851); the context owns the device workspace and stream. */
+int rcwa_gpu_create(const rcwa_gpu_config* config, rcwa_gpu_ctx** ctx);
+void rcwa_gpu_destroy(rcwa_gpu_ctx* ctx);
+/* Copies the last error message of this context (or of a failed create when ctx is NULL). */
+int rcwa_gpu_last_error(const rcwa_gpu_ctx* ctx, char* buffer, size_t size);
+
+/* Batched 1-D TE/TM solve over sweep points on one stack: replaces rcwa::sweep
+ * (include/stablercwa/rcwa1d.hpp:1084-1091) and, with n_points = 1, rcwa::solve
+ * (include/stablercwa/rcwa1d.hpp:1077-1080). Host buffers in and out. */
+int rcwa_gpu_solve1d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point1d* points,
+                           int n_points, int M, int polarization, const rcwa_options* options,
+                           rcwa_result1d* out);
+
+/* Same solve with device-resident sweep points and device-resident result arrays (every pointer in
+ * out is a device pointer). The stack description is host memory. Asynchronous with respect to the
+ * host on the context's stream; rcwa_gpu_synchronize waits for it. */
+int rcwa_gpu_solve1d_batch_dev(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point1d* d_points,
+                               int n_points, int M, int polarization, const rcwa_options* options,
+                               rcwa_result1d* d_out);
+int rcwa_gpu_synchronize(rcwa_gpu_ctx* ctx);
+
+/* Batched general complex eigensolver, CORTH + COMQR2 (include/stablercwa/eig_qr.hpp:1008-1124):
+ * the engine behind Options::custom_eig (include/stablercwa/rcwa1d.hpp:122-124). a holds batch
+ * n x n matrices; values[batch*n], vectors[batch*n*n] (2-norm normalised columns), info[batch]
+ * (0 or the 1-based index of the eigenvalue that hit max_iter), sweeps[batch] (may be NULL). */
+int rcwa_gpu_eig_batch(rcwa_gpu_ctx* ctx, int n, int batch, const rcwa_complex* a, double eps, int max_iter,
+                       rcwa_complex* values, rcwa_complex* vectors, int* info, int* sweeps);
+int rcwa_gpu_eig_batch_dev(rcwa_gpu_ctx* ctx, int n, int batch, const rcwa_complex* d_a, double eps,
+                           int max_iter, rcwa_complex* d_values, rcwa_complex* d_vectors, int* d_info,
+                           int* d_sweeps);
+
+/* Batched A X = B with partial-pivot LU (include/stablercwa/lu.hpp:427-436): the engine behind
+ * Options::custom_solve (include/stablercwa/rcwa1d.hpp:130-136). a: batch n x n, b: batch n x nrhs,
+ * x: batch n x nrhs. singular[batch] is 1 where a zero pivot appeared (the reference throws
+ * std::runtime_error there); x is then NaN. */
+int rcwa_gpu_solve_batch(rcwa_gpu_ctx* ctx, int n, int nrhs, int batch, const rcwa_complex* a,
+                         const rcwa_complex* b, rcwa_complex* x, int* singular);
+
+/* Batched C = A B (include/stablercwa/matrix.hpp:170-192): the engine behind
+ * Options::custom_multiply (include/stablercwa/rcwa1d.hpp:125-129). a: batch m x k, b: batch k x n. */
+int rcwa_gpu_multiply_batch(rcwa_gpu_ctx* ctx, int m, int k, int n, int batch, const rcwa_complex* a,
+                            const rcwa_complex* b, rcwa_complex* c);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* STABLERCWA_GB300_H */

@@ -1,0 +1,177 @@
+// oracle_capi.cpp -- C entry points of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+//
+// Built into oracle/_build/liboracle.so by oracle/build.py. Loaded by tests/ (as the parity
+// checker), by __graft_entry__.smoke() and by bench.py's CPU-baseline leg; never by the engine.
+// The structs are the engine's public C ABI (include/stablercwa_gb300.h), so both sides read the
+// same inputs.
+#include <atomic>
+#include <mutex>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../include/stablercwa_gb300.h"
+#include "oracle_rcwa1d.hpp"
+
+using namespace oracle;
+
+namespace {
+
+cplx C(rcwa_complex z) { return {z.re, z.im}; }
+rcwa_complex R(cplx z) { return {z.real(), z.imag()}; }
+
+void put_error(char* err, size_t len, const std::string& msg) {
+    if (!err || len == 0) return;
+    std::strncpy(err, msg.c_str(), len - 1);
+    err[len - 1] = '\0';
+}
+
+Stack1D to_stack(const rcwa_stack1d* s) {
+    Stack1D out;
+    out.nI = C(s->nI);
+    out.nII = C(s->nII);
+    out.period = s->period;
+    for (int k = 0; k < s->n_layers; ++k) {
+        const rcwa_layer1d& L = s->layers[k];
+        Layer1D l;
+        l.d = L.d;
+        l.homogeneous = L.homogeneous != 0;
+        l.n = C(L.n);
+        if (!l.homogeneous) {
+            for (int j = 0; j <= L.n_segments; ++j) l.edges.push_back(L.edges[j]);
+            for (int j = 0; j < L.n_segments; ++j) l.n_values.push_back(C(L.n_values[j]));
+        }
+        out.layers.push_back(std::move(l));
+    }
+    return out;
+}
+
+Mat to_mat(const rcwa_complex* p, int rows, int cols) {
+    Mat m(rows, cols);
+    for (std::size_t k = 0; k < m.a.size(); ++k) m.a[k] = C(p[k]);
+    return m;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Batched 1-D solve on the CPU: rcwa::sweep semantics (include/stablercwa/rcwa1d.hpp:1084-1091),
+// points split over n_threads std::threads. Returns 0, or -1 with a message for invalid input.
+int oracle_solve1d_batch(const rcwa_stack1d* stack, const rcwa_point1d* points, int n_points, int M, int pol,
+                         int diagnostics, rcwa_result1d* out, int n_threads, char* err, size_t err_len) {
+    Stack1D s;
+    try {
+        s = to_stack(stack);
+    } catch (...) {
+        put_error(err, err_len, "oracle: bad stack");
+        return -1;
+    }
+    const int n = 2 * M + 1;
+    std::atomic<int> next{0};
+    std::atomic<int> failed{0};
+    std::string first_error;
+    std::mutex error_lock;
+    const auto worker = [&]() {
+        for (;;) {
+            const int p = next.fetch_add(1);
+            if (p >= n_points) return;
+            try {
+                const Result1D r = solve1d(s, points[p].wavelength, points[p].theta_deg, M, pol, diagnostics != 0);
+                for (int j = 0; j < n; ++j) {
+                    out->R[static_cast<std::size_t>(p) * n + j] = R(r.R[j]);
+                    out->T[static_cast<std::size_t>(p) * n + j] = R(r.T[j]);
+                    out->DEr[static_cast<std::size_t>(p) * n + j] = r.DEr[j];
+                    out->DEt[static_cast<std::size_t>(p) * n + j] = r.DEt[j];
+                }
+                if (out->status) out->status[p] = !r.failed ? RCWA_SAMPLE_OK : (r.eig_info ? RCWA_SAMPLE_EIG_NOCONV : RCWA_SAMPLE_NUMERICAL);
+                if (out->eig_info) out->eig_info[p] = r.eig_info;
+                if (out->n_eig) out->n_eig[p] = r.n_eig;
+                if (out->n_dense_solve) out->n_dense_solve[p] = r.n_dense_solve;
+                if (out->max_eig_residual) out->max_eig_residual[p] = r.max_eig_residual;
+            } catch (const InvalidArgument& e) {
+                std::lock_guard<std::mutex> hold(error_lock);
+                if (failed.fetch_add(1) == 0) first_error = e.what;
+            }
+        }
+    };
+    if (n_threads <= 1) {
+        worker();
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < n_threads; ++t) pool.emplace_back(worker);
+        for (std::thread& t : pool) t.join();
+    }
+    if (failed.load()) {
+        put_error(err, err_len, first_error);
+        return -1;
+    }
+    return 0;
+}
+
+// One eigensolve (include/stablercwa/eig_qr.hpp:1008-1124). vectors may be NULL.
+int oracle_eig(int n, const rcwa_complex* a, double eps, int max_iter, rcwa_complex* values, rcwa_complex* vectors,
+               int* info, int* sweeps) {
+    const EigOut r = eig_qr(to_mat(a, n, n), eps, max_iter, vectors != nullptr);
+    for (int j = 0; j < n; ++j) values[j] = R(r.values[j]);
+    if (vectors && r.info == 0)
+        for (std::size_t k = 0; k < r.vectors.a.size(); ++k) vectors[k] = R(r.vectors.a[k]);
+    if (info) *info = r.info;
+    if (sweeps) *sweeps = r.sweeps;
+    return 0;
+}
+
+// Schur form with the accumulated transform: Z^H A Z = T (keep_transform in include/stablercwa/eig_qr.hpp:1106-1122).
+int oracle_schur(int n, const rcwa_complex* a, rcwa_complex* z, rcwa_complex* t, int* info) {
+    const EigOut r = eig_qr(to_mat(a, n, n), kEps, 30, false, true);
+    for (std::size_t k = 0; k < r.Z.a.size(); ++k) z[k] = R(r.Z.a[k]);
+    for (std::size_t k = 0; k < r.T.a.size(); ++k) t[k] = R(r.T.a[k]);
+    if (info) *info = r.info;
+    return 0;
+}
+
+// A X = B with partial-pivot LU (include/stablercwa/lu.hpp:427-436); singular -> 1 and X untouched.
+int oracle_solve(int n, int nrhs, const rcwa_complex* a, const rcwa_complex* b, rcwa_complex* x, int* singular) {
+    const LUF f = lu_factor(to_mat(a, n, n));
+    if (singular) *singular = f.singular ? 1 : 0;
+    if (f.singular) return 0;
+    const Mat s = lu_solve(f, to_mat(b, n, nrhs));
+    for (std::size_t k = 0; k < s.a.size(); ++k) x[k] = R(s.a[k]);
+    return 0;
+}
+
+// C = A B (include/stablercwa/matrix.hpp:170-192)
+int oracle_multiply(int m, int k, int n, const rcwa_complex* a, const rcwa_complex* b, rcwa_complex* c) {
+    const Mat r = matmul(to_mat(a, m, k), to_mat(b, k, n));
+    for (std::size_t q = 0; q < r.a.size(); ++q) c[q] = R(r.a[q]);
+    return 0;
+}
+
+// Relative eigen-pair residual (include/stablercwa/eig.hpp:38-69)
+double oracle_eig_residual(int n, const rcwa_complex* a, const rcwa_complex* values, const rcwa_complex* vectors) {
+    CVec w(n);
+    for (int j = 0; j < n; ++j) w[j] = C(values[j]);
+    return eig_residual(to_mat(a, n, n), w, to_mat(vectors, n, n));
+}
+
+// TE/TM layer matrix the solve hands to the eigensolver (include/stablercwa/rcwa1d.hpp:1098-1110).
+int oracle_layer_matrix(const rcwa_layer1d* layer, double period, double wavelength, double nI, double theta_deg,
+                        int M, int pol, rcwa_complex* a) {
+    rcwa_stack1d st{};
+    st.period = period;
+    st.n_layers = 1;
+    st.layers = layer;
+    const Stack1D s = to_stack(&st);
+    const CVec kx = r1::transverse_wavevectors(nI, theta_deg, wavelength, period, M);
+    r1::Work w;
+    try {
+        const r1::LayerOp op = r1::assemble_layer(s.layers[0], period, kx, M, pol, w);
+        for (std::size_t k = 0; k < op.a.a.size(); ++k) a[k] = R(op.a.a[k]);
+    } catch (const r1::NumericalFailure&) {
+        return -1;
+    }
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,144 @@
+"""ctypes mirror of the engine's C ABI (include/stablercwa_gb300.h).
+
+The structs here are laid out exactly as the header declares them; marshal_stack1d turns the Python
+Stack/Layer description into an rcwa_stack1d that stays valid while the returned keep-alive tuple
+is referenced.
+"""
+import ctypes as C
+
+import numpy as np
+
+RCWA_OK = 0
+RCWA_EINVAL = -1
+RCWA_ECUDA = -2
+RCWA_ENOMEM = -3
+RCWA_EUNSUPPORTED = -4
+
+RCWA_SAMPLE_OK = 0
+RCWA_SAMPLE_NUMERICAL = 1
+RCWA_SAMPLE_EIG_NOCONV = 2
+
+RCWA_TE = 0
+RCWA_TM = 1
+
+
+class rcwa_complex(C.Structure):
+    _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+
+class rcwa_layer1d(C.Structure):
+    _fields_ = [
+        ("d", C.c_double),
+        ("homogeneous", C.c_int),
+        ("n", rcwa_complex),
+        ("n_segments", C.c_int),
+        ("edges", C.POINTER(C.c_double)),
+        ("n_values", C.POINTER(rcwa_complex)),
+        ("fourier_method", C.c_int),
+        ("fft_samples", C.c_int),
+    ]
+
+
+class rcwa_stack1d(C.Structure):
+    _fields_ = [
+        ("nI", rcwa_complex),
+        ("nII", rcwa_complex),
+        ("period", C.c_double),
+        ("n_layers", C.c_int),
+        ("layers", C.POINTER(rcwa_layer1d)),
+    ]
+
+
+class rcwa_point1d(C.Structure):
+    _fields_ = [("wavelength", C.c_double), ("theta_deg", C.c_double)]
+
+
+class rcwa_options(C.Structure):
+    _fields_ = [
+        ("eig_method", C.c_int),
+        ("linear_solver", C.c_int),
+        ("homogeneous_fast_path", C.c_int),
+        ("diagnostics", C.c_int),
+        ("eig_max_iter", C.c_int),
+        ("eig_eps", C.c_double),
+    ]
+
+
+class rcwa_result1d(C.Structure):
+    _fields_ = [
+        ("R", C.c_void_p),
+        ("T", C.c_void_p),
+        ("DEr", C.c_void_p),
+        ("DEt", C.c_void_p),
+        ("status", C.c_void_p),
+        ("eig_info", C.c_void_p),
+        ("n_eig", C.c_void_p),
+        ("n_dense_solve", C.c_void_p),
+        ("max_eig_residual", C.c_void_p),
+    ]
+
+
+class rcwa_gpu_config(C.Structure):
+    _fields_ = [("device", C.c_int), ("workspace_limit", C.c_size_t)]
+
+
+def cplx(z):
+    z = complex(z)
+    return rcwa_complex(z.real, z.imag)
+
+
+def marshal_stack1d(stack):
+    """Build an rcwa_stack1d from an object with nI, nII, period and layers (each layer with d,
+    homogeneous, n, edges, n_values). Returns (struct, keepalive)."""
+    keep = []
+    layers = (rcwa_layer1d * max(1, len(stack.layers)))()
+    for k, L in enumerate(stack.layers):
+        s = layers[k]
+        s.d = float(L.d)
+        s.homogeneous = 1 if L.homogeneous else 0
+        s.n = cplx(L.n if L.homogeneous else 1.0)
+        s.fourier_method = 0
+        s.fft_samples = 0
+        if not L.homogeneous:
+            e = np.ascontiguousarray(np.asarray(L.edges, dtype=np.float64))
+            v = np.ascontiguousarray(np.asarray(L.n_values, dtype=np.complex128))
+            keep += [e, v]
+            s.n_segments = len(v)
+            s.edges = e.ctypes.data_as(C.POINTER(C.c_double))
+            s.n_values = C.cast(v.ctypes.data, C.POINTER(rcwa_complex))
+        else:
+            s.n_segments = 0
+    st = rcwa_stack1d()
+    st.nI = cplx(stack.nI)
+    st.nII = cplx(stack.nII)
+    st.period = float(stack.period)
+    st.n_layers = len(stack.layers)
+    st.layers = C.cast(layers, C.POINTER(rcwa_layer1d))
+    keep.append(layers)
+    return st, keep
+
+
+def points_array(points):
+    """Sweep points as an (n, 2) float64 array of (wavelength, theta_deg)."""
+    p = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 2))
+    return p
+
+
+def result_views(n_points, M, with_diag=True):
+    """Host arrays for rcwa_result1d and the struct pointing at them."""
+    n = 2 * M + 1
+    arrays = {
+        "R": np.empty((n_points, n), np.complex128),
+        "T": np.empty((n_points, n), np.complex128),
+        "DEr": np.empty((n_points, n), np.float64),
+        "DEt": np.empty((n_points, n), np.float64),
+        "status": np.empty(n_points, np.int32),
+        "eig_info": np.empty(n_points, np.int32),
+        "n_eig": np.empty(n_points, np.int32),
+        "n_dense_solve": np.empty(n_points, np.int32),
+        "max_eig_residual": np.zeros(n_points, np.float64),
+    }
+    res = rcwa_result1d()
+    for name, arr in arrays.items():
+        setattr(res, name, arr.ctypes.data)
+    return res, arrays

@@ -1,0 +1,37 @@
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); runs the engine's kernels")
+
+
+def load_jsonl(name):
+    with open(os.path.join(GOLDEN, name)) as f:
+        return [json.loads(line) for line in f if line.strip()]
+
+
+def cvec(v):
+    return np.array([complex(float(a), float(b)) for a, b in v], dtype=np.complex128)
+
+
+def rvec(v):
+    return np.array([float(x) for x in v], dtype=np.float64)
+
+
+@pytest.fixture(scope="session")
+def cases1d():
+    return load_jsonl("rcwa1d_cases.jsonl")
+
+
+@pytest.fixture(scope="session")
+def eig_cases():
+    return load_jsonl("eig_cases.jsonl")
