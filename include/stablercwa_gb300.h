@@ -114,6 +114,9 @@ typedef struct rcwa_gpu_ctx rcwa_gpu_ctx;
 
 int rcwa_gpu_abi_version(void);
 void rcwa_options_default(rcwa_options* options);
+/* Number of engine kernels launched by this process so far (all contexts). No reference
+ * counterpart; it lets a caller count the device launches of a call. */
+long long rcwa_gpu_launch_count(void);
 
 /* Context lifetime. No reference counterpart: the reference keeps no state between calls
  * (include/stablercwa/rcwa1d.hpp:851); the context owns the device workspace and stream. */

@@ -1,0 +1,318 @@
+// capi.cu -- the C ABI of libstablercwa_gb300.so (declared in include/stablercwa_gb300.h).
+//
+// Every entry point validates its arguments the way the reference does before any work, runs on
+// the context's stream under the context's lock, and turns engine errors into return codes with a
+// message kept in the context.
+#include <cfloat>
+#include <cmath>
+#include <complex>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+
+struct rcwa_gpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex lock;
+    std::string last_error;
+    size_t workspace_limit = 0;
+};
+
+namespace {
+
+using namespace rcwa_gb300;
+
+std::mutex g_create_lock;
+std::string g_create_error;
+
+int fail(rcwa_gpu_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return code;
+}
+
+template <class F>
+int guarded(rcwa_gpu_ctx* ctx, F&& body) {
+    if (!ctx) return RCWA_EINVAL;
+    std::lock_guard<std::mutex> hold(ctx->lock);
+    try {
+        RCWA_CUDA(cudaSetDevice(ctx->device));
+        body();
+        return RCWA_OK;
+    } catch (const EngineError& e) {
+        return fail(ctx, e.code, e.message);
+    } catch (const std::bad_alloc&) {
+        return fail(ctx, RCWA_ENOMEM, "host allocation failed");
+    }
+}
+
+Options to_options(const rcwa_options* o) {
+    Options opt;
+    if (!o) return opt;
+    if (o->eig_method != 0) throw EngineError{RCWA_EUNSUPPORTED, "rcwa: only the QR eigensolver (EigMethod::QR) is implemented"};
+    if (o->linear_solver != 0)
+        throw EngineError{RCWA_EUNSUPPORTED, "rcwa: only partial-pivot LU (LinearSolver::LUPartial) is implemented"};
+    if (!o->homogeneous_fast_path)
+        throw EngineError{RCWA_EUNSUPPORTED, "rcwa: homogeneous_fast_path = false is not implemented"};
+    if (o->eig_max_iter < 1) throw EngineError{RCWA_EINVAL, "eig_qr: max_iter must be >= 1"};
+    if (!(o->eig_eps >= 0.0) || !std::isfinite(o->eig_eps)) throw EngineError{RCWA_EINVAL, "eig_qr: eps must be finite and >= 0"};
+    opt.diagnostics = o->diagnostics != 0;
+    opt.max_iter = o->eig_max_iter;
+    opt.eps = o->eig_eps;
+    if (const char* g = std::getenv("RCWA_GB300_EIG_GROUP")) opt.eig_group = std::atoi(g);
+    return opt;
+}
+
+size_t chunk_bytes(const rcwa_gpu_ctx* ctx) {
+    if (ctx->workspace_limit) return ctx->workspace_limit;
+    size_t free_b = 0, total = 0;
+    if (cudaMemGetInfo(&free_b, &total) != cudaSuccess) return size_t(8) << 30;
+    return std::min<size_t>(free_b / 2, size_t(48) << 30);
+}
+
+void check_result_ptrs(const rcwa_result1d* out) {
+    if (!out || !out->R || !out->T || !out->DEr || !out->DEt)
+        throw EngineError{RCWA_EINVAL, "rcwa: result arrays R, T, DEr, DEt are required"};
+}
+
+template <class T>
+void copy_back(T* host, const T* dev, size_t count, cudaStream_t st) {
+    if (host && dev && count) RCWA_CUDA(cudaMemcpyAsync(host, dev, count * sizeof(T), cudaMemcpyDeviceToHost, st));
+}
+
+}  // namespace
+
+extern "C" {
+
+int rcwa_gpu_abi_version(void) { return RCWA_GB300_ABI_VERSION; }
+
+void rcwa_options_default(rcwa_options* o) {
+    if (!o) return;
+    o->eig_method = 0;
+    o->linear_solver = 0;
+    o->homogeneous_fast_path = 1;
+    o->diagnostics = 0;
+    o->eig_max_iter = 30;
+    o->eig_eps = DBL_EPSILON;
+}
+
+long long rcwa_gpu_launch_count(void) { return launch_count(); }
+
+int rcwa_gpu_create(const rcwa_gpu_config* config, rcwa_gpu_ctx** out) {
+    std::lock_guard<std::mutex> hold(g_create_lock);
+    if (!out) return RCWA_EINVAL;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        g_create_error = std::string("no CUDA device: ") + cudaGetErrorString(e);
+        return RCWA_ECUDA;
+    }
+    const int dev = config ? config->device : 0;
+    if (dev < 0 || dev >= count) {
+        g_create_error = "device ordinal out of range";
+        return RCWA_EINVAL;
+    }
+    auto* ctx = new rcwa_gpu_ctx();
+    ctx->device = dev;
+    ctx->workspace_limit = config ? config->workspace_limit : 0;
+    if ((e = cudaSetDevice(dev)) != cudaSuccess || (e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        g_create_error = cudaGetErrorString(e);
+        delete ctx;
+        return RCWA_ECUDA;
+    }
+    // keep stream-ordered allocations cached in the device pool between calls
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t threshold = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+    }
+    *out = ctx;
+    return RCWA_OK;
+}
+
+void rcwa_gpu_destroy(rcwa_gpu_ctx* ctx) {
+    if (!ctx) return;
+    {
+        std::lock_guard<std::mutex> hold(ctx->lock);
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        cudaStreamDestroy(ctx->stream);
+    }
+    delete ctx;
+}
+
+int rcwa_gpu_last_error(const rcwa_gpu_ctx* ctx, char* buffer, size_t size) {
+    if (!buffer || size == 0) return RCWA_EINVAL;
+    const std::string& msg = ctx ? ctx->last_error : g_create_error;
+    std::strncpy(buffer, msg.c_str(), size - 1);
+    buffer[size - 1] = '\0';
+    return RCWA_OK;
+}
+
+int rcwa_gpu_synchronize(rcwa_gpu_ctx* ctx) {
+    return guarded(ctx, [&] { RCWA_CUDA(cudaStreamSynchronize(ctx->stream)); });
+}
+
+int rcwa_gpu_solve1d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point1d* points, int n_points, int M,
+                           int polarization, const rcwa_options* options, rcwa_result1d* out) {
+    return guarded(ctx, [&] {
+        if (!stack || (n_points > 0 && !points) || n_points < 0) throw EngineError{RCWA_EINVAL, "rcwa: null argument"};
+        check_result_ptrs(out);
+        validate1d(*stack, points, n_points, M, polarization);
+        const Options opt = to_options(options);
+        if (n_points == 0) return;
+        const cudaStream_t st = ctx->stream;
+        const int n = 2 * M + 1;
+        // s = nI sin(theta) with the host libm, the reference's own expression (rcwa1d.hpp:411)
+        std::vector<double> hs(n_points), hw(n_points);
+        const double kPi = 3.141592653589793238462643383279502884;
+        for (int p = 0; p < n_points; ++p) {
+            hs[p] = stack->nI.re * std::sin(points[p].theta_deg * kPi / 180.0);
+            hw[p] = points[p].wavelength;
+        }
+        DeviceScratch mem(st);
+        double* ds = mem.get<double>(n_points);
+        double* dw = mem.get<double>(n_points);
+        RCWA_CUDA(cudaMemcpyAsync(ds, hs.data(), n_points * sizeof(double), cudaMemcpyHostToDevice, st));
+        RCWA_CUDA(cudaMemcpyAsync(dw, hw.data(), n_points * sizeof(double), cudaMemcpyHostToDevice, st));
+        const size_t nv = (size_t)n_points * n;
+        rcwa_result1d d{};
+        d.R = reinterpret_cast<rcwa_complex*>(mem.get<zc>(nv));
+        d.T = reinterpret_cast<rcwa_complex*>(mem.get<zc>(nv));
+        d.DEr = mem.get<double>(nv);
+        d.DEt = mem.get<double>(nv);
+        d.status = mem.get<int>(n_points);
+        d.eig_info = mem.get<int>(n_points);
+        d.n_eig = mem.get<int>(n_points);
+        d.n_dense_solve = mem.get<int>(n_points);
+        d.max_eig_residual = opt.diagnostics ? mem.zeros<double>(n_points) : nullptr;
+        solve1d_device(st, *stack, ds, dw, n_points, M, polarization, opt, d, chunk_bytes(ctx));
+        copy_back(out->R, d.R, nv, st);
+        copy_back(out->T, d.T, nv, st);
+        copy_back(out->DEr, d.DEr, nv, st);
+        copy_back(out->DEt, d.DEt, nv, st);
+        copy_back(out->status, d.status, n_points, st);
+        copy_back(out->eig_info, d.eig_info, n_points, st);
+        copy_back(out->n_eig, d.n_eig, n_points, st);
+        copy_back(out->n_dense_solve, d.n_dense_solve, n_points, st);
+        if (opt.diagnostics) copy_back(out->max_eig_residual, d.max_eig_residual, n_points, st);
+        RCWA_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int rcwa_gpu_solve1d_batch_dev(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point1d* d_points, int n_points,
+                               int M, int polarization, const rcwa_options* options, rcwa_result1d* d_out) {
+    return guarded(ctx, [&] {
+        if (!stack || (n_points > 0 && !d_points) || n_points < 0) throw EngineError{RCWA_EINVAL, "rcwa: null argument"};
+        check_result_ptrs(d_out);
+        validate1d(*stack, nullptr, 0, M, polarization);
+        const Options opt = to_options(options);
+        if (n_points == 0) return;
+        const cudaStream_t st = ctx->stream;
+        DeviceScratch mem(st);
+        double* ds = mem.get<double>(n_points);
+        double* dw = mem.get<double>(n_points);
+        if (!prepare_points_device(st, d_points, n_points, stack->nI.re, ds, dw))
+            throw EngineError{RCWA_EINVAL, "rcwa: every point needs a finite positive wavelength and |theta| < 90 degrees"};
+        solve1d_device(st, *stack, ds, dw, n_points, M, polarization, opt, *d_out, chunk_bytes(ctx));
+    });
+}
+
+int rcwa_gpu_eig_batch_dev(rcwa_gpu_ctx* ctx, int n, int batch, const rcwa_complex* d_a, double eps, int max_iter,
+                           rcwa_complex* d_values, rcwa_complex* d_vectors, int* d_info, int* d_sweeps) {
+    return guarded(ctx, [&] {
+        if (n < 0 || batch < 0) throw EngineError{RCWA_EINVAL, "eig: negative size"};
+        if (max_iter < 1) throw EngineError{RCWA_EINVAL, "eig_qr: max_iter must be >= 1"};
+        if (!(eps >= 0.0) || !std::isfinite(eps)) throw EngineError{RCWA_EINVAL, "eig_qr: eps must be finite and >= 0"};
+        if (n == 0 || batch == 0) return;
+        if (!d_a || !d_values || !d_vectors || !d_info) throw EngineError{RCWA_EINVAL, "eig: null argument"};
+        DeviceScratch mem(ctx->stream);
+        zc* ws = mem.get<zc>((size_t)(eig_workspace_bytes(n, batch) / sizeof(zc)) + 1);
+        int group = 0;
+        if (const char* g = std::getenv("RCWA_GB300_EIG_GROUP")) group = std::atoi(g);
+        launch_eig(ctx->stream, n, batch, reinterpret_cast<const zc*>(d_a), (long long)n * n,
+                   reinterpret_cast<zc*>(d_values), reinterpret_cast<zc*>(d_vectors), d_info, d_sweeps, ws, eps, max_iter,
+                   group);
+    });
+}
+
+int rcwa_gpu_eig_batch(rcwa_gpu_ctx* ctx, int n, int batch, const rcwa_complex* a, double eps, int max_iter,
+                       rcwa_complex* values, rcwa_complex* vectors, int* info, int* sweeps) {
+    return guarded(ctx, [&] {
+        if (n < 0 || batch < 0) throw EngineError{RCWA_EINVAL, "eig: negative size"};
+        if (max_iter < 1) throw EngineError{RCWA_EINVAL, "eig_qr: max_iter must be >= 1"};
+        if (!(eps >= 0.0) || !std::isfinite(eps)) throw EngineError{RCWA_EINVAL, "eig_qr: eps must be finite and >= 0"};
+        if (n == 0 || batch == 0) return;
+        if (!a || !values || !vectors || !info) throw EngineError{RCWA_EINVAL, "eig: null argument"};
+        const size_t nn = (size_t)n * n * batch;
+        for (size_t k = 0; k < nn; ++k)
+            if (!std::isfinite(a[k].re) || !std::isfinite(a[k].im))
+                throw EngineError{RCWA_EINVAL, "eig_qr: matrix has non-finite entries"};
+        const cudaStream_t st = ctx->stream;
+        DeviceScratch mem(st);
+        zc* da = mem.get<zc>(nn);
+        zc* dw = mem.get<zc>((size_t)n * batch);
+        zc* dv = mem.get<zc>(nn);
+        int* di = mem.get<int>(batch);
+        int* dsw = mem.get<int>(batch);
+        zc* ws = mem.get<zc>((size_t)(eig_workspace_bytes(n, batch) / sizeof(zc)) + 1);
+        RCWA_CUDA(cudaMemcpyAsync(da, a, nn * sizeof(zc), cudaMemcpyHostToDevice, st));
+        int group = 0;
+        if (const char* g = std::getenv("RCWA_GB300_EIG_GROUP")) group = std::atoi(g);
+        launch_eig(st, n, batch, da, (long long)n * n, dw, dv, di, dsw, ws, eps, max_iter, group);
+        copy_back(reinterpret_cast<zc*>(values), dw, (size_t)n * batch, st);
+        copy_back(reinterpret_cast<zc*>(vectors), dv, nn, st);
+        copy_back(info, di, batch, st);
+        copy_back(sweeps, dsw, batch, st);
+        RCWA_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int rcwa_gpu_solve_batch(rcwa_gpu_ctx* ctx, int n, int nrhs, int batch, const rcwa_complex* a, const rcwa_complex* b,
+                         rcwa_complex* x, int* singular) {
+    return guarded(ctx, [&] {
+        if (n < 0 || nrhs < 0 || batch < 0) throw EngineError{RCWA_EINVAL, "solve: negative size"};
+        if (n == 0 || nrhs == 0 || batch == 0) return;
+        if (!a || !b || !x || !singular) throw EngineError{RCWA_EINVAL, "solve: null argument"};
+        const cudaStream_t st = ctx->stream;
+        const size_t na = (size_t)n * n * batch, nb = (size_t)n * nrhs * batch;
+        DeviceScratch mem(st);
+        zc* da = mem.get<zc>(na);
+        zc* db = mem.get<zc>(nb);
+        int* ds = mem.zeros<int>(batch);
+        RCWA_CUDA(cudaMemcpyAsync(da, a, na * sizeof(zc), cudaMemcpyHostToDevice, st));
+        RCWA_CUDA(cudaMemcpyAsync(db, b, nb * sizeof(zc), cudaMemcpyHostToDevice, st));
+        launch_lu_solve(st, n, nrhs, batch, da, (long long)n * n, da, (long long)n * n, RHS_DENSE, db, (long long)n * nrhs,
+                        db, (long long)n * nrhs, ds);
+        copy_back(reinterpret_cast<zc*>(x), db, nb, st);
+        copy_back(singular, ds, batch, st);
+        RCWA_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int rcwa_gpu_multiply_batch(rcwa_gpu_ctx* ctx, int m, int k, int n, int batch, const rcwa_complex* a,
+                            const rcwa_complex* b, rcwa_complex* c) {
+    return guarded(ctx, [&] {
+        if (m < 0 || k < 0 || n < 0 || batch < 0) throw EngineError{RCWA_EINVAL, "multiply: negative size"};
+        if (m == 0 || n == 0 || batch == 0) return;
+        if (!a || !b || !c) throw EngineError{RCWA_EINVAL, "multiply: null argument"};
+        const cudaStream_t st = ctx->stream;
+        const size_t na = (size_t)m * k * batch, nb = (size_t)k * n * batch, nc = (size_t)m * n * batch;
+        DeviceScratch mem(st);
+        zc* da = mem.get<zc>(na);
+        zc* db = mem.get<zc>(nb);
+        zc* dc = mem.get<zc>(nc);
+        RCWA_CUDA(cudaMemcpyAsync(da, a, na * sizeof(zc), cudaMemcpyHostToDevice, st));
+        RCWA_CUDA(cudaMemcpyAsync(db, b, nb * sizeof(zc), cudaMemcpyHostToDevice, st));
+        launch_zgemm(st, m, n, k, batch, da, m, (long long)m * k, db, k, (long long)k * n, nullptr, 0, dc, m,
+                     (long long)m * n, 1.0, 0.0);
+        copy_back(reinterpret_cast<zc*>(c), dc, nc, st);
+        RCWA_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,430 @@
+// eig.cuh -- batched general complex eigensolver for sm_103a: unitary Hessenberg reduction plus
+// shifted complex QR with deflation and eigenvector back-transformation (EISPACK CORTH + COMQR2,
+// as restated by include/stablercwa/eig_qr.hpp).
+//
+// Mapping to GB300. The FP64 pipe (about 2 lane-operations per clock per SM) issues a warp
+// instruction in the same time whether 1 or 32 lanes are active, so every FP64 instruction must carry
+// 32 lanes of useful work. A group of G adjacent lanes owns one matrix and a warp holds 32/G
+// matrices; the inherently serial steps of QR (forming a rotation, the shift, the deflation test)
+// are computed by all lanes of a group from the same data, so each warp instruction forms the
+// rotations of 32/G matrices at once, and the O(n^2)-per-sweep updates are split across the G lanes
+// by row or by column. Groups synchronise with __syncwarp only; there is no block-wide barrier and
+// no spin-wait. H, Z and the back-substitution vectors live in a per-matrix global workspace (the FP64
+// pipe, not memory, bounds every phase: about one 16-byte load per 12 FP64 operations).
+//
+// Per-element arithmetic follows the reference: the same Householder vector scaling, rotation
+// formulas (eig_qr.hpp:450-528), Wilkinson and exceptional shifts (:535-544, :1082-1086), the
+// deflation test (:1063-1065), max_iter/info semantics (:1074-1077) and the back substitution with
+// its coincident-eigenvalue floor and overflow control (:886-951). Reductions are lane trees instead
+// of the reference's four-way partial sums, so results agree to rounding, not bit for bit.
+#pragma once
+
+#include <float.h>
+
+#include "common.cuh"
+
+namespace rcwa_gb300 {
+
+struct Rot {
+    double cr, ci, s;
+};
+
+// Per-matrix workspace layout in units of zc.
+__host__ __device__ inline long long eig_workspace_elems(int n) { return 3LL * n * n + 4LL * n + 8; }
+
+template <int G>
+__device__ __forceinline__ int first_owned(int start, int g) {
+    // smallest r >= start with r % G == g
+    const int r0 = start + ((g - start) % G + G) % G;
+    return r0;
+}
+
+// unit-modulus z/|z| and |z| with power-of-two pre-scaling (eig_qr.hpp:216-222)
+__device__ __forceinline__ zc unit_phase(zc z, double& modulus) {
+    const int e = bexp(fmax(fabs(z.re), fabs(z.im)));
+    z = scale2(z, -e);
+    const double r = hypot(z.re, z.im);
+    modulus = ldexp(r, e);
+    return zc{z.re / r, z.im / r};
+}
+
+// Rotation that zeroes the real subdiagonal below x (eig_qr.hpp:450-464).
+__device__ __forceinline__ Rot make_rotation(zc x, double sub, zc& top) {
+    double xr = x.re, xi = x.im;
+    const double m = fmax(fmax(fabs(xr), fabs(xi)), fabs(sub));
+    int e = 0;
+    if (!(m > 1e-140 && m < 1e140)) {
+        e = bexp(m);
+        xr = ldexp(xr, -e);
+        xi = ldexp(xi, -e);
+        sub = ldexp(sub, -e);
+    }
+    const double nrm = sqrt(xr * xr + xi * xi + sub * sub);
+    top = zc{e ? ldexp(nrm, e) : nrm, 0.0};
+    return Rot{xr / nrm, xi / nrm, sub / nrm};
+}
+
+// Wilkinson shift from the trailing 2x2 block [a b; c d] (eig_qr.hpp:535-544)
+__device__ __forceinline__ zc wilkinson_shift(zc a, zc b, double c, zc d) {
+    const zc y = zc{(a.re - d.re) / 2.0, (a.im - d.im) / 2.0};
+    const int e = bexp(fmax(fmax(abs1(b), fabs(c)), abs1(y)));
+    const zc x = scale2(b, -e) * ldexp(c, -e);
+    if (is_zero(x)) return d;
+    const zc ys = scale2(y, -e);
+    zc zz = zsqrt(ys * ys + x);
+    if (ys.re * zz.re + ys.im * zz.im < 0.0) zz = -zz;
+    return d - scale2(zdiv(x, ys + zz), e);
+}
+
+template <int G>
+__device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc* __restrict__ V,
+                        int* __restrict__ info_out, int* __restrict__ sweeps_out, zc* __restrict__ ws, double eps,
+                        int max_iter) {
+    const int g = threadIdx.x & (G - 1);
+    const unsigned mask = group_mask<G>();
+    zc* __restrict__ H = ws;
+    zc* __restrict__ Z = H + (long long)n * n;
+    zc* __restrict__ X = Z + (long long)n * n;
+    zc* __restrict__ ort = X + (long long)n * n;
+    zc* __restrict__ wk = ort + n;
+    double* __restrict__ rotd = reinterpret_cast<double*>(wk + n);  // 3n doubles (<= 2n zc)
+
+    for (long long idx = g; idx < (long long)n * n; idx += G) H[idx] = A[idx];
+    __syncwarp(mask);
+
+    // ---------------- CORTH: Householder reduction to upper Hessenberg (eig_qr.hpp:231-272)
+    // lane g owns rows r with r % G == g in every column.
+    for (int m = 1; m < n - 1; ++m) {
+        zc* x = H + (long long)(m - 1) * n;
+        const int r0 = first_owned<G>(m, g);
+        double sc = 0.0;
+        for (int i = r0; i < n; i += G) sc += abs1(x[i]);
+        sc = group_sum<G>(sc, mask);
+        if (sc == 0.0) {
+            if (g == 0) ort[m] = zc{0.0, 0.0};
+            __syncwarp(mask);
+            continue;
+        }
+        double h = 0.0;
+        for (int i = r0; i < n; i += G) {
+            const zc u = zdivr(x[i], sc);
+            ort[i] = u;
+            h += norm2(u);
+        }
+        h = group_sum<G>(h, mask);
+        __syncwarp(mask);
+        double gg = sqrt(h);
+        zc om = ort[m];
+        const double f = zabs(om);
+        if (f == 0.0) {
+            om = zc{gg, 0.0};
+        } else {
+            h += f * gg;
+            gg /= f;
+            om = om * (1.0 + gg);
+        }
+        __syncwarp(mask);
+        if ((m % G) == g) {
+            ort[m] = om;
+            if (f == 0.0) x[m] = zc{sc, 0.0};
+        }
+        __syncwarp(mask);
+        // left multiply P_m on columns n-1 .. m (rows >= m), accumulating wk = (P_m A)(:, m:) u
+        for (int i = g; i < n; i += G) wk[i] = zc{0.0, 0.0};
+        for (int j = n - 1; j >= m; --j) {
+            zc* aj = H + (long long)j * n;
+            double dr = 0.0, di = 0.0;
+            for (int i = r0; i < n; i += G) {
+                const zc u = ort[i], a = aj[i];
+                dr += u.re * a.re + u.im * a.im;
+                di += u.re * a.im - u.im * a.re;
+            }
+            dr = group_sum<G>(dr, mask);
+            di = group_sum<G>(di, mask);
+            const zc t = zc{-dr / h, -di / h};
+            for (int i = r0; i < n; i += G) aj[i] = zfma(t, ort[i], aj[i]);
+            const zc uj = ort[j];
+            for (int i = g; i < n; i += G) wk[i] = zfma(uj, aj[i], wk[i]);
+        }
+        // right multiply: A(:, m:) -= (wk / h) u^H
+        for (int i = g; i < n; i += G) wk[i] = zdivr(wk[i], h);
+        for (int j = m; j < n; ++j) {
+            zc* aj = H + (long long)j * n;
+            const zc cu = -conj(ort[j]);
+            for (int i = g; i < n; i += G) aj[i] = zfma(cu, wk[i], aj[i]);
+        }
+        __syncwarp(mask);
+        if ((m % G) == g) {
+            ort[m] = om * sc;
+            x[m] = x[m] * (-gg);
+        }
+        __syncwarp(mask);
+    }
+
+    // ---------------- accumulate the reflectors into Z (eig_qr.hpp:354-373)
+    for (long long idx = g; idx < (long long)n * n; idx += G) {
+        const int c = (int)(idx / n), r = (int)(idx - (long long)c * n);
+        Z[idx] = zc{r == c ? 1.0 : 0.0, 0.0};
+    }
+    __syncwarp(mask);
+    for (int i = n - 2; i >= 1; --i) {
+        const zc oi = ort[i];
+        const zc hs = H[(long long)(i - 1) * n + i];
+        if (is_zero(oi) || is_zero(hs)) continue;
+        const int e = bexp(abs1(oi));
+        const zc sub = scale2(hs, -e);
+        const zc v0 = scale2(oi, -e);
+        const double minus_h = sub.re * v0.re + sub.im * v0.im;
+        const int r0 = first_owned<G>(i, g);
+        for (int k = r0; k < n; k += G) ort[k] = k == i ? v0 : scale2(H[(long long)(i - 1) * n + k], -e);
+        for (int j = i; j < n; ++j) {
+            zc* zj = Z + (long long)j * n;
+            double dr = 0.0, di = 0.0;
+            for (int k = r0; k < n; k += G) {
+                const zc u = ort[k], a = zj[k];
+                dr += u.re * a.re + u.im * a.im;
+                di += u.re * a.im - u.im * a.re;
+            }
+            dr = group_sum<G>(dr, mask);
+            di = group_sum<G>(di, mask);
+            const zc t = zc{dr / minus_h, di / minus_h};
+            for (int k = r0; k < n; k += G) zj[k] = zfma(t, ort[k], zj[k]);
+        }
+    }
+    __syncwarp(mask);
+
+    // ---------------- clean Hessenberg form, real subdiagonal (eig_qr.hpp:420-439)
+    for (int j = 0; j + 2 < n; ++j)
+        for (int r = first_owned<G>(j + 2, g); r < n; r += G) H[(long long)j * n + r] = zc{0.0, 0.0};
+    __syncwarp(mask);
+    for (int i = 1; i < n; ++i) {
+        const zc sub = H[(long long)(i - 1) * n + i];
+        if (sub.im == 0.0) continue;
+        double nrm = 0.0;
+        const zc y = unit_phase(sub, nrm);
+        const zc cy = conj(y);
+        for (int j = first_owned<G>(i, g); j < n; j += G) {  // row i, by column owner
+            zc* p = H + (long long)j * n + i;
+            *p = cy * *p;
+        }
+        __syncwarp(mask);
+        if ((i % G) == g) H[(long long)(i - 1) * n + i] = zc{nrm, 0.0};
+        const int last = min(i + 1, n - 1);
+        for (int r = g; r <= last; r += G) {
+            zc* p = H + (long long)i * n + r;
+            *p = y * *p;
+        }
+        for (int r = g; r < n; r += G) {
+            zc* p = Z + (long long)i * n + r;
+            *p = y * *p;
+        }
+        __syncwarp(mask);
+    }
+
+    // ---------------- shifted QR (eig_qr.hpp:1039-1096), full updates of H and Z
+    zc t = zc{0.0, 0.0};
+    int en = n - 1, its = 0, sweeps = 0, info = 0;
+    while (en >= 0) {
+        // deflation: largest l <= en with negligible h(l, l-1); lanes test G candidates at a time
+        int l = 0;
+        for (int base = en; base >= 1; base -= G) {
+            const int cand = base - g;
+            bool ok = false;
+            if (cand >= 1) {
+                const zc hsub = H[(long long)(cand - 1) * n + cand];
+                const zc hd0 = H[(long long)(cand - 1) * n + cand - 1];
+                const zc hd1 = H[(long long)cand * n + cand];
+                ok = abs1(hsub) <= eps * (abs1(hd0) + abs1(hd1));
+            }
+            const unsigned bits = __ballot_sync(mask, ok);
+            const unsigned mine = G == 32 ? bits : (bits >> ((threadIdx.x & 31) & ~(G - 1))) & ((1u << G) - 1u);
+            if (mine) {
+                l = base - (__ffs(mine) - 1);
+                break;
+            }
+        }
+        if (l == en) {
+            const zc hd = H[(long long)en * n + en];
+            const zc wv = hd + t;
+            __syncwarp(mask);
+            if ((en % G) == g) H[(long long)en * n + en] = wv;
+            if (g == 0) W[en] = wv;
+            __syncwarp(mask);
+            --en;
+            its = 0;
+            continue;
+        }
+        if (its == max_iter) {
+            info = en + 1;
+            break;
+        }
+        zc s;
+        if (its == 10 || its == 20) {
+            s = zc{fabs(H[(long long)(en - 1) * n + en].re) + (en >= 2 ? fabs(H[(long long)(en - 2) * n + en - 1].re) : 0.0), 0.0};
+        } else {
+            s = wilkinson_shift(H[(long long)(en - 1) * n + en - 1], H[(long long)en * n + en - 1],
+                                H[(long long)(en - 1) * n + en].re, H[(long long)en * n + en]);
+        }
+        __syncwarp(mask);
+        for (int r = g; r <= en; r += G) {
+            zc* p = H + (long long)r * n + r;
+            *p = *p - s;
+        }
+        t = t + s;
+        ++its;
+        ++sweeps;
+        __syncwarp(mask);
+
+        // (1) left multiply Q^H: rotation G_i from column i-1, applied to columns i..n-1 (rows i-1, i)
+        for (int i = l + 1; i <= en; ++i) {
+            zc* cprev = H + (long long)(i - 1) * n;
+            zc top;
+            const Rot q = make_rotation(cprev[i - 1], cprev[i].re, top);
+            __syncwarp(mask);
+            if (((i - 1) % G) == g) {
+                cprev[i - 1] = top;
+                cprev[i] = zc{0.0, 0.0};
+            }
+            if (g == 0) {
+                rotd[3 * i] = q.cr;
+                rotd[3 * i + 1] = q.ci;
+                rotd[3 * i + 2] = q.s;
+            }
+            for (int c = first_owned<G>(i, g); c < n; c += G) {
+                zc* col = H + (long long)c * n;
+                const zc y = col[i - 1], z = col[i];
+                col[i - 1] = zc{q.cr * y.re + q.ci * y.im + q.s * z.re, q.cr * y.im - q.ci * y.re + q.s * z.im};
+                col[i] = zc{q.cr * z.re - q.ci * z.im - q.s * y.re, q.cr * z.im + q.ci * z.re - q.s * y.im};
+            }
+            __syncwarp(mask);
+        }
+        // (2) phase that makes r(en, en) real (eig_qr.hpp:588-596)
+        const zc hee = H[(long long)en * n + en];
+        const bool has_phase = hee.im != 0.0;
+        zc phase = zc{1.0, 0.0};
+        if (has_phase) {
+            double nrm = 0.0;
+            phase = unit_phase(hee, nrm);
+            __syncwarp(mask);
+            if ((en % G) == g) H[(long long)en * n + en] = zc{nrm, 0.0};
+            const zc cp = conj(phase);
+            for (int j = first_owned<G>(en + 1, g); j < n; j += G) {
+                zc* p = H + (long long)j * n + en;
+                *p = cp * *p;
+            }
+        }
+        __syncwarp(mask);
+        // (3) right multiply by Q on H rows 0..en and on all rows of Z (eig_qr.hpp:598-606)
+        for (int r = g; r <= en; r += G) {
+            int j = max(l + 1, r);
+            if (j > en) continue;
+            zc a = H[(long long)(j - 1) * n + r];
+            for (; j <= en; ++j) {
+                const double cr = rotd[3 * j], ci = rotd[3 * j + 1], sn = rotd[3 * j + 2];
+                const zc b = H[(long long)j * n + r];
+                H[(long long)(j - 1) * n + r] = zc{cr * a.re - ci * a.im + sn * b.re, cr * a.im + ci * a.re + sn * b.im};
+                a = zc{cr * b.re + ci * b.im - sn * a.re, cr * b.im - ci * b.re - sn * a.im};
+            }
+            H[(long long)en * n + r] = has_phase ? phase * a : a;
+        }
+        for (int r = g; r < n; r += G) {
+            zc a = Z[(long long)l * n + r];
+            for (int j = l + 1; j <= en; ++j) {
+                const double cr = rotd[3 * j], ci = rotd[3 * j + 1], sn = rotd[3 * j + 2];
+                const zc b = Z[(long long)j * n + r];
+                Z[(long long)(j - 1) * n + r] = zc{cr * a.re - ci * a.im + sn * b.re, cr * a.im + ci * a.re + sn * b.im};
+                a = zc{cr * b.re + ci * b.im - sn * a.re, cr * b.im - ci * b.re - sn * a.im};
+            }
+            Z[(long long)en * n + r] = has_phase ? phase * a : a;
+        }
+        __syncwarp(mask);
+    }
+    if (g == 0) {
+        *info_out = info;
+        if (sweeps_out) *sweeps_out = sweeps;
+    }
+    if (info != 0) {
+        // not converged: unconverged diagonal plus accumulated shift (eig_qr.hpp:1098-1103); no vectors
+        for (int i = g; i <= en; i += G) W[i] = H[(long long)i * n + i] + t;
+        return;
+    }
+
+    // ---------------- eigenvectors of T by back substitution, times Z, normalised (eig_qr.hpp:886-961)
+    double tn = 0.0;
+    for (int j = 0; j < n; ++j)
+        for (int i = g; i <= j; i += G) tn = fmax(tn, abs1(H[(long long)j * n + i]));
+    tn = group_max<G>(tn, mask);
+    const double rel = fmax(eps, DBL_EPSILON);
+    double tiny = rel * tn;
+    if (tiny == 0.0) tiny = DBL_MIN;
+    __syncwarp(mask);
+    // the diagonal of H now holds the eigenvalues; read them from W (written above) for clarity
+    const double kQuotientMax = 1e300;
+    const double kShrink = 0x1p-512;
+    for (int j = g; j < n; j += G) {
+        zc* x = X + (long long)j * n;
+        for (int k = 0; k < j; ++k) x[k] = H[(long long)j * n + k];
+        x[j] = zc{1.0, 0.0};
+        const zc wj = W[j];
+        for (int i = j - 1; i >= 0; --i) {
+            const zc wi = W[i];
+            zc y = wj - wi;
+            if (is_zero(y)) {
+                y = zc{tiny, 0.0};
+            } else {
+                const double floor_value = rel * fmax(abs1(wj), abs1(wi));
+                if (abs1(y) < floor_value) y = zc{floor_value, 0.0};
+            }
+            for (int pass = 0; pass < 3 && abs1(x[i]) > abs1(y) * kQuotientMax; ++pass)
+                for (int k = 0; k <= j; ++k) x[k] = x[k] * kShrink;
+            const zc xi = zdiv(x[i], y);
+            x[i] = xi;
+            const double tr = abs1(xi);
+            zc xs = xi;
+            if (tr != 0.0 && tr + 1.0 / tr <= tr) {
+                for (int k = 0; k <= j; ++k) x[k] = zdivr(x[k], tr);
+                xs = x[i];
+            }
+            const zc* ti = H + (long long)i * n;
+            for (int k = 0; k < i; ++k) x[k] = zfma(xs, ti[k], x[k]);
+        }
+    }
+    __syncwarp(mask);
+    // V = Z X (X upper triangular), then each column scaled to unit 2-norm
+    for (int j = 0; j < n; ++j) {
+        const zc* xj = X + (long long)j * n;
+        zc* vj = V + (long long)j * n;
+        double big = 0.0;
+        for (int r = g; r < n; r += G) {
+            zc acc = zc{0.0, 0.0};
+            for (int k = 0; k <= j; ++k) acc = zfma(xj[k], Z[(long long)k * n + r], acc);
+            vj[r] = acc;
+            big = fmax(big, fmax(fabs(acc.re), fabs(acc.im)));
+        }
+        big = group_max<G>(big, mask);
+        if (big == 0.0 || !isfinite(big)) continue;
+        double ssq = 0.0;
+        for (int r = g; r < n; r += G) {
+            const zc u = zdivr(vj[r], big);
+            ssq += norm2(u);
+        }
+        ssq = group_sum<G>(ssq, mask);
+        const double inv = 1.0 / sqrt(ssq);
+        for (int r = g; r < n; r += G) vj[r] = zdivr(vj[r], big) * inv;
+    }
+}
+
+// One group of G lanes per matrix; matrices at a_stride / w_stride / v_stride elements apart.
+template <int G>
+__global__ void __launch_bounds__(128) eig_batch_kernel(int n, int batch, const zc* __restrict__ a, long long a_stride,
+                                                        zc* __restrict__ w, zc* __restrict__ v, int* __restrict__ info,
+                                                        int* __restrict__ sweeps, zc* __restrict__ ws, double eps,
+                                                        int max_iter, const int* __restrict__ skip) {
+    const long long gid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    if (gid >= batch) return;
+    if (skip && skip[gid]) return;
+    eig_one<G>(n, a + gid * a_stride, w + gid * n, v + gid * (long long)n * n, info + gid, sweeps ? sweeps + gid : nullptr,
+               ws + gid * eig_workspace_elems(n), eps, max_iter);
+}
+
+}  // namespace rcwa_gb300

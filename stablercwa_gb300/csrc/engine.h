@@ -1,0 +1,110 @@
+// engine.h -- internal interfaces between the engine's translation units (not installed).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/stablercwa_gb300.h"
+#include "common.cuh"
+
+namespace rcwa_gb300 {
+
+// Thrown inside the engine, turned into a return code at the C ABI.
+struct EngineError {
+    int code;
+    std::string message;
+};
+
+#define RCWA_CUDA(call)                                                                                   \
+    do {                                                                                                  \
+        cudaError_t err_ = (call);                                                                        \
+        if (err_ != cudaSuccess)                                                                          \
+            throw ::rcwa_gb300::EngineError{err_ == cudaErrorMemoryAllocation ? RCWA_ENOMEM : RCWA_ECUDA,   \
+                                            std::string(#call) + ": " + cudaGetErrorString(err_)};        \
+    } while (0)
+
+// Stream-ordered device allocations released together when the scope ends.
+class DeviceScratch {
+public:
+    explicit DeviceScratch(cudaStream_t s) : stream_(s) {}
+    ~DeviceScratch() { release(); }
+    DeviceScratch(const DeviceScratch&) = delete;
+    DeviceScratch& operator=(const DeviceScratch&) = delete;
+    template <class T>
+    T* get(size_t count) {
+        void* p = nullptr;
+        if (count == 0) count = 1;
+        RCWA_CUDA(cudaMallocAsync(&p, count * sizeof(T), stream_));
+        ptrs_.push_back(p);
+        return static_cast<T*>(p);
+    }
+    template <class T>
+    T* zeros(size_t count) {
+        T* p = get<T>(count);
+        RCWA_CUDA(cudaMemsetAsync(p, 0, (count ? count : 1) * sizeof(T), stream_));
+        return p;
+    }
+    void free(void* p) {
+        for (size_t k = 0; k < ptrs_.size(); ++k)
+            if (ptrs_[k] == p) {
+                cudaFreeAsync(p, stream_);
+                ptrs_[k] = ptrs_.back();
+                ptrs_.pop_back();
+                return;
+            }
+    }
+    void release() {
+        for (void* p : ptrs_) cudaFreeAsync(p, stream_);
+        ptrs_.clear();
+    }
+
+private:
+    cudaStream_t stream_;
+    std::vector<void*> ptrs_;
+};
+
+struct KernelCounter {
+    long long launches = 0;
+};
+
+// Launchers (linalg.cu, eig.cu)
+void launch_lu_solve(cudaStream_t st, int n, int nrhs, int batch, const zc* a, long long a_stride, zc* lu,
+                     long long lu_stride, int rhs_kind, const zc* rhs, long long rhs_stride, zc* x, long long x_stride,
+                     int* singular, const int* skip = nullptr, int skip_value = 1);
+void launch_zgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride, const zc* B,
+                  int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc, long long c_stride,
+                  double s_ab, double s_c, const int* skip = nullptr, int skip_value = 1);
+// group: lanes per matrix (0 = choose)
+void launch_eig(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info, int* sweeps,
+                zc* ws, double eps, int max_iter, int group, const int* skip = nullptr);
+long long eig_workspace_bytes(int n, int batch);
+int eig_default_group(int n, int batch);
+
+// Kernel launch accounting for the benchmark's gpu_launches claim.
+long long& launch_count();
+
+struct Options {
+    int fast_path = 1;
+    int diagnostics = 0;
+    int max_iter = 30;
+    double eps = 2.220446049250313e-16;
+    int eig_group = 0;
+};
+
+// Batched 1-D solve (rcwa1d.cu). d_s[p] = nI sin(theta_p) and d_wl[p] = wavelength_p are device
+// arrays; results go to the device arrays of d_out. Throws EngineError.
+void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_s, const double* d_wl, int n_points,
+                    int M, int pol, const Options& opt, const rcwa_result1d& d_out, size_t chunk_bytes);
+// Device-side check of the sweep points (finite positive wavelength, |theta| < 90) and
+// s = nI sin(theta) with the device sin; returns false when some point is invalid.
+bool prepare_points_device(cudaStream_t st, const rcwa_point1d* d_points, int n_points, double nI, double* d_s,
+                           double* d_wl);
+
+// Validation of a 1-D problem exactly where the reference throws std::invalid_argument.
+void validate1d(const rcwa_stack1d& stack, const rcwa_point1d* h_points, int n_points, int M, int pol);
+
+}  // namespace rcwa_gb300

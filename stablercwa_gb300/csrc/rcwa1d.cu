@@ -1,0 +1,842 @@
+// rcwa1d.cu -- batched 1-D TE/TM RCWA solve on the GPU (the engine behind rcwa::solve / rcwa::sweep).
+//
+// The host code here mirrors include/stablercwa/rcwa1d.hpp:853-1074 step by step, but every step
+// is one batched kernel launch over a chunk of sweep points: per-layer assembly, the batched
+// eigensolver (eig.cuh), and the S-matrix recursion in which each Zero/Diag/Dense operator of the
+// reference (rcwa1d.hpp:549-629) becomes a B x n vector or a B x n x n matrix in device memory.
+// Operator kinds depend only on the stack (which layers are gratings), so one launch sequence
+// serves the whole chunk. The single sample-dependent kind change of the reference -- an exact
+// q == 0 inside a layer whose propagation block meets a dense reflection (rcwa1d.hpp:751-784,
+// :797-805) -- is taken by the affected samples only, through masked launches.
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+#include "engine.h"
+#include "rcwa1d_kernels.cuh"
+
+namespace rcwa_gb300 {
+namespace {
+
+constexpr int kTpb = 256;
+inline unsigned nblocks(long long total, int tpb = kTpb) {
+    return static_cast<unsigned>((total + tpb - 1) / tpb > 0 ? (total + tpb - 1) / tpb : 1);
+}
+inline unsigned warp_blocks(long long warps) { return static_cast<unsigned>((warps * 32 + 127) / 128); }
+
+#define LAUNCH(kernel, grid, block, st, ...)                      \
+    do {                                                         \
+        kernel<<<(grid), (block), 0, (st)>>>(__VA_ARGS__);       \
+        ++launch_count();                                        \
+        RCWA_CUDA(cudaGetLastError());                           \
+    } while (0)
+
+// ---------------------------------------------------------------- small per-sample vector kernels
+
+__global__ void k0_kernel(int B, const double* __restrict__ wl, double* __restrict__ k0) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < B) k0[b] = __ddiv_rn(2.0 * 3.141592653589793238462643383279502884, wl[b]);
+}
+
+__global__ void finite_check_kernel(int B, long long per, const zc* __restrict__ a, int* __restrict__ fail) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * per) return;
+    if (!zfinite(a[idx])) fail[idx / per] = 1;
+}
+
+__global__ void eig_info_kernel(int B, const int* __restrict__ info, int* __restrict__ eig_info, int* __restrict__ fail) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    if (info[b] != 0) {
+        if (eig_info[b] == 0) eig_info[b] = info[b];
+        fail[b] = 1;
+    }
+}
+
+__global__ void col_extract_kernel(int B, int n, const zc* __restrict__ m, int col, zc* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * n) return;
+    const int b = (int)(idx / n), i = (int)(idx - (long long)b * n);
+    out[idx] = m[(long long)b * n * n + (long long)col * n + i];
+}
+
+// y = s_c * y0 + s_ab * (A x), warp per sample, lanes along rows; the sum over columns is ascending
+// like the reference's matrix-vector product (include/stablercwa/matrix.hpp:186-194).
+__global__ void matvec_kernel(int B, int n, const zc* __restrict__ A, const zc* __restrict__ x, const zc* y0,
+                              zc* y, double s_ab, double s_c) {
+    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (b >= B) return;
+    const int lane = threadIdx.x & 31;
+    const zc* As = A + b * n * n;
+    const zc* xs = x + b * n;
+    for (int i = lane; i < n; i += 32) {
+        zc acc = zc{0.0, 0.0};
+        for (int k = 0; k < n; ++k) acc = zfma(As[(long long)k * n + i], xs[k], acc);
+        zc v = zc{s_ab * acc.re, s_ab * acc.im};
+        if (y0 && s_c != 0.0) v = zc{s_c * y0[b * n + i].re + v.re, s_c * y0[b * n + i].im + v.im};
+        y[b * n + i] = v;
+    }
+}
+
+// g applied to a vector: diagonal g, or the per-sample dense alternative where alt_flag is set.
+__global__ void apply_g_kernel(int B, int n, int kind, const zc* __restrict__ g, const zc* __restrict__ alt,
+                               const int* __restrict__ alt_flag, const zc* __restrict__ x, zc* __restrict__ y) {
+    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (b >= B) return;
+    const int lane = threadIdx.x & 31;
+    const zc* xs = x + b * n;
+    const bool dense = kind == 2 || (alt_flag && alt_flag[b]);
+    const zc* Ms = kind == 2 ? g + b * n * n : (alt ? alt + b * n * n : nullptr);
+    for (int i = lane; i < n; i += 32) {
+        zc v;
+        if (kind == 0) {
+            v = zc{0.0, 0.0};
+        } else if (!dense) {
+            v = g[b * n + i] * xs[i];
+        } else {
+            zc acc = zc{0.0, 0.0};
+            for (int k = 0; k < n; ++k) acc = zfma(Ms[(long long)k * n + i], xs[k], acc);
+            v = acc;
+        }
+        y[b * n + i] = v;
+    }
+}
+
+__global__ void any_flag_kernel(int B, const int* __restrict__ f, int* __restrict__ any) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < B && f[b]) atomicOr(any, 1);
+}
+__global__ void inc_flagged_kernel(int B, const int* __restrict__ f, int* __restrict__ cnt) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < B && f[b]) cnt[b] += 1;
+}
+
+__global__ void vec_mul_kernel(long long total, const zc* __restrict__ d, const zc* __restrict__ x, zc* __restrict__ y) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < total) y[idx] = d ? d[idx] * x[idx] : zc{0.0, 0.0};
+}
+__global__ void vec_add_kernel(long long total, const zc* __restrict__ a, zc* __restrict__ y) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < total) y[idx] = a[idx] + y[idx];
+}
+// down[j] = down[j] / (1 - k[j])  (include/stablercwa/rcwa1d.hpp:997-998)
+__global__ void vec_div_one_minus_kernel(long long total, zc* __restrict__ down, const zc* __restrict__ k) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < total) down[idx] = zdiv(down[idx], zc{1.0, 0.0} - k[idx]);
+}
+// top block of two analytic regions: only column M of Tdd and Rud (include/stablercwa/rcwa1d.hpp:723-732)
+__global__ void top_diag_vectors_kernel(int B, int n, int M, const zc* __restrict__ tdd_d, const zc* __restrict__ rud_d,
+                                        zc* __restrict__ tdd, zc* __restrict__ rud) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * n) return;
+    const int i = (int)(idx % n);
+    tdd[idx] = i == M ? tdd_d[idx] : zc{0.0, 0.0};
+    rud[idx] = i == M ? rud_d[idx] : zc{0.0, 0.0};
+}
+
+// Efficiencies and the failure contract (include/stablercwa/rcwa1d.hpp:1024-1055, :810-816).
+__global__ void finalize_kernel(int B, int n, int M, int pol, int pure_films, const zc* __restrict__ R,
+                                const zc* __restrict__ T, const zc* __restrict__ qI, const zc* __restrict__ qII,
+                                const double* __restrict__ k0, zc nI, zc nII, int* __restrict__ fail,
+                                zc* __restrict__ outR, zc* __restrict__ outT, double* __restrict__ DEr,
+                                double* __restrict__ DEt) {
+    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (b >= B) return;
+    const int lane = threadIdx.x & 31;
+    const double kk = k0[b];
+    const zc qIM = qI[b * n + M];
+    const zc den = zc{-kk * qIM.im, kk * qIM.re};
+    const zc nI2 = nI * nI, nII2 = nII * nII;
+    bool bad = fail[b] != 0;
+    for (int j = lane; j < n; j += 32) {
+        zc r = R[b * n + j], t = T[b * n + j];
+        if (pure_films && j != M) {
+            if (!zfinite(r)) r = zc{0.0, 0.0};
+            if (!zfinite(t)) t = zc{0.0, 0.0};
+        }
+        if (!zfinite(r) || !zfinite(t)) bad = true;
+        const zc q1 = qI[b * n + j], q2 = qII[b * n + j];
+        const zc kIz = zc{-kk * q1.im, kk * q1.re};
+        const zc kIIz = zc{-kk * q2.im, kk * q2.re};
+        const double der = norm2(r) * zdiv(kIz, den).re;
+        const zc factor = pol == 0 ? zdiv(kIIz, den) : zdiv(zdiv(kIIz, nII2), zdiv(den, nI2));
+        const double det = norm2(t) * factor.re;
+        if (!isfinite(der) || !isfinite(det)) bad = true;
+        outR[b * n + j] = r;
+        outT[b * n + j] = t;
+        DEr[b * n + j] = der;
+        DEt[b * n + j] = det;
+    }
+    bad = __any_sync(0xffffffffu, bad);
+    if (bad) {
+        const double nan = __longlong_as_double(0x7ff8000000000000LL);
+        for (int j = lane; j < n; j += 32) {
+            outR[b * n + j] = zc{nan, nan};
+            outT[b * n + j] = zc{nan, nan};
+            DEr[b * n + j] = nan;
+            DEt[b * n + j] = nan;
+        }
+        if (lane == 0) fail[b] = 1;
+    }
+}
+
+__global__ void status_kernel(int B, const int* __restrict__ fail, const int* __restrict__ eig_info, int base_solves,
+                              const int* __restrict__ extra_solves, int n_eig, int* __restrict__ status,
+                              int* __restrict__ info_out, int* __restrict__ n_eig_out, int* __restrict__ n_solve_out) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    if (status) status[b] = fail[b] ? (eig_info[b] ? RCWA_SAMPLE_EIG_NOCONV : RCWA_SAMPLE_NUMERICAL) : RCWA_SAMPLE_OK;
+    if (info_out) info_out[b] = eig_info[b];
+    if (n_eig_out) n_eig_out[b] = n_eig;
+    if (n_solve_out) n_solve_out[b] = base_solves + extra_solves[b];
+}
+
+// Relative eigen-pair residual max_j ||A v_j - l_j v_j|| / (||A||_F ||v_j||), warp per sample
+// (include/stablercwa/eig.hpp:38-69); av = A V precomputed.
+__global__ void eig_residual_kernel(int B, int n, const zc* __restrict__ A, const zc* __restrict__ AV,
+                                    const zc* __restrict__ V, const zc* __restrict__ lam, const int* __restrict__ info,
+                                    double* __restrict__ out) {
+    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (b >= B) return;
+    const int lane = threadIdx.x & 31;
+    const long long nn = (long long)n * n;
+    double fro = 0.0;
+    for (long long k = lane; k < nn; k += 32) fro += norm2(A[b * nn + k]);
+    for (int o = 16; o > 0; o >>= 1) fro += __shfl_xor_sync(0xffffffffu, fro, o);
+    fro = sqrt(fro);
+    double worst = 0.0;
+    bool nan = info[b] != 0;
+    for (int j = 0; j < n; ++j) {
+        double dn = 0.0, vn = 0.0;
+        const zc l = lam[b * n + j];
+        for (int i = lane; i < n; i += 32) {
+            const zc v = V[b * nn + (long long)j * n + i];
+            dn += norm2(AV[b * nn + (long long)j * n + i] - l * v);
+            vn += norm2(v);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            dn += __shfl_xor_sync(0xffffffffu, dn, o);
+            vn += __shfl_xor_sync(0xffffffffu, vn, o);
+        }
+        const double val = (sqrt(dn) / fro) / sqrt(vn);
+        if (isnan(val)) nan = true;
+        worst = fmax(worst, val);
+    }
+    if (lane == 0) out[b] = (nan || isnan(out[b])) ? __longlong_as_double(0x7ff8000000000000LL) : fmax(out[b], worst);
+}
+
+// ---------------------------------------------------------------- batched operator algebra
+
+enum Kind { KZero = 0, KDiag = 1, KDense = 2 };
+struct DOp {
+    Kind kind = KZero;
+    zc* p = nullptr;
+    zc* alt = nullptr;           // per-sample dense alternative of a Diag g (exact q == 0 under dense r)
+    const int* alt_flag = nullptr;
+};
+struct DSBlock {
+    DOp Tdd, Rdu, Rud, Tuu;
+};
+struct DModes {
+    bool analytic = true;
+    bool fzb = false;
+    zc* q = nullptr;
+    zc* p = nullptr;
+    zc* W = nullptr;
+    zc* V = nullptr;
+};
+
+struct Batch {
+    cudaStream_t st;
+    DeviceScratch* mem;
+    int B, n, M;
+    int* fail;
+    int* extra_solves;
+    int n_solve = 0;
+    long long nn() const { return (long long)n * n; }
+    zc* dense() { return mem->get<zc>((size_t)B * nn()); }
+    zc* vec() { return mem->get<zc>((size_t)B * n); }
+};
+
+// linear_solve (include/stablercwa/rcwa1d.hpp:248-281): a zero pivot fails the sample.
+zc* solve(Batch& c, zc* a, bool consume_a, int rhs_kind, const zc* rhs, int nrhs = -1) {
+    ++c.n_solve;
+    if (nrhs < 0) nrhs = c.n;
+    zc* x = c.mem->get<zc>((size_t)c.B * c.n * nrhs);
+    zc* lu = consume_a ? a : c.dense();
+    launch_lu_solve(c.st, c.n, nrhs, c.B, a, c.nn(), lu, c.nn(), rhs_kind, rhs,
+                    rhs_kind == RHS_DIAG ? c.n : (long long)c.n * nrhs, x, (long long)c.n * nrhs, c.fail);
+    if (!consume_a) c.mem->free(lu);
+    return x;
+}
+
+zc* gemm(Batch& c, const zc* A, long long a_stride, const zc* Bm, const zc* C0, double s_ab, double s_c,
+         zc* out = nullptr, const int* skip = nullptr, int skip_value = 1) {
+    if (!out) out = c.dense();
+    launch_zgemm(c.st, c.n, c.n, c.n, c.B, A, c.n, a_stride, Bm, c.n, c.nn(), C0, c.nn(), out, c.n, c.nn(), s_ab, s_c, skip,
+                 skip_value);
+    return out;
+}
+
+// a * b (include/stablercwa/rcwa1d.hpp:569-580)
+DOp op_mul(Batch& c, const DOp& a, const DOp& b) {
+    DOp o;
+    if (a.kind == KZero || b.kind == KZero) return o;
+    const long long nv = (long long)c.B * c.n, nd = (long long)c.B * c.nn();
+    if (a.kind == KDiag && b.kind == KDiag) {
+        o.kind = KDiag;
+        o.p = c.vec();
+        LAUNCH(vec_mul_kernel, nblocks(nv), kTpb, c.st, nv, a.p, b.p, o.p);
+        return o;
+    }
+    o.kind = KDense;
+    o.p = c.dense();
+    if (a.kind == KDiag) {
+        LAUNCH(scale_rows_kernel, nblocks(nd), kTpb, c.st, c.B, c.n, b.p, a.p, o.p, nullptr, 1);
+    } else if (b.kind == KDiag) {
+        LAUNCH(scale_cols_kernel, nblocks(nd), kTpb, c.st, c.B, c.n, a.p, b.p, o.p, nullptr, 1);
+    } else {
+        gemm(c, a.p, c.nn(), b.p, nullptr, 1.0, 0.0, o.p);
+    }
+    return o;
+}
+
+// a + b (include/stablercwa/rcwa1d.hpp:583-603); reuses a's or b's storage
+DOp op_add(Batch& c, DOp a, const DOp& b) {
+    if (b.kind == KZero) return a;
+    if (a.kind == KZero) return b;
+    const long long nv = (long long)c.B * c.n, nd = (long long)c.B * c.nn();
+    if (a.kind == KDiag && b.kind == KDiag) {
+        LAUNCH(vec_add_kernel, nblocks(nv), kTpb, c.st, nv, b.p, a.p);  // a += b
+        return a;
+    }
+    if (a.kind == KDense && b.kind == KDense) {
+        LAUNCH(add_dense_kernel, nblocks(nd), kTpb, c.st, nd, a.p, b.p);
+        return a;
+    }
+    if (a.kind == KDense) {
+        LAUNCH(add_diag_kernel, nblocks(nv), kTpb, c.st, c.B, c.n, a.p, b.p, nullptr, 1);
+        return a;
+    }
+    DOp out = b;  // diag a + dense b: dense b with a added to its diagonal
+    LAUNCH(add_diag_kernel, nblocks(nv), kTpb, c.st, c.B, c.n, out.p, a.p, nullptr, 1);
+    return out;
+}
+
+zc* to_dense(Batch& c, const DOp& a) {
+    if (a.kind == KDense) return a.p;
+    zc* m = c.mem->zeros<zc>((size_t)c.B * c.nn());
+    if (a.kind == KDiag) LAUNCH(diag_to_dense_kernel, nblocks((long long)c.B * c.nn()), kTpb, c.st, c.B, c.n, a.p, m, nullptr, 1);
+    return m;
+}
+
+// tp, tm of an interface with at least one general side (include/stablercwa/rcwa1d.hpp:664-692).
+// The lower side's W and V are consumed (factored in place): this interface is their last use.
+void interface_matching(Batch& c, const DModes& up, const DModes& low, zc*& tp, zc*& tm) {
+    const long long nd = (long long)c.B * c.nn();
+    tp = c.dense();
+    tm = c.dense();
+    if (low.analytic) {
+        LAUNCH(tp_tm_kernel, nblocks(nd), kTpb, c.st, c.B, c.n, up.W, up.V, low.p, tp, tm);
+        return;
+    }
+    zc *mm, *nn;
+    if (up.analytic) {
+        mm = solve(c, low.W, true, RHS_IDENTITY, nullptr);
+        nn = solve(c, low.V, true, RHS_DIAG, up.p);
+    } else {
+        mm = solve(c, low.W, true, RHS_DENSE, up.W);
+        nn = solve(c, low.V, true, RHS_DENSE, up.V);
+    }
+    LAUNCH(tp_tm_kernel, nblocks(nd), kTpb, c.st, c.B, c.n, mm, nn, nullptr, tp, tm);
+    c.mem->free(mm);
+    c.mem->free(nn);
+}
+
+// include/stablercwa/rcwa1d.hpp:694-712
+DSBlock interface_block(Batch& c, const DModes& up, const DModes& low) {
+    DSBlock s;
+    if (up.analytic && low.analytic) {
+        const long long nv = (long long)c.B * c.n;
+        s.Tdd = {KDiag, c.vec()};
+        s.Rdu = {KDiag, c.vec()};
+        s.Rud = {KDiag, c.vec()};
+        s.Tuu = {KDiag, c.vec()};
+        LAUNCH(diagonal_interface_kernel, nblocks(nv), kTpb, c.st, nv, up.p, low.p, s.Tdd.p, s.Rdu.p, s.Rud.p, s.Tuu.p);
+        return s;
+    }
+    zc *tp, *tm;
+    interface_matching(c, up, low, tp, tm);
+    zc* tpi = solve(c, tp, false, RHS_IDENTITY, nullptr);
+    zc* rdu = gemm(c, tm, c.nn(), tpi, nullptr, 1.0, 0.0);
+    gemm(c, rdu, c.nn(), tm, tp, -1.0, 1.0, tp);  // tp -= rdu tm: tp is now Tdd
+    zc* rud = gemm(c, tpi, c.nn(), tm, nullptr, -1.0, 0.0);
+    c.mem->free(tm);
+    s.Tdd = {KDense, tp};
+    s.Rdu = {KDense, rdu};
+    s.Rud = {KDense, rud};
+    s.Tuu = {KDense, tpi};
+    return s;
+}
+
+struct Seam {
+    DOp g, r;
+};
+
+// include/stablercwa/rcwa1d.hpp:794-808 for blocks whose kinds are uniform over the batch
+Seam stack_on(Batch& c, DSBlock&& s, const DOp& r) {
+    Seam out;
+    DOp k = op_mul(c, s.Rdu, r);
+    const long long nv = (long long)c.B * c.n;
+    if (k.kind == KZero) {
+        out.g = s.Tdd;
+    } else if (k.kind == KDiag) {
+        // g = (1/(1-k)) Tdd
+        if (s.Tdd.kind == KDiag) {
+            out.g = {KDiag, c.vec()};
+            zc* one = c.vec();
+            // reuse the diagonal stack_on kernel for the scalar recurrence on each order
+            LAUNCH(stack_on_diag_kernel, nblocks(nv), kTpb, c.st, nv, s.Tdd.p, s.Rdu.p, nullptr, s.Tdd.p, r.p,
+                   out.g.p, one);
+            c.mem->free(one);
+        } else {
+            throw EngineError{RCWA_EUNSUPPORTED, "diagonal Rdu r with a dense Tdd"};
+        }
+    } else {
+        zc* ik = k.p;
+        LAUNCH(identity_minus_kernel, nblocks((long long)c.B * c.nn()), kTpb, c.st, c.B, c.n, ik, nullptr, 1);
+        zc* td = to_dense(c, s.Tdd);
+        out.g = {KDense, solve(c, ik, true, RHS_DENSE, td)};
+        c.mem->free(ik);
+        if (td != s.Tdd.p) c.mem->free(td);
+    }
+    out.r = op_add(c, s.Rud, op_mul(c, s.Tuu, op_mul(c, r, out.g)));
+    return out;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- validation
+
+namespace {
+void check_index(rcwa_complex n) {
+    const bool fin = std::isfinite(n.re) && std::isfinite(n.im);
+    if (!fin || std::abs(std::complex<double>(n.re, n.im)) == 0.0 || n.re < 0.0 || n.im < 0.0)
+        throw EngineError{RCWA_EINVAL, "rcwa: refractive index must be finite, nonzero, with Re n >= 0 and Im n >= 0"};
+}
+}  // namespace
+
+// include/stablercwa/rcwa1d.hpp:191-229 and :859-866
+void validate1d(const rcwa_stack1d& stack, const rcwa_point1d* h_points, int n_points, int M, int pol) {
+    if (M < 0 || M > (2147483647 - 1) / 4) throw EngineError{RCWA_EINVAL, "rcwa: invalid truncation order M"};
+    if (pol != RCWA_TE && pol != RCWA_TM) throw EngineError{RCWA_EINVAL, "rcwa: polarization must be TE or TM"};
+    if (!std::isfinite(stack.period) || stack.period <= 0.0)
+        throw EngineError{RCWA_EINVAL, "rcwa: wavelength and period must be finite and positive"};
+    if (h_points)
+        for (int p = 0; p < n_points; ++p) {
+            if (!std::isfinite(h_points[p].wavelength) || h_points[p].wavelength <= 0.0)
+                throw EngineError{RCWA_EINVAL, "rcwa: wavelength and period must be finite and positive"};
+            if (!std::isfinite(h_points[p].theta_deg) || std::fabs(h_points[p].theta_deg) >= 90.0)
+                throw EngineError{RCWA_EINVAL, "rcwa: incidence angle must lie strictly between -90 and 90 degrees"};
+        }
+    check_index(stack.nI);
+    if (stack.nI.im != 0.0 || stack.nI.re <= 0.0)
+        throw EngineError{RCWA_EINVAL, "rcwa: the incident medium must have a real positive index"};
+    check_index(stack.nII);
+    if (stack.n_layers < 0 || (stack.n_layers > 0 && !stack.layers))
+        throw EngineError{RCWA_EINVAL, "rcwa: layer array missing"};
+    for (int k = 0; k < stack.n_layers; ++k) {
+        const rcwa_layer1d& L = stack.layers[k];
+        if (L.fourier_method != 0)
+            throw EngineError{RCWA_EUNSUPPORTED, "rcwa: only analytic Fourier coefficients are implemented"};
+        if (!std::isfinite(L.d) || L.d < 0.0) throw EngineError{RCWA_EINVAL, "rcwa: layer thickness must be finite and >= 0"};
+        if (L.homogeneous) {
+            check_index(L.n);
+            continue;
+        }
+        if (L.n_segments < 1 || !L.edges || !L.n_values)
+            throw EngineError{RCWA_EINVAL, "rcwa: a grating layer needs K indices and K+1 edges"};
+        for (int j = 0; j <= L.n_segments; ++j)
+            if (!std::isfinite(L.edges[j]) || (j > 0 && L.edges[j] <= L.edges[j - 1]))
+                throw EngineError{RCWA_EINVAL, "rcwa: grating edges must be finite and strictly increasing"};
+        if (std::fabs((L.edges[L.n_segments] - L.edges[0]) - stack.period) > 1e-10 * stack.period)
+            throw EngineError{RCWA_EINVAL, "rcwa: grating edges must span exactly one period"};
+        for (int j = 0; j < L.n_segments; ++j) check_index(L.n_values[j]);
+    }
+}
+
+// ---------------------------------------------------------------- Fourier coefficients (host)
+
+namespace {
+using cd = std::complex<double>;
+constexpr double kPiD = 3.141592653589793238462643383279502884;
+
+// c_h, h = -hmax..hmax, of a piecewise-constant profile (include/stablercwa/rcwa1d.hpp:366-388)
+std::vector<cd> fourier_coefficients(const std::vector<double>& edges, const std::vector<cd>& values, double period,
+                                     int hmax) {
+    std::vector<cd> c(2 * hmax + 1);
+    const size_t segments = values.size();
+    std::vector<cd> phase(edges.size());
+    for (int h = -hmax; h <= hmax; ++h) {
+        cd sum{};
+        if (h == 0) {
+            for (size_t j = 0; j < segments; ++j) sum += values[j] * (edges[j + 1] - edges[j]) / period;
+        } else {
+            for (size_t k = 0; k < edges.size(); ++k) {
+                const double arg = -2.0 * kPiD * h * edges[k] / period;
+                phase[k] = cd{std::cos(arg), std::sin(arg)};
+            }
+            const double w = -2.0 * kPiD * h;
+            for (size_t j = 0; j < segments; ++j) {
+                const cd t = values[j] * (phase[j + 1] - phase[j]);
+                sum += cd{t.imag() / w, -t.real() / w};
+            }
+        }
+        c[h + hmax] = sum;
+    }
+    return c;
+}
+
+__global__ void toeplitz_kernel(int M, const zc* __restrict__ c, zc* __restrict__ m) {
+    const int n = 2 * M + 1;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n * n) return;
+    const int j = idx / n, i = idx - j * n;
+    m[idx] = c[i - j + 2 * M];
+}
+}  // namespace
+
+// ---------------------------------------------------------------- the solve
+
+void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_s, const double* d_wl, int n_points,
+                    int M, int pol, const Options& opt, const rcwa_result1d& d_out, size_t chunk_bytes) {
+    const int n = 2 * M + 1;
+    const long long nn = (long long)n * n;
+    const int L = stack.n_layers;
+    if (n_points <= 0) return;
+    std::vector<int> grating;
+    for (int k = 0; k < L; ++k)
+        if (!stack.layers[k].homogeneous) grating.push_back(k);
+    const bool pure_films = grating.empty();
+    const zc nI{stack.nI.re, stack.nI.im}, nII{stack.nII.re, stack.nII.im};
+
+    // Per-layer, sample-independent operators: Toeplitz coefficients; for TM the inverse of [[eps]] and
+    // of [[1/eps]] and [[1/eps]] itself (include/stablercwa/rcwa1d.hpp:432-468).
+    DeviceScratch persist(st);
+    int* layer_fail = persist.zeros<int>(1);
+    struct LayerData {
+        zc* c_eps = nullptr;
+        zc* inv_eps = nullptr;   // [[1/eps]] (TM)
+        zc* einv = nullptr;      // [[eps]]^{-1} (TM)
+        zc* cinv = nullptr;      // [[1/eps]]^{-1} (TM)
+    };
+    std::vector<LayerData> ld(L);
+    for (int k : grating) {
+        const rcwa_layer1d& Ly = stack.layers[k];
+        std::vector<double> edges(Ly.edges, Ly.edges + Ly.n_segments + 1);
+        std::vector<cd> eps, inv;
+        for (int j = 0; j < Ly.n_segments; ++j) {
+            const cd nv{Ly.n_values[j].re, Ly.n_values[j].im};
+            eps.push_back(nv * nv);
+            inv.push_back(1.0 / (nv * nv));
+        }
+        const std::vector<cd> ce = fourier_coefficients(edges, eps, stack.period, 2 * M);
+        ld[k].c_eps = persist.get<zc>(ce.size());
+        RCWA_CUDA(cudaMemcpyAsync(ld[k].c_eps, ce.data(), ce.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
+        if (pol == RCWA_TM) {
+            const std::vector<cd> ci = fourier_coefficients(edges, inv, stack.period, 2 * M);
+            zc* c_inv = persist.get<zc>(ci.size());
+            RCWA_CUDA(cudaMemcpyAsync(c_inv, ci.data(), ci.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
+            zc* E = persist.get<zc>(nn);
+            ld[k].inv_eps = persist.get<zc>(nn);
+            LAUNCH(toeplitz_kernel, nblocks(nn), kTpb, st, M, ld[k].c_eps, E);
+            LAUNCH(toeplitz_kernel, nblocks(nn), kTpb, st, M, c_inv, ld[k].inv_eps);
+            zc* C = persist.get<zc>(nn);
+            RCWA_CUDA(cudaMemcpyAsync(C, ld[k].inv_eps, nn * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+            ld[k].einv = persist.get<zc>(nn);
+            ld[k].cinv = persist.get<zc>(nn);
+            launch_lu_solve(st, n, n, 1, E, nn, E, nn, RHS_IDENTITY, nullptr, nn, ld[k].einv, nn, layer_fail);
+            launch_lu_solve(st, n, n, 1, C, nn, C, nn, RHS_IDENTITY, nullptr, nn, ld[k].cinv, nn, layer_fail);
+        }
+    }
+
+    // chunk size: rough upper bound of live device bytes per sample
+    const long long per_sample = 16LL * (nn * (12 + 4 * (long long)grating.size()) + (long long)n * (8LL * (L + 2) + 64)) +
+                                 eig_workspace_bytes(n, 1);
+    long long chunk = chunk_bytes > 0 ? (long long)chunk_bytes / std::max(1LL, per_sample) : n_points;
+    chunk = std::max(1LL, std::min<long long>(chunk, n_points));
+
+    for (int p0 = 0; p0 < n_points; p0 += (int)chunk) {
+        const int B = (int)std::min<long long>(chunk, n_points - p0);
+        DeviceScratch mem(st);
+        Batch c{st, &mem, B, n, M, nullptr, nullptr};
+        c.fail = mem.zeros<int>(B);
+        c.extra_solves = mem.zeros<int>(B);
+        int* eig_info = mem.zeros<int>(B);
+        int* zero_any = mem.zeros<int>(1);
+        const long long nv = (long long)B * n, nd = (long long)B * nn;
+
+        double* kx = mem.get<double>(nv);
+        double* k0 = mem.get<double>(B);
+        LAUNCH(kx_kernel, nblocks(nv), kTpb, st, B, M, d_s + p0, d_wl + p0, stack.period, kx);
+        LAUNCH(k0_kernel, nblocks(B), kTpb, st, B, d_wl + p0, k0);
+
+        // ---- 1. modes of every region (region 0: nI, region j+1: layer j, region L+1: nII)
+        std::vector<DModes> modes(L + 2);
+        const auto analytic = [&](DModes& m, rcwa_complex idx, int fzb) {
+            m.analytic = true;
+            m.fzb = fzb != 0;
+            m.q = c.vec();
+            m.p = c.vec();
+            LAUNCH(analytic_modes_kernel, nblocks(nv), kTpb, st, B, n, kx, zc{idx.re, idx.im}, pol, fzb, m.q, m.p, nullptr);
+        };
+        analytic(modes[0], stack.nI, 0);
+        analytic(modes[L + 1], stack.nII, 0);
+        for (int k = 0; k < L; ++k)
+            if (stack.layers[k].homogeneous) analytic(modes[k + 1], stack.layers[k].n, 1);
+
+        if (!grating.empty()) {
+            zc* ws = mem.get<zc>((size_t)(eig_workspace_bytes(n, B) / sizeof(zc)) + 1);
+            int* info = mem.get<int>(B);
+            double* resid = nullptr;
+            if (opt.diagnostics) resid = mem.zeros<double>(B);
+            for (int k : grating) {
+                // 1a. layer matrix
+                zc* A = c.dense();
+                if (pol == RCWA_TE) {
+                    LAUNCH(assemble_te_kernel, nblocks(nd), kTpb, st, B, M, ld[k].c_eps, kx, A);
+                } else {
+                    zc* mid = c.dense();
+                    LAUNCH(tm_middle_kernel, nblocks(nd), kTpb, st, B, n, ld[k].einv, kx, mid);
+                    gemm(c, ld[k].cinv, 0, mid, nullptr, 1.0, 0.0, A);
+                    mem.free(mid);
+                    c.n_solve += 2;  // the reference forms A with two dense solves per sample
+                }
+                LAUNCH(finite_check_kernel, nblocks(nd), kTpb, st, B, nn, A, c.fail);
+                // 1b. eigen-decomposition
+                DModes& m = modes[k + 1];
+                m.analytic = false;
+                m.fzb = true;
+                zc* lam = c.vec();
+                m.W = c.dense();
+                launch_eig(st, n, B, A, nn, lam, m.W, info, nullptr, ws, opt.eps, opt.max_iter, opt.eig_group);
+                LAUNCH(eig_info_kernel, nblocks(B), kTpb, st, B, info, eig_info, c.fail);
+                if (opt.diagnostics) {
+                    zc* av = gemm(c, A, nn, m.W, nullptr, 1.0, 0.0);
+                    LAUNCH(eig_residual_kernel, warp_blocks(B), 128, st, B, n, A, av, m.W, lam, info, resid);
+                    mem.free(av);
+                }
+                mem.free(A);
+                // 1c. q = branch(sqrt(lambda)), V = W q (TE) or [[1/eps]] W q (TM)
+                m.q = c.vec();
+                zc* bq = c.vec();
+                int* zf = mem.zeros<int>(B);
+                LAUNCH(eig_modes_q_kernel, nblocks(nv), kTpb, st, B, n, lam, m.q, bq, zf);
+                m.V = c.dense();
+                if (pol == RCWA_TE) {
+                    LAUNCH(scale_cols_kernel, nblocks(nd), kTpb, st, B, n, m.W, bq, m.V, nullptr, 1);
+                } else {
+                    zc* cw = gemm(c, ld[k].inv_eps, 0, m.W, nullptr, 1.0, 0.0);
+                    LAUNCH(scale_cols_kernel, nblocks(nd), kTpb, st, B, n, cw, bq, m.V, nullptr, 1);
+                    mem.free(cw);
+                }
+                mem.free(lam);
+                mem.free(bq);
+            }
+            if (opt.diagnostics)
+                RCWA_CUDA(cudaMemcpyAsync(d_out.max_eig_residual + p0, resid, B * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            mem.free(ws);
+        } else if (opt.diagnostics && d_out.max_eig_residual) {
+            RCWA_CUDA(cudaMemsetAsync(d_out.max_eig_residual + p0, 0, B * sizeof(double), st));
+        }
+
+        // ---- 2. bottom-up recursion (include/stablercwa/rcwa1d.hpp:965-987)
+        const int block_count = 2 * L + 1;
+        std::vector<DOp> g(block_count);
+        DOp r;  // Zero: nothing comes up from the exit medium
+        for (int b = block_count - 1; b >= 1; --b) {
+            const int j = b / 2;
+            if (b % 2 == 0 && modes[j].analytic && modes[j + 1].analytic && r.kind != KDense) {
+                // Fresnel block between two analytic regions stacked on a diagonal (or zero) reflection
+                DSBlock blk = interface_block(c, modes[j], modes[j + 1]);
+                zc* gv = c.vec();
+                zc* rv = c.vec();
+                LAUNCH(stack_on_diag_kernel, nblocks(nv), kTpb, st, nv, blk.Tdd.p, blk.Rdu.p, blk.Rud.p, blk.Tuu.p,
+                       r.kind == KZero ? nullptr : r.p, gv, rv);
+                mem.free(blk.Tdd.p);
+                mem.free(blk.Rdu.p);
+                mem.free(blk.Rud.p);
+                mem.free(blk.Tuu.p);
+                if (r.kind == KDiag) mem.free(r.p);
+                g[b] = {KDiag, gv};
+                r = {KDiag, rv};
+                continue;
+            }
+            if (b % 2 == 0) {
+                DSBlock blk = interface_block(c, modes[j], modes[j + 1]);
+                Seam seam = stack_on(c, std::move(blk), r);
+                g[b] = seam.g;
+                r = seam.r;
+                continue;
+            }
+            // propagation through layer j (include/stablercwa/rcwa1d.hpp:751-784)
+            const DModes& m = modes[j + 1];
+            zc* x = c.vec();
+            zc* refl = c.vec();
+            int* hz = mem.zeros<int>(B);
+            LAUNCH(propagation_kernel, nblocks(nv), kTpb, st, B, n, m.q, k0, stack.layers[j].d, m.fzb ? 1 : 0, x, refl, hz,
+                   c.fail);
+            if (r.kind != KDense) {
+                // every operator diagonal: k = Rdu r is zero unless q == 0 somewhere, which the diagonal
+                // recurrence evaluates exactly as the reference's Zero path would
+                zc* gv = c.vec();
+                zc* rv = c.vec();
+                LAUNCH(stack_on_diag_kernel, nblocks(nv), kTpb, st, nv, x, refl, refl, x, r.kind == KZero ? nullptr : r.p, gv, rv);
+                g[b] = {KDiag, gv};
+                r = {KDiag, rv};
+                continue;
+            }
+            // dense r: g = Tdd (diagonal) and r' = x r x, except for samples with an exact q == 0 in this
+            // layer, which take the dense branch g = (I - Rdu r)^{-1} Tdd, r' = Rud + Tuu r g.
+            zc* rn = c.dense();
+            LAUNCH(scale_both_kernel, nblocks(nd), kTpb, st, B, n, r.p, x, x, rn, hz, 1);
+            {
+                int any = 0;
+                const unsigned rb = nblocks(B);
+                // reduce the per-sample flags into one word and read it back
+                RCWA_CUDA(cudaMemsetAsync(zero_any, 0, sizeof(int), st));
+                LAUNCH(any_flag_kernel, rb, kTpb, st, B, hz, zero_any);
+                RCWA_CUDA(cudaMemcpyAsync(&any, zero_any, sizeof(int), cudaMemcpyDeviceToHost, st));
+                RCWA_CUDA(cudaStreamSynchronize(st));
+                if (any) {
+                    zc* k = c.dense();
+                    LAUNCH(scale_rows_kernel, nblocks(nd), kTpb, st, B, n, r.p, refl, k, hz, 0);
+                    LAUNCH(identity_minus_kernel, nblocks(nd), kTpb, st, B, n, k, hz, 0);
+                    zc* td = c.mem->zeros<zc>((size_t)nd);
+                    LAUNCH(diag_to_dense_kernel, nblocks(nd), kTpb, st, B, n, x, td, hz, 0);
+                    zc* gd = c.dense();
+                    launch_lu_solve(st, n, n, B, k, nn, k, nn, RHS_DENSE, td, nn, gd, nn, c.fail, hz, 0);
+                    LAUNCH(inc_flagged_kernel, rb, kTpb, st, B, hz, c.extra_solves);
+                    zc* y = gemm(c, r.p, nn, gd, nullptr, 1.0, 0.0, nullptr, hz, 0);
+                    LAUNCH(scale_rows_kernel, nblocks(nd), kTpb, st, B, n, y, x, rn, hz, 0);
+                    LAUNCH(add_diag_kernel, nblocks(nv), kTpb, st, B, n, rn, refl, hz, 0);
+                    mem.free(k);
+                    mem.free(td);
+                    mem.free(y);
+                    g[b] = {KDiag, x, gd, hz};
+                } else {
+                    g[b] = {KDiag, x};
+                }
+            }
+            r = {KDense, rn};
+        }
+
+        // ---- 3. top interface, only column M (include/stablercwa/rcwa1d.hpp:714-746, :989-1023)
+        zc* tdd = c.vec();
+        zc* rud = c.vec();
+        DOp topRdu, topTuu;
+        if (modes[0].analytic && modes[1].analytic) {
+            zc* Tdd = c.vec();
+            zc* Rdu = c.vec();
+            zc* Rud = c.vec();
+            zc* Tuu = c.vec();
+            LAUNCH(diagonal_interface_kernel, nblocks(nv), kTpb, st, nv, modes[0].p, modes[1].p, Tdd, Rdu, Rud, Tuu);
+            LAUNCH(top_diag_vectors_kernel, nblocks(nv), kTpb, st, B, n, M, Tdd, Rud, tdd, rud);
+            topRdu = {KDiag, Rdu};
+            topTuu = {KDiag, Tuu};
+        } else {
+            zc *tp, *tm;
+            interface_matching(c, modes[0], modes[1], tp, tm);
+            zc* tpi = solve(c, tp, false, RHS_IDENTITY, nullptr);
+            zc* rdu = gemm(c, tm, nn, tpi, nullptr, 1.0, 0.0);
+            zc* tm_e = c.vec();
+            LAUNCH(col_extract_kernel, nblocks(nv), kTpb, st, B, n, tm, M, tm_e);
+            LAUNCH(col_extract_kernel, nblocks(nv), kTpb, st, B, n, tp, M, tdd);
+            LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, rdu, tm_e, tdd, tdd, 1.0 * -1.0, 1.0);
+            LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, tpi, tm_e, nullptr, rud, -1.0, 0.0);
+            mem.free(tp);
+            mem.free(tm);
+            topRdu = {KDense, rdu};
+            topTuu = {KDense, tpi};
+        }
+        DOp k = op_mul(c, topRdu, r);
+        zc* down = tdd;
+        if (k.kind == KDiag) {
+            LAUNCH(vec_div_one_minus_kernel, nblocks(nv), kTpb, st, nv, down, k.p);
+        } else if (k.kind == KDense) {
+            LAUNCH(identity_minus_kernel, nblocks(nd), kTpb, st, B, n, k.p, nullptr, 1);
+            down = solve(c, k.p, true, RHS_DENSE, tdd, 1);
+        }
+        // R = rud + Tuu (r down)
+        zc* rdn = c.vec();
+        LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, (int)r.kind, r.p, nullptr, nullptr, down, rdn);
+        zc* back = c.vec();
+        LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, (int)topTuu.kind, topTuu.p, nullptr, nullptr, rdn, back);
+        LAUNCH(vec_add_kernel, nblocks(nv), kTpb, st, nv, back, rud);  // rud = back + rud
+        zc* Rv = rud;
+        // T = g[2L] ... g[1] down
+        zc* cur = down;
+        zc* nxt = c.vec();
+        for (int b = 1; b < block_count; ++b) {
+            LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, (int)g[b].kind, g[b].p, g[b].alt, g[b].alt_flag, cur, nxt);
+            std::swap(cur, nxt);
+        }
+        zc* Tv = cur;
+
+        // ---- 4. efficiencies, NaN fill, status
+        LAUNCH(finalize_kernel, warp_blocks(B), 128, st, B, n, M, pol, pure_films ? 1 : 0, Rv, Tv, modes[0].q,
+               modes[L + 1].q, k0, nI, nII, c.fail, reinterpret_cast<zc*>(d_out.R) + (long long)p0 * n,
+               reinterpret_cast<zc*>(d_out.T) + (long long)p0 * n, d_out.DEr + (long long)p0 * n,
+               d_out.DEt + (long long)p0 * n);
+        LAUNCH(status_kernel, nblocks(B), kTpb, st, B, c.fail, eig_info, c.n_solve, c.extra_solves, (int)grating.size(),
+               d_out.status ? d_out.status + p0 : nullptr, d_out.eig_info ? d_out.eig_info + p0 : nullptr,
+               d_out.n_eig ? d_out.n_eig + p0 : nullptr, d_out.n_dense_solve ? d_out.n_dense_solve + p0 : nullptr);
+        mem.release();
+    }
+    // A singular [[eps]] or [[1/eps]] (TM) fails every sample; checked once at the end.
+    int lf = 0;
+    RCWA_CUDA(cudaMemcpyAsync(&lf, layer_fail, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RCWA_CUDA(cudaStreamSynchronize(st));
+    if (lf) {
+        // reference: the TM assembly solve throws NumericalFailure for every point
+        const double nan = std::nan("");
+        std::vector<double> nans((size_t)n_points * n * 2, nan);
+        RCWA_CUDA(cudaMemcpyAsync(d_out.R, nans.data(), (size_t)n_points * n * sizeof(zc), cudaMemcpyHostToDevice, st));
+        RCWA_CUDA(cudaMemcpyAsync(d_out.T, nans.data(), (size_t)n_points * n * sizeof(zc), cudaMemcpyHostToDevice, st));
+        RCWA_CUDA(cudaMemcpyAsync(d_out.DEr, nans.data(), (size_t)n_points * n * sizeof(double), cudaMemcpyHostToDevice, st));
+        RCWA_CUDA(cudaMemcpyAsync(d_out.DEt, nans.data(), (size_t)n_points * n * sizeof(double), cudaMemcpyHostToDevice, st));
+        if (d_out.status) {
+            std::vector<int> s(n_points, RCWA_SAMPLE_NUMERICAL);
+            RCWA_CUDA(cudaMemcpyAsync(d_out.status, s.data(), n_points * sizeof(int), cudaMemcpyHostToDevice, st));
+        }
+        RCWA_CUDA(cudaStreamSynchronize(st));
+    }
+}
+
+// ---------------------------------------------------------------- device-side point preparation
+
+namespace {
+__global__ void prepare_points_kernel(int N, const rcwa_point1d* __restrict__ pts, double nI, double* __restrict__ s,
+                                      double* __restrict__ wl, int* __restrict__ bad) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= N) return;
+    const double w = pts[p].wavelength, th = pts[p].theta_deg;
+    if (!isfinite(w) || w <= 0.0 || !isfinite(th) || fabs(th) >= 90.0) atomicOr(bad, 1);
+    wl[p] = w;
+    s[p] = nI * sin(th * 3.141592653589793238462643383279502884 / 180.0);
+}
+}  // namespace
+
+bool prepare_points_device(cudaStream_t st, const rcwa_point1d* d_points, int n_points, double nI, double* d_s,
+                           double* d_wl) {
+    DeviceScratch mem(st);
+    int* bad = mem.zeros<int>(1);
+    LAUNCH(prepare_points_kernel, nblocks(n_points), kTpb, st, n_points, d_points, nI, d_s, d_wl, bad);
+    int h = 0;
+    RCWA_CUDA(cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RCWA_CUDA(cudaStreamSynchronize(st));
+    return h == 0;
+}
+
+}  // namespace rcwa_gb300

@@ -1,0 +1,264 @@
+// rcwa1d_kernels.cuh -- per-sample elementwise kernels of the batched 1-D TE/TM solve.
+//
+// Every kernel works on a chunk of B sweep points. Diagonal operators are B x n vectors, dense
+// operators B x n x n column-major matrices. Where the reference's result depends on an exact
+// floating-point equality (q == 0 selects the linear-field branch, include/stablercwa/rcwa1d.hpp:
+// 534, :756, :956), the operands are formed with explicitly rounded intrinsics so that no fused
+// multiply-add changes which branch a sample takes.
+#pragma once
+
+#include "common.cuh"
+
+namespace rcwa_gb300 {
+
+// kx_m = s - (m - M) lambda / period (include/stablercwa/rcwa1d.hpp:410-415). s = nI sin(theta) is
+// computed on the host with the host's libm, exactly as the reference does, and passed per sample.
+__global__ void kx_kernel(int B, int M, const double* __restrict__ s, const double* __restrict__ wl, double period,
+                          double* __restrict__ kx) {
+    const int n = 2 * M + 1;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * n) return;
+    const int b = (int)(idx / n), j = (int)(idx - (long long)b * n);
+    kx[idx] = __dsub_rn(s[b], __ddiv_rn(__dmul_rn((double)(j - M), wl[b]), period));
+}
+
+// Analytic modes of a homogeneous region of index nidx (include/stablercwa/rcwa1d.hpp:522-544):
+// kz = sqrt(n^2 - kx^2) with Im kz >= 0 (Re >= 0 when Im ~ 0), q = -i kz, p = q (TE) or q/n^2 (TM);
+// with finite_zero_basis an exact q == 0 uses the auxiliary basis q = 1 in p.
+__global__ void analytic_modes_kernel(int B, int n, const double* __restrict__ kx, zc nidx, int pol, int fzb,
+                                      zc* __restrict__ q, zc* __restrict__ p, int* __restrict__ zero_flag) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * n) return;
+    const double k = kx[idx];
+    const zc n2 = zc{__dsub_rn(__dmul_rn(nidx.re, nidx.re), __dmul_rn(nidx.im, nidx.im)),
+                     __dadd_rn(__dmul_rn(nidx.re, nidx.im), __dmul_rn(nidx.im, nidx.re))};
+    zc kz = zsqrt(zc{__dsub_rn(n2.re, __dmul_rn(k, k)), n2.im});
+    if (kz.im < 0.0) kz = -kz;
+    if (fabs(kz.im) < 1e-12 && kz.re < 0.0) kz = -kz;
+    const zc qq = zc{kz.im, -kz.re};
+    q[idx] = qq;
+    const bool zero = is_zero(qq);
+    const zc bq = (fzb && zero) ? zc{1.0, 0.0} : qq;
+    p[idx] = pol == 0 ? bq : zdiv(bq, n2);
+    if (zero_flag && fzb && zero) zero_flag[idx / n] = 1;
+}
+
+// TE layer matrix A = Kx^2 - [[eps]] from the Toeplitz coefficients c_h, h = -2M..2M
+// (include/stablercwa/rcwa1d.hpp:450-457): A(i,j) = -c_{i-j}, plus kx_i^2 on the diagonal.
+__global__ void assemble_te_kernel(int B, int M, const zc* __restrict__ c, const double* __restrict__ kx,
+                                   zc* __restrict__ A) {
+    const int n = 2 * M + 1;
+    const long long nn = (long long)n * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * nn) return;
+    const int b = (int)(idx / nn);
+    const int rem = (int)(idx - (long long)b * nn);
+    const int j = rem / n, i = rem - j * n;
+    const zc v = c[i - j + 2 * M];
+    zc a = zc{-v.re, -v.im};
+    if (i == j) {
+        const double k = kx[(long long)b * n + i];
+        a.re = __dadd_rn(a.re, __dmul_rn(k, k));
+    }
+    A[idx] = a;
+}
+
+// TM: the per-sample middle factor Kx [[eps]]^{-1} Kx - I of
+// A = [[1/eps]]^{-1} (Kx [[eps]]^{-1} Kx - I) (include/stablercwa/rcwa1d.hpp:459-466).
+// einv is the sample-independent inverse of [[eps]].
+__global__ void tm_middle_kernel(int B, int n, const zc* __restrict__ einv, const double* __restrict__ kx,
+                                 zc* __restrict__ out) {
+    const long long nn = (long long)n * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * nn) return;
+    const int b = (int)(idx / nn);
+    const int rem = (int)(idx - (long long)b * nn);
+    const int j = rem / n, i = rem - j * n;
+    const double kj = kx[(long long)b * n + j], ki = kx[(long long)b * n + i];
+    const zc e = einv[rem];
+    zc v = zc{(e.re * kj) * ki, (e.im * kj) * ki};
+    if (i == j) v.re -= 1.0;
+    out[idx] = v;
+}
+
+// Modes of an eigen-decomposed layer (include/stablercwa/rcwa1d.hpp:949-958):
+// q = branch(sqrt(lambda)) with Re q >= 0 and Im q <= 0 when Re q < 1e-10; basis q = 1 where q == 0.
+__device__ __forceinline__ zc branch(zc q) {
+    if (q.re < 0.0) q = -q;
+    if (q.re < 1e-10 && q.im > 0.0) q = -q;
+    return q;
+}
+__global__ void eig_modes_q_kernel(int B, int n, const zc* __restrict__ lambda, zc* __restrict__ q,
+                                   zc* __restrict__ bq, int* __restrict__ zero_flag) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * n) return;
+    const zc qq = branch(zsqrt(lambda[idx]));
+    q[idx] = qq;
+    const bool zero = is_zero(qq);
+    bq[idx] = zero ? zc{1.0, 0.0} : qq;
+    if (zero) zero_flag[idx / n] = 1;
+}
+
+// dst(i,j) = src(i,j) * d_j  (scale_columns, include/stablercwa/matrix.hpp:194-201)
+__global__ void scale_cols_kernel(int B, int n, const zc* __restrict__ src, const zc* __restrict__ d,
+                                  zc* __restrict__ dst, const int* __restrict__ skip, int skip_value) {
+    const long long nn = (long long)n * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * nn) return;
+    const int b = (int)(idx / nn);
+    if (skip && skip[b] == skip_value) return;
+    const int j = (int)((idx - (long long)b * nn) / n);
+    dst[idx] = src[idx] * d[(long long)b * n + j];
+}
+// dst(i,j) = d_i * src(i,j)  (scale_rows, include/stablercwa/matrix.hpp:202-210)
+__global__ void scale_rows_kernel(int B, int n, const zc* __restrict__ src, const zc* __restrict__ d,
+                                  zc* __restrict__ dst, const int* __restrict__ skip, int skip_value) {
+    const long long nn = (long long)n * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * nn) return;
+    const int b = (int)(idx / nn);
+    if (skip && skip[b] == skip_value) return;
+    const int rem = (int)(idx - (long long)b * nn);
+    const int j = rem / n, i = rem - j * n;
+    (void)j;
+    dst[idx] = src[idx] * d[(long long)b * n + i];
+}
+// dst(i,j) = d_i * src(i,j) * e_j  (Diag * Dense * Diag)
+__global__ void scale_both_kernel(int B, int n, const zc* __restrict__ src, const zc* __restrict__ dl,
+                                  const zc* __restrict__ dr, zc* __restrict__ dst, const int* __restrict__ skip,
+                                  int skip_value) {
+    const long long nn = (long long)n * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * nn) return;
+    const int b = (int)(idx / nn);
+    if (skip && skip[b] == skip_value) return;
+    const int rem = (int)(idx - (long long)b * nn);
+    const int j = rem / n, i = rem - j * n;
+    dst[idx] = dl[(long long)b * n + i] * (src[idx] * dr[(long long)b * n + j]);
+}
+
+// tp = (mm + nn)/2, tm = (mm - nn)/2 with nn = rows of V scaled by 1/p_low (the lower side analytic)
+// or nn given (include/stablercwa/rcwa1d.hpp:664-692).
+__global__ void tp_tm_kernel(int B, int n, const zc* __restrict__ mm, const zc* __restrict__ nn_or_v,
+                             const zc* __restrict__ p_low, zc* __restrict__ tp, zc* __restrict__ tm) {
+    const long long nn = (long long)n * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * nn) return;
+    zc v = nn_or_v[idx];
+    if (p_low) {
+        const int b = (int)(idx / nn);
+        const int i = (int)((idx - (long long)b * nn) % n);
+        v = v * zinv(p_low[(long long)b * n + i]);
+    }
+    const zc m = mm[idx];
+    tp[idx] = 0.5 * (m + v);
+    tm[idx] = 0.5 * (m - v);
+}
+
+// I - m in place (include/stablercwa/rcwa1d.hpp:623-629)
+__global__ void identity_minus_kernel(int B, int n, zc* __restrict__ m, const int* __restrict__ skip, int skip_value) {
+    const long long nn = (long long)n * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * nn) return;
+    const int b = (int)(idx / nn);
+    if (skip && skip[b] == skip_value) return;
+    const int rem = (int)(idx - (long long)b * nn);
+    const int j = rem / n, i = rem - j * n;
+    zc v = -m[idx];
+    if (i == j) v.re += 1.0;
+    m[idx] = v;
+}
+
+// dense += diag (or dense = diag + dense when the diagonal comes first; same sums)
+__global__ void add_diag_kernel(int B, int n, zc* __restrict__ m, const zc* __restrict__ d, const int* __restrict__ skip,
+                                int skip_value) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * n) return;
+    const int b = (int)(idx / n);
+    if (skip && skip[b] == skip_value) return;
+    const int i = (int)(idx - (long long)b * n);
+    zc* p = m + (long long)b * n * n + (long long)i * n + i;
+    *p = *p + d[idx];
+}
+
+// dense a += dense b
+__global__ void add_dense_kernel(long long total, zc* __restrict__ a, const zc* __restrict__ b) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < total) a[idx] = a[idx] + b[idx];
+}
+
+// densify a diagonal operator
+__global__ void diag_to_dense_kernel(int B, int n, const zc* __restrict__ d, zc* __restrict__ m,
+                                     const int* __restrict__ skip, int skip_value) {
+    const long long nn = (long long)n * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * nn) return;
+    const int b = (int)(idx / nn);
+    if (skip && skip[b] == skip_value) return;
+    const int rem = (int)(idx - (long long)b * nn);
+    const int j = rem / n, i = rem - j * n;
+    m[idx] = i == j ? d[(long long)b * n + i] : zc{0.0, 0.0};
+}
+
+// Fresnel blocks between two analytic regions (include/stablercwa/rcwa1d.hpp:644-661)
+__global__ void diagonal_interface_kernel(long long total, const zc* __restrict__ p1, const zc* __restrict__ p2,
+                                          zc* __restrict__ tdd, zc* __restrict__ rdu, zc* __restrict__ rud,
+                                          zc* __restrict__ tuu) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const zc a = p1[idx], b = p2[idx];
+    const zc inv = zinv(a + b);
+    tdd[idx] = (2.0 * a) * inv;
+    rdu[idx] = (b - a) * inv;
+    rud[idx] = (a - b) * inv;
+    tuu[idx] = (2.0 * b) * inv;
+}
+
+// Propagation factors exp(-k0 d q) and the exact q == 0 linear-field block
+// (include/stablercwa/rcwa1d.hpp:751-784): Tdd = Tuu = 1/(1 + h/2), Rdu = Rud = (h/2)/(1 + h/2), h = k0 d.
+__global__ void propagation_kernel(int B, int n, const zc* __restrict__ q, const double* __restrict__ k0, double d,
+                                   int fzb, zc* __restrict__ x, zc* __restrict__ refl, int* __restrict__ has_zero,
+                                   int* __restrict__ fail) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * n) return;
+    const int b = (int)(idx / n);
+    const zc qq = q[idx];
+    const double kd = k0[b];
+    if (fzb && is_zero(qq)) {
+        const double h = kd * d;
+        if (!isfinite(h)) fail[b] = 1;
+        const double den = 1.0 + 0.5 * h;
+        x[idx] = zc{1.0 / den, 0.0};
+        refl[idx] = zc{(0.5 * h) / den, 0.0};
+        has_zero[b] = 1;
+    } else {
+        const double f = -kd * d;
+        x[idx] = zexp(zc{f * qq.re, f * qq.im});
+        refl[idx] = zc{0.0, 0.0};
+    }
+}
+
+// Diagonal stack_on step: k = Rdu r, g = Tdd / (1 - k), r' = Rud + Tuu r g
+// (include/stablercwa/rcwa1d.hpp:794-808 with every operator diagonal; a missing Rdu/Rud is zero).
+__global__ void stack_on_diag_kernel(long long total, const zc* __restrict__ tdd, const zc* __restrict__ rdu,
+                                     const zc* __restrict__ rud, const zc* __restrict__ tuu, const zc* __restrict__ r,
+                                     zc* __restrict__ g, zc* __restrict__ rout) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const zc t = tdd[idx];
+    const zc rv = r ? r[idx] : zc{0.0, 0.0};
+    zc gv;
+    if (rdu && r) {
+        const zc k = rdu[idx] * rv;
+        const zc f = zinv(zc{1.0, 0.0} - k);
+        gv = f * t;
+    } else {
+        gv = t;
+    }
+    g[idx] = gv;
+    zc out = r ? tuu[idx] * (rv * gv) : zc{0.0, 0.0};
+    if (rud) out = rud[idx] + out;
+    rout[idx] = out;
+}
+
+}  // namespace rcwa_gb300

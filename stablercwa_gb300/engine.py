@@ -1,0 +1,205 @@
+"""Host-side mirror of StableRCWA's solve API over the engine's C ABI.
+
+    from stablercwa_gb300 import Layer, Stack, TE
+    from stablercwa_gb300.engine import Engine
+    eng = Engine()
+    r = eng.solve(stack, 1.053, 66.36, 20, TE)      # rcwa::solve (include/stablercwa/rcwa1d.hpp:1077)
+    rs = eng.sweep(stack, points, 60, TE)            # rcwa::sweep (include/stablercwa/rcwa1d.hpp:1084)
+
+Invalid arguments raise ValueError where the reference throws std::invalid_argument; numerical
+failures give NaN results with a status, as the reference does. The compute path is
+libstablercwa_gb300.so; there is no CPU fallback: without the library or a CUDA device the
+constructor raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .types import Options, Result
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "_build", "libstablercwa_gb300.so")
+_lib = None
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(f"rcwa_gb300 error {code}: {message}")
+        self.code = code
+
+
+class UnsupportedOption(EngineError):
+    pass
+
+
+def library_path():
+    return _LIB
+
+
+def load_library(build_if_missing=True):
+    """Load libstablercwa_gb300.so (building it in-tree first if it is missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        from . import build as _build
+        _build.build()
+    if not os.path.exists(_LIB):
+        raise EngineError(abi.RCWA_ECUDA, f"{_LIB} is missing: run stablercwa_gb300/build.py")
+    L = C.CDLL(_LIB)
+    vp, ci, cd = C.c_void_p, C.c_int, C.c_double
+    L.rcwa_gpu_create.argtypes = [C.POINTER(abi.rcwa_gpu_config), C.POINTER(vp)]
+    L.rcwa_gpu_destroy.argtypes = [vp]
+    L.rcwa_gpu_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+    L.rcwa_gpu_synchronize.argtypes = [vp]
+    L.rcwa_gpu_launch_count.restype = C.c_longlong
+    L.rcwa_options_default.argtypes = [C.POINTER(abi.rcwa_options)]
+    L.rcwa_gpu_solve1d_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack1d), vp, ci, ci, ci, C.POINTER(abi.rcwa_options),
+                                         C.POINTER(abi.rcwa_result1d)]
+    L.rcwa_gpu_solve1d_batch_dev.argtypes = L.rcwa_gpu_solve1d_batch.argtypes
+    L.rcwa_gpu_eig_batch.argtypes = [vp, ci, ci, vp, cd, ci, vp, vp, vp, vp]
+    L.rcwa_gpu_eig_batch_dev.argtypes = [vp, ci, ci, vp, cd, ci, vp, vp, vp, vp]
+    L.rcwa_gpu_solve_batch.argtypes = [vp, ci, ci, ci, vp, vp, vp, vp]
+    L.rcwa_gpu_multiply_batch.argtypes = [vp, ci, ci, ci, ci, vp, vp, vp]
+    _lib = L
+    return L
+
+
+def launch_count():
+    return int(load_library().rcwa_gpu_launch_count())
+
+
+def _options(opt):
+    o = abi.rcwa_options()
+    load_library().rcwa_options_default(C.byref(o))
+    if opt is not None:
+        o.homogeneous_fast_path = 1 if opt.homogeneous_fast_path else 0
+        o.diagnostics = 1 if opt.diagnostics else 0
+        o.eig_max_iter = int(opt.eig_max_iter)
+        o.eig_eps = float(opt.eig_eps)
+    return o
+
+
+def _colmajor(a):
+    """(batch, n, m) row-indexed arrays -> column-major per matrix (contiguous)."""
+    a = np.asarray(a, dtype=np.complex128)
+    return np.ascontiguousarray(a.transpose(0, 2, 1))
+
+
+class Engine:
+    """One engine context on one CUDA device (rcwa_gpu_create / rcwa_gpu_destroy)."""
+
+    def __init__(self, device=0, workspace_limit=0):
+        self.L = load_library()
+        cfg = abi.rcwa_gpu_config(device, workspace_limit)
+        h = C.c_void_p()
+        rc = self.L.rcwa_gpu_create(C.byref(cfg), C.byref(h))
+        if rc != 0:
+            raise EngineError(rc, self._err(None))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.rcwa_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _err(self, h):
+        buf = C.create_string_buffer(1024)
+        self.L.rcwa_gpu_last_error(h, buf, 1024)
+        return buf.value.decode(errors="replace")
+
+    def _check(self, rc):
+        if rc == abi.RCWA_EINVAL:
+            raise ValueError(self._err(self.h))
+        if rc == abi.RCWA_EUNSUPPORTED:
+            raise UnsupportedOption(rc, self._err(self.h))
+        if rc != 0:
+            raise EngineError(rc, self._err(self.h))
+
+    # ---------------------------------------------------------------- 1-D solve
+
+    def solve1d_arrays(self, stack, points, M, pol, options=None):
+        """Batched solve with host buffers; returns a dict of numpy arrays (R, T, DEr, DEt, status,
+        eig_info, n_eig, n_dense_solve, max_eig_residual)."""
+        st, keep = abi.marshal_stack1d(stack)
+        pts = abi.points_array(points)
+        res, arrays = abi.result_views(len(pts), M)
+        o = _options(options)
+        self._check(self.L.rcwa_gpu_solve1d_batch(self.h, C.byref(st), pts.ctypes.data, len(pts), M, pol, C.byref(o),
+                                                  C.byref(res)))
+        return arrays
+
+    def solve1d_device(self, stack, d_points, n_points, M, pol, d_out, options=None):
+        """Batched solve on device memory. d_points: device address of n_points (wavelength, theta)
+        double pairs; d_out: dict of device addresses for R, T, DEr, DEt, status (others optional)."""
+        st, keep = abi.marshal_stack1d(stack)
+        res = abi.rcwa_result1d()
+        for k in ("R", "T", "DEr", "DEt", "status", "eig_info", "n_eig", "n_dense_solve", "max_eig_residual"):
+            setattr(res, k, d_out.get(k))
+        o = _options(options)
+        self._check(self.L.rcwa_gpu_solve1d_batch_dev(self.h, C.byref(st), d_points, n_points, M, pol, C.byref(o),
+                                                      C.byref(res)))
+
+    def synchronize(self):
+        self._check(self.L.rcwa_gpu_synchronize(self.h))
+
+    def sweep(self, stack, points, M, pol, options=None):
+        a = self.solve1d_arrays(stack, points, M, pol, options)
+        orders = np.arange(-M, M + 1)
+        return [Result(orders=orders, R=a["R"][p], T=a["T"][p], DEr=a["DEr"][p], DEt=a["DEt"][p],
+                       eig_info=int(a["eig_info"][p]), n_eig=int(a["n_eig"][p]),
+                       n_dense_solve=int(a["n_dense_solve"][p]), status=int(a["status"][p]),
+                       max_eig_residual=float(a["max_eig_residual"][p])) for p in range(len(a["status"]))]
+
+    def solve(self, stack, wavelength, theta_deg, M, pol=0, options=None):
+        return self.sweep(stack, [(wavelength, theta_deg)], M, pol, options)[0]
+
+    # ---------------------------------------------------------------- dense kernels (custom_* hooks)
+
+    def eig_batch(self, a, eps=float(np.finfo(np.float64).eps), max_iter=30):
+        """a: (batch, n, n). Returns values (batch, n), vectors (batch, n, n) with columns the
+        eigenvectors, info (batch,), sweeps (batch,)."""
+        a = np.asarray(a, dtype=np.complex128)
+        batch, n = a.shape[0], a.shape[1]
+        cm = _colmajor(a)
+        w = np.empty((batch, n), np.complex128)
+        v = np.empty((batch, n, n), np.complex128)
+        info = np.empty(batch, np.int32)
+        sweeps = np.empty(batch, np.int32)
+        self._check(self.L.rcwa_gpu_eig_batch(self.h, n, batch, cm.ctypes.data, eps, max_iter, w.ctypes.data,
+                                              v.ctypes.data, info.ctypes.data, sweeps.ctypes.data))
+        return w, v.transpose(0, 2, 1), info, sweeps
+
+    def eig_batch_device(self, n, batch, d_a, d_w, d_v, d_info, d_sweeps=None, eps=float(np.finfo(np.float64).eps),
+                         max_iter=30):
+        self._check(self.L.rcwa_gpu_eig_batch_dev(self.h, n, batch, d_a, eps, max_iter, d_w, d_v, d_info, d_sweeps))
+
+    def solve_batch(self, a, b):
+        """Solve a[k] x[k] = b[k]; a: (batch, n, n), b: (batch, n, nrhs). Returns x, singular."""
+        a = np.asarray(a, dtype=np.complex128)
+        b = np.asarray(b, dtype=np.complex128)
+        batch, n, nrhs = b.shape
+        ca, cb = _colmajor(a), _colmajor(b)
+        x = np.empty((batch, nrhs, n), np.complex128)
+        sing = np.zeros(batch, np.int32)
+        self._check(self.L.rcwa_gpu_solve_batch(self.h, n, nrhs, batch, ca.ctypes.data, cb.ctypes.data, x.ctypes.data,
+                                                sing.ctypes.data))
+        return x.transpose(0, 2, 1), sing.astype(bool)
+
+    def multiply_batch(self, a, b):
+        a = np.asarray(a, dtype=np.complex128)
+        b = np.asarray(b, dtype=np.complex128)
+        batch, m, k = a.shape
+        n = b.shape[2]
+        ca, cb = _colmajor(a), _colmajor(b)
+        c = np.empty((batch, n, m), np.complex128)
+        self._check(self.L.rcwa_gpu_multiply_batch(self.h, m, k, n, batch, ca.ctypes.data, cb.ctypes.data, c.ctypes.data))
+        return c.transpose(0, 2, 1)

@@ -1,0 +1,58 @@
+"""The engine library builds, loads and exports every entry point its header declares (no GPU)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from stablercwa_gb300 import abi
+from stablercwa_gb300.engine import EngineError, load_library
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if not h.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:int|void|long long|double)\s+\**(rcwa_\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    L = load_library()
+    names = declared_functions()
+    assert len(names) >= 12
+    for name in sorted(names):
+        assert hasattr(L, name), name
+
+
+def test_struct_layouts_match_header():
+    # sizes the C compiler gives the header's structs on LP64 targets
+    assert C.sizeof(abi.rcwa_complex) == 16
+    assert C.sizeof(abi.rcwa_layer1d) == 8 + 8 + 16 + 8 + 8 + 8 + 8
+    assert C.sizeof(abi.rcwa_stack1d) == 16 + 16 + 8 + 8 + 8
+    assert C.sizeof(abi.rcwa_options) == 24 + 8
+    assert C.sizeof(abi.rcwa_result1d) == 9 * 8
+
+
+def test_abi_version_and_defaults():
+    L = load_library()
+    assert L.rcwa_gpu_abi_version() == 1
+    o = abi.rcwa_options()
+    L.rcwa_options_default(C.byref(o))
+    assert (o.eig_method, o.linear_solver, o.homogeneous_fast_path, o.eig_max_iter) == (0, 0, 1, 30)
+    assert o.eig_eps == 2.220446049250313e-16
+
+
+def test_create_without_device_reports_error():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from stablercwa_gb300.engine import Engine
+    with pytest.raises(EngineError):
+        Engine()

@@ -1,0 +1,102 @@
+"""GPU eigensolver, LU solve and GEMM through the C ABI, against the oracle and the reference's
+golden eigenvalues (tests/test_eig_qr.cpp matrices)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import cvec
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def eng():
+    from stablercwa_gb300.engine import Engine
+    e = Engine()
+    yield e
+    e.close()
+
+
+def residual(a, w, v):
+    # max_j ||A v_j - l_j v_j|| / (||A||_F ||v_j||)  (include/stablercwa/eig.hpp:38-69)
+    fro = np.linalg.norm(a)
+    d = a @ v - v * w[None, :]
+    return np.max(np.linalg.norm(d, axis=0) / (fro * np.linalg.norm(v, axis=0)))
+
+
+def match_values(got, ref):
+    """max over ref of distance to the nearest unused got value (permutation-invariant)."""
+    got = list(got)
+    worst = 0.0
+    for r in ref:
+        k = int(np.argmin([abs(g - r) for g in got]))
+        worst = max(worst, abs(got[k] - r))
+        got.pop(k)
+    return worst
+
+
+@pytest.mark.parametrize("group", ["4", "8", "16", "32"])
+def test_eig_golden(eng, eig_cases, group, monkeypatch):
+    monkeypatch.setenv("RCWA_GB300_EIG_GROUP", group)
+    for case in eig_cases:
+        n = case["n"]
+        a = cvec(case["a"]).reshape((n, n), order="F")
+        w, v, info, sweeps = eng.eig_batch(a[None], max_iter=case["max_iter"])
+        assert info[0] == case["info"], (case["name"], info[0])
+        ref = cvec(case["values"])
+        scale = max(1.0, np.max(np.abs(ref)))
+        if info[0] == 0:
+            assert match_values(w[0], ref) <= 1e-11 * scale, case["name"]
+            assert residual(a, w[0], v[0]) <= 1e-13, case["name"]
+            assert np.allclose(np.linalg.norm(v[0], axis=0), 1.0, atol=1e-13)
+        else:
+            i = info[0]
+            assert match_values(w[0][i:], ref[i:]) <= 1e-11 * scale, case["name"]
+
+
+def rcwa_matrix(n, index, fill=0.4, lop=0.61, sin_theta=0.2):
+    M = n // 2
+    e1, e2 = index * index, 1.0
+    h = np.subtract.outer(np.arange(n), np.arange(n))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        eps = np.where(h == 0, fill * e1 + (1 - fill) * e2, (e1 - e2) * np.sin(np.pi * h * fill) / (np.pi * h))
+    kx = sin_theta + (np.arange(n) - M) * lop
+    return -eps + np.diag(kx * kx)
+
+
+@pytest.mark.parametrize("n", [41, 81, 121])
+def test_eig_batch_vs_oracle(eng, n):
+    rng = np.random.default_rng(n)
+    mats = [rcwa_matrix(n, complex(rng.uniform(1.3, 2.2), rng.uniform(0, 0.2)), fill=rng.uniform(0.2, 0.6),
+                        sin_theta=rng.uniform(-0.5, 0.5)) for _ in range(6)]
+    a = np.array(mats)
+    w, v, info, sweeps = eng.eig_batch(a)
+    for k in range(len(mats)):
+        assert info[k] == 0
+        wo, vo, io, so = oracle.eig(mats[k])
+        assert match_values(w[k], wo) <= 1e-11 * np.max(np.abs(wo))
+        assert residual(mats[k], w[k], v[k]) <= 1e-13
+
+
+def test_lu_solve_and_gemm(eng):
+    rng = np.random.default_rng(5)
+    for n, nrhs in [(1, 1), (7, 3), (41, 41), (121, 121), (121, 1), (60, 20)]:
+        a = rng.standard_normal((4, n, n)) + 1j * rng.standard_normal((4, n, n))
+        b = rng.standard_normal((4, n, nrhs)) + 1j * rng.standard_normal((4, n, nrhs))
+        x, sing = eng.solve_batch(a, b)
+        assert not sing.any()
+        for k in range(4):
+            xo, so = oracle.solve(a[k], b[k])
+            assert np.max(np.abs(x[k] - xo)) <= 1e-10 * max(1.0, np.max(np.abs(xo)))
+    z = np.zeros((1, 3, 3), complex)
+    z[0, :, 0] = 1.0
+    x, sing = eng.solve_batch(z, np.ones((1, 3, 1), complex))
+    assert sing[0] and np.isnan(x[0]).all()          # zero pivot: lu.hpp:427-436 throws
+    for m, k, n in [(1, 1, 1), (33, 17, 9), (121, 121, 121)]:
+        a = rng.standard_normal((3, m, k)) + 1j * rng.standard_normal((3, m, k))
+        b = rng.standard_normal((3, k, n)) + 1j * rng.standard_normal((3, k, n))
+        c = eng.multiply_batch(a, b)
+        for q in range(3):
+            assert np.max(np.abs(c[q] - oracle.multiply(a[q], b[q]))) <= 1e-12 * max(1.0, k)
