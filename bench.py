@@ -1,0 +1,338 @@
+"""Benchmark: batched 1-D TE+TM RCWA solves per second on GB300.
+
+Workload (the headline batched configuration): one seeded grating-on-mirror structure -- a binary
+grating (fill and depth uniform in 0.3..0.5, n = 1.46 / 1.0, period 0.574) on a 20-layer quarter-wave
+mirror (n = 2.1 / 1.46 at 1.053, H first), substrate 1.46 -- swept over 4096 seeded points
+(lambda uniform in 0.9..1.2, theta uniform in 50..70 degrees), each solved for TE and TM at M = 60
+(N = 121). One step = the two sweeps = 8192 solves, all in FP64 (complex128).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value      solves/s with inputs resident in device memory (the *_dev C entry points), timed with
+           CUDA events on the engine's stream, L2 flushed between steps.
+e2e        the same metric through the host-buffer C entry point (host -> device copy of the points
+           and device -> host copy of all results inside the timed region).
+roofline   the eigensolver kernel (the dominant kernel): algorithmic FP64 flops per launch / its
+           event-timed duration, against the FP64 peak measured here with cuBLAS DGEMM.
+cpu_baseline  the CPU oracle (a C++ restatement of the reference's solve) on the host cores.
+--impl reference  times that CPU implementation alone on the same workload definition.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = 20241203
+N_POINTS = 4096
+M = 60
+PERIOD = 0.574
+METRIC = "solves/s, batched 1-D TE+TM sweep (M=60, N=121), per-order efficiency error <= 1e-10 vs the FP64 CPU oracle"
+WORKLOAD = ("config 2: batched 1-D TE+TM sweep, M=60 (N=121), binary grating on a 20-layer quarter-wave mirror, "
+            "4096 seeded (lambda, theta) points x 2 polarizations per step")
+
+
+def workload(seed=SEED, n_points=N_POINTS):
+    from stablercwa_gb300 import Layer, Stack
+    rng = np.random.default_rng(seed)
+    fill, depth = rng.uniform(0.3, 0.5), rng.uniform(0.3, 0.5)
+    layers = [Layer.grating(depth, [0.0, fill * PERIOD, PERIOD], [1.46, 1.0])]
+    for _ in range(10):
+        layers.append(Layer.uniform(1.053 / (4 * 2.1), 2.1))
+        layers.append(Layer.uniform(1.053 / (4 * 1.46), 1.46))
+    stack = Stack(nI=1.0, nII=1.46, period=PERIOD, layers=layers)
+    pts = np.stack([rng.uniform(0.9, 1.2, n_points), rng.uniform(50.0, 70.0, n_points)], axis=1)
+    return stack, pts, {"fill": float(fill), "depth": float(depth)}
+
+
+def flops_per_solve(n, pol):
+    """Algorithmic FP64 flops of one solve of this stack, counted op by op as the reference issues
+    them: eigensolve 105 n^3, LU factor 8/3 n^3, triangular solves 8 n^2 per right-hand side,
+    GEMM 8 n^3. TE: 1 eig, 6 LU (5 with n RHS, 1 with one), 6 GEMM; TM adds 2 LU with n RHS and
+    1 GEMM for the layer matrix and V."""
+    eig = 105 * n ** 3
+    if pol == 0:
+        return eig + 6 * (8 / 3) * n ** 3 + 5 * 8 * n ** 3 + 8 * n ** 2 + 6 * 8 * n ** 3
+    return eig + 8 * (8 / 3) * n ** 3 + 7 * 8 * n ** 3 + 8 * n ** 2 + 7 * 8 * n ** 3
+
+
+# ------------------------------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------- CPU side
+
+def cpu_sample_points(pts, count):
+    idx = np.linspace(0, len(pts) - 1, count).astype(int)
+    return pts[idx]
+
+
+def cpu_rate(stack, pts, threads):
+    """Oracle solves/s on `threads` host threads over TE + TM of the given points."""
+    from oracle import oracle
+    t0 = time.perf_counter()
+    out = [oracle.solve1d_batch(stack, pts, M, pol, threads=threads) for pol in (0, 1)]
+    dt = time.perf_counter() - t0
+    return 2 * len(pts) / dt, out, dt
+
+
+def run_reference(args):
+    """--impl reference: the reference's algorithm on the host cores (the oracle port; the
+    reference sources are not on the benchmark host), same workload definition and metric."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    stack, pts, geo = workload()
+    threads = os.cpu_count() or 1
+    sample = cpu_sample_points(pts, args.ref_points)
+    for _ in range(args.warmup):
+        cpu_rate(stack, sample[: max(1, len(sample) // 8)], threads)
+    times = []
+    for _ in range(args.steps):
+        _, _, dt = cpu_rate(stack, sample, threads)
+        times.append(dt)
+    solves = 2 * len(sample)
+    value = solves * args.steps / sum(times)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (complex128)",
+            "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "points": N_POINTS, "M": M, "seed": SEED, **geo},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": f"{len(sample)} of the {N_POINTS} points x TE+TM = {solves} solves per step"},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------------- GPU side
+
+def fp64_peak_tflops(torch):
+    """FP64 peak of this GPU, measured: cuBLAS DGEMM 4096^3 through torch, best of 5."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from stablercwa_gb300.engine import Engine, launch_count
+
+    if args.eig_group:
+        os.environ["RCWA_GB300_EIG_GROUP"] = str(args.eig_group)
+    stack, pts, geo = workload()
+    n = 2 * M + 1
+    P = len(pts)
+    eng = Engine(device=local)
+    est = torch.cuda.ExternalStream(eng.stream())
+    d_pts = torch.tensor(pts, dtype=torch.float64, device="cuda")
+    outs = []
+    for pol in (0, 1):
+        outs.append({"R": torch.empty((P, n, 2), dtype=torch.float64, device="cuda"),
+                     "T": torch.empty((P, n, 2), dtype=torch.float64, device="cuda"),
+                     "DEr": torch.empty((P, n), dtype=torch.float64, device="cuda"),
+                     "DEt": torch.empty((P, n), dtype=torch.float64, device="cuda"),
+                     "status": torch.empty(P, dtype=torch.int32, device="cuda")})
+    ptrs = [{k: v.data_ptr() for k, v in o.items()} for o in outs]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+
+    def step():
+        for pol in (0, 1):
+            eng.solve1d_device(stack, d_pts.data_ptr(), P, M, pol, ptrs[pol])
+
+    peak = fp64_peak_tflops(torch)
+    for _ in range(args.warmup):
+        step()
+    eng.synchronize()
+    torch.cuda.synchronize()
+
+    # ---- timed region: device-resident inputs
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    eng.set_kernel_timing(True)
+    launches0 = launch_count()
+    total_ms = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(est)
+        step()
+        e1.record(est)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+    launches = launch_count() - launches0
+    eig_ms, eig_launches = eng.kernel_time("eig")
+    lu_ms, lu_launches = eng.kernel_time("lu")
+    gemm_ms, gemm_launches = eng.kernel_time("gemm")
+    eng.set_kernel_timing(False)
+    clocks = sampler.stop()
+    torch.cuda.synchronize()
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    solves_per_step = 2 * P
+    value = world * solves_per_step * args.steps / (total_ms * 1e-3)
+
+    # ---- end to end through the host-buffer entry point
+    e2e_times = []
+    for _ in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host = [eng.solve1d_arrays(stack, pts, M, pol) for pol in (0, 1)]
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_value = world * solves_per_step / (sum(e2e_times) / len(e2e_times))
+    h2d = 2 * (P * 16)  # per polarization: s and wavelength per point
+    d2h = 2 * (P * n * (16 + 16 + 8 + 8) + P * 4 * 4)
+
+    # ---- accuracy and CPU baseline (rank 0): the oracle on a bounded sample of the same points
+    line_extra = {}
+    if rank == 0:
+        threads = os.cpu_count() or 1
+        sample_idx = np.linspace(0, P - 1, args.cpu_points).astype(int)
+        rate, cpu_out, cpu_dt = cpu_rate(stack, pts[sample_idx], threads)
+        err = 0.0
+        for pol in (0, 1):
+            for key in ("DEr", "DEt"):
+                err = max(err, float(np.max(np.abs(host[pol][key][sample_idx] - cpu_out[pol][key]))))
+        ok = all((host[pol]["status"] == 0).all() for pol in (0, 1))
+        energy = max(float(np.max(np.abs(host[pol]["DEr"].sum(1) + host[pol]["DEt"].sum(1) - 1))) for pol in (0, 1))
+        line_extra["cpu_baseline"] = {"value": rate, "unit": "solves/s", "cores": threads, "kind": "port",
+                                      "sample": f"{len(sample_idx)} of the {P} points x TE+TM = {2 * len(sample_idx)} "
+                                                f"solves, {cpu_dt:.1f} s wall"}
+        line_extra["accuracy"] = {"max_abs_dDE_vs_oracle": err, "sample_solves": 2 * len(sample_idx),
+                                  "all_status_ok": bool(ok), "max_energy_defect_all_points": energy}
+
+    eig_avg_ms = eig_ms / max(1, eig_launches)
+    eig_flops_launch = P * 105 * n ** 3
+    achieved = eig_flops_launch / (eig_avg_ms * 1e-3) / 1e12
+    total_flops = P * (flops_per_solve(n, 0) + flops_per_solve(n, 1))
+    step_ms = total_ms / args.steps
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64 (complex128)", "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD, "points": P, "M": M, "solves_per_step": solves_per_step,
+                           "seed": SEED, **geo, "parallelism": f"replicas x{world}",
+                           "l2": "flushed between steps (256 MB write); per-step device footprint is also > L2",
+                           "eig_group": int(os.environ.get("RCWA_GB300_EIG_GROUP", "0") or 0)},
+                "clocks": clocks,
+                "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "gpu_launches": launches,
+                "roofline": {"bound": "fp64", "kernel": "eig_batch_kernel", "achieved": achieved, "peak": peak,
+                             "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                             "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (torch.matmul float64), best of 5",
+                             "flops_per_launch": eig_flops_launch, "avg_launch_ms": eig_avg_ms,
+                             "launches": eig_launches},
+                "kernels_ms_per_step": {"eig": eig_ms / args.steps, "lu": lu_ms / args.steps, "gemm": gemm_ms / args.steps,
+                                        "other": step_ms - (eig_ms + lu_ms + gemm_ms) / args.steps},
+                "step_fp64": {"algorithmic_tflop": total_flops / 1e12,
+                              "achieved_tflops": total_flops / (step_ms * 1e-3) / 1e12,
+                              "frac_of_peak": total_flops / (step_ms * 1e-3) / 1e12 / peak},
+                **line_extra}
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--eig-group", type=int, default=0)
+    ap.add_argument("--cpu-points", type=int, default=128)
+    ap.add_argument("--ref-points", type=int, default=128)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -140,6 +140,18 @@ int rcwa_gpu_solve1d_batch_dev(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, con
                                rcwa_result1d* d_out);
 int rcwa_gpu_synchronize(rcwa_gpu_ctx* ctx);
 
+/* The context's CUDA stream (a cudaStream_t), for callers that order their own work or events
+ * against the engine's. No reference counterpart. */
+void* rcwa_gpu_stream(rcwa_gpu_ctx* ctx);
+
+/* Per-kernel device timing on the context's stream. No reference counterpart: the reference's
+ * Timing{eig, linear, product} (include/stablercwa/rcwa1d.hpp:141-143) is host wall time per solve.
+ * With timing enabled, CUDA events bracket every launch of the eigensolver ("eig"), the LU solve
+ * ("lu") and the GEMM ("gemm"); rcwa_gpu_kernel_time reads the accumulated milliseconds and launch
+ * count of one kind (after the work has finished) and resets it. */
+int rcwa_gpu_set_kernel_timing(rcwa_gpu_ctx* ctx, int enable);
+int rcwa_gpu_kernel_time(rcwa_gpu_ctx* ctx, const char* kind, double* milliseconds, long long* launches);
+
 /* Batched general complex eigensolver, CORTH + COMQR2 (include/stablercwa/eig_qr.hpp:1008-1124):
  * the engine behind Options::custom_eig (include/stablercwa/rcwa1d.hpp:122-124). a holds batch
  * n x n matrices; values[batch*n], vectors[batch*n*n] (2-norm normalised columns), info[batch]

@@ -20,6 +20,8 @@ struct rcwa_gpu_ctx {
     std::mutex lock;
     std::string last_error;
     size_t workspace_limit = 0;
+    bool timing = false;
+    rcwa_gb300::KernelTimer timer;
 };
 
 namespace {
@@ -38,6 +40,10 @@ template <class F>
 int guarded(rcwa_gpu_ctx* ctx, F&& body) {
     if (!ctx) return RCWA_EINVAL;
     std::lock_guard<std::mutex> hold(ctx->lock);
+    struct TimerScope {
+        explicit TimerScope(rcwa_gpu_ctx* c) { current_timer() = c->timing ? &c->timer : nullptr; }
+        ~TimerScope() { current_timer() = nullptr; }
+    } scope(ctx);
     try {
         RCWA_CUDA(cudaSetDevice(ctx->device));
         body();
@@ -151,6 +157,31 @@ int rcwa_gpu_last_error(const rcwa_gpu_ctx* ctx, char* buffer, size_t size) {
     std::strncpy(buffer, msg.c_str(), size - 1);
     buffer[size - 1] = '\0';
     return RCWA_OK;
+}
+
+void* rcwa_gpu_stream(rcwa_gpu_ctx* ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
+
+int rcwa_gpu_set_kernel_timing(rcwa_gpu_ctx* ctx, int enable) {
+    return guarded(ctx, [&] {
+        ctx->timer.collect();
+        ctx->timing = enable != 0;
+    });
+}
+
+int rcwa_gpu_kernel_time(rcwa_gpu_ctx* ctx, const char* kind, double* milliseconds, long long* launches) {
+    return guarded(ctx, [&] {
+        if (!kind || !milliseconds) throw EngineError{RCWA_EINVAL, "kernel_time: null argument"};
+        int k = -1;
+        if (!std::strcmp(kind, "eig")) k = TK_EIG;
+        if (!std::strcmp(kind, "lu")) k = TK_LU;
+        if (!std::strcmp(kind, "gemm")) k = TK_GEMM;
+        if (k < 0) throw EngineError{RCWA_EINVAL, "kernel_time: kind must be eig, lu or gemm"};
+        ctx->timer.collect();
+        *milliseconds = ctx->timer.ms[k];
+        if (launches) *launches = ctx->timer.count[k];
+        ctx->timer.ms[k] = 0.0;
+        ctx->timer.count[k] = 0;
+    });
 }
 
 int rcwa_gpu_synchronize(rcwa_gpu_ctx* ctx) {

@@ -24,6 +24,7 @@ void launch_eig(cudaStream_t st, int n, int batch, const zc* a, long long a_stri
     const int tpb = 128;
     const long long threads = (long long)batch * group;
     const unsigned blocks = (unsigned)((threads + tpb - 1) / tpb);
+    TimedLaunch timed(TK_EIG, st);
     switch (group) {
         case 4: eig_batch_kernel<4><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, sweeps, ws, eps, max_iter, skip); break;
         case 8: eig_batch_kernel<8><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, sweeps, ws, eps, max_iter, skip); break;

@@ -87,6 +87,32 @@ int eig_default_group(int n, int batch);
 // Kernel launch accounting for the benchmark's gpu_launches claim.
 long long& launch_count();
 
+// Optional CUDA-event timing of the heavy kernels (enabled per context; the context installs its
+// timer as the calling thread's current timer for the duration of a call).
+enum TimedKind : int { TK_EIG = 0, TK_LU = 1, TK_GEMM = 2, TK_COUNT = 3 };
+struct KernelTimer {
+    struct Rec {
+        int kind;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> pending;
+    double ms[TK_COUNT] = {0, 0, 0};
+    long long count[TK_COUNT] = {0, 0, 0};
+    void collect();
+    ~KernelTimer();
+};
+KernelTimer*& current_timer();
+class TimedLaunch {
+public:
+    TimedLaunch(int kind, cudaStream_t st);
+    ~TimedLaunch();
+
+private:
+    KernelTimer* t_;
+    cudaStream_t st_;
+    size_t idx_ = 0;
+};
+
 struct Options {
     int fast_path = 1;
     int diagnostics = 0;

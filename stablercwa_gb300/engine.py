@@ -55,6 +55,10 @@ def load_library(build_if_missing=True):
     L.rcwa_gpu_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
     L.rcwa_gpu_synchronize.argtypes = [vp]
     L.rcwa_gpu_launch_count.restype = C.c_longlong
+    L.rcwa_gpu_stream.restype = vp
+    L.rcwa_gpu_stream.argtypes = [vp]
+    L.rcwa_gpu_set_kernel_timing.argtypes = [vp, ci]
+    L.rcwa_gpu_kernel_time.argtypes = [vp, C.c_char_p, C.POINTER(cd), C.POINTER(C.c_longlong)]
     L.rcwa_options_default.argtypes = [C.POINTER(abi.rcwa_options)]
     L.rcwa_gpu_solve1d_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack1d), vp, ci, ci, ci, C.POINTER(abi.rcwa_options),
                                          C.POINTER(abi.rcwa_result1d)]
@@ -147,6 +151,20 @@ class Engine:
         o = _options(options)
         self._check(self.L.rcwa_gpu_solve1d_batch_dev(self.h, C.byref(st), d_points, n_points, M, pol, C.byref(o),
                                                       C.byref(res)))
+
+    def stream(self):
+        """The context's cudaStream_t as an integer (torch.cuda.ExternalStream accepts it)."""
+        return int(self.L.rcwa_gpu_stream(self.h) or 0)
+
+    def set_kernel_timing(self, enable):
+        self._check(self.L.rcwa_gpu_set_kernel_timing(self.h, 1 if enable else 0))
+
+    def kernel_time(self, kind):
+        """(milliseconds, launches) accumulated for 'eig', 'lu' or 'gemm' since the last read."""
+        ms = C.c_double()
+        n = C.c_longlong()
+        self._check(self.L.rcwa_gpu_kernel_time(self.h, kind.encode(), C.byref(ms), C.byref(n)))
+        return ms.value, n.value
 
     def synchronize(self):
         self._check(self.L.rcwa_gpu_synchronize(self.h))
