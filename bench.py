@@ -319,6 +319,39 @@ def run_ours(args):
     return 0
 
 
+def run_eig_only(n, batch, group):
+    """Profiling case for the eigensolver alone: `batch` lossy layer matrices of order n in the
+    benchmark's form (Toeplitz of a binary grating, index 1.46+0.01i, fill 0.4, plus Kx^2 with
+    sin(theta) in 0.75..0.95, lambda/period 0.61), eigensolved twice on device."""
+    import torch
+    from stablercwa_gb300.engine import Engine
+    if group:
+        os.environ["RCWA_GB300_EIG_GROUP"] = str(group)
+    rng = np.random.default_rng(1)
+    M = n // 2
+    h = np.subtract.outer(np.arange(n), np.arange(n))
+    e1 = complex(1.46, 0.01) ** 2
+    with np.errstate(invalid="ignore", divide="ignore"):
+        eps = np.where(h == 0, 0.4 * e1 + 0.6, (e1 - 1) * np.sin(np.pi * h * 0.4) / (np.pi * h))
+    mats = []
+    for _ in range(32):
+        kx = rng.uniform(0.75, 0.95) + (np.arange(n) - M) * 0.61
+        mats.append((-eps + np.diag(kx * kx)).astype(np.complex128))
+    A = np.ascontiguousarray(np.array(mats)[np.arange(batch) % 32].transpose(0, 2, 1)).astype(np.complex128)
+    dA = torch.tensor(A.view(np.float64), device="cuda")
+    assert dA.numel() * 8 == batch * n * n * 16
+    dW = torch.empty((batch, n, 2), dtype=torch.float64, device="cuda")
+    dV = torch.empty((batch, n, n, 2), dtype=torch.float64, device="cuda")
+    dI = torch.empty(batch, dtype=torch.int32, device="cuda")
+    eng = Engine()
+    for _ in range(2):
+        eng.eig_batch_device(n, batch, dA.data_ptr(), dW.data_ptr(), dV.data_ptr(), dI.data_ptr())
+        eng.synchronize()
+    bad = int((dI != 0).sum().item())
+    print(json.dumps({"eig_only": {"n": n, "batch": batch, "group": group, "not_converged": bad}}))
+    return 0 if bad == 0 else 1
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -328,7 +361,11 @@ def main():
     ap.add_argument("--eig-group", type=int, default=0)
     ap.add_argument("--cpu-points", type=int, default=128)
     ap.add_argument("--ref-points", type=int, default=128)
+    ap.add_argument("--eig-only", nargs=2, type=int, metavar=("N", "BATCH"), default=None,
+                    help="profiling case: the eigensolver alone on BATCH layer matrices of order N")
     args = ap.parse_args()
+    if args.eig_only:
+        return run_eig_only(args.eig_only[0], args.eig_only[1], args.eig_group)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
