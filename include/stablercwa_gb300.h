@@ -105,6 +105,35 @@ typedef struct rcwa_result1d {
     double* max_eig_residual;  /* optional, filled when options.diagnostics */
 } rcwa_result1d;
 
+/* One conical sweep point (include/stablercwa/rcwa1d_conical.hpp:186). */
+typedef struct rcwa_point_conical {
+    double wavelength;
+    double theta_deg;
+    double phi_deg;
+} rcwa_point_conical;
+
+/* Batched conical results (include/stablercwa/rcwa1d_conical.hpp:105-183), caller-allocated.
+ * n = 2M+1 orders; point p, order m (index m+M): Jones entries at [(p*n + m+M)*4 + k] with
+ * k = 0 ss, 1 sp, 2 ps, 3 pp (output <- input); channel efficiencies in the same layout.
+ * Optional arrays may be NULL. */
+typedef struct rcwa_result_conical {
+    rcwa_complex* Jr;
+    rcwa_complex* Jt;
+    double* DEr;
+    double* DEt;
+    int* status;                   /* RCWA_SAMPLE_* */
+    int* eig_info;                 /* optional */
+    int* n_eig;                    /* optional */
+    int* n_dense_solve;            /* optional */
+    int* n_schur;                  /* optional: layers switched to Schur propagation */
+    double* min_abs_lambda;        /* optional */
+    int* degenerate_mode_warning;  /* optional */
+    double* kx;                    /* optional, n_points * n */
+    double* ky;                    /* optional, n_points */
+    double* flux_r;                /* optional, n_points * n */
+    double* flux_t;                /* optional, n_points * n */
+} rcwa_result_conical;
+
 typedef struct rcwa_gpu_config {
     int device;                /* CUDA device ordinal */
     size_t workspace_limit;    /* bytes of device workspace the context may hold; 0 = 8 GiB */
@@ -139,6 +168,12 @@ int rcwa_gpu_solve1d_batch_dev(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, con
                                int n_points, int M, int polarization, const rcwa_options* options,
                                rcwa_result1d* d_out);
 int rcwa_gpu_synchronize(rcwa_gpu_ctx* ctx);
+
+/* Batched conical-incidence solve over (lambda, theta, phi) points on one stack: replaces
+ * rcwa::sweep_conical (include/stablercwa/rcwa1d_conical.hpp:992-999) and, with n_points = 1,
+ * rcwa::solve_conical (:985-988). Host buffers in and out. */
+int rcwa_gpu_solve_conical_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point_conical* points,
+                                 int n_points, int M, const rcwa_options* options, rcwa_result_conical* out);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that order their own work or events
  * against the engine's. No reference counterpart. */

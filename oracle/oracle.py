@@ -24,6 +24,9 @@ def lib():
         L.oracle_solve1d_batch.restype = C.c_int
         L.oracle_solve1d_batch.argtypes = [C.POINTER(abi.rcwa_stack1d), C.c_void_p, C.c_int, C.c_int, C.c_int,
                                            C.c_int, C.POINTER(abi.rcwa_result1d), C.c_int, C.c_char_p, C.c_size_t]
+        L.oracle_solve_conical_batch.restype = C.c_int
+        L.oracle_solve_conical_batch.argtypes = [C.POINTER(abi.rcwa_stack1d), C.c_void_p, C.c_int, C.c_int,
+                                                 C.POINTER(abi.rcwa_result_conical), C.c_int, C.c_char_p, C.c_size_t]
         L.oracle_eig.argtypes = [C.c_int, C.c_void_p, C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_schur.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_solve.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -48,6 +51,18 @@ def solve1d_batch(stack, points, M, pol, threads=1, diagnostics=False):
     err = C.create_string_buffer(512)
     rc = lib().oracle_solve1d_batch(C.byref(st), pts.ctypes.data, len(pts), M, pol, 1 if diagnostics else 0,
                                     C.byref(res), threads, err, 512)
+    if rc != 0:
+        raise OracleInvalidArgument(err.value.decode())
+    return arrays
+
+
+def solve_conical_batch(stack, points, M, threads=1):
+    """rcwa::sweep_conical on the CPU: dict of numpy arrays (Jr, Jt, DEr, DEt: (P, 2M+1, 4), ...)."""
+    st, keep = abi.marshal_stack1d(stack)
+    pts = abi.conical_points_array(points)
+    res, arrays = abi.conical_views(len(pts), M)
+    err = C.create_string_buffer(512)
+    rc = lib().oracle_solve_conical_batch(C.byref(st), pts.ctypes.data, len(pts), M, C.byref(res), threads, err, 512)
     if rc != 0:
         raise OracleInvalidArgument(err.value.decode())
     return arrays

@@ -12,7 +12,7 @@
 #include <vector>
 
 #include "../include/stablercwa_gb300.h"
-#include "oracle_rcwa1d.hpp"
+#include "oracle_conical.hpp"
 
 using namespace oracle;
 
@@ -90,6 +90,63 @@ int oracle_solve1d_batch(const rcwa_stack1d* stack, const rcwa_point1d* points, 
                 if (out->n_eig) out->n_eig[p] = r.n_eig;
                 if (out->n_dense_solve) out->n_dense_solve[p] = r.n_dense_solve;
                 if (out->max_eig_residual) out->max_eig_residual[p] = r.max_eig_residual;
+            } catch (const InvalidArgument& e) {
+                std::lock_guard<std::mutex> hold(error_lock);
+                if (failed.fetch_add(1) == 0) first_error = e.what;
+            }
+        }
+    };
+    if (n_threads <= 1) {
+        worker();
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < n_threads; ++t) pool.emplace_back(worker);
+        for (std::thread& t : pool) t.join();
+    }
+    if (failed.load()) {
+        put_error(err, err_len, first_error);
+        return -1;
+    }
+    return 0;
+}
+
+// Batched conical solve on the CPU: rcwa::sweep_conical (include/stablercwa/rcwa1d_conical.hpp:992-999).
+int oracle_solve_conical_batch(const rcwa_stack1d* stack, const rcwa_point_conical* points, int n_points, int M,
+                               rcwa_result_conical* out, int n_threads, char* err, size_t err_len) {
+    const Stack1D s = to_stack(stack);
+    const int n = 2 * M + 1;
+    std::atomic<int> next{0};
+    std::atomic<int> failed{0};
+    std::string first_error;
+    std::mutex error_lock;
+    const auto worker = [&]() {
+        for (;;) {
+            const int p = next.fetch_add(1);
+            if (p >= n_points) return;
+            try {
+                const ConicalResult r = solve_conical(s, points[p].wavelength, points[p].theta_deg, points[p].phi_deg, M);
+                for (int j = 0; j < n; ++j) {
+                    const size_t o = (static_cast<size_t>(p) * n + j) * 4;
+                    const cplx jr[4] = {r.Jr[j].ss, r.Jr[j].sp, r.Jr[j].ps, r.Jr[j].pp};
+                    const cplx jt[4] = {r.Jt[j].ss, r.Jt[j].sp, r.Jt[j].ps, r.Jt[j].pp};
+                    for (int k = 0; k < 4; ++k) {
+                        out->Jr[o + k] = R(jr[k]);
+                        out->Jt[o + k] = R(jt[k]);
+                        out->DEr[o + k] = r.DEr[j][k];
+                        out->DEt[o + k] = r.DEt[j][k];
+                    }
+                    if (out->kx) out->kx[static_cast<size_t>(p) * n + j] = r.kx[j];
+                    if (out->flux_r) out->flux_r[static_cast<size_t>(p) * n + j] = r.flux_r[j];
+                    if (out->flux_t) out->flux_t[static_cast<size_t>(p) * n + j] = r.flux_t[j];
+                }
+                if (out->ky) out->ky[p] = r.ky;
+                if (out->status) out->status[p] = !r.failed ? RCWA_SAMPLE_OK : (r.eig_info ? RCWA_SAMPLE_EIG_NOCONV : RCWA_SAMPLE_NUMERICAL);
+                if (out->eig_info) out->eig_info[p] = r.eig_info;
+                if (out->n_eig) out->n_eig[p] = r.n_eig;
+                if (out->n_dense_solve) out->n_dense_solve[p] = r.n_dense_solve;
+                if (out->n_schur) out->n_schur[p] = r.n_schur;
+                if (out->min_abs_lambda) out->min_abs_lambda[p] = r.min_abs_lambda;
+                if (out->degenerate_mode_warning) out->degenerate_mode_warning[p] = r.degenerate_mode_warning ? 1 : 0;
             } catch (const InvalidArgument& e) {
                 std::lock_guard<std::mutex> hold(error_lock);
                 if (failed.fetch_add(1) == 0) first_error = e.what;

@@ -78,6 +78,16 @@ class rcwa_result1d(C.Structure):
     ]
 
 
+class rcwa_point_conical(C.Structure):
+    _fields_ = [("wavelength", C.c_double), ("theta_deg", C.c_double), ("phi_deg", C.c_double)]
+
+
+class rcwa_result_conical(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name in (
+        "Jr", "Jt", "DEr", "DEt", "status", "eig_info", "n_eig", "n_dense_solve", "n_schur", "min_abs_lambda",
+        "degenerate_mode_warning", "kx", "ky", "flux_r", "flux_t")]
+
+
 class rcwa_gpu_config(C.Structure):
     _fields_ = [("device", C.c_int), ("workspace_limit", C.c_size_t)]
 
@@ -142,3 +152,33 @@ def result_views(n_points, M, with_diag=True):
     for name, arr in arrays.items():
         setattr(res, name, arr.ctypes.data)
     return res, arrays
+
+
+def conical_views(n_points, M):
+    """Host arrays for rcwa_result_conical and the struct pointing at them."""
+    n = 2 * M + 1
+    arrays = {
+        "Jr": np.empty((n_points, n, 4), np.complex128),
+        "Jt": np.empty((n_points, n, 4), np.complex128),
+        "DEr": np.empty((n_points, n, 4), np.float64),
+        "DEt": np.empty((n_points, n, 4), np.float64),
+        "status": np.empty(n_points, np.int32),
+        "eig_info": np.empty(n_points, np.int32),
+        "n_eig": np.empty(n_points, np.int32),
+        "n_dense_solve": np.empty(n_points, np.int32),
+        "n_schur": np.empty(n_points, np.int32),
+        "min_abs_lambda": np.empty(n_points, np.float64),
+        "degenerate_mode_warning": np.empty(n_points, np.int32),
+        "kx": np.empty((n_points, n), np.float64),
+        "ky": np.empty(n_points, np.float64),
+        "flux_r": np.empty((n_points, n), np.float64),
+        "flux_t": np.empty((n_points, n), np.float64),
+    }
+    res = rcwa_result_conical()
+    for name, arr in arrays.items():
+        setattr(res, name, arr.ctypes.data)
+    return res, arrays
+
+
+def conical_points_array(points):
+    return np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))

@@ -35,3 +35,26 @@ def cases1d():
 @pytest.fixture(scope="session")
 def eig_cases():
     return load_jsonl("eig_cases.jsonl")
+
+
+@pytest.fixture(scope="session")
+def conical_cases():
+    return load_jsonl("conical_cases.jsonl")
+
+
+def jones_from_table(rows):
+    """(n, 4) complex from rows of 8 doubles: ss, sp, ps, pp as (re, im) pairs."""
+    a = np.array(rows, dtype=np.float64).reshape(-1, 4, 2)
+    return a[..., 0] + 1j * a[..., 1]
+
+
+def jones_from_ref(rows):
+    out = np.empty((len(rows), 4), np.complex128)
+    for j, row in enumerate(rows):
+        for k in range(4):
+            out[j, k] = complex(float(row[k][0]), float(row[k][1]))
+    return out
+
+
+def de_from_ref(rows):
+    return np.array([[float(v) for v in row] for row in rows], dtype=np.float64)

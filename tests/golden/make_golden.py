@@ -20,6 +20,7 @@ EXPORTERS = [
     # (source, output, reference test directory it includes from)
     ("export_rcwa1d.cpp", "rcwa1d_cases.jsonl"),
     ("export_eig.cpp", "eig_cases.jsonl"),
+    ("export_conical.cpp", "conical_cases.jsonl"),
 ]
 
 
