@@ -18,7 +18,7 @@ int eig_default_group(int n, int batch) {
 }
 
 void launch_eig(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info, int* sweeps,
-                zc* ws, double eps, int max_iter, int group, const int* skip) {
+                zc* ws, double eps, int max_iter, int group, const int* skip, int skip_value, zc* t_out) {
     if (batch <= 0 || n <= 0) return;
     if (group <= 0) group = eig_default_group(n, batch);
     const int tpb = 128;
@@ -26,10 +26,10 @@ void launch_eig(cudaStream_t st, int n, int batch, const zc* a, long long a_stri
     const unsigned blocks = (unsigned)((threads + tpb - 1) / tpb);
     TimedLaunch timed(TK_EIG, st);
     switch (group) {
-        case 4: eig_batch_kernel<4><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, sweeps, ws, eps, max_iter, skip); break;
-        case 8: eig_batch_kernel<8><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, sweeps, ws, eps, max_iter, skip); break;
-        case 16: eig_batch_kernel<16><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, sweeps, ws, eps, max_iter, skip); break;
-        case 32: eig_batch_kernel<32><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, sweeps, ws, eps, max_iter, skip); break;
+        case 4: eig_batch_kernel<4><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, sweeps, ws, eps, max_iter, skip, skip_value, t_out); break;
+        case 8: eig_batch_kernel<8><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, sweeps, ws, eps, max_iter, skip, skip_value, t_out); break;
+        case 16: eig_batch_kernel<16><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, sweeps, ws, eps, max_iter, skip, skip_value, t_out); break;
+        case 32: eig_batch_kernel<32><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, sweeps, ws, eps, max_iter, skip, skip_value, t_out); break;
         default: throw EngineError{RCWA_EINVAL, "eig: group must be 4, 8, 16 or 32"};
     }
     ++launch_count();

@@ -76,10 +76,13 @@ __device__ __forceinline__ zc wilkinson_shift(zc a, zc b, double c, zc d) {
     return d - scale2(zdiv(x, ys + zz), e);
 }
 
+// With T != nullptr the call returns the Schur form instead of eigenvectors (keep_transform with
+// vectors = false, eig_qr.hpp:1106-1122): V receives Z and T receives the upper triangular T with
+// Z^H A Z = T.
 template <int G>
 __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc* __restrict__ V,
                         int* __restrict__ info_out, int* __restrict__ sweeps_out, zc* __restrict__ ws, double eps,
-                        int max_iter) {
+                        int max_iter, zc* __restrict__ T = nullptr) {
     const int g = threadIdx.x & (G - 1);
     const unsigned mask = group_mask<G>();
     zc* __restrict__ H = ws;
@@ -348,6 +351,15 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
         for (int i = g; i <= en; i += G) W[i] = H[(long long)i * n + i] + t;
         return;
     }
+    if (T) {
+        // Schur form: T = H with the negligible subdiagonal cleared, Z as accumulated
+        for (long long idx = g; idx < (long long)n * n; idx += G) {
+            const int c = (int)(idx / n), r = (int)(idx - (long long)c * n);
+            T[idx] = r > c ? zc{0.0, 0.0} : H[idx];
+            V[idx] = Z[idx];
+        }
+        return;
+    }
 
     // ---------------- eigenvectors of T by back substitution, times Z, normalised (eig_qr.hpp:886-961)
     double tn = 0.0;
@@ -419,12 +431,13 @@ template <int G>
 __global__ void __launch_bounds__(128) eig_batch_kernel(int n, int batch, const zc* __restrict__ a, long long a_stride,
                                                         zc* __restrict__ w, zc* __restrict__ v, int* __restrict__ info,
                                                         int* __restrict__ sweeps, zc* __restrict__ ws, double eps,
-                                                        int max_iter, const int* __restrict__ skip) {
+                                                        int max_iter, const int* __restrict__ skip, int skip_value,
+                                                        zc* __restrict__ t_out) {
     const long long gid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
     if (gid >= batch) return;
-    if (skip && skip[gid]) return;
+    if (skip && skip[gid] == skip_value) return;
     eig_one<G>(n, a + gid * a_stride, w + gid * n, v + gid * (long long)n * n, info + gid, sweeps ? sweeps + gid : nullptr,
-               ws + gid * eig_workspace_elems(n), eps, max_iter);
+               ws + gid * eig_workspace_elems(n), eps, max_iter, t_out ? t_out + gid * (long long)n * n : nullptr);
 }
 
 }  // namespace rcwa_gb300

@@ -79,8 +79,11 @@ void launch_zgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A, 
                   int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc, long long c_stride,
                   double s_ab, double s_c, const int* skip = nullptr, int skip_value = 1);
 // group: lanes per matrix (0 = choose)
+// skip: optional per-matrix flags, a matrix whose flag equals skip_value is left untouched.
+// t_out: when non-null, the Schur form is returned instead of eigenvectors (v receives Z, t_out T).
 void launch_eig(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info, int* sweeps,
-                zc* ws, double eps, int max_iter, int group, const int* skip = nullptr);
+                zc* ws, double eps, int max_iter, int group, const int* skip = nullptr, int skip_value = 1,
+                zc* t_out = nullptr);
 long long eig_workspace_bytes(int n, int batch);
 int eig_default_group(int n, int batch);
 
@@ -129,6 +132,16 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
 // s = nI sin(theta) with the device sin; returns false when some point is invalid.
 bool prepare_points_device(cudaStream_t st, const rcwa_point1d* d_points, int n_points, double nI, double* d_s,
                            double* d_wl);
+
+// Batched conical solve (conical.cu). Per-point host-evaluated trigonometry: s_cphi = nI sin(theta)
+// cos(phi), ky = nI sin(theta) sin(phi), cphi = cos(phi), sphi = sin(phi), ctheta = cos(theta), wl;
+// all device arrays of n_points. Results go to the device arrays of d_out.
+struct ConicalPointsDev {
+    const double *s_cphi, *ky, *cphi, *sphi, *ctheta, *wl;
+};
+void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const ConicalPointsDev& pts, int n_points, int M,
+                          const Options& opt, const rcwa_result_conical& d_out, size_t chunk_bytes);
+void validate_conical(const rcwa_stack1d& stack, const rcwa_point_conical* h_points, int n_points, int M);
 
 // Validation of a 1-D problem exactly where the reference throws std::invalid_argument.
 void validate1d(const rcwa_stack1d& stack, const rcwa_point1d* h_points, int n_points, int M, int pol);

@@ -10,6 +10,7 @@
 #include "common.cuh"
 
 namespace rcwa_gb300 {
+namespace {  // internal linkage: included by several translation units
 
 // kx_m = s - (m - M) lambda / period (include/stablercwa/rcwa1d.hpp:410-415). s = nI sin(theta) is
 // computed on the host with the host's libm, exactly as the reference does, and passed per sample.
@@ -261,4 +262,5 @@ __global__ void stack_on_diag_kernel(long long total, const zc* __restrict__ tdd
     rout[idx] = out;
 }
 
+}  // namespace
 }  // namespace rcwa_gb300

@@ -63,6 +63,8 @@ def load_library(build_if_missing=True):
     L.rcwa_gpu_solve1d_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack1d), vp, ci, ci, ci, C.POINTER(abi.rcwa_options),
                                          C.POINTER(abi.rcwa_result1d)]
     L.rcwa_gpu_solve1d_batch_dev.argtypes = L.rcwa_gpu_solve1d_batch.argtypes
+    L.rcwa_gpu_solve_conical_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack1d), vp, ci, ci,
+                                               C.POINTER(abi.rcwa_options), C.POINTER(abi.rcwa_result_conical)]
     L.rcwa_gpu_eig_batch.argtypes = [vp, ci, ci, vp, cd, ci, vp, vp, vp, vp]
     L.rcwa_gpu_eig_batch_dev.argtypes = [vp, ci, ci, vp, cd, ci, vp, vp, vp, vp]
     L.rcwa_gpu_solve_batch.argtypes = [vp, ci, ci, ci, vp, vp, vp, vp]
@@ -179,6 +181,24 @@ class Engine:
 
     def solve(self, stack, wavelength, theta_deg, M, pol=0, options=None):
         return self.sweep(stack, [(wavelength, theta_deg)], M, pol, options)[0]
+
+    # ---------------------------------------------------------------- conical incidence
+
+    def solve_conical_arrays(self, stack, points, M, options=None):
+        """rcwa::sweep_conical over (wavelength, theta, phi) points: dict of numpy arrays with Jr, Jt
+        (P, 2M+1, 4 complex: ss, sp, ps, pp), DEr, DEt (P, 2M+1, 4), status, eig_info, n_eig,
+        n_dense_solve, n_schur, min_abs_lambda, degenerate_mode_warning, kx, ky, flux_r, flux_t."""
+        st, keep = abi.marshal_stack1d(stack)
+        pts = abi.conical_points_array(points)
+        res, arrays = abi.conical_views(len(pts), M)
+        o = _options(options)
+        self._check(self.L.rcwa_gpu_solve_conical_batch(self.h, C.byref(st), pts.ctypes.data, len(pts), M, C.byref(o),
+                                                        C.byref(res)))
+        return arrays
+
+    def solve_conical(self, stack, wavelength, theta_deg, phi_deg, M, options=None):
+        a = self.solve_conical_arrays(stack, [(wavelength, theta_deg, phi_deg)], M, options)
+        return {k: v[0] for k, v in a.items()}
 
     # ---------------------------------------------------------------- dense kernels (custom_* hooks)
 
