@@ -36,6 +36,7 @@ extern "C" {
 #define RCWA_ECUDA (-2)        /* CUDA runtime error (no device, launch failure, ...) */
 #define RCWA_ENOMEM (-3)       /* device allocation failed */
 #define RCWA_EUNSUPPORTED (-4) /* option value the engine does not implement */
+#define RCWA_ESCRATCH (-5)     /* problem larger than rcwa_gpu_eig_batch_static's fixed workspace */
 
 /* per-sample status word */
 #define RCWA_SAMPLE_OK 0
@@ -196,6 +197,24 @@ int rcwa_gpu_eig_batch(rcwa_gpu_ctx* ctx, int n, int batch, const rcwa_complex* 
 int rcwa_gpu_eig_batch_dev(rcwa_gpu_ctx* ctx, int n, int batch, const rcwa_complex* d_a, double eps,
                            int max_iter, rcwa_complex* d_values, rcwa_complex* d_vectors, int* d_info,
                            int* d_sweeps);
+
+/* Batched eigensolver that allocates nothing. No counterpart in the reference: it is the
+ * rcwa_gpu_eig_batch_dev computation (same kernel and default lanes per matrix, so the same results) for callers
+ * that may not allocate device memory -- a host whose own caching allocator holds the HBM, or a
+ * latency-bound loop that cannot pay for an allocator call or the synchronisation a free implies.
+ * The per-matrix workspace, 16 * (3n^2 + 4n + 8) bytes, comes from one fixed device array of
+ * RCWA_GPU_EIG_STATIC_SCRATCH_BYTES per device (about 94 matrices of n = 121); a larger
+ * batch * workspace returns RCWA_ESCRATCH without launching. Arguments as rcwa_gpu_eig_batch_dev,
+ * all device pointers, with stream a cudaStream_t (NULL: the legacy default stream) in place of a
+ * context; the work is queued on that stream and the call returns without waiting for it.
+ * The first call with a device current looks up that device's array and loads the kernels; make it
+ * before any stream capture begins on the device. Calls that overlap in time on one device (on
+ * different streams, or unordered host threads) share the array and race; calls on one stream are
+ * ordered. Errors are reported by the return code only. */
+#define RCWA_GPU_EIG_STATIC_SCRATCH_BYTES (64ULL << 20)
+int rcwa_gpu_eig_batch_static(void* stream, int n, int batch, const rcwa_complex* d_a, double eps,
+                              int max_iter, rcwa_complex* d_values, rcwa_complex* d_vectors, int* d_info,
+                              int* d_sweeps);
 
 /* Batched A X = B with partial-pivot LU (include/stablercwa/lu.hpp:427-436): the engine behind
  * Options::custom_solve (include/stablercwa/rcwa1d.hpp:130-136). a: batch n x n, b: batch n x nrhs,
