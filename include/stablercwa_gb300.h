@@ -42,9 +42,15 @@ extern "C" {
 #define RCWA_SAMPLE_OK 0
 #define RCWA_SAMPLE_NUMERICAL 1      /* zero pivot / non-finite value: results are NaN */
 #define RCWA_SAMPLE_EIG_NOCONV 2     /* an eigensolve hit max_iter: results NaN, eig_info set */
+#define RCWA_SAMPLE_RAYLEIGH 3       /* 2-D: an order has kz exactly 0 in a homogeneous region
+                                        (include/stablercwa/rcwa2d.hpp:1099-1113): results NaN */
 
 #define RCWA_TE 0
 #define RCWA_TM 1
+
+/* 2-D factorization rule (include/stablercwa/rcwa2d_types.hpp:30) */
+#define RCWA_FACTORIZATION_LI 0
+#define RCWA_FACTORIZATION_LAURENT 1
 
 typedef struct rcwa_complex {
     double re, im;
@@ -135,6 +141,81 @@ typedef struct rcwa_result_conical {
     double* flux_t;                /* optional, n_points * n */
 } rcwa_result_conical;
 
+/* ---- 2-D crossed gratings ------------------------------------------------------------------ */
+
+/* Piecewise-constant x profile of one y strip (include/stablercwa/rcwa2d_types.hpp:40-43):
+ * n_segments + 1 increasing edges spanning one x period, n_segments complex indices. */
+typedef struct rcwa_xprofile2d {
+    int n_segments;
+    const double* edges;
+    const rcwa_complex* n_values;
+} rcwa_xprofile2d;
+
+/* Layer2D (include/stablercwa/rcwa2d_types.hpp:45-71): a uniform layer of index n, or n_strips
+ * y strips (n_strips + 1 increasing y_edges spanning one y period), strip k having x_profiles[k]. */
+typedef struct rcwa_layer2d {
+    double d;
+    int homogeneous;
+    rcwa_complex n;
+    int n_strips;
+    const double* y_edges;
+    const rcwa_xprofile2d* x_profiles;
+} rcwa_layer2d;
+
+/* Stack2D (include/stablercwa/rcwa2d_types.hpp:73-78): incident medium nI (real), layers top
+ * down, exit medium nII, periods Lx, Ly. */
+typedef struct rcwa_stack2d {
+    double nI;
+    rcwa_complex nII;
+    double Lx;
+    double Ly;
+    int n_layers;
+    const rcwa_layer2d* layers;
+} rcwa_stack2d;
+
+/* One 2-D point: the wavelength, angles and Jones vector [Es, Ep] of one rcwa::solve2d call
+ * (include/stablercwa/rcwa2d.hpp:1359). */
+typedef struct rcwa_point2d {
+    double wavelength;
+    double theta_deg;
+    double phi_deg;
+    rcwa_complex Es;
+    rcwa_complex Ep;
+} rcwa_point2d;
+
+/* Result2D arrays (include/stablercwa/rcwa2d_types.hpp:112-130), caller-allocated, point p and
+ * harmonic i = (m+M1)(2M2+1) + (n+M2) at [p*N + i], N = (2M1+1)(2M2+1). Kinematic arrays (Kx, Ky,
+ * kzI, kzII, prop_r, prop_t) are filled for every point; the amplitudes and efficiencies are NaN
+ * where status is not RCWA_SAMPLE_OK. rayleigh_regions[p*(n_layers+2) + r] is 1 where region r
+ * (0 incident medium, 1..n_layers the layers, n_layers+1 exit medium) has an order with kz exactly
+ * 0. Arrays marked optional may be NULL. */
+typedef struct rcwa_result2d {
+    double* Kx;
+    double* Ky;
+    rcwa_complex* kzI;
+    rcwa_complex* kzII;
+    rcwa_complex* Ex_r;
+    rcwa_complex* Ey_r;
+    rcwa_complex* Ez_r;
+    rcwa_complex* Ex_t;
+    rcwa_complex* Ey_t;
+    rcwa_complex* Ez_t;
+    rcwa_complex* Rs;
+    rcwa_complex* Rp;
+    rcwa_complex* Ts;
+    rcwa_complex* Tp;
+    double* DEr;
+    double* DEt;
+    unsigned char* prop_r;
+    unsigned char* prop_t;
+    int* status;                    /* RCWA_SAMPLE_* */
+    int* eig_info;                  /* optional */
+    int* n_eig;                     /* optional */
+    int* n_dense_solve;             /* optional */
+    double* max_eig_residual;       /* optional, filled when options.diagnostics */
+    unsigned char* rayleigh_regions; /* optional, n_points * (n_layers + 2) */
+} rcwa_result2d;
+
 typedef struct rcwa_gpu_config {
     int device;                /* CUDA device ordinal */
     size_t workspace_limit;    /* bytes of device workspace the context may hold; 0 = 8 GiB */
@@ -175,6 +256,21 @@ int rcwa_gpu_synchronize(rcwa_gpu_ctx* ctx);
  * rcwa::solve_conical (:985-988). Host buffers in and out. */
 int rcwa_gpu_solve_conical_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point_conical* points,
                                  int n_points, int M, const rcwa_options* options, rcwa_result_conical* out);
+
+/* Batched 2-D solve over points on one stack: replaces rcwa::solve2d
+ * (include/stablercwa/rcwa2d.hpp:1359-1413) called once per point, with Options2D::factorization
+ * = factorization and the eigensolver / fast-path / diagnostics fields of options (QR and the
+ * homogeneous fast path only). Host buffers in and out. */
+int rcwa_gpu_solve2d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points,
+                           int M1, int M2, int factorization, const rcwa_options* options, rcwa_result2d* out);
+
+/* The Fourier operators Eps, Cx, Cy of one patterned layer, each N x N column-major with row and
+ * column index (m+M1)(2M2+1) + (n+M2): replaces rcwa::detail2d::layer_operators
+ * (include/stablercwa/rcwa2d_operators.hpp:325-429). Invalid geometry or indices return
+ * RCWA_EINVAL (the reference's std::invalid_argument); a singular inverse-rule Toeplitz matrix or
+ * a non-finite operator (the reference's std::runtime_error) sets *singular to 1. */
+int rcwa_gpu_layer_operators2d(rcwa_gpu_ctx* ctx, const rcwa_layer2d* layer, double Lx, double Ly, int M1, int M2,
+                               int factorization, rcwa_complex* eps, rcwa_complex* cx, rcwa_complex* cy, int* singular);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that order their own work or events
  * against the engine's. No reference counterpart. */

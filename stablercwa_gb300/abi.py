@@ -182,3 +182,121 @@ def conical_views(n_points, M):
 
 def conical_points_array(points):
     return np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, 3))
+
+
+# ---------------------------------------------------------------- 2-D crossed gratings
+
+RCWA_SAMPLE_RAYLEIGH = 3
+RCWA_FACTORIZATION_LI = 0
+RCWA_FACTORIZATION_LAURENT = 1
+
+
+class rcwa_xprofile2d(C.Structure):
+    _fields_ = [("n_segments", C.c_int), ("edges", C.POINTER(C.c_double)), ("n_values", C.POINTER(rcwa_complex))]
+
+
+class rcwa_layer2d(C.Structure):
+    _fields_ = [
+        ("d", C.c_double),
+        ("homogeneous", C.c_int),
+        ("n", rcwa_complex),
+        ("n_strips", C.c_int),
+        ("y_edges", C.POINTER(C.c_double)),
+        ("x_profiles", C.POINTER(rcwa_xprofile2d)),
+    ]
+
+
+class rcwa_stack2d(C.Structure):
+    _fields_ = [
+        ("nI", C.c_double),
+        ("nII", rcwa_complex),
+        ("Lx", C.c_double),
+        ("Ly", C.c_double),
+        ("n_layers", C.c_int),
+        ("layers", C.POINTER(rcwa_layer2d)),
+    ]
+
+
+class rcwa_point2d(C.Structure):
+    _fields_ = [("wavelength", C.c_double), ("theta_deg", C.c_double), ("phi_deg", C.c_double),
+                ("Es", rcwa_complex), ("Ep", rcwa_complex)]
+
+
+RESULT2D_FIELDS = ("Kx", "Ky", "kzI", "kzII", "Ex_r", "Ey_r", "Ez_r", "Ex_t", "Ey_t", "Ez_t", "Rs", "Rp", "Ts", "Tp",
+                   "DEr", "DEt", "prop_r", "prop_t", "status", "eig_info", "n_eig", "n_dense_solve",
+                   "max_eig_residual", "rayleigh_regions")
+
+
+class rcwa_result2d(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name in RESULT2D_FIELDS]
+
+
+def marshal_layer2d(L, s, keep):
+    """Fill the rcwa_layer2d s from a Layer2D-like object; arrays it points at are appended to keep."""
+    s.d = float(L.d)
+    s.homogeneous = 1 if L.homogeneous else 0
+    s.n = cplx(L.n if L.homogeneous else 1.0)
+    if L.homogeneous:
+        s.n_strips = 0
+        return
+    ye = np.ascontiguousarray(np.asarray(L.y_edges, dtype=np.float64))
+    rows = (rcwa_xprofile2d * max(1, len(L.x_profiles)))()
+    keep += [ye, rows]
+    for k, p in enumerate(L.x_profiles):
+        e = np.ascontiguousarray(np.asarray(p.edges, dtype=np.float64))
+        v = np.ascontiguousarray(np.asarray(p.n_values, dtype=np.complex128))
+        keep += [e, v]
+        rows[k].n_segments = len(v)
+        rows[k].edges = e.ctypes.data_as(C.POINTER(C.c_double))
+        rows[k].n_values = C.cast(v.ctypes.data, C.POINTER(rcwa_complex))
+    s.n_strips = len(L.x_profiles)
+    s.y_edges = ye.ctypes.data_as(C.POINTER(C.c_double))
+    s.x_profiles = C.cast(rows, C.POINTER(rcwa_xprofile2d))
+
+
+def marshal_stack2d(stack):
+    """rcwa_stack2d from a Stack2D-like object. Returns (struct, keepalive)."""
+    keep = []
+    layers = (rcwa_layer2d * max(1, len(stack.layers)))()
+    for k, L in enumerate(stack.layers):
+        marshal_layer2d(L, layers[k], keep)
+    st = rcwa_stack2d()
+    st.nI = float(stack.nI)
+    st.nII = cplx(stack.nII)
+    st.Lx = float(stack.Lx)
+    st.Ly = float(stack.Ly)
+    st.n_layers = len(stack.layers)
+    st.layers = C.cast(layers, C.POINTER(rcwa_layer2d))
+    keep.append(layers)
+    return st, keep
+
+
+def points2d_array(points):
+    """Points (wavelength, theta_deg, phi_deg, Es, Ep) as an rcwa_point2d array."""
+    pts = (rcwa_point2d * max(1, len(points)))()
+    for k, (wl, th, ph, es, ep) in enumerate(points):
+        pts[k].wavelength = float(wl)
+        pts[k].theta_deg = float(th)
+        pts[k].phi_deg = float(ph)
+        pts[k].Es = cplx(es)
+        pts[k].Ep = cplx(ep)
+    return pts
+
+
+def result2d_views(n_points, N, n_layers):
+    """Host arrays for rcwa_result2d and the struct pointing at them."""
+    arrays = {}
+    for name in ("Kx", "Ky", "DEr", "DEt"):
+        arrays[name] = np.empty((n_points, N), np.float64)
+    for name in ("kzI", "kzII", "Ex_r", "Ey_r", "Ez_r", "Ex_t", "Ey_t", "Ez_t", "Rs", "Rp", "Ts", "Tp"):
+        arrays[name] = np.empty((n_points, N), np.complex128)
+    arrays["prop_r"] = np.empty((n_points, N), np.uint8)
+    arrays["prop_t"] = np.empty((n_points, N), np.uint8)
+    for name in ("status", "eig_info", "n_eig", "n_dense_solve"):
+        arrays[name] = np.empty(n_points, np.int32)
+    arrays["max_eig_residual"] = np.zeros(n_points, np.float64)
+    arrays["rayleigh_regions"] = np.zeros((n_points, n_layers + 2), np.uint8)
+    res = rcwa_result2d()
+    for name, arr in arrays.items():
+        setattr(res, name, arr.ctypes.data)
+    return res, arrays

@@ -79,6 +79,22 @@ size_t chunk_bytes(const rcwa_gpu_ctx* ctx) {
     return std::min<size_t>(free_b / 2, size_t(48) << 30);
 }
 
+// Device bytes a 2-D call may hold: free memory plus what the stream-ordered pool caches unused.
+size_t chunk_bytes2d(const rcwa_gpu_ctx* ctx) {
+    if (ctx->workspace_limit) return ctx->workspace_limit;
+    size_t free_b = 0, total = 0;
+    if (cudaMemGetInfo(&free_b, &total) != cudaSuccess) return size_t(8) << 30;
+    size_t cached = 0;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) {
+        uint64_t reserved = 0, used = 0;
+        if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess &&
+            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess && reserved > used)
+            cached = (size_t)(reserved - used);
+    }
+    return (size_t)(0.8 * (double)(free_b + cached));
+}
+
 void check_result_ptrs(const rcwa_result1d* out) {
     if (!out || !out->R || !out->T || !out->DEr || !out->DEt)
         throw EngineError{RCWA_EINVAL, "rcwa: result arrays R, T, DEr, DEt are required"};
@@ -232,6 +248,29 @@ int rcwa_gpu_solve1d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const r
         copy_back(out->n_dense_solve, d.n_dense_solve, n_points, st);
         if (opt.diagnostics) copy_back(out->max_eig_residual, d.max_eig_residual, n_points, st);
         RCWA_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int rcwa_gpu_solve2d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points,
+                           int M1, int M2, int factorization, const rcwa_options* options, rcwa_result2d* out) {
+    return guarded(ctx, [&] {
+        if (!stack || n_points < 0 || (n_points > 0 && !points)) throw EngineError{RCWA_EINVAL, "rcwa2d: stack and points are required"};
+        if (!out || !out->Kx || !out->Ky || !out->kzI || !out->kzII || !out->Ex_r || !out->Ey_r || !out->Ez_r || !out->Ex_t ||
+            !out->Ey_t || !out->Ez_t || !out->Rs || !out->Rp || !out->Ts || !out->Tp || !out->DEr || !out->DEt ||
+            !out->prop_r || !out->prop_t || !out->status)
+            throw EngineError{RCWA_EINVAL, "rcwa2d: every result array but the optional ones is required"};
+        validate2d(*stack, points, n_points, M1, M2, factorization);
+        const Options opt = to_options(options);
+        if (n_points == 0) return;
+        solve2d_host(ctx->stream, *stack, points, n_points, M1, M2, factorization, opt, *out, chunk_bytes2d(ctx));
+    });
+}
+
+int rcwa_gpu_layer_operators2d(rcwa_gpu_ctx* ctx, const rcwa_layer2d* layer, double Lx, double Ly, int M1, int M2,
+                               int factorization, rcwa_complex* eps, rcwa_complex* cx, rcwa_complex* cy, int* singular) {
+    return guarded(ctx, [&] {
+        if (!layer) throw EngineError{RCWA_EINVAL, "rcwa2d: layer is required"};
+        layer_operators2d(ctx->stream, *layer, Lx, Ly, M1, M2, factorization, eps, cx, cy, singular);
     });
 }
 

@@ -143,6 +143,14 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                           const Options& opt, const rcwa_result_conical& d_out, size_t chunk_bytes);
 void validate_conical(const rcwa_stack1d& stack, const rcwa_point_conical* h_points, int n_points, int M);
 
+// 2-D crossed gratings (rcwa2d.cu): validation where the reference throws std::invalid_argument,
+// the batched solve over host points into host result arrays, and one layer's Fourier operators.
+void validate2d(const rcwa_stack2d& stack, const rcwa_point2d* points, int n_points, int M1, int M2, int factorization);
+void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d* points, int n_points, int M1, int M2,
+                  int factorization, const Options& opt, const rcwa_result2d& out, size_t chunk_bytes);
+void layer_operators2d(cudaStream_t st, const rcwa_layer2d& layer, double Lx, double Ly, int M1, int M2,
+                       int factorization, rcwa_complex* eps, rcwa_complex* cx, rcwa_complex* cy, int* singular);
+
 // Validation of a 1-D problem exactly where the reference throws std::invalid_argument.
 void validate1d(const rcwa_stack1d& stack, const rcwa_point1d* h_points, int n_points, int M, int pol);
 

@@ -65,6 +65,9 @@ def load_library(build_if_missing=True):
     L.rcwa_gpu_solve1d_batch_dev.argtypes = L.rcwa_gpu_solve1d_batch.argtypes
     L.rcwa_gpu_solve_conical_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack1d), vp, ci, ci,
                                                C.POINTER(abi.rcwa_options), C.POINTER(abi.rcwa_result_conical)]
+    L.rcwa_gpu_solve2d_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack2d), vp, ci, ci, ci, ci,
+                                         C.POINTER(abi.rcwa_options), C.POINTER(abi.rcwa_result2d)]
+    L.rcwa_gpu_layer_operators2d.argtypes = [vp, C.POINTER(abi.rcwa_layer2d), cd, cd, ci, ci, ci, vp, vp, vp, vp]
     L.rcwa_gpu_eig_batch.argtypes = [vp, ci, ci, vp, cd, ci, vp, vp, vp, vp]
     L.rcwa_gpu_eig_batch_dev.argtypes = [vp, ci, ci, vp, cd, ci, vp, vp, vp, vp]
     L.rcwa_gpu_solve_batch.argtypes = [vp, ci, ci, ci, vp, vp, vp, vp]
@@ -200,6 +203,46 @@ class Engine:
         a = self.solve_conical_arrays(stack, [(wavelength, theta_deg, phi_deg)], M, options)
         return {k: v[0] for k, v in a.items()}
 
+    # ---------------------------------------------------------------- 2-D crossed gratings
+
+    def solve2d_arrays(self, stack, points, M1, M2, laurent=False, options=None):
+        """rcwa::solve2d at every (wavelength, theta_deg, phi_deg, Es, Ep) point: dict of numpy arrays
+        (P, N) for Kx, Ky, kzI, kzII, Ex_r .. Ez_t, Rs, Rp, Ts, Tp, DEr, DEt, prop_r, prop_t and (P,)
+        for status, eig_info, n_eig, n_dense_solve, max_eig_residual, plus rayleigh_regions
+        (P, n_layers + 2)."""
+        st, keep = abi.marshal_stack2d(stack)
+        pts = abi.points2d_array(points)
+        N = (2 * M1 + 1) * (2 * M2 + 1)
+        res, arrays = abi.result2d_views(len(points), N, len(stack.layers))
+        o = _options(options)
+        fact = abi.RCWA_FACTORIZATION_LAURENT if laurent else abi.RCWA_FACTORIZATION_LI
+        self._check(self.L.rcwa_gpu_solve2d_batch(self.h, C.byref(st), C.cast(pts, C.c_void_p), len(points), M1, M2,
+                                                  fact, C.byref(o), C.byref(res)))
+        return arrays
+
+    def solve2d(self, stack, wavelength, theta_deg, phi_deg, M1, M2, jones, laurent=False, options=None):
+        """One rcwa::solve2d (include/stablercwa/rcwa2d.hpp:1359): arrays of that point, plus the
+        reference's message for a Rayleigh anomaly (region and (m, n) list)."""
+        a = self.solve2d_arrays(stack, [(wavelength, theta_deg, phi_deg, jones[0], jones[1])], M1, M2, laurent, options)
+        r = {k: v[0] for k, v in a.items()}
+        r["message"] = rayleigh_message(stack, r, M1, M2) if r["status"] == abi.RCWA_SAMPLE_RAYLEIGH else ""
+        return r
+
+    def layer_operators2d(self, layer, Lx, Ly, M1, M2, laurent=False):
+        """Eps, Cx, Cy (N x N) of one layer (rcwa::detail2d::layer_operators,
+        include/stablercwa/rcwa2d_operators.hpp:325) and the singular flag."""
+        keep = []
+        s = abi.rcwa_layer2d()
+        abi.marshal_layer2d(layer, s, keep)
+        N = (2 * M1 + 1) * (2 * M2 + 1)
+        mats = [np.empty((N, N), np.complex128) for _ in range(3)]  # column-major storage: transposed below
+        sing = C.c_int(0)
+        fact = abi.RCWA_FACTORIZATION_LAURENT if laurent else abi.RCWA_FACTORIZATION_LI
+        self._check(self.L.rcwa_gpu_layer_operators2d(self.h, C.byref(s), float(Lx), float(Ly), M1, M2, fact,
+                                                      mats[0].ctypes.data, mats[1].ctypes.data, mats[2].ctypes.data,
+                                                      C.byref(sing)))
+        return mats[0].T.copy(), mats[1].T.copy(), mats[2].T.copy(), bool(sing.value)
+
     # ---------------------------------------------------------------- dense kernels (custom_* hooks)
 
     def eig_batch(self, a, eps=float(np.finfo(np.float64).eps), max_iter=30):
@@ -241,3 +284,26 @@ class Engine:
         c = np.empty((batch, n, m), np.complex128)
         self._check(self.L.rcwa_gpu_multiply_batch(self.h, m, k, n, batch, ca.ctypes.data, cb.ctypes.data, c.ctypes.data))
         return c.transpose(0, 2, 1)
+
+
+def rayleigh_message(stack, r, M1, M2):
+    """Regions and (m, n) orders with kz exactly 0, listed as the reference lists them
+    (report_rayleigh, include/stablercwa/rcwa2d.hpp:1012-1026), in English."""
+    n2 = 2 * M2 + 1
+    N = (2 * M1 + 1) * n2
+    mn = [(i // n2 - M1, i % n2 - M2) for i in range(N)]
+    parts = []
+
+    def region(name, kz):
+        orders = [mn[i] for i in range(N) if kz[i] == 0]
+        if orders:
+            parts.append(f"{name}: " + ", ".join(f"({m}, {n})" for m, n in orders))
+
+    region("incident medium", r["kzI"])
+    region("exit medium", r["kzII"])
+    for j, L in enumerate(stack.layers):
+        if L.homogeneous and r["rayleigh_regions"][j + 1]:
+            nn = complex(L.n)
+            kz = np.sqrt(nn * nn - r["Kx"] ** 2 - r["Ky"] ** 2)
+            region(f"layer {j + 1}", kz)
+    return "; ".join(parts)

@@ -79,3 +79,71 @@ def stack_from_json(d):
         else:
             layers.append(Layer.grating(L["d"], L["edges"], [c(v) for v in L["n_values"]]))
     return Stack(nI=c(d["nI"]), layers=layers, nII=c(d["nII"]), period=d["period"])
+
+
+# ---------------------------------------------------------------- 2-D crossed gratings
+
+RAYLEIGH_ANOMALY = 3  # RCWA_SAMPLE_RAYLEIGH
+
+
+@dataclass
+class XProfile2D:
+    """Piecewise-constant x profile of one y strip (include/stablercwa/rcwa2d_types.hpp:40-43)."""
+    edges: List[float] = field(default_factory=list)
+    n_values: List[complex] = field(default_factory=list)
+
+
+@dataclass
+class Layer2D:
+    """A uniform layer or K y strips each with an x profile (include/stablercwa/rcwa2d_types.hpp:45-71)."""
+    d: float = 0.0
+    homogeneous: bool = True
+    n: complex = 1.0
+    y_edges: List[float] = field(default_factory=list)
+    x_profiles: List[XProfile2D] = field(default_factory=list)
+    name: str = ""
+
+    @staticmethod
+    def uniform(thickness, index, label=""):
+        return Layer2D(d=float(thickness), homogeneous=True, n=complex(index), name=label)
+
+    @staticmethod
+    def patterned(thickness, y_boundaries, rows, label=""):
+        return Layer2D(d=float(thickness), homogeneous=False, y_edges=[float(y) for y in y_boundaries],
+                       x_profiles=list(rows), name=label)
+
+
+@dataclass
+class Stack2D:
+    """Incident medium nI (real) | layers | exit medium nII, periods Lx, Ly
+    (include/stablercwa/rcwa2d_types.hpp:73-78)."""
+    nI: float = 1.0
+    nII: complex = 1.0
+    layers: List[Layer2D] = field(default_factory=list)
+    Lx: float = 1.0
+    Ly: float = 1.0
+
+
+def harmonic_index_2d(m, n, M1, M2):
+    """include/stablercwa/rcwa2d_types.hpp:110"""
+    return (m + M1) * (2 * M2 + 1) + (n + M2)
+
+
+def jones_from_angles_2d(psi_deg=90.0, delta_deg=0.0):
+    """[Es, Ep] = [sin psi exp(i delta), cos psi] (include/stablercwa/rcwa2d_types.hpp:104-108)."""
+    psi, delta = np.deg2rad(psi_deg), np.deg2rad(delta_deg)
+    return (np.sin(psi) * np.exp(1j * delta), complex(np.cos(psi)))
+
+
+def stack2d_from_json(d):
+    """Stack2D from the fixture layout written by tests/golden/export_rcwa2d.cpp."""
+    def c(v):
+        return complex(v[0], v[1])
+    layers = []
+    for L in d["layers"]:
+        if "n" in L:
+            layers.append(Layer2D.uniform(L["d"], c(L["n"])))
+        else:
+            rows = [XProfile2D(list(p["edges"]), [c(v) for v in p["n_values"]]) for p in L["x_profiles"]]
+            layers.append(Layer2D.patterned(L["d"], L["y_edges"], rows))
+    return Stack2D(nI=float(d["nI"]), nII=c(d["nII"]), layers=layers, Lx=float(d["Lx"]), Ly=float(d["Ly"]))

@@ -1,3 +1,4 @@
+import gzip
 import json
 import os
 import sys
@@ -15,7 +16,8 @@ def pytest_configure(config):
 
 
 def load_jsonl(name):
-    with open(os.path.join(GOLDEN, name)) as f:
+    opener = gzip.open if name.endswith(".gz") else open
+    with opener(os.path.join(GOLDEN, name), "rt") as f:
         return [json.loads(line) for line in f if line.strip()]
 
 
@@ -40,6 +42,11 @@ def eig_cases():
 @pytest.fixture(scope="session")
 def conical_cases():
     return load_jsonl("conical_cases.jsonl")
+
+
+@pytest.fixture(scope="session")
+def cases2d():
+    return load_jsonl("rcwa2d_cases.jsonl.gz")
 
 
 def jones_from_table(rows):

@@ -9,6 +9,7 @@ g++ and the reference checkout; the fixtures it writes are committed, so the tes
 need the reference.
 """
 import argparse
+import gzip
 import os
 import subprocess
 import sys
@@ -21,6 +22,7 @@ EXPORTERS = [
     ("export_rcwa1d.cpp", "rcwa1d_cases.jsonl"),
     ("export_eig.cpp", "eig_cases.jsonl"),
     ("export_conical.cpp", "conical_cases.jsonl"),
+    ("export_rcwa2d.cpp", "rcwa2d_cases.jsonl.gz"),
 ]
 
 
@@ -42,8 +44,15 @@ def main():
                    os.path.join(HERE, src), "-o", exe]
             print(" ".join(cmd), flush=True)
             subprocess.check_call(cmd)
-            subprocess.check_call([exe, os.path.join(HERE, out)])
-            with open(os.path.join(HERE, out)) as f:
+            dest = os.path.join(HERE, out)
+            plain = os.path.join(tmp, out[:-3]) if out.endswith(".gz") else dest
+            subprocess.check_call([exe, plain])
+            if plain != dest:  # compressed without a timestamp, so the bytes depend on the content only
+                with open(plain, "rb") as src, open(dest, "wb") as raw:
+                    with gzip.GzipFile(filename="", mode="wb", fileobj=raw, compresslevel=9, mtime=0) as gz:
+                        gz.write(src.read())
+            opener = gzip.open if dest.endswith(".gz") else open
+            with opener(dest, "rt") as f:
                 print(f"  {out}: {sum(1 for _ in f)} cases")
 
 
