@@ -319,6 +319,161 @@ def run_ours(args):
     return 0
 
 
+# ------------------------------------------------------------------------------------- other configurations
+
+C3_POINTS, C3_M = 1024, 40
+C4_POINTS, C4_M = 256, 10
+
+
+def workload_c3(seed=SEED):
+    """Batched conical incidence, M = 40 (N = 81, 2N = 162): three gratings with 2-4 random
+    segments (n 1.0..2.5, d 0.05..0.3) and one absorbing film n = 1.5+U(0,.5) + i U(0,.1), period
+    0.574, nI 1.0, nII 1.46; 1024 points lambda 0.5..1.6, theta 0..60, phi 0..90 degrees."""
+    from stablercwa_gb300 import Layer, Stack
+    rng = np.random.default_rng(seed + 3)
+    layers = []
+
+    def grating():
+        K = int(rng.integers(2, 5))
+        inner = np.sort(rng.uniform(0.0, PERIOD, K - 1))
+        return Layer.grating(rng.uniform(0.05, 0.3), [0.0, *inner, PERIOD], list(rng.uniform(1.0, 2.5, K)))
+    layers += [grating(), grating()]
+    layers.append(Layer.uniform(rng.uniform(0.05, 0.3), complex(1.5 + rng.uniform(0, 0.5), rng.uniform(0, 0.1))))
+    layers.append(grating())
+    stack = Stack(nI=1.0, nII=1.46, period=PERIOD, layers=layers)
+    pts = np.stack([rng.uniform(0.5, 1.6, C3_POINTS), rng.uniform(0.0, 60.0, C3_POINTS),
+                    rng.uniform(0.0, 90.0, C3_POINTS)], axis=1)
+    return stack, pts
+
+
+def workload_c4(seed=SEED):
+    """Batched 2-D crossed grating, Mx = My = 10 (N = 441, 2N = 882): square lattice P 0.6..1.0,
+    three patterned layers (d 0.05..0.3; a circular pillar r = 0.15..0.4 P staircased into 16 y strips
+    or a w x h = 0.2..0.7 P rectangle, n = 2.0 in air) between five films (n 1.3..2.2, d 0.05..0.2),
+    nI 1.0, nII 1.46; 256 points lambda 0.4..1.2 at normal incidence, s polarisation."""
+    from stablercwa_gb300 import Layer2D, Stack2D, XProfile2D, jones_from_angles_2d
+    rng = np.random.default_rng(seed + 4)
+    P = rng.uniform(0.6, 1.0)
+
+    def row(x0, x1):
+        if x1 <= x0:
+            return XProfile2D([0.0, P], [1.0])
+        return XProfile2D([0.0, x0, x1, P], [1.0, 2.0, 1.0])
+
+    def patterned():
+        d = rng.uniform(0.05, 0.3)
+        if rng.uniform() < 0.5:
+            r = rng.uniform(0.15, 0.4) * P
+            K = 16
+            ye = [P * k / K for k in range(K + 1)]
+            rows = []
+            for k in range(K):
+                yc = 0.5 * (ye[k] + ye[k + 1]) - 0.5 * P
+                w = np.sqrt(max(r * r - yc * yc, 0.0))
+                rows.append(row(0.5 * P - w, 0.5 * P + w))
+            return Layer2D.patterned(d, ye, rows)
+        w, h = rng.uniform(0.2, 0.7, 2) * P
+        return Layer2D.patterned(d, [0.0, 0.5 * (P - h), 0.5 * (P + h), P],
+                                 [row(0, 0), row(0.5 * (P - w), 0.5 * (P + w)), row(0, 0)])
+
+    def film():
+        return Layer2D.uniform(rng.uniform(0.05, 0.2), rng.uniform(1.3, 2.2))
+    layers = [film(), patterned(), film(), patterned(), film(), patterned(), film(), film()]
+    stack = Stack2D(nI=1.0, nII=1.46, layers=layers, Lx=P, Ly=P)
+    es, ep = jones_from_angles_2d(90.0)
+    pts = [(wl, 0.0, 0.0, es, ep) for wl in rng.uniform(0.4, 1.2, C4_POINTS)]
+    return stack, pts, {"period": float(P)}
+
+
+def run_secondary(args):
+    """--workload c3 | c4 | plain: the conical and 2-D batched configurations, and the C2 structure
+    solved one point per call (the plain path). Measured through the host-buffer entry points (these
+    paths take host arrays), so value and e2e are the same number."""
+    import torch
+    from stablercwa_gb300.engine import Engine, launch_count
+    eng = Engine()
+    peak = fp64_peak_tflops(torch)
+    if args.workload == "c3":
+        stack, pts = workload_c3()
+        n_eig_layers = sum(1 for L in stack.layers if not L.homogeneous)
+        def step():
+            return eng.solve_conical_arrays(stack, pts, C3_M)
+        solves = len(pts)
+        eig_flops = solves * n_eig_layers * 2 * 105 * (2 * C3_M + 1) ** 3
+        metric = "solves/s, batched conical sweep (M=40, 2N=162), full Jones per order"
+        config = {"workload": workload_c3.__doc__.split(":")[0].strip() + " (config 3)", "points": len(pts), "M": C3_M,
+                  "seed": SEED + 3}
+    elif args.workload == "c4":
+        stack, pts, geo = workload_c4()
+        n_pat = sum(1 for L in stack.layers if not L.homogeneous)
+        def step():
+            return eng.solve2d_arrays(stack, pts, C4_M, C4_M)
+        solves = len(pts)
+        eig_flops = solves * n_pat * 105 * (2 * (2 * C4_M + 1) ** 2) ** 3
+        metric = "solves/s, batched 2-D solve2d sweep (Mx=My=10, N=441, 2N=882)"
+        config = {"workload": "batched 2-D crossed grating (config 4)", "points": len(pts), "M1": C4_M, "M2": C4_M,
+                  "seed": SEED + 4, **geo}
+    else:
+        stack, all_pts, geo = workload()
+        pts = all_pts[np.linspace(0, len(all_pts) - 1, 64).astype(int)]
+        def step():
+            return [eng.solve1d_arrays(stack, pts[k:k + 1], M, pol) for pol in (0, 1) for k in range(len(pts))]
+        solves = 2 * len(pts)
+        eig_flops = solves * 105 * (2 * M + 1) ** 3
+        metric = "solves/s, plain path: the C2 structure solved one point per call (M=60, N=121)"
+        config = {"workload": "config 2 structure, 64 of its points x TE+TM, one solve per call", "M": M, "seed": SEED,
+                  **geo}
+    for _ in range(args.warmup):
+        out = step()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0)
+    sampler.start()
+    eng.set_kernel_timing(True)
+    l0 = launch_count()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        out = step()
+        times.append(time.perf_counter() - t0)
+    launches = launch_count() - l0
+    eig_ms, _ = eng.kernel_time("eig")
+    lu_ms, _ = eng.kernel_time("lu")
+    gemm_ms, _ = eng.kernel_time("gemm")
+    eng.set_kernel_timing(False)
+    clocks = sampler.stop()
+    step_s = sum(times) / len(times)
+    value = solves / step_s
+    achieved = eig_flops * args.steps / (eig_ms * 1e-3) / 1e12 if eig_ms > 0 else None
+    line = {"metric": metric, "value": value, "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 (complex128)", "data": "synthetic (seeded)", "config": config,
+            "clocks": clocks, "e2e": {"value": value, "unit": "solves/s", "note": "host-buffer entry point"},
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp64", "kernel": "eig_batch_kernel", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak if achieved else None,
+                         "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (torch.matmul float64), best of 5"},
+            "kernels_ms_per_step": {"eig": eig_ms / args.steps, "lu": lu_ms / args.steps, "gemm": gemm_ms / args.steps,
+                                    "other": 1e3 * step_s - (eig_ms + lu_ms + gemm_ms) / args.steps}}
+    if args.workload == "c3":
+        from oracle import oracle
+        threads = os.cpu_count() or 1
+        idx = np.linspace(0, len(pts) - 1, args.cpu_points).astype(int)
+        t0 = time.perf_counter()
+        ref = oracle.solve_conical_batch(stack, pts[idx], C3_M, threads=threads)
+        dt = time.perf_counter() - t0
+        err = max(float(np.nanmax(np.abs(out[k][idx] - ref[k]))) for k in ("DEr", "DEt"))
+        line["cpu_baseline"] = {"value": len(idx) / dt, "unit": "solves/s", "cores": threads, "kind": "port",
+                                "sample": f"{len(idx)} of the {len(pts)} points, {dt:.1f} s wall"}
+        line["accuracy"] = {"max_abs_dDE_vs_oracle": err, "sample_solves": len(idx),
+                            "all_status_ok": bool((out["status"] == 0).all())}
+    elif args.workload == "c4":
+        line["accuracy"] = {"all_status_ok": bool((out["status"] == 0).all()),
+                            "max_energy_defect": float(np.max(np.abs(out["DEr"].sum(1) + out["DEt"].sum(1) - 1.0)))}
+    print(json.dumps(line), flush=True)
+    eng.close()
+    return 0
+
+
 def run_eig_only(n, batch, group):
     """Profiling case for the eigensolver alone: `batch` lossy layer matrices of order n in the
     benchmark's form (Toeplitz of a binary grating, index 1.46+0.01i, fill 0.4, plus Kx^2 with
@@ -361,6 +516,8 @@ def main():
     ap.add_argument("--eig-group", type=int, default=0)
     ap.add_argument("--cpu-points", type=int, default=128)
     ap.add_argument("--ref-points", type=int, default=128)
+    ap.add_argument("--workload", choices=["c2", "c3", "c4", "plain"], default="c2",
+                    help="c2 (default, the headline line), c3 conical, c4 2-D, plain one-point-per-call")
     ap.add_argument("--eig-only", nargs=2, type=int, metavar=("N", "BATCH"), default=None,
                     help="profiling case: the eigensolver alone on BATCH layer matrices of order N")
     args = ap.parse_args()
@@ -368,6 +525,8 @@ def main():
         return run_eig_only(args.eig_only[0], args.eig_only[1], args.eig_group)
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "c2":
+        return run_secondary(args)
     return run_ours(args)
 
 

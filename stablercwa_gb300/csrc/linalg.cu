@@ -1,4 +1,7 @@
 // linalg.cu -- launchers of the batched LU solve and GEMM (kernels in linalg.cuh).
+#include <algorithm>
+#include <cstdlib>
+
 #include "engine.h"
 #include "linalg.cuh"
 
@@ -43,10 +46,93 @@ TimedLaunch::~TimedLaunch() {
     if (t_) cudaEventRecord(t_->pending[idx_].b, st_);
 }
 
+namespace {
+
+// Orders from which the blocked LU replaces the warp-per-system kernel (RCWA_GB300_LU_BLOCKED_MIN_N
+// overrides it for measurements).
+int lu_blocked_min_n() {
+    static const int v = [] {
+        const char* e = std::getenv("RCWA_GB300_LU_BLOCKED_MIN_N");
+        return e ? std::atoi(e) : 100;
+    }();
+    return v;
+}
+
+constexpr int kPanel = 32;
+
+void zgemm_raw(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride, const zc* B,
+               int ldb, long long b_stride, zc* C, int ldc, long long c_stride, double s_ab, const int* skip, int skip_value) {
+    if (batch <= 0 || m <= 0 || n <= 0 || k <= 0) return;
+    const long long warps = (long long)batch * ((m + 31) / 32) * ((n + 7) / 8);
+    const unsigned blocks = (unsigned)((warps * 32 + 127) / 128);
+    zgemm_kernel<<<blocks, 128, 0, st>>>(m, n, k, batch, A, lda, a_stride, B, ldb, b_stride, C, c_stride, C, ldc,
+                                         c_stride, s_ab, 1.0, skip, skip_value);
+    ++launch_count();
+    RCWA_CUDA(cudaGetLastError());
+}
+
+void lu_solve_blocked(cudaStream_t st, int n, int nrhs, int batch, const zc* a, long long a_stride, zc* lu,
+                      long long lu_stride, int rhs_kind, const zc* rhs, long long rhs_stride, zc* x, long long x_stride,
+                      int* singular, const int* skip, int skip_value) {
+    int* sing_local = nullptr;
+    RCWA_CUDA(cudaMallocAsync(&sing_local, (size_t)batch * sizeof(int), st));
+    RCWA_CUDA(cudaMemsetAsync(sing_local, 0, (size_t)batch * sizeof(int), st));
+    const long long init = (long long)batch * n * (n + nrhs);
+    lu_init_kernel<<<(unsigned)((init + 255) / 256), 256, 0, st>>>(n, nrhs, batch, a, a_stride, lu, lu_stride, rhs_kind, rhs,
+                                                                   rhs_stride, x, x_stride, skip, skip_value);
+    ++launch_count();
+    RCWA_CUDA(cudaGetLastError());
+    for (int k0 = 0; k0 < n; k0 += kPanel) {
+        const int kend = std::min(k0 + kPanel, n);
+        lu_panel_kernel<<<(unsigned)batch, 256, 0, st>>>(n, nrhs, batch, lu, lu_stride, x, x_stride, k0, kPanel, sing_local,
+                                                         skip, skip_value);
+        ++launch_count();
+        RCWA_CUDA(cudaGetLastError());
+        const long long tcols = (long long)batch * (n + nrhs - kend);
+        if (tcols > 0) {
+            lu_trsm_lower_kernel<<<(unsigned)((tcols + 127) / 128), 128, 0, st>>>(n, nrhs, batch, lu, lu_stride, x, x_stride,
+                                                                                  k0, kend, skip, skip_value);
+            ++launch_count();
+            RCWA_CUDA(cudaGetLastError());
+        }
+        const int rest = n - kend, w = kend - k0;
+        // trailing matrix and right-hand sides: C -= L21 U12
+        zgemm_raw(st, rest, rest, w, batch, lu + (long long)k0 * n + kend, n, lu_stride, lu + (long long)kend * n + k0, n,
+                  lu_stride, lu + (long long)kend * n + kend, n, lu_stride, -1.0, skip, skip_value);
+        zgemm_raw(st, rest, nrhs, w, batch, lu + (long long)k0 * n + kend, n, lu_stride, x + k0, n, x_stride, x + kend, n,
+                  x_stride, -1.0, skip, skip_value);
+    }
+    const int nblk = (n + kPanel - 1) / kPanel;
+    for (int kb = nblk - 1; kb >= 0; --kb) {
+        const int r0 = kb * kPanel, r1 = std::min(r0 + kPanel, n);
+        const long long t = (long long)batch * nrhs;
+        lu_trsm_upper_kernel<<<(unsigned)((t + 127) / 128), 128, 0, st>>>(n, nrhs, batch, lu, lu_stride, x, x_stride, r0, r1,
+                                                                          skip, skip_value);
+        ++launch_count();
+        RCWA_CUDA(cudaGetLastError());
+        // rows above: X[0:r0] -= U[0:r0, r0:r1] X[r0:r1]
+        zgemm_raw(st, r0, nrhs, r1 - r0, batch, lu + (long long)r0 * n, n, lu_stride, x + r0, n, x_stride, x, n, x_stride,
+                  -1.0, skip, skip_value);
+    }
+    const long long xt = (long long)batch * n * nrhs;
+    lu_nan_fill_kernel<<<(unsigned)((xt + 255) / 256), 256, 0, st>>>(n, nrhs, batch, x, x_stride, sing_local, singular);
+    ++launch_count();
+    RCWA_CUDA(cudaGetLastError());
+    RCWA_CUDA(cudaFreeAsync(sing_local, st));
+}
+
+}  // namespace
+
 void launch_lu_solve(cudaStream_t st, int n, int nrhs, int batch, const zc* a, long long a_stride, zc* lu,
                      long long lu_stride, int rhs_kind, const zc* rhs, long long rhs_stride, zc* x, long long x_stride,
                      int* singular, const int* skip, int skip_value) {
     if (batch <= 0 || n <= 0) return;
+    if (n >= lu_blocked_min_n() && nrhs > 0) {
+        TimedLaunch timed(TK_LU, st);
+        lu_solve_blocked(st, n, nrhs, batch, a, a_stride, lu, lu_stride, rhs_kind, rhs, rhs_stride, x, x_stride, singular,
+                         skip, skip_value);
+        return;
+    }
     const long long threads = (long long)batch * 32;
     const unsigned blocks = (unsigned)((threads + 127) / 128);
     TimedLaunch timed(TK_LU, st);

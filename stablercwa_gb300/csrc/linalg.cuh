@@ -146,6 +146,180 @@ __global__ void __launch_bounds__(128) lu_solve_kernel(int n, int nrhs, int batc
     }
 }
 
+// ---------------------------------------------------------------- blocked LU for large n
+//
+// The same partial-pivot elimination of [A | B] as lu_solve_kernel, reorganised for orders where a
+// warp per system cannot keep the trailing matrix anywhere near the FP64 pipe: panels of nb columns
+// are factored by one CTA per system (pivot search, full-row swaps over A and the right-hand sides,
+// multipliers, rank-1 updates inside the panel), the panel rows of the remaining columns are solved
+// with the unit lower triangle (same subtraction order as the unblocked sweep), and the trailing
+// matrix and right-hand sides are updated with zgemm_kernel. Back substitution runs block by block
+// from the bottom: a triangular solve of the block rows, then a GEMM update of the rows above.
+
+__device__ __forceinline__ zc* aug_col(zc* L, zc* X, int n, int c) {
+    return c < n ? L + (long long)c * n : X + (long long)(c - n) * n;
+}
+
+// lu = a (if distinct), x = rhs (dense, identity or diagonal)
+__global__ void lu_init_kernel(int n, int nrhs, int batch, const zc* a, long long a_stride, zc* lu, long long lu_stride,
+                               int rhs_kind, const zc* rhs, long long rhs_stride, zc* x, long long x_stride,
+                               const int* __restrict__ skip, int skip_value) {
+    const long long per = (long long)n * (n + nrhs);
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)batch * per) return;
+    const long long sys = idx / per;
+    if (skip && skip[sys] == skip_value) return;
+    const long long e = idx - sys * per;
+    const long long nn = (long long)n * n;
+    if (e < nn) {
+        const zc* A = a + sys * a_stride;
+        zc* L = lu + sys * lu_stride;
+        if (L != A) L[e] = A[e];
+        return;
+    }
+    const long long xe = e - nn;
+    zc* Xs = x + sys * x_stride;
+    if (rhs_kind == RHS_DENSE) {
+        const zc* Bs = rhs + sys * rhs_stride;
+        if (Bs != Xs) Xs[xe] = Bs[xe];
+    } else {
+        const int c = (int)(xe / n), r = (int)(xe - (long long)c * n);
+        const zc* d = rhs_kind == RHS_DIAG ? rhs + sys * rhs_stride : nullptr;
+        Xs[xe] = r == c ? (d ? d[r] : zc{1.0, 0.0}) : zc{0.0, 0.0};
+    }
+}
+
+// Factor columns k0 .. k0+nb-1 (all rows below the diagonal), one 256-thread CTA per system.
+__global__ void __launch_bounds__(256) lu_panel_kernel(int n, int nrhs, int batch, zc* lu, long long lu_stride, zc* x,
+                                                       long long x_stride, int k0, int nb, int* __restrict__ sing_local,
+                                                       const int* __restrict__ skip, int skip_value) {
+    const long long sys = blockIdx.x;
+    if (sys >= batch) return;
+    if (skip && skip[sys] == skip_value) return;
+    __shared__ double s_best[8];
+    __shared__ int s_idx[8];
+    __shared__ int s_piv;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    zc* L = lu + sys * lu_stride;
+    zc* X = x + sys * x_stride;
+    const int kend = min(k0 + nb, n);
+    for (int j = k0; j < kend; ++j) {
+        zc* col = L + (long long)j * n;
+        double best = -1.0;
+        int bi = n;
+        for (int i = j + tid; i < n; i += 256) {
+            const double v = zabs(col[i]);
+            if (v > best) {
+                best = v;
+                bi = i;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > best || (ov == best && oi < bi)) {
+                best = ov;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            s_best[warp] = best;
+            s_idx[warp] = bi;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double b = s_best[0];
+            int ix = s_idx[0];
+            for (int w = 1; w < 8; ++w)
+                if (s_best[w] > b || (s_best[w] == b && s_idx[w] < ix)) {
+                    b = s_best[w];
+                    ix = s_idx[w];
+                }
+            s_piv = (b < 0.0 || ix >= n) ? j : ix;  // all-NaN column: keep the diagonal
+        }
+        __syncthreads();
+        const int p = s_piv;
+        if (p != j) {
+            for (int c = tid; c < n + nrhs; c += 256) {
+                zc* cc = aug_col(L, X, n, c);
+                const zc t = cc[j];
+                cc[j] = cc[p];
+                cc[p] = t;
+            }
+            __syncthreads();
+        }
+        const zc piv = col[j];
+        if (is_zero(piv)) {
+            if (tid == 0) sing_local[sys] = 1;
+            for (int i = j + 1 + tid; i < n; i += 256) col[i] = zc{0.0, 0.0};
+            __syncthreads();
+            continue;
+        }
+        const zc inv = zinv(piv);
+        const bool inv_ok = zfinite(inv);
+        for (int i = j + 1 + tid; i < n; i += 256) col[i] = inv_ok ? col[i] * inv : zdiv(col[i], piv);
+        __syncthreads();
+        const int rows = n - j - 1, cols = kend - j - 1;
+        const long long total = (long long)rows * cols;
+        for (long long t = tid; t < total; t += 256) {
+            const int c = j + 1 + (int)(t / rows), i = j + 1 + (int)(t % rows);
+            zc* cc = L + (long long)c * n;
+            cc[i] = zfms(col[i], cc[j], cc[i]);
+        }
+        __syncthreads();
+    }
+}
+
+// Rows k0+1 .. kend-1 of columns kend .. n+nrhs-1: forward substitution with the panel's unit lower
+// triangle, one thread per (system, column).
+__global__ void lu_trsm_lower_kernel(int n, int nrhs, int batch, zc* lu, long long lu_stride, zc* x, long long x_stride,
+                                     int k0, int kend, const int* __restrict__ skip, int skip_value) {
+    const int cols = n + nrhs - kend;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)batch * cols) return;
+    const long long sys = idx / cols;
+    if (skip && skip[sys] == skip_value) return;
+    const int c = kend + (int)(idx - sys * cols);
+    zc* L = lu + sys * lu_stride;
+    zc* cc = aug_col(L, x + sys * x_stride, n, c);
+    for (int r = k0 + 1; r < kend; ++r) {
+        zc acc = cc[r];
+        for (int q = k0; q < r; ++q) acc = zfms(L[(long long)q * n + r], cc[q], acc);
+        cc[r] = acc;
+    }
+}
+
+// Rows r0 .. r1-1 of the right-hand sides: backward substitution with the diagonal block of U.
+__global__ void lu_trsm_upper_kernel(int n, int nrhs, int batch, const zc* lu, long long lu_stride, zc* x,
+                                     long long x_stride, int r0, int r1, const int* __restrict__ skip, int skip_value) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)batch * nrhs) return;
+    const long long sys = idx / nrhs;
+    if (skip && skip[sys] == skip_value) return;
+    const int c = (int)(idx - sys * nrhs);
+    const zc* U = lu + sys * lu_stride;
+    zc* xc = x + sys * x_stride + (long long)c * n;
+    for (int r = r1 - 1; r >= r0; --r) {
+        zc acc = xc[r];
+        for (int q = r + 1; q < r1; ++q) acc = zfms(U[(long long)q * n + r], xc[q], acc);
+        xc[r] = zdiv(acc, U[(long long)r * n + r]);
+    }
+}
+
+// a zero pivot in this call: the reference refuses to solve; the solution is reported as NaN
+__global__ void lu_nan_fill_kernel(int n, int nrhs, int batch, zc* x, long long x_stride, const int* __restrict__ sing_local,
+                                   int* __restrict__ singular) {
+    const long long per = (long long)n * nrhs;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)batch * per) return;
+    const long long sys = idx / per;
+    if (!sing_local[sys]) return;
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    x[sys * x_stride + (idx - sys * per)] = zc{nan, nan};
+    if (idx - sys * per == 0) singular[sys] = 1;
+}
+
 // Batched complex GEMM: C = s_ab * (A B) + s_c * C0, one warp per 32 x 8 tile of C, lanes along rows.
 // A: m x k (lda), B: k x n (ldb), C/C0: m x n (ldc); any stride may be 0 to broadcast one operand
 // to the whole batch. s_ab, s_c in {-1, 0, 1}. C may alias C0 (each element is read then written by

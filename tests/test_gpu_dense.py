@@ -94,6 +94,27 @@ def test_lu_solve_and_gemm(eng):
     z[0, :, 0] = 1.0
     x, sing = eng.solve_batch(z, np.ones((1, 3, 1), complex))
     assert sing[0] and np.isnan(x[0]).all()          # zero pivot: lu.hpp:427-436 throws
+
+
+@pytest.mark.parametrize("n, nrhs", [(160, 160), (161, 7), (200, 200), (330, 1), (257, 300)])
+def test_blocked_lu(eng, n, nrhs):
+    """Orders from 100 up run the panel / triangular-solve / GEMM form of the same elimination."""
+    rng = np.random.default_rng(n + nrhs)
+    a = rng.standard_normal((3, n, n)) + 1j * rng.standard_normal((3, n, n))
+    b = rng.standard_normal((3, n, nrhs)) + 1j * rng.standard_normal((3, n, nrhs))
+    x, sing = eng.solve_batch(a, b)
+    assert not sing.any()
+    for k in range(3):
+        xo, so = oracle.solve(a[k], b[k])
+        assert np.max(np.abs(x[k] - xo)) <= 1e-10 * max(1.0, np.max(np.abs(xo)))
+    # a zero pivot in the second panel: singular flag and NaN solution, other systems unaffected
+    z = a.copy()
+    z[1, :, 40] = 0.0
+    z[1, :, 41] = 0.0
+    z[1, 41, :] = 0.0
+    x, sing = eng.solve_batch(z, b)
+    assert sing.tolist() == [False, True, False]
+    assert np.isnan(x[1]).all() and np.isfinite(x[0]).all() and np.isfinite(x[2]).all()
     for m, k, n in [(1, 1, 1), (33, 17, 9), (121, 121, 121)]:
         a = rng.standard_normal((3, m, k)) + 1j * rng.standard_normal((3, m, k))
         b = rng.standard_normal((3, k, n)) + 1j * rng.standard_normal((3, k, n))
