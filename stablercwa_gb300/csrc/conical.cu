@@ -381,39 +381,40 @@ __global__ void right_triangular_solve_kernel(int B, int n, zc* __restrict__ Vm,
     if (bad && lane == 0) fail[b] = 1;
 }
 
-// exp(-k0 d G) for the Schur samples by scaling and squaring (rcwa1d_conical.hpp:439-464).
-// Warp per sample; e, term, tmp are n x n workspaces per sample.
-__device__ void tri_product(const zc* a, const zc* b, zc* c, int n, int lane) {
-    for (long long k = lane; k < (long long)n * n; k += 32) {
-        const int j = (int)(k / n), i = (int)(k - (long long)j * n);
-        zc acc = zc{0.0, 0.0};
-        for (int q = 0; q < n; ++q) acc = zfma(a[(long long)q * n + i], b[(long long)j * n + q], acc);
-        c[k] = acc;
-    }
-    __syncwarp();
-}
-__global__ void triangular_exp_kernel(int B, int n, const zc* __restrict__ G, const double* __restrict__ k0, double d,
-                                      zc* __restrict__ E, zc* __restrict__ work, const int* __restrict__ schur,
-                                      int* __restrict__ fail) {
+// exp(-k0 d G) for the Schur samples by scaling and squaring (rcwa1d_conical.hpp:439-464), with the
+// n x n products done by batched GEMMs over the Schur samples (a product of two upper triangular
+// matrices by a full GEMM adds only exact zeros outside the triangle, so every entry equals the
+// triangular product). Host-driven: prep, Taylor
+// terms until every sample has converged (at most 40), then the squarings. Per sample, work holds
+// a = -k0 d G, bm = a 2^-s, term and tmp; iter[b] is 1 while sample b sums Taylor terms, done[b]
+// is 1 once its sum has converged.
+__global__ void texp_prep_kernel(int B, int n, const zc* __restrict__ G, const double* __restrict__ k0, double d,
+                                 zc* __restrict__ E, zc* __restrict__ work, const int* __restrict__ schur,
+                                 int* __restrict__ iter, int* __restrict__ done, int* __restrict__ scal,
+                                 int* __restrict__ max_scal, int* __restrict__ fail) {
     const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (b >= B || !schur[b]) return;
+    if (b >= B) return;
     const int lane = threadIdx.x & 31;
+    if (lane == 0) {
+        iter[b] = 0;
+        done[b] = 0;
+        scal[b] = 0;
+    }
+    if (!schur[b]) return;
     const long long nn = (long long)n * n;
     const double f = -k0[b] * d;
     zc* a = work + b * 4 * nn;
     zc* bm = a + nn;
     zc* term = bm + nn;
-    zc* tmp = term + nn;
     zc* e = E + b * nn;
     const zc* g = G + b * nn;
-    bool bad = false;
     for (long long k = lane; k < nn; k += 32) a[k] = zc{f * g[k].re, f * g[k].im};
     __syncwarp();
     const double size = warp_norm1_upper(a, n, lane);
-    if (!isfinite(size)) bad = true;
+    bool bad = !isfinite(size);
     const int scaling = size > .25 ? max(0, (int)ceil(log2(size) + 2.)) : 0;
     if (scaling > 1020) bad = true;
-    if (__any_sync(0xffffffffu, bad)) {
+    if (bad) {
         if (lane == 0) fail[b] = 1;
         return;
     }
@@ -424,48 +425,83 @@ __global__ void triangular_exp_kernel(int B, int n, const zc* __restrict__ G, co
         e[k] = zc{i == j ? 1.0 : 0.0, 0.0};
         term[k] = e[k];
     }
+    if (lane == 0) {
+        if (n == 0) done[b] = 1;
+        else iter[b] = 1;
+        scal[b] = scaling;
+        atomicMax(max_scal, scaling);
+    }
+}
+
+// term = tmp / kk, e += term, then the convergence test ||term||_1 <= eps max(1, ||e||_1)
+__global__ void texp_term_kernel(int B, int n, int kk, zc* __restrict__ E, zc* __restrict__ work, int* __restrict__ iter,
+                                 int* __restrict__ done, int* __restrict__ any_iter, int* __restrict__ fail) {
+    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (b >= B || !iter[b]) return;
+    const int lane = threadIdx.x & 31;
+    const long long nn = (long long)n * n;
+    zc* term = work + b * 4 * nn + 2 * nn;
+    const zc* tmp = term + nn;
+    zc* e = E + b * nn;
+    const double inv = 1. / kk;
+    bool bad = false;
+    for (long long k = lane; k < nn; k += 32) {
+        term[k] = tmp[k] * zc{inv, 0.0};
+        e[k] = e[k] + term[k];
+        if (!zfinite(e[k]) || !zfinite(term[k])) bad = true;
+    }
     __syncwarp();
-    bool converged = n == 0;
-    for (int kk = 1; kk <= 40 && !converged; ++kk) {
-        tri_product(term, bm, tmp, n, lane);
-        const double inv = 1. / kk;
-        for (long long k = lane; k < nn; k += 32) {
-            term[k] = tmp[k] * zc{inv, 0.0};
-            e[k] = e[k] + term[k];
-            if (!zfinite(e[k]) || !zfinite(term[k])) bad = true;
+    bad = __any_sync(0xffffffffu, bad);
+    bool converged = false;
+    if (!bad) converged = warp_norm1_upper(term, n, lane) <= 2.220446049250313e-16 * fmax(1., warp_norm1_upper(e, n, lane));
+    if (lane == 0) {
+        if (bad || (!converged && kk == 40)) {
+            fail[b] = 1;
+            iter[b] = 0;
+        } else if (converged) {
+            iter[b] = 0;
+            done[b] = 1;
+        } else {
+            atomicOr(any_iter, 1);
         }
-        __syncwarp();
-        if (__any_sync(0xffffffffu, bad)) {
-            if (lane == 0) fail[b] = 1;
-            return;
-        }
-        converged = warp_norm1_upper(term, n, lane) <= 2.220446049250313e-16 * fmax(1., warp_norm1_upper(e, n, lane));
     }
-    if (!converged) {
-        if (lane == 0) fail[b] = 1;
-        return;
-    }
-    for (int i = lane; i < n; i += 32) {
-        const zc ai = a[(long long)i * n + i];
-        e[(long long)i * n + i] = zexp(zc{ai.re * sf, ai.im * sf});
-    }
-    __syncwarp();
-    for (int k = 0; k < scaling; ++k) {
-        tri_product(e, e, tmp, n, lane);
-        const double s2 = ldexp(1., k + 1 - scaling);
+}
+
+// e_ii = exp(a_ii 2^(k+1-s)): after the Taylor sum (mode 0, k = -1), or after squaring k (mode 1,
+// which first copies the product in), for converged samples with k < s
+__global__ void texp_fix_kernel(int B, int n, int k, int mode, zc* __restrict__ E, const zc* __restrict__ work,
+                                const int* __restrict__ done, const int* __restrict__ scal, int* __restrict__ fail) {
+    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (b >= B || !done[b]) return;
+    const int s_ = scal[b];
+    if (mode == 1 && k >= s_) return;
+    const int lane = threadIdx.x & 31;
+    const long long nn = (long long)n * n;
+    const zc* a = work + b * 4 * nn;
+    const zc* tmp = a + 3 * nn;
+    zc* e = E + b * nn;
+    bool bad = false;
+    if (mode == 1) {
         for (long long q = lane; q < nn; q += 32) {
             e[q] = tmp[q];
             if (!zfinite(e[q])) bad = true;
         }
         __syncwarp();
-        for (int i = lane; i < n; i += 32) {
-            const zc ai = a[(long long)i * n + i];
-            e[(long long)i * n + i] = zexp(zc{ai.re * s2, ai.im * s2});
-        }
-        __syncwarp();
+    }
+    const double s2 = ldexp(1., k + 1 - s_);
+    for (int i = lane; i < n; i += 32) {
+        const zc ai = a[(long long)i * n + i];
+        e[(long long)i * n + i] = zexp(zc{ai.re * s2, ai.im * s2});
     }
     bad = __any_sync(0xffffffffu, bad);
     if (bad && lane == 0) fail[b] = 1;
+}
+
+// 1 where sample b squares at step k
+__global__ void texp_square_mask_kernel(int B, int k, const int* __restrict__ done, const int* __restrict__ scal,
+                                        int* __restrict__ mask) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < B) mask[b] = done[b] && k < scal[b];
 }
 
 // Fresnel blocks between two analytic regions in the (w, v) form (rcwa1d_conical.hpp:513-533)
@@ -614,6 +650,40 @@ __global__ void schur_info_kernel(int B, const int* __restrict__ info, const int
         if (eig_info[b] == 0) eig_info[b] = info[b];
         fail[b] = 1;
     }
+}
+
+// exp(-k0 d G) of the Schur samples into E (B x n x n); work holds 4 n x n per sample
+void batched_triangular_exp(Batch& c, int n, const zc* G, const double* k0, double d, zc* E, zc* work, const int* schur) {
+    const cudaStream_t st = c.st;
+    const int B = c.B;
+    const long long nn = (long long)n * n;
+    int* iter = c.mem->zeros<int>(B);
+    int* done = c.mem->zeros<int>(B);
+    int* scal = c.mem->zeros<int>(B);
+    int* mask = c.mem->zeros<int>(B);
+    int* flags = c.mem->zeros<int>(2);  // [0] largest scaling, [1] any sample still summing terms
+    LAUNCH(texp_prep_kernel, warp_blocks(B), 128, st, B, n, G, k0, d, E, work, schur, iter, done, scal, flags, c.fail);
+    for (int kk = 1; kk <= 40; ++kk) {
+        // tmp = term bm for the samples still summing
+        launch_zgemm(st, n, n, n, B, work + 2 * nn, n, 4 * nn, work + nn, n, 4 * nn, nullptr, 0, work + 3 * nn, n, 4 * nn,
+                     1.0, 0.0, iter, 0);
+        RCWA_CUDA(cudaMemsetAsync(flags + 1, 0, sizeof(int), st));
+        LAUNCH(texp_term_kernel, warp_blocks(B), 128, st, B, n, kk, E, work, iter, done, flags + 1, c.fail);
+        int any = 0;
+        RCWA_CUDA(cudaMemcpyAsync(&any, flags + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        RCWA_CUDA(cudaStreamSynchronize(st));
+        if (!any) break;
+    }
+    LAUNCH(texp_fix_kernel, warp_blocks(B), 128, st, B, n, -1, 0, E, work, done, scal, c.fail);
+    int max_scal = 0;
+    RCWA_CUDA(cudaMemcpyAsync(&max_scal, flags, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RCWA_CUDA(cudaStreamSynchronize(st));
+    for (int k = 0; k < max_scal; ++k) {
+        LAUNCH(texp_square_mask_kernel, nblocks(B), kTpb, st, B, k, done, scal, mask);
+        launch_zgemm(st, n, n, n, B, E, n, nn, E, n, nn, nullptr, 0, work + 3 * nn, n, 4 * nn, 1.0, 0.0, mask, 0);
+        LAUNCH(texp_fix_kernel, warp_blocks(B), 128, st, B, n, k, 1, E, work, done, scal, c.fail);
+    }
+    for (int* p : {iter, done, scal, mask, flags}) c.mem->free(p);
 }
 
 struct Region {
@@ -917,7 +987,7 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                 // Schur samples: Tdd = Tuu = exp(-k0 d G), r' = E (r E) (rcwa1d_conical.hpp:871-874)
                 zc* E = c.dense();
                 zc* work = mem.get<zc>(4 * (size_t)nd);
-                LAUNCH(triangular_exp_kernel, warp_blocks(B), 128, st, B, n, m.G, k0, d, E, work, m.schur, c.fail);
+                batched_triangular_exp(c, n, m.G, k0, d, E, work, m.schur);
                 mem.free(work);
                 zc* y = gemm(c, r.p, nn, E, nullptr, 1.0, 0.0, nullptr, m.schur, 0);
                 gemm(c, E, nn, y, nullptr, 1.0, 0.0, rn, m.schur, 0);
