@@ -37,6 +37,7 @@ extern "C" {
 #define RCWA_ENOMEM (-3)       /* device allocation failed */
 #define RCWA_EUNSUPPORTED (-4) /* option value the engine does not implement */
 #define RCWA_ESCRATCH (-5)     /* problem larger than rcwa_gpu_eig_batch_static's fixed workspace */
+#define RCWA_ETIMEOUT (-6)     /* rcwa_gpu_server_wait: the request has not finished yet */
 
 /* per-sample status word */
 #define RCWA_SAMPLE_OK 0
@@ -324,6 +325,61 @@ int rcwa_gpu_solve_batch(rcwa_gpu_ctx* ctx, int n, int nrhs, int batch, const rc
 int rcwa_gpu_multiply_batch(rcwa_gpu_ctx* ctx, int m, int k, int n, int batch, const rcwa_complex* a,
                             const rcwa_complex* b, rcwa_complex* c);
 
+/* ---- Serving: a request loop over worker slots -------------------------------------------- */
+
+/* No reference counterpart: the reference serves one solve per call (rcwa_json.hpp:1287-1312,
+ * the CLI). The server keeps `slots` engine contexts, each with its own CUDA stream and host
+ * worker. Submitted requests (deep-copied, so the caller's buffers may be released at once) wait
+ * in queues bucketed by matrix order; a free slot takes the oldest request whose estimated device
+ * footprint fits what remains of hbm_budget, else the oldest smaller one (backfilling, bounded so
+ * the oldest is never passed over for longer than max_bypass_ms). Requests on different slots run
+ * concurrently on the device. Each request is one solve: 1-D (rcwa::solve), conical
+ * (rcwa::solve_conical) or 2-D (rcwa::solve2d). */
+#define RCWA_REQ_1D 0
+#define RCWA_REQ_CONICAL 1
+#define RCWA_REQ_2D 2
+
+typedef struct rcwa_server_config {
+    int device;
+    int slots;              /* concurrent requests on the device (worker slots); 0 = 32 */
+    size_t hbm_budget;      /* bytes the admitted requests may hold together; 0 = 80 % of free memory */
+    int max_bypass_ms;      /* how long backfilling may pass over the oldest request; 0 = 2000 */
+} rcwa_server_config;
+
+typedef struct rcwa_request {
+    int kind;                       /* RCWA_REQ_* */
+    const rcwa_stack1d* stack1d;    /* 1-D and conical */
+    const rcwa_stack2d* stack2d;    /* 2-D */
+    double wavelength;
+    double theta_deg;
+    double phi_deg;                 /* conical and 2-D */
+    int M;                          /* 1-D and conical truncation */
+    int polarization;               /* 1-D: RCWA_TE / RCWA_TM */
+    int M1, M2, factorization;      /* 2-D */
+    rcwa_complex Es, Ep;            /* 2-D Jones vector */
+    rcwa_options options;
+} rcwa_request;
+
+/* Timing of one request on the server's clock (seconds since the server was created). */
+typedef struct rcwa_response {
+    int code;           /* return code of the solve (RCWA_OK or an RCWA_E* code) */
+    int slot;           /* worker slot that ran it */
+    double submit_s;
+    double start_s;
+    double finish_s;
+    double footprint_bytes;  /* device footprint the admission charged */
+} rcwa_response;
+
+typedef struct rcwa_gpu_server rcwa_gpu_server;
+int rcwa_gpu_server_create(const rcwa_server_config* config, rcwa_gpu_server** server);
+void rcwa_gpu_server_destroy(rcwa_gpu_server* server);
+/* Validates the request's shape (the solve itself validates the physics) and queues it. */
+int rcwa_gpu_server_submit(rcwa_gpu_server* server, const rcwa_request* request, unsigned long long* ticket);
+/* Waits up to timeout_ms (< 0: forever) for the request, then copies its result into result (an
+ * rcwa_result1d*, rcwa_result_conical* or rcwa_result2d* of host arrays sized for one point, by
+ * kind; may be NULL) and releases it. Returns RCWA_OK, or RCWA_ETIMEOUT if it has not finished. */
+int rcwa_gpu_server_wait(rcwa_gpu_server* server, unsigned long long ticket, int timeout_ms, rcwa_response* response,
+                         void* result);
 #ifdef __cplusplus
 }
 #endif

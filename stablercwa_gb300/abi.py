@@ -300,3 +300,39 @@ def result2d_views(n_points, N, n_layers):
     for name, arr in arrays.items():
         setattr(res, name, arr.ctypes.data)
     return res, arrays
+
+
+# ---------------------------------------------------------------- serving
+
+RCWA_ETIMEOUT = -6
+RCWA_REQ_1D = 0
+RCWA_REQ_CONICAL = 1
+RCWA_REQ_2D = 2
+
+
+class rcwa_server_config(C.Structure):
+    _fields_ = [("device", C.c_int), ("slots", C.c_int), ("hbm_budget", C.c_size_t), ("max_bypass_ms", C.c_int)]
+
+
+class rcwa_request(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int),
+        ("stack1d", C.POINTER(rcwa_stack1d)),
+        ("stack2d", C.POINTER(rcwa_stack2d)),
+        ("wavelength", C.c_double),
+        ("theta_deg", C.c_double),
+        ("phi_deg", C.c_double),
+        ("M", C.c_int),
+        ("polarization", C.c_int),
+        ("M1", C.c_int),
+        ("M2", C.c_int),
+        ("factorization", C.c_int),
+        ("Es", rcwa_complex),
+        ("Ep", rcwa_complex),
+        ("options", rcwa_options),
+    ]
+
+
+class rcwa_response(C.Structure):
+    _fields_ = [("code", C.c_int), ("slot", C.c_int), ("submit_s", C.c_double), ("start_s", C.c_double),
+                ("finish_s", C.c_double), ("footprint_bytes", C.c_double)]

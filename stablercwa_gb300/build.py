@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libstablercwa_gb300.so")
-SOURCES = ["capi.cu", "rcwa1d.cu", "conical.cu", "rcwa2d.cu", "eig.cu", "eig_static.cu", "linalg.cu"]
+SOURCES = ["capi.cu", "rcwa1d.cu", "conical.cu", "rcwa2d.cu", "eig.cu", "eig_static.cu", "linalg.cu", "server.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-diag-suppress", "177"]
 
@@ -43,7 +43,7 @@ def build(force=False, verbose=False, extra=()):
     nvcc = _nvcc()
 
     def compile_one(src):
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         cmd = [nvcc, *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
@@ -55,7 +55,7 @@ def build(force=False, verbose=False, extra=()):
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs]
+    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

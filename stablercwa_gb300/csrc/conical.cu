@@ -811,7 +811,7 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
     const int base_solves = 2 * static_cast<int>(grating.size());
 
     const long long per_sample = 16LL * (nn * 16 + NN * 12 * (long long)grating.size() + (long long)n * 8 * (L + 2)) +
-                                 2 * eig_workspace_bytes(N, 1);
+                                 2 * eig_workspace_bytes(N, 1) * (long long)std::max<size_t>(1, grating.size());
     long long chunk = chunk_bytes > 0 ? (long long)chunk_bytes / std::max(1LL, per_sample) : n_points;
     chunk = std::max(1LL, std::min<long long>(chunk, n_points));
 
@@ -863,11 +863,15 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                 analytic(modes[k + 1], Ly.homogeneous ? Ly.n : Ly.n_values[0], 1);
             }
         if (!grating.empty()) {
-            zc* ws = mem.get<zc>((size_t)(eig_workspace_bytes(N, 2 * B) / sizeof(zc)) + 1);
-            int* info = mem.get<int>(2 * B);
-            for (int k : grating) {
-                // assemble A and B C into one batch of 2B matrices
-                zc* AB = mem.get<zc>(2 * ndN);
+            // A and B C of every grating layer, then one eigensolve launch over all of them
+            const int n_gr = (int)grating.size();
+            zc* ABall = mem.get<zc>(2 * ndN * n_gr);
+            zc* lamall = mem.get<zc>(2 * nvN * n_gr);
+            zc* vecall = mem.get<zc>(2 * ndN * n_gr);
+            int* infoall = mem.get<int>(2 * (size_t)B * n_gr);
+            for (int gi = 0; gi < n_gr; ++gi) {
+                const int k = grating[gi];
+                zc* AB = ABall + 2 * ndN * gi;
                 LAUNCH(assemble_te_kernel, nblocks(ndN), kTpb, st, B, M, ld[k].c_eps, kx, AB);
                 zc* Bm = mem.get<zc>(ndN);
                 LAUNCH(conical_b_kernel, nblocks(ndN), kTpb, st, B, N, ld[k].einv, kx, Bm);
@@ -875,9 +879,19 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                 mem.free(Bm);
                 LAUNCH(finite_check_kernel, nblocks(ndN), kTpb, st, B, NN, AB, c.fail);
                 LAUNCH(finite_check_kernel, nblocks(ndN), kTpb, st, B, NN, AB + ndN, c.fail);
-                zc* lam = mem.get<zc>(2 * nvN);
-                zc* vec = mem.get<zc>(2 * ndN);
-                launch_eig(st, N, 2 * B, AB, NN, lam, vec, info, nullptr, ws, opt.eps, opt.max_iter, opt.eig_group);
+            }
+            {
+                zc* ws = mem.get<zc>((size_t)(eig_workspace_bytes(N, 2 * B * n_gr) / sizeof(zc)) + 1);
+                launch_eig(st, N, 2 * B * n_gr, ABall, NN, lamall, vecall, infoall, nullptr, ws, opt.eps, opt.max_iter,
+                           opt.eig_group);
+                mem.free(ws);
+            }
+            for (int gi = 0; gi < n_gr; ++gi) {
+                const int k = grating[gi];
+                zc* AB = ABall + 2 * ndN * gi;
+                zc* lam = lamall + 2 * nvN * gi;
+                zc* vec = vecall + 2 * ndN * gi;
+                int* info = infoall + 2 * (size_t)B * gi;
                 LAUNCH(eig_info_pair_kernel, nblocks(B), kTpb, st, B, info, eig_info, c.fail);
                 Region& R = modes[k + 1];
                 R.analytic = false;
@@ -936,11 +950,8 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                     for (zc* ptr : {gg, Tm, Z, w2, Pm, Qm, RE, RV, t1}) mem.free(ptr);
                     mem.free(info2);
                 }
-                mem.free(lam);
-                mem.free(vec);
-                mem.free(AB);
             }
-            mem.free(ws);
+            for (void* p : {(void*)ABall, (void*)lamall, (void*)vecall, (void*)infoall}) mem.free(p);
         }
 
         // ---- 2. bottom-up recursion at order 2N

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <mutex>
 #include <stdexcept>
 #include <string>
@@ -88,7 +89,7 @@ long long eig_workspace_bytes(int n, int batch);
 int eig_default_group(int n, int batch);
 
 // Kernel launch accounting for the benchmark's gpu_launches claim.
-long long& launch_count();
+std::atomic<long long>& launch_count();  // engine launches of this process (all threads)
 
 // Optional CUDA-event timing of the heavy kernels (enabled per context; the context installs its
 // timer as the calling thread's current timer for the duration of a call).

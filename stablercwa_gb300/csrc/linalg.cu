@@ -7,8 +7,8 @@
 
 namespace rcwa_gb300 {
 
-long long& launch_count() {
-    static long long count = 0;
+std::atomic<long long>& launch_count() {
+    static std::atomic<long long> count{0};
     return count;
 }
 

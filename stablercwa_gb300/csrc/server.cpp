@@ -1,0 +1,474 @@
+// server.cpp -- the serving request loop declared in include/stablercwa_gb300.h.
+//
+// Worker slots, each a host thread with its own engine context (and so its own CUDA stream), take
+// requests from queues bucketed by matrix order. Admission charges each request its estimated
+// device footprint against the server's HBM budget: a free slot takes the oldest request if it
+// fits, otherwise the oldest request of another bucket that fits (backfilling), unless the oldest
+// request has already waited longer than max_bypass_ms, in which case the slot waits for memory to
+// be released. A request alone on the device is always admitted. Requests on different slots run
+// concurrently, so work arriving while others are on the device overlaps with them.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/stablercwa_gb300.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+// ------------------------------------------------------------------ owned copies of a request
+
+struct Owned1D {
+    std::vector<rcwa_layer1d> layers;
+    std::vector<std::vector<double>> edges;
+    std::vector<std::vector<rcwa_complex>> values;
+    rcwa_stack1d stack{};
+    int gratings = 0;
+
+    void copy(const rcwa_stack1d& s) {
+        stack = s;
+        const int L = std::max(0, s.n_layers);
+        layers.assign(s.layers, s.layers + L);
+        edges.resize(L);
+        values.resize(L);
+        for (int k = 0; k < L; ++k) {
+            const rcwa_layer1d& l = s.layers[k];
+            if (!l.homogeneous && l.n_segments > 0 && l.edges && l.n_values) {
+                edges[k].assign(l.edges, l.edges + l.n_segments + 1);
+                values[k].assign(l.n_values, l.n_values + l.n_segments);
+                ++gratings;
+            }
+        }
+        for (int k = 0; k < L; ++k) {
+            layers[k].edges = edges[k].empty() ? nullptr : edges[k].data();
+            layers[k].n_values = values[k].empty() ? nullptr : values[k].data();
+        }
+        stack.layers = layers.empty() ? nullptr : layers.data();
+    }
+};
+
+struct Owned2D {
+    std::vector<rcwa_layer2d> layers;
+    std::vector<std::vector<double>> y_edges;
+    std::vector<std::vector<rcwa_xprofile2d>> rows;
+    std::vector<std::vector<std::vector<double>>> x_edges;
+    std::vector<std::vector<std::vector<rcwa_complex>>> n_values;
+    rcwa_stack2d stack{};
+    int patterned = 0;
+
+    void copy(const rcwa_stack2d& s) {
+        stack = s;
+        const int L = std::max(0, s.n_layers);
+        layers.assign(s.layers, s.layers + L);
+        y_edges.resize(L);
+        rows.resize(L);
+        x_edges.resize(L);
+        n_values.resize(L);
+        for (int k = 0; k < L; ++k) {
+            const rcwa_layer2d& l = s.layers[k];
+            if (l.homogeneous || l.n_strips <= 0 || !l.y_edges || !l.x_profiles) continue;
+            ++patterned;
+            y_edges[k].assign(l.y_edges, l.y_edges + l.n_strips + 1);
+            rows[k].assign(l.x_profiles, l.x_profiles + l.n_strips);
+            x_edges[k].resize(l.n_strips);
+            n_values[k].resize(l.n_strips);
+            for (int r = 0; r < l.n_strips; ++r) {
+                const rcwa_xprofile2d& p = l.x_profiles[r];
+                if (p.n_segments > 0 && p.edges && p.n_values) {
+                    x_edges[k][r].assign(p.edges, p.edges + p.n_segments + 1);
+                    n_values[k][r].assign(p.n_values, p.n_values + p.n_segments);
+                }
+            }
+        }
+        for (int k = 0; k < L; ++k) {
+            for (size_t r = 0; r < rows[k].size(); ++r) {
+                rows[k][r].edges = x_edges[k][r].empty() ? nullptr : x_edges[k][r].data();
+                rows[k][r].n_values = n_values[k][r].empty() ? nullptr : n_values[k][r].data();
+            }
+            layers[k].y_edges = y_edges[k].empty() ? nullptr : y_edges[k].data();
+            layers[k].x_profiles = rows[k].empty() ? nullptr : rows[k].data();
+        }
+        stack.layers = layers.empty() ? nullptr : layers.data();
+    }
+};
+
+// ------------------------------------------------------------------ result storage per kind
+
+template <class T>
+void put(T* dst, const std::vector<T>& src) {
+    if (dst && !src.empty()) std::memcpy(dst, src.data(), src.size() * sizeof(T));
+}
+template <class T>
+void put1(T* dst, T v) {
+    if (dst) *dst = v;
+}
+
+struct Res1D {
+    std::vector<rcwa_complex> R, T;
+    std::vector<double> DEr, DEt;
+    int status = 0, eig_info = 0, n_eig = 0, n_dense = 0;
+    double resid = 0;
+    rcwa_result1d view(int n) {
+        R.resize(n);
+        T.resize(n);
+        DEr.resize(n);
+        DEt.resize(n);
+        return rcwa_result1d{R.data(), T.data(), DEr.data(), DEt.data(), &status, &eig_info, &n_eig, &n_dense, &resid};
+    }
+    void out(rcwa_result1d* o) const {
+        put(o->R, R);
+        put(o->T, T);
+        put(o->DEr, DEr);
+        put(o->DEt, DEt);
+        put1(o->status, status);
+        put1(o->eig_info, eig_info);
+        put1(o->n_eig, n_eig);
+        put1(o->n_dense_solve, n_dense);
+        put1(o->max_eig_residual, resid);
+    }
+};
+
+struct ResConical {
+    std::vector<rcwa_complex> Jr, Jt;
+    std::vector<double> DEr, DEt, kx, flux_r, flux_t;
+    int status = 0, eig_info = 0, n_eig = 0, n_dense = 0, n_schur = 0, warn = 0;
+    double min_abs = 0, ky = 0;
+    rcwa_result_conical view(int n) {
+        Jr.resize(4 * n);
+        Jt.resize(4 * n);
+        DEr.resize(4 * n);
+        DEt.resize(4 * n);
+        kx.resize(n);
+        flux_r.resize(n);
+        flux_t.resize(n);
+        return rcwa_result_conical{Jr.data(), Jt.data(), DEr.data(), DEt.data(), &status, &eig_info, &n_eig, &n_dense,
+                                   &n_schur, &min_abs, &warn, kx.data(), &ky, flux_r.data(), flux_t.data()};
+    }
+    void out(rcwa_result_conical* o) const {
+        put(o->Jr, Jr);
+        put(o->Jt, Jt);
+        put(o->DEr, DEr);
+        put(o->DEt, DEt);
+        put1(o->status, status);
+        put1(o->eig_info, eig_info);
+        put1(o->n_eig, n_eig);
+        put1(o->n_dense_solve, n_dense);
+        put1(o->n_schur, n_schur);
+        put1(o->min_abs_lambda, min_abs);
+        put1(o->degenerate_mode_warning, warn);
+        put(o->kx, kx);
+        put1(o->ky, ky);
+        put(o->flux_r, flux_r);
+        put(o->flux_t, flux_t);
+    }
+};
+
+struct Res2D {
+    std::vector<double> Kx, Ky, DEr, DEt;
+    std::vector<rcwa_complex> c[12];  // kzI, kzII, Ex_r, Ey_r, Ez_r, Ex_t, Ey_t, Ez_t, Rs, Rp, Ts, Tp
+    std::vector<unsigned char> prop_r, prop_t, regions;
+    int status = 0, eig_info = 0, n_eig = 0, n_dense = 0;
+    double resid = 0;
+    rcwa_result2d view(int N, int L) {
+        for (auto* v : {&Kx, &Ky, &DEr, &DEt}) v->resize(N);
+        for (auto& v : c) v.resize(N);
+        prop_r.resize(N);
+        prop_t.resize(N);
+        regions.resize(L + 2);
+        rcwa_result2d r{};
+        r.Kx = Kx.data();
+        r.Ky = Ky.data();
+        rcwa_complex** z[12] = {&r.kzI, &r.kzII, &r.Ex_r, &r.Ey_r, &r.Ez_r, &r.Ex_t, &r.Ey_t, &r.Ez_t, &r.Rs, &r.Rp, &r.Ts, &r.Tp};
+        for (int k = 0; k < 12; ++k) *z[k] = c[k].data();
+        r.DEr = DEr.data();
+        r.DEt = DEt.data();
+        r.prop_r = prop_r.data();
+        r.prop_t = prop_t.data();
+        r.status = &status;
+        r.eig_info = &eig_info;
+        r.n_eig = &n_eig;
+        r.n_dense_solve = &n_dense;
+        r.max_eig_residual = &resid;
+        r.rayleigh_regions = regions.data();
+        return r;
+    }
+    void out(rcwa_result2d* o) const {
+        put(o->Kx, Kx);
+        put(o->Ky, Ky);
+        rcwa_complex* z[12] = {o->kzI, o->kzII, o->Ex_r, o->Ey_r, o->Ez_r, o->Ex_t, o->Ey_t, o->Ez_t, o->Rs, o->Rp, o->Ts, o->Tp};
+        for (int k = 0; k < 12; ++k) put(z[k], c[k]);
+        put(o->DEr, DEr);
+        put(o->DEt, DEt);
+        put(o->prop_r, prop_r);
+        put(o->prop_t, prop_t);
+        put1(o->status, status);
+        put1(o->eig_info, eig_info);
+        put1(o->n_eig, n_eig);
+        put1(o->n_dense_solve, n_dense);
+        put1(o->max_eig_residual, resid);
+        put(o->rayleigh_regions, regions);
+    }
+};
+
+struct Job {
+    unsigned long long ticket = 0;
+    rcwa_request req{};
+    Owned1D s1;
+    Owned2D s2;
+    int order = 0;
+    int bucket = 0;
+    double footprint = 0;
+    Clock::time_point submitted;
+    double submit_s = 0, start_s = 0, finish_s = 0;
+    int slot = -1, code = RCWA_OK;
+    bool done = false;
+    Res1D r1;
+    ResConical rc;
+    Res2D r2;
+};
+
+// Device bytes one solve holds at its peak, from the engines' own working-set estimates: the
+// eigensolver workspace and the dense operators of the S-matrix recursion at the algebra order n.
+double footprint_of(const Job& j) {
+    const double z = 16.0;
+    switch (j.req.kind) {
+        case RCWA_REQ_1D: {
+            const double n = 2.0 * j.req.M + 1;
+            return z * n * n * (3.0 * (j.s1.stack.n_layers + 1) + 12.0) + (1 << 20);
+        }
+        case RCWA_REQ_CONICAL: {
+            const double N = 2.0 * j.req.M + 1, n = 2 * N;
+            return z * (n * n * 16.0 + N * N * 12.0 * j.s1.gratings + n * 8.0 * (j.s1.stack.n_layers + 2)) +
+                   2.0 * z * (3 * N * N + 4 * N + 8) * std::max(1, j.s1.gratings) + (1 << 20);
+        }
+        default: {
+            const double N = (2.0 * j.req.M1 + 1) * (2.0 * j.req.M2 + 1), n = 2 * N;
+            return z * n * n * (5.0 * j.s2.patterned + 3.0 * (j.s2.stack.n_layers + 1) + 8.0) + (1 << 20);
+        }
+    }
+}
+
+int order_of(const rcwa_request& r) {
+    if (r.kind == RCWA_REQ_1D) return 2 * r.M + 1;
+    if (r.kind == RCWA_REQ_CONICAL) return 2 * (2 * r.M + 1);
+    return 2 * (2 * r.M1 + 1) * (2 * r.M2 + 1);
+}
+
+int bucket_of(int order) {
+    int b = 0;
+    while ((1 << b) < order && b < 30) ++b;
+    return b;
+}
+
+}  // namespace
+
+struct rcwa_gpu_server {
+    int device = 0;
+    std::vector<rcwa_gpu_ctx*> ctxs;
+    std::vector<std::thread> workers;
+    std::mutex m;
+    std::condition_variable cv_work, cv_done;
+    std::map<int, std::deque<Job*>> buckets;
+    std::map<unsigned long long, std::unique_ptr<Job>> jobs;
+    double budget = 0, in_use = 0;
+    int running = 0;
+    std::chrono::milliseconds max_bypass{2000};
+    bool stop = false;
+    unsigned long long next_ticket = 1;
+    Clock::time_point t0 = Clock::now();
+
+    double now_s() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+
+    // under the lock: the next request a free slot may start, or null
+    Job* pick() {
+        Job* oldest = nullptr;
+        for (auto& kv : buckets)
+            if (!kv.second.empty() && (!oldest || kv.second.front()->ticket < oldest->ticket)) oldest = kv.second.front();
+        if (!oldest) return nullptr;
+        const double room = budget - in_use;
+        Job* chosen = nullptr;
+        if (running == 0 || oldest->footprint <= room) {
+            chosen = oldest;
+        } else if (Clock::now() - oldest->submitted < max_bypass) {
+            for (auto& kv : buckets) {
+                if (kv.second.empty()) continue;
+                Job* f = kv.second.front();
+                if (f->footprint <= room && (!chosen || f->ticket < chosen->ticket)) chosen = f;
+            }
+        }
+        if (chosen) buckets[chosen->bucket].pop_front();
+        return chosen;
+    }
+
+    void run(Job& j, rcwa_gpu_ctx* ctx) {
+        rcwa_options o = j.req.options;
+        if (j.req.kind == RCWA_REQ_1D) {
+            const rcwa_point1d p{j.req.wavelength, j.req.theta_deg};
+            rcwa_result1d v = j.r1.view(2 * j.req.M + 1);
+            j.code = rcwa_gpu_solve1d_batch(ctx, &j.s1.stack, &p, 1, j.req.M, j.req.polarization, &o, &v);
+        } else if (j.req.kind == RCWA_REQ_CONICAL) {
+            const rcwa_point_conical p{j.req.wavelength, j.req.theta_deg, j.req.phi_deg};
+            rcwa_result_conical v = j.rc.view(2 * j.req.M + 1);
+            j.code = rcwa_gpu_solve_conical_batch(ctx, &j.s1.stack, &p, 1, j.req.M, &o, &v);
+        } else {
+            const rcwa_point2d p{j.req.wavelength, j.req.theta_deg, j.req.phi_deg, j.req.Es, j.req.Ep};
+            rcwa_result2d v = j.r2.view((2 * j.req.M1 + 1) * (2 * j.req.M2 + 1), j.s2.stack.n_layers);
+            j.code = rcwa_gpu_solve2d_batch(ctx, &j.s2.stack, &p, 1, j.req.M1, j.req.M2, j.req.factorization, &o, &v);
+        }
+    }
+
+    void worker(int slot) {
+        cudaSetDevice(device);
+        for (;;) {
+            Job* j = nullptr;
+            {
+                std::unique_lock<std::mutex> lk(m);
+                cv_work.wait(lk, [&] { return stop || (j = pick()) != nullptr; });
+                if (!j) return;
+                in_use += j->footprint;
+                ++running;
+                j->slot = slot;
+                j->start_s = now_s();
+            }
+            run(*j, ctxs[slot]);
+            {
+                std::lock_guard<std::mutex> lk(m);
+                in_use -= j->footprint;
+                --running;
+                j->finish_s = now_s();
+                j->done = true;
+            }
+            cv_done.notify_all();
+            cv_work.notify_all();
+        }
+    }
+};
+
+extern "C" {
+
+int rcwa_gpu_server_create(const rcwa_server_config* config, rcwa_gpu_server** out) {
+    if (!out) return RCWA_EINVAL;
+    *out = nullptr;
+    const int slots = config && config->slots > 0 ? config->slots : 32;
+    if (slots > 1024) return RCWA_EINVAL;
+    std::unique_ptr<rcwa_gpu_server> s;
+    try {
+        s.reset(new rcwa_gpu_server());
+    } catch (const std::bad_alloc&) {
+        return RCWA_ENOMEM;
+    }
+    s->device = config ? config->device : 0;
+    if (config && config->max_bypass_ms > 0) s->max_bypass = std::chrono::milliseconds(config->max_bypass_ms);
+    for (int k = 0; k < slots; ++k) {
+        rcwa_gpu_config c{s->device, 0};
+        rcwa_gpu_ctx* ctx = nullptr;
+        const int rc = rcwa_gpu_create(&c, &ctx);
+        if (rc != RCWA_OK) {
+            for (rcwa_gpu_ctx* p : s->ctxs) rcwa_gpu_destroy(p);
+            return rc;
+        }
+        s->ctxs.push_back(ctx);
+    }
+    if (config && config->hbm_budget) {
+        s->budget = (double)config->hbm_budget;
+    } else {
+        size_t free_b = 0, total = 0;
+        cudaSetDevice(s->device);
+        s->budget = cudaMemGetInfo(&free_b, &total) == cudaSuccess ? 0.8 * (double)free_b : 8.0 * (1 << 30);
+    }
+    for (int k = 0; k < slots; ++k) s->workers.emplace_back(&rcwa_gpu_server::worker, s.get(), k);
+    *out = s.release();
+    return RCWA_OK;
+}
+
+void rcwa_gpu_server_destroy(rcwa_gpu_server* s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->m);
+        s->stop = true;
+        for (auto& kv : s->buckets) kv.second.clear();
+    }
+    s->cv_work.notify_all();
+    for (std::thread& t : s->workers) t.join();
+    for (rcwa_gpu_ctx* c : s->ctxs) rcwa_gpu_destroy(c);
+    delete s;
+}
+
+int rcwa_gpu_server_submit(rcwa_gpu_server* s, const rcwa_request* r, unsigned long long* ticket) {
+    if (!s || !r || !ticket) return RCWA_EINVAL;
+    if (r->kind == RCWA_REQ_2D ? !r->stack2d : (r->kind == RCWA_REQ_1D || r->kind == RCWA_REQ_CONICAL ? !r->stack1d : true))
+        return RCWA_EINVAL;
+    std::unique_ptr<Job> j;
+    try {
+        j.reset(new Job());
+        j->req = *r;
+        if (r->kind == RCWA_REQ_2D) {
+            if (r->stack2d->n_layers < 0 || (r->stack2d->n_layers > 0 && !r->stack2d->layers)) return RCWA_EINVAL;
+            j->s2.copy(*r->stack2d);
+            j->req.stack2d = &j->s2.stack;
+            j->req.stack1d = nullptr;
+            if (r->M1 < 0 || r->M2 < 0 || r->M1 > 64 || r->M2 > 64) return RCWA_EINVAL;
+        } else {
+            if (r->stack1d->n_layers < 0 || (r->stack1d->n_layers > 0 && !r->stack1d->layers)) return RCWA_EINVAL;
+            j->s1.copy(*r->stack1d);
+            j->req.stack1d = &j->s1.stack;
+            j->req.stack2d = nullptr;
+            if (r->M < 0 || r->M > 4096) return RCWA_EINVAL;
+        }
+    } catch (const std::bad_alloc&) {
+        return RCWA_ENOMEM;
+    }
+    j->order = order_of(j->req);
+    j->bucket = bucket_of(j->order);
+    j->footprint = footprint_of(*j);
+    {
+        std::lock_guard<std::mutex> lk(s->m);
+        j->ticket = s->next_ticket++;
+        j->submitted = Clock::now();
+        j->submit_s = s->now_s();
+        *ticket = j->ticket;
+        s->buckets[j->bucket].push_back(j.get());
+        s->jobs[j->ticket] = std::move(j);
+    }
+    s->cv_work.notify_one();
+    return RCWA_OK;
+}
+
+int rcwa_gpu_server_wait(rcwa_gpu_server* s, unsigned long long ticket, int timeout_ms, rcwa_response* resp, void* result) {
+    if (!s) return RCWA_EINVAL;
+    std::unique_ptr<Job> j;
+    {
+        std::unique_lock<std::mutex> lk(s->m);
+        auto it = s->jobs.find(ticket);
+        if (it == s->jobs.end()) return RCWA_EINVAL;
+        Job* p = it->second.get();
+        if (timeout_ms < 0) {
+            s->cv_done.wait(lk, [&] { return p->done; });
+        } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return p->done; })) {
+            return RCWA_ETIMEOUT;
+        }
+        j = std::move(it->second);
+        s->jobs.erase(it);
+    }
+    if (resp) *resp = rcwa_response{j->code, j->slot, j->submit_s, j->start_s, j->finish_s, j->footprint};
+    if (result) {
+        if (j->req.kind == RCWA_REQ_1D) j->r1.out(static_cast<rcwa_result1d*>(result));
+        else if (j->req.kind == RCWA_REQ_CONICAL) j->rc.out(static_cast<rcwa_result_conical*>(result));
+        else j->r2.out(static_cast<rcwa_result2d*>(result));
+    }
+    return RCWA_OK;
+}
+
+}  // extern "C"

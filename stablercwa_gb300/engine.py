@@ -68,6 +68,10 @@ def load_library(build_if_missing=True):
     L.rcwa_gpu_solve2d_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack2d), vp, ci, ci, ci, ci,
                                          C.POINTER(abi.rcwa_options), C.POINTER(abi.rcwa_result2d)]
     L.rcwa_gpu_layer_operators2d.argtypes = [vp, C.POINTER(abi.rcwa_layer2d), cd, cd, ci, ci, ci, vp, vp, vp, vp]
+    L.rcwa_gpu_server_create.argtypes = [C.POINTER(abi.rcwa_server_config), C.POINTER(vp)]
+    L.rcwa_gpu_server_destroy.argtypes = [vp]
+    L.rcwa_gpu_server_submit.argtypes = [vp, C.POINTER(abi.rcwa_request), C.POINTER(C.c_ulonglong)]
+    L.rcwa_gpu_server_wait.argtypes = [vp, C.c_ulonglong, ci, C.POINTER(abi.rcwa_response), vp]
     L.rcwa_gpu_eig_batch.argtypes = [vp, ci, ci, vp, cd, ci, vp, vp, vp, vp]
     L.rcwa_gpu_eig_batch_dev.argtypes = [vp, ci, ci, vp, cd, ci, vp, vp, vp, vp]
     L.rcwa_gpu_solve_batch.argtypes = [vp, ci, ci, ci, vp, vp, vp, vp]
@@ -307,3 +311,78 @@ def rayleigh_message(stack, r, M1, M2):
             kz = np.sqrt(nn * nn - r["Kx"] ** 2 - r["Ky"] ** 2)
             region(f"layer {j + 1}", kz)
     return "; ".join(parts)
+
+
+class Server:
+    """The serving request loop (rcwa_gpu_server_*): submit single solves of any kind, collect them
+    with wait(). Requests run concurrently on `slots` worker slots, admitted by device footprint."""
+
+    def __init__(self, device=0, slots=32, hbm_budget=0, max_bypass_ms=0):
+        self.L = load_library()
+        cfg = abi.rcwa_server_config(device, slots, hbm_budget, max_bypass_ms)
+        h = C.c_void_p()
+        rc = self.L.rcwa_gpu_server_create(C.byref(cfg), C.byref(h))
+        if rc != 0:
+            raise EngineError(rc, "rcwa_gpu_server_create failed")
+        self.h = h
+        self.meta = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.rcwa_gpu_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _submit(self, req, meta):
+        t = C.c_ulonglong()
+        rc = self.L.rcwa_gpu_server_submit(self.h, C.byref(req), C.byref(t))
+        if rc != 0:
+            raise ValueError(f"rcwa_gpu_server_submit: error {rc}")
+        self.meta[t.value] = meta
+        return t.value
+
+    def submit_1d(self, stack, wavelength, theta_deg, M, pol=0, options=None):
+        st, keep = abi.marshal_stack1d(stack)
+        req = abi.rcwa_request(kind=abi.RCWA_REQ_1D, stack1d=C.pointer(st), wavelength=wavelength, theta_deg=theta_deg,
+                               M=M, polarization=pol, options=_options(options))
+        return self._submit(req, ("1d", 2 * M + 1, 0))
+
+    def submit_conical(self, stack, wavelength, theta_deg, phi_deg, M, options=None):
+        st, keep = abi.marshal_stack1d(stack)
+        req = abi.rcwa_request(kind=abi.RCWA_REQ_CONICAL, stack1d=C.pointer(st), wavelength=wavelength,
+                               theta_deg=theta_deg, phi_deg=phi_deg, M=M, options=_options(options))
+        return self._submit(req, ("conical", 2 * M + 1, 0))
+
+    def submit_2d(self, stack, wavelength, theta_deg, phi_deg, M1, M2, jones, laurent=False, options=None):
+        st, keep = abi.marshal_stack2d(stack)
+        fact = abi.RCWA_FACTORIZATION_LAURENT if laurent else abi.RCWA_FACTORIZATION_LI
+        req = abi.rcwa_request(kind=abi.RCWA_REQ_2D, stack2d=C.pointer(st), wavelength=wavelength, theta_deg=theta_deg,
+                               phi_deg=phi_deg, M1=M1, M2=M2, factorization=fact, Es=abi.cplx(jones[0]),
+                               Ep=abi.cplx(jones[1]), options=_options(options))
+        return self._submit(req, ("2d", (2 * M1 + 1) * (2 * M2 + 1), len(stack.layers)))
+
+    def wait(self, ticket, timeout_ms=-1):
+        """(response dict, result arrays of the one point) or None on timeout."""
+        kind, n, L = self.meta[ticket]
+        if kind == "1d":
+            res, arrays = abi.result_views(1, (n - 1) // 2)
+        elif kind == "conical":
+            res, arrays = abi.conical_views(1, (n - 1) // 2)
+        else:
+            res, arrays = abi.result2d_views(1, n, L)
+        resp = abi.rcwa_response()
+        rc = self.L.rcwa_gpu_server_wait(self.h, ticket, timeout_ms, C.byref(resp), C.cast(C.byref(res), C.c_void_p))
+        if rc == abi.RCWA_ETIMEOUT:
+            return None
+        if rc != 0:
+            raise ValueError(f"rcwa_gpu_server_wait: error {rc}")
+        del self.meta[ticket]
+        r = {k: v[0] for k, v in arrays.items()}
+        info = {"code": resp.code, "slot": resp.slot, "submit_s": resp.submit_s, "start_s": resp.start_s,
+                "finish_s": resp.finish_s, "footprint_bytes": resp.footprint_bytes, "kind": kind}
+        return info, r

@@ -61,3 +61,12 @@ def test_create_without_device_reports_error():
     from stablercwa_gb300.engine import Engine
     with pytest.raises(EngineError):
         Engine()
+
+
+def test_server_create_without_device_reports_error():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from stablercwa_gb300.engine import Server
+    with pytest.raises(EngineError):
+        Server(slots=1)
