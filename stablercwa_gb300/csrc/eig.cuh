@@ -32,6 +32,69 @@ struct Rot {
 // Per-matrix workspace layout in units of zc.
 __host__ __device__ inline long long eig_workspace_elems(int n) { return 3LL * n * n + 4LL * n + 8; }
 
+// Synchronisation and reductions of the threads that own one matrix: a group of G <= 32 lanes inside
+// a warp (32/G matrices per warp, __syncwarp only), or a whole CTA of G = 64..256 threads for one
+// matrix when the batch is too small to fill the GPU with warp groups (CTA barriers and a shared-
+// memory reduction over the warps). Either way every member ends with the same reduced value.
+template <int G, bool Block = (G > 32)>
+struct Grp;
+
+template <int G>
+struct Grp<G, false> {
+    unsigned mask;
+    __device__ __forceinline__ Grp(double*, int*) : mask(group_mask<G>()) {}
+    __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+    __device__ __forceinline__ double sum(double v) const { return group_sum<G>(v, mask); }
+    __device__ __forceinline__ double max(double v) const { return group_max<G>(v, mask); }
+    // smallest member index whose ok is set, or -1
+    __device__ __forceinline__ int first(bool ok) const {
+        const unsigned bits = __ballot_sync(mask, ok);
+        const unsigned mine = G == 32 ? bits : (bits >> ((threadIdx.x & 31) & ~(G - 1))) & ((1u << G) - 1u);
+        return mine ? __ffs(mine) - 1 : -1;
+    }
+};
+
+template <int G>
+struct Grp<G, true> {
+    double* red;  // G / 32 doubles of shared memory
+    int* ired;    // G / 32 ints of shared memory
+    __device__ __forceinline__ Grp(double* r, int* ir) : red(r), ired(ir) {}
+    __device__ __forceinline__ void sync() const { __syncthreads(); }
+    __device__ __forceinline__ double sum(double v) const {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        __syncthreads();  // earlier readers of red are done
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+        __syncthreads();
+        double s = red[0];
+#pragma unroll
+        for (int w = 1; w < G / 32; ++w) s += red[w];
+        return s;
+    }
+    __device__ __forceinline__ double max(double v) const {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+        __syncthreads();
+        double s = red[0];
+#pragma unroll
+        for (int w = 1; w < G / 32; ++w) s = fmax(s, red[w]);
+        return s;
+    }
+    __device__ __forceinline__ int first(bool ok) const {
+        const unsigned bits = __ballot_sync(0xffffffffu, ok);
+        const int f = bits ? (int)(threadIdx.x & ~31u) + __ffs(bits) - 1 : G;
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) ired[threadIdx.x >> 5] = f;
+        __syncthreads();
+        int m = ired[0];
+#pragma unroll
+        for (int w = 1; w < G / 32; ++w) m = min(m, ired[w]);
+        return m < G ? m : -1;
+    }
+};
+
 template <int G>
 __device__ __forceinline__ int first_owned(int start, int g) {
     // smallest r >= start with r % G == g
@@ -82,9 +145,9 @@ __device__ __forceinline__ zc wilkinson_shift(zc a, zc b, double c, zc d) {
 template <int G>
 __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc* __restrict__ V,
                         int* __restrict__ info_out, int* __restrict__ sweeps_out, zc* __restrict__ ws, double eps,
-                        int max_iter, zc* __restrict__ T = nullptr) {
+                        int max_iter, zc* __restrict__ T = nullptr, double* red = nullptr, int* ired = nullptr) {
     const int g = threadIdx.x & (G - 1);
-    const unsigned mask = group_mask<G>();
+    const Grp<G> grp(red, ired);
     zc* __restrict__ H = ws;
     zc* __restrict__ Z = H + (long long)n * n;
     zc* __restrict__ X = Z + (long long)n * n;
@@ -93,7 +156,7 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
     double* __restrict__ rotd = reinterpret_cast<double*>(wk + n);  // 3n doubles (<= 2n zc)
 
     for (long long idx = g; idx < (long long)n * n; idx += G) H[idx] = A[idx];
-    __syncwarp(mask);
+    grp.sync();
 
     // ---------------- CORTH: Householder reduction to upper Hessenberg (eig_qr.hpp:231-272)
     // lane g owns rows r with r % G == g in every column.
@@ -102,10 +165,10 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
         const int r0 = first_owned<G>(m, g);
         double sc = 0.0;
         for (int i = r0; i < n; i += G) sc += abs1(x[i]);
-        sc = group_sum<G>(sc, mask);
+        sc = grp.sum(sc);
         if (sc == 0.0) {
             if (g == 0) ort[m] = zc{0.0, 0.0};
-            __syncwarp(mask);
+            grp.sync();
             continue;
         }
         double h = 0.0;
@@ -114,8 +177,8 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
             ort[i] = u;
             h += norm2(u);
         }
-        h = group_sum<G>(h, mask);
-        __syncwarp(mask);
+        h = grp.sum(h);
+        grp.sync();
         double gg = sqrt(h);
         zc om = ort[m];
         const double f = zabs(om);
@@ -126,12 +189,12 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
             gg /= f;
             om = om * (1.0 + gg);
         }
-        __syncwarp(mask);
+        grp.sync();
         if ((m % G) == g) {
             ort[m] = om;
             if (f == 0.0) x[m] = zc{sc, 0.0};
         }
-        __syncwarp(mask);
+        grp.sync();
         // left multiply P_m on columns n-1 .. m (rows >= m), accumulating wk = (P_m A)(:, m:) u
         for (int i = g; i < n; i += G) wk[i] = zc{0.0, 0.0};
         for (int j = n - 1; j >= m; --j) {
@@ -142,8 +205,8 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
                 dr += u.re * a.re + u.im * a.im;
                 di += u.re * a.im - u.im * a.re;
             }
-            dr = group_sum<G>(dr, mask);
-            di = group_sum<G>(di, mask);
+            dr = grp.sum(dr);
+            di = grp.sum(di);
             const zc t = zc{-dr / h, -di / h};
             for (int i = r0; i < n; i += G) aj[i] = zfma(t, ort[i], aj[i]);
             const zc uj = ort[j];
@@ -156,12 +219,12 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
             const zc cu = -conj(ort[j]);
             for (int i = g; i < n; i += G) aj[i] = zfma(cu, wk[i], aj[i]);
         }
-        __syncwarp(mask);
+        grp.sync();
         if ((m % G) == g) {
             ort[m] = om * sc;
             x[m] = x[m] * (-gg);
         }
-        __syncwarp(mask);
+        grp.sync();
     }
 
     // ---------------- accumulate the reflectors into Z (eig_qr.hpp:354-373)
@@ -169,10 +232,11 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
         const int c = (int)(idx / n), r = (int)(idx - (long long)c * n);
         Z[idx] = zc{r == c ? 1.0 : 0.0, 0.0};
     }
-    __syncwarp(mask);
+    grp.sync();
     for (int i = n - 2; i >= 1; --i) {
         const zc oi = ort[i];
         const zc hs = H[(long long)(i - 1) * n + i];
+        grp.sync();  // every member has read ort[i] before the owner of row i overwrites it below
         if (is_zero(oi) || is_zero(hs)) continue;
         const int e = bexp(abs1(oi));
         const zc sub = scale2(hs, -e);
@@ -188,18 +252,18 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
                 dr += u.re * a.re + u.im * a.im;
                 di += u.re * a.im - u.im * a.re;
             }
-            dr = group_sum<G>(dr, mask);
-            di = group_sum<G>(di, mask);
+            dr = grp.sum(dr);
+            di = grp.sum(di);
             const zc t = zc{dr / minus_h, di / minus_h};
             for (int k = r0; k < n; k += G) zj[k] = zfma(t, ort[k], zj[k]);
         }
     }
-    __syncwarp(mask);
+    grp.sync();
 
     // ---------------- clean Hessenberg form, real subdiagonal (eig_qr.hpp:420-439)
     for (int j = 0; j + 2 < n; ++j)
         for (int r = first_owned<G>(j + 2, g); r < n; r += G) H[(long long)j * n + r] = zc{0.0, 0.0};
-    __syncwarp(mask);
+    grp.sync();
     for (int i = 1; i < n; ++i) {
         const zc sub = H[(long long)(i - 1) * n + i];
         if (sub.im == 0.0) continue;
@@ -210,7 +274,7 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
             zc* p = H + (long long)j * n + i;
             *p = cy * *p;
         }
-        __syncwarp(mask);
+        grp.sync();
         if ((i % G) == g) H[(long long)(i - 1) * n + i] = zc{nrm, 0.0};
         const int last = min(i + 1, n - 1);
         for (int r = g; r <= last; r += G) {
@@ -221,7 +285,7 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
             zc* p = Z + (long long)i * n + r;
             *p = y * *p;
         }
-        __syncwarp(mask);
+        grp.sync();
     }
 
     // ---------------- shifted QR (eig_qr.hpp:1039-1096), full updates of H and Z
@@ -239,20 +303,19 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
                 const zc hd1 = H[(long long)cand * n + cand];
                 ok = abs1(hsub) <= eps * (abs1(hd0) + abs1(hd1));
             }
-            const unsigned bits = __ballot_sync(mask, ok);
-            const unsigned mine = G == 32 ? bits : (bits >> ((threadIdx.x & 31) & ~(G - 1))) & ((1u << G) - 1u);
-            if (mine) {
-                l = base - (__ffs(mine) - 1);
+            const int f = grp.first(ok);
+            if (f >= 0) {
+                l = base - f;
                 break;
             }
         }
         if (l == en) {
             const zc hd = H[(long long)en * n + en];
             const zc wv = hd + t;
-            __syncwarp(mask);
+            grp.sync();
             if ((en % G) == g) H[(long long)en * n + en] = wv;
             if (g == 0) W[en] = wv;
-            __syncwarp(mask);
+            grp.sync();
             --en;
             its = 0;
             continue;
@@ -268,7 +331,7 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
             s = wilkinson_shift(H[(long long)(en - 1) * n + en - 1], H[(long long)en * n + en - 1],
                                 H[(long long)(en - 1) * n + en].re, H[(long long)en * n + en]);
         }
-        __syncwarp(mask);
+        grp.sync();
         for (int r = g; r <= en; r += G) {
             zc* p = H + (long long)r * n + r;
             *p = *p - s;
@@ -276,14 +339,14 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
         t = t + s;
         ++its;
         ++sweeps;
-        __syncwarp(mask);
+        grp.sync();
 
         // (1) left multiply Q^H: rotation G_i from column i-1, applied to columns i..n-1 (rows i-1, i)
         for (int i = l + 1; i <= en; ++i) {
             zc* cprev = H + (long long)(i - 1) * n;
             zc top;
             const Rot q = make_rotation(cprev[i - 1], cprev[i].re, top);
-            __syncwarp(mask);
+            grp.sync();
             if (((i - 1) % G) == g) {
                 cprev[i - 1] = top;
                 cprev[i] = zc{0.0, 0.0};
@@ -299,7 +362,7 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
                 col[i - 1] = zc{q.cr * y.re + q.ci * y.im + q.s * z.re, q.cr * y.im - q.ci * y.re + q.s * z.im};
                 col[i] = zc{q.cr * z.re - q.ci * z.im - q.s * y.re, q.cr * z.im + q.ci * z.re - q.s * y.im};
             }
-            __syncwarp(mask);
+            grp.sync();
         }
         // (2) phase that makes r(en, en) real (eig_qr.hpp:588-596)
         const zc hee = H[(long long)en * n + en];
@@ -308,7 +371,7 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
         if (has_phase) {
             double nrm = 0.0;
             phase = unit_phase(hee, nrm);
-            __syncwarp(mask);
+            grp.sync();
             if ((en % G) == g) H[(long long)en * n + en] = zc{nrm, 0.0};
             const zc cp = conj(phase);
             for (int j = first_owned<G>(en + 1, g); j < n; j += G) {
@@ -316,7 +379,7 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
                 *p = cp * *p;
             }
         }
-        __syncwarp(mask);
+        grp.sync();
         // (3) right multiply by Q on H rows 0..en and on all rows of Z (eig_qr.hpp:598-606)
         for (int r = g; r <= en; r += G) {
             int j = max(l + 1, r);
@@ -340,7 +403,7 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
             }
             Z[(long long)en * n + r] = has_phase ? phase * a : a;
         }
-        __syncwarp(mask);
+        grp.sync();
     }
     if (g == 0) {
         *info_out = info;
@@ -365,11 +428,11 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
     double tn = 0.0;
     for (int j = 0; j < n; ++j)
         for (int i = g; i <= j; i += G) tn = fmax(tn, abs1(H[(long long)j * n + i]));
-    tn = group_max<G>(tn, mask);
+    tn = grp.max(tn);
     const double rel = fmax(eps, DBL_EPSILON);
     double tiny = rel * tn;
     if (tiny == 0.0) tiny = DBL_MIN;
-    __syncwarp(mask);
+    grp.sync();
     // the diagonal of H now holds the eigenvalues; read them from W (written above) for clarity
     const double kQuotientMax = 1e300;
     const double kShrink = 0x1p-512;
@@ -401,7 +464,7 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
             for (int k = 0; k < i; ++k) x[k] = zfma(xs, ti[k], x[k]);
         }
     }
-    __syncwarp(mask);
+    grp.sync();
     // V = Z X (X upper triangular), then each column scaled to unit 2-norm
     for (int j = 0; j < n; ++j) {
         const zc* xj = X + (long long)j * n;
@@ -413,20 +476,20 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
             vj[r] = acc;
             big = fmax(big, fmax(fabs(acc.re), fabs(acc.im)));
         }
-        big = group_max<G>(big, mask);
+        big = grp.max(big);
         if (big == 0.0 || !isfinite(big)) continue;
         double ssq = 0.0;
         for (int r = g; r < n; r += G) {
             const zc u = zdivr(vj[r], big);
             ssq += norm2(u);
         }
-        ssq = group_sum<G>(ssq, mask);
+        ssq = grp.sum(ssq);
         const double inv = 1.0 / sqrt(ssq);
         for (int r = g; r < n; r += G) vj[r] = zdivr(vj[r], big) * inv;
     }
 }
 
-// One group of G lanes per matrix; matrices at a_stride / w_stride / v_stride elements apart.
+// One group of G <= 32 lanes per matrix; matrices at a_stride / w_stride / v_stride elements apart.
 template <int G>
 __global__ void __launch_bounds__(128) eig_batch_kernel(int n, int batch, const zc* __restrict__ a, long long a_stride,
                                                         zc* __restrict__ w, zc* __restrict__ v, int* __restrict__ info,
@@ -438,6 +501,24 @@ __global__ void __launch_bounds__(128) eig_batch_kernel(int n, int batch, const 
     if (skip && skip[gid] == skip_value) return;
     eig_one<G>(n, a + gid * a_stride, w + gid * n, v + gid * (long long)n * n, info + gid, sweeps ? sweeps + gid : nullptr,
                ws + gid * eig_workspace_elems(n), eps, max_iter, t_out ? t_out + gid * (long long)n * n : nullptr);
+}
+
+// One CTA of G = 64..256 threads per matrix (grid = batch), for batches too small to fill the GPU
+// with warp groups.
+template <int G>
+__global__ void __launch_bounds__(G) eig_block_kernel(int n, int batch, const zc* __restrict__ a, long long a_stride,
+                                                      zc* __restrict__ w, zc* __restrict__ v, int* __restrict__ info,
+                                                      int* __restrict__ sweeps, zc* __restrict__ ws, double eps,
+                                                      int max_iter, const int* __restrict__ skip, int skip_value,
+                                                      zc* __restrict__ t_out) {
+    static_assert(G > 32 && G % 32 == 0, "block groups are whole warps");
+    __shared__ double red[G / 32];
+    __shared__ int ired[G / 32];
+    const long long gid = blockIdx.x;
+    if (gid >= batch) return;
+    if (skip && skip[gid] == skip_value) return;
+    eig_one<G>(n, a + gid * a_stride, w + gid * n, v + gid * (long long)n * n, info + gid, sweeps ? sweeps + gid : nullptr,
+               ws + gid * eig_workspace_elems(n), eps, max_iter, t_out ? t_out + gid * (long long)n * n : nullptr, red, ired);
 }
 
 }  // namespace rcwa_gb300

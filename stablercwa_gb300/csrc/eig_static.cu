@@ -10,7 +10,7 @@
 // allocates nothing.
 //
 // Set-up is once per device: the first call made with a device current looks up the array's
-// address with cudaGetSymbolAddress and loads the four kernel variants. Make that first call before
+// address with cudaGetSymbolAddress and loads the kernel variants. Make that first call before
 // any stream capture begins on the device. Every call uses the same array, so calls that overlap in
 // time on one device (issued on different streams, or from several host threads without ordering)
 // race on it; calls on one stream are ordered and safe.
@@ -37,7 +37,8 @@ zc* g_scratch[kMaxDevices] = {};
 template <int G>
 cudaError_t load_kernel() {
     cudaFuncAttributes attr;
-    return cudaFuncGetAttributes(&attr, rcwa_gb300::eig_batch_kernel<G>);
+    if constexpr (G > 32) return cudaFuncGetAttributes(&attr, rcwa_gb300::eig_block_kernel<G>);
+    else return cudaFuncGetAttributes(&attr, rcwa_gb300::eig_batch_kernel<G>);
 }
 
 // Address of this device's copy of the array; looked up on the device's first call.
@@ -50,7 +51,7 @@ int scratch_for_current_device(zc** out) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, eig_static_scratch) != cudaSuccess || !p) return RCWA_ECUDA;
         if (load_kernel<4>() != cudaSuccess || load_kernel<8>() != cudaSuccess || load_kernel<16>() != cudaSuccess ||
-            load_kernel<32>() != cudaSuccess)
+            load_kernel<32>() != cudaSuccess || load_kernel<128>() != cudaSuccess || load_kernel<256>() != cudaSuccess)
             return RCWA_ECUDA;
         g_scratch[dev] = static_cast<zc*>(p);
     }
@@ -86,6 +87,8 @@ extern "C" int rcwa_gpu_eig_batch_static(void* stream, int n, int batch, const r
         case 4: eig_batch_kernel<4><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, d_info, d_sweeps, ws, eps, max_iter, nullptr, 1, nullptr); break;
         case 8: eig_batch_kernel<8><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, d_info, d_sweeps, ws, eps, max_iter, nullptr, 1, nullptr); break;
         case 16: eig_batch_kernel<16><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, d_info, d_sweeps, ws, eps, max_iter, nullptr, 1, nullptr); break;
+        case 128: eig_block_kernel<128><<<(unsigned)batch, 128, 0, st>>>(n, batch, a, a_stride, w, v, d_info, d_sweeps, ws, eps, max_iter, nullptr, 1, nullptr); break;
+        case 256: eig_block_kernel<256><<<(unsigned)batch, 256, 0, st>>>(n, batch, a, a_stride, w, v, d_info, d_sweeps, ws, eps, max_iter, nullptr, 1, nullptr); break;
         default: eig_batch_kernel<32><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, d_info, d_sweeps, ws, eps, max_iter, nullptr, 1, nullptr); break;
     }
     ++launch_count();

@@ -37,7 +37,7 @@ def match_values(got, ref):
     return worst
 
 
-@pytest.mark.parametrize("group", ["4", "8", "16", "32"])
+@pytest.mark.parametrize("group", ["4", "8", "16", "32", "64", "128", "256"])
 def test_eig_golden(eng, eig_cases, group, monkeypatch):
     monkeypatch.setenv("RCWA_GB300_EIG_GROUP", group)
     for case in eig_cases:
