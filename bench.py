@@ -474,6 +474,113 @@ def run_secondary(args):
     return 0
 
 
+# ------------------------------------------------------------------------------------- serving
+
+def serve_requests(seed, count):
+    """The serving mix: 70 % 1-D (M 20..150, 1..30 layers, each a grating with p 0.3 and at least one,
+    K 2..5 random edges, n 1.0..2.5 + i 0..0.05, films likewise, period 0.5..1.5, lambda 0.4..1.6,
+    theta 0..70, TE/TM), 20 % conical (M 20..60, built like config 3), 10 % 2-D (Mx = My 5..12,
+    built like config 4). Returns (kind, stack, args) tuples."""
+    from stablercwa_gb300 import Layer, Stack
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        u = rng.uniform()
+        if u < 0.7:
+            period = rng.uniform(0.5, 1.5)
+            L = int(rng.integers(1, 31))
+            is_grating = rng.uniform(size=L) < 0.3
+            if not is_grating.any():
+                is_grating[int(rng.integers(0, L))] = True
+            layers = []
+            for g in is_grating:
+                d = rng.uniform(0.05, 0.3)
+                if g:
+                    K = int(rng.integers(2, 6))
+                    inner = np.sort(rng.uniform(0.0, period, K - 1))
+                    vals = [complex(rng.uniform(1.0, 2.5), rng.uniform(0.0, 0.05)) for _ in range(K)]
+                    layers.append(Layer.grating(d, [0.0, *inner, period], vals))
+                else:
+                    layers.append(Layer.uniform(d, complex(rng.uniform(1.0, 2.5), rng.uniform(0.0, 0.05))))
+            stack = Stack(nI=1.0, nII=1.46, period=period, layers=layers)
+            out.append(("1d", stack, dict(wavelength=rng.uniform(0.4, 1.6), theta=rng.uniform(0.0, 70.0),
+                                          M=int(rng.integers(20, 151)), pol=int(rng.integers(0, 2)))))
+        elif u < 0.9:
+            stack, _ = workload_c3(int(rng.integers(0, 1 << 30)))
+            out.append(("conical", stack, dict(wavelength=rng.uniform(0.5, 1.6), theta=rng.uniform(0.0, 60.0),
+                                               phi=rng.uniform(0.0, 90.0), M=int(rng.integers(20, 61)))))
+        else:
+            stack, pts, _ = workload_c4(int(rng.integers(0, 1 << 30)))
+            Mx = int(rng.integers(5, 13))
+            out.append(("2d", stack, dict(wavelength=rng.uniform(0.4, 1.2), M1=Mx, M2=Mx, jones=(pts[0][3], pts[0][4]))))
+    return out
+
+
+def serve_submit(srv, req):
+    kind, stack, a = req
+    if kind == "1d":
+        return srv.submit_1d(stack, a["wavelength"], a["theta"], a["M"], a["pol"])
+    if kind == "conical":
+        return srv.submit_conical(stack, a["wavelength"], a["theta"], a["phi"], a["M"])
+    return srv.submit_2d(stack, a["wavelength"], 0.0, 0.0, a["M1"], a["M2"], a["jones"])
+
+
+def serve_run(reqs, slots, rate=None, seed=0):
+    """Submit reqs (all at once, or with Poisson arrivals at `rate` per second) to a server with
+    `slots` worker slots; returns (makespan s, latencies s, per-kind latencies, statuses)."""
+    from stablercwa_gb300.engine import Server
+    srv = Server(slots=slots)
+    rng = np.random.default_rng(seed)
+    arrivals = np.zeros(len(reqs)) if rate is None else np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
+    t0 = time.perf_counter()
+    tickets = []
+    for req, at in zip(reqs, arrivals):
+        delay = at - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        tickets.append(serve_submit(srv, req))
+    done = [srv.wait(t) for t in tickets]
+    srv.close()
+    first = min(i["submit_s"] for i, _ in done)
+    makespan = max(i["finish_s"] for i, _ in done) - first
+    lat = np.array([i["finish_s"] - i["submit_s"] for i, _ in done])
+    kinds = {}
+    for (kind, _, _), l in zip(reqs, lat):
+        kinds.setdefault(kind, []).append(l)
+    ok = all(i["code"] == 0 and int(r["status"]) == 0 for i, r in done)
+    return makespan, lat, kinds, ok
+
+
+def run_serve(args):
+    reqs = serve_requests(SEED + 5, args.serve_requests)
+    stats = {}
+
+    def summary(lat):
+        return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                "mean_s": float(np.mean(lat))}
+    makespan, lat, kinds, ok = serve_run(reqs, args.serve_slots)
+    capacity = len(reqs) / makespan
+    stats["saturated"] = {"solves_per_s": capacity, "makespan_s": makespan, **summary(lat), "all_ok": ok,
+                          "by_kind": {k: {**summary(np.array(v)), "count": len(v)} for k, v in kinds.items()}}
+    for frac in args.serve_rates:
+        mk, lat, kinds, ok = serve_run(reqs, args.serve_slots, rate=frac * capacity, seed=SEED + 6)
+        stats[f"poisson_{frac:g}x"] = {"offered_per_s": frac * capacity, "solves_per_s": len(reqs) / mk, **summary(lat),
+                                        "all_ok": ok,
+                                        "by_kind": {k: {**summary(np.array(v)), "count": len(v)} for k, v in kinds.items()}}
+    mk, lat, kinds, ok = serve_run(reqs, 1)
+    stats["plain_one_slot"] = {"solves_per_s": len(reqs) / mk, "makespan_s": mk, **summary(lat), "all_ok": ok,
+                               "by_kind": {k: {**summary(np.array(v)), "count": len(v)} for k, v in kinds.items()}}
+    head = stats.get("poisson_1x", stats["saturated"])
+    line = {"metric": "served solves/s and p50/p99 latency, mixed 1-D / conical / 2-D requests (70/20/10)",
+            "value": head["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+            "dtype": "f64 (complex128)", "data": "synthetic (seeded)",
+            "config": {"workload": "serving mix", "requests": len(reqs), "slots": args.serve_slots, "seed": SEED + 5},
+            "p50_s": head["p50_s"], "p99_s": head["p99_s"],
+            "vs_plain": head["solves_per_s"] / stats["plain_one_slot"]["solves_per_s"], "runs": stats}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_eig_only(n, batch, group):
     """Profiling case for the eigensolver alone: `batch` lossy layer matrices of order n in the
     benchmark's form (Toeplitz of a binary grating, index 1.46+0.01i, fill 0.4, plus Kx^2 with
@@ -516,7 +623,10 @@ def main():
     ap.add_argument("--eig-group", type=int, default=0)
     ap.add_argument("--cpu-points", type=int, default=128)
     ap.add_argument("--ref-points", type=int, default=128)
-    ap.add_argument("--workload", choices=["c2", "c3", "c4", "plain"], default="c2",
+    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-slots", type=int, default=48)
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[0.5, 1.0])
+    ap.add_argument("--workload", choices=["c2", "c3", "c4", "plain", "serve"], default="c2",
                     help="c2 (default, the headline line), c3 conical, c4 2-D, plain one-point-per-call")
     ap.add_argument("--eig-only", nargs=2, type=int, metavar=("N", "BATCH"), default=None,
                     help="profiling case: the eigensolver alone on BATCH layer matrices of order N")
@@ -525,6 +635,8 @@ def main():
         return run_eig_only(args.eig_only[0], args.eig_only[1], args.eig_group)
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "serve":
+        return run_serve(args)
     if args.workload != "c2":
         return run_secondary(args)
     return run_ours(args)
