@@ -140,7 +140,7 @@ __global__ void conical_lambda_kernel(int B, int N, const zc* __restrict__ lam, 
         const double scale = fabs(k) * sqrt(fabs(k));
         const int s = (k != 0.0 && loc_all < kDegenerateWarn * scale) ? 1 : 0;
         schur[b] = s;
-        if (s) atomicOr(any_schur, 1);
+        if (s) atomicAdd(any_schur, 1);  // the number of Schur samples
     }
 }
 
@@ -935,7 +935,9 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                     zc* Z = c.dense();
                     zc* Tm = c.dense();
                     int* info2 = mem.zeros<int>(B);
-                    launch_eig(st, n, B, H, nn, w2, Z, info2, nullptr, ws2, 2.220446049250313e-16, 100, opt.eig_group,
+                    // few flagged samples: size the lanes per matrix by their number, not by the chunk
+                    const int schur_group = opt.eig_group ? opt.eig_group : eig_default_group(n, any);
+                    launch_eig(st, n, B, H, nn, w2, Z, info2, nullptr, ws2, 2.220446049250313e-16, 100, schur_group,
                                R.schur, 0, Tm);
                     mem.free(ws2);
                     LAUNCH(schur_info_kernel, nblocks(B), kTpb, st, B, info2, R.schur, eig_info, c.fail);
