@@ -59,7 +59,8 @@ typedef struct rcwa_complex {
 
 /* One layer (include/stablercwa/rcwa1d.hpp:80-106). homogeneous != 0: a uniform film of index n.
  * Otherwise a grating: n_segments indices n_values[K] and K+1 strictly increasing edges spanning one
- * period. fourier_method 0 = analytic coefficients (the reference default). */
+ * period. fourier_method 0 = analytic coefficients (the reference default), 1 = FFT-sampled with
+ * fft_samples samples (0: automatic; rcwa::FourierMethod, include/stablercwa/fourier.hpp:15-43). */
 typedef struct rcwa_layer1d {
     double d;
     int homogeneous;
@@ -257,6 +258,15 @@ int rcwa_gpu_synchronize(rcwa_gpu_ctx* ctx);
  * rcwa::solve_conical (:985-988). Host buffers in and out. */
 int rcwa_gpu_solve_conical_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point_conical* points,
                                  int n_points, int M, const rcwa_options* options, rcwa_result_conical* out);
+
+/* Fourier coefficients c[h + hmax], h = -hmax..hmax, of a piecewise-constant profile (K values, K + 1
+ * increasing edges spanning one period). method 0: the closed form (rcwa::detail::fourier_coefficients,
+ * include/stablercwa/rcwa1d.hpp:366-388), on the host; method 1: the FFT of `samples` cell-midpoint
+ * samples with the origin and half-cell phase correction (rcwa::fourier_coefficients_fft,
+ * include/stablercwa/fourier.hpp:49-83), evaluated on the device. Layers select the same two forms
+ * through rcwa_layer1d.fourier_method / fft_samples (0 samples: automatic, as resolve_fft_samples). */
+int rcwa_gpu_fourier_coefficients(rcwa_gpu_ctx* ctx, const double* edges, const rcwa_complex* values, int K,
+                                  double period, int hmax, int method, int samples, rcwa_complex* out);
 
 /* Batched 2-D solve over points on one stack: replaces rcwa::solve2d
  * (include/stablercwa/rcwa2d.hpp:1359-1413) called once per point, with Options2D::factorization

@@ -38,6 +38,8 @@ Stack1D to_stack(const rcwa_stack1d* s) {
         l.d = L.d;
         l.homogeneous = L.homogeneous != 0;
         l.n = C(L.n);
+        if (!l.homogeneous && L.fourier_method != 0)
+            throw InvalidArgument{"oracle: FFT-sampled coefficients are not restated here (the tests use the reference's outputs)"};
         if (!l.homogeneous) {
             for (int j = 0; j <= L.n_segments; ++j) l.edges.push_back(L.edges[j]);
             for (int j = 0; j < L.n_segments; ++j) l.n_values.push_back(C(L.n_values[j]));
@@ -64,6 +66,9 @@ int oracle_solve1d_batch(const rcwa_stack1d* stack, const rcwa_point1d* points, 
     Stack1D s;
     try {
         s = to_stack(stack);
+    } catch (const InvalidArgument& e) {
+        put_error(err, err_len, e.what.c_str());
+        return -1;
     } catch (...) {
         put_error(err, err_len, "oracle: bad stack");
         return -1;
@@ -113,7 +118,13 @@ int oracle_solve1d_batch(const rcwa_stack1d* stack, const rcwa_point1d* points, 
 // Batched conical solve on the CPU: rcwa::sweep_conical (include/stablercwa/rcwa1d_conical.hpp:992-999).
 int oracle_solve_conical_batch(const rcwa_stack1d* stack, const rcwa_point_conical* points, int n_points, int M,
                                rcwa_result_conical* out, int n_threads, char* err, size_t err_len) {
-    const Stack1D s = to_stack(stack);
+    Stack1D s;
+    try {
+        s = to_stack(stack);
+    } catch (const InvalidArgument& e) {
+        put_error(err, err_len, e.what.c_str());
+        return -1;
+    }
     const int n = 2 * M + 1;
     std::atomic<int> next{0};
     std::atomic<int> failed{0};
@@ -219,7 +230,12 @@ int oracle_layer_matrix(const rcwa_layer1d* layer, double period, double wavelen
     st.period = period;
     st.n_layers = 1;
     st.layers = layer;
-    const Stack1D s = to_stack(&st);
+    Stack1D s;
+    try {
+        s = to_stack(&st);
+    } catch (const InvalidArgument&) {
+        return -1;
+    }
     const CVec kx = r1::transverse_wavevectors(nI, theta_deg, wavelength, period, M);
     r1::Work w;
     try {

@@ -107,8 +107,8 @@ def marshal_stack1d(stack):
         s.d = float(L.d)
         s.homogeneous = 1 if L.homogeneous else 0
         s.n = cplx(L.n if L.homogeneous else 1.0)
-        s.fourier_method = 0
-        s.fft_samples = 0
+        s.fourier_method = int(getattr(L, "fourier_method", 0))
+        s.fft_samples = int(getattr(L, "fft_samples", 0))
         if not L.homogeneous:
             e = np.ascontiguousarray(np.asarray(L.edges, dtype=np.float64))
             v = np.ascontiguousarray(np.asarray(L.n_values, dtype=np.complex128))

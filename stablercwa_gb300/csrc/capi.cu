@@ -251,6 +251,11 @@ int rcwa_gpu_solve1d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const r
     });
 }
 
+int rcwa_gpu_fourier_coefficients(rcwa_gpu_ctx* ctx, const double* edges, const rcwa_complex* values, int K,
+                                  double period, int hmax, int method, int samples, rcwa_complex* out) {
+    return guarded(ctx, [&] { fourier_coefficients_api(ctx->stream, edges, values, K, period, hmax, method, samples, out); });
+}
+
 int rcwa_gpu_solve2d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points,
                            int M1, int M2, int factorization, const rcwa_options* options, rcwa_result2d* out) {
     return guarded(ctx, [&] {

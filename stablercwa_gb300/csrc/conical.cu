@@ -793,12 +793,10 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
             eps.push_back(nv * nv);
             inv.push_back(1.0 / (nv * nv));
         }
-        const auto ce = fourier_coefficients(edges, eps, stack.period, 2 * M);
-        const auto ci = fourier_coefficients(edges, inv, stack.period, 2 * M);
-        ld[k].c_eps = persist.get<zc>(ce.size());
-        zc* c_inv = persist.get<zc>(ci.size());
-        RCWA_CUDA(cudaMemcpyAsync(ld[k].c_eps, ce.data(), ce.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
-        RCWA_CUDA(cudaMemcpyAsync(c_inv, ci.data(), ci.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
+        ld[k].c_eps = layer_coefficients(st, persist, edges, eps, stack.period, M, Ly.fourier_method, Ly.fft_samples,
+                                         layer_fail);
+        zc* c_inv = layer_coefficients(st, persist, edges, inv, stack.period, M, Ly.fourier_method, Ly.fft_samples,
+                                       layer_fail);
         zc* E = persist.get<zc>(NN);
         zc* Ci = persist.get<zc>(NN);
         LAUNCH(toeplitz_kernel, nblocks(NN), kTpb, st, M, ld[k].c_eps, E);

@@ -152,6 +152,10 @@ void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d
 void layer_operators2d(cudaStream_t st, const rcwa_layer2d& layer, double Lx, double Ly, int M1, int M2,
                        int factorization, rcwa_complex* eps, rcwa_complex* cx, rcwa_complex* cy, int* singular);
 
+// Coefficients of one piecewise-constant profile, closed form (method 0) or FFT-sampled (method 1).
+void fourier_coefficients_api(cudaStream_t st, const double* edges, const rcwa_complex* values, int K, double period,
+                              int hmax, int method, int samples, rcwa_complex* out);
+
 // Validation of a 1-D problem exactly where the reference throws std::invalid_argument.
 void validate1d(const rcwa_stack1d& stack, const rcwa_point1d* h_points, int n_points, int M, int pol);
 

@@ -176,8 +176,10 @@ void validate1d(const rcwa_stack1d& stack, const rcwa_point1d* h_points, int n_p
         throw EngineError{RCWA_EINVAL, "rcwa: layer array missing"};
     for (int k = 0; k < stack.n_layers; ++k) {
         const rcwa_layer1d& L = stack.layers[k];
-        if (L.fourier_method != 0)
-            throw EngineError{RCWA_EUNSUPPORTED, "rcwa: only analytic Fourier coefficients are implemented"};
+        if (L.fourier_method != 0 && L.fourier_method != 1) throw EngineError{RCWA_EINVAL, "rcwa: invalid Fourier method"};
+        if (L.fft_samples < 0 || L.fft_samples > kMaxFFTSamples)
+            throw EngineError{RCWA_EINVAL, "rcwa: fft_samples must be 0..4194304 (0 for automatic)"};
+        if (!L.homogeneous && L.fourier_method == 1 && M >= 0) (void)resolve_fft_samples(M, L.fft_samples);
         if (!std::isfinite(L.d) || L.d < 0.0) throw EngineError{RCWA_EINVAL, "rcwa: layer thickness must be finite and >= 0"};
         if (L.homogeneous) {
             check_index(L.n);
@@ -229,13 +231,11 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
             eps.push_back(nv * nv);
             inv.push_back(1.0 / (nv * nv));
         }
-        const std::vector<cd> ce = fourier_coefficients(edges, eps, stack.period, 2 * M);
-        ld[k].c_eps = persist.get<zc>(ce.size());
-        RCWA_CUDA(cudaMemcpyAsync(ld[k].c_eps, ce.data(), ce.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
+        ld[k].c_eps = layer_coefficients(st, persist, edges, eps, stack.period, M, Ly.fourier_method, Ly.fft_samples,
+                                         layer_fail);
         if (pol == RCWA_TM) {
-            const std::vector<cd> ci = fourier_coefficients(edges, inv, stack.period, 2 * M);
-            zc* c_inv = persist.get<zc>(ci.size());
-            RCWA_CUDA(cudaMemcpyAsync(c_inv, ci.data(), ci.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
+            zc* c_inv = layer_coefficients(st, persist, edges, inv, stack.period, M, Ly.fourier_method, Ly.fft_samples,
+                                           layer_fail);
             zc* E = persist.get<zc>(nn);
             ld[k].inv_eps = persist.get<zc>(nn);
             LAUNCH(toeplitz_kernel, nblocks(nn), kTpb, st, M, ld[k].c_eps, E);
@@ -525,6 +525,40 @@ bool prepare_points_device(cudaStream_t st, const rcwa_point1d* d_points, int n_
     RCWA_CUDA(cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
     RCWA_CUDA(cudaStreamSynchronize(st));
     return h == 0;
+}
+
+// One profile's coefficients for the C entry point rcwa_gpu_fourier_coefficients, validated like
+// rcwa::fourier_coefficients_fft (include/stablercwa/fourier.hpp:49-63).
+void fourier_coefficients_api(cudaStream_t st, const double* edges, const rcwa_complex* values, int K, double period,
+                              int hmax, int method, int samples, rcwa_complex* out) {
+    if (method != 0 && method != 1) throw EngineError{RCWA_EINVAL, "rcwa: invalid Fourier method"};
+    if (method == 1 && (samples < 0 || samples > kMaxFFTSamples))
+        throw EngineError{RCWA_EINVAL, "rcwa: fft_samples must be 0..4194304 (0 for automatic)"};
+    if (hmax < 0 || (method == 1 && samples <= 2LL * hmax))
+        throw EngineError{RCWA_EINVAL, "rcwa: FFT sample count must exceed 2*hmax"};
+    if (!std::isfinite(period) || period <= 0 || K < 1 || !edges || !values || !out)
+        throw EngineError{RCWA_EINVAL, "rcwa: FFT needs a positive period, K values and K+1 edges"};
+    for (int j = 0; j <= K; ++j)
+        if (!std::isfinite(edges[j]) || (j && edges[j] <= edges[j - 1]))
+            throw EngineError{RCWA_EINVAL, "rcwa: FFT edges must be finite and strictly increasing"};
+    if (std::abs((edges[K] - edges[0]) - period) > 1e-10 * period)
+        throw EngineError{RCWA_EINVAL, "rcwa: FFT edges must span exactly one period"};
+    std::vector<double> e(edges, edges + K + 1);
+    std::vector<cd> v(K);
+    for (int j = 0; j < K; ++j) {
+        if (!std::isfinite(values[j].re) || !std::isfinite(values[j].im))
+            throw EngineError{RCWA_EINVAL, "rcwa: FFT material values must be finite"};
+        v[j] = cd{values[j].re, values[j].im};
+    }
+    if (method == 0) {
+        const std::vector<cd> c = fourier_coefficients(e, v, period, hmax);
+        std::memcpy(out, c.data(), c.size() * sizeof(cd));
+        return;
+    }
+    DeviceScratch mem(st);
+    zc* d = fft_coefficients_dev(st, mem, e, v, period, hmax, samples);
+    RCWA_CUDA(cudaMemcpyAsync(out, d, (2 * (size_t)hmax + 1) * sizeof(zc), cudaMemcpyDeviceToHost, st));
+    RCWA_CUDA(cudaStreamSynchronize(st));
 }
 
 }  // namespace rcwa_gb300

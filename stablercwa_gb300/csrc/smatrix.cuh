@@ -7,6 +7,8 @@
 // right-hand sides (the conical s and p inputs) are B x n x cols, column-major per sample.
 #pragma once
 
+#include <algorithm>
+#include <cmath>
 #include <complex>
 #include <vector>
 
@@ -328,6 +330,129 @@ std::vector<cd> fourier_coefficients(const std::vector<double>& edges, const std
         c[h + hmax] = sum;
     }
     return c;
+}
+
+// ---------------------------------------------------------------- FFT-sampled coefficients
+
+// The reference's FFT alternative (include/stablercwa/fourier.hpp:26-83): the profile is sampled at
+// S cell midpoints u_j = (j + 1/2) P / S, forward-transformed with 1/S scaling, and bin h is phase-
+// corrected by exp(-2 pi i h (origin/P + 1/(2S))). The samples of one segment form a run of equal
+// values, and the transform of a run of m samples starting at sample a is the Dirichlet kernel
+//     sum_j exp(-2 pi i h j / S) = exp(-i pi h (2a + m - 1) / S) sin(pi h m / S) / sin(pi h / S),
+// so the device evaluates exactly the sampled DFT the reference's FFT computes, in O(K H) instead
+// of touching all S samples. Angles are reduced in integer arithmetic before sinpi/cospi.
+constexpr int kMaxFFTSamples = 4194304;
+
+// Sample count for truncation M (resolve_fft_samples, fourier.hpp:26-43); throws like the reference.
+inline int resolve_fft_samples(int M, int samples) {
+    if (samples < 0 || samples > kMaxFFTSamples)
+        throw EngineError{RCWA_EINVAL, "rcwa: fft_samples must be 0..4194304 (0 for automatic)"};
+    if (M < 0) throw EngineError{RCWA_EINVAL, "rcwa: FFT truncation order M must be nonnegative"};
+    if (M > (kMaxFFTSamples - 1) / 4) throw EngineError{RCWA_EINVAL, "rcwa: FFT truncation requires more than 4194304 samples"};
+    if (samples == 0) {
+        const long long target = std::max(8192LL, 64LL * (2LL * M + 1));
+        if (target > kMaxFFTSamples) throw EngineError{RCWA_EINVAL, "rcwa: automatic FFT exceeds 4194304 samples"};
+        samples = 1;
+        while (samples < target) samples *= 2;
+    }
+    if (samples <= 4 * M) throw EngineError{RCWA_EINVAL, "rcwa: fft_samples must be at least 4*M+1"};
+    return samples;
+}
+
+// first sample of each segment (K + 1 entries, the last = S): sample j belongs to the last segment
+// s with u_j >= edges[s] - edges[0], with u_j evaluated as the reference evaluates it
+inline std::vector<long long> fft_runs(const std::vector<double>& edges, int S, double period) {
+    const int K = (int)edges.size() - 1;
+    std::vector<long long> start(K + 1, 0);
+    const auto u = [&](long long j) { return (static_cast<double>(j) + 0.5) / S * period; };
+    for (int s = 1; s < K; ++s) {
+        const double t = edges[s] - edges.front();
+        long long j = (long long)std::ceil(t / period * S - 0.5);
+        j = std::min<long long>(std::max<long long>(j, 0), S);
+        while (j > 0 && u(j - 1) >= t) --j;
+        while (j < S && u(j) < t) ++j;
+        start[s] = std::max(j, start[s - 1]);
+    }
+    start[K] = S;
+    return start;
+}
+
+__global__ void fft_coeff_kernel(int hmax, int K, long long S, const long long* __restrict__ start,
+                                 const zc* __restrict__ vals, const zc* __restrict__ phase, zc* __restrict__ c) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > 2 * hmax) return;
+    const long long h = t - hmax;
+    const long long two_s = 2 * S;
+    zc acc{0.0, 0.0};
+    for (int s = 0; s < K; ++s) {
+        const long long a = start[s], m = start[s + 1] - a;
+        if (m <= 0) continue;
+        zc d;
+        if (h == 0) {
+            d = zc{(double)m, 0.0};
+        } else {
+            long long r1 = (h * (2 * a + m - 1)) % two_s;
+            if (r1 < 0) r1 += two_s;
+            long long r2 = (h * m) % two_s;
+            if (r2 < 0) r2 += two_s;
+            double sp, cp;
+            sincospi((double)r1 / (double)S, &sp, &cp);
+            const double ratio = sinpi((double)r2 / (double)S) / sinpi((double)h / (double)S);
+            d = zc{cp * ratio, -sp * ratio};
+        }
+        acc = acc + vals[s] * d;
+    }
+    const double inv = 1.0 / (double)S;
+    c[t] = zc{acc.re * inv, acc.im * inv} * phase[t];
+}
+
+// FFT-sampled coefficients c[h + hmax] (h = -hmax..hmax) with S samples into device memory
+inline zc* fft_coefficients_dev(cudaStream_t st, DeviceScratch& mem, const std::vector<double>& edges,
+                                const std::vector<cd>& values, double period, int hmax, int S) {
+    const int H = 2 * hmax + 1;
+    zc* d = mem.get<zc>(H);
+    const std::vector<long long> start = fft_runs(edges, S, period);
+    double origin = std::fmod(edges.front(), period);
+    if (origin < 0) origin += period;
+    const double offset = origin / period + 0.5 / S;
+    std::vector<cd> phase(H);
+    for (int h = -hmax; h <= hmax; ++h) {
+        const double arg = -2.0 * kPiD * h * offset;
+        phase[h + hmax] = cd{std::cos(arg), std::sin(arg)};
+    }
+    long long* d_start = mem.get<long long>(start.size());
+    zc* d_vals = mem.get<zc>(values.size());
+    zc* d_phase = mem.get<zc>(H);
+    RCWA_CUDA(cudaMemcpyAsync(d_start, start.data(), start.size() * sizeof(long long), cudaMemcpyHostToDevice, st));
+    RCWA_CUDA(cudaMemcpyAsync(d_vals, values.data(), values.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
+    RCWA_CUDA(cudaMemcpyAsync(d_phase, phase.data(), H * sizeof(zc), cudaMemcpyHostToDevice, st));
+    LAUNCH(fft_coeff_kernel, nblocks(H), kTpb, st, hmax, (int)values.size(), (long long)S, d_start, d_vals, d_phase, d);
+    RCWA_CUDA(cudaStreamSynchronize(st));  // the host staging vectors end with this function
+    mem.free(d_start);
+    mem.free(d_vals);
+    mem.free(d_phase);
+    return d;
+}
+
+// Coefficients c[h + 2M] (h = -2M..2M) of a grating layer's segment values on the device: the closed
+// form (fourier_method 0, rcwa1d.hpp:366-388) or the FFT-sampled form (fourier_method 1). A non-finite
+// value with the FFT method is the reference's numerical failure (rcwa1d.hpp:392-397): *fail is set.
+inline zc* layer_coefficients(cudaStream_t st, DeviceScratch& mem, const std::vector<double>& edges,
+                              const std::vector<cd>& values, double period, int M, int method, int samples, int* fail) {
+    if (method != 1) {
+        zc* d = mem.get<zc>(4 * M + 1);
+        const std::vector<cd> c = fourier_coefficients(edges, values, period, 2 * M);
+        RCWA_CUDA(cudaMemcpyAsync(d, c.data(), c.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
+        return d;
+    }
+    for (const cd& v : values)
+        if (!std::isfinite(v.real()) || !std::isfinite(v.imag())) {
+            zc* d = mem.zeros<zc>(4 * M + 1);
+            static const int one = 1;
+            RCWA_CUDA(cudaMemcpyAsync(fail, &one, sizeof(int), cudaMemcpyHostToDevice, st));
+            return d;
+        }
+    return fft_coefficients_dev(st, mem, edges, values, period, 2 * M, resolve_fft_samples(M, samples));
 }
 
 __global__ void toeplitz_kernel(int M, const zc* __restrict__ c, zc* __restrict__ m) {

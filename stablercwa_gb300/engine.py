@@ -72,6 +72,7 @@ def load_library(build_if_missing=True):
     L.rcwa_gpu_server_destroy.argtypes = [vp]
     L.rcwa_gpu_server_submit.argtypes = [vp, C.POINTER(abi.rcwa_request), C.POINTER(C.c_ulonglong)]
     L.rcwa_gpu_server_wait.argtypes = [vp, C.c_ulonglong, ci, C.POINTER(abi.rcwa_response), vp]
+    L.rcwa_gpu_fourier_coefficients.argtypes = [vp, vp, vp, ci, cd, ci, ci, ci, vp]
     L.rcwa_gpu_eig_batch.argtypes = [vp, ci, ci, vp, cd, ci, vp, vp, vp, vp]
     L.rcwa_gpu_eig_batch_dev.argtypes = [vp, ci, ci, vp, cd, ci, vp, vp, vp, vp]
     L.rcwa_gpu_solve_batch.argtypes = [vp, ci, ci, ci, vp, vp, vp, vp]
@@ -246,6 +247,16 @@ class Engine:
                                                       mats[0].ctypes.data, mats[1].ctypes.data, mats[2].ctypes.data,
                                                       C.byref(sing)))
         return mats[0].T.copy(), mats[1].T.copy(), mats[2].T.copy(), bool(sing.value)
+
+    def fourier_coefficients(self, edges, values, period, hmax, method=0, samples=0):
+        """c[h + hmax], h = -hmax..hmax: closed form (method 0, rcwa::detail::fourier_coefficients) or
+        FFT-sampled with `samples` samples (method 1, rcwa::fourier_coefficients_fft)."""
+        e = np.ascontiguousarray(np.asarray(edges, dtype=np.float64))
+        v = np.ascontiguousarray(np.asarray(values, dtype=np.complex128))
+        out = np.empty(2 * hmax + 1, np.complex128)
+        self._check(self.L.rcwa_gpu_fourier_coefficients(self.h, e.ctypes.data, v.ctypes.data, len(v), float(period), hmax,
+                                                         method, samples, out.ctypes.data))
+        return out
 
     # ---------------------------------------------------------------- dense kernels (custom_* hooks)
 

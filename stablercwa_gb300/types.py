@@ -18,15 +18,18 @@ class Layer:
     edges: List[float] = field(default_factory=list)
     n_values: List[complex] = field(default_factory=list)
     homogeneous: bool = True
+    fourier_method: int = 0      # 0 analytic, 1 FFT-sampled (include/stablercwa/fourier.hpp:15)
+    fft_samples: int = 0         # 0: automatic
 
     @staticmethod
     def uniform(thickness, index):
         return Layer(d=float(thickness), n=complex(index), homogeneous=True)
 
     @staticmethod
-    def grating(thickness, boundaries, indices):
+    def grating(thickness, boundaries, indices, fourier_method=0, fft_samples=0):
         return Layer(d=float(thickness), edges=[float(e) for e in boundaries],
-                     n_values=[complex(v) for v in indices], homogeneous=False)
+                     n_values=[complex(v) for v in indices], homogeneous=False, fourier_method=int(fourier_method),
+                     fft_samples=int(fft_samples))
 
 
 @dataclass
@@ -77,7 +80,8 @@ def stack_from_json(d):
         if "n" in L:
             layers.append(Layer.uniform(L["d"], c(L["n"])))
         else:
-            layers.append(Layer.grating(L["d"], L["edges"], [c(v) for v in L["n_values"]]))
+            layers.append(Layer.grating(L["d"], L["edges"], [c(v) for v in L["n_values"]], L.get("fourier_method", 0),
+                                        L.get("fft_samples", 0)))
     return Stack(nI=c(d["nI"]), layers=layers, nII=c(d["nII"]), period=d["period"])
 
 

@@ -23,6 +23,7 @@ EXPORTERS = [
     ("export_eig.cpp", "eig_cases.jsonl"),
     ("export_conical.cpp", "conical_cases.jsonl"),
     ("export_rcwa2d.cpp", "rcwa2d_cases.jsonl.gz"),
+    ("export_fft.cpp", "fft_cases.jsonl"),
 ]
 
 
