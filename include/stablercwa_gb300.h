@@ -48,6 +48,7 @@ extern "C" {
 
 #define RCWA_TE 0
 #define RCWA_TM 1
+#define RCWA_TE_TM 2  /* rcwa_gpu_solve1d_batch_dev only: both polarizations, TE results then TM */
 
 /* 2-D factorization rule (include/stablercwa/rcwa2d_types.hpp:30) */
 #define RCWA_FACTORIZATION_LI 0
@@ -247,7 +248,10 @@ int rcwa_gpu_solve1d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const r
 
 /* Same solve with device-resident sweep points and device-resident result arrays (every pointer in
  * out is a device pointer). The stack description is host memory. Asynchronous with respect to the
- * host on the context's stream; rcwa_gpu_synchronize waits for it. */
+ * host on the context's stream; rcwa_gpu_synchronize waits for it. polarization = RCWA_TE_TM solves
+ * both polarizations of the points in one call (two sweeps of the reference): every result array
+ * then holds 2 n_points entries per point slot, the TE sweep first and the TM sweep after it, and the
+ * two sweeps run concurrently on the device (the context's stream and a second one it owns). */
 int rcwa_gpu_solve1d_batch_dev(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point1d* d_points,
                                int n_points, int M, int polarization, const rcwa_options* options,
                                rcwa_result1d* d_out);
@@ -294,6 +298,9 @@ void* rcwa_gpu_stream(rcwa_gpu_ctx* ctx);
  * count of one kind (after the work has finished) and resets it. */
 int rcwa_gpu_set_kernel_timing(rcwa_gpu_ctx* ctx, int enable);
 int rcwa_gpu_kernel_time(rcwa_gpu_ctx* ctx, const char* kind, double* milliseconds, long long* launches);
+/* Busy time of one kind since the last query: the length of the union of its launch intervals, which
+ * is less than the summed durations when launches of both polarizations overlap. */
+int rcwa_gpu_kernel_busy(rcwa_gpu_ctx* ctx, const char* kind, double* milliseconds);
 
 /* Batched general complex eigensolver, CORTH + COMQR2 (include/stablercwa/eig_qr.hpp:1008-1124):
  * the engine behind Options::custom_eig (include/stablercwa/rcwa1d.hpp:122-124). a holds batch

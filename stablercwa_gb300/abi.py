@@ -20,6 +20,7 @@ RCWA_SAMPLE_EIG_NOCONV = 2
 
 RCWA_TE = 0
 RCWA_TM = 1
+RCWA_TE_TM = 2
 
 
 class rcwa_complex(C.Structure):

@@ -8,8 +8,10 @@
 #include <complex>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "engine.h"
@@ -22,6 +24,8 @@ struct rcwa_gpu_ctx {
     size_t workspace_limit = 0;
     bool timing = false;
     rcwa_gb300::KernelTimer timer;
+    cudaStream_t stream2 = nullptr;  // second stream of the both-polarization call, created on first use
+    cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 namespace {
@@ -95,6 +99,56 @@ size_t chunk_bytes2d(const rcwa_gpu_ctx* ctx) {
     return (size_t)(0.8 * (double)(free_b + cached));
 }
 
+// Both polarizations of the same points: TE on the context's stream, TM on a second stream driven from
+// a second host thread. The two sweeps share nothing but the prepared points, so their kernels
+// overlap on the device. Results: TE block first, then the TM block, in every array of d_out.
+void solve_both(rcwa_gpu_ctx* ctx, const rcwa_stack1d& stack, const double* ds, const double* dw, int n_points, int M,
+                const Options& opt, const rcwa_result1d& d_out) {
+    const cudaStream_t st = ctx->stream;
+    if (!ctx->stream2) {
+        RCWA_CUDA(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
+        RCWA_CUDA(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
+        RCWA_CUDA(cudaEventCreateWithFlags(&ctx->join, cudaEventDisableTiming));
+    }
+    RCWA_CUDA(cudaEventRecord(ctx->fork, st));
+    RCWA_CUDA(cudaStreamWaitEvent(ctx->stream2, ctx->fork, 0));
+    const int n = 2 * M + 1;
+    const size_t pn = (size_t)n_points * n;
+    rcwa_result1d te = d_out, tm = d_out;
+    tm.R = d_out.R + pn;
+    tm.T = d_out.T + pn;
+    tm.DEr = d_out.DEr + pn;
+    tm.DEt = d_out.DEt + pn;
+    tm.status = d_out.status ? d_out.status + n_points : nullptr;
+    tm.eig_info = d_out.eig_info ? d_out.eig_info + n_points : nullptr;
+    tm.n_eig = d_out.n_eig ? d_out.n_eig + n_points : nullptr;
+    tm.n_dense_solve = d_out.n_dense_solve ? d_out.n_dense_solve + n_points : nullptr;
+    tm.max_eig_residual = d_out.max_eig_residual ? d_out.max_eig_residual + n_points : nullptr;
+    const size_t cb = chunk_bytes(ctx) / 2;
+    std::exception_ptr tm_error;
+    std::thread worker([&] {
+        try {
+            RCWA_CUDA(cudaSetDevice(ctx->device));
+            current_timer() = ctx->timing ? &ctx->timer : nullptr;
+            solve1d_device(ctx->stream2, stack, ds, dw, n_points, M, RCWA_TM, opt, tm, cb);
+        } catch (...) {
+            tm_error = std::current_exception();
+        }
+        current_timer() = nullptr;
+    });
+    std::exception_ptr te_error;
+    try {
+        solve1d_device(st, stack, ds, dw, n_points, M, RCWA_TE, opt, te, cb);
+    } catch (...) {
+        te_error = std::current_exception();
+    }
+    worker.join();
+    RCWA_CUDA(cudaEventRecord(ctx->join, ctx->stream2));
+    RCWA_CUDA(cudaStreamWaitEvent(st, ctx->join, 0));
+    if (te_error) std::rethrow_exception(te_error);
+    if (tm_error) std::rethrow_exception(tm_error);
+}
+
 void check_result_ptrs(const rcwa_result1d* out) {
     if (!out || !out->R || !out->T || !out->DEr || !out->DEt)
         throw EngineError{RCWA_EINVAL, "rcwa: result arrays R, T, DEr, DEt are required"};
@@ -163,6 +217,12 @@ void rcwa_gpu_destroy(rcwa_gpu_ctx* ctx) {
         cudaSetDevice(ctx->device);
         cudaStreamSynchronize(ctx->stream);
         cudaStreamDestroy(ctx->stream);
+        if (ctx->stream2) {
+            cudaStreamSynchronize(ctx->stream2);
+            cudaStreamDestroy(ctx->stream2);
+        }
+        if (ctx->fork) cudaEventDestroy(ctx->fork);
+        if (ctx->join) cudaEventDestroy(ctx->join);
     }
     delete ctx;
 }
@@ -181,6 +241,24 @@ int rcwa_gpu_set_kernel_timing(rcwa_gpu_ctx* ctx, int enable) {
     return guarded(ctx, [&] {
         ctx->timer.collect();
         ctx->timing = enable != 0;
+        if (ctx->timing) {
+            if (!ctx->timer.base) RCWA_CUDA(cudaEventCreate(&ctx->timer.base));
+            RCWA_CUDA(cudaEventRecord(ctx->timer.base, ctx->stream));
+            RCWA_CUDA(cudaEventSynchronize(ctx->timer.base));
+            for (auto& v : ctx->timer.spans) v.clear();
+        }
+    });
+}
+
+int rcwa_gpu_kernel_busy(rcwa_gpu_ctx* ctx, const char* kind, double* milliseconds) {
+    return guarded(ctx, [&] {
+        if (!kind || !milliseconds) throw EngineError{RCWA_EINVAL, "kernel_busy: null argument"};
+        int k = -1;
+        if (!std::strcmp(kind, "eig")) k = TK_EIG;
+        if (!std::strcmp(kind, "lu")) k = TK_LU;
+        if (!std::strcmp(kind, "gemm")) k = TK_GEMM;
+        if (k < 0) throw EngineError{RCWA_EINVAL, "kernel_busy: kind must be eig, lu or gemm"};
+        *milliseconds = ctx->timer.busy_ms(k);
     });
 }
 
@@ -209,11 +287,14 @@ int rcwa_gpu_solve1d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const r
     return guarded(ctx, [&] {
         if (!stack || (n_points > 0 && !points) || n_points < 0) throw EngineError{RCWA_EINVAL, "rcwa: null argument"};
         check_result_ptrs(out);
-        validate1d(*stack, points, n_points, M, polarization);
+        const bool both = polarization == RCWA_TE_TM;
+        validate1d(*stack, points, n_points, M, both ? RCWA_TE : polarization);
+        if (both) validate1d(*stack, points, n_points, M, RCWA_TM);
         const Options opt = to_options(options);
         if (n_points == 0) return;
         const cudaStream_t st = ctx->stream;
         const int n = 2 * M + 1;
+        const int sweeps = both ? 2 : 1;
         // s = nI sin(theta) with the host libm, the reference's own expression (rcwa1d.hpp:411)
         std::vector<double> hs(n_points), hw(n_points);
         const double kPi = 3.141592653589793238462643383279502884;
@@ -226,27 +307,28 @@ int rcwa_gpu_solve1d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const r
         double* dw = mem.get<double>(n_points);
         RCWA_CUDA(cudaMemcpyAsync(ds, hs.data(), n_points * sizeof(double), cudaMemcpyHostToDevice, st));
         RCWA_CUDA(cudaMemcpyAsync(dw, hw.data(), n_points * sizeof(double), cudaMemcpyHostToDevice, st));
-        const size_t nv = (size_t)n_points * n;
+        const size_t nv = (size_t)n_points * n * sweeps, np = (size_t)n_points * sweeps;
         rcwa_result1d d{};
         d.R = reinterpret_cast<rcwa_complex*>(mem.get<zc>(nv));
         d.T = reinterpret_cast<rcwa_complex*>(mem.get<zc>(nv));
         d.DEr = mem.get<double>(nv);
         d.DEt = mem.get<double>(nv);
-        d.status = mem.get<int>(n_points);
-        d.eig_info = mem.get<int>(n_points);
-        d.n_eig = mem.get<int>(n_points);
-        d.n_dense_solve = mem.get<int>(n_points);
-        d.max_eig_residual = opt.diagnostics ? mem.zeros<double>(n_points) : nullptr;
-        solve1d_device(st, *stack, ds, dw, n_points, M, polarization, opt, d, chunk_bytes(ctx));
+        d.status = mem.get<int>(np);
+        d.eig_info = mem.get<int>(np);
+        d.n_eig = mem.get<int>(np);
+        d.n_dense_solve = mem.get<int>(np);
+        d.max_eig_residual = opt.diagnostics ? mem.zeros<double>(np) : nullptr;
+        if (both) solve_both(ctx, *stack, ds, dw, n_points, M, opt, d);
+        else solve1d_device(st, *stack, ds, dw, n_points, M, polarization, opt, d, chunk_bytes(ctx));
         copy_back(out->R, d.R, nv, st);
         copy_back(out->T, d.T, nv, st);
         copy_back(out->DEr, d.DEr, nv, st);
         copy_back(out->DEt, d.DEt, nv, st);
-        copy_back(out->status, d.status, n_points, st);
-        copy_back(out->eig_info, d.eig_info, n_points, st);
-        copy_back(out->n_eig, d.n_eig, n_points, st);
-        copy_back(out->n_dense_solve, d.n_dense_solve, n_points, st);
-        if (opt.diagnostics) copy_back(out->max_eig_residual, d.max_eig_residual, n_points, st);
+        copy_back(out->status, d.status, np, st);
+        copy_back(out->eig_info, d.eig_info, np, st);
+        copy_back(out->n_eig, d.n_eig, np, st);
+        copy_back(out->n_dense_solve, d.n_dense_solve, np, st);
+        if (opt.diagnostics) copy_back(out->max_eig_residual, d.max_eig_residual, np, st);
         RCWA_CUDA(cudaStreamSynchronize(st));
     });
 }
@@ -352,7 +434,9 @@ int rcwa_gpu_solve1d_batch_dev(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, con
     return guarded(ctx, [&] {
         if (!stack || (n_points > 0 && !d_points) || n_points < 0) throw EngineError{RCWA_EINVAL, "rcwa: null argument"};
         check_result_ptrs(d_out);
-        validate1d(*stack, nullptr, 0, M, polarization);
+        const bool both = polarization == RCWA_TE_TM;
+        validate1d(*stack, nullptr, 0, M, both ? RCWA_TE : polarization);
+        if (both) validate1d(*stack, nullptr, 0, M, RCWA_TM);
         const Options opt = to_options(options);
         if (n_points == 0) return;
         const cudaStream_t st = ctx->stream;
@@ -361,7 +445,11 @@ int rcwa_gpu_solve1d_batch_dev(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, con
         double* dw = mem.get<double>(n_points);
         if (!prepare_points_device(st, d_points, n_points, stack->nI.re, ds, dw))
             throw EngineError{RCWA_EINVAL, "rcwa: every point needs a finite positive wavelength and |theta| < 90 degrees"};
-        solve1d_device(st, *stack, ds, dw, n_points, M, polarization, opt, *d_out, chunk_bytes(ctx));
+        if (!both) {
+            solve1d_device(st, *stack, ds, dw, n_points, M, polarization, opt, *d_out, chunk_bytes(ctx));
+            return;
+        }
+        solve_both(ctx, *stack, ds, dw, n_points, M, opt, *d_out);
     });
 }
 

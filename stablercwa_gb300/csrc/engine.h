@@ -99,10 +99,15 @@ struct KernelTimer {
         int kind;
         cudaEvent_t a, b;
     };
+    std::mutex lock;  // calls may run two streams from two host threads (both polarizations at once)
     std::vector<Rec> pending;
     double ms[TK_COUNT] = {0, 0, 0};
     long long count[TK_COUNT] = {0, 0, 0};
+    // launch intervals in ms after `base` (recorded when timing is switched on), for busy-time unions
+    cudaEvent_t base = nullptr;
+    std::vector<std::pair<double, double>> spans[TK_COUNT];
     void collect();
+    double busy_ms(int kind);  // length of the union of the kind's launch intervals
     ~KernelTimer();
 };
 KernelTimer*& current_timer();

@@ -18,11 +18,15 @@ KernelTimer*& current_timer() {
 }
 
 void KernelTimer::collect() {
+    std::lock_guard<std::mutex> hold(lock);
     for (Rec& r : pending) {
-        float ms_ = 0.0f;
+        float ms_ = 0.0f, t0 = 0.0f, t1 = 0.0f;
         if (cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&ms_, r.a, r.b) == cudaSuccess) {
             ms[r.kind] += ms_;
             count[r.kind] += 1;
+            if (base && cudaEventElapsedTime(&t0, base, r.a) == cudaSuccess &&
+                cudaEventElapsedTime(&t1, base, r.b) == cudaSuccess)
+                spans[r.kind].push_back({t0, t1});
         }
         cudaEventDestroy(r.a);
         cudaEventDestroy(r.b);
@@ -30,7 +34,30 @@ void KernelTimer::collect() {
     pending.clear();
 }
 
-KernelTimer::~KernelTimer() { collect(); }
+double KernelTimer::busy_ms(int kind) {
+    collect();
+    std::lock_guard<std::mutex> hold(lock);
+    std::vector<std::pair<double, double>>& v = spans[kind];
+    std::sort(v.begin(), v.end());
+    double total = 0.0, lo = 0.0, hi = -1.0;
+    for (const auto& iv : v) {
+        if (iv.first > hi) {
+            if (hi > lo) total += hi - lo;
+            lo = iv.first;
+            hi = iv.second;
+        } else {
+            hi = std::max(hi, iv.second);
+        }
+    }
+    if (hi > lo) total += hi - lo;
+    v.clear();
+    return total;
+}
+
+KernelTimer::~KernelTimer() {
+    collect();
+    if (base) cudaEventDestroy(base);
+}
 
 TimedLaunch::TimedLaunch(int kind, cudaStream_t st) : t_(current_timer()), st_(st) {
     if (!t_) return;
@@ -38,12 +65,15 @@ TimedLaunch::TimedLaunch(int kind, cudaStream_t st) : t_(current_timer()), st_(s
     cudaEventCreate(&r.a);
     cudaEventCreate(&r.b);
     cudaEventRecord(r.a, st);
+    std::lock_guard<std::mutex> hold(t_->lock);
     idx_ = t_->pending.size();
     t_->pending.push_back(r);
 }
 
 TimedLaunch::~TimedLaunch() {
-    if (t_) cudaEventRecord(t_->pending[idx_].b, st_);
+    if (!t_) return;
+    std::lock_guard<std::mutex> hold(t_->lock);
+    cudaEventRecord(t_->pending[idx_].b, st_);
 }
 
 namespace {

@@ -59,6 +59,7 @@ def load_library(build_if_missing=True):
     L.rcwa_gpu_stream.argtypes = [vp]
     L.rcwa_gpu_set_kernel_timing.argtypes = [vp, ci]
     L.rcwa_gpu_kernel_time.argtypes = [vp, C.c_char_p, C.POINTER(cd), C.POINTER(C.c_longlong)]
+    L.rcwa_gpu_kernel_busy.argtypes = [vp, C.c_char_p, C.POINTER(cd)]
     L.rcwa_options_default.argtypes = [C.POINTER(abi.rcwa_options)]
     L.rcwa_gpu_solve1d_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack1d), vp, ci, ci, ci, C.POINTER(abi.rcwa_options),
                                          C.POINTER(abi.rcwa_result1d)]
@@ -142,10 +143,11 @@ class Engine:
 
     def solve1d_arrays(self, stack, points, M, pol, options=None):
         """Batched solve with host buffers; returns a dict of numpy arrays (R, T, DEr, DEt, status,
-        eig_info, n_eig, n_dense_solve, max_eig_residual)."""
+        eig_info, n_eig, n_dense_solve, max_eig_residual). pol = 2 (RCWA_TE_TM): both polarizations,
+        every array holding the TE rows then the TM rows (2 x points)."""
         st, keep = abi.marshal_stack1d(stack)
         pts = abi.points_array(points)
-        res, arrays = abi.result_views(len(pts), M)
+        res, arrays = abi.result_views(len(pts) * (2 if pol == abi.RCWA_TE_TM else 1), M)
         o = _options(options)
         self._check(self.L.rcwa_gpu_solve1d_batch(self.h, C.byref(st), pts.ctypes.data, len(pts), M, pol, C.byref(o),
                                                   C.byref(res)))
@@ -153,7 +155,8 @@ class Engine:
 
     def solve1d_device(self, stack, d_points, n_points, M, pol, d_out, options=None):
         """Batched solve on device memory. d_points: device address of n_points (wavelength, theta)
-        double pairs; d_out: dict of device addresses for R, T, DEr, DEt, status (others optional)."""
+        double pairs; d_out: dict of device addresses for R, T, DEr, DEt, status (others optional).
+        pol = 2 (RCWA_TE_TM) solves both polarizations: every array holds TE results then TM results."""
         st, keep = abi.marshal_stack1d(stack)
         res = abi.rcwa_result1d()
         for k in ("R", "T", "DEr", "DEt", "status", "eig_info", "n_eig", "n_dense_solve", "max_eig_residual"):
@@ -175,6 +178,13 @@ class Engine:
         n = C.c_longlong()
         self._check(self.L.rcwa_gpu_kernel_time(self.h, kind.encode(), C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def kernel_busy(self, kind):
+        """Milliseconds during which at least one 'eig' / 'lu' / 'gemm' launch was running, since the
+        last read (launches of the two polarizations of a RCWA_TE_TM call overlap)."""
+        ms = C.c_double()
+        self._check(self.L.rcwa_gpu_kernel_busy(self.h, kind.encode(), C.byref(ms)))
+        return ms.value
 
     def synchronize(self):
         self._check(self.L.rcwa_gpu_synchronize(self.h))

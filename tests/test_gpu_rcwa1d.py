@@ -127,3 +127,16 @@ def test_device_resident_path_matches_host_path(eng):
     assert np.max(np.abs(out["DEr"].cpu().numpy() - o["DEr"])) <= 1e-10
     assert np.max(np.abs(out["DEt"].cpu().numpy() - o["DEt"])) <= 1e-10
     assert np.max(np.abs(out["DEr"].cpu().numpy() - host["DEr"])) <= 1e-11
+
+
+def test_both_polarizations_in_one_call(eng, cases1d):
+    """RCWA_TE_TM runs the TE and TM sweeps concurrently; each block equals its own single-polarization sweep."""
+    from stablercwa_gb300 import abi
+    c = next(c for c in cases1d if c["M"] >= 10)
+    stack = stack_from_json(c["stack"])
+    pts = [(c["wavelength"], c["theta"]), (c["wavelength"] * 1.07, c["theta"] * 0.5), (c["wavelength"] * 0.93, 3.0)]
+    both = eng.solve1d_arrays(stack, pts, c["M"], abi.RCWA_TE_TM)
+    for pol in (0, 1):
+        one = eng.solve1d_arrays(stack, pts, c["M"], pol)
+        for key in ("R", "T", "DEr", "DEt", "status", "n_dense_solve"):
+            assert np.array_equal(both[key][pol * len(pts):(pol + 1) * len(pts)], one[key]), (pol, key)
