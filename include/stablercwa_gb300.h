@@ -246,6 +246,16 @@ int rcwa_gpu_solve1d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const r
                            int n_points, int M, int polarization, const rcwa_options* options,
                            rcwa_result1d* out);
 
+/* 1-D solve with near fields: rcwa::solve_with_fields + field_at (include/stablercwa/rcwa1d_fields.hpp:55-198)
+ * at every point. Besides the results of rcwa_gpu_solve1d_batch, fields receives the harmonics of the six
+ * field components at the nz depths zs (z = 0 at the top of the first layer, increasing downwards; z < 0
+ * the incident medium, z past the last layer the exit medium; a depth on an interface belongs to the
+ * layer above): fields[((p * 6 + c) * (2M+1) + j) * nz + iz], c = Ex, Ey, Ez, Hx, Hy, Hz (H is Z0 H),
+ * j the order m + M. Taken from the modes and amplitudes of the same solve; NaN where the point failed. */
+int rcwa_gpu_solve1d_fields(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point1d* points, int n_points,
+                            int M, int polarization, const rcwa_options* options, const double* zs, int nz,
+                            rcwa_result1d* out, rcwa_complex* fields);
+
 /* Same solve with device-resident sweep points and device-resident result arrays (every pointer in
  * out is a device pointer). The stack description is host memory. Asynchronous with respect to the
  * host on the context's stream; rcwa_gpu_synchronize waits for it. polarization = RCWA_TE_TM solves

@@ -429,6 +429,58 @@ int rcwa_gpu_solve_conical_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, c
     });
 }
 
+int rcwa_gpu_solve1d_fields(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point1d* points, int n_points,
+                            int M, int polarization, const rcwa_options* options, const double* zs, int nz,
+                            rcwa_result1d* out, rcwa_complex* fields) {
+    return guarded(ctx, [&] {
+        if (!stack || (n_points > 0 && !points) || n_points < 0 || nz < 0 || (nz > 0 && (!zs || !fields)))
+            throw EngineError{RCWA_EINVAL, "rcwa: null argument"};
+        check_result_ptrs(out);
+        validate1d(*stack, points, n_points, M, polarization);
+        for (int k = 0; k < nz; ++k)
+            if (!std::isfinite(zs[k])) throw EngineError{RCWA_EINVAL, "rcwa: field depths must be finite"};
+        const Options opt = to_options(options);
+        if (n_points == 0) return;
+        const cudaStream_t st = ctx->stream;
+        const int n = 2 * M + 1;
+        std::vector<double> hs(n_points), hw(n_points);
+        const double kPi = 3.141592653589793238462643383279502884;
+        for (int p = 0; p < n_points; ++p) {
+            hs[p] = stack->nI.re * std::sin(points[p].theta_deg * kPi / 180.0);
+            hw[p] = points[p].wavelength;
+        }
+        DeviceScratch mem(st);
+        double* ds = mem.get<double>(n_points);
+        double* dw = mem.get<double>(n_points);
+        RCWA_CUDA(cudaMemcpyAsync(ds, hs.data(), n_points * sizeof(double), cudaMemcpyHostToDevice, st));
+        RCWA_CUDA(cudaMemcpyAsync(dw, hw.data(), n_points * sizeof(double), cudaMemcpyHostToDevice, st));
+        const size_t nv = (size_t)n_points * n, nf = (size_t)n_points * 6 * n * nz;
+        rcwa_result1d d{};
+        d.R = reinterpret_cast<rcwa_complex*>(mem.get<zc>(nv));
+        d.T = reinterpret_cast<rcwa_complex*>(mem.get<zc>(nv));
+        d.DEr = mem.get<double>(nv);
+        d.DEt = mem.get<double>(nv);
+        d.status = mem.get<int>(n_points);
+        d.eig_info = mem.get<int>(n_points);
+        d.n_eig = mem.get<int>(n_points);
+        d.n_dense_solve = mem.get<int>(n_points);
+        FieldSpec fs;
+        fs.zs.assign(zs, zs + nz);
+        fs.out = nz > 0 ? mem.get<zc>(nf) : nullptr;
+        solve1d_device(st, *stack, ds, dw, n_points, M, polarization, opt, d, chunk_bytes(ctx), nz > 0 ? &fs : nullptr);
+        copy_back(out->R, d.R, nv, st);
+        copy_back(out->T, d.T, nv, st);
+        copy_back(out->DEr, d.DEr, nv, st);
+        copy_back(out->DEt, d.DEt, nv, st);
+        copy_back(out->status, d.status, n_points, st);
+        copy_back(out->eig_info, d.eig_info, n_points, st);
+        copy_back(out->n_eig, d.n_eig, n_points, st);
+        copy_back(out->n_dense_solve, d.n_dense_solve, n_points, st);
+        if (nz > 0) copy_back(reinterpret_cast<zc*>(fields), fs.out, nf, st);
+        RCWA_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
 int rcwa_gpu_solve1d_batch_dev(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point1d* d_points, int n_points,
                                int M, int polarization, const rcwa_options* options, rcwa_result1d* d_out) {
     return guarded(ctx, [&] {

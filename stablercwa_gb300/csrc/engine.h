@@ -132,8 +132,16 @@ struct Options {
 
 // Batched 1-D solve (rcwa1d.cu). d_s[p] = nI sin(theta_p) and d_wl[p] = wavelength_p are device
 // arrays; results go to the device arrays of d_out. Throws EngineError.
+// Near fields of a 1-D solve (include/stablercwa/rcwa1d_fields.hpp:55-189): harmonics of the six field
+// components (Ex, Ey, Ez, Hx, Hy, Hz; H is Z0 H) at depths zs (z = 0 at the top of the first layer,
+// increasing downwards), from the modes and amplitudes of the same solve. out: device memory of
+// n_points x 6 x (2M+1) x nz, out[((p * 6 + c) * (2M+1) + j) * nz + iz].
+struct FieldSpec {
+    std::vector<double> zs;
+    zc* out = nullptr;
+};
 void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_s, const double* d_wl, int n_points,
-                    int M, int pol, const Options& opt, const rcwa_result1d& d_out, size_t chunk_bytes);
+                    int M, int pol, const Options& opt, const rcwa_result1d& d_out, size_t chunk_bytes, const FieldSpec* fields = nullptr);
 // Device-side check of the sweep points (finite positive wavelength, |theta| < 90) and
 // s = nI sin(theta) with the device sin; returns false when some point is invalid.
 bool prepare_points_device(cudaStream_t st, const rcwa_point1d* d_points, int n_points, double nI, double* d_s,

@@ -199,8 +199,110 @@ void validate1d(const rcwa_stack1d& stack, const rcwa_point1d* h_points, int n_p
 
 // ---------------------------------------------------------------- the solve
 
+namespace {
+
+// The field harmonics of one chunk (PlanarFieldSampler::sample, include/stablercwa/rcwa1d_fields.hpp:107-189):
+// depths grouped by region like field_depth_groups (rcwa_fields.hpp:253-279), S and U per group, W S and
+// V U for eigen-decomposed layers, Ez from [[eps]]^{-1} (TM), then scattered per component. Failed
+// samples get NaN fields (the reference leaves their context unavailable).
+void sample_fields(Batch& c, const FieldSpec& f, const rcwa_stack1d& stack, int pol, int M, int p0,
+                   const std::vector<DModes>& modes, const std::vector<zc*>& capW, const std::vector<zc*>& capV,
+                   const std::vector<const zc*>& einv, const std::vector<zc*>& ap, const std::vector<zc*>& am,
+                   const double* kx, const double* k0, const zc* R, const zc* T) {
+    const cudaStream_t st = c.st;
+    DeviceScratch& mem = *c.mem;
+    const int B = c.B, n = c.n, L = stack.n_layers, nz = (int)f.zs.size();
+    if (nz == 0) return;
+    const long long nn = (long long)n * n;
+    zc* out = f.out + (size_t)p0 * 6 * n * nz;
+    RCWA_CUDA(cudaMemsetAsync(out, 0, (size_t)B * 6 * n * nz * sizeof(zc), st));
+    std::vector<double> ztop(L), zbot(L);
+    double z = 0.0;
+    bool finite_layer = false;
+    for (int j = 0; j < L; ++j) {
+        ztop[j] = z;
+        z += stack.layers[j].d;
+        zbot[j] = z;
+        finite_layer = finite_layer || stack.layers[j].d > 0.0;
+    }
+    const double zb = z;
+    std::vector<std::vector<int>> groups(L + 2);  // 0 incident side, 1 exit side, 2 + j layer j
+    for (int iz = 0; iz < nz; ++iz) {
+        const double zz = f.zs[iz];
+        int g = zz < 0.0 ? 0 : 1;
+        if (zz >= 0.0 && zz <= zb && finite_layer)
+            for (int j = 0; j < L; ++j)
+                if (zz <= zbot[j] + 1e-12) {
+                    g = 2 + j;
+                    break;
+                }
+        groups[g].push_back(iz);
+    }
+    const cd nI{stack.nI.re, stack.nI.im}, nII{stack.nII.re, stack.nII.im};
+    for (int g = 0; g < L + 2; ++g) {
+        const std::vector<int>& cols = groups[g];
+        if (cols.empty()) continue;
+        const int cnt = (int)cols.size();
+        const long long tot = (long long)B * n * cnt;
+        std::vector<double> local(cnt);
+        for (int k = 0; k < cnt; ++k) local[k] = g >= 2 ? f.zs[cols[k]] - ztop[g - 2] : f.zs[cols[k]];
+        double* d_z = mem.get<double>(cnt);
+        int* d_cols = mem.get<int>(cnt);
+        RCWA_CUDA(cudaMemcpyAsync(d_z, local.data(), cnt * sizeof(double), cudaMemcpyHostToDevice, st));
+        RCWA_CUDA(cudaMemcpyAsync(d_cols, cols.data(), cnt * sizeof(int), cudaMemcpyHostToDevice, st));
+        zc* S = mem.get<zc>(tot);
+        zc* U = mem.get<zc>(tot);
+        zc* Ez = pol == RCWA_TM ? mem.get<zc>(tot) : nullptr;
+        if (g < 2) {
+            const DModes& m = g == 0 ? modes[0] : modes[L + 1];
+            LAUNCH(region_su_kernel, nblocks(tot), kTpb, st, B, n, M, cnt, d_z, g == 0 ? -1 : -2, zb, k0, m.q, m.p, R, T, S, U);
+            if (Ez) {
+                const cd ie = 1.0 / (g == 0 ? nI * nI : nII * nII);
+                LAUNCH(ez_scalar_kernel, nblocks(tot), kTpb, st, tot, n, kx, cnt, S, zc{ie.real(), ie.imag()}, Ez);
+            }
+        } else {
+            const int j = g - 2;
+            const DModes& m = modes[j + 1];
+            LAUNCH(layer_su_kernel, nblocks(tot), kTpb, st, B, n, cnt, d_z, stack.layers[j].d, k0, ap[j], am[j], m.q,
+                   m.fzb ? 1 : 0, m.analytic ? m.p : nullptr, S, U);
+            if (!m.analytic) {
+                zc* S2 = mem.get<zc>(tot);
+                zc* U2 = mem.get<zc>(tot);
+                launch_zgemm(st, n, cnt, n, B, capW[j], n, nn, S, n, (long long)n * cnt, nullptr, 0, S2, n, (long long)n * cnt,
+                             1.0, 0.0);
+                launch_zgemm(st, n, cnt, n, B, capV[j], n, nn, U, n, (long long)n * cnt, nullptr, 0, U2, n, (long long)n * cnt,
+                             1.0, 0.0);
+                mem.free(S);
+                mem.free(U);
+                S = S2;
+                U = U2;
+            }
+            if (Ez) {
+                if (m.analytic) {
+                    const cd nl{stack.layers[j].n.re, stack.layers[j].n.im};
+                    const cd ie = 1.0 / (nl * nl);
+                    LAUNCH(ez_scalar_kernel, nblocks(tot), kTpb, st, tot, n, kx, cnt, S, zc{ie.real(), ie.imag()}, Ez);
+                } else {
+                    zc* ks = mem.get<zc>(tot);
+                    LAUNCH(kx_rows_kernel, nblocks(tot), kTpb, st, tot, n, kx, cnt, S, ks);
+                    launch_zgemm(st, n, cnt, n, B, einv[j], n, 0, ks, n, (long long)n * cnt, nullptr, 0, Ez, n,
+                                 (long long)n * cnt, 1.0, 0.0);
+                    mem.free(ks);
+                }
+            }
+        }
+        LAUNCH(field_out_kernel, nblocks(tot), kTpb, st, B, n, cnt, nz, d_cols, pol, kx, S, U, Ez, out);
+        RCWA_CUDA(cudaStreamSynchronize(st));  // the host vectors of this group end here
+        for (void* p : {(void*)S, (void*)U, (void*)Ez, (void*)d_z, (void*)d_cols})
+            if (p) mem.free(p);
+    }
+    LAUNCH(nan_fields_kernel, nblocks((long long)B * 6 * n * nz), kTpb, st, B, 6LL * n * nz, c.fail, out);
+}
+
+}  // namespace
+
 void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_s, const double* d_wl, int n_points,
-                    int M, int pol, const Options& opt, const rcwa_result1d& d_out, size_t chunk_bytes) {
+                    int M, int pol, const Options& opt, const rcwa_result1d& d_out, size_t chunk_bytes, const FieldSpec* fields) {
     const int n = 2 * M + 1;
     const long long nn = (long long)n * n;
     const int L = stack.n_layers;
@@ -249,6 +351,8 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
         }
     }
 
+    std::vector<const zc*> ld_einv(L, nullptr);  // [[eps]]^{-1} of TM grating layers, for Ez in the fields
+    for (int k = 0; k < L; ++k) ld_einv[k] = ld[k].einv;
     // chunk size: rough upper bound of live device bytes per sample
     const long long per_sample = 16LL * (nn * (12 + 4 * (long long)grating.size()) + (long long)n * (8LL * (L + 2) + 64)) +
                                  eig_workspace_bytes(n, 1);
@@ -272,6 +376,8 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
 
         // ---- 1. modes of every region (region 0: nI, region j+1: layer j, region L+1: nII)
         std::vector<DModes> modes(L + 2);
+        std::vector<zc*> cap_W(L, nullptr), cap_V(L, nullptr);  // retained W, V of grating layers (fields)
+        std::vector<DOp> r_below(L);                             // reflection below each layer (fields)
         const auto analytic = [&](DModes& m, rcwa_complex idx, int fzb) {
             m.analytic = true;
             m.fzb = fzb != 0;
@@ -331,6 +437,12 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
                 }
                 mem.free(lam);
                 mem.free(bq);
+                if (fields) {  // the interface above consumes W and V; the field sampler needs them after
+                    cap_W[k] = c.dense();
+                    cap_V[k] = c.dense();
+                    RCWA_CUDA(cudaMemcpyAsync(cap_W[k], m.W, nd * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+                    RCWA_CUDA(cudaMemcpyAsync(cap_V[k], m.V, nd * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+                }
             }
             if (opt.diagnostics)
                 RCWA_CUDA(cudaMemcpyAsync(d_out.max_eig_residual + p0, resid, B * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -369,6 +481,14 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
                 continue;
             }
             // propagation through layer j (include/stablercwa/rcwa1d.hpp:751-784)
+            if (fields) {  // the reflection seen below layer j's bottom (rcwa1d.hpp:981)
+                r_below[j].kind = r.kind;
+                if (r.kind != KZero) {
+                    const size_t cnt = r.kind == KDiag ? (size_t)nv : (size_t)nd;
+                    r_below[j].p = mem.get<zc>(cnt);
+                    RCWA_CUDA(cudaMemcpyAsync(r_below[j].p, r.p, cnt * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+                }
+            }
             const DModes& m = modes[j + 1];
             zc* x = c.vec();
             zc* refl = c.vec();
@@ -466,9 +586,31 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
         // T = g[2L] ... g[1] down
         zc* cur = down;
         zc* nxt = c.vec();
+        std::vector<zc*> a_plus(L, nullptr), a_minus(L, nullptr);
         for (int b = 1; b < block_count; ++b) {
+            const int j = b / 2;
+            if (fields && b % 2 != 0) {  // amplitude at the layer's top (rcwa1d.hpp:1008-1012)
+                a_plus[j] = c.vec();
+                RCWA_CUDA(cudaMemcpyAsync(a_plus[j], cur, nv * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+                if (pure_films) LAUNCH(clear_unexcited_kernel, nblocks(nv), kTpb, st, B, n, M, a_plus[j]);
+            }
             LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 1, (int)g[b].kind, g[b].p, g[b].alt, g[b].alt_flag, cur, nxt);
             std::swap(cur, nxt);
+            if (fields && b % 2 != 0) {  // the reflection below applied at the layer's bottom (:1013-1020)
+                zc* bottom = cur;
+                if (pure_films) {
+                    bottom = c.vec();
+                    RCWA_CUDA(cudaMemcpyAsync(bottom, cur, nv * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+                    LAUNCH(clear_unexcited_kernel, nblocks(nv), kTpb, st, B, n, M, bottom);
+                }
+                a_minus[j] = c.vec();
+                LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 1, (int)r_below[j].kind, r_below[j].p, nullptr, nullptr,
+                       bottom, a_minus[j]);
+                if (pure_films) {
+                    LAUNCH(clear_unexcited_kernel, nblocks(nv), kTpb, st, B, n, M, a_minus[j]);
+                    mem.free(bottom);
+                }
+            }
         }
         zc* Tv = cur;
 
@@ -480,6 +622,9 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
         LAUNCH(status_kernel, nblocks(B), kTpb, st, B, c.fail, eig_info, c.n_solve, c.extra_solves, (int)grating.size(),
                d_out.status ? d_out.status + p0 : nullptr, d_out.eig_info ? d_out.eig_info + p0 : nullptr,
                d_out.n_eig ? d_out.n_eig + p0 : nullptr, d_out.n_dense_solve ? d_out.n_dense_solve + p0 : nullptr);
+        if (fields) sample_fields(c, *fields, stack, pol, M, p0, modes, cap_W, cap_V, ld_einv, a_plus, a_minus, kx, k0,
+                                  reinterpret_cast<zc*>(d_out.R) + (long long)p0 * n,
+                                  reinterpret_cast<zc*>(d_out.T) + (long long)p0 * n);
         mem.release();
     }
     // A singular [[eps]] or [[1/eps]] (TM) fails every sample; checked once at the end.

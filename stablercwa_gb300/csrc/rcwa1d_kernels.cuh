@@ -262,5 +262,133 @@ __global__ void stack_on_diag_kernel(long long total, const zc* __restrict__ tdd
     rout[idx] = out;
 }
 
+// ---------------------------------------------------------------- near fields (rcwa1d_fields.hpp:107-189)
+
+// Orders other than M carry nothing in a stack of films (clear_unexcited, rcwa1d.hpp:1011-1019)
+__global__ void clear_unexcited_kernel(int B, int n, int M, zc* __restrict__ v) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * n) return;
+    if ((int)(idx % n) != M) v[idx] = zc{0.0, 0.0};
+}
+
+// S and U harmonics of layer j at the given depths from the amplitudes anchored at the layer's top
+// (a+) and bottom (a-); U is scaled by the analytic V diagonal p when p != null. Layout per sample:
+// n x nz column-major.
+__global__ void layer_su_kernel(int B, int n, int nz, const double* __restrict__ zl, double d, const double* __restrict__ k0,
+                                const zc* __restrict__ ap, const zc* __restrict__ am, const zc* __restrict__ q, int fzb,
+                                const zc* __restrict__ p, zc* __restrict__ S, zc* __restrict__ U) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per = (long long)n * nz;
+    if (idx >= (long long)B * per) return;
+    const long long b = idx / per;
+    const long long r = idx - b * per;
+    const int col = (int)(r / n), j = (int)(r - (long long)col * n);
+    const double z = fmax(0.0, fmin(d, zl[col]));
+    const double k = k0[b];
+    const zc a = ap[b * n + j], bm = am[b * n + j], qj = q[b * n + j];
+    zc s, u;
+    if (fzb && is_zero(qj)) {
+        const double den = 1.0 + 0.5 * k * d;
+        const double from_bottom = (1.0 + k * (d - z)) / den, from_top = (1.0 + k * z) / den;
+        s = from_bottom * a + from_top * bm;
+        u = zdivr(-a, den) + zdivr(bm, den);
+    } else {
+        const zc pp = is_zero(a) ? zc{0.0, 0.0} : a * zexp((-k * z) * qj);
+        const zc mm = is_zero(bm) ? zc{0.0, 0.0} : bm * zexp((-k * (d - z)) * qj);
+        s = pp + mm;
+        u = mm - pp;
+    }
+    if (p) u = p[b * n + j] * u;
+    S[idx] = s;
+    U[idx] = u;
+}
+
+// S and U of the incident (region -1) or exit (region -2) medium (rcwa1d_fields.hpp:147-161)
+__global__ void region_su_kernel(int B, int n, int M, int nz, const double* __restrict__ zs, int region, double z_bottom,
+                                 const double* __restrict__ k0, const zc* __restrict__ q, const zc* __restrict__ p,
+                                 const zc* __restrict__ R, const zc* __restrict__ T, zc* __restrict__ S, zc* __restrict__ U) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per = (long long)n * nz;
+    if (idx >= (long long)B * per) return;
+    const long long b = idx / per;
+    const long long r = idx - b * per;
+    const int col = (int)(r / n), j = (int)(r - (long long)col * n);
+    const double z = zs[col], k = k0[b];
+    const zc qj = q[b * n + j];
+    const zc kz{-k * qj.im, k * qj.re};  // kz = i k0 q
+    zc pp{0.0, 0.0}, rr{0.0, 0.0}, tt{0.0, 0.0};
+    if (region == -1) {
+        if (j == M) {
+            const zc q0 = q[b * n + M];
+            const zc kz0{-k * q0.im, k * q0.re};
+            pp = zexp(zc{-kz0.im * z, kz0.re * z});  // exp(i kz0 z)
+        }
+        const zc Rj = R[b * n + j];
+        if (!is_zero(Rj)) rr = Rj * zexp(zc{kz.im * z, -kz.re * z});  // exp(-i kz z)
+    } else {
+        const zc Tj = T[b * n + j];
+        const double dz = z - z_bottom;
+        if (!is_zero(Tj)) tt = Tj * zexp(zc{-kz.im * dz, kz.re * dz});  // exp(i kz (z - z_bottom))
+    }
+    S[idx] = pp + rr + tt;
+    U[idx] = p[b * n + j] * ((rr - pp) - tt);
+}
+
+// Scatter S, U (and Ez for TM) of one depth group into the field harmonics out[b][c][j][iz]
+// (components Ex, Ey, Ez, Hx, Hy, Hz): TE Ey = S, Hx = i U, Hz = -kx S; TM Ex = -i U, Ez, Hy = S.
+__global__ void field_out_kernel(int B, int n, int nzg, int nz, const int* __restrict__ cols, int pol,
+                                 const double* __restrict__ kx, const zc* __restrict__ S, const zc* __restrict__ U,
+                                 const zc* __restrict__ Ez, zc* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per = (long long)n * nzg;
+    if (idx >= (long long)B * per) return;
+    const long long b = idx / per;
+    const long long r = idx - b * per;
+    const int col = (int)(r / n), j = (int)(r - (long long)col * n);
+    const int iz = cols[col];
+    const zc s = S[idx], u = U[idx];
+    zc* o = out + b * 6LL * n * nz + (long long)j * nz + iz;
+    const long long cstride = (long long)n * nz;
+    if (pol == 0) {
+        o[1 * cstride] = s;
+        o[3 * cstride] = zc{-u.im, u.re};
+        o[5 * cstride] = -kx[b * n + j] * s;
+    } else {
+        o[0 * cstride] = zc{u.im, -u.re};
+        o[2 * cstride] = Ez[idx];
+        o[4 * cstride] = s;
+    }
+}
+
+// Ez = kx S / eps for a scalar eps (analytic layers and the two media)
+__global__ void ez_scalar_kernel(long long total, int n, const double* __restrict__ kx, int nzg, const zc* __restrict__ S,
+                                 zc inv_eps, zc* __restrict__ Ez) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const long long per = (long long)n * nzg;
+    const long long b = idx / per;
+    const int j = (int)((idx - b * per) % n);
+    Ez[idx] = (kx[b * n + j] * S[idx]) * inv_eps;
+}
+
+// rows of S scaled by kx (the right-hand side of the Eps solve for Ez in a grating layer)
+__global__ void kx_rows_kernel(long long total, int n, const double* __restrict__ kx, int nzg, const zc* __restrict__ S,
+                               zc* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const long long per = (long long)n * nzg;
+    const long long b = idx / per;
+    const int j = (int)((idx - b * per) % n);
+    out[idx] = kx[b * n + j] * S[idx];
+}
+
+__global__ void nan_fields_kernel(int B, long long per, const int* __restrict__ fail, zc* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * per) return;
+    if (!fail[idx / per]) return;
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    out[idx] = zc{nan, nan};
+}
+
 }  // namespace
 }  // namespace rcwa_gb300

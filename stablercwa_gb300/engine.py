@@ -64,6 +64,8 @@ def load_library(build_if_missing=True):
     L.rcwa_gpu_solve1d_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack1d), vp, ci, ci, ci, C.POINTER(abi.rcwa_options),
                                          C.POINTER(abi.rcwa_result1d)]
     L.rcwa_gpu_solve1d_batch_dev.argtypes = L.rcwa_gpu_solve1d_batch.argtypes
+    L.rcwa_gpu_solve1d_fields.argtypes = [vp, C.POINTER(abi.rcwa_stack1d), vp, ci, ci, ci, C.POINTER(abi.rcwa_options), vp,
+                                          ci, C.POINTER(abi.rcwa_result1d), vp]
     L.rcwa_gpu_solve_conical_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack1d), vp, ci, ci,
                                                C.POINTER(abi.rcwa_options), C.POINTER(abi.rcwa_result_conical)]
     L.rcwa_gpu_solve2d_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack2d), vp, ci, ci, ci, ci,
@@ -152,6 +154,26 @@ class Engine:
         self._check(self.L.rcwa_gpu_solve1d_batch(self.h, C.byref(st), pts.ctypes.data, len(pts), M, pol, C.byref(o),
                                                   C.byref(res)))
         return arrays
+
+    def solve1d_fields(self, stack, points, M, pol, zs, options=None):
+        """rcwa::solve_with_fields + field_at at every point: (result arrays, fields) with fields of shape
+        (points, 6, 2M+1, nz), components Ex, Ey, Ez, Hx, Hy, Hz (H = Z0 H), harmonics per order and depth."""
+        st, keep = abi.marshal_stack1d(stack)
+        pts = abi.points_array(points)
+        z = np.ascontiguousarray(np.asarray(zs, dtype=np.float64).reshape(-1))
+        res, arrays = abi.result_views(len(pts), M)
+        fields = np.empty((len(pts), 6, 2 * M + 1, len(z)), np.complex128)
+        o = _options(options)
+        self._check(self.L.rcwa_gpu_solve1d_fields(self.h, C.byref(st), pts.ctypes.data, len(pts), M, pol, C.byref(o),
+                                                   z.ctypes.data, len(z), C.byref(res), fields.ctypes.data))
+        return arrays, fields
+
+    def field_map(self, fields, kxm, period, nx=256, y=0.0):
+        """Real-space field on an x grid from harmonics (reconstruct_field_grid, rcwa_fields.hpp:326-355):
+        fields (6, n, nz) of one point, kxm the physical kx of each order; returns (6, nz, nx)."""
+        x = np.arange(nx) / nx * period
+        carrier = np.exp(-1j * (np.outer(x, kxm)))
+        return np.einsum("xj,cjz->czx", carrier, fields)
 
     def solve1d_device(self, stack, d_points, n_points, M, pol, d_out, options=None):
         """Batched solve on device memory. d_points: device address of n_points (wavelength, theta)

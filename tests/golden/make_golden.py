@@ -24,6 +24,7 @@ EXPORTERS = [
     ("export_conical.cpp", "conical_cases.jsonl"),
     ("export_rcwa2d.cpp", "rcwa2d_cases.jsonl.gz"),
     ("export_fft.cpp", "fft_cases.jsonl"),
+    ("export_fields.cpp", "fields1d_cases.jsonl.gz"),
 ]
 
 
