@@ -273,6 +273,15 @@ int rcwa_gpu_synchronize(rcwa_gpu_ctx* ctx);
 int rcwa_gpu_solve_conical_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point_conical* points,
                                  int n_points, int M, const rcwa_options* options, rcwa_result_conical* out);
 
+/* Conical solve with near fields: rcwa::solve_conical_with_fields + field_at(context, zs, jones)
+ * (include/stablercwa/rcwa1d_conical_fields.hpp:52-97, :243-248) at every point. jones: 2 complex per
+ * point (Es, Ep of the incident field), normalised like rcwa::normalized_jones (rcwa_fields.hpp:218-230);
+ * nullptr means (1, 0) everywhere; a non-finite or zero Jones vector is RCWA_EINVAL. Depths and the
+ * layout of fields are those of rcwa_gpu_solve1d_fields; NaN where the point failed. */
+int rcwa_gpu_solve_conical_fields(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point_conical* points,
+                                  int n_points, int M, const rcwa_options* options, const rcwa_complex* jones,
+                                  const double* zs, int nz, rcwa_result_conical* out, rcwa_complex* fields);
+
 /* Fourier coefficients c[h + hmax], h = -hmax..hmax, of a piecewise-constant profile (K values, K + 1
  * increasing edges spanning one period). method 0: the closed form (rcwa::detail::fourier_coefficients,
  * include/stablercwa/rcwa1d.hpp:366-388), on the host; method 1: the FFT of `samples` cell-midpoint

@@ -361,71 +361,117 @@ int rcwa_gpu_layer_operators2d(rcwa_gpu_ctx* ctx, const rcwa_layer2d* layer, dou
     });
 }
 
+namespace {
+// rcwa_gpu_solve_conical_batch and, with fs, rcwa_gpu_solve_conical_fields (fs->out: host fields)
+void conical_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point_conical* points, int n_points, int M,
+                   const rcwa_options* options, rcwa_result_conical* out, const FieldSpec* fs) {
+    if (!stack || (n_points > 0 && !points) || n_points < 0) throw EngineError{RCWA_EINVAL, "rcwa: null argument"};
+    if (!out || !out->Jr || !out->Jt || !out->DEr || !out->DEt)
+        throw EngineError{RCWA_EINVAL, "rcwa: result arrays Jr, Jt, DEr, DEt are required"};
+    validate_conical(*stack, points, n_points, M);
+    const Options opt = to_options(options);
+    if (n_points == 0) return;
+    const cudaStream_t st = ctx->stream;
+    const int n = 2 * M + 1;
+    // the incidence trigonometry with the host libm, the reference's own expressions
+    // (include/stablercwa/rcwa1d_conical.hpp:704-730)
+    const double kPi = 3.141592653589793238462643383279502884;
+    const double nI = stack->nI.re;
+    std::vector<double> h(6 * (size_t)n_points);
+    for (int p = 0; p < n_points; ++p) {
+        const double theta = points[p].theta_deg * kPi / 180.0, phi = points[p].phi_deg * kPi / 180.0;
+        const double sine = nI * std::sin(theta);
+        h[0 * (size_t)n_points + p] = sine * std::cos(phi);
+        h[1 * (size_t)n_points + p] = sine * std::sin(phi);
+        h[2 * (size_t)n_points + p] = std::cos(phi);
+        h[3 * (size_t)n_points + p] = std::sin(phi);
+        h[4 * (size_t)n_points + p] = std::cos(theta);
+        h[5 * (size_t)n_points + p] = points[p].wavelength;
+    }
+    DeviceScratch mem(st);
+    double* dh = mem.get<double>(h.size());
+    RCWA_CUDA(cudaMemcpyAsync(dh, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    const ConicalPointsDev P{dh, dh + n_points, dh + 2 * (size_t)n_points, dh + 3 * (size_t)n_points,
+                             dh + 4 * (size_t)n_points, dh + 5 * (size_t)n_points};
+    const size_t nv = (size_t)n_points * n;
+    rcwa_result_conical d{};
+    d.Jr = reinterpret_cast<rcwa_complex*>(mem.get<zc>(nv * 4));
+    d.Jt = reinterpret_cast<rcwa_complex*>(mem.get<zc>(nv * 4));
+    d.DEr = mem.get<double>(nv * 4);
+    d.DEt = mem.get<double>(nv * 4);
+    d.status = mem.get<int>(n_points);
+    d.eig_info = mem.get<int>(n_points);
+    d.n_eig = mem.get<int>(n_points);
+    d.n_dense_solve = mem.get<int>(n_points);
+    d.n_schur = mem.get<int>(n_points);
+    d.min_abs_lambda = mem.get<double>(n_points);
+    d.degenerate_mode_warning = mem.get<int>(n_points);
+    d.kx = mem.get<double>(nv);
+    d.ky = mem.get<double>(n_points);
+    d.flux_r = mem.get<double>(nv);
+    d.flux_t = mem.get<double>(nv);
+    FieldSpec dfs;
+    const size_t nf = fs ? (size_t)n_points * 6 * n * fs->zs.size() : 0;
+    if (fs) {
+        dfs.zs = fs->zs;
+        dfs.jones = fs->jones;
+        dfs.out = nf > 0 ? mem.get<zc>(nf) : nullptr;
+    }
+    solve_conical_device(st, *stack, P, n_points, M, opt, d, chunk_bytes(ctx), fs && nf > 0 ? &dfs : nullptr);
+    if (nf > 0) copy_back(fs->out, dfs.out, nf, st);
+    copy_back(out->Jr, d.Jr, nv * 4, st);
+    copy_back(out->Jt, d.Jt, nv * 4, st);
+    copy_back(out->DEr, d.DEr, nv * 4, st);
+    copy_back(out->DEt, d.DEt, nv * 4, st);
+    copy_back(out->status, d.status, n_points, st);
+    copy_back(out->eig_info, d.eig_info, n_points, st);
+    copy_back(out->n_eig, d.n_eig, n_points, st);
+    copy_back(out->n_dense_solve, d.n_dense_solve, n_points, st);
+    copy_back(out->n_schur, d.n_schur, n_points, st);
+    copy_back(out->min_abs_lambda, d.min_abs_lambda, n_points, st);
+    copy_back(out->degenerate_mode_warning, d.degenerate_mode_warning, n_points, st);
+    copy_back(out->kx, d.kx, nv, st);
+    copy_back(out->ky, d.ky, n_points, st);
+    copy_back(out->flux_r, d.flux_r, nv, st);
+    copy_back(out->flux_t, d.flux_t, nv, st);
+    RCWA_CUDA(cudaStreamSynchronize(st));
+}
+}  // namespace
+
 int rcwa_gpu_solve_conical_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point_conical* points,
                                  int n_points, int M, const rcwa_options* options, rcwa_result_conical* out) {
+    return guarded(ctx, [&] { conical_batch(ctx, stack, points, n_points, M, options, out, nullptr); });
+}
+
+int rcwa_gpu_solve_conical_fields(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point_conical* points,
+                                  int n_points, int M, const rcwa_options* options, const rcwa_complex* jones,
+                                  const double* zs, int nz, rcwa_result_conical* out, rcwa_complex* fields) {
     return guarded(ctx, [&] {
-        if (!stack || (n_points > 0 && !points) || n_points < 0) throw EngineError{RCWA_EINVAL, "rcwa: null argument"};
-        if (!out || !out->Jr || !out->Jt || !out->DEr || !out->DEt)
-            throw EngineError{RCWA_EINVAL, "rcwa: result arrays Jr, Jt, DEr, DEt are required"};
-        validate_conical(*stack, points, n_points, M);
-        const Options opt = to_options(options);
-        if (n_points == 0) return;
-        const cudaStream_t st = ctx->stream;
-        const int n = 2 * M + 1;
-        // the incidence trigonometry with the host libm, the reference's own expressions
-        // (include/stablercwa/rcwa1d_conical.hpp:704-730)
-        const double kPi = 3.141592653589793238462643383279502884;
-        const double nI = stack->nI.re;
-        std::vector<double> h(6 * (size_t)n_points);
-        for (int p = 0; p < n_points; ++p) {
-            const double theta = points[p].theta_deg * kPi / 180.0, phi = points[p].phi_deg * kPi / 180.0;
-            const double sine = nI * std::sin(theta);
-            h[0 * (size_t)n_points + p] = sine * std::cos(phi);
-            h[1 * (size_t)n_points + p] = sine * std::sin(phi);
-            h[2 * (size_t)n_points + p] = std::cos(phi);
-            h[3 * (size_t)n_points + p] = std::sin(phi);
-            h[4 * (size_t)n_points + p] = std::cos(theta);
-            h[5 * (size_t)n_points + p] = points[p].wavelength;
+        if (nz < 0 || (nz > 0 && (!zs || !fields)) || n_points < 0) throw EngineError{RCWA_EINVAL, "rcwa: null argument"};
+        FieldSpec fs;
+        fs.zs.assign(zs, zs + nz);
+        for (int k = 0; k < nz; ++k)
+            if (!std::isfinite(zs[k])) throw EngineError{RCWA_EINVAL, "rcwa: field depths must be finite"};
+        if (jones) {  // rcwa::normalized_jones (include/stablercwa/rcwa_fields.hpp:218-230)
+            fs.jones.resize(2 * (size_t)n_points);
+            for (int p = 0; p < n_points; ++p) {
+                std::complex<double> v[2] = {{jones[2 * p].re, jones[2 * p].im}, {jones[2 * p + 1].re, jones[2 * p + 1].im}};
+                double scale = 0.0;
+                for (const auto& x : v) {
+                    if (!std::isfinite(x.real()) || !std::isfinite(x.imag()))
+                        throw EngineError{RCWA_EINVAL, "rcwa: Jones input must be finite and nonzero"};
+                    scale = std::max(scale, std::max(std::abs(x.real()), std::abs(x.imag())));
+                }
+                if (scale == 0.0) throw EngineError{RCWA_EINVAL, "rcwa: Jones input must be finite and nonzero"};
+                for (auto& x : v) x /= scale;
+                const double norm = std::sqrt(std::norm(v[0]) + std::norm(v[1]));
+                for (auto& x : v) x /= norm;
+                fs.jones[2 * p] = v[0];
+                fs.jones[2 * p + 1] = v[1];
+            }
         }
-        DeviceScratch mem(st);
-        double* dh = mem.get<double>(h.size());
-        RCWA_CUDA(cudaMemcpyAsync(dh, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-        const ConicalPointsDev P{dh, dh + n_points, dh + 2 * (size_t)n_points, dh + 3 * (size_t)n_points,
-                                 dh + 4 * (size_t)n_points, dh + 5 * (size_t)n_points};
-        const size_t nv = (size_t)n_points * n;
-        rcwa_result_conical d{};
-        d.Jr = reinterpret_cast<rcwa_complex*>(mem.get<zc>(nv * 4));
-        d.Jt = reinterpret_cast<rcwa_complex*>(mem.get<zc>(nv * 4));
-        d.DEr = mem.get<double>(nv * 4);
-        d.DEt = mem.get<double>(nv * 4);
-        d.status = mem.get<int>(n_points);
-        d.eig_info = mem.get<int>(n_points);
-        d.n_eig = mem.get<int>(n_points);
-        d.n_dense_solve = mem.get<int>(n_points);
-        d.n_schur = mem.get<int>(n_points);
-        d.min_abs_lambda = mem.get<double>(n_points);
-        d.degenerate_mode_warning = mem.get<int>(n_points);
-        d.kx = mem.get<double>(nv);
-        d.ky = mem.get<double>(n_points);
-        d.flux_r = mem.get<double>(nv);
-        d.flux_t = mem.get<double>(nv);
-        solve_conical_device(st, *stack, P, n_points, M, opt, d, chunk_bytes(ctx));
-        copy_back(out->Jr, d.Jr, nv * 4, st);
-        copy_back(out->Jt, d.Jt, nv * 4, st);
-        copy_back(out->DEr, d.DEr, nv * 4, st);
-        copy_back(out->DEt, d.DEt, nv * 4, st);
-        copy_back(out->status, d.status, n_points, st);
-        copy_back(out->eig_info, d.eig_info, n_points, st);
-        copy_back(out->n_eig, d.n_eig, n_points, st);
-        copy_back(out->n_dense_solve, d.n_dense_solve, n_points, st);
-        copy_back(out->n_schur, d.n_schur, n_points, st);
-        copy_back(out->min_abs_lambda, d.min_abs_lambda, n_points, st);
-        copy_back(out->degenerate_mode_warning, d.degenerate_mode_warning, n_points, st);
-        copy_back(out->kx, d.kx, nv, st);
-        copy_back(out->ky, d.ky, n_points, st);
-        copy_back(out->flux_r, d.flux_r, nv, st);
-        copy_back(out->flux_t, d.flux_t, nv, st);
-        RCWA_CUDA(cudaStreamSynchronize(st));
+        fs.out = reinterpret_cast<zc*>(fields);
+        conical_batch(ctx, stack, points, n_points, M, options, out, &fs);
     });
 }
 

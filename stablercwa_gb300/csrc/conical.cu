@@ -686,6 +686,164 @@ void batched_triangular_exp(Batch& c, int n, const zc* G, const double* k0, doub
     for (int* p : {iter, done, scal, mask, flags}) c.mem->free(p);
 }
 
+// ---------------------------------------------------------------- near fields (rcwa1d_conical_fields.hpp)
+
+// rows whose order is not M cleared in B x cols x 2N vectors (clear_unexcited, rcwa1d_conical.hpp:239-243)
+__global__ void conical_clear_unexcited_kernel(long long total, int n, int N, int M, zc* __restrict__ v) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    if ((int)(idx % n) % N != M) v[idx] = zc{0.0, 0.0};
+}
+
+// a = A(:, 0) Es + A(:, 1) Ep per sample, A of B x 2 x n (field_jones_response, rcwa1d_conical_fields.hpp:100-104)
+__global__ void jones_response_kernel(int B, int n, const zc* __restrict__ A, const zc* __restrict__ jones,
+                                      zc* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * n) return;
+    const long long b = idx / n;
+    const int i = (int)(idx - b * n);
+    out[idx] = A[(b * 2) * n + i] * jones[2 * b] + A[(b * 2 + 1) * n + i] * jones[2 * b + 1];
+}
+
+// Down and up parts at the group's depths, P = a exp(-k0 q t), Mm = b exp(-k0 q (d - t)) with t the depth
+// below the layer's top clamped to [0, d], for the samples that propagate mode by mode (Schur samples are
+// filled by conical_schur_apply_kernel). Per sample n x cnt, column-major (rcwa1d_conical_fields.hpp:179-190).
+__global__ void conical_layer_pm_kernel(int B, int n, int cnt, const double* __restrict__ zl, double d,
+                                        const double* __restrict__ k0, const zc* __restrict__ a, const zc* __restrict__ bm,
+                                        const zc* __restrict__ q, const int* __restrict__ schur, zc* __restrict__ P,
+                                        zc* __restrict__ Mm) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per = (long long)n * cnt;
+    if (idx >= (long long)B * per) return;
+    const long long b = idx / per;
+    if (schur && schur[b]) return;
+    const long long r = idx - b * per;
+    const int col = (int)(r / n), j = (int)(r - (long long)col * n);
+    const double from_top = fmax(0.0, fmin(d, zl[col])), from_bottom = d - from_top;
+    const double k = k0[b];
+    const zc av = a[b * n + j], bv = bm[b * n + j], qj = q[b * n + j];
+    P[idx] = is_zero(av) ? zc{0.0, 0.0} : av * zexp((-k * from_top) * qj);
+    Mm[idx] = is_zero(bv) ? zc{0.0, 0.0} : bv * zexp((-k * from_bottom) * qj);
+}
+
+// out column col of the Schur samples = E x (E = nullptr: x itself, a zero distance); warp per sample
+__global__ void conical_schur_apply_kernel(int B, int n, const zc* __restrict__ E, const zc* __restrict__ x,
+                                           const int* __restrict__ schur, zc* __restrict__ out, int cnt, int col) {
+    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (b >= B || !schur[b]) return;
+    const int lane = threadIdx.x & 31;
+    const zc* xs = x + b * n;
+    zc* o = out + (b * cnt + col) * n;
+    if (!E) {
+        for (int i = lane; i < n; i += 32) o[i] = xs[i];
+        return;
+    }
+    const zc* Es = E + b * (long long)n * n;
+    for (int i = lane; i < n; i += 32) {
+        zc acc{0.0, 0.0};
+        for (int k = 0; k < n; ++k) acc = zfma(Es[(long long)k * n + i], xs[k], acc);
+        o[i] = acc;
+    }
+}
+
+// F = P + Mm and G = Mm - P, scaled by the diagonal modes w, v of an analytic region
+__global__ void conical_fg_kernel(long long total, int n, int cnt, const zc* __restrict__ P, const zc* __restrict__ Mm,
+                                  const zc* __restrict__ w, const zc* __restrict__ v, zc* __restrict__ F,
+                                  zc* __restrict__ G) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    zc f = P[idx] + Mm[idx], g = -P[idx] + Mm[idx];
+    if (w) {
+        const long long per = (long long)n * cnt;
+        const long long b = idx / per;
+        const int j = (int)((idx - b * per) % n);
+        f = f * w[b * n + j];
+        g = g * v[b * n + j];
+    }
+    F[idx] = f;
+    G[idx] = g;
+}
+
+// F and G of the incident (region -1) or exit (region -2) medium from the Jones-combined response
+// (rcwa1d_conical_fields.hpp:195-210); kz is the normalised kzI or kzII of the region
+__global__ void conical_region_fg_kernel(int B, int N, int M, int cnt, const double* __restrict__ zs, int region,
+                                         double z_bottom, const double* __restrict__ k0, const zc* __restrict__ kz,
+                                         const zc* __restrict__ resp, const zc* __restrict__ jones,
+                                         const zc* __restrict__ w, const zc* __restrict__ v, zc* __restrict__ F,
+                                         zc* __restrict__ G) {
+    const int n = 2 * N;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per = (long long)n * cnt;
+    if (idx >= (long long)B * per) return;
+    const long long b = idx / per;
+    const long long r = idx - b * per;
+    const int col = (int)(r / n), j = (int)(r - (long long)col * n);
+    const int order = j % N;
+    const double z = zs[col], k = k0[b];
+    const zc kzo = k * kz[b * N + order];  // physical kz of this order
+    const zc rj = resp[b * n + j];
+    zc a{0.0, 0.0}, bb{0.0, 0.0}, t{0.0, 0.0};
+    if (region == -1) {
+        if (order == M) {
+            const zc kz0 = k * kz[b * N + M];
+            const zc inc = zexp(zc{-kz0.im * z, kz0.re * z});  // exp(i kz z)
+            a = (j < N ? jones[2 * b] : jones[2 * b + 1]) * inc;
+        }
+        if (!is_zero(rj)) bb = rj * zexp(zc{kzo.im * z, -kzo.re * z});  // exp(-i kz z)
+    } else if (!is_zero(rj)) {
+        const double dz = z - z_bottom;
+        t = rj * zexp(zc{-kzo.im * dz, kzo.re * dz});  // exp(i kz (z - z_bottom))
+    }
+    F[idx] = w[b * n + j] * ((a + bb) + t);
+    G[idx] = v[b * n + j] * ((-a + bb) - t);
+}
+
+// The six components from the (s, t) parts of F and G (rcwa1d_conical_fields.hpp:212-222): Ex, Ey, Hx, Hy, Hz
+// into out[b][c][j][iz]; Ez before the 1/eps factor into ez (per sample N x cnt).
+__global__ void conical_field_out_kernel(int B, int N, int cnt, int nz, const int* __restrict__ cols,
+                                         const double* __restrict__ kx, const double* __restrict__ ky,
+                                         const double* __restrict__ cs, const double* __restrict__ sn,
+                                         const zc* __restrict__ F, const zc* __restrict__ G, zc* __restrict__ ez,
+                                         zc* __restrict__ out) {
+    const int n = 2 * N;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per = (long long)N * cnt;
+    if (idx >= (long long)B * per) return;
+    const long long b = idx / per;
+    const long long r = idx - b * per;
+    const int col = (int)(r / N), j = (int)(r - (long long)col * N);
+    const long long base = (b * cnt + col) * n;
+    const zc f1 = F[base + j], f2 = F[base + N + j], g1 = G[base + j], g2 = G[base + N + j];
+    const double c = cs[b * N + j], s = sn[b * N + j], kxj = kx[b * N + j], kyb = ky[b];
+    const zc ex = (-s) * f1 + c * f2;
+    const zc ey = c * f1 + s * f2;
+    const zc hx = (-c) * g1 - s * g2;
+    const zc hy = (-s) * g1 + c * g2;
+    const zc hz = kyb * ex - kxj * ey;
+    const zc e = kyb * hx - kxj * hy;
+    const long long cstride = (long long)N * nz;
+    zc* o = out + b * 6LL * N * nz + (long long)j * nz + cols[col];
+    o[0 * cstride] = ex;
+    o[1 * cstride] = ey;
+    o[3 * cstride] = zc{hx.im, -hx.re};  // -i hx
+    o[4 * cstride] = zc{hy.im, -hy.re};  // -i hy
+    o[5 * cstride] = hz;
+    ez[idx] = zc{-e.im, e.re};  // i (ky hx - kx hy)
+}
+
+// Ez (per sample N x cnt) into out[b][2][j][iz], times the scalar 1/eps when scale != null
+__global__ void ez_out_kernel(int B, int N, int cnt, int nz, const int* __restrict__ cols, const zc* __restrict__ ez,
+                              const zc* scale, zc* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per = (long long)N * cnt;
+    if (idx >= (long long)B * per) return;
+    const long long b = idx / per;
+    const long long r = idx - b * per;
+    const int col = (int)(r / N), j = (int)(r - (long long)col * N);
+    const zc e = scale ? ez[idx] * *scale : ez[idx];
+    out[b * 6LL * N * nz + 2LL * N * nz + (long long)j * nz + cols[col]] = e;
+}
+
 struct Region {
     bool analytic = true;
     zc *q = nullptr, *w = nullptr, *v = nullptr;  // analytic: B x 2N diagonals
@@ -741,6 +899,156 @@ DSBlock interface_block(Batch& c, const Region& up, const Region& low) {
     return s;
 }
 
+// The field harmonics of one chunk (ConicalFieldSampler::sample, include/stablercwa/rcwa1d_conical_fields.hpp:163-236):
+// depths grouped by region like field_depth_groups (rcwa_fields.hpp:253-279) over the layers of nonzero
+// thickness, the Jones-combined amplitudes propagated mode by mode (or by exp(-k0 t G) for Schur samples),
+// W F and V G for eigen-decomposed layers, the six components, Ez through [[eps]]^{-1} or 1/eps. Failed
+// samples get NaN fields (the reference leaves their context unavailable).
+struct ConicalCapture {
+    std::vector<zc*> W, V;           // retained mode matrices of the grating layers (B x n x n)
+    std::vector<DOp> r_below;        // reflection below each layer
+    std::vector<zc*> a_plus, a_minus;  // B x 2 x n per layer, columns s and p input
+    std::vector<const zc*> einv;     // [[eps]]^{-1} of grating layers (N x N, shared by the samples)
+    std::vector<std::complex<double>> inv_eps;  // 1/eps of uniform layers
+};
+
+void sample_conical_fields(Batch& c, const FieldSpec& f, const std::vector<const rcwa_layer1d*>& layers,
+                           const rcwa_stack1d& stack, int M, int p0, const std::vector<Region>& modes,
+                           const ConicalCapture& cap, const zc* refl, const zc* trans, const double* kx, const double* ky,
+                           const double* cs, const double* sn, const zc* kzI, const zc* kzII, const double* k0) {
+    const cudaStream_t st = c.st;
+    DeviceScratch& mem = *c.mem;
+    const int B = c.B, n = c.n, N = n / 2, L = (int)layers.size(), nz = (int)f.zs.size();
+    if (nz == 0) return;
+    const long long nn = (long long)n * n, NN = (long long)N * N, nv = (long long)B * n;
+    zc* out = f.out + (size_t)p0 * 6 * N * nz;
+    RCWA_CUDA(cudaMemsetAsync(out, 0, (size_t)B * 6 * N * nz * sizeof(zc), st));
+    // the normalised Jones vectors of this chunk
+    std::vector<zc> hj(2 * (size_t)B);
+    for (int b = 0; b < B; ++b) {
+        if (f.jones.empty()) {
+            hj[2 * b] = zc{1.0, 0.0};
+            hj[2 * b + 1] = zc{0.0, 0.0};
+        } else {
+            const std::complex<double> e = f.jones[2 * (size_t)(p0 + b)], p = f.jones[2 * (size_t)(p0 + b) + 1];
+            hj[2 * b] = zc{e.real(), e.imag()};
+            hj[2 * b + 1] = zc{p.real(), p.imag()};
+        }
+    }
+    zc* jones = mem.get<zc>(2 * (size_t)B);
+    RCWA_CUDA(cudaMemcpyAsync(jones, hj.data(), 2 * (size_t)B * sizeof(zc), cudaMemcpyHostToDevice, st));
+    std::vector<double> ztop(L), zbot(L);
+    double z = 0.0;
+    for (int j = 0; j < L; ++j) {
+        ztop[j] = z;
+        z += layers[j]->d;
+        zbot[j] = z;
+    }
+    const double zb = z;
+    std::vector<std::vector<int>> groups(L + 2);  // 0 incident side, 1 exit side, 2 + j layer j
+    for (int iz = 0; iz < nz; ++iz) {
+        const double zz = f.zs[iz];
+        int g = zz < 0.0 ? 0 : 1;
+        if (zz >= 0.0 && zz <= zb && L > 0)
+            for (int j = 0; j < L; ++j)
+                if (zz <= zbot[j] + 1e-12) {
+                    g = 2 + j;
+                    break;
+                }
+        groups[g].push_back(iz);
+    }
+    const std::complex<double> nI{stack.nI.re, stack.nI.im}, nII{stack.nII.re, stack.nII.im};
+    zc* a = mem.get<zc>(nv);
+    zc* bmv = mem.get<zc>(nv);
+    zc* scale = mem.get<zc>(1);
+    for (int g = 0; g < L + 2; ++g) {
+        const std::vector<int>& cols = groups[g];
+        if (cols.empty()) continue;
+        const int cnt = (int)cols.size();
+        const long long tot = (long long)B * n * cnt, totN = (long long)B * N * cnt;
+        std::vector<double> local(cnt);
+        for (int k = 0; k < cnt; ++k) local[k] = g >= 2 ? f.zs[cols[k]] - ztop[g - 2] : f.zs[cols[k]];
+        double* d_z = mem.get<double>(cnt);
+        int* d_cols = mem.get<int>(cnt);
+        RCWA_CUDA(cudaMemcpyAsync(d_z, local.data(), cnt * sizeof(double), cudaMemcpyHostToDevice, st));
+        RCWA_CUDA(cudaMemcpyAsync(d_cols, cols.data(), cnt * sizeof(int), cudaMemcpyHostToDevice, st));
+        zc* F = mem.get<zc>(tot);
+        zc* G = mem.get<zc>(tot);
+        zc* ez = mem.get<zc>(totN);
+        std::complex<double> ie{0.0, 0.0};
+        const zc* einv = nullptr;
+        if (g < 2) {
+            const Region& m = g == 0 ? modes[0] : modes[L + 1];
+            LAUNCH(jones_response_kernel, nblocks(nv), kTpb, st, B, n, g == 0 ? refl : trans, jones, a);
+            LAUNCH(conical_region_fg_kernel, nblocks(tot), kTpb, st, B, N, M, cnt, d_z, g == 0 ? -1 : -2, zb, k0,
+                   g == 0 ? kzI : kzII, a, jones, m.w, m.v, F, G);
+            ie = 1.0 / (g == 0 ? nI * nI : nII * nII);
+        } else {
+            const int j = g - 2;
+            const Region& m = modes[j + 1];
+            const double d = layers[j]->d;
+            LAUNCH(jones_response_kernel, nblocks(nv), kTpb, st, B, n, cap.a_plus[j], jones, a);
+            LAUNCH(jones_response_kernel, nblocks(nv), kTpb, st, B, n, cap.a_minus[j], jones, bmv);
+            zc* P = mem.get<zc>(tot);
+            zc* Mm = mem.get<zc>(tot);
+            LAUNCH(conical_layer_pm_kernel, nblocks(tot), kTpb, st, B, n, cnt, d_z, d, k0, a, bmv, m.q, m.G ? m.schur : nullptr,
+                   P, Mm);
+            if (m.G) {  // Schur samples: exp(-k0 t G) applied to the anchors (rcwa1d_conical_fields.hpp:109-160)
+                zc* E = mem.get<zc>((size_t)B * nn);
+                zc* work = mem.get<zc>(4 * (size_t)B * nn);
+                for (int col = 0; col < cnt; ++col) {
+                    const double from_top = std::max(0.0, std::min(d, local[col])), from_bottom = d - from_top;
+                    for (int side = 0; side < 2; ++side) {
+                        const double dist = side == 0 ? from_top : from_bottom;
+                        if (dist != 0.0) batched_triangular_exp(c, n, m.G, k0, dist, E, work, m.schur);
+                        LAUNCH(conical_schur_apply_kernel, warp_blocks(B), 128, st, B, n, dist != 0.0 ? E : nullptr,
+                               side == 0 ? a : bmv, m.schur, side == 0 ? P : Mm, cnt, col);
+                    }
+                }
+                mem.free(work);
+                mem.free(E);
+            }
+            LAUNCH(conical_fg_kernel, nblocks(tot), kTpb, st, tot, n, cnt, P, Mm, m.analytic ? m.w : nullptr,
+                   m.analytic ? m.v : nullptr, F, G);
+            mem.free(P);
+            mem.free(Mm);
+            if (!m.analytic) {
+                zc* F2 = mem.get<zc>(tot);
+                zc* G2 = mem.get<zc>(tot);
+                launch_zgemm(st, n, cnt, n, B, cap.W[j], n, nn, F, n, (long long)n * cnt, nullptr, 0, F2, n, (long long)n * cnt,
+                             1.0, 0.0);
+                launch_zgemm(st, n, cnt, n, B, cap.V[j], n, nn, G, n, (long long)n * cnt, nullptr, 0, G2, n, (long long)n * cnt,
+                             1.0, 0.0);
+                mem.free(F);
+                mem.free(G);
+                F = F2;
+                G = G2;
+                einv = cap.einv[j];
+            } else {
+                ie = cap.inv_eps[j];
+            }
+        }
+        LAUNCH(conical_field_out_kernel, nblocks(totN), kTpb, st, B, N, cnt, nz, d_cols, kx, ky, cs, sn, F, G, ez, out);
+        if (einv) {
+            zc* ez2 = mem.get<zc>(totN);
+            launch_zgemm(st, N, cnt, N, B, einv, N, 0, ez, N, (long long)N * cnt, nullptr, 0, ez2, N, (long long)N * cnt, 1.0,
+                         0.0);
+            LAUNCH(ez_out_kernel, nblocks(totN), kTpb, st, B, N, cnt, nz, d_cols, ez2, nullptr, out);
+            RCWA_CUDA(cudaStreamSynchronize(st));
+            mem.free(ez2);
+        } else {
+            const zc hs{ie.real(), ie.imag()};
+            RCWA_CUDA(cudaMemcpyAsync(scale, &hs, sizeof(zc), cudaMemcpyHostToDevice, st));
+            LAUNCH(ez_out_kernel, nblocks(totN), kTpb, st, B, N, cnt, nz, d_cols, ez, scale, out);
+            RCWA_CUDA(cudaStreamSynchronize(st));  // the host values of this group end here
+        }
+        for (void* p : {(void*)F, (void*)G, (void*)ez, (void*)d_z, (void*)d_cols}) mem.free(p);
+    }
+    for (void* p : {(void*)a, (void*)bmv, (void*)scale, (void*)jones}) mem.free(p);
+    LAUNCH(nan_fields_kernel, nblocks((long long)B * 6 * N * nz), kTpb, st, B, 6LL * N * nz, c.fail, out);
+    (void)NN;
+}
+
 }  // namespace
 
 // include/stablercwa/rcwa1d_conical.hpp:684-695 (the checks the reference adds to rcwa1d's)
@@ -756,7 +1064,8 @@ void validate_conical(const rcwa_stack1d& stack, const rcwa_point_conical* h_poi
 }
 
 void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const ConicalPointsDev& pts, int n_points, int M,
-                          const Options& opt, const rcwa_result_conical& d_out, size_t chunk_bytes) {
+                          const Options& opt, const rcwa_result_conical& d_out, size_t chunk_bytes,
+                          const FieldSpec* fields) {
     const int N = 2 * M + 1, n = 2 * N;
     const long long NN = (long long)N * N, nn = (long long)n * n;
     if (n_points <= 0) return;
@@ -808,8 +1117,11 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
     }
     const int base_solves = 2 * static_cast<int>(grating.size());
 
-    const long long per_sample = 16LL * (nn * 16 + NN * 12 * (long long)grating.size() + (long long)n * 8 * (L + 2)) +
-                                 2 * eig_workspace_bytes(N, 1) * (long long)std::max<size_t>(1, grating.size());
+    long long per_sample = 16LL * (nn * 16 + NN * 12 * (long long)grating.size() + (long long)n * 8 * (L + 2)) +
+                           2 * eig_workspace_bytes(N, 1) * (long long)std::max<size_t>(1, grating.size());
+    if (fields)  // retained W, V and reflections, amplitudes, one depth group's buffers
+        per_sample += 16LL * (nn * 3 * (long long)grating.size() + (long long)n * 8 * L +
+                              (long long)n * 6 * (long long)fields->zs.size());
     long long chunk = chunk_bytes > 0 ? (long long)chunk_bytes / std::max(1LL, per_sample) : n_points;
     chunk = std::max(1LL, std::min<long long>(chunk, n_points));
 
@@ -953,6 +1265,29 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
             }
             for (void* p : {(void*)ABall, (void*)lamall, (void*)vecall, (void*)infoall}) mem.free(p);
         }
+        ConicalCapture cap;
+        if (fields) {  // the interface above a layer consumes its W and V; the field sampler needs them after
+            cap.W.assign(L, nullptr);
+            cap.V.assign(L, nullptr);
+            cap.r_below.assign(L, DOp{});
+            cap.a_plus.assign(L, nullptr);
+            cap.a_minus.assign(L, nullptr);
+            cap.einv.assign(L, nullptr);
+            cap.inv_eps.assign(L, {0.0, 0.0});
+            for (int k = 0; k < L; ++k) {
+                if (modes[k + 1].analytic) {
+                    const rcwa_complex idx = layers[k]->homogeneous ? layers[k]->n : layers[k]->n_values[0];
+                    const std::complex<double> nl{idx.re, idx.im};
+                    cap.inv_eps[k] = 1.0 / (nl * nl);
+                    continue;
+                }
+                cap.W[k] = c.dense();
+                cap.V[k] = c.dense();
+                RCWA_CUDA(cudaMemcpyAsync(cap.W[k], modes[k + 1].W, nd * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+                RCWA_CUDA(cudaMemcpyAsync(cap.V[k], modes[k + 1].V, nd * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+                cap.einv[k] = ld[k].einv;
+            }
+        }
 
         // ---- 2. bottom-up recursion at order 2N
         const int block_count = 2 * L + 1;
@@ -978,6 +1313,14 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
             }
             const Region& m = modes[j + 1];
             const double d = layers[j]->d;
+            if (fields) {  // the reflection seen below layer j's bottom (rcwa1d_conical.hpp:866)
+                cap.r_below[j].kind = r.kind;
+                if (r.kind != KZero) {
+                    const size_t cnt = r.kind == KDense ? (size_t)nd : (size_t)nv;
+                    cap.r_below[j].p = mem.get<zc>(cnt);
+                    RCWA_CUDA(cudaMemcpyAsync(cap.r_below[j].p, r.p, cnt * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+                }
+            }
             zc* x = c.vec();
             zc* refl = c.vec();
             int* hz = mem.zeros<int>(B);
@@ -1057,9 +1400,32 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
         zc* cur = down;
         zc* nxt = mem.get<zc>(2 * nv);
         for (int b = 1; b < block_count; ++b) {
+            const int j = b / 2;
+            if (fields && b % 2 != 0) {  // amplitudes at the layer's top (rcwa1d_conical.hpp:921-925)
+                cap.a_plus[j] = mem.get<zc>(2 * nv);
+                RCWA_CUDA(cudaMemcpyAsync(cap.a_plus[j], cur, 2 * nv * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+                if (pure_films)
+                    LAUNCH(conical_clear_unexcited_kernel, nblocks(2 * nv), kTpb, st, 2 * nv, n, N, M, cap.a_plus[j]);
+            }
             LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 2, (int)g[b].kind, g[b].p, g[b].alt, g[b].alt_flag, cur,
                    nxt);
             std::swap(cur, nxt);
+            if (fields && b % 2 != 0) {  // the reflection below applied at the layer's bottom (:926-931)
+                zc* bottom = cur;
+                zc* cleared = nullptr;
+                if (pure_films) {
+                    cleared = mem.get<zc>(2 * nv);
+                    RCWA_CUDA(cudaMemcpyAsync(cleared, cur, 2 * nv * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+                    LAUNCH(conical_clear_unexcited_kernel, nblocks(2 * nv), kTpb, st, 2 * nv, n, N, M, cleared);
+                    bottom = cleared;
+                }
+                cap.a_minus[j] = mem.get<zc>(2 * nv);
+                LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 2, (int)cap.r_below[j].kind, cap.r_below[j].p, nullptr,
+                       nullptr, bottom, cap.a_minus[j]);
+                if (pure_films)
+                    LAUNCH(conical_clear_unexcited_kernel, nblocks(2 * nv), kTpb, st, 2 * nv, n, N, M, cap.a_minus[j]);
+                if (cleared) mem.free(cleared);
+            }
         }
 
         // ---- 4. Jones matrices, efficiencies, status
@@ -1073,6 +1439,13 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                d_out.n_dense_solve ? d_out.n_dense_solve + p0 : nullptr, d_out.n_schur ? d_out.n_schur + p0 : nullptr,
                d_out.min_abs_lambda ? d_out.min_abs_lambda + p0 : nullptr,
                d_out.degenerate_mode_warning ? d_out.degenerate_mode_warning + p0 : nullptr);
+        if (fields) {
+            if (pure_films) {  // rcwa1d_conical.hpp:963-966
+                LAUNCH(conical_clear_unexcited_kernel, nblocks(2 * nv), kTpb, st, 2 * nv, n, N, M, rud);
+                LAUNCH(conical_clear_unexcited_kernel, nblocks(2 * nv), kTpb, st, 2 * nv, n, N, M, cur);
+            }
+            sample_conical_fields(c, *fields, layers, stack, M, p0, modes, cap, rud, cur, kx, P.ky, cs, sn, kzI, kzII, k0);
+        }
         mem.release();
     }
     int lf = 0;
@@ -1089,6 +1462,12 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
         if (d_out.status) {
             std::vector<int> s(n_points, RCWA_SAMPLE_NUMERICAL);
             RCWA_CUDA(cudaMemcpyAsync(d_out.status, s.data(), n_points * sizeof(int), cudaMemcpyHostToDevice, st));
+        }
+        if (fields && !fields->zs.empty()) {
+            const size_t cf = (size_t)n_points * 6 * N * fields->zs.size();
+            std::vector<double> fn(cf * 2, nan);
+            RCWA_CUDA(cudaMemcpyAsync(fields->out, fn.data(), cf * sizeof(zc), cudaMemcpyHostToDevice, st));
+            RCWA_CUDA(cudaStreamSynchronize(st));
         }
         RCWA_CUDA(cudaStreamSynchronize(st));
     }

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <complex>
 #include <mutex>
 #include <stdexcept>
 #include <string>
@@ -139,6 +140,7 @@ struct Options {
 struct FieldSpec {
     std::vector<double> zs;
     zc* out = nullptr;
+    std::vector<std::complex<double>> jones;  // conical: normalised (Es, Ep) per point; empty = (1, 0)
 };
 void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_s, const double* d_wl, int n_points,
                     int M, int pol, const Options& opt, const rcwa_result1d& d_out, size_t chunk_bytes, const FieldSpec* fields = nullptr);
@@ -154,7 +156,8 @@ struct ConicalPointsDev {
     const double *s_cphi, *ky, *cphi, *sphi, *ctheta, *wl;
 };
 void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const ConicalPointsDev& pts, int n_points, int M,
-                          const Options& opt, const rcwa_result_conical& d_out, size_t chunk_bytes);
+                          const Options& opt, const rcwa_result_conical& d_out, size_t chunk_bytes,
+                          const FieldSpec* fields = nullptr);
 void validate_conical(const rcwa_stack1d& stack, const rcwa_point_conical* h_points, int n_points, int M);
 
 // 2-D crossed gratings (rcwa2d.cu): validation where the reference throws std::invalid_argument,

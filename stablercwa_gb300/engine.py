@@ -68,6 +68,8 @@ def load_library(build_if_missing=True):
                                           ci, C.POINTER(abi.rcwa_result1d), vp]
     L.rcwa_gpu_solve_conical_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack1d), vp, ci, ci,
                                                C.POINTER(abi.rcwa_options), C.POINTER(abi.rcwa_result_conical)]
+    L.rcwa_gpu_solve_conical_fields.argtypes = [vp, C.POINTER(abi.rcwa_stack1d), vp, ci, ci, C.POINTER(abi.rcwa_options),
+                                                vp, vp, ci, C.POINTER(abi.rcwa_result_conical), vp]
     L.rcwa_gpu_solve2d_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack2d), vp, ci, ci, ci, ci,
                                          C.POINTER(abi.rcwa_options), C.POINTER(abi.rcwa_result2d)]
     L.rcwa_gpu_layer_operators2d.argtypes = [vp, C.POINTER(abi.rcwa_layer2d), cd, cd, ci, ci, ci, vp, vp, vp, vp]
@@ -235,6 +237,25 @@ class Engine:
         self._check(self.L.rcwa_gpu_solve_conical_batch(self.h, C.byref(st), pts.ctypes.data, len(pts), M, C.byref(o),
                                                         C.byref(res)))
         return arrays
+
+    def solve_conical_fields(self, stack, points, M, zs, jones=None, options=None):
+        """rcwa::solve_conical_with_fields + field_at(context, zs, jones) at every (wavelength, theta, phi)
+        point: (result arrays, fields (P, 6, 2M+1, nz)). jones: None for (1, 0), one (Es, Ep) pair for
+        every point, or one pair per point; normalised like rcwa::normalized_jones."""
+        st, keep = abi.marshal_stack1d(stack)
+        pts = abi.conical_points_array(points)
+        res, arrays = abi.conical_views(len(pts), M)
+        z = np.ascontiguousarray(np.asarray(zs, dtype=np.float64).reshape(-1))
+        fields = np.empty((len(pts), 6, 2 * M + 1, len(z)), np.complex128)
+        jp = None
+        if jones is not None:
+            j = np.asarray(jones, dtype=np.complex128)
+            j = np.ascontiguousarray(np.broadcast_to(j.reshape(-1, 2), (len(pts), 2)))
+            jp = j.ctypes.data
+        o = _options(options)
+        self._check(self.L.rcwa_gpu_solve_conical_fields(self.h, C.byref(st), pts.ctypes.data, len(pts), M, C.byref(o),
+                                                         jp, z.ctypes.data, len(z), C.byref(res), fields.ctypes.data))
+        return arrays, fields
 
     def solve_conical(self, stack, wavelength, theta_deg, phi_deg, M, options=None):
         a = self.solve_conical_arrays(stack, [(wavelength, theta_deg, phi_deg)], M, options)

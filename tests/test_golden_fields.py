@@ -15,14 +15,23 @@ def test_fixture_inventory():
     names = {c["name"] for c in cases}
     for stem in ("mixed", "mixed_far", "schur", "readme_M20", "films", "multi_grating"):
         assert {stem + "_TE", stem + "_TM"} <= names
+    assert sum(c["kind"] == "conical" for c in cases) >= 8
+    assert next(c for c in cases if c["name"] == "conical_schur_M8")["n_schur"] == 1
     for c in cases:
         assert c["available"] == 1
         assert fields(c).shape == (6, 2 * c["M"] + 1, len(c["zs"]))
+        assert np.all(np.isfinite(fields(c)))
+
+
+def test_conical_zero_thickness_layers_change_nothing():
+    # tests/test_rcwa_public_fields.cpp:213-216: zero-thickness layers are skipped, bit for bit
+    cases = {c["name"]: c for c in load_jsonl("fields1d_cases.jsonl.gz")}
+    assert np.array_equal(fields(cases["conical_mixed_jones"]), fields(cases["conical_zero_layers"]))
 
 
 def test_tangential_continuity_in_fixtures():
     for c in load_jsonl("fields1d_cases.jsonl.gz"):
-        if c["name"].startswith("mixed_far"):
+        if c["name"].startswith("mixed_far") or c["kind"] != "planar":
             continue
         f = fields(c)
         zs = c["zs"]
@@ -35,7 +44,7 @@ def test_tangential_continuity_in_fixtures():
 
 def test_repeated_and_clipped_depths():
     for c in load_jsonl("fields1d_cases.jsonl.gz"):
-        if not c["name"].startswith("mixed_far"):
+        if not (c["name"].startswith("mixed_far") or c["name"] == "conical_mixed_jones"):
             continue
         f = fields(c)
         # zs = .083, -.12, .42, .2, .2+5e-13, .42+5e-13, .083, .245, 0, 100, -100

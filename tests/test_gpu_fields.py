@@ -25,7 +25,13 @@ def eng():
 
 @pytest.fixture(scope="module")
 def cases():
-    return load_jsonl("fields1d_cases.jsonl.gz")
+    return [c for c in load_jsonl("fields1d_cases.jsonl.gz") if c["kind"] == "planar"]
+
+
+@pytest.fixture(scope="module")
+def conical_cases():
+    return [c for c in load_jsonl("fields1d_cases.jsonl.gz") if c["kind"] == "conical"]
+
 
 
 def golden_fields(c):
@@ -101,3 +107,55 @@ def test_empty_and_invalid_depths(eng, cases):
     for bad in (np.inf, np.nan):
         with pytest.raises(ValueError):
             eng.solve1d_fields(stack, [(c["wavelength"], c["theta"])], c["M"], 0, [0.1, bad])
+
+
+def run_conical(eng, c):
+    stack = stack_from_json(c["stack"])
+    jones = [complex(*c["jones"][0]), complex(*c["jones"][1])]
+    return eng.solve_conical_fields(stack, [(c["wavelength"], c["theta"], c["phi"])], c["M"], c["zs"], jones)
+
+
+def test_conical_fields_match_reference(eng, conical_cases):
+    worst = {}
+    for c in conical_cases:
+        arrays, fields = run_conical(eng, c)
+        assert arrays["status"][0] == 0, c["name"]
+        assert int(arrays["n_schur"][0]) == c["n_schur"], c["name"]
+        assert np.max(np.abs(arrays["DEr"][0][:, 0] - rvec(c["DEr_ss"]))) <= 1e-10, c["name"]
+        want = golden_fields(c)
+        err = np.max(np.abs(fields[0] - want) / (1.0 + np.abs(want)))
+        worst[c["name"]] = err
+        assert err <= TOL, (c["name"], err)  # the Schur case included: measured below 1e-13
+    assert len(conical_cases) >= 8
+    print("worst relative conical field difference", {k: f"{v:.2e}" for k, v in worst.items()})
+
+
+def test_conical_jones_linearity(eng, conical_cases):
+    # a common phase on the Jones vector multiplies every field by it (tests/test_rcwa_public_fields.cpp:105-107)
+    c = next(c for c in conical_cases if c["name"] == "conical_mixed_jones")
+    stack = stack_from_json(c["stack"])
+    pt = [(c["wavelength"], c["theta"], c["phi"])]
+    j = np.array([complex(*c["jones"][0]), complex(*c["jones"][1])])
+    carrier = np.exp(0.73j)
+    _, a = eng.solve_conical_fields(stack, pt, c["M"], c["zs"], j)
+    _, b = eng.solve_conical_fields(stack, pt, c["M"], c["zs"], j * carrier)
+    assert np.all(np.abs(b - carrier * a) <= 2e-12 * (1.0 + np.abs(carrier * a)))
+    # the two basis columns combine linearly (after the normalisation of the Jones vector)
+    _, s = eng.solve_conical_fields(stack, pt, c["M"], c["zs"], [1.0, 0.0])
+    _, p = eng.solve_conical_fields(stack, pt, c["M"], c["zs"], [0.0, 1.0])
+    jn = j / np.max(np.abs(np.r_[j.real, j.imag]))
+    jn = jn / np.linalg.norm(jn)
+    assert np.allclose(jn[0] * s + jn[1] * p, a, rtol=1e-11, atol=1e-12)
+    for bad in ([0.0, 0.0], [np.inf, 0.0]):
+        with pytest.raises(ValueError):
+            eng.solve_conical_fields(stack, pt, c["M"], c["zs"], bad)
+
+
+def test_conical_batch_equals_single(eng, conical_cases):
+    c = next(c for c in conical_cases if c["name"] == "conical_multi_grating")
+    stack = stack_from_json(c["stack"])
+    pts = [(0.95, -18.0, 63.0), (0.9, 5.0, 10.0), (1.1, 33.0, 80.0)]
+    _, many = eng.solve_conical_fields(stack, pts, c["M"], c["zs"], [0.0, 1.0])
+    for p, pt in enumerate(pts):
+        _, one = eng.solve_conical_fields(stack, [pt], c["M"], c["zs"], [0.0, 1.0])
+        assert np.max(np.abs(many[p] - one[0]) / (1.0 + np.abs(one[0]))) <= 1e-13
