@@ -298,6 +298,17 @@ int rcwa_gpu_fourier_coefficients(rcwa_gpu_ctx* ctx, const double* edges, const 
 int rcwa_gpu_solve2d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points,
                            int M1, int M2, int factorization, const rcwa_options* options, rcwa_result2d* out);
 
+/* 2-D solve with near fields: rcwa::solve2d_with_fields + field_at (include/stablercwa/rcwa2d_fields.hpp:356-390)
+ * at every point. Besides the results of rcwa_gpu_solve2d_batch, fields receives the harmonics of the six
+ * components at the nz depths zs: fields[((p * 6 + c) * N + j) * nz + iz], N = (2 M1 + 1)(2 M2 + 1), j the
+ * harmonic index (m + M1)(2 M2 + 1) + (n + M2), c = Ex, Ey, Ez, Hx, Hy, Hz (H is Z0 H). Region rule of
+ * rcwa2d_fields.hpp:117-124: z < 0 region I, z > the stack's bottom region II, else the first layer (zero
+ * thickness included) with z <= its bottom + 1e-12. The Jones vector of each point is not normalised (the
+ * incident |E| is its 2-norm). NaN where the point failed or hit a Rayleigh anomaly. */
+int rcwa_gpu_solve2d_fields(rcwa_gpu_ctx* ctx, const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points,
+                            int M1, int M2, int factorization, const rcwa_options* options, const double* zs, int nz,
+                            rcwa_result2d* out, rcwa_complex* fields);
+
 /* The Fourier operators Eps, Cx, Cy of one patterned layer, each N x N column-major with row and
  * column index (m+M1)(2M2+1) + (n+M2): replaces rcwa::detail2d::layer_operators
  * (include/stablercwa/rcwa2d_operators.hpp:325-429). Invalid geometry or indices return

@@ -338,18 +338,37 @@ int rcwa_gpu_fourier_coefficients(rcwa_gpu_ctx* ctx, const double* edges, const 
     return guarded(ctx, [&] { fourier_coefficients_api(ctx->stream, edges, values, K, period, hmax, method, samples, out); });
 }
 
+namespace {
+void solve2d_entry(rcwa_gpu_ctx* ctx, const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points, int M1, int M2,
+                   int factorization, const rcwa_options* options, rcwa_result2d* out, const FieldSpec* fs) {
+    if (!stack || n_points < 0 || (n_points > 0 && !points)) throw EngineError{RCWA_EINVAL, "rcwa2d: stack and points are required"};
+    if (!out || !out->Kx || !out->Ky || !out->kzI || !out->kzII || !out->Ex_r || !out->Ey_r || !out->Ez_r || !out->Ex_t ||
+        !out->Ey_t || !out->Ez_t || !out->Rs || !out->Rp || !out->Ts || !out->Tp || !out->DEr || !out->DEt ||
+        !out->prop_r || !out->prop_t || !out->status)
+        throw EngineError{RCWA_EINVAL, "rcwa2d: every result array but the optional ones is required"};
+    validate2d(*stack, points, n_points, M1, M2, factorization);
+    const Options opt = to_options(options);
+    if (n_points == 0) return;
+    solve2d_host(ctx->stream, *stack, points, n_points, M1, M2, factorization, opt, *out, chunk_bytes2d(ctx), fs);
+}
+}  // namespace
+
 int rcwa_gpu_solve2d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points,
                            int M1, int M2, int factorization, const rcwa_options* options, rcwa_result2d* out) {
+    return guarded(ctx, [&] { solve2d_entry(ctx, stack, points, n_points, M1, M2, factorization, options, out, nullptr); });
+}
+
+int rcwa_gpu_solve2d_fields(rcwa_gpu_ctx* ctx, const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points,
+                            int M1, int M2, int factorization, const rcwa_options* options, const double* zs, int nz,
+                            rcwa_result2d* out, rcwa_complex* fields) {
     return guarded(ctx, [&] {
-        if (!stack || n_points < 0 || (n_points > 0 && !points)) throw EngineError{RCWA_EINVAL, "rcwa2d: stack and points are required"};
-        if (!out || !out->Kx || !out->Ky || !out->kzI || !out->kzII || !out->Ex_r || !out->Ey_r || !out->Ez_r || !out->Ex_t ||
-            !out->Ey_t || !out->Ez_t || !out->Rs || !out->Rp || !out->Ts || !out->Tp || !out->DEr || !out->DEt ||
-            !out->prop_r || !out->prop_t || !out->status)
-            throw EngineError{RCWA_EINVAL, "rcwa2d: every result array but the optional ones is required"};
-        validate2d(*stack, points, n_points, M1, M2, factorization);
-        const Options opt = to_options(options);
-        if (n_points == 0) return;
-        solve2d_host(ctx->stream, *stack, points, n_points, M1, M2, factorization, opt, *out, chunk_bytes2d(ctx));
+        if (nz < 0 || (nz > 0 && (!zs || !fields))) throw EngineError{RCWA_EINVAL, "rcwa2d: null argument"};
+        FieldSpec fs;
+        fs.zs.assign(zs, zs + nz);
+        for (int k = 0; k < nz; ++k)
+            if (!std::isfinite(zs[k])) throw EngineError{RCWA_EINVAL, "rcwa2d: field depths must be finite"};
+        fs.out = reinterpret_cast<zc*>(fields);
+        solve2d_entry(ctx, stack, points, n_points, M1, M2, factorization, options, out, nz > 0 ? &fs : nullptr);
     });
 }
 

@@ -164,7 +164,8 @@ void validate_conical(const rcwa_stack1d& stack, const rcwa_point_conical* h_poi
 // the batched solve over host points into host result arrays, and one layer's Fourier operators.
 void validate2d(const rcwa_stack2d& stack, const rcwa_point2d* points, int n_points, int M1, int M2, int factorization);
 void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d* points, int n_points, int M1, int M2,
-                  int factorization, const Options& opt, const rcwa_result2d& out, size_t chunk_bytes);
+                  int factorization, const Options& opt, const rcwa_result2d& out, size_t chunk_bytes,
+                  const FieldSpec* fields = nullptr);  // fields->out: HOST memory, n_points x 6 x N x nz
 void layer_operators2d(cudaStream_t st, const rcwa_layer2d& layer, double Lx, double Ly, int M1, int M2,
                        int factorization, rcwa_complex* eps, rcwa_complex* cx, rcwa_complex* cy, int* singular);
 

@@ -305,6 +305,111 @@ void replace_r(DeviceScratch& mem, RState& r, RState next) {
     r = next;
 }
 
+// The field harmonics of one chunk (sample_field_2d, include/stablercwa/rcwa2d_fields.hpp:282-320): depths
+// grouped like field_region_2d (:117-124: z < 0 region I, z > z_bot region II, else the first layer with
+// z <= z_top + d + 1e-12, zero-thickness layers included), S and D per layer group, W S and V D for
+// patterned layers (block-diagonal V for homogeneous ones), the six components, Ez through Ei = Eps^-1
+// or 1/eps. The result goes to out (device, B x 6 x N x nz); failed samples get NaN.
+struct Capture2D {
+    std::vector<zc*> W, V;            // retained modes of the patterned layers
+    std::vector<RState> r_below;      // reflection below each layer (deep copies)
+    std::vector<zc*> a_plus, a_minus;  // B x 2N per layer
+};
+
+void sample_fields2d(Batch& c, const std::vector<double>& zs, const std::vector<HostLayer>& layers, double nI, cd nII,
+                     int N, int i0, const std::vector<Region>& reg, const Capture2D& cap, const std::vector<int>& patterned,
+                     const std::vector<zc*>& Ei, const zc* inc, const zc* R, const zc* T, const double* dKx, const double* dKy,
+                     const double* dk0, zc* out) {
+    const cudaStream_t st = c.st;
+    DeviceScratch& mem = *c.mem;
+    const int B = c.B, n = 2 * N, L = (int)layers.size(), nz = (int)zs.size();
+    const long long nn = (long long)n * n;
+    std::vector<double> ztop(L);
+    double z = 0.0;
+    for (int j = 0; j < L; ++j) {
+        ztop[j] = z;
+        z += layers[j].d;
+    }
+    const double zb = z;
+    std::vector<std::vector<int>> groups(L + 2);  // 0 region I, 1 region II, 2 + j layer j
+    for (int iz = 0; iz < nz; ++iz) {
+        const double zz = zs[iz];
+        int g = 1;
+        if (zz < 0.0) {
+            g = 0;
+        } else if (!(zz > zb)) {
+            for (int j = 0; j < L; ++j)
+                if (zz <= ztop[j] + layers[j].d + 1e-12) {
+                    g = 2 + j;
+                    break;
+                }
+        }
+        groups[g].push_back(iz);
+    }
+    std::vector<int> ei_of(L, -1);
+    for (size_t k = 0; k < patterned.size(); ++k) ei_of[patterned[k]] = (int)k;
+    zc* scale = mem.get<zc>(1);
+    for (int g = 0; g < L + 2; ++g) {
+        const std::vector<int>& cols = groups[g];
+        if (cols.empty()) continue;
+        const int cnt = (int)cols.size();
+        const long long tot = (long long)B * n * cnt, totN = (long long)B * N * cnt;
+        std::vector<double> local(cnt);
+        for (int k = 0; k < cnt; ++k) local[k] = g >= 2 ? zs[cols[k]] - ztop[g - 2] : zs[cols[k]];
+        double* d_z = mem.get<double>(cnt);
+        int* d_cols = mem.get<int>(cnt);
+        RCWA_CUDA(cudaMemcpyAsync(d_z, local.data(), cnt * sizeof(double), cudaMemcpyHostToDevice, st));
+        RCWA_CUDA(cudaMemcpyAsync(d_cols, cols.data(), cnt * sizeof(int), cudaMemcpyHostToDevice, st));
+        zc* F = mem.get<zc>(tot);
+        zc* G = mem.get<zc>(tot);
+        const zc* ei = nullptr;
+        cd ie{0.0, 0.0};
+        if (g < 2) {
+            const Region& m = g == 0 ? reg[0] : reg[L + 1];
+            LAUNCH(fields2d_region_kernel, nblocks(totN), kTpb, st, B, N, i0, cnt, d_z, g == 0 ? -1 : -2, zb, dk0, m.q, m.vb,
+                   inc, g == 0 ? R : T, F, G);
+            ie = g == 0 ? cd{1.0 / (nI * nI), 0.0} : cd{1.0, 0.0} / (nII * nII);
+        } else {
+            const int j = g - 2;
+            const Region& m = reg[j + 1];
+            zc* S = mem.get<zc>(tot);
+            zc* D = mem.get<zc>(tot);
+            LAUNCH(fields2d_layer_kernel, nblocks(tot), kTpb, st, B, n, cnt, d_z, layers[j].d, dk0, cap.a_plus[j],
+                   cap.a_minus[j], m.q, S, D);
+            if (m.homog) {
+                RCWA_CUDA(cudaMemcpyAsync(F, S, tot * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+                LAUNCH(bd_rows_kernel, nblocks(totN), kTpb, st, B, N, cnt, m.vb, D, G);
+                ie = cd{1.0, 0.0} / (layers[j].n * layers[j].n);
+            } else {
+                launch_zgemm(st, n, cnt, n, B, cap.W[j], n, nn, S, n, (long long)n * cnt, nullptr, 0, F, n, (long long)n * cnt,
+                             1.0, 0.0);
+                launch_zgemm(st, n, cnt, n, B, cap.V[j], n, nn, D, n, (long long)n * cnt, nullptr, 0, G, n, (long long)n * cnt,
+                             1.0, 0.0);
+                ei = Ei[ei_of[j]];
+            }
+            mem.free(S);
+            mem.free(D);
+        }
+        zc* t = mem.get<zc>(totN);
+        LAUNCH(fields2d_out_kernel, nblocks(totN), kTpb, st, B, N, cnt, nz, d_cols, dKx, dKy, F, G, t, out);
+        if (ei) {
+            zc* e = mem.get<zc>(totN);
+            launch_zgemm(st, N, cnt, N, B, ei, N, 0, t, N, (long long)N * cnt, nullptr, 0, e, N, (long long)N * cnt, 1.0, 0.0);
+            LAUNCH(fields2d_ez_kernel, nblocks(totN), kTpb, st, B, N, cnt, nz, d_cols, e, nullptr, out);
+            RCWA_CUDA(cudaStreamSynchronize(st));
+            mem.free(e);
+        } else {
+            const zc hs{ie.real(), ie.imag()};
+            RCWA_CUDA(cudaMemcpyAsync(scale, &hs, sizeof(zc), cudaMemcpyHostToDevice, st));
+            LAUNCH(fields2d_ez_kernel, nblocks(totN), kTpb, st, B, N, cnt, nz, d_cols, t, scale, out);
+            RCWA_CUDA(cudaStreamSynchronize(st));  // the host values of this group end here
+        }
+        for (void* p : {(void*)F, (void*)G, (void*)t, (void*)d_z, (void*)d_cols}) mem.free(p);
+    }
+    mem.free(scale);
+    LAUNCH(nan_fields2d_kernel, nblocks((long long)B * 6 * N * nz), kTpb, st, B, 6LL * N * nz, c.fail, out);
+}
+
 }  // namespace
 
 // ============================================================== validation (rcwa2d.hpp:928-1006, rcwa2d_operators.hpp:252-320)
@@ -401,7 +506,8 @@ void layer_operators2d(cudaStream_t st, const rcwa_layer2d& layer, double Lx, do
 // ============================================================== the solve
 
 void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d* points, int n_points, int M1, int M2,
-                  int factorization, const Options& opt, const rcwa_result2d& out, size_t chunk_bytes) {
+                  int factorization, const Options& opt, const rcwa_result2d& out, size_t chunk_bytes,
+                  const FieldSpec* fields) {
     const int n1 = 2 * M1 + 1, n2 = 2 * M2 + 1, N = n1 * n2, n = 2 * N;
     const long long NN = (long long)N * N, nn = (long long)n * n;
     const int L = stack.n_layers;
@@ -472,8 +578,18 @@ void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d
             out.DEt[(size_t)p * N + i] = nan;
         }
     };
+    const int nz = fields ? (int)fields->zs.size() : 0;
+    const size_t fper = (size_t)6 * N * nz;  // field values per point
+    auto nan_fields = [&](int p) {
+        if (nz == 0) return;
+        zc* f = fields->out + (size_t)p * fper;
+        for (size_t k = 0; k < fper; ++k) f[k] = zc{nan, nan};
+    };
     for (int p = 0; p < n_points; ++p)
-        if (out.status[p] == RCWA_SAMPLE_RAYLEIGH) nan_point(p);
+        if (out.status[p] == RCWA_SAMPLE_RAYLEIGH) {
+            nan_point(p);
+            nan_fields(p);
+        }
     if (valid.empty()) return;
 
     DeviceScratch call_mem(st);  // per-call data: operators and Ei
@@ -505,12 +621,15 @@ void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d
             if (out.n_dense_solve) out.n_dense_solve[p] = 0;
             if (out.max_eig_residual) out.max_eig_residual[p] = 0.0;
             nan_point(p);
+            nan_fields(p);
         }
         return;
     }
 
     // ---- chunk size from a per-point estimate of the device working set
-    const double per_point = 16.0 * (double)nn * (5.0 * P + 3.0 * (L + 1) + 8.0) + 64.0 * N * (L + 8);
+    double per_point = 16.0 * (double)nn * (5.0 * P + 3.0 * (L + 1) + 8.0) + 64.0 * N * (L + 8);
+    if (nz > 0)  // retained W, V and reflections, amplitudes, the field output and one depth group's buffers
+        per_point += 16.0 * ((double)nn * (2.0 * P + L) + 4.0 * n * L + 12.0 * (double)N * nz);
     const int B_max = (int)std::max(1.0, std::min((double)valid.size(), (double)chunk_bytes / per_point));
 
     for (size_t start = 0; start < valid.size(); start += B_max) {
@@ -635,6 +754,20 @@ void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d
             // Wall / Vall / qall stay allocated until the chunk ends; the per-layer views are released with them
             (void)Vall;
         }
+        Capture2D cap;
+        if (nz > 0) {  // the interface above a layer consumes its W and V; the field sampler needs them after
+            cap.W.assign(L, nullptr);
+            cap.V.assign(L, nullptr);
+            cap.r_below.assign(L, RState{});
+            cap.a_plus.assign(L, nullptr);
+            cap.a_minus.assign(L, nullptr);
+            for (int j : patterned) {
+                cap.W[j] = c.dense();
+                cap.V[j] = c.dense();
+                RCWA_CUDA(cudaMemcpyAsync(cap.W[j], reg[j + 1].W, (size_t)B * nn * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+                RCWA_CUDA(cudaMemcpyAsync(cap.V[j], reg[j + 1].V, (size_t)B * nn * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+            }
+        }
 
         // ---- bottom-up (rcwa2d.hpp:1176-1197)
         const int blocks = 2 * L + 1;
@@ -727,6 +860,16 @@ void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d
             } else {
                 // propagation in layer j (propagation_block + stack_on, rcwa2d.hpp:612-627, :706-713)
                 const Region& rg = reg[j + 1];
+                if (nz > 0) {  // the reflection below layer j's bottom (rcwa2d.hpp:1202)
+                    RState& rb = cap.r_below[j];
+                    rb.kind = r.kind;
+                    if (r.kind != R_ZERO) {
+                        const size_t cnt = r.kind == R_DENSE ? (size_t)B * nn : (size_t)B * 4 * N;
+                        rb.p = mem.get<zc>(cnt);
+                        rb.owned = true;
+                        RCWA_CUDA(cudaMemcpyAsync(rb.p, r.p, cnt * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+                    }
+                }
                 zc* gt = mem.get<zc>((size_t)B * 4 * N);
                 if (r.kind != R_DENSE) {
                     zc* rout = mem.get<zc>((size_t)B * 4 * N);
@@ -809,6 +952,11 @@ void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d
         // ---- top-down (rcwa2d.hpp:1210-1219)
         for (int b = 1; b < blocks; ++b) {
             Step& s = steps[b];
+            const int jl = b / 2;
+            if (nz > 0 && b % 2 != 0) {  // amplitude at the layer's top (rcwa2d.hpp:1221)
+                cap.a_plus[jl] = c.vec();
+                RCWA_CUDA(cudaMemcpyAsync(cap.a_plus[jl], down, (size_t)B * n * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+            }
             zc* y = c.vec();
             if (s.kind == S_BDMAT) {
                 LAUNCH(bd_apply_vec_kernel, nblocks((long long)B * N), kTpb, st, B, N, s.bd, down, y);
@@ -830,6 +978,17 @@ void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d
             for (zc* p : {s.bd, s.tm, s.nn, s.rp})
                 if (p) mem.free(p);
             s = Step{};
+            if (nz > 0 && b % 2 != 0) {  // the reflection below applied at the layer's bottom (rcwa2d.hpp:1224-1225)
+                const RState& rb = cap.r_below[jl];
+                zc* am = c.vec();
+                if (rb.kind == R_ZERO)
+                    RCWA_CUDA(cudaMemsetAsync(am, 0, (size_t)B * n * sizeof(zc), st));
+                else if (rb.kind == R_BD)
+                    LAUNCH(bd_apply_vec_kernel, nblocks((long long)B * N), kTpb, st, B, N, rb.p, down, am);
+                else
+                    LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 1, rb.p, down, nullptr, am, 1.0, 0.0);
+                cap.a_minus[jl] = am;
+            }
         }
 
         // ---- outputs (rcwa2d.hpp:1225-1270)
@@ -841,6 +1000,14 @@ void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d
         LAUNCH(finalize2d_kernel, nblocks((long long)B * N), kTpb, st, B, N, R, down, dKx, dKy, dkzI, dkzII, nI,
                zc{nII.real(), nII.imag()}, dnic, dsin, dcos, o, fail);
         LAUNCH(nan_fill2d_kernel, nblocks((long long)B * N), kTpb, st, B, N, o, fail);
+        std::vector<zc> hfields;
+        if (nz > 0) {
+            zc* fout = mem.get<zc>((size_t)B * fper);
+            RCWA_CUDA(cudaMemsetAsync(fout, 0, (size_t)B * fper * sizeof(zc), st));
+            sample_fields2d(c, fields->zs, layers, nI, nII, N, i0, reg, cap, patterned, Ei, inc, R, down, dKx, dKy, dk0, fout);
+            hfields.resize((size_t)B * fper);
+            RCWA_CUDA(cudaMemcpyAsync(hfields.data(), fout, (size_t)B * fper * sizeof(zc), cudaMemcpyDeviceToHost, st));
+        }
 
         std::vector<cd> hz[10];
         for (auto& v : hz) v.resize((size_t)B * N);
@@ -867,6 +1034,7 @@ void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d
             if (out.n_eig) out.n_eig[p] = P;
             if (out.n_dense_solve) out.n_dense_solve[p] = hinfo[b] != 0 ? P : n_solve;
             if (out.max_eig_residual) out.max_eig_residual[p] = opt.diagnostics ? hres[b] : 0.0;
+            if (nz > 0) std::memcpy(fields->out + (size_t)p * fper, hfields.data() + (size_t)b * fper, fper * sizeof(zc));
         }
     }
 }

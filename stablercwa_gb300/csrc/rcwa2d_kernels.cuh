@@ -583,5 +583,132 @@ __global__ void eig_info_layers_kernel(int B, int P, const int* __restrict__ inf
     if (first != 0) fail[b] = 1;
 }
 
+// ---------------------------------------------------------------- near fields (rcwa2d_fields.hpp:169-290)
+
+// S = p + m and D = m - p at the group's depths in layer j: p = a+ exp(-k0 q t), m = a- exp(-k0 q (d - t)),
+// t the depth below the layer's top clamped to [0, d] (layer_chunk_fields, rcwa2d_fields.hpp:209-223).
+// Per sample 2N x cnt column-major.
+__global__ void fields2d_layer_kernel(int B, int n, int cnt, const double* __restrict__ zl, double d,
+                                      const double* __restrict__ k0, const zc* __restrict__ ap, const zc* __restrict__ am,
+                                      const zc* __restrict__ q, zc* __restrict__ S, zc* __restrict__ D) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per = (long long)n * cnt;
+    if (idx >= (long long)B * per) return;
+    const long long b = idx / per;
+    const long long r = idx - b * per;
+    const int col = (int)(r / n), j = (int)(r - (long long)col * n);
+    const double from_top = fmax(0.0, fmin(d, zl[col])), from_bottom = d - from_top;
+    const double k = k0[b];
+    const zc a = ap[b * n + j], bm = am[b * n + j], qj = q[b * n + j];
+    const zc p = is_zero(a) ? zc{0.0, 0.0} : a * zexp((-k * from_top) * qj);
+    const zc m = is_zero(bm) ? zc{0.0, 0.0} : bm * zexp((-k * from_bottom) * qj);
+    S[idx] = p + m;
+    D[idx] = m - p;
+}
+
+// Y = BD X for every column of X (2N x cnt per sample; b2_apply_rows, rcwa2d.hpp:253-265)
+__global__ void bd_rows_kernel(int B, int N, int cnt, const zc* __restrict__ bd, const zc* __restrict__ X,
+                               zc* __restrict__ Y) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per = (long long)N * cnt;
+    if (idx >= (long long)B * per) return;
+    const long long b = idx / per;
+    const long long r = idx - b * per;
+    const int col = (int)(r / N), i = (int)(r - (long long)col * N);
+    const Bd l = bd_load(bd + b * 4 * N, N, i);
+    const long long base = (b * cnt + col) * 2 * N;
+    const zc x1 = X[base + i], x2 = X[base + N + i];
+    Y[base + i] = l.a11 * x1 + l.a12 * x2;
+    Y[base + N + i] = l.a21 * x1 + l.a22 * x2;
+}
+
+// F = [Ex; Ey] and G = [hx; hy] in region I (z < 0: reflected orders exp(+k0 q z), the incident (0,0)
+// order exp(-k0 q z)) or region II (transmitted exp(-k0 q (z - z_bot))), G = V v with V the region's
+// block-diagonal modes (region_I/II_chunk_fields, rcwa2d_fields.hpp:226-279). Thread per (sample, depth, i < N).
+__global__ void fields2d_region_kernel(int B, int N, int i0, int cnt, const double* __restrict__ zs, int region,
+                                       double z_bot, const double* __restrict__ k0, const zc* __restrict__ q,
+                                       const zc* __restrict__ vb, const zc* __restrict__ inc, const zc* __restrict__ amp,
+                                       zc* __restrict__ F, zc* __restrict__ G) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per = (long long)N * cnt;
+    if (idx >= (long long)B * per) return;
+    const long long b = idx / per;
+    const long long r = idx - b * per;
+    const int col = (int)(r / N), i = (int)(r - (long long)col * N);
+    const int n = 2 * N;
+    const double z = zs[col], k = k0[b];
+    zc f[2], v[2];
+    for (int h = 0; h < 2; ++h) {
+        const int j = h * N + i;
+        const zc a = amp[b * n + j], qj = q[b * n + j];
+        if (region == -1) {
+            f[h] = is_zero(a) ? zc{0.0, 0.0} : a * zexp((k * z) * qj);
+            v[h] = f[h];
+            if (i == i0) {
+                const zc in = inc[b * n + j];
+                const zc ix = is_zero(in) ? zc{0.0, 0.0} : in * zexp((-k * z) * qj);
+                f[h] = f[h] + ix;
+                v[h] = v[h] - ix;
+            }
+        } else {
+            f[h] = is_zero(a) ? zc{0.0, 0.0} : a * zexp((-k * (z - z_bot)) * qj);
+            v[h] = -f[h];
+        }
+    }
+    const Bd l = bd_load(vb + b * 4 * N, N, i);
+    const long long base = (b * cnt + col) * n;
+    F[base + i] = f[0];
+    F[base + N + i] = f[1];
+    G[base + i] = l.a11 * v[0] + l.a12 * v[1];
+    G[base + N + i] = l.a21 * v[0] + l.a22 * v[1];
+}
+
+// Ex, Ey, Hx = -i hx, Hy = -i hy, Hz = -i hz with hz = i (Ky Ex - Kx Ey) into out[b][c][j][iz]; the
+// right-hand side Ky hx - Kx hy of Ez into t (per sample N x cnt) (emit_field_chunk, rcwa2d_fields.hpp:169-205)
+__global__ void fields2d_out_kernel(int B, int N, int cnt, int nz, const int* __restrict__ cols, const double* __restrict__ Kx,
+                                    const double* __restrict__ Ky, const zc* __restrict__ F, const zc* __restrict__ G,
+                                    zc* __restrict__ t, zc* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per = (long long)N * cnt;
+    if (idx >= (long long)B * per) return;
+    const long long b = idx / per;
+    const long long r = idx - b * per;
+    const int col = (int)(r / N), j = (int)(r - (long long)col * N);
+    const long long base = (b * cnt + col) * 2 * N;
+    const zc ex = F[base + j], ey = F[base + N + j], hx = G[base + j], hy = G[base + N + j];
+    const double kx = Kx[b * N + j], ky = Ky[b * N + j];
+    const zc w = ky * ex - kx * ey;
+    const zc hz{-w.im, w.re};  // i (Ky Ex - Kx Ey)
+    const long long cstride = (long long)N * nz;
+    zc* o = out + b * 6LL * N * nz + (long long)j * nz + cols[col];
+    o[0 * cstride] = ex;
+    o[1 * cstride] = ey;
+    o[3 * cstride] = zc{hx.im, -hx.re};
+    o[4 * cstride] = zc{hy.im, -hy.re};
+    o[5 * cstride] = zc{hz.im, -hz.re};
+    t[idx] = ky * hx - kx * hy;
+}
+
+// Ez = i (Ei t) (e = Ei t given) or i (inv_eps t) into out[b][2][j][iz]
+__global__ void fields2d_ez_kernel(int B, int N, int cnt, int nz, const int* __restrict__ cols, const zc* __restrict__ e,
+                                   const zc* inv_eps, zc* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per = (long long)N * cnt;
+    if (idx >= (long long)B * per) return;
+    const long long b = idx / per;
+    const long long r = idx - b * per;
+    const int col = (int)(r / N), j = (int)(r - (long long)col * N);
+    const zc v = inv_eps ? *inv_eps * e[idx] : e[idx];
+    out[b * 6LL * N * nz + 2LL * N * nz + (long long)j * nz + cols[col]] = zc{-v.im, v.re};
+}
+
+__global__ void nan_fields2d_kernel(int B, long long per, const int* __restrict__ fail, zc* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * per) return;
+    if (!fail[idx / per]) return;
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    out[idx] = zc{nan, nan};
+}
+
 }  // namespace
 }  // namespace rcwa_gb300

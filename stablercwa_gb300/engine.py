@@ -72,6 +72,8 @@ def load_library(build_if_missing=True):
                                                 vp, vp, ci, C.POINTER(abi.rcwa_result_conical), vp]
     L.rcwa_gpu_solve2d_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack2d), vp, ci, ci, ci, ci,
                                          C.POINTER(abi.rcwa_options), C.POINTER(abi.rcwa_result2d)]
+    L.rcwa_gpu_solve2d_fields.argtypes = [vp, C.POINTER(abi.rcwa_stack2d), vp, ci, ci, ci, ci, C.POINTER(abi.rcwa_options),
+                                          vp, ci, C.POINTER(abi.rcwa_result2d), vp]
     L.rcwa_gpu_layer_operators2d.argtypes = [vp, C.POINTER(abi.rcwa_layer2d), cd, cd, ci, ci, ci, vp, vp, vp, vp]
     L.rcwa_gpu_server_create.argtypes = [C.POINTER(abi.rcwa_server_config), C.POINTER(vp)]
     L.rcwa_gpu_server_destroy.argtypes = [vp]
@@ -277,6 +279,21 @@ class Engine:
         self._check(self.L.rcwa_gpu_solve2d_batch(self.h, C.byref(st), C.cast(pts, C.c_void_p), len(points), M1, M2,
                                                   fact, C.byref(o), C.byref(res)))
         return arrays
+
+    def solve2d_fields(self, stack, points, M1, M2, zs, laurent=False, options=None):
+        """rcwa::solve2d_with_fields + field_at(result, zs) at every (wavelength, theta_deg, phi_deg, Es, Ep)
+        point: (result arrays, fields (P, 6, N, nz)), N = (2 M1 + 1)(2 M2 + 1)."""
+        st, keep = abi.marshal_stack2d(stack)
+        pts = abi.points2d_array(points)
+        N = (2 * M1 + 1) * (2 * M2 + 1)
+        res, arrays = abi.result2d_views(len(points), N, len(stack.layers))
+        z = np.ascontiguousarray(np.asarray(zs, dtype=np.float64).reshape(-1))
+        fields = np.empty((len(points), 6, N, len(z)), np.complex128)
+        o = _options(options)
+        fact = abi.RCWA_FACTORIZATION_LAURENT if laurent else abi.RCWA_FACTORIZATION_LI
+        self._check(self.L.rcwa_gpu_solve2d_fields(self.h, C.byref(st), C.cast(pts, C.c_void_p), len(points), M1, M2, fact,
+                                                   C.byref(o), z.ctypes.data, len(z), C.byref(res), fields.ctypes.data))
+        return arrays, fields
 
     def solve2d(self, stack, wavelength, theta_deg, phi_deg, M1, M2, jones, laurent=False, options=None):
         """One rcwa::solve2d (include/stablercwa/rcwa2d.hpp:1359): arrays of that point, plus the

@@ -25,6 +25,7 @@ EXPORTERS = [
     ("export_rcwa2d.cpp", "rcwa2d_cases.jsonl.gz"),
     ("export_fft.cpp", "fft_cases.jsonl"),
     ("export_fields.cpp", "fields1d_cases.jsonl.gz"),
+    ("export_fields2d.cpp", "fields2d_cases.jsonl.gz"),
 ]
 
 

@@ -50,3 +50,18 @@ def test_repeated_and_clipped_depths():
         # zs = .083, -.12, .42, .2, .2+5e-13, .42+5e-13, .083, .245, 0, 100, -100
         assert np.array_equal(f[:, :, 0], f[:, :, 6])
         assert np.array_equal(f[:, :, 3], f[:, :, 4])
+
+
+def test_fields2d_fixture_pinned_to_frozen_python():
+    # the reference's C++ harmonics agree with the frozen harmonics of its Python authority within the
+    # tolerances frozen beside them (tests/test_rcwa2d_fields.cpp:270-290)
+    cases = load_jsonl("fields2d_cases.jsonl.gz")
+    frozen = [c for c in cases if "frozen" in c]
+    assert len(frozen) >= 20
+    for c in frozen:
+        got, want = fields(c), np.array([[[complex(*z) for z in row] for row in comp] for comp in c["frozen"]])
+        assert got.shape == want.shape
+        assert np.all(np.abs(got - want) <= c["near_atol"] + c["near_rtol"] * np.abs(want)), c["name"]
+    for c in cases:
+        assert c["status"] == 0 and c["available"] == 1
+        assert fields(c).shape == (6, (2 * c["M1"] + 1) * (2 * c["M2"] + 1), len(c["zs"]))

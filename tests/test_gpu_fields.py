@@ -13,6 +13,8 @@ pytestmark = pytest.mark.gpu
 # close() (tests/test_rcwa_public_fields.cpp:24) and at its tolerance; the largest difference measured
 # on these stacks is below 1e-13.
 TOL = 5e-12
+# 2-D: the same bound (measured worst 2.5e-13, over the reference's frozen cases and problems A-C)
+TOL2D = TOL
 
 
 @pytest.fixture(scope="module")
@@ -159,3 +161,41 @@ def test_conical_batch_equals_single(eng, conical_cases):
     for p, pt in enumerate(pts):
         _, one = eng.solve_conical_fields(stack, [pt], c["M"], c["zs"], [0.0, 1.0])
         assert np.max(np.abs(many[p] - one[0]) / (1.0 + np.abs(one[0]))) <= 1e-13
+
+
+def test_fields2d_match_reference(eng):
+    from stablercwa_gb300.types import stack2d_from_json
+    worst = {}
+    for c in load_jsonl("fields2d_cases.jsonl.gz"):
+        stack = stack2d_from_json(c["stack"])
+        jones = [complex(*c["jones"][0]), complex(*c["jones"][1])]
+        arrays, fields = eng.solve2d_fields(stack, [(c["wavelength"], c["theta"], c["phi"], jones[0], jones[1])], c["M1"],
+                                            c["M2"], c["zs"], laurent=bool(c["laurent"]))
+        assert arrays["status"][0] == 0, c["name"]
+        assert np.max(np.abs(arrays["DEr"][0] - rvec(c["DEr"]))) <= 1e-10, c["name"]
+        want = golden_fields(c)
+        err = np.max(np.abs(fields[0] - want) / (1.0 + np.abs(want)))
+        worst[c["name"]] = err
+        if "frozen" in c:  # and the frozen Python harmonics within their own tolerances
+            fz = np.array([[[complex(*z) for z in row] for row in comp] for comp in c["frozen"]])
+            assert np.all(np.abs(fields[0] - fz) <= c["near_atol"] + c["near_rtol"] * np.abs(fz)), c["name"]
+    print("worst relative 2-D field difference", {k: f"{v:.2e}" for k, v in worst.items()})
+    for name, err in worst.items():
+        assert err <= TOL2D, (name, err)
+    assert len(worst) >= 28
+
+
+def test_fields2d_failure_and_depth_checks(eng):
+    from stablercwa_gb300.types import stack2d_from_json
+    c = next(c for c in load_jsonl("fields2d_cases.jsonl.gz") if c["name"] == "problem_a")
+    stack = stack2d_from_json(c["stack"])
+    jones = [complex(*c["jones"][0]), complex(*c["jones"][1])]
+    pt = (c["wavelength"], c["theta"], c["phi"], jones[0], jones[1])
+    with pytest.raises(ValueError):
+        eng.solve2d_fields(stack, [pt], 1, 1, [0.1, np.nan])
+    arrays, f = eng.solve2d_fields(stack, [pt], 1, 1, [])
+    assert f.shape == (1, 6, 9, 0) and arrays["status"][0] == 0
+    # a point that fails with max_iter = 1 carries NaN fields; the other point of the batch is unaffected
+    from stablercwa_gb300.types import Options
+    arrays, f = eng.solve2d_fields(stack, [pt], 1, 1, [0.1, 0.5], options=Options(eig_max_iter=1))
+    assert arrays["status"][0] != 0 and np.isnan(f).all()
