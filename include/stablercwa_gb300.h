@@ -38,6 +38,7 @@ extern "C" {
 #define RCWA_EUNSUPPORTED (-4) /* option value the engine does not implement */
 #define RCWA_ESCRATCH (-5)     /* problem larger than rcwa_gpu_eig_batch_static's fixed workspace */
 #define RCWA_ETIMEOUT (-6)     /* rcwa_gpu_server_wait: the request has not finished yet */
+#define RCWA_ENUMERIC (-7)     /* non-finite result where the reference throws std::runtime_error */
 
 /* per-sample status word */
 #define RCWA_SAMPLE_OK 0
@@ -308,6 +309,40 @@ int rcwa_gpu_solve2d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack2d* stack, const r
 int rcwa_gpu_solve2d_fields(rcwa_gpu_ctx* ctx, const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points,
                             int M1, int M2, int factorization, const rcwa_options* options, const double* zs, int nz,
                             rcwa_result2d* out, rcwa_complex* fields);
+
+/* Real-space slice of one point's field harmonics: rcwa::field_slice / field_map
+ * (detail::reconstruct_field_slice and reconstruct_field_grid, include/stablercwa/rcwa_fields.hpp:326-385).
+ * harmonics: host, 6 x n x nz in the layout of the field entries above ([(c * n + j) * nz + iz]); kx, ky: the
+ * physical wavevector components of each harmonic (the reference's kxm and, per harmonic, its ky: the constant
+ * k0 ky of a 1-D solve, kyn of a 2-D one). The horizontal axis is x (RCWA_SLICE_XZ, y = at) or y
+ * (RCWA_SLICE_YZ, x = at) at t_it = (it / nt) period. out: host, 6 x nz x nt, out[(c * nz + iz) * nt + it],
+ * the value at (t_it, z_iz) = sum_j exp(-i (kx_j x + ky_j y)) harmonics[c][j][iz]. nt <= 0, a non-finite
+ * at or a non-positive period is RCWA_EINVAL; a non-finite carrier or result is RCWA_ENUMERIC. */
+#define RCWA_SLICE_XZ 0
+#define RCWA_SLICE_YZ 1
+int rcwa_gpu_field_slice(rcwa_gpu_ctx* ctx, const rcwa_complex* harmonics, int n, int nz, const double* kx,
+                         const double* ky, int plane, int nt, double period, double at, rcwa_complex* out);
+
+/* Phase map of one complex scalar grid: rcwa::phase_data (include/stablercwa/rcwa_phase.hpp:229-271).
+ * field: host, nz x nt, field[iz * nt + it]. reference: RCWA_PHASE_ABSOLUTE, RCWA_PHASE_INCIDENT (the carrier
+ * exp(i (-kx0 x_it - ky0 y_it + kz0 z_iz)) with incident_k = {kx0, ky0, kz0}, the real parts of the incident
+ * order's physical wavevector, and the grid coordinates x, y (nt each) and z (nz)) or RCWA_PHASE_CUSTOM
+ * (custom: nz x nt values, already broadcast). A value is masked when it is non-finite, its amplitude is at
+ * most phase_floor times the largest finite amplitude, or its reference is non-finite or zero. unwrap: none,
+ * along the horizontal axis, along z, or both (horizontal first). Outputs (host, nz x nt): phase (NaN where
+ * masked), amplitude, mask (1 = masked) and, when reference_out != NULL and a reference is used, the
+ * reference. */
+#define RCWA_PHASE_ABSOLUTE 0
+#define RCWA_PHASE_INCIDENT 1
+#define RCWA_PHASE_CUSTOM 2
+#define RCWA_UNWRAP_NONE 0
+#define RCWA_UNWRAP_X 1
+#define RCWA_UNWRAP_Z 2
+#define RCWA_UNWRAP_BOTH 3
+int rcwa_gpu_phase_data(rcwa_gpu_ctx* ctx, const rcwa_complex* field, int nt, int nz, int reference,
+                        const double* incident_k, const double* x, const double* y, const double* z,
+                        const rcwa_complex* custom, double phase_floor, int unwrap, double* phase, double* amplitude,
+                        unsigned char* mask, rcwa_complex* reference_out);
 
 /* The Fourier operators Eps, Cx, Cy of one patterned layer, each N x N column-major with row and
  * column index (m+M1)(2M2+1) + (n+M2): replaces rcwa::detail2d::layer_operators

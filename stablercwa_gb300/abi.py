@@ -306,6 +306,10 @@ def result2d_views(n_points, N, n_layers):
 # ---------------------------------------------------------------- serving
 
 RCWA_ETIMEOUT = -6
+RCWA_ENUMERIC = -7
+RCWA_SLICE_XZ, RCWA_SLICE_YZ = 0, 1
+RCWA_PHASE_ABSOLUTE, RCWA_PHASE_INCIDENT, RCWA_PHASE_CUSTOM = 0, 1, 2
+RCWA_UNWRAP_NONE, RCWA_UNWRAP_X, RCWA_UNWRAP_Z, RCWA_UNWRAP_BOTH = 0, 1, 2, 3
 RCWA_REQ_1D = 0
 RCWA_REQ_CONICAL = 1
 RCWA_REQ_2D = 2

@@ -333,6 +333,21 @@ int rcwa_gpu_solve1d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const r
     });
 }
 
+int rcwa_gpu_field_slice(rcwa_gpu_ctx* ctx, const rcwa_complex* harmonics, int n, int nz, const double* kx,
+                         const double* ky, int plane, int nt, double period, double at, rcwa_complex* out) {
+    return guarded(ctx, [&] { field_slice_api(ctx->stream, harmonics, n, nz, kx, ky, plane, nt, period, at, out); });
+}
+
+int rcwa_gpu_phase_data(rcwa_gpu_ctx* ctx, const rcwa_complex* field, int nt, int nz, int reference,
+                        const double* incident_k, const double* x, const double* y, const double* z,
+                        const rcwa_complex* custom, double phase_floor, int unwrap, double* phase, double* amplitude,
+                        unsigned char* mask, rcwa_complex* reference_out) {
+    return guarded(ctx, [&] {
+        phase_data_api(ctx->stream, field, nt, nz, reference, incident_k, x, y, z, custom, phase_floor, unwrap, phase,
+                       amplitude, mask, reference_out);
+    });
+}
+
 int rcwa_gpu_fourier_coefficients(rcwa_gpu_ctx* ctx, const double* edges, const rcwa_complex* values, int K,
                                   double period, int hmax, int method, int samples, rcwa_complex* out) {
     return guarded(ctx, [&] { fourier_coefficients_api(ctx->stream, edges, values, K, period, hmax, method, samples, out); });

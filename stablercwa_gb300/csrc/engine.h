@@ -169,6 +169,13 @@ void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d
 void layer_operators2d(cudaStream_t st, const rcwa_layer2d& layer, double Lx, double Ly, int M1, int M2,
                        int factorization, rcwa_complex* eps, rcwa_complex* cx, rcwa_complex* cy, int* singular);
 
+// Field slices and phase maps (fields_post.cu).
+void field_slice_api(cudaStream_t st, const rcwa_complex* harmonics, int n, int nz, const double* kx, const double* ky,
+                     int plane, int nt, double period, double at, rcwa_complex* out);
+void phase_data_api(cudaStream_t st, const rcwa_complex* field, int nt, int nz, int reference, const double* incident_k,
+                    const double* x, const double* y, const double* z, const rcwa_complex* custom, double phase_floor,
+                    int unwrap, double* phase, double* amplitude, unsigned char* mask, rcwa_complex* reference_out);
+
 // Coefficients of one piecewise-constant profile, closed form (method 0) or FFT-sampled (method 1).
 void fourier_coefficients_api(cudaStream_t st, const double* edges, const rcwa_complex* values, int K, double period,
                               int hmax, int method, int samples, rcwa_complex* out);

@@ -74,6 +74,8 @@ def load_library(build_if_missing=True):
                                          C.POINTER(abi.rcwa_options), C.POINTER(abi.rcwa_result2d)]
     L.rcwa_gpu_solve2d_fields.argtypes = [vp, C.POINTER(abi.rcwa_stack2d), vp, ci, ci, ci, ci, C.POINTER(abi.rcwa_options),
                                           vp, ci, C.POINTER(abi.rcwa_result2d), vp]
+    L.rcwa_gpu_field_slice.argtypes = [vp, vp, ci, ci, vp, vp, ci, ci, cd, cd, vp]
+    L.rcwa_gpu_phase_data.argtypes = [vp, vp, ci, ci, ci, vp, vp, vp, vp, vp, cd, ci, vp, vp, vp, vp]
     L.rcwa_gpu_layer_operators2d.argtypes = [vp, C.POINTER(abi.rcwa_layer2d), cd, cd, ci, ci, ci, vp, vp, vp, vp]
     L.rcwa_gpu_server_create.argtypes = [C.POINTER(abi.rcwa_server_config), C.POINTER(vp)]
     L.rcwa_gpu_server_destroy.argtypes = [vp]
@@ -172,12 +174,61 @@ class Engine:
                                                    z.ctypes.data, len(z), C.byref(res), fields.ctypes.data))
         return arrays, fields
 
-    def field_map(self, fields, kxm, period, nx=256, y=0.0):
-        """Real-space field on an x grid from harmonics (reconstruct_field_grid, rcwa_fields.hpp:326-355):
-        fields (6, n, nz) of one point, kxm the physical kx of each order; returns (6, nz, nx)."""
-        x = np.arange(nx) / nx * period
-        carrier = np.exp(-1j * (np.outer(x, kxm)))
-        return np.einsum("xj,cjz->czx", carrier, fields)
+    def field_slice(self, fields, kx, ky, plane, nt, period, at=0.0):
+        """Real-space slice of one point's harmonics on the device (rcwa::field_slice, reconstruct_field_slice,
+        rcwa_fields.hpp:357-385): fields (6, n, nz), kx and ky the physical wavevector of each harmonic (ky a
+        scalar for a 1-D solve), plane abi.RCWA_SLICE_XZ (y = at) or RCWA_SLICE_YZ (x = at); returns
+        (6, nz, nt) at t = (it / nt) period."""
+        h = np.ascontiguousarray(fields, dtype=np.complex128)
+        n, nz = h.shape[1], h.shape[2]
+        kxa = np.ascontiguousarray(np.broadcast_to(np.asarray(kx, dtype=np.float64), (n,)))
+        kya = np.ascontiguousarray(np.broadcast_to(np.asarray(ky, dtype=np.float64), (n,)))
+        out = np.empty((6, nz, int(nt)), np.complex128)
+        self._check(self.L.rcwa_gpu_field_slice(self.h, h.ctypes.data, n, nz, kxa.ctypes.data, kya.ctypes.data, int(plane),
+                                                int(nt), float(period), float(at), out.ctypes.data))
+        return out
+
+    def field_map(self, fields, kxm, period, nx=256, y=0.0, ky=0.0):
+        """The x-z map of rcwa::field_map (reconstruct_field_grid, rcwa_fields.hpp:326-355) on the device:
+        fields (6, n, nz) of one point, kxm the physical kx of each order, ky the physical ky (0 for a planar
+        solve, k0 ky for a conical one); returns (6, nz, nx)."""
+        return self.field_slice(fields, kxm, ky, abi.RCWA_SLICE_XZ, nx, period, y)
+
+    def phase_data(self, field, reference="absolute", phase_floor=1e-6, unwrap="none", incident_k=None, x=None, y=None,
+                   z=None, custom=None):
+        """rcwa::phase_data of one complex grid (nz, nt) on the device (rcwa_phase.hpp:229-271): dict of phase
+        (NaN where masked), amplitude, mask and reference, each (nz, nt). reference: "absolute", "incident"
+        (incident_k = (kx0, ky0, kz0) and the grid coordinates x, y (nt) and z (nz)) or "custom" (custom
+        broadcast to the grid like numpy). unwrap: "none", "x", "z" or "both"."""
+        f = np.ascontiguousarray(field, dtype=np.complex128)
+        nz, nt = f.shape
+        kinds = {"absolute": abi.RCWA_PHASE_ABSOLUTE, "incident": abi.RCWA_PHASE_INCIDENT, "custom": abi.RCWA_PHASE_CUSTOM}
+        axes = {"none": abi.RCWA_UNWRAP_NONE, "x": abi.RCWA_UNWRAP_X, "t": abi.RCWA_UNWRAP_X, "horizontal": abi.RCWA_UNWRAP_X,
+                "z": abi.RCWA_UNWRAP_Z, "vertical": abi.RCWA_UNWRAP_Z, "both": abi.RCWA_UNWRAP_BOTH}
+        kind = kinds[reference] if isinstance(reference, str) else int(reference)
+        ax = axes[unwrap] if isinstance(unwrap, str) else int(unwrap)
+        keep = []
+
+        def arr(v, dtype, shape=None):
+            if v is None:
+                return None
+            a = np.asarray(v, dtype=dtype)
+            if shape is not None:
+                a = np.broadcast_to(a, shape)
+            a = np.ascontiguousarray(a)
+            keep.append(a)
+            return a.ctypes.data
+        out = {"phase": np.empty((nz, nt)), "amplitude": np.empty((nz, nt)), "mask": np.empty((nz, nt), np.uint8),
+               "reference": np.empty((nz, nt), np.complex128)}
+        self._check(self.L.rcwa_gpu_phase_data(
+            self.h, f.ctypes.data, nt, nz, kind, arr(incident_k, np.float64), arr(x, np.float64), arr(y, np.float64),
+            arr(z, np.float64), arr(custom, np.complex128, (nz, nt)) if custom is not None else None, float(phase_floor), ax,
+            out["phase"].ctypes.data, out["amplitude"].ctypes.data, out["mask"].ctypes.data,
+            out["reference"].ctypes.data if kind != abi.RCWA_PHASE_ABSOLUTE else None))
+        out["mask"] = out["mask"].astype(bool)
+        if kind == abi.RCWA_PHASE_ABSOLUTE:
+            out["reference"] = None
+        return out
 
     def solve1d_device(self, stack, d_points, n_points, M, pol, d_out, options=None):
         """Batched solve on device memory. d_points: device address of n_points (wavelength, theta)

@@ -26,6 +26,7 @@ EXPORTERS = [
     ("export_fft.cpp", "fft_cases.jsonl"),
     ("export_fields.cpp", "fields1d_cases.jsonl.gz"),
     ("export_fields2d.cpp", "fields2d_cases.jsonl.gz"),
+    ("export_phase.cpp", "phase_cases.jsonl.gz"),
 ]
 
 

@@ -65,3 +65,31 @@ def test_fields2d_fixture_pinned_to_frozen_python():
     for c in cases:
         assert c["status"] == 0 and c["available"] == 1
         assert fields(c).shape == (6, (2 * c["M1"] + 1) * (2 * c["M2"] + 1), len(c["zs"]))
+
+
+def test_phase_fixture_pinned_to_frozen_python():
+    # the reference's slices and phase maps agree with the frozen arrays of its Python authority by the
+    # reference test's own criteria (tests/test_rcwa2d_fields.cpp:332-395)
+    seen = 0
+    for c in load_jsonl("phase_cases.jsonl.gz"):
+        if c["kind"] != "slice2d":
+            continue
+        cv = lambda v: np.array([complex(*z) for z in v])
+        got, frozen = cv(c["slice"]), cv(c["frozen_slice"])
+        assert np.all(np.abs(got - frozen) <= c["near_atol"] + c["near_rtol"] * np.abs(frozen)), c["name"]
+        n = c["nz"] * c["nt"]
+        fmask = np.frombuffer(c["frozen_mask"].encode(), np.uint8) == ord("1")
+        fcmp = np.frombuffer(c["frozen_comparison"].encode(), np.uint8) == ord("1")
+        for comp in range(6):
+            sl = slice(comp * n, (comp + 1) * n)
+            for key, fkey in (("abs", "frozen_phase_absolute"), ("inc", "frozen_phase_incident")):
+                mask = np.frombuffer(c[f"{key}{comp}_mask"].encode(), np.uint8) == ord("1")
+                assert np.array_equal(mask, fmask[sl]), (c["name"], comp, key)
+                use = ~fcmp[sl]
+                ph = np.array([float(x) for x in c[f"{key}{comp}_phase"]])[use]
+                want = np.array([float(x) for x in c[fkey]])[sl][use]
+                amp = np.abs(frozen[sl][use])
+                chord = np.abs(np.exp(1j * ph) - np.exp(1j * want))
+                assert np.all(chord <= 2.0 * (c["near_atol"] + c["near_rtol"] * amp) / amp + 5e-14), (c["name"], comp, key)
+        seen += 1
+    assert seen == 14
