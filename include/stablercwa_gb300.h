@@ -462,6 +462,24 @@ int rcwa_gpu_server_submit(rcwa_gpu_server* server, const rcwa_request* request,
  * kind; may be NULL) and releases it. Returns RCWA_OK, or RCWA_ETIMEOUT if it has not finished. */
 int rcwa_gpu_server_wait(rcwa_gpu_server* server, unsigned long long ticket, int timeout_ms, rcwa_response* response,
                          void* result);
+/* ---- JSON front end ------------------------------------------------------------------------- */
+
+/* rcwa::solve_json_reply (include/stablercwa/rcwa_json.hpp:1287-1309): one JSON request (mode "planar",
+ * "conical" or "periodic2d"; one point or a "points" array) in, one JSON reply out, in the reference's wire
+ * format: {"ok": true, "version": 1, "mode", "M", ["My",] "orders", "threads", "results": [...]} with the
+ * reference's per-point fields and order, or {"ok": false, "error": message, "where": field path} for a
+ * request error (unknown keys, invalid values, and the options this engine does not implement: eig "lr",
+ * linear "lu_nopivot" / "qr", homogeneous_fast_path false, backend "mkl"). Numbers are the engine's results
+ * written with the shortest round-trip decimal (NaN and infinities as null). indent < 0: one line; >= 0:
+ * objects one item per line. *reply is allocated here (free it with rcwa_json_free); *ok (may be NULL) is the
+ * reply's "ok". rcwa_gpu_solve_json runs all points as one batched call on ctx; rcwa_gpu_server_solve_json
+ * submits one serving-loop request per point and waits for them; rcwa_json_validate only checks the request
+ * (*reply is "" when it is valid) and needs no device. Return RCWA_OK whenever a reply was produced. */
+int rcwa_gpu_solve_json(rcwa_gpu_ctx* ctx, const char* request, int indent, char** reply, int* ok);
+int rcwa_gpu_server_solve_json(rcwa_gpu_server* server, const char* request, int indent, char** reply, int* ok);
+int rcwa_json_validate(const char* request, int indent, char** reply, int* ok);
+void rcwa_json_free(char* reply);
+
 #ifdef __cplusplus
 }
 #endif

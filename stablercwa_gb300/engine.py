@@ -74,6 +74,10 @@ def load_library(build_if_missing=True):
                                          C.POINTER(abi.rcwa_options), C.POINTER(abi.rcwa_result2d)]
     L.rcwa_gpu_solve2d_fields.argtypes = [vp, C.POINTER(abi.rcwa_stack2d), vp, ci, ci, ci, ci, C.POINTER(abi.rcwa_options),
                                           vp, ci, C.POINTER(abi.rcwa_result2d), vp]
+    for name in ("rcwa_gpu_solve_json", "rcwa_gpu_server_solve_json"):
+        getattr(L, name).argtypes = [vp, C.c_char_p, ci, C.POINTER(C.c_void_p), C.POINTER(ci)]
+    L.rcwa_json_validate.argtypes = [C.c_char_p, ci, C.POINTER(C.c_void_p), C.POINTER(ci)]
+    L.rcwa_json_free.argtypes = [C.c_void_p]
     L.rcwa_gpu_field_slice.argtypes = [vp, vp, ci, ci, vp, vp, ci, ci, cd, cd, vp]
     L.rcwa_gpu_phase_data.argtypes = [vp, vp, ci, ci, ci, vp, vp, vp, vp, vp, cd, ci, vp, vp, vp, vp]
     L.rcwa_gpu_layer_operators2d.argtypes = [vp, C.POINTER(abi.rcwa_layer2d), cd, cd, ci, ci, ci, vp, vp, vp, vp]
@@ -173,6 +177,11 @@ class Engine:
         self._check(self.L.rcwa_gpu_solve1d_fields(self.h, C.byref(st), pts.ctypes.data, len(pts), M, pol, C.byref(o),
                                                    z.ctypes.data, len(z), C.byref(res), fields.ctypes.data))
         return arrays, fields
+
+    def solve_json(self, request, indent=-1):
+        """rcwa::solve_json_reply (include/stablercwa/rcwa_json.hpp:1287-1309) on this context, every point
+        of the request in one batched call: (ok, reply text)."""
+        return _json_call(self.L.rcwa_gpu_solve_json, self.h, request, indent)
 
     def field_slice(self, fields, kx, ky, plane, nt, period, at=0.0):
         """Real-space slice of one point's harmonics on the device (rcwa::field_slice, reconstruct_field_slice,
@@ -422,6 +431,27 @@ class Engine:
         return c.transpose(0, 2, 1)
 
 
+def _json_call(fn, handle, request, indent):
+    L = load_library()
+    out = C.c_void_p()
+    ok = C.c_int(0)
+    args = ([handle] if handle is not None else []) + [request.encode("utf-8"), int(indent), C.byref(out), C.byref(ok)]
+    rc = fn(*args)
+    if rc != 0:
+        raise EngineError(rc, "JSON front end failed")
+    try:
+        text = C.cast(out, C.c_char_p).value.decode("utf-8")
+    finally:
+        L.rcwa_json_free(out)
+    return bool(ok.value), text
+
+
+def json_validate(request, indent=-1):
+    """Checks a JSON request like the reference's reader (rcwa_json.hpp:739-800) without solving it:
+    (True, "") when it is valid, else (False, the reference's error reply). Needs no GPU."""
+    return _json_call(load_library().rcwa_json_validate, None, request, indent)
+
+
 def rayleigh_message(stack, r, M1, M2):
     """Regions and (m, n) orders with kz exactly 0, listed as the reference lists them
     (report_rayleigh, include/stablercwa/rcwa2d.hpp:1012-1026), in English."""
@@ -469,6 +499,10 @@ class Server:
             self.close()
         except Exception:
             pass
+
+    def solve_json(self, request, indent=-1):
+        """The JSON front end on the serving loop: one request per point, run on the worker slots; (ok, reply)."""
+        return _json_call(self.L.rcwa_gpu_server_solve_json, self.h, request, indent)
 
     def _submit(self, req, meta):
         t = C.c_ulonglong()

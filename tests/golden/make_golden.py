@@ -27,6 +27,7 @@ EXPORTERS = [
     ("export_fields.cpp", "fields1d_cases.jsonl.gz"),
     ("export_fields2d.cpp", "fields2d_cases.jsonl.gz"),
     ("export_phase.cpp", "phase_cases.jsonl.gz"),
+    ("export_json.cpp", "json_cases.jsonl.gz"),
 ]
 
 
