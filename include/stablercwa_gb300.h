@@ -252,10 +252,12 @@ int rcwa_gpu_solve1d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const r
  * field components at the nz depths zs (z = 0 at the top of the first layer, increasing downwards; z < 0
  * the incident medium, z past the last layer the exit medium; a depth on an interface belongs to the
  * layer above): fields[((p * 6 + c) * (2M+1) + j) * nz + iz], c = Ex, Ey, Ez, Hx, Hy, Hz (H is Z0 H),
- * j the order m + M. Taken from the modes and amplitudes of the same solve; NaN where the point failed. */
+ * j the order m + M. Taken from the modes and amplitudes of the same solve; NaN where the point failed.
+ * layer_info (optional, n_points x n_layers): the number of the layer's modes with q exactly 0, which the
+ * reference propagates in its finite-zero basis (FieldLayerInfo::finite_zero_mode_count). */
 int rcwa_gpu_solve1d_fields(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point1d* points, int n_points,
                             int M, int polarization, const rcwa_options* options, const double* zs, int nz,
-                            rcwa_result1d* out, rcwa_complex* fields);
+                            rcwa_result1d* out, rcwa_complex* fields, int* layer_info);
 
 /* Same solve with device-resident sweep points and device-resident result arrays (every pointer in
  * out is a device pointer). The stack description is host memory. Asynchronous with respect to the
@@ -278,10 +280,12 @@ int rcwa_gpu_solve_conical_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, c
  * (include/stablercwa/rcwa1d_conical_fields.hpp:52-97, :243-248) at every point. jones: 2 complex per
  * point (Es, Ep of the incident field), normalised like rcwa::normalized_jones (rcwa_fields.hpp:218-230);
  * nullptr means (1, 0) everywhere; a non-finite or zero Jones vector is RCWA_EINVAL. Depths and the
- * layout of fields are those of rcwa_gpu_solve1d_fields; NaN where the point failed. */
+ * layout of fields are those of rcwa_gpu_solve1d_fields; NaN where the point failed. layer_info (optional,
+ * n_points x n_layers): 1 where the layer took the Schur basis at that point (FieldPropagation::Schur). */
 int rcwa_gpu_solve_conical_fields(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point_conical* points,
                                   int n_points, int M, const rcwa_options* options, const rcwa_complex* jones,
-                                  const double* zs, int nz, rcwa_result_conical* out, rcwa_complex* fields);
+                                  const double* zs, int nz, rcwa_result_conical* out, rcwa_complex* fields,
+                                  int* layer_info);
 
 /* Fourier coefficients c[h + hmax], h = -hmax..hmax, of a piecewise-constant profile (K values, K + 1
  * increasing edges spanning one period). method 0: the closed form (rcwa::detail::fourier_coefficients,
@@ -479,6 +483,22 @@ int rcwa_gpu_solve_json(rcwa_gpu_ctx* ctx, const char* request, int indent, char
 int rcwa_gpu_server_solve_json(rcwa_gpu_server* server, const char* request, int indent, char** reply, int* ok);
 int rcwa_json_validate(const char* request, int indent, char** reply, int* ok);
 void rcwa_json_free(char* reply);
+
+/* The near-field protocol, rcwa::solve_fields_json_reply (include/stablercwa/rcwa_fields_json.hpp):
+ * {"solve": <a one-point request of rcwa_gpu_solve_json; conical needs an "input">, "sampling": {"z": [...],
+ * "nx": n, "y": y} (planar / conical) or {"z": [...], "plane": "xz" | "yz", "nt": n, "at": a} (periodic2d),
+ * "output_dir": a directory that must not exist yet, "request_id": a 1..128 byte token}. The point is solved
+ * with its fields on ctx; the map / slice at the depths and its absolute and incident-referenced phase maps
+ * (floor 1e-6, not unwrapped) are formed on the device and written as fields.npy <c16 [6, nz, n],
+ * phase.npy <f8 [2, 6, nz, n], phase_mask.npy |u1 [2, 6, nz, n], x.npy (and t.npy, y.npy in 2-D) and z.npy
+ * into a temporary sibling directory that is renamed onto output_dir at the end. The reply is the far-field
+ * reply of that point followed by "protocol": "stablercwa-fields" and the "field_data" manifest; a failed
+ * solve, a non-finite sample or an existing output_dir gives {"ok": false, ..., "where": "fields"} and
+ * publishes nothing. Reply handling as rcwa_gpu_solve_json. */
+int rcwa_gpu_solve_fields_json(rcwa_gpu_ctx* ctx, const char* request, int indent, char** reply, int* ok);
+/* The request checks of rcwa_gpu_solve_fields_json alone (no solve, no files, no device): *reply is "" when
+ * the request is valid, else the error reply. */
+int rcwa_fields_json_validate(const char* request, int indent, char** reply, int* ok);
 
 #ifdef __cplusplus
 }

@@ -446,13 +446,16 @@ void conical_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_poin
     d.flux_t = mem.get<double>(nv);
     FieldSpec dfs;
     const size_t nf = fs ? (size_t)n_points * 6 * n * fs->zs.size() : 0;
+    const size_t ni = fs && fs->layer_info ? (size_t)n_points * stack->n_layers : 0;
     if (fs) {
         dfs.zs = fs->zs;
         dfs.jones = fs->jones;
         dfs.out = nf > 0 ? mem.get<zc>(nf) : nullptr;
+        dfs.layer_info = ni > 0 ? mem.zeros<int>(ni) : nullptr;
     }
-    solve_conical_device(st, *stack, P, n_points, M, opt, d, chunk_bytes(ctx), fs && nf > 0 ? &dfs : nullptr);
+    solve_conical_device(st, *stack, P, n_points, M, opt, d, chunk_bytes(ctx), fs && (nf > 0 || ni > 0) ? &dfs : nullptr);
     if (nf > 0) copy_back(fs->out, dfs.out, nf, st);
+    if (ni > 0) copy_back(fs->layer_info, dfs.layer_info, ni, st);
     copy_back(out->Jr, d.Jr, nv * 4, st);
     copy_back(out->Jt, d.Jt, nv * 4, st);
     copy_back(out->DEr, d.DEr, nv * 4, st);
@@ -479,7 +482,8 @@ int rcwa_gpu_solve_conical_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, c
 
 int rcwa_gpu_solve_conical_fields(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point_conical* points,
                                   int n_points, int M, const rcwa_options* options, const rcwa_complex* jones,
-                                  const double* zs, int nz, rcwa_result_conical* out, rcwa_complex* fields) {
+                                  const double* zs, int nz, rcwa_result_conical* out, rcwa_complex* fields,
+                                  int* layer_info) {
     return guarded(ctx, [&] {
         if (nz < 0 || (nz > 0 && (!zs || !fields)) || n_points < 0) throw EngineError{RCWA_EINVAL, "rcwa: null argument"};
         FieldSpec fs;
@@ -505,13 +509,14 @@ int rcwa_gpu_solve_conical_fields(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, 
             }
         }
         fs.out = reinterpret_cast<zc*>(fields);
+        fs.layer_info = layer_info;  // host here; conical_batch stages it on the device
         conical_batch(ctx, stack, points, n_points, M, options, out, &fs);
     });
 }
 
 int rcwa_gpu_solve1d_fields(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point1d* points, int n_points,
                             int M, int polarization, const rcwa_options* options, const double* zs, int nz,
-                            rcwa_result1d* out, rcwa_complex* fields) {
+                            rcwa_result1d* out, rcwa_complex* fields, int* layer_info) {
     return guarded(ctx, [&] {
         if (!stack || (n_points > 0 && !points) || n_points < 0 || nz < 0 || (nz > 0 && (!zs || !fields)))
             throw EngineError{RCWA_EINVAL, "rcwa: null argument"};
@@ -547,7 +552,11 @@ int rcwa_gpu_solve1d_fields(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const 
         FieldSpec fs;
         fs.zs.assign(zs, zs + nz);
         fs.out = nz > 0 ? mem.get<zc>(nf) : nullptr;
-        solve1d_device(st, *stack, ds, dw, n_points, M, polarization, opt, d, chunk_bytes(ctx), nz > 0 ? &fs : nullptr);
+        const size_t ni = (size_t)n_points * stack->n_layers;
+        if (layer_info && ni > 0) fs.layer_info = mem.zeros<int>(ni);
+        solve1d_device(st, *stack, ds, dw, n_points, M, polarization, opt, d, chunk_bytes(ctx),
+                       nz > 0 || fs.layer_info ? &fs : nullptr);
+        if (fs.layer_info) copy_back(layer_info, fs.layer_info, ni, st);
         copy_back(out->R, d.R, nv, st);
         copy_back(out->T, d.T, nv, st);
         copy_back(out->DEr, d.DEr, nv, st);

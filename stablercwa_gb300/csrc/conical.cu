@@ -1445,6 +1445,18 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                 LAUNCH(conical_clear_unexcited_kernel, nblocks(2 * nv), kTpb, st, 2 * nv, n, N, M, cur);
             }
             sample_conical_fields(c, *fields, layers, stack, M, p0, modes, cap, rud, cur, kx, P.ky, cs, sn, kzI, kzII, k0);
+            if (fields->layer_info) {  // per original layer: 1 where it took the Schur basis
+                const int LO = stack.n_layers;
+                RCWA_CUDA(cudaMemset2DAsync(fields->layer_info + (size_t)p0 * LO, LO * sizeof(int), 0, LO * sizeof(int), B, st));
+                for (int k = 0, e = 0; k < LO; ++k) {
+                    if (!(stack.layers[k].d > 0.0)) continue;
+                    const Region& m = modes[e + 1];
+                    if (m.schur)
+                        RCWA_CUDA(cudaMemcpy2DAsync(fields->layer_info + (size_t)p0 * LO + k, LO * sizeof(int), m.schur, sizeof(int),
+                                                    sizeof(int), B, cudaMemcpyDeviceToDevice, st));
+                    ++e;
+                }
+            }
         }
         mem.release();
     }

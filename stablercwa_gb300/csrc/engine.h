@@ -141,6 +141,8 @@ struct FieldSpec {
     std::vector<double> zs;
     zc* out = nullptr;
     std::vector<std::complex<double>> jones;  // conical: normalised (Es, Ep) per point; empty = (1, 0)
+    int* layer_info = nullptr;  // optional, device, n_points x stack layers: planar the number of modes with q
+                                // exactly 0 (finite-zero basis), conical 1 where the layer took the Schur basis
 };
 void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_s, const double* d_wl, int n_points,
                     int M, int pol, const Options& opt, const rcwa_result1d& d_out, size_t chunk_bytes, const FieldSpec* fields = nullptr);

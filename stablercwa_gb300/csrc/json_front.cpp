@@ -15,6 +15,10 @@
 // rcwa_gpu_solve2d_batch, rcwa_gpu_server_submit / wait).
 #include <algorithm>
 #include <chrono>
+#include <filesystem>
+#include <fstream>
+#include <random>
+#include <stdexcept>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -814,7 +818,361 @@ double sum(const double* v, std::size_t n) {
     return s;
 }
 
-std::string run_planar(const Request& rq, Runner& run, int indent) {
+// ------------------------------------------------------------------ near-field protocol (rcwa_fields_json.hpp)
+//
+// {"solve": <one-point request>, "sampling": {...}, "output_dir": "...", "request_id": "..."}: the one point is
+// solved with its fields, the x-z map (1-D: nx points at y) or the x-z / y-z slice (2-D: nt points at `at`)
+// is formed on the device at the requested depths, with its absolute and incident-referenced phase maps
+// (floor 1e-6, no unwrapping), and written as NPY files into a new directory published by one rename.
+
+constexpr std::size_t kFieldsMaxSamples = 4000000;
+
+struct FieldsRequest {
+    Request solve;
+    std::vector<double> z;
+    int nx = 0, nt = 0;
+    double y = 0.0, at = 0.0;
+    int plane = RCWA_SLICE_XZ;
+    std::filesystem::path output_dir;
+    std::string id;
+};
+
+struct FieldsJob {
+    const FieldsRequest* fr = nullptr;
+    std::vector<rcwa_complex> harmonics;  // 6 x n x nz
+    std::vector<int> layer_info;          // per layer (1-D and conical)
+    double solve_seconds = 0.0;
+};
+
+// rcwa_fields_json.hpp:68-151
+FieldsRequest read_fields_request(const Value& root) {
+    need_object(root, "");
+    check_keys(root, "", {"solve", "sampling", "output_dir", "request_id"});
+    FieldsRequest fr;
+    fr.solve = read_request(member(root, "solve", ""));
+    if (fr.solve.points.size() != 1) fail("solve.points", "fields 协议每次只接受一个入射点");
+    if (fr.solve.mode == Mode::Conical && fr.solve.input == Input::None)
+        fail("solve.input", "圆锥场采样必须指定入射 Jones 或偏振角");
+    const Value& sampling = member(root, "sampling", "");
+    need_object(sampling, "sampling");
+    if (fr.solve.mode == Mode::Periodic2D) {
+        check_keys(sampling, "sampling", {"z", "plane", "nt", "at"});
+        const std::string plane = text(member(sampling, "plane", "sampling"), "sampling.plane");
+        if (plane == "xz") fr.plane = RCWA_SLICE_XZ;
+        else if (plane == "yz") fr.plane = RCWA_SLICE_YZ;
+        else fail("sampling.plane", "只能是 \"xz\"（固定 y，沿 x）或 \"yz\"（固定 x，沿 y）");
+        fr.nt = integer(member(sampling, "nt", "sampling"), "sampling.nt");
+        if (fr.nt < 1) fail("sampling.nt", "必须是正整数");
+        const Value& depths = member(sampling, "z", "sampling");
+        need_array(depths, "sampling.z");
+        if (depths.size() == 0 || depths.size() > kFieldsMaxSamples / static_cast<std::size_t>(fr.nt))
+            fail("sampling", "采样网格为空或超过 4000000 个点");
+        for (std::size_t j = 0; j < depths.size(); ++j) {
+            fr.z.push_back(number(depths.at(j), child("sampling.z", j)));
+            if (!std::isfinite(fr.z.back())) fail(child("sampling.z", j), "必须是有限的数");
+        }
+        if (const Value* at = sampling.find("at")) {
+            fr.at = number(*at, "sampling.at");
+            if (!std::isfinite(fr.at)) fail("sampling.at", "必须是有限的数");
+        }
+    } else {
+        check_keys(sampling, "sampling", {"z", "nx", "y"});
+        fr.nx = integer(member(sampling, "nx", "sampling"), "sampling.nx");
+        if (fr.nx < 1) fail("sampling.nx", "必须是正整数");
+        const Value& depths = member(sampling, "z", "sampling");
+        need_array(depths, "sampling.z");
+        if (depths.size() == 0 || depths.size() > kFieldsMaxSamples / static_cast<std::size_t>(fr.nx))
+            fail("sampling", "采样网格为空或超过 4000000 个点");
+        for (std::size_t j = 0; j < depths.size(); ++j) fr.z.push_back(number(depths.at(j), child("sampling.z", j)));
+        if (const Value* y = sampling.find("y")) fr.y = number(*y, "sampling.y");
+        if (fr.solve.mode != Mode::Conical && fr.y != 0.0) fail("sampling.y", "planar 场采样的 y 必须是 0");
+    }
+    const std::string path = text(member(root, "output_dir", ""), "output_dir");
+    if (path.empty() || path.find('\0') != std::string::npos) fail("output_dir", "输出目录不能为空或含 NUL");
+    fr.output_dir = std::filesystem::absolute(std::filesystem::u8path(path)).lexically_normal();
+    if (fr.output_dir.filename().empty()) fail("output_dir", "必须是本次新建的子目录");
+    fr.id = text(member(root, "request_id", ""), "request_id");
+    if (fr.id.empty() || fr.id.size() > 128) fail("request_id", "必须是 1 到 128 字节的本次请求标记");
+    return fr;
+}
+
+// A temporary sibling directory, renamed onto the requested one when everything is written; removed otherwise.
+class DirectoryOutput {
+public:
+    explicit DirectoryOutput(const std::filesystem::path& final_path) : final_(final_path) {
+        namespace fs = std::filesystem;
+        if (fs::exists(final_)) throw std::invalid_argument("fields 输出目录已存在，拒绝覆盖历史文件");
+        if (!fs::is_directory(final_.parent_path())) throw std::invalid_argument("fields 输出目录的父目录不存在");
+        std::random_device random;
+        for (int attempt = 0; attempt < 20; ++attempt) {
+            temporary_ = final_.parent_path() /
+                         fs::u8path(final_.filename().u8string() + ".tmp-" + std::to_string(random()) + "-" + std::to_string(random()));
+            if (fs::create_directory(temporary_)) {
+                owned_ = true;
+                return;
+            }
+        }
+        throw std::runtime_error("fields 不能建立临时输出目录");
+    }
+    ~DirectoryOutput() {
+        if (owned_) {
+            std::error_code ignored;
+            std::filesystem::remove_all(temporary_, ignored);
+        }
+    }
+    DirectoryOutput(const DirectoryOutput&) = delete;
+    DirectoryOutput& operator=(const DirectoryOutput&) = delete;
+    std::filesystem::path file(const char* name) const { return temporary_ / name; }
+    void publish() {
+        if (std::filesystem::exists(final_)) throw std::runtime_error("fields 输出目录在发布前已存在");
+        std::filesystem::rename(temporary_, final_);
+        owned_ = false;
+    }
+
+private:
+    std::filesystem::path final_, temporary_;
+    bool owned_ = false;
+};
+
+// NPY version 1.0: magic, header length, the dict padded so the data starts on a 64-byte boundary, then the
+// little-endian data in C order.
+void write_npy(const std::filesystem::path& path, const char* dtype, const std::vector<std::size_t>& shape, const void* data,
+               std::size_t bytes) {
+    std::string tuple = "(";
+    for (std::size_t d : shape) tuple += std::to_string(d) + ", ";
+    tuple += ")";
+    std::string header = std::string("{'descr': '") + dtype + "', 'fortran_order': False, 'shape': " + tuple + ", }";
+    header.append((64 - (10 + header.size() + 1) % 64) % 64, ' ');
+    header += '\n';
+    const unsigned char prefix[10] = {0x93, 'N', 'U', 'M', 'P', 'Y', 1, 0, static_cast<unsigned char>(header.size() & 255),
+                                      static_cast<unsigned char>(header.size() >> 8)};
+    std::ofstream out(path, std::ios::binary | std::ios::trunc);
+    if (!out) throw std::runtime_error("NPY: cannot create output file");
+    out.write(reinterpret_cast<const char*>(prefix), sizeof prefix);
+    out.write(header.data(), static_cast<std::streamsize>(header.size()));
+    out.write(static_cast<const char*>(data), static_cast<std::streamsize>(bytes));  // this build's hosts are little-endian
+    out.close();
+    if (!out) throw std::runtime_error("NPY: writing output failed");
+}
+
+void write_shape(Writer& w, const std::vector<std::size_t>& shape) {
+    w.begin_array(true);
+    for (std::size_t d : shape) w.value(static_cast<long long>(d));
+    w.end_array();
+}
+void write_file(Writer& w, const char* key, const char* name, const char* dtype, const std::vector<std::size_t>& shape) {
+    w.key(key);
+    w.begin_object(true);
+    w.key("name");
+    w.value(name);
+    w.key("dtype");
+    w.value(dtype);
+    w.key("shape");
+    write_shape(w, shape);
+    w.end_object();
+}
+
+// Everything after the far-field result: slice, phases, files, manifest (rcwa_fields_json.hpp:156-301, :303-459).
+// kx, ky: the physical wavevector of each harmonic; kinc: real (kx, ky, kz) of the incident order; layers:
+// (original index, effective index, z_top, z_bottom, finite-zero modes, Schur) per stack layer.
+struct LayerRow {
+    long long original;
+    int effective;
+    double z_top, z_bottom;
+    int finite_zero;
+    bool schur;
+};
+void fields_tail(Writer& w, rcwa_gpu_ctx* ctx, FieldsJob& fj, const std::vector<double>& kx, const std::vector<double>& ky,
+                 const double kinc[3], double period, double norm_E, double norm_H, const std::vector<LayerRow>& layers) {
+    using Clock = std::chrono::steady_clock;
+    const FieldsRequest& fr = *fj.fr;
+    const bool two_d = fr.solve.mode == Mode::Periodic2D;
+    const int n = static_cast<int>(kx.size()), nz = static_cast<int>(fr.z.size());
+    const int nt = two_d ? fr.nt : fr.nx;
+    const int plane = two_d ? fr.plane : RCWA_SLICE_XZ;
+    const double at = two_d ? fr.at : fr.y;
+    DirectoryOutput output(fr.output_dir);
+    auto started = Clock::now();
+    std::vector<rcwa_complex> grid((std::size_t)6 * nz * nt);
+    int rc = rcwa_gpu_field_slice(ctx, fj.harmonics.data(), n, nz, kx.data(), ky.data(), plane, nt, period, at, grid.data());
+    if (rc == RCWA_ENUMERIC) throw std::runtime_error("fields 采样产生非有限复场，拒绝发布");
+    if (rc != RCWA_OK) throw std::runtime_error("fields 采样失败：rcwa_gb300 error " + std::to_string(rc));
+    for (const rcwa_complex& v : grid)
+        if (!std::isfinite(v.re) || !std::isfinite(v.im)) throw std::runtime_error("fields 采样产生非有限复场，拒绝发布");
+    const double sample_seconds = std::chrono::duration<double>(Clock::now() - started).count();
+    std::vector<double> t(nt), x(nt), y(nt);
+    for (int it = 0; it < nt; ++it) {
+        t[it] = (static_cast<double>(it) / nt) * period;
+        x[it] = plane == RCWA_SLICE_XZ ? t[it] : at;
+        y[it] = plane == RCWA_SLICE_XZ ? at : t[it];
+    }
+    const std::size_t plane_size = static_cast<std::size_t>(nz) * nt;
+    std::vector<double> phase(2 * 6 * plane_size), amplitude(plane_size);
+    std::vector<unsigned char> mask(2 * 6 * plane_size);
+    started = Clock::now();
+    for (int reference = 0; reference < 2; ++reference)
+        for (int c = 0; c < 6; ++c) {
+            const std::size_t off = (static_cast<std::size_t>(reference) * 6 + c) * plane_size;
+            rc = rcwa_gpu_phase_data(ctx, &grid[c * plane_size], nt, nz, reference == 0 ? RCWA_PHASE_ABSOLUTE : RCWA_PHASE_INCIDENT,
+                                     kinc, x.data(), y.data(), fr.z.data(), nullptr, 1e-6, RCWA_UNWRAP_NONE, &phase[off],
+                                     amplitude.data(), &mask[off], nullptr);
+            if (rc != RCWA_OK) throw std::runtime_error("fields 相位计算失败：rcwa_gb300 error " + std::to_string(rc));
+        }
+    const double phase_seconds = std::chrono::duration<double>(Clock::now() - started).count();
+    started = Clock::now();
+    const std::size_t sz = static_cast<std::size_t>(nz), snt = static_cast<std::size_t>(nt);
+    write_npy(output.file("fields.npy"), "<c16", {6, sz, snt}, grid.data(), grid.size() * sizeof(rcwa_complex));
+    write_npy(output.file("phase.npy"), "<f8", {2, 6, sz, snt}, phase.data(), phase.size() * sizeof(double));
+    write_npy(output.file("phase_mask.npy"), "|u1", {2, 6, sz, snt}, mask.data(), mask.size());
+    if (two_d) {
+        write_npy(output.file("t.npy"), "<f8", {snt}, t.data(), snt * sizeof(double));
+        write_npy(output.file("x.npy"), "<f8", {snt}, x.data(), snt * sizeof(double));
+        write_npy(output.file("y.npy"), "<f8", {snt}, y.data(), snt * sizeof(double));
+    } else {
+        write_npy(output.file("x.npy"), "<f8", {snt}, x.data(), snt * sizeof(double));
+    }
+    write_npy(output.file("z.npy"), "<f8", {sz}, fr.z.data(), sz * sizeof(double));
+    const double write_seconds = std::chrono::duration<double>(Clock::now() - started).count();
+
+    w.key("protocol");
+    w.value("stablercwa-fields");
+    w.key("field_data");
+    w.begin_object();
+    w.key("version");
+    w.value(1);
+    w.key("producer");
+    w.value("stablercwa.cpp.rcwa_fields");
+    w.key("request_id");
+    w.value(fr.id);
+    w.key("directory");
+    w.value(fr.output_dir.u8string());
+    w.key("layout");
+    w.value("C");
+    w.key("shape");
+    write_shape(w, {sz, snt});
+    w.key("components");
+    w.begin_array(true);
+    for (const char* name : {"Ex", "Ey", "Ez", "Hx", "Hy", "Hz"}) w.value(name);
+    w.end_array();
+    if (two_d) {
+        w.key("slice");
+        w.begin_object(true);
+        w.key("plane");
+        w.value(plane == RCWA_SLICE_XZ ? "xz" : "yz");
+        w.key("at");
+        w.value(at);
+        w.key("period");
+        w.value(period);
+        w.end_object();
+        w.key("harmonics");
+        w.begin_object(true);
+        w.key("M");
+        w.value(fr.solve.M);
+        w.key("My");
+        w.value(fr.solve.My);
+        w.key("N");
+        w.value(static_cast<long long>(n));
+        w.end_object();
+    } else {
+        w.key("y");
+        w.value(fr.y);
+    }
+    w.key("phase");
+    w.begin_object(true);
+    w.key("references");
+    w.begin_array(true);
+    w.value("absolute");
+    w.value("incident");
+    w.end_array();
+    w.key("floor");
+    w.value(1e-6);
+    w.key("unwrap");
+    w.value("none");
+    w.key("unit");
+    w.value("rad");
+    w.key("mask_true");
+    w.value("undefined");
+    w.end_object();
+    w.key("normalization");
+    w.begin_object(true);
+    w.key("E");
+    w.value(norm_E);
+    w.key("H");
+    w.value(norm_H);
+    w.key("H_convention");
+    w.value("Z0 H_physical");
+    w.end_object();
+    w.key("files");
+    w.begin_object();
+    write_file(w, "fields", "fields.npy", "<c16", {6, sz, snt});
+    write_file(w, "phase", "phase.npy", "<f8", {2, 6, sz, snt});
+    write_file(w, "phase_mask", "phase_mask.npy", "|u1", {2, 6, sz, snt});
+    if (two_d) {
+        write_file(w, "t", "t.npy", "<f8", {snt});
+        write_file(w, "x", "x.npy", "<f8", {snt});
+        write_file(w, "y", "y.npy", "<f8", {snt});
+    } else {
+        write_file(w, "x", "x.npy", "<f8", {snt});
+    }
+    write_file(w, "z", "z.npy", "<f8", {sz});
+    w.end_object();
+    w.key("layers");
+    w.begin_array();
+    for (const LayerRow& L : layers) {
+        w.begin_object(true);
+        w.key("original_index");
+        w.value(L.original);
+        w.key("effective_index");
+        w.value(L.effective);
+        w.key("z_top");
+        w.value(L.z_top);
+        w.key("z_bottom");
+        w.value(L.z_bottom);
+        w.key("finite_zero_modes");
+        w.value(L.finite_zero);
+        w.key("schur");
+        w.value(L.schur);
+        w.end_object();
+    }
+    w.end_array();
+    w.key("timing");
+    w.begin_object(true);
+    w.key("solve");
+    w.value(fj.solve_seconds);
+    w.key("sample");
+    w.value(sample_seconds);
+    w.key("phase");
+    w.value(phase_seconds);
+    w.key("write");
+    w.value(write_seconds);
+    w.end_object();
+    w.end_object();
+    w.end_object();
+    output.publish();
+}
+
+// z_top / z_bottom per stack layer, effective indices skipping zero thickness when skip_zero
+template <class Layers>
+std::vector<LayerRow> layer_rows(const Layers& layers, bool skip_zero, const std::vector<int>& info, bool info_is_schur) {
+    std::vector<LayerRow> rows;
+    double z = 0.0;
+    int effective = 0;
+    for (std::size_t j = 0; j < layers.size(); ++j) {
+        LayerRow r{};
+        r.original = static_cast<long long>(j);
+        r.effective = skip_zero && layers[j].d == 0.0 ? -1 : effective++;
+        r.z_top = z;
+        z += layers[j].d;
+        r.z_bottom = z;
+        const int v = j < info.size() ? info[j] : 0;
+        r.finite_zero = info_is_schur ? 0 : v;
+        r.schur = info_is_schur && v != 0;
+        rows.push_back(r);
+    }
+    return rows;
+}
+
+std::string run_planar(const Request& rq, Runner& run, int indent, FieldsJob* fj = nullptr) {
     const int n = 2 * rq.M + 1;
     const std::size_t P = rq.points.size();
     Marshal1 m(rq.stack);
@@ -849,8 +1207,16 @@ std::string run_planar(const Request& rq, Runner& run, int indent) {
     } req{rq, m, res, o, n, run.server};
     run.run(P, [&] {
         rcwa_result1d v = res.view(0, n);
+        if (fj) {  // one point with its fields at the requested depths
+            const int nz = static_cast<int>(fj->fr->z.size());
+            fj->harmonics.resize((std::size_t)6 * n * nz);
+            fj->layer_info.assign(std::max<std::size_t>(1, rq.stack.layers.size()), 0);
+            return rcwa_gpu_solve1d_fields(run.ctx, &m.st, pts.data(), 1, rq.M, rq.polarization, &o, fj->fr->z.data(), nz, &v,
+                                           fj->harmonics.data(), fj->layer_info.data());
+        }
         return rcwa_gpu_solve1d_batch(run.ctx, &m.st, pts.data(), static_cast<int>(P), rq.M, rq.polarization, &o, &v);
     }, req);
+    if (fj && res.status[0] != RCWA_SAMPLE_OK) throw std::logic_error("rcwa: planar field context is unavailable");
     Writer w(indent);
     write_head(w, rq);
     for (std::size_t p = 0; p < P; ++p) {
@@ -875,6 +1241,20 @@ std::string run_planar(const Request& rq, Runner& run, int indent) {
         w.end_object();
     }
     w.end_array();
+    if (fj) {
+        // metadata of the planar fields (rcwa1d_fields.hpp:55-103): kxm = k0 kx, ky = 0, kzI from the incident mode
+        const PointSpec& pt = rq.points[0];
+        const double k0 = 2.0 * kPi / pt.wavelength, nI = rq.stack.nI.real();
+        const double s0 = nI * std::sin(pt.theta_deg * kPi / 180.0);
+        std::vector<double> kx(n), ky(n, 0.0);
+        for (int j = 0; j < n; ++j) kx[j] = k0 * (s0 - (j - rq.M) * pt.wavelength / rq.stack.period);
+        const double kinc[3] = {kx[rq.M], 0.0, k0 * std::sqrt((nI - s0) * (nI + s0))};
+        const bool te = rq.polarization == RCWA_TE;
+        fj->solve_seconds = run.seconds[0];
+        fields_tail(w, run.ctx, *fj, kx, ky, kinc, rq.stack.period, te ? 1.0 : 1.0 / nI, te ? nI : 1.0,
+                    layer_rows(rq.stack.layers, false, fj->layer_info, false));
+        return w.take();
+    }
     w.end_object();
     return w.take();
 }
@@ -897,7 +1277,7 @@ cd longitudinal0(cd n, double nI, double cosine) {
     return kz;
 }
 
-std::string run_conical(const Request& rq, Runner& run, int indent) {
+std::string run_conical(const Request& rq, Runner& run, int indent, FieldsJob* fj = nullptr) {
     const int n = 2 * rq.M + 1;
     const std::size_t P = rq.points.size();
     Marshal1 m(rq.stack);
@@ -931,8 +1311,23 @@ std::string run_conical(const Request& rq, Runner& run, int indent) {
     } req{rq, m, res, o, n, run.server};
     run.run(P, [&] {
         rcwa_result_conical v = res.view(0, n);
+        if (fj) {  // one point with its fields, for the request's input polarization
+            const int nz = static_cast<int>(fj->fr->z.size());
+            fj->harmonics.resize((std::size_t)6 * n * nz);
+            fj->layer_info.assign(std::max<std::size_t>(1, rq.stack.layers.size()), 0);
+            cd Es = rq.Es, Ep = rq.Ep;
+            if (rq.input == Input::Angles) {
+                const double psi = rq.psi_deg * kPi / 180.0, delta = rq.delta_deg * kPi / 180.0;
+                Es = std::sin(psi) * cd{std::cos(delta), std::sin(delta)};
+                Ep = cd{std::cos(psi), 0.0};
+            }
+            const rcwa_complex jones[2] = {{Es.real(), Es.imag()}, {Ep.real(), Ep.imag()}};
+            return rcwa_gpu_solve_conical_fields(run.ctx, &m.st, pts.data(), 1, rq.M, &o, jones, fj->fr->z.data(), nz, &v,
+                                                 fj->harmonics.data(), fj->layer_info.data());
+        }
         return rcwa_gpu_solve_conical_batch(run.ctx, &m.st, pts.data(), static_cast<int>(P), rq.M, &o, &v);
     }, req);
+    if (fj && res.status[0] != RCWA_SAMPLE_OK) throw std::logic_error("rcwa: conical field context is unavailable");
 
     const double nI = rq.stack.nI.real();
     Writer w(indent);
@@ -1068,6 +1463,18 @@ std::string run_conical(const Request& rq, Runner& run, int indent) {
         w.end_object();
     }
     w.end_array();
+    if (fj) {
+        // metadata of the conical fields (rcwa1d_conical_fields.hpp:52-97): kxm = k0 kx, ky = k0 ky
+        const PointSpec& pt = rq.points[0];
+        const double k0 = 2.0 * kPi / pt.wavelength, nI = rq.stack.nI.real();
+        std::vector<double> kx(n), ky(n, k0 * res.ky[0]);
+        for (int j = 0; j < n; ++j) kx[j] = k0 * res.kx[j];
+        const cd kz0 = longitudinal0(rq.stack.nI, nI, std::cos(pt.theta_deg * kPi / 180.0));
+        const double kinc[3] = {kx[rq.M], k0 * res.ky[0], (k0 * kz0).real()};
+        fj->solve_seconds = run.seconds[0];
+        fields_tail(w, run.ctx, *fj, kx, ky, kinc, rq.stack.period, 1.0, nI, layer_rows(rq.stack.layers, true, fj->layer_info, true));
+        return w.take();
+    }
     w.end_object();
     return w.take();
 }
@@ -1124,7 +1531,7 @@ std::string message_2d(const Request& rq, Grid2& g, std::size_t p, int N) {
     return "数值失败：求解中出现奇异的线性方程组或 NaN/Inf";
 }
 
-std::string run_periodic2d(const Request& rq, Runner& run, int indent) {
+std::string run_periodic2d(const Request& rq, Runner& run, int indent, FieldsJob* fj = nullptr) {
     const int N = (2 * rq.M + 1) * (2 * rq.My + 1);
     const std::size_t P = rq.points.size();
     Marshal2 m(rq.stack2d);
@@ -1167,8 +1574,18 @@ std::string run_periodic2d(const Request& rq, Runner& run, int indent) {
     } req{rq, m, g, o, pts, N, fact, run.server};
     run.run(P, [&] {
         rcwa_result2d v = g.view(0, N);
+        if (fj) {
+            const int nz = static_cast<int>(fj->fr->z.size());
+            fj->harmonics.resize((std::size_t)6 * N * nz);
+            return rcwa_gpu_solve2d_fields(run.ctx, &m.st, pts.data(), 1, rq.M, rq.My, fact, &o, fj->fr->z.data(), nz, &v,
+                                           fj->harmonics.data());
+        }
         return rcwa_gpu_solve2d_batch(run.ctx, &m.st, pts.data(), static_cast<int>(P), rq.M, rq.My, fact, &o, &v);
     }, req);
+    if (fj && g.status[0] != RCWA_SAMPLE_OK) {  // rcwa_fields_json.hpp:313-314
+        const std::string why = message_2d(rq, g, 0, N);
+        throw std::runtime_error(why.empty() ? std::string("fields 求解失败") : why);
+    }
 
     Writer w(indent);
     write_head(w, rq);
@@ -1258,6 +1675,25 @@ std::string run_periodic2d(const Request& rq, Runner& run, int indent) {
         w.end_object();
     }
     w.end_array();
+    if (fj) {
+        // metadata of the 2-D fields (rcwa2d_fields.hpp:138-177): kxm = k0 Kx, kyn = k0 Ky, |E_inc| = |Jones|
+        const PointSpec& pt = rq.points[0];
+        const double k0 = 2.0 * kPi / pt.wavelength;
+        std::vector<double> kx(N), ky(N);
+        for (int i = 0; i < N; ++i) {
+            kx[i] = k0 * g.Kx[i];
+            ky[i] = k0 * g.Ky[i];
+        }
+        const int i0 = rq.M * (2 * rq.My + 1) + rq.My;
+        const cd kz0{g.kzI[i0].re, g.kzI[i0].im};
+        const double kinc[3] = {kx[i0], ky[i0], (k0 * kz0).real()};
+        const double jn = std::hypot(std::abs(rq.Es), std::abs(rq.Ep));
+        fj->solve_seconds = run.seconds[0];
+        const double period = fj->fr->plane == RCWA_SLICE_XZ ? rq.stack2d.Lx : rq.stack2d.Ly;
+        fields_tail(w, run.ctx, *fj, kx, ky, kinc, period, jn, rq.stack2d.nI * jn,
+                    layer_rows(rq.stack2d.layers, false, std::vector<int>{}, false));
+        return w.take();
+    }
     w.end_object();
     return w.take();
 }
@@ -1302,6 +1738,42 @@ std::string answer(const char* request, int indent, Runner* run, bool& ok) {
     return "{\"ok\": false, \"error\": \"out of memory\", \"where\": \"\"}";
 }
 
+// rcwa::solve_fields_json_reply (rcwa_fields_json.hpp:462-474); never throws
+std::string answer_fields(const char* request, int indent, rcwa_gpu_ctx* ctx, bool& ok) {
+    ok = false;
+    try {
+        try {
+            Value root;
+            try {
+                root = jtext::parse(request ? std::string(request) : std::string());
+            } catch (const jtext::ParseError& e) {
+                throw std::invalid_argument("json: " + e.reason + " at offset " + std::to_string(e.offset) + " (line " +
+                                            std::to_string(e.line) + ", column " + std::to_string(e.column) + ")");
+            }
+            const FieldsRequest fr = read_fields_request(root);
+            if (!ctx) {  // validation only
+                ok = true;
+                return "";
+            }
+            Runner run;
+            run.ctx = ctx;
+            FieldsJob fj;
+            fj.fr = &fr;
+            std::string reply = fr.solve.mode == Mode::Periodic2D ? run_periodic2d(fr.solve, run, indent, &fj)
+                                : fr.solve.mode == Mode::Conical  ? run_conical(fr.solve, run, indent, &fj)
+                                                                  : run_planar(fr.solve, run, indent, &fj);
+            ok = true;
+            return reply;
+        } catch (const RequestError& e) {
+            return error_reply(e.message, e.where, indent);
+        } catch (const std::exception& e) {
+            return error_reply(e.what(), "fields", indent);
+        }
+    } catch (...) {
+    }
+    return "{\"ok\": false, \"error\": \"fields 未识别的求解或输出错误\", \"where\": \"fields\"}";
+}
+
 int hand_out(const std::string& text, bool ok, char** reply, int* ok_out) {
     char* p = static_cast<char*>(std::malloc(text.size() + 1));
     if (!p) return RCWA_ENOMEM;
@@ -1339,6 +1811,20 @@ int rcwa_json_validate(const char* request, int indent, char** reply, int* ok) {
     if (!reply) return RCWA_EINVAL;
     bool good = false;
     const std::string text = rcwa_gb300::jfront::answer(request, indent, nullptr, good);
+    return rcwa_gb300::jfront::hand_out(text, good, reply, ok);
+}
+
+int rcwa_fields_json_validate(const char* request, int indent, char** reply, int* ok) {
+    if (!reply) return RCWA_EINVAL;
+    bool good = false;
+    const std::string text = rcwa_gb300::jfront::answer_fields(request, indent, nullptr, good);
+    return rcwa_gb300::jfront::hand_out(text, good, reply, ok);
+}
+
+int rcwa_gpu_solve_fields_json(rcwa_gpu_ctx* ctx, const char* request, int indent, char** reply, int* ok) {
+    if (!ctx || !reply) return RCWA_EINVAL;
+    bool good = false;
+    const std::string text = rcwa_gb300::jfront::answer_fields(request, indent, ctx, good);
     return rcwa_gb300::jfront::hand_out(text, good, reply, ok);
 }
 

@@ -622,6 +622,9 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
         LAUNCH(status_kernel, nblocks(B), kTpb, st, B, c.fail, eig_info, c.n_solve, c.extra_solves, (int)grating.size(),
                d_out.status ? d_out.status + p0 : nullptr, d_out.eig_info ? d_out.eig_info + p0 : nullptr,
                d_out.n_eig ? d_out.n_eig + p0 : nullptr, d_out.n_dense_solve ? d_out.n_dense_solve + p0 : nullptr);
+        if (fields && fields->layer_info)
+            for (int k = 0; k < L; ++k)
+                LAUNCH(zero_q_count_kernel, nblocks(B), kTpb, st, B, n, modes[k + 1].q, fields->layer_info + (size_t)p0 * L + k, L);
         if (fields) sample_fields(c, *fields, stack, pol, M, p0, modes, cap_W, cap_V, ld_einv, a_plus, a_minus, kx, k0,
                                   reinterpret_cast<zc*>(d_out.R) + (long long)p0 * n,
                                   reinterpret_cast<zc*>(d_out.T) + (long long)p0 * n);

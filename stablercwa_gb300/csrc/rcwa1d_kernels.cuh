@@ -382,6 +382,16 @@ __global__ void kx_rows_kernel(long long total, int n, const double* __restrict_
     out[idx] = kx[b * n + j] * S[idx];
 }
 
+// number of modes with q exactly 0 in one layer, per sample (the finite-zero-basis modes of the field metadata,
+// include/stablercwa/rcwa1d_fields.hpp:99)
+__global__ void zero_q_count_kernel(int B, int n, const zc* __restrict__ q, int* __restrict__ out, int stride) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    int count = 0;
+    for (int j = 0; j < n; ++j) count += is_zero(q[(long long)b * n + j]) ? 1 : 0;
+    out[(long long)b * stride] = count;
+}
+
 __global__ void nan_fields_kernel(int B, long long per, const int* __restrict__ fail, zc* __restrict__ out) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)B * per) return;

@@ -65,11 +65,11 @@ def load_library(build_if_missing=True):
                                          C.POINTER(abi.rcwa_result1d)]
     L.rcwa_gpu_solve1d_batch_dev.argtypes = L.rcwa_gpu_solve1d_batch.argtypes
     L.rcwa_gpu_solve1d_fields.argtypes = [vp, C.POINTER(abi.rcwa_stack1d), vp, ci, ci, ci, C.POINTER(abi.rcwa_options), vp,
-                                          ci, C.POINTER(abi.rcwa_result1d), vp]
+                                          ci, C.POINTER(abi.rcwa_result1d), vp, vp]
     L.rcwa_gpu_solve_conical_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack1d), vp, ci, ci,
                                                C.POINTER(abi.rcwa_options), C.POINTER(abi.rcwa_result_conical)]
     L.rcwa_gpu_solve_conical_fields.argtypes = [vp, C.POINTER(abi.rcwa_stack1d), vp, ci, ci, C.POINTER(abi.rcwa_options),
-                                                vp, vp, ci, C.POINTER(abi.rcwa_result_conical), vp]
+                                                vp, vp, ci, C.POINTER(abi.rcwa_result_conical), vp, vp]
     L.rcwa_gpu_solve2d_batch.argtypes = [vp, C.POINTER(abi.rcwa_stack2d), vp, ci, ci, ci, ci,
                                          C.POINTER(abi.rcwa_options), C.POINTER(abi.rcwa_result2d)]
     L.rcwa_gpu_solve2d_fields.argtypes = [vp, C.POINTER(abi.rcwa_stack2d), vp, ci, ci, ci, ci, C.POINTER(abi.rcwa_options),
@@ -77,6 +77,8 @@ def load_library(build_if_missing=True):
     for name in ("rcwa_gpu_solve_json", "rcwa_gpu_server_solve_json"):
         getattr(L, name).argtypes = [vp, C.c_char_p, ci, C.POINTER(C.c_void_p), C.POINTER(ci)]
     L.rcwa_json_validate.argtypes = [C.c_char_p, ci, C.POINTER(C.c_void_p), C.POINTER(ci)]
+    L.rcwa_fields_json_validate.argtypes = L.rcwa_json_validate.argtypes
+    L.rcwa_gpu_solve_fields_json.argtypes = [vp, C.c_char_p, ci, C.POINTER(C.c_void_p), C.POINTER(ci)]
     L.rcwa_json_free.argtypes = [C.c_void_p]
     L.rcwa_gpu_field_slice.argtypes = [vp, vp, ci, ci, vp, vp, ci, ci, cd, cd, vp]
     L.rcwa_gpu_phase_data.argtypes = [vp, vp, ci, ci, ci, vp, vp, vp, vp, vp, cd, ci, vp, vp, vp, vp]
@@ -173,15 +175,23 @@ class Engine:
         z = np.ascontiguousarray(np.asarray(zs, dtype=np.float64).reshape(-1))
         res, arrays = abi.result_views(len(pts), M)
         fields = np.empty((len(pts), 6, 2 * M + 1, len(z)), np.complex128)
+        info = np.zeros((len(pts), max(1, len(stack.layers))), np.int32)
         o = _options(options)
         self._check(self.L.rcwa_gpu_solve1d_fields(self.h, C.byref(st), pts.ctypes.data, len(pts), M, pol, C.byref(o),
-                                                   z.ctypes.data, len(z), C.byref(res), fields.ctypes.data))
+                                                   z.ctypes.data, len(z), C.byref(res), fields.ctypes.data,
+                                                   info.ctypes.data))
+        arrays["layer_info"] = info
         return arrays, fields
 
     def solve_json(self, request, indent=-1):
         """rcwa::solve_json_reply (include/stablercwa/rcwa_json.hpp:1287-1309) on this context, every point
         of the request in one batched call: (ok, reply text)."""
         return _json_call(self.L.rcwa_gpu_solve_json, self.h, request, indent)
+
+    def solve_fields_json(self, request, indent=-1):
+        """rcwa::solve_fields_json_reply (include/stablercwa/rcwa_fields_json.hpp): one point with its fields,
+        NPY files published into the request's output_dir; (ok, reply text)."""
+        return _json_call(self.L.rcwa_gpu_solve_fields_json, self.h, request, indent)
 
     def field_slice(self, fields, kx, ky, plane, nt, period, at=0.0):
         """Real-space slice of one point's harmonics on the device (rcwa::field_slice, reconstruct_field_slice,
@@ -315,8 +325,11 @@ class Engine:
             j = np.ascontiguousarray(np.broadcast_to(j.reshape(-1, 2), (len(pts), 2)))
             jp = j.ctypes.data
         o = _options(options)
+        info = np.zeros((len(pts), max(1, len(stack.layers))), np.int32)
         self._check(self.L.rcwa_gpu_solve_conical_fields(self.h, C.byref(st), pts.ctypes.data, len(pts), M, C.byref(o),
-                                                         jp, z.ctypes.data, len(z), C.byref(res), fields.ctypes.data))
+                                                         jp, z.ctypes.data, len(z), C.byref(res), fields.ctypes.data,
+                                                         info.ctypes.data))
+        arrays["layer_info"] = info
         return arrays, fields
 
     def solve_conical(self, stack, wavelength, theta_deg, phi_deg, M, options=None):
@@ -450,6 +463,12 @@ def json_validate(request, indent=-1):
     """Checks a JSON request like the reference's reader (rcwa_json.hpp:739-800) without solving it:
     (True, "") when it is valid, else (False, the reference's error reply). Needs no GPU."""
     return _json_call(load_library().rcwa_json_validate, None, request, indent)
+
+
+def fields_json_validate(request, indent=-1):
+    """The request checks of the near-field protocol (rcwa_fields_json.hpp:68-151) alone: (True, "") or
+    (False, the error reply). Needs no GPU."""
+    return _json_call(load_library().rcwa_fields_json_validate, None, request, indent)
 
 
 def rayleigh_message(stack, r, M1, M2):

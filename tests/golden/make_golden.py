@@ -28,6 +28,7 @@ EXPORTERS = [
     ("export_fields2d.cpp", "fields2d_cases.jsonl.gz"),
     ("export_phase.cpp", "phase_cases.jsonl.gz"),
     ("export_json.cpp", "json_cases.jsonl.gz"),
+    ("export_fields_json.cpp", "fields_json_cases.jsonl.gz"),
 ]
 
 

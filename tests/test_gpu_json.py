@@ -100,3 +100,47 @@ def test_numbers_round_trip(eng, cases):
     for p, item in enumerate(reply["results"]):
         assert np.array_equal(np.array(item["DEr"]), direct["DEr"][p])
         assert np.array_equal(np.array([complex(*z) for z in item["R"]]), direct["R"][p])
+
+
+def chord(a, b):
+    return np.abs(np.exp(1j * a) - np.exp(1j * b))
+
+
+def test_fields_protocol(eng, tmp_path):
+    """rcwa_gpu_solve_fields_json against rcwa::solve_fields_json_reply (tests/golden/export_fields_json.cpp):
+    the reply text (numbers masked), and the published arrays: fields within 1e-10 (1 + |b|), masks equal,
+    phases within 1e-9 on the unit circle, coordinates to rounding. Failures publish nothing."""
+    import os
+    seen = 0
+    for k, c in enumerate(load_jsonl("fields_json_cases.jsonl.gz")):
+        out = tmp_path / f"case{k}"
+        if c["pre_create"]:
+            out.mkdir()
+        ok, text = eng.solve_fields_json(c["request"].replace("OUTPUT_DIR", str(out)))
+        text = text.replace(str(out), "OUTPUT_DIR")
+        assert ok == bool(c["ok"]), (c["name"], text[:300])
+        if not ok:
+            assert text == c["reply"], (c["name"], text)
+            if not c["pre_create"]:
+                assert not out.exists()
+            continue
+        seen += 1
+        want, got = json.loads(c["reply"]), json.loads(text)
+        assert masked(text) == masked(c["reply"]), c["name"]
+        compare(got["results"], want["results"], "", c["name"])
+        meta_w, meta_g = want["field_data"], got["field_data"]
+        assert meta_g["layers"] == meta_w["layers"] and meta_g["files"] == meta_w["files"], c["name"]
+        assert sorted(os.listdir(out)) == sorted(v["name"] for v in meta_w["files"].values())
+        f = np.load(out / "fields.npy")
+        fw = np.array([complex(*v) for v in c["fields"]]).reshape(f.shape)
+        assert np.max(np.abs(f - fw) / (1.0 + np.abs(fw))) <= 1e-10, c["name"]
+        m = np.load(out / "phase_mask.npy").astype(bool).ravel()
+        mw = np.frombuffer(c["phase_mask"].encode(), np.uint8) == ord("1")
+        assert np.array_equal(m, mw), c["name"]
+        ph = np.load(out / "phase.npy").ravel()
+        pw = np.array([float(v) for v in c["phase"]])
+        assert np.all(np.isnan(ph[m])) and np.max(chord(ph[~m], pw[~m])) <= 1e-9, c["name"]
+        for key in ("x", "z", "t", "y"):
+            if key in c:
+                assert np.allclose(np.load(out / f"{key}.npy"), [float(v) for v in c[key]], rtol=0, atol=1e-15)
+    assert seen == 6

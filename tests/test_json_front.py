@@ -53,3 +53,18 @@ def test_parser_edge_cases():
         assert not ok and r["where"] == "" and frag in r["error"], (text[:20], r)
     ok, reply = json_validate('﻿{"mode": 3}')   # a leading BOM is skipped
     assert json.loads(reply)["where"] == "mode"
+
+
+def test_fields_protocol_request_errors():
+    """The near-field protocol's request checks (rcwa_fields_json.hpp:68-151) give the reference's reply."""
+    from stablercwa_gb300.engine import fields_json_validate
+    seen = 0
+    for c in load_jsonl("fields_json_cases.jsonl.gz"):
+        ref = json.loads(c["reply"])
+        ok, reply = fields_json_validate(c["request"].replace("OUTPUT_DIR", "/tmp/never_created_here/out"))
+        if ref["ok"] or ref["where"] == "fields":   # solved, or failing only when run
+            assert ok and reply == "", c["name"]
+            continue
+        seen += 1
+        assert not ok and reply == c["reply"], (c["name"], reply)
+    assert seen >= 8
