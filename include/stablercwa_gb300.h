@@ -232,6 +232,10 @@ void rcwa_options_default(rcwa_options* options);
 /* Number of engine kernels launched by this process so far (all contexts). No reference
  * counterpart; it lets a caller count the device launches of a call. */
 long long rcwa_gpu_launch_count(void);
+/* QL rotations applied by the Hermitian eigensolver (the solve path for layers of real permittivity) on the
+ * current device since the previous call; reading resets the count and synchronises the device. For work
+ * accounting: each rotation is 12 n real flops on the eigenvector matrix. -1 on a device error. */
+long long rcwa_gpu_eig_rotations(void);
 
 /* Context lifetime. No reference counterpart: the reference keeps no state between calls
  * (include/stablercwa/rcwa1d.hpp:851); the context owns the device workspace and stream. */

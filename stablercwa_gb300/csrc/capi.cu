@@ -177,6 +177,14 @@ void rcwa_options_default(rcwa_options* o) {
 
 long long rcwa_gpu_launch_count(void) { return launch_count(); }
 
+long long rcwa_gpu_eig_rotations(void) {
+    try {
+        return take_rotation_count();
+    } catch (...) {
+        return -1;
+    }
+}
+
 int rcwa_gpu_create(const rcwa_gpu_config* config, rcwa_gpu_ctx** out) {
     std::lock_guard<std::mutex> hold(g_create_lock);
     if (!out) return RCWA_EINVAL;

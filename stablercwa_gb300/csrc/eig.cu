@@ -56,4 +56,82 @@ void launch_eig(cudaStream_t st, int n, int batch, const zc* a, long long a_stri
     RCWA_CUDA(cudaGetLastError());
 }
 
+// QL rotations applied by the Hermitian eigensolver since the last read (the work of its sweeps, 12 n flops
+// each, for the benchmark's roofline)
+unsigned long long* rotation_counter() {
+    static unsigned long long* d = nullptr;
+    if (!d) {
+        RCWA_CUDA(cudaMalloc(&d, sizeof(unsigned long long)));
+        RCWA_CUDA(cudaMemset(d, 0, sizeof(unsigned long long)));
+    }
+    return d;
+}
+long long take_rotation_count() {
+    unsigned long long h = 0;
+    unsigned long long* d = rotation_counter();
+    RCWA_CUDA(cudaDeviceSynchronize());
+    RCWA_CUDA(cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost));
+    RCWA_CUDA(cudaMemset(d, 0, sizeof(unsigned long long)));
+    return (long long)h;
+}
+
+// Hermitian matrices: the reduction with G lanes per matrix, the QL iteration one lane per matrix, the
+// rotations applied row-parallel, and the fused kernel for any matrix whose rotation log overflowed.
+void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info, zc* ws,
+                     double eps, int max_iter, int group) {
+    if (batch <= 0 || n <= 0) return;
+    if (group <= 0) group = eig_default_group(n, batch);
+    TimedLaunch timed(TK_EIG, st);
+    if (group > 32) {
+        switch (group) {
+            case 64: herm_reduce_block_kernel<64><<<(unsigned)batch, 64, 0, st>>>(n, batch, a, a_stride, v, ws); break;
+            case 128: herm_reduce_block_kernel<128><<<(unsigned)batch, 128, 0, st>>>(n, batch, a, a_stride, v, ws); break;
+            case 256: herm_reduce_block_kernel<256><<<(unsigned)batch, 256, 0, st>>>(n, batch, a, a_stride, v, ws); break;
+            default: throw EngineError{RCWA_EINVAL, "eig: group must be 4, 8, 16, 32, 64, 128 or 256"};
+        }
+    } else {
+        const int tpb = 128;
+        const unsigned blocks = (unsigned)(((long long)batch * group + tpb - 1) / tpb);
+        switch (group) {
+            case 4: herm_reduce_batch_kernel<4><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, v, ws); break;
+            case 8: herm_reduce_batch_kernel<8><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, v, ws); break;
+            case 16: herm_reduce_batch_kernel<16><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, v, ws); break;
+            case 32: herm_reduce_batch_kernel<32><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, v, ws); break;
+            default: throw EngineError{RCWA_EINVAL, "eig: group must be 4, 8, 16, 32, 64, 128 or 256"};
+        }
+    }
+    RCWA_CUDA(cudaGetLastError());
+    herm_ql_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, st>>>(n, batch, w, info, ws, eps, max_iter, rotation_counter());
+    RCWA_CUDA(cudaGetLastError());
+    herm_apply_kernel<<<(unsigned)(((long long)batch * n + 127) / 128), 128, 0, st>>>(n, batch, v, ws, info);
+    RCWA_CUDA(cudaGetLastError());
+    // matrices whose log overflowed: the fused kernel, masked to them
+    int* only = nullptr;
+    RCWA_CUDA(cudaMallocAsync(&only, (size_t)batch * sizeof(int), st));
+    herm_overflow_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, st>>>(n, batch, ws, only);
+    RCWA_CUDA(cudaGetLastError());
+    launch_count() += 4;
+    if (group > 32) {
+        switch (group) {
+            case 64: herm_block_kernel<64><<<(unsigned)batch, 64, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rotation_counter(), only); break;
+            case 128: herm_block_kernel<128><<<(unsigned)batch, 128, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rotation_counter(), only); break;
+            case 256: herm_block_kernel<256><<<(unsigned)batch, 256, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rotation_counter(), only); break;
+            default: throw EngineError{RCWA_EINVAL, "eig: group must be 4, 8, 16, 32, 64, 128 or 256"};
+        }
+    } else {
+        const int tpb = 128;
+        const unsigned blocks = (unsigned)(((long long)batch * group + tpb - 1) / tpb);
+        switch (group) {
+            case 4: herm_batch_kernel<4><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rotation_counter(), only); break;
+            case 8: herm_batch_kernel<8><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rotation_counter(), only); break;
+            case 16: herm_batch_kernel<16><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rotation_counter(), only); break;
+            case 32: herm_batch_kernel<32><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rotation_counter(), only); break;
+            default: throw EngineError{RCWA_EINVAL, "eig: group must be 4, 8, 16, 32, 64, 128 or 256"};
+        }
+    }
+    ++launch_count();
+    RCWA_CUDA(cudaGetLastError());
+    RCWA_CUDA(cudaFreeAsync(only, st));
+}
+
 }  // namespace rcwa_gb300

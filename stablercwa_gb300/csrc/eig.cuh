@@ -139,22 +139,13 @@ __device__ __forceinline__ zc wilkinson_shift(zc a, zc b, double c, zc d) {
     return d - scale2(zdiv(x, ys + zz), e);
 }
 
-// With T != nullptr the call returns the Schur form instead of eigenvectors (keep_transform with
-// vectors = false, eig_qr.hpp:1106-1122): V receives Z and T receives the upper triangular T with
-// Z^H A Z = T.
+// Householder reduction of A to upper Hessenberg form H with the reflectors accumulated into Z, the
+// entries below the subdiagonal cleared and the subdiagonal made real by a unitary diagonal similarity
+// (CORTH and the preparation of COMQR2, eig_qr.hpp:231-439). For a Hermitian A the result is Hermitian
+// tridiagonal up to rounding: real diagonal and real subdiagonal.
 template <int G>
-__device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc* __restrict__ V,
-                        int* __restrict__ info_out, int* __restrict__ sweeps_out, zc* __restrict__ ws, double eps,
-                        int max_iter, zc* __restrict__ T = nullptr, double* red = nullptr, int* ired = nullptr) {
-    const int g = threadIdx.x & (G - 1);
-    const Grp<G> grp(red, ired);
-    zc* __restrict__ H = ws;
-    zc* __restrict__ Z = H + (long long)n * n;
-    zc* __restrict__ X = Z + (long long)n * n;
-    zc* __restrict__ ort = X + (long long)n * n;
-    zc* __restrict__ wk = ort + n;
-    double* __restrict__ rotd = reinterpret_cast<double*>(wk + n);  // 3n doubles (<= 2n zc)
-
+__device__ void reduce_to_hessenberg(int n, const zc* __restrict__ A, zc* __restrict__ H, zc* __restrict__ Z,
+                                     zc* __restrict__ ort, zc* __restrict__ wk, const Grp<G>& grp, int g) {
     for (long long idx = g; idx < (long long)n * n; idx += G) H[idx] = A[idx];
     grp.sync();
 
@@ -287,6 +278,26 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
         }
         grp.sync();
     }
+
+}
+
+// With T != nullptr the call returns the Schur form instead of eigenvectors (keep_transform with
+// vectors = false, eig_qr.hpp:1106-1122): V receives Z and T receives the upper triangular T with
+// Z^H A Z = T.
+template <int G>
+__device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc* __restrict__ V,
+                        int* __restrict__ info_out, int* __restrict__ sweeps_out, zc* __restrict__ ws, double eps,
+                        int max_iter, zc* __restrict__ T = nullptr, double* red = nullptr, int* ired = nullptr) {
+    const int g = threadIdx.x & (G - 1);
+    const Grp<G> grp(red, ired);
+    zc* __restrict__ H = ws;
+    zc* __restrict__ Z = H + (long long)n * n;
+    zc* __restrict__ X = Z + (long long)n * n;
+    zc* __restrict__ ort = X + (long long)n * n;
+    zc* __restrict__ wk = ort + n;
+    double* __restrict__ rotd = reinterpret_cast<double*>(wk + n);  // 3n doubles (<= 2n zc)
+
+    reduce_to_hessenberg<G>(n, A, H, Z, ort, wk, grp, g);
 
     // ---------------- shifted QR (eig_qr.hpp:1039-1096), full updates of H and Z
     zc t = zc{0.0, 0.0};
@@ -487,6 +498,326 @@ __device__ void eig_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc*
         const double inv = 1.0 / sqrt(ssq);
         for (int r = g; r < n; r += G) vj[r] = zdivr(vj[r], big) * inv;
     }
+}
+
+// Eigen-decomposition of a Hermitian matrix: the reduction above gives a Hermitian tridiagonal matrix with
+// real diagonal d and real subdiagonal e (entries of order eps |A| elsewhere are rounding and are dropped),
+// whose eigenvalues and eigenvectors follow from the implicit symmetric QL iteration with Wilkinson's
+// shift (Bowdler, Martin, Reinsch and Wilkinson, "The QR and QL algorithms for symmetric matrices",
+// Numer. Math. 11, 1968). The plane rotations of a QL sweep act on the columns of Z, whose columns are
+// then orthonormal eigenvectors; the eigenvalues are real. One lane per group runs the scalar sweep and
+// records its rotations; then every lane applies them to its rows of Z, each row's entries read and written
+// once per sweep. info = l + 1 when eigenvalue l does not converge within max_iter sweeps.
+template <int G>
+__device__ void herm_one(int n, const zc* __restrict__ A, zc* __restrict__ W, zc* __restrict__ V, int* __restrict__ info_out,
+                         zc* __restrict__ ws, double eps, int max_iter, unsigned long long* rotations,
+                         double* red = nullptr, int* ired = nullptr) {
+    const int g = threadIdx.x & (G - 1);
+    const Grp<G> grp(red, ired);
+    zc* __restrict__ H = ws;
+    zc* __restrict__ Z = H + (long long)n * n;
+    zc* __restrict__ X = Z + (long long)n * n;
+    zc* __restrict__ ort = X + (long long)n * n;
+    zc* __restrict__ wk = ort + n;
+    double* __restrict__ d = reinterpret_cast<double*>(X);  // n doubles
+    double* __restrict__ e = d + n;                          // n doubles, e[i] couples i and i+1
+    double* __restrict__ rc = e + n;                         // cosines of a sweep
+    double* __restrict__ rs = rc + n;                        // sines of a sweep
+    int* __restrict__ meta = reinterpret_cast<int*>(rs + n);  // [0] first rotation, [1] last, [2] state
+
+    reduce_to_hessenberg<G>(n, A, H, Z, ort, wk, grp, g);
+    for (int i = g; i < n; i += G) {
+        d[i] = H[(long long)i * n + i].re;
+        e[i] = i + 1 < n ? H[(long long)i * n + i + 1].re : 0.0;
+    }
+    grp.sync();
+
+    int info = 0;
+    unsigned long long applied = 0;
+    for (int l = 0; l < n && info == 0; ++l) {
+        for (int its = 0;; ++its) {
+            if (g == 0) {
+                // m: first index >= l whose coupling to m+1 is negligible (n-1 when there is none)
+                int m = l;
+                for (; m < n - 1; ++m) {
+                    const double dd = fabs(d[m]) + fabs(d[m + 1]);
+                    if (fabs(e[m]) <= eps * dd || fabs(e[m]) <= DBL_MIN) break;
+                }
+                int state = 0, first = m, last = m;  // state 0: sweep recorded, 1: converged, 2: no convergence
+                if (m == l) {
+                    state = 1;
+                } else if (its >= max_iter) {
+                    state = 2;
+                } else {
+                    // Wilkinson shift from the leading 2x2 block of [l, m]
+                    double gg = (d[l + 1] - d[l]) / (2.0 * e[l]);
+                    double r = hypot(gg, 1.0);
+                    gg = d[m] - d[l] + e[l] / (gg + copysign(r, gg));
+                    double s = 1.0, c = 1.0, p = 0.0;
+                    bool split = false;
+                    int i = m - 1;
+                    for (; i >= l; --i) {
+                        const double f = s * e[i], b = c * e[i];
+                        r = hypot(f, gg);
+                        e[i + 1] = r;
+                        if (r == 0.0) {  // the sweep splits the block: recover and restart
+                            d[i + 1] -= p;
+                            e[m] = 0.0;
+                            split = true;
+                            break;
+                        }
+                        s = f / r;
+                        c = gg / r;
+                        gg = d[i + 1] - p;
+                        r = (d[i] - gg) * s + 2.0 * c * b;
+                        p = s * r;
+                        d[i + 1] = gg + p;
+                        gg = c * r - b;
+                        rc[i] = c;
+                        rs[i] = s;
+                    }
+                    if (!split) {
+                        d[l] -= p;
+                        e[l] = gg;
+                        e[m] = 0.0;
+                        first = l;
+                    } else {
+                        first = i + 1;
+                    }
+                    last = m - 1;
+                }
+                meta[0] = first;
+                meta[1] = last;
+                meta[2] = state;
+            }
+            grp.sync();
+            const int first = meta[0], last = meta[1], state = meta[2];
+            grp.sync();  // every member has read meta before the next sweep may rewrite it
+            if (state == 1) break;
+            if (state == 2) {
+                info = l + 1;
+                break;
+            }
+            // the recorded rotations i = last .. first mix columns i and i+1 of Z
+            applied += (unsigned long long)(last - first + 1);
+            for (int r = g; r < n; r += G) {
+                zc cur = Z[(long long)(last + 1) * n + r];
+                for (int i = last; i >= first; --i) {
+                    const double c = rc[i], s = rs[i];
+                    const zc zi = Z[(long long)i * n + r];
+                    Z[(long long)(i + 1) * n + r] = zc{s * zi.re + c * cur.re, s * zi.im + c * cur.im};
+                    cur = zc{c * zi.re - s * cur.re, c * zi.im - s * cur.im};
+                }
+                Z[(long long)first * n + r] = cur;
+            }
+            grp.sync();
+        }
+    }
+    if (g == 0) {
+        *info_out = info;
+        if (rotations) atomicAdd(rotations, applied);
+    }
+    if (info != 0) {
+        for (int i = g; i < n; i += G) W[i] = zc{d[i], 0.0};
+        return;
+    }
+    for (int i = g; i < n; i += G) W[i] = zc{d[i], 0.0};
+    for (long long idx = g; idx < (long long)n * n; idx += G) V[idx] = Z[idx];
+}
+
+template <int G>
+__global__ void __launch_bounds__(128) herm_batch_kernel(int n, int batch, const zc* __restrict__ a, long long a_stride,
+                                                         zc* __restrict__ w, zc* __restrict__ v, int* __restrict__ info,
+                                                         zc* __restrict__ ws, double eps, int max_iter,
+                                                         unsigned long long* rotations, const int* __restrict__ only) {
+    const long long gid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    if (gid >= batch) return;
+    if (only && !only[gid]) return;
+    herm_one<G>(n, a + gid * a_stride, w + gid * n, v + gid * (long long)n * n, info + gid, ws + gid * eig_workspace_elems(n),
+                eps, max_iter, rotations);
+}
+
+template <int G>
+__global__ void __launch_bounds__(G) herm_block_kernel(int n, int batch, const zc* __restrict__ a, long long a_stride,
+                                                       zc* __restrict__ w, zc* __restrict__ v, int* __restrict__ info,
+                                                       zc* __restrict__ ws, double eps, int max_iter,
+                                                       unsigned long long* rotations, const int* __restrict__ only) {
+    __shared__ double red[G / 32];
+    __shared__ int ired[G / 32];
+    const long long gid = blockIdx.x;
+    if (gid >= batch) return;
+    if (only && !only[gid]) return;
+    herm_one<G>(n, a + gid * a_stride, w + gid * n, v + gid * (long long)n * n, info + gid, ws + gid * eig_workspace_elems(n),
+                eps, max_iter, rotations, red, ired);
+}
+
+
+// ---------------------------------------------------------------- the Hermitian solver in three launches
+//
+// The fused herm_one runs the scalar QL sweep on one lane of its group; on this GPU a warp FP64
+// instruction costs the same pipe time whatever the number of active lanes, so that chain is paid at
+// 1/G utilisation. The batched form splits the work: (1) the reduction with G lanes per matrix, Z written
+// to the output and (d, e) kept; (2) the QL iteration with one lane per matrix, 32 matrices per warp
+// instruction, which logs each sweep's rotations; (3) the rotations applied to Z with one thread per
+// (matrix, row): within a sweep a row's entries are read and written once, with the running column kept
+// in registers. A matrix whose log would overflow its capacity is flagged and redone by the fused kernel.
+//
+// Per-matrix workspace (eig_workspace_elems(n) zc): [0, n^2) H, then d, e (2n doubles) and the sweep
+// table (first, last) pairs; [n^2, 3n^2) Z during the reduction, then the rotation log (c, s) with room
+// for 2 n^2 rotations; the tail holds the counts and the overflow flag.
+
+__host__ __device__ inline long long herm_log_capacity(int n) { return 2LL * n * n; }
+__host__ __device__ inline long long herm_table_capacity(int n) { return 2LL * ((long long)n * n - n); }
+
+template <int G>
+__device__ void herm_reduce_one(int n, const zc* __restrict__ A, zc* __restrict__ V, zc* __restrict__ ws, double* red,
+                                int* ired) {
+    const int g = threadIdx.x & (G - 1);
+    const Grp<G> grp(red, ired);
+    zc* __restrict__ H = ws;
+    zc* __restrict__ Z = H + (long long)n * n;
+    zc* __restrict__ ort = Z + 2LL * n * n;
+    zc* __restrict__ wk = ort + n;
+    reduce_to_hessenberg<G>(n, A, H, Z, ort, wk, grp, g);
+    // d and e into the unused third block; the QL kernel moves them to the H block before logging
+    double* d = reinterpret_cast<double*>(Z + (long long)n * n);
+    for (int i = g; i < n; i += G) {
+        d[i] = H[(long long)i * n + i].re;
+        d[n + i] = i + 1 < n ? H[(long long)i * n + i + 1].re : 0.0;
+    }
+    for (long long idx = g; idx < (long long)n * n; idx += G) V[idx] = Z[idx];
+}
+
+template <int G>
+__global__ void __launch_bounds__(128) herm_reduce_batch_kernel(int n, int batch, const zc* __restrict__ a, long long a_stride,
+                                                                zc* __restrict__ v, zc* __restrict__ ws) {
+    const long long gid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    if (gid >= batch) return;
+    herm_reduce_one<G>(n, a + gid * a_stride, v + gid * (long long)n * n, ws + gid * eig_workspace_elems(n), nullptr, nullptr);
+}
+template <int G>
+__global__ void __launch_bounds__(G) herm_reduce_block_kernel(int n, int batch, const zc* __restrict__ a, long long a_stride,
+                                                              zc* __restrict__ v, zc* __restrict__ ws) {
+    __shared__ double red[G / 32];
+    __shared__ int ired[G / 32];
+    const long long gid = blockIdx.x;
+    if (gid >= batch) return;
+    herm_reduce_one<G>(n, a + gid * a_stride, v + gid * (long long)n * n, ws + gid * eig_workspace_elems(n), red, ired);
+}
+
+// (2) implicit symmetric QL with Wilkinson's shift on (d, e), one thread per matrix; rotations logged
+static __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, zc* __restrict__ w, int* __restrict__ info,
+                                                      zc* __restrict__ ws, double eps, int max_iter,
+                                                      unsigned long long* rotations) {
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= batch) return;
+    zc* base = ws + gid * eig_workspace_elems(n);
+    double* d = reinterpret_cast<double*>(base);
+    double* e = d + n;
+    const double* src = reinterpret_cast<const double*>(base + 2LL * n * n);  // written by the reduction
+    for (int k = 0; k < 2 * n; ++k) d[k] = src[k];
+    int2* table = reinterpret_cast<int2*>(e + n);
+    double* log = reinterpret_cast<double*>(base + (long long)n * n);
+    int* tail = reinterpret_cast<int*>(base + 3LL * n * n);  // [0] sweeps, [1] overflow
+    const long long log_cap = herm_log_capacity(n), table_cap = herm_table_capacity(n);
+    long long pos = 0, sweeps = 0;
+    int status = 0, overflow = 0;
+    for (int l = 0; l < n && status == 0 && !overflow; ++l) {
+        for (int its = 0;; ++its) {
+            int m = l;
+            for (; m < n - 1; ++m) {
+                const double dd = fabs(d[m]) + fabs(d[m + 1]);
+                if (fabs(e[m]) <= eps * dd || fabs(e[m]) <= DBL_MIN) break;
+            }
+            if (m == l) break;
+            if (its >= max_iter) {
+                status = l + 1;
+                break;
+            }
+            if (pos + (m - l) > log_cap || sweeps + 1 > table_cap) {
+                overflow = 1;
+                break;
+            }
+            double gg = (d[l + 1] - d[l]) / (2.0 * e[l]);
+            double r = hypot(gg, 1.0);
+            gg = d[m] - d[l] + e[l] / (gg + copysign(r, gg));
+            double s = 1.0, c = 1.0, p = 0.0;
+            bool split = false;
+            int i = m - 1;
+            for (; i >= l; --i) {
+                const double f = s * e[i], b = c * e[i];
+                r = hypot(f, gg);
+                e[i + 1] = r;
+                if (r == 0.0) {
+                    d[i + 1] -= p;
+                    e[m] = 0.0;
+                    split = true;
+                    break;
+                }
+                const double inv = 1.0 / r;
+                s = f * inv;
+                c = gg * inv;
+                gg = d[i + 1] - p;
+                r = (d[i] - gg) * s + 2.0 * c * b;
+                p = s * r;
+                d[i + 1] = gg + p;
+                gg = c * r - b;
+                log[2 * pos] = c;
+                log[2 * pos + 1] = s;
+                ++pos;
+            }
+            const int first = split ? i + 1 : l;
+            if (!split) {
+                d[l] -= p;
+                e[l] = gg;
+                e[m] = 0.0;
+            }
+            if (m - 1 >= first) table[sweeps++] = make_int2(first, m - 1);
+        }
+    }
+    tail[0] = (int)sweeps;
+    tail[1] = overflow;
+    info[gid] = overflow ? 0 : status;
+    if (!overflow) {
+        for (int k = 0; k < n; ++k) w[gid * n + k] = zc{d[k], 0.0};
+        if (rotations) atomicAdd(rotations, (unsigned long long)pos);
+    }
+}
+
+// (3) the logged rotations applied to Z (in v), thread per (matrix, row)
+static __global__ void __launch_bounds__(128) herm_apply_kernel(int n, int batch, zc* __restrict__ v, const zc* __restrict__ ws,
+                                                         const int* __restrict__ info) {
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= (long long)batch * n) return;
+    const long long gid = tid / n;
+    const int r = (int)(tid - gid * n);
+    const zc* base = ws + gid * eig_workspace_elems(n);
+    const int* tail = reinterpret_cast<const int*>(base + 3LL * n * n);
+    if (tail[1] || info[gid]) return;  // overflow (redone by the fused kernel) or not converged
+    const int2* table = reinterpret_cast<const int2*>(reinterpret_cast<const double*>(base) + 2 * n);
+    const double* log = reinterpret_cast<const double*>(base + (long long)n * n);
+    zc* z = v + gid * (long long)n * n + r;
+    const int sweeps = tail[0];
+    long long pos = 0;
+    for (int k = 0; k < sweeps; ++k) {
+        const int2 fl = table[k];
+        zc cur = z[(long long)(fl.y + 1) * n];
+        for (int i = fl.y; i >= fl.x; --i, ++pos) {
+            const double c = log[2 * pos], s = log[2 * pos + 1];
+            const zc zi = z[(long long)i * n];
+            z[(long long)(i + 1) * n] = zc{s * zi.re + c * cur.re, s * zi.im + c * cur.im};
+            cur = zc{c * zi.re - s * cur.re, c * zi.im - s * cur.im};
+        }
+        z[(long long)fl.x * n] = cur;
+    }
+}
+
+// 1 where the matrix overflowed its log (the fused kernel redoes it)
+static __global__ void herm_overflow_kernel(int n, int batch, const zc* __restrict__ ws, int* __restrict__ flag) {
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= batch) return;
+    const int* tail = reinterpret_cast<const int*>(ws + gid * eig_workspace_elems(n) + 3LL * n * n);
+    flag[gid] = tail[1];
 }
 
 // One group of G <= 32 lanes per matrix; matrices at a_stride / w_stride / v_stride elements apart.

@@ -86,6 +86,12 @@ void launch_zgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A, 
 void launch_eig(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info, int* sweeps,
                 zc* ws, double eps, int max_iter, int group, const int* skip = nullptr, int skip_value = 1,
                 zc* t_out = nullptr);
+// Hermitian A (only the Hermitian part is used): real eigenvalues in w (imaginary parts 0), orthonormal
+// eigenvectors in v; info as launch_eig.
+void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info, zc* ws,
+                     double eps, int max_iter, int group);
+unsigned long long* rotation_counter();  // device counter the Hermitian eigensolver adds its QL rotations to
+long long take_rotation_count();         // read and reset it (synchronises the device)
 long long eig_workspace_bytes(int n, int batch);
 int eig_default_group(int n, int batch);
 

@@ -322,7 +322,11 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
         zc* inv_eps = nullptr;   // [[1/eps]] (TM)
         zc* einv = nullptr;      // [[eps]]^{-1} (TM)
         zc* cinv = nullptr;      // [[1/eps]]^{-1} (TM)
+        bool herm = false;       // Hermitian operators: the Hermitian eigensolver path
+        zc* einv_h = nullptr;    // Hermitian part of [[eps]]^{-1} (TM, herm)
+        zc *Linv = nullptr, *LinvH = nullptr;  // L^{-1}, L^{-H} of [[1/eps]] = L L^H (TM, herm)
     };
+    const bool try_herm = hermitian_path_enabled(opt);
     std::vector<LayerData> ld(L);
     for (int k : grating) {
         const rcwa_layer1d& Ly = stack.layers[k];
@@ -335,9 +339,13 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
         }
         ld[k].c_eps = layer_coefficients(st, persist, edges, eps, stack.period, M, Ly.fourier_method, Ly.fft_samples,
                                          layer_fail);
+        ld[k].herm = try_herm && make_hermitian_coefficients(st, ld[k].c_eps, M);
         if (pol == RCWA_TM) {
             zc* c_inv = layer_coefficients(st, persist, edges, inv, stack.period, M, Ly.fourier_method, Ly.fft_samples,
                                            layer_fail);
+            if (ld[k].herm)
+                ld[k].herm = make_hermitian_coefficients(st, c_inv, M) &&
+                             toeplitz_cholesky_inverse(st, c_inv, M, persist, ld[k].Linv, ld[k].LinvH);
             zc* E = persist.get<zc>(nn);
             ld[k].inv_eps = persist.get<zc>(nn);
             LAUNCH(toeplitz_kernel, nblocks(nn), kTpb, st, M, ld[k].c_eps, E);
@@ -348,6 +356,10 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
             ld[k].cinv = persist.get<zc>(nn);
             launch_lu_solve(st, n, n, 1, E, nn, E, nn, RHS_IDENTITY, nullptr, nn, ld[k].einv, nn, layer_fail);
             launch_lu_solve(st, n, n, 1, C, nn, C, nn, RHS_IDENTITY, nullptr, nn, ld[k].cinv, nn, layer_fail);
+            if (ld[k].herm) {
+                ld[k].einv_h = persist.get<zc>(nn);
+                LAUNCH(hermitian_part_kernel, nblocks(nn), kTpb, st, n, ld[k].einv, ld[k].einv_h);
+            }
         }
     }
 
@@ -397,14 +409,23 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
             if (opt.diagnostics) resid = mem.zeros<double>(B);
             for (int k : grating) {
                 // 1a. layer matrix
+                const bool herm = ld[k].herm;
                 zc* A = c.dense();
+                zc* mid = nullptr;
                 if (pol == RCWA_TE) {
                     LAUNCH(assemble_te_kernel, nblocks(nd), kTpb, st, B, M, ld[k].c_eps, kx, A);
                 } else {
-                    zc* mid = c.dense();
-                    LAUNCH(tm_middle_kernel, nblocks(nd), kTpb, st, B, n, ld[k].einv, kx, mid);
-                    gemm(c, ld[k].cinv, 0, mid, nullptr, 1.0, 0.0, A);
-                    mem.free(mid);
+                    mid = c.dense();
+                    LAUNCH(tm_middle_kernel, nblocks(nd), kTpb, st, B, n, herm ? ld[k].einv_h : ld[k].einv, kx, mid);
+                    if (herm) {
+                        // the pencil (mid, [[1/eps]]) as the Hermitian L^{-1} mid L^{-H}
+                        zc* t = c.dense();
+                        launch_zgemm(st, n, n, n, B, mid, n, nn, ld[k].LinvH, n, 0, nullptr, 0, t, n, nn, 1.0, 0.0);
+                        launch_zgemm(st, n, n, n, B, ld[k].Linv, n, 0, t, n, nn, nullptr, 0, A, n, nn, 1.0, 0.0);
+                        mem.free(t);
+                    } else {
+                        gemm(c, ld[k].cinv, 0, mid, nullptr, 1.0, 0.0, A);
+                    }
                     c.n_solve += 2;  // the reference forms A with two dense solves per sample
                 }
                 LAUNCH(finite_check_kernel, nblocks(nd), kTpb, st, B, nn, A, c.fail);
@@ -414,7 +435,20 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
                 m.fzb = true;
                 zc* lam = c.vec();
                 m.W = c.dense();
-                launch_eig(st, n, B, A, nn, lam, m.W, info, nullptr, ws, opt.eps, opt.max_iter, opt.eig_group);
+                if (herm) {
+                    launch_eig_herm(st, n, B, A, nn, lam, m.W, info, ws, opt.eps, opt.max_iter, opt.eig_group);
+                    if (pol == RCWA_TM) {  // x = L^{-H} y, unit 2-norm like the general solver's vectors
+                        zc* y = m.W;
+                        m.W = c.dense();
+                        launch_zgemm(st, n, n, n, B, ld[k].LinvH, n, 0, y, n, nn, nullptr, 0, m.W, n, nn, 1.0, 0.0);
+                        mem.free(y);
+                        LAUNCH(normalize_cols_kernel, warp_blocks(nv), 128, st, B, n, m.W);
+                        if (opt.diagnostics) gemm(c, ld[k].cinv, 0, mid, nullptr, 1.0, 0.0, A);  // the solve's A
+                    }
+                } else {
+                    launch_eig(st, n, B, A, nn, lam, m.W, info, nullptr, ws, opt.eps, opt.max_iter, opt.eig_group);
+                }
+                if (mid) mem.free(mid);
                 LAUNCH(eig_info_kernel, nblocks(B), kTpb, st, B, info, eig_info, c.fail);
                 if (opt.diagnostics) {
                     zc* av = gemm(c, A, nn, m.W, nullptr, 1.0, 0.0);

@@ -8,6 +8,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <complex>
 #include <vector>
@@ -453,6 +454,124 @@ inline zc* layer_coefficients(cudaStream_t st, DeviceScratch& mem, const std::ve
             return d;
         }
     return fft_coefficients_dev(st, mem, edges, values, period, 2 * M, resolve_fft_samples(M, samples));
+}
+
+
+// ---------------------------------------------------------------- Hermitian layer operators
+//
+// A layer of real permittivities has Hermitian Toeplitz operators ([[eps]], [[1/eps]]: c_{-h} = conj(c_h)),
+// so its TE matrix Kx^2 - [[eps]] is Hermitian and its TM (and conical B C) eigenproblem is the Hermitian-
+// definite pencil (Kx [[eps]]^{-1} Kx - I, [[1/eps]]). Those are solved with the Hermitian eigensolver
+// (launch_eig_herm): the same eigenpairs as the general QR to rounding (eigenvectors up to a phase per
+// eigenvalue, and any orthonormal basis of a repeated eigenvalue), with orthonormal W. Only with the
+// default iteration settings, so that non-default eps / max_iter keep the general solver's semantics.
+
+inline bool hermitian_path_enabled(const Options& opt) {
+    const char* env = std::getenv("RCWA_GB300_HERMITIAN");
+    if (env && env[0] == '0') return false;
+    return opt.eps == 2.220446049250313e-16 && opt.max_iter == 30;
+}
+
+// c[h + 2M], h = -2M..2M, on the device: true when c_{-h} = conj(c_h) to 8 eps max|c|, and then c is made
+// exactly Hermitian (the average of the two, imaginary part of c_0 dropped).
+inline bool make_hermitian_coefficients(cudaStream_t st, zc* c, int M) {
+    const int K = 4 * M + 1;
+    std::vector<zc> h(K);
+    RCWA_CUDA(cudaMemcpyAsync(h.data(), c, K * sizeof(zc), cudaMemcpyDeviceToHost, st));
+    RCWA_CUDA(cudaStreamSynchronize(st));
+    double big = 0.0;
+    for (const zc& z : h) {
+        if (!std::isfinite(z.re) || !std::isfinite(z.im)) return false;
+        big = std::max(big, std::hypot(z.re, z.im));
+    }
+    const double tol = 8.0 * 2.220446049250313e-16 * big;
+    if (std::fabs(h[2 * M].im) > tol) return false;
+    for (int k = 1; k <= 2 * M; ++k) {
+        const zc a = h[2 * M + k], b = h[2 * M - k];
+        if (std::hypot(a.re - b.re, a.im + b.im) > tol) return false;
+    }
+    h[2 * M].im = 0.0;
+    for (int k = 1; k <= 2 * M; ++k) {
+        const zc a = h[2 * M + k], b = h[2 * M - k];
+        const zc avg{0.5 * (a.re + b.re), 0.5 * (a.im - b.im)};
+        h[2 * M + k] = avg;
+        h[2 * M - k] = zc{avg.re, -avg.im};
+    }
+    RCWA_CUDA(cudaMemcpyAsync(c, h.data(), K * sizeof(zc), cudaMemcpyHostToDevice, st));
+    RCWA_CUDA(cudaStreamSynchronize(st));
+    return true;
+}
+
+// Cholesky factor T = L L^H of the Hermitian Toeplitz matrix of the device coefficients c (host arithmetic,
+// once per layer), then Linv = L^{-1} and LinvH = L^{-H} on the device (column-major n x n). False when T
+// is not positive definite.
+inline bool toeplitz_cholesky_inverse(cudaStream_t st, const zc* c, int M, DeviceScratch& mem, zc*& Linv, zc*& LinvH) {
+    const int n = 2 * M + 1, K = 4 * M + 1;
+    std::vector<zc> h(K);
+    RCWA_CUDA(cudaMemcpyAsync(h.data(), c, K * sizeof(zc), cudaMemcpyDeviceToHost, st));
+    RCWA_CUDA(cudaStreamSynchronize(st));
+    std::vector<cd> L((size_t)n * n, cd{0.0, 0.0});  // column-major, lower triangle
+    const auto T = [&](int i, int j) { const zc z = h[i - j + 2 * M]; return cd{z.re, z.im}; };
+    for (int j = 0; j < n; ++j) {
+        double dj = T(j, j).real();
+        for (int k = 0; k < j; ++k) dj -= std::norm(L[(size_t)k * n + j]);
+        if (!(dj > 0.0) || !std::isfinite(dj)) return false;
+        const double ljj = std::sqrt(dj);
+        L[(size_t)j * n + j] = ljj;
+        for (int i = j + 1; i < n; ++i) {
+            cd s = T(i, j);
+            for (int k = 0; k < j; ++k) s -= L[(size_t)k * n + i] * std::conj(L[(size_t)k * n + j]);
+            L[(size_t)j * n + i] = s / ljj;
+        }
+    }
+    std::vector<cd> X((size_t)n * n, cd{0.0, 0.0});  // X = L^{-1}, lower triangular, column by column
+    for (int j = 0; j < n; ++j) {
+        X[(size_t)j * n + j] = 1.0 / L[(size_t)j * n + j];
+        for (int i = j + 1; i < n; ++i) {
+            cd s{0.0, 0.0};
+            for (int k = j; k < i; ++k) s += L[(size_t)k * n + i] * X[(size_t)j * n + k];
+            X[(size_t)j * n + i] = -s / L[(size_t)i * n + i];
+        }
+    }
+    std::vector<zc> xi((size_t)n * n), xh((size_t)n * n);
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+            const cd v = X[(size_t)j * n + i];
+            xi[(size_t)j * n + i] = zc{v.real(), v.imag()};
+            xh[(size_t)i * n + j] = zc{v.real(), -v.imag()};
+        }
+    Linv = mem.get<zc>((size_t)n * n);
+    LinvH = mem.get<zc>((size_t)n * n);
+    RCWA_CUDA(cudaMemcpyAsync(Linv, xi.data(), xi.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
+    RCWA_CUDA(cudaMemcpyAsync(LinvH, xh.data(), xh.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
+    RCWA_CUDA(cudaStreamSynchronize(st));
+    return true;
+}
+
+// out = (E + E^H) / 2 of one n x n matrix
+__global__ void hermitian_part_kernel(int n, const zc* __restrict__ E, zc* __restrict__ out) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n * n) return;
+    const int j = idx / n, i = idx - j * n;
+    const zc a = E[idx], b = E[(long long)i * n + j];
+    out[idx] = zc{0.5 * (a.re + b.re), 0.5 * (a.im - b.im)};
+}
+
+// every column of every matrix scaled to unit 2-norm (warp per column)
+__global__ void normalize_cols_kernel(int B, int n, zc* __restrict__ W) {
+    const long long col = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (col >= (long long)B * n) return;
+    const int lane = threadIdx.x & 31;
+    zc* w = W + col * n;
+    double big = 0.0;
+    for (int i = lane; i < n; i += 32) big = fmax(big, fmax(fabs(w[i].re), fabs(w[i].im)));
+    for (int o = 16; o > 0; o >>= 1) big = fmax(big, __shfl_xor_sync(0xffffffffu, big, o));
+    if (!(big > 0.0) || !isfinite(big)) return;
+    double ssq = 0.0;
+    for (int i = lane; i < n; i += 32) ssq += norm2(zdivr(w[i], big));
+    for (int o = 16; o > 0; o >>= 1) ssq += __shfl_xor_sync(0xffffffffu, ssq, o);
+    const double inv = 1.0 / (big * sqrt(ssq));
+    for (int i = lane; i < n; i += 32) w[i] = w[i] * inv;
 }
 
 __global__ void toeplitz_kernel(int M, const zc* __restrict__ c, zc* __restrict__ m) {

@@ -100,6 +100,13 @@ def launch_count():
     return int(load_library().rcwa_gpu_launch_count())
 
 
+def eig_rotations():
+    """QL rotations of the Hermitian eigensolver since the previous call (resets the count)."""
+    L = load_library()
+    L.rcwa_gpu_eig_rotations.restype = C.c_longlong
+    return int(L.rcwa_gpu_eig_rotations())
+
+
 def _options(opt):
     o = abi.rcwa_options()
     load_library().rcwa_options_default(C.byref(o))
