@@ -143,6 +143,33 @@ DSBlock interface_block(Batch& c, const DModes& up, const DModes& low) {
     return s;
 }
 
+// The seam of a dense region over an analytic one with a diagonal (or zero) reflection r below it. The
+// reference stacks the interface block (Tdd, Rdu, Rud, Tuu from tp^-1; rcwa1d.hpp:694-712) on r
+// (:794-808). Across the interface the amplitudes obey d_b = tp d_a + tm u_a and u_b = tm d_a + tp u_a (b
+// below, a above); with u_b = r d_b the same seam is
+//     r' = (tp - r tm)^-1 (r tp - tm),    g = tp + tm r',
+// one LU with n right-hand sides and one product instead of two LUs and four products. tp - r tm =
+// (I - r Rdu) tp is singular exactly when the reference's tp or I - Rdu r is (Sylvester's determinant
+// identity), so the samples that fail are the same ones.
+Seam dense_on_analytic_seam(Batch& c, const DModes& up, const DModes& low, const DOp& r) {
+    zc *tp, *tm;
+    interface_matching(c, up, low, tp, tm);
+    zc* lhs = c.dense();
+    zc* rhs = c.dense();
+    LAUNCH(seam_system_kernel, nblocks((long long)c.B * c.nn()), kTpb, c.st, c.B, c.n, tp, tm,
+           r.kind == KDiag ? r.p : nullptr, lhs, rhs);
+    zc* rp = solve(c, lhs, true, RHS_DENSE, rhs);
+    if (r.kind == KDiag) ++c.n_solve;  // the reference's (I - Rdu r)^-1 Tdd
+    c.mem->free(lhs);
+    c.mem->free(rhs);
+    gemm(c, tm, c.nn(), rp, tp, 1.0, 1.0, tp);  // tp is now g
+    c.mem->free(tm);
+    Seam out;
+    out.g = {KDense, tp};
+    out.r = {KDense, rp};
+    return out;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- validation
@@ -311,6 +338,7 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
     for (int k = 0; k < L; ++k)
         if (!stack.layers[k].homogeneous) grating.push_back(k);
     const bool pure_films = grating.empty();
+    const bool reduced = reduced_seams_enabled();
     const zc nI{stack.nI.re, stack.nI.im}, nII{stack.nII.re, stack.nII.im};
 
     // Per-layer, sample-independent operators: Toeplitz coefficients; for TM the inverse of [[eps]] and
@@ -507,6 +535,13 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
                 r = {KDiag, rv};
                 continue;
             }
+            if (b % 2 == 0 && reduced && !modes[j].analytic && modes[j + 1].analytic && r.kind != KDense) {
+                Seam seam = dense_on_analytic_seam(c, modes[j], modes[j + 1], r);
+                if (r.kind == KDiag) mem.free(r.p);
+                g[b] = seam.g;
+                r = seam.r;
+                continue;
+            }
             if (b % 2 == 0) {
                 DSBlock blk = interface_block(c, modes[j], modes[j + 1]);
                 Seam seam = stack_on(c, std::move(blk), r);
@@ -575,48 +610,75 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
         }
 
         // ---- 3. top interface, only column M (include/stablercwa/rcwa1d.hpp:714-746, :989-1023)
-        zc* tdd = c.vec();
-        zc* rud = c.vec();
-        DOp topRdu, topTuu;
-        if (modes[0].analytic && modes[1].analytic) {
-            zc* Tdd = c.vec();
-            zc* Rdu = c.vec();
-            zc* Rud = c.vec();
-            zc* Tuu = c.vec();
-            LAUNCH(diagonal_interface_kernel, nblocks(nv), kTpb, st, nv, modes[0].p, modes[1].p, Tdd, Rdu, Rud, Tuu);
-            LAUNCH(top_diag_vectors_kernel, nblocks(nv), kTpb, st, B, n, M, Tdd, Rud, tdd, rud);
-            topRdu = {KDiag, Rdu};
-            topTuu = {KDiag, Tuu};
+        zc* down = nullptr;
+        zc* Rv = nullptr;
+        if (reduced && modes[0].analytic && !modes[1].analytic && r.kind == KDense) {
+            // Analytic incident medium over a dense region with the dense reflection r below the interface:
+            // with W (I + r) d_b = d_a + u_a, V (I - r) d_b = p0 (d_a - u_a) and d_a = e_M,
+            //     (p0 W + V + (p0 W - V) r) d_b = 2 p0_M e_M,    R = u_a = W (d_b + r d_b) - e_M:
+            // one LU with one right-hand side for the reference's three with n (W^-1, V^-1 p0, tp^-1) and one
+            // with a single column; no division by p0, so an order grazing in the incident medium is fine.
+            zc* P = c.dense();
+            zc* Q = c.dense();
+            LAUNCH(top_pq_kernel, nblocks(nd), kTpb, st, B, n, modes[1].W, modes[1].V, modes[0].p, P, Q);
+            gemm(c, Q, nn, r.p, P, 1.0, 1.0, P);
+            mem.free(Q);
+            zc* rhs = c.vec();
+            LAUNCH(top_rhs_kernel, nblocks(nv), kTpb, st, B, n, M, modes[0].p, rhs);
+            down = solve(c, P, true, RHS_DENSE, rhs, 1);
+            c.n_solve += 3;
+            mem.free(P);
+            mem.free(rhs);
+            zc* t = c.vec();
+            LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 1, r.p, down, down, t, 1.0, 1.0);
+            Rv = c.vec();
+            LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 1, modes[1].W, t, nullptr, Rv, 1.0, 0.0);
+            LAUNCH(sub_incident_kernel, nblocks(B), kTpb, st, B, n, M, Rv);
+            mem.free(t);
         } else {
-            zc *tp, *tm;
-            interface_matching(c, modes[0], modes[1], tp, tm);
-            zc* tpi = solve(c, tp, false, RHS_IDENTITY, nullptr);
-            zc* rdu = gemm(c, tm, nn, tpi, nullptr, 1.0, 0.0);
-            zc* tm_e = c.vec();
-            LAUNCH(col_extract_kernel, nblocks(nv), kTpb, st, B, n, tm, M, tm_e, 1, 0);
-            LAUNCH(col_extract_kernel, nblocks(nv), kTpb, st, B, n, tp, M, tdd, 1, 0);
-            LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 1, rdu, tm_e, tdd, tdd, -1.0, 1.0);
-            LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 1, tpi, tm_e, nullptr, rud, -1.0, 0.0);
-            mem.free(tp);
-            mem.free(tm);
-            topRdu = {KDense, rdu};
-            topTuu = {KDense, tpi};
+            zc* tdd = c.vec();
+            zc* rud = c.vec();
+            DOp topRdu, topTuu;
+            if (modes[0].analytic && modes[1].analytic) {
+                zc* Tdd = c.vec();
+                zc* Rdu = c.vec();
+                zc* Rud = c.vec();
+                zc* Tuu = c.vec();
+                LAUNCH(diagonal_interface_kernel, nblocks(nv), kTpb, st, nv, modes[0].p, modes[1].p, Tdd, Rdu, Rud, Tuu);
+                LAUNCH(top_diag_vectors_kernel, nblocks(nv), kTpb, st, B, n, M, Tdd, Rud, tdd, rud);
+                topRdu = {KDiag, Rdu};
+                topTuu = {KDiag, Tuu};
+            } else {
+                zc *tp, *tm;
+                interface_matching(c, modes[0], modes[1], tp, tm);
+                zc* tpi = solve(c, tp, false, RHS_IDENTITY, nullptr);
+                zc* rdu = gemm(c, tm, nn, tpi, nullptr, 1.0, 0.0);
+                zc* tm_e = c.vec();
+                LAUNCH(col_extract_kernel, nblocks(nv), kTpb, st, B, n, tm, M, tm_e, 1, 0);
+                LAUNCH(col_extract_kernel, nblocks(nv), kTpb, st, B, n, tp, M, tdd, 1, 0);
+                LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 1, rdu, tm_e, tdd, tdd, -1.0, 1.0);
+                LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 1, tpi, tm_e, nullptr, rud, -1.0, 0.0);
+                mem.free(tp);
+                mem.free(tm);
+                topRdu = {KDense, rdu};
+                topTuu = {KDense, tpi};
+            }
+            DOp k = op_mul(c, topRdu, r);
+            down = tdd;
+            if (k.kind == KDiag) {
+                LAUNCH(vec_div_one_minus_kernel, nblocks(nv), kTpb, st, B, n, 1, down, k.p);
+            } else if (k.kind == KDense) {
+                LAUNCH(identity_minus_kernel, nblocks(nd), kTpb, st, B, n, k.p, nullptr, 1);
+                down = solve(c, k.p, true, RHS_DENSE, tdd, 1);
+            }
+            // R = rud + Tuu (r down)
+            zc* rdn = c.vec();
+            LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 1, (int)r.kind, r.p, nullptr, nullptr, down, rdn);
+            zc* back = c.vec();
+            LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 1, (int)topTuu.kind, topTuu.p, nullptr, nullptr, rdn, back);
+            LAUNCH(vec_add_kernel, nblocks(nv), kTpb, st, nv, back, rud);  // rud = back + rud
+            Rv = rud;
         }
-        DOp k = op_mul(c, topRdu, r);
-        zc* down = tdd;
-        if (k.kind == KDiag) {
-            LAUNCH(vec_div_one_minus_kernel, nblocks(nv), kTpb, st, B, n, 1, down, k.p);
-        } else if (k.kind == KDense) {
-            LAUNCH(identity_minus_kernel, nblocks(nd), kTpb, st, B, n, k.p, nullptr, 1);
-            down = solve(c, k.p, true, RHS_DENSE, tdd, 1);
-        }
-        // R = rud + Tuu (r down)
-        zc* rdn = c.vec();
-        LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 1, (int)r.kind, r.p, nullptr, nullptr, down, rdn);
-        zc* back = c.vec();
-        LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 1, (int)topTuu.kind, topTuu.p, nullptr, nullptr, rdn, back);
-        LAUNCH(vec_add_kernel, nblocks(nv), kTpb, st, nv, back, rud);  // rud = back + rud
-        zc* Rv = rud;
         // T = g[2L] ... g[1] down
         zc* cur = down;
         zc* nxt = c.vec();

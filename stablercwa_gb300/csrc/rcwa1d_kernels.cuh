@@ -156,6 +156,50 @@ __global__ void tp_tm_kernel(int B, int n, const zc* __restrict__ mm, const zc* 
     tm[idx] = 0.5 * (m - v);
 }
 
+// lhs = tp - r tm, rhs = r tp - tm with r diagonal (r = null: zero), for the seam of a dense region
+// over an analytic one
+__global__ void seam_system_kernel(int B, int n, const zc* __restrict__ tp, const zc* __restrict__ tm,
+                                   const zc* __restrict__ r, zc* __restrict__ lhs, zc* __restrict__ rhs) {
+    const long long nn = (long long)n * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * nn) return;
+    const zc a = tp[idx], m = tm[idx];
+    if (!r) {
+        lhs[idx] = a;
+        rhs[idx] = zc{-m.re, -m.im};
+        return;
+    }
+    const long long b = idx / nn;
+    const zc ri = r[b * n + (idx - b * nn) % n];
+    lhs[idx] = a - ri * m;
+    rhs[idx] = ri * a - m;
+}
+// P = p0 W + V, Q = p0 W - V (rows of W scaled by the incident medium's p0), for the top interface
+__global__ void top_pq_kernel(int B, int n, const zc* __restrict__ W, const zc* __restrict__ V, const zc* __restrict__ p0,
+                              zc* __restrict__ P, zc* __restrict__ Q) {
+    const long long nn = (long long)n * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * nn) return;
+    const long long b = idx / nn;
+    const zc pw = p0[b * n + (idx - b * nn) % n] * W[idx], v = V[idx];
+    P[idx] = pw + v;
+    Q[idx] = pw - v;
+}
+// rhs = 2 p0_M e_M per sample
+__global__ void top_rhs_kernel(int B, int n, int M, const zc* __restrict__ p0, zc* __restrict__ rhs) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * n) return;
+    const long long b = idx / n;
+    const int i = (int)(idx - b * n);
+    rhs[idx] = i == M ? 2.0 * p0[b * n + M] : zc{0.0, 0.0};
+}
+// R_M -= 1 (the incident order's own amplitude)
+__global__ void sub_incident_kernel(int B, int n, int M, zc* __restrict__ R) {
+    const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    R[b * n + M].re -= 1.0;
+}
+
 // I - m in place (include/stablercwa/rcwa1d.hpp:623-629)
 __global__ void identity_minus_kernel(int B, int n, zc* __restrict__ m, const int* __restrict__ skip, int skip_value) {
     const long long nn = (long long)n * n;

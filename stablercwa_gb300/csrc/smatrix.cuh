@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 #include <cmath>
 #include <complex>
 #include <vector>
@@ -465,6 +466,13 @@ inline zc* layer_coefficients(cudaStream_t st, DeviceScratch& mem, const std::ve
 // (launch_eig_herm): the same eigenpairs as the general QR to rounding (eigenvectors up to a phase per
 // eigenvalue, and any orthonormal basis of a repeated eigenvalue), with orthonormal W. Only with the
 // default iteration settings, so that non-default eps / max_iter keep the general solver's semantics.
+
+// The reduced seam algebra (one LU per seam); RCWA_GB300_SEAMS=reference keeps the reference's sequence of
+// interface blocks and stacking for timing and comparison.
+inline bool reduced_seams_enabled() {
+    const char* env = std::getenv("RCWA_GB300_SEAMS");
+    return !(env && std::strcmp(env, "reference") == 0);
+}
 
 inline bool hermitian_path_enabled(const Options& opt) {
     const char* env = std::getenv("RCWA_GB300_HERMITIAN");
