@@ -37,6 +37,14 @@ __host__ __device__ __forceinline__ bool zfinite(zc a) { return isfinite(a.re) &
 __host__ __device__ __forceinline__ zc zfma(zc a, zc b, zc c) {
     return {c.re + (a.re * b.re - a.im * b.im), c.im + (a.re * b.im + a.im * b.re)};
 }
+// c + a*b and c + conj(a)*b as four fused multiply-adds each (a*b is not rounded on its own), for the
+// eigensolver's inner loops
+__host__ __device__ __forceinline__ zc zmac(zc a, zc b, zc c) {
+    return {fma(-a.im, b.im, fma(a.re, b.re, c.re)), fma(a.im, b.re, fma(a.re, b.im, c.im))};
+}
+__host__ __device__ __forceinline__ zc zmacc(zc a, zc b, zc c) {
+    return {fma(a.im, b.im, fma(a.re, b.re, c.re)), fma(-a.im, b.re, fma(a.re, b.im, c.im))};
+}
 // c - a*b
 __host__ __device__ __forceinline__ zc zfms(zc a, zc b, zc c) {
     return {c.re - a.re * b.re + a.im * b.im, c.im - a.re * b.im - a.im * b.re};
@@ -165,5 +173,8 @@ __device__ __forceinline__ int group_max_int(int v, unsigned mask) {
     for (int o = G / 2; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(mask, v, o, G));
     return v;
 }
+
+// triangular factors of a product (launch_zgemm): the zero part's terms are exact zeros and are skipped
+enum { TRI_NONE = 0, TRI_A_LOWER = 1, TRI_A_UPPER = 2, TRI_B_UPPER = 3 };
 
 }  // namespace rcwa_gb300

@@ -656,36 +656,159 @@ __global__ void __launch_bounds__(G) herm_block_kernel(int n, int batch, const z
 //
 // The fused herm_one runs the scalar QL sweep on one lane of its group; on this GPU a warp FP64
 // instruction costs the same pipe time whatever the number of active lanes, so that chain is paid at
-// 1/G utilisation. The batched form splits the work: (1) the reduction with G lanes per matrix, Z written
-// to the output and (d, e) kept; (2) the QL iteration with one lane per matrix, 32 matrices per warp
+// 1/G utilisation. The batched form splits the work: (1) the Householder tridiagonalisation with G lanes
+// per matrix, Q written to the output and (d, e) kept; (2) the QL iteration with one lane per matrix, 32 matrices per warp
 // instruction, which logs each sweep's rotations; (3) the rotations applied to Z with one thread per
 // (matrix, row): within a sweep a row's entries are read and written once, with the running column kept
 // in registers. A matrix whose log would overflow its capacity is flagged and redone by the fused kernel.
 //
-// Per-matrix workspace (eig_workspace_elems(n) zc): [0, n^2) H, then d, e (2n doubles) and the sweep
-// table (first, last) pairs; [n^2, 3n^2) Z during the reduction, then the rotation log (c, s) with room
-// for 2 n^2 rotations; the tail holds the counts and the overflow flag.
+// Per-matrix workspace (eig_workspace_elems(n) zc): during the reduction [0, n^2) the matrix and its
+// reflectors, [n^2, 2n^2) Q, d and e from 2n^2, w and tau from 3n^2. Then [0, n^2) holds d, e (2n doubles)
+// and the sweep table (first, last) pairs, [n^2, 3n^2) the rotation log (c, s) with room for 2 n^2
+// rotations, and the tail the counts and the overflow flag.
 
 __host__ __device__ inline long long herm_log_capacity(int n) { return 2LL * n * n; }
 __host__ __device__ inline long long herm_table_capacity(int n) { return 2LL * ((long long)n * n - n); }
 
+// Householder tridiagonalisation of a Hermitian A (only used through A = A^H): T = Q^H A Q with T real
+// symmetric tridiagonal, Q = H_0 H_1 ... H_{n-2}, H_k = I - tau_k v_k v_k^H acting on indices k+1..n-1 and
+// chosen so that H_k^H x = beta_k e_1 with beta_k real (Golub and Van Loan, Matrix Computations, 4th ed.,
+// sections 5.1 and 8.3.1). The trailing block is updated as A - v w^H - w v^H with y = A v,
+// w = tau y - (|tau|^2 (v^H y) / 2) v. Every lane owns whole rows (i % G) of the trailing block, so the
+// product A v and the rank-2 update read and write consecutive rows across the group (coalesced); a column
+// step needs three group barriers and one group reduction. Q = H_0 (H_1 (... (H_{n-2} I))) is then formed
+// in V with every lane owning whole columns: H_k touches only rows and columns k+1.. of the partial product
+// and each lane applies the reflectors in order to its own columns, so no barrier is needed there.
+// Output: Q in V, d (n) and e (n-1, e_i = T(i+1, i)) in the third block of ws.
 template <int G>
-__device__ void herm_reduce_one(int n, const zc* __restrict__ A, zc* __restrict__ V, zc* __restrict__ ws, double* red,
-                                int* ired) {
+__device__ void herm_tridiag_one(int n, const zc* __restrict__ A0, zc* __restrict__ V, zc* __restrict__ ws, double* red,
+                                 int* ired) {
     const int g = threadIdx.x & (G - 1);
     const Grp<G> grp(red, ired);
-    zc* __restrict__ H = ws;
-    zc* __restrict__ Z = H + (long long)n * n;
-    zc* __restrict__ ort = Z + 2LL * n * n;
-    zc* __restrict__ wk = ort + n;
-    reduce_to_hessenberg<G>(n, A, H, Z, ort, wk, grp, g);
-    // d and e into the unused third block; the QL kernel moves them to the H block before logging
-    double* d = reinterpret_cast<double*>(Z + (long long)n * n);
-    for (int i = g; i < n; i += G) {
-        d[i] = H[(long long)i * n + i].re;
-        d[n + i] = i + 1 < n ? H[(long long)i * n + i + 1].re : 0.0;
+    zc* __restrict__ A = ws;
+    double* __restrict__ d = reinterpret_cast<double*>(ws + 2LL * n * n);
+    double* __restrict__ e = d + n;
+    zc* __restrict__ ww = ws + 3LL * n * n;  // y, then w, of the current step (n)
+    zc* __restrict__ taus = ww + n;          // tau_k (n)
+    for (long long idx = g; idx < (long long)n * n; idx += G) A[idx] = A0[idx];
+    grp.sync();
+    for (int k = 0; k + 1 < n; ++k) {
+        zc* __restrict__ col = A + (long long)k * n;  // rows k+2.. become v_k (v_{k+1} = 1 implied)
+        if (g == 0) d[k] = col[k].re;
+        const zc alpha = col[k + 1];
+        const int r2 = first_owned<G>(k + 2, g), r1 = first_owned<G>(k + 1, g);
+        double xs = 0.0;
+        for (int i = r2; i < n; i += G) xs += norm2(col[i]);
+        xs = grp.sum(xs);
+        zc tau{0.0, 0.0};
+        double beta = alpha.re;
+        if (xs != 0.0 || alpha.im != 0.0) {
+            const double nrm = hypot(hypot(alpha.re, alpha.im), sqrt(xs));
+            beta = alpha.re >= 0.0 ? -nrm : nrm;
+            tau = zc{(beta - alpha.re) / beta, -alpha.im / beta};
+            const zc scal = zinv(alpha - zc{beta, 0.0});
+            for (int i = r2; i < n; i += G) col[i] = col[i] * scal;
+        }
+        if (g == 0) {
+            e[k] = beta;
+            taus[k] = tau;
+        }
+        if (is_zero(tau)) {
+            grp.sync();
+            continue;
+        }
+        grp.sync();  // v is complete
+        // y_i = sum_j A(i, j) v_j over the trailing block, for owned rows i, four rows per pass with their
+        // sums in registers (independent chains sharing each v_j)
+        for (int i0 = r1; i0 < n; i0 += 4 * G) {
+            zc acc[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int i = i0 + u * G;
+                acc[u] = i < n ? A[(long long)(k + 1) * n + i] : zc{0.0, 0.0};
+            }
+            for (int j = k + 2; j < n; ++j) {
+                const zc vj = col[j];
+                const zc* aj = A + (long long)j * n;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int i = i0 + u * G;
+                    if (i < n) acc[u] = zmac(aj[i], vj, acc[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int i = i0 + u * G;
+                if (i < n) ww[i] = acc[u];
+            }
+        }
+        double mr = 0.0;
+        for (int i = r1; i < n; i += G) {
+            const zc vi = i == k + 1 ? zc{1.0, 0.0} : col[i];
+            mr += vi.re * ww[i].re + vi.im * ww[i].im;  // Re(conj(v_i) y_i); v^H y is real for Hermitian A
+        }
+        const double half = 0.5 * norm2(tau) * grp.sum(mr);
+        for (int i = r1; i < n; i += G) {
+            const zc vi = i == k + 1 ? zc{1.0, 0.0} : col[i];
+            ww[i] = tau * ww[i] - zc{half * vi.re, half * vi.im};
+        }
+        grp.sync();  // w is complete
+        // A(i, j) -= v_i conj(w_j) + w_i conj(v_j) over the trailing block, owned rows i, four rows per pass
+        // with their v_i and w_i in registers
+        for (int i0 = r1; i0 < n; i0 += 4 * G) {
+            zc vi[4], wi[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int i = i0 + u * G;
+                vi[u] = i < n ? (i == k + 1 ? zc{1.0, 0.0} : col[i]) : zc{0.0, 0.0};
+                wi[u] = i < n ? ww[i] : zc{0.0, 0.0};
+            }
+            for (int j = k + 1; j < n; ++j) {
+                zc* aj = A + (long long)j * n;
+                const zc cvj = j == k + 1 ? zc{1.0, 0.0} : conj(col[j]);
+                const zc cwj = conj(ww[j]);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int i = i0 + u * G;
+                    if (i < n) aj[i] = zfms(vi[u], cwj, zfms(wi[u], cvj, aj[i]));
+                }
+            }
+        }
+        grp.sync();  // the next column reads the updated block
     }
-    for (long long idx = g; idx < (long long)n * n; idx += G) V[idx] = Z[idx];
+    if (g == 0) {
+        d[n - 1] = A[(long long)(n - 1) * n + n - 1].re;
+        e[n - 1] = 0.0;
+    }
+    for (int j = g; j < n; j += G) {
+        zc* vj = V + (long long)j * n;
+        for (int i = 0; i < n; ++i) vj[i] = zc{i == j ? 1.0 : 0.0, 0.0};
+    }
+    for (int k = n - 2; k >= 0; --k) {
+        const zc tau = taus[k];
+        if (is_zero(tau)) continue;
+        const zc* vk = A + (long long)k * n;
+        // two owned columns per pass: independent dot products sharing the loads of v_k
+        for (int j = first_owned<G>(k + 1, g); j < n; j += 2 * G) {
+            zc* v0 = V + (long long)j * n;
+            zc* v1 = V + (long long)(j + G) * n;
+            const bool two = j + G < n;
+            zc t0 = v0[k + 1], t1 = two ? v1[k + 1] : zc{0.0, 0.0};
+            for (int i = k + 2; i < n; ++i) {
+                const zc x = vk[i];
+                t0 = zmacc(x, v0[i], t0);
+                if (two) t1 = zmacc(x, v1[i], t1);
+            }
+            const zc f0 = tau * t0, f1 = tau * t1;
+            v0[k + 1] = v0[k + 1] - f0;
+            if (two) v1[k + 1] = v1[k + 1] - f1;
+            for (int i = k + 2; i < n; ++i) {
+                const zc x = vk[i];
+                v0[i] = zfms(x, f0, v0[i]);
+                if (two) v1[i] = zfms(x, f1, v1[i]);
+            }
+        }
+    }
 }
 
 template <int G>
@@ -693,7 +816,7 @@ __global__ void __launch_bounds__(128) herm_reduce_batch_kernel(int n, int batch
                                                                 zc* __restrict__ v, zc* __restrict__ ws) {
     const long long gid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
     if (gid >= batch) return;
-    herm_reduce_one<G>(n, a + gid * a_stride, v + gid * (long long)n * n, ws + gid * eig_workspace_elems(n), nullptr, nullptr);
+    herm_tridiag_one<G>(n, a + gid * a_stride, v + gid * (long long)n * n, ws + gid * eig_workspace_elems(n), nullptr, nullptr);
 }
 template <int G>
 __global__ void __launch_bounds__(G) herm_reduce_block_kernel(int n, int batch, const zc* __restrict__ a, long long a_stride,
@@ -702,7 +825,7 @@ __global__ void __launch_bounds__(G) herm_reduce_block_kernel(int n, int batch, 
     __shared__ int ired[G / 32];
     const long long gid = blockIdx.x;
     if (gid >= batch) return;
-    herm_reduce_one<G>(n, a + gid * a_stride, v + gid * (long long)n * n, ws + gid * eig_workspace_elems(n), red, ired);
+    herm_tridiag_one<G>(n, a + gid * a_stride, v + gid * (long long)n * n, ws + gid * eig_workspace_elems(n), red, ired);
 }
 
 // (2) implicit symmetric QL with Wilkinson's shift on (d, e), one thread per matrix; rotations logged
@@ -746,7 +869,18 @@ static __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, z
             int i = m - 1;
             for (; i >= l; --i) {
                 const double f = s * e[i], b = c * e[i];
-                r = hypot(f, gg);
+                // r = |(f, g)| and 1/r from one reciprocal square root: the rotation chain is the whole cost
+                // of this one-thread-per-matrix kernel; hypot and a division where f^2 + g^2 could under- or
+                // overflow
+                const double q = fma(f, f, gg * gg);
+                double inv;
+                if (q > 1e-290 && q < 1e290) {
+                    inv = rsqrt(q);
+                    r = q * inv;
+                } else {
+                    r = hypot(f, gg);
+                    inv = r == 0.0 ? 0.0 : 1.0 / r;
+                }
                 e[i + 1] = r;
                 if (r == 0.0) {
                     d[i + 1] -= p;
@@ -754,7 +888,6 @@ static __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, z
                     split = true;
                     break;
                 }
-                const double inv = 1.0 / r;
                 s = f * inv;
                 c = gg * inv;
                 gg = d[i + 1] - p;

@@ -96,7 +96,7 @@ void zgemm_raw(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int
     const long long warps = (long long)batch * ((m + 31) / 32) * ((n + 7) / 8);
     const unsigned blocks = (unsigned)((warps * 32 + 127) / 128);
     zgemm_kernel<<<blocks, 128, 0, st>>>(m, n, k, batch, A, lda, a_stride, B, ldb, b_stride, C, c_stride, C, ldc,
-                                         c_stride, s_ab, 1.0, skip, skip_value);
+                                         c_stride, s_ab, 1.0, skip, skip_value, TRI_NONE);
     ++launch_count();
     RCWA_CUDA(cudaGetLastError());
 }
@@ -174,13 +174,13 @@ void launch_lu_solve(cudaStream_t st, int n, int nrhs, int batch, const zc* a, l
 
 void launch_zgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride, const zc* B,
                   int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc, long long c_stride,
-                  double s_ab, double s_c, const int* skip, int skip_value) {
+                  double s_ab, double s_c, const int* skip, int skip_value, int tri) {
     if (batch <= 0 || m <= 0 || n <= 0) return;
     const long long warps = (long long)batch * ((m + 31) / 32) * ((n + 7) / 8);
     const unsigned blocks = (unsigned)((warps * 32 + 127) / 128);
     TimedLaunch timed(TK_GEMM, st);
     zgemm_kernel<<<blocks, 128, 0, st>>>(m, n, k, batch, A, lda, a_stride, B, ldb, b_stride, C0, c0_stride, C, ldc,
-                                         c_stride, s_ab, s_c, skip, skip_value);
+                                         c_stride, s_ab, s_c, skip, skip_value, tri);
     ++launch_count();
     RCWA_CUDA(cudaGetLastError());
 }

@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(128) zgemm_kernel(int m, int n, int k, int bat
                                                     long long a_stride, const zc* __restrict__ B, int ldb,
                                                     long long b_stride, const zc* C0, long long c0_stride, zc* C,
                                                     int ldc, long long c_stride, double s_ab, double s_c,
-                                                    const int* __restrict__ skip, int skip_value) {
+                                                    const int* __restrict__ skip, int skip_value, int tri) {
     const int tiles_m = (m + 31) / 32, tiles_n = (n + 7) / 8;
     const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long per = (long long)tiles_m * tiles_n;
@@ -347,8 +347,13 @@ __global__ void __launch_bounds__(128) zgemm_kernel(int m, int n, int k, int bat
     double ar[8], ai[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) ar[j] = ai[j] = 0.0;
+    // a triangular factor: the k range that can hold nonzeros for this warp's rows / columns
+    int p_begin = 0, p_end = k;
+    if (tri == TRI_A_LOWER) p_end = min(k, tm * 32 + 32);
+    else if (tri == TRI_A_UPPER) p_begin = tm * 32;
+    else if (tri == TRI_B_UPPER) p_end = min(k, c0 + 8);
     if (row < m) {
-        for (int p = 0; p < k; ++p) {
+        for (int p = p_begin; p < p_end; ++p) {
             const zc av = As[(long long)p * lda + row];
 #pragma unroll
             for (int j = 0; j < 8; ++j) {

@@ -148,9 +148,9 @@ DSBlock interface_block(Batch& c, const DModes& up, const DModes& low) {
 // (:794-808). Across the interface the amplitudes obey d_b = tp d_a + tm u_a and u_b = tm d_a + tp u_a (b
 // below, a above); with u_b = r d_b the same seam is
 //     r' = (tp - r tm)^-1 (r tp - tm),    g = tp + tm r',
-// one LU with n right-hand sides and one product instead of two LUs and four products. tp - r tm =
-// (I - r Rdu) tp is singular exactly when the reference's tp or I - Rdu r is (Sylvester's determinant
-// identity), so the samples that fail are the same ones.
+// one LU with n right-hand sides instead of two LUs and four products; g is only ever applied to vectors,
+// so it stays as its factors (KSeam). tp - r tm = (I - r Rdu) tp is singular exactly when the reference's tp
+// or I - Rdu r is (Sylvester's determinant identity), so the samples that fail are the same ones.
 Seam dense_on_analytic_seam(Batch& c, const DModes& up, const DModes& low, const DOp& r) {
     zc *tp, *tm;
     interface_matching(c, up, low, tp, tm);
@@ -162,10 +162,8 @@ Seam dense_on_analytic_seam(Batch& c, const DModes& up, const DModes& low, const
     if (r.kind == KDiag) ++c.n_solve;  // the reference's (I - Rdu r)^-1 Tdd
     c.mem->free(lhs);
     c.mem->free(rhs);
-    gemm(c, tm, c.nn(), rp, tp, 1.0, 1.0, tp);  // tp is now g
-    c.mem->free(tm);
     Seam out;
-    out.g = {KDense, tp};
+    out.g = {KSeam, tp, tm, nullptr, rp};
     out.r = {KDense, rp};
     return out;
 }
@@ -352,7 +350,7 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
         zc* cinv = nullptr;      // [[1/eps]]^{-1} (TM)
         bool herm = false;       // Hermitian operators: the Hermitian eigensolver path
         zc* einv_h = nullptr;    // Hermitian part of [[eps]]^{-1} (TM, herm)
-        zc *Linv = nullptr, *LinvH = nullptr;  // L^{-1}, L^{-H} of [[1/eps]] = L L^H (TM, herm)
+        zc *Lchol = nullptr, *Linv = nullptr, *LinvH = nullptr;  // L, L^{-1}, L^{-H} of [[1/eps]] = L L^H (TM, herm)
     };
     const bool try_herm = hermitian_path_enabled(opt);
     std::vector<LayerData> ld(L);
@@ -373,7 +371,7 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
                                            layer_fail);
             if (ld[k].herm)
                 ld[k].herm = make_hermitian_coefficients(st, c_inv, M) &&
-                             toeplitz_cholesky_inverse(st, c_inv, M, persist, ld[k].Linv, ld[k].LinvH);
+                             toeplitz_cholesky_inverse(st, c_inv, M, persist, ld[k].Lchol, ld[k].Linv, ld[k].LinvH);
             zc* E = persist.get<zc>(nn);
             ld[k].inv_eps = persist.get<zc>(nn);
             LAUNCH(toeplitz_kernel, nblocks(nn), kTpb, st, M, ld[k].c_eps, E);
@@ -448,8 +446,10 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
                     if (herm) {
                         // the pencil (mid, [[1/eps]]) as the Hermitian L^{-1} mid L^{-H}
                         zc* t = c.dense();
-                        launch_zgemm(st, n, n, n, B, mid, n, nn, ld[k].LinvH, n, 0, nullptr, 0, t, n, nn, 1.0, 0.0);
-                        launch_zgemm(st, n, n, n, B, ld[k].Linv, n, 0, t, n, nn, nullptr, 0, A, n, nn, 1.0, 0.0);
+                        launch_zgemm(st, n, n, n, B, mid, n, nn, ld[k].LinvH, n, 0, nullptr, 0, t, n, nn, 1.0, 0.0,
+                                     nullptr, 1, TRI_B_UPPER);
+                        launch_zgemm(st, n, n, n, B, ld[k].Linv, n, 0, t, n, nn, nullptr, 0, A, n, nn, 1.0, 0.0,
+                                     nullptr, 1, TRI_A_LOWER);
                         mem.free(t);
                     } else {
                         gemm(c, ld[k].cinv, 0, mid, nullptr, 1.0, 0.0, A);
@@ -463,14 +463,21 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
                 m.fzb = true;
                 zc* lam = c.vec();
                 m.W = c.dense();
+                zc* ly = nullptr;  // [[1/eps]] W (TM, herm)
                 if (herm) {
                     launch_eig_herm(st, n, B, A, nn, lam, m.W, info, ws, opt.eps, opt.max_iter, opt.eig_group);
-                    if (pol == RCWA_TM) {  // x = L^{-H} y, unit 2-norm like the general solver's vectors
+                    if (pol == RCWA_TM) {
+                        // x = L^{-H} y, unit 2-norm like the general solver's vectors, and [[1/eps]] x = L y with the
+                        // same column scale (V = [[1/eps]] W q without a full product)
                         zc* y = m.W;
                         m.W = c.dense();
-                        launch_zgemm(st, n, n, n, B, ld[k].LinvH, n, 0, y, n, nn, nullptr, 0, m.W, n, nn, 1.0, 0.0);
+                        ly = c.dense();
+                        launch_zgemm(st, n, n, n, B, ld[k].LinvH, n, 0, y, n, nn, nullptr, 0, m.W, n, nn, 1.0, 0.0,
+                                     nullptr, 1, TRI_A_UPPER);
+                        launch_zgemm(st, n, n, n, B, ld[k].Lchol, n, 0, y, n, nn, nullptr, 0, ly, n, nn, 1.0, 0.0, nullptr, 1,
+                                     TRI_A_LOWER);
                         mem.free(y);
-                        LAUNCH(normalize_cols_kernel, warp_blocks(nv), 128, st, B, n, m.W);
+                        LAUNCH(normalize_cols_kernel, warp_blocks(nv), 128, st, B, n, m.W, ly);
                         if (opt.diagnostics) gemm(c, ld[k].cinv, 0, mid, nullptr, 1.0, 0.0, A);  // the solve's A
                     }
                 } else {
@@ -492,6 +499,9 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
                 m.V = c.dense();
                 if (pol == RCWA_TE) {
                     LAUNCH(scale_cols_kernel, nblocks(nd), kTpb, st, B, n, m.W, bq, m.V, nullptr, 1);
+                } else if (ly) {
+                    LAUNCH(scale_cols_kernel, nblocks(nd), kTpb, st, B, n, ly, bq, m.V, nullptr, 1);
+                    mem.free(ly);
                 } else {
                     zc* cw = gemm(c, ld[k].inv_eps, 0, m.W, nullptr, 1.0, 0.0);
                     LAUNCH(scale_cols_kernel, nblocks(nd), kTpb, st, B, n, cw, bq, m.V, nullptr, 1);
@@ -682,6 +692,7 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
         // T = g[2L] ... g[1] down
         zc* cur = down;
         zc* nxt = c.vec();
+        zc* seam_t = c.vec();
         std::vector<zc*> a_plus(L, nullptr), a_minus(L, nullptr);
         for (int b = 1; b < block_count; ++b) {
             const int j = b / 2;
@@ -690,7 +701,14 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
                 RCWA_CUDA(cudaMemcpyAsync(a_plus[j], cur, nv * sizeof(zc), cudaMemcpyDeviceToDevice, st));
                 if (pure_films) LAUNCH(clear_unexcited_kernel, nblocks(nv), kTpb, st, B, n, M, a_plus[j]);
             }
-            LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 1, (int)g[b].kind, g[b].p, g[b].alt, g[b].alt_flag, cur, nxt);
+            if (g[b].kind == KSeam) {  // nxt = tp cur + tm (r' cur)
+                LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 1, g[b].rp, cur, nullptr, seam_t, 1.0, 0.0);
+                LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 1, g[b].alt, seam_t, nullptr, nxt, 1.0, 0.0);
+                LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 1, g[b].p, cur, nxt, nxt, 1.0, 1.0);
+            } else {
+                LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 1, (int)g[b].kind, g[b].p, g[b].alt, g[b].alt_flag,
+                       cur, nxt);
+            }
             std::swap(cur, nxt);
             if (fields && b % 2 != 0) {  // the reflection below applied at the layer's bottom (:1013-1020)
                 zc* bottom = cur;

@@ -173,12 +173,14 @@ __global__ void eig_residual_kernel(int B, int n, const zc* __restrict__ A, cons
 
 // ---------------------------------------------------------------- batched operator algebra
 
-enum Kind { KZero = 0, KDiag = 1, KDense = 2 };
+// KSeam: g = p + alt rp (tp + tm r' of a reduced seam), kept as its three factors and applied to vectors only
+enum Kind { KZero = 0, KDiag = 1, KDense = 2, KSeam = 3 };
 struct DOp {
     Kind kind = KZero;
     zc* p = nullptr;
     zc* alt = nullptr;           // per-sample dense alternative of a Diag g (exact q == 0 under dense r)
     const int* alt_flag = nullptr;
+    zc* rp = nullptr;            // KSeam: r'
 };
 struct DSBlock {
     DOp Tdd, Rdu, Rud, Tuu;
@@ -513,7 +515,8 @@ inline bool make_hermitian_coefficients(cudaStream_t st, zc* c, int M) {
 // Cholesky factor T = L L^H of the Hermitian Toeplitz matrix of the device coefficients c (host arithmetic,
 // once per layer), then Linv = L^{-1} and LinvH = L^{-H} on the device (column-major n x n). False when T
 // is not positive definite.
-inline bool toeplitz_cholesky_inverse(cudaStream_t st, const zc* c, int M, DeviceScratch& mem, zc*& Linv, zc*& LinvH) {
+inline bool toeplitz_cholesky_inverse(cudaStream_t st, const zc* c, int M, DeviceScratch& mem, zc*& Lfac, zc*& Linv,
+                                      zc*& LinvH) {
     const int n = 2 * M + 1, K = 4 * M + 1;
     std::vector<zc> h(K);
     RCWA_CUDA(cudaMemcpyAsync(h.data(), c, K * sizeof(zc), cudaMemcpyDeviceToHost, st));
@@ -541,15 +544,18 @@ inline bool toeplitz_cholesky_inverse(cudaStream_t st, const zc* c, int M, Devic
             X[(size_t)j * n + i] = -s / L[(size_t)i * n + i];
         }
     }
-    std::vector<zc> xi((size_t)n * n), xh((size_t)n * n);
+    std::vector<zc> lf((size_t)n * n), xi((size_t)n * n), xh((size_t)n * n);
     for (int j = 0; j < n; ++j)
         for (int i = 0; i < n; ++i) {
-            const cd v = X[(size_t)j * n + i];
+            const cd v = X[(size_t)j * n + i], l = L[(size_t)j * n + i];
+            lf[(size_t)j * n + i] = zc{l.real(), l.imag()};
             xi[(size_t)j * n + i] = zc{v.real(), v.imag()};
             xh[(size_t)i * n + j] = zc{v.real(), -v.imag()};
         }
+    Lfac = mem.get<zc>((size_t)n * n);
     Linv = mem.get<zc>((size_t)n * n);
     LinvH = mem.get<zc>((size_t)n * n);
+    RCWA_CUDA(cudaMemcpyAsync(Lfac, lf.data(), lf.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
     RCWA_CUDA(cudaMemcpyAsync(Linv, xi.data(), xi.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
     RCWA_CUDA(cudaMemcpyAsync(LinvH, xh.data(), xh.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
     RCWA_CUDA(cudaStreamSynchronize(st));
@@ -565,8 +571,9 @@ __global__ void hermitian_part_kernel(int n, const zc* __restrict__ E, zc* __res
     out[idx] = zc{0.5 * (a.re + b.re), 0.5 * (a.im - b.im)};
 }
 
-// every column of every matrix scaled to unit 2-norm (warp per column)
-__global__ void normalize_cols_kernel(int B, int n, zc* __restrict__ W) {
+// every column of every matrix scaled to unit 2-norm (warp per column); the same column of U (if given) is
+// scaled by the same factor
+__global__ void normalize_cols_kernel(int B, int n, zc* __restrict__ W, zc* __restrict__ U) {
     const long long col = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (col >= (long long)B * n) return;
     const int lane = threadIdx.x & 31;
@@ -580,6 +587,8 @@ __global__ void normalize_cols_kernel(int B, int n, zc* __restrict__ W) {
     for (int o = 16; o > 0; o >>= 1) ssq += __shfl_xor_sync(0xffffffffu, ssq, o);
     const double inv = 1.0 / (big * sqrt(ssq));
     for (int i = lane; i < n; i += 32) w[i] = w[i] * inv;
+    if (U)
+        for (int i = lane; i < n; i += 32) U[col * n + i] = U[col * n + i] * inv;
 }
 
 __global__ void toeplitz_kernel(int M, const zc* __restrict__ c, zc* __restrict__ m) {
