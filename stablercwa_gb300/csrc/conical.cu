@@ -242,6 +242,51 @@ __global__ void conical_scale_kykx_kernel(int B, int N, const zc* __restrict__ c
     out[idx] = (ky[b] * kx[(long long)b * N + m]) * cw[idx];
 }
 
+// Top interface in the reduced form: P = v W + w V, Q = v W - w V (rows scaled by the incident medium's
+// diagonal field factors w, v)
+__global__ void conical_top_pq_kernel(int B, int n, const zc* __restrict__ W, const zc* __restrict__ V,
+                                      const zc* __restrict__ w, const zc* __restrict__ v, zc* __restrict__ P,
+                                      zc* __restrict__ Q) {
+    const long long nn = (long long)n * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * nn) return;
+    const long long b = idx / nn;
+    const long long bi = b * n + (idx - b * nn) % n;
+    const zc a = v[bi] * W[idx], c = w[bi] * V[idx];
+    P[idx] = a + c;
+    Q[idx] = a - c;
+}
+// right-hand sides 2 w_j v_j e_j for the incident orders j = M (s input) and N + M (p input)
+__global__ void conical_top_rhs_kernel(int B, int n, int N, int M, const zc* __restrict__ w, const zc* __restrict__ v,
+                                       zc* __restrict__ rhs) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 2LL * B * n) return;
+    const long long b = idx / (2LL * n);
+    const int rem = (int)(idx - b * 2 * n), col = rem / n, i = rem - col * n;
+    const int j = col == 0 ? M : N + M;
+    rhs[idx] = i == j ? 2.0 * (w[b * n + j] * v[b * n + j]) : zc{0.0, 0.0};
+}
+// R from X = W (d_b + r d_b) and Y = V (d_b - r d_b), with d_a the unit incident column: row i from the
+// tangential E relation w_i (d_a + R)_i = X_i when |w_i| >= |v_i|, else from the H relation
+// v_i (d_a - R)_i = Y_i (w_i and v_i never vanish together)
+__global__ void conical_top_reflection_kernel(int B, int n, int N, int M, const zc* __restrict__ w,
+                                              const zc* __restrict__ v, const zc* __restrict__ X,
+                                              const zc* __restrict__ Y, zc* __restrict__ R) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 2LL * B * n) return;
+    const long long b = idx / (2LL * n);
+    const int rem = (int)(idx - b * 2 * n), col = rem / n, i = rem - col * n;
+    const double d = i == (col == 0 ? M : N + M) ? 1.0 : 0.0;
+    const zc wi = w[b * n + i], vi = v[b * n + i];
+    if (zabs(wi) >= zabs(vi)) {
+        const zc x = zdiv(X[idx], wi);
+        R[idx] = zc{x.re - d, x.im};
+    } else {
+        const zc y = zdiv(Y[idx], vi);
+        R[idx] = zc{d - y.re, -y.im};
+    }
+}
+
 // Full 2N operators P, Q and the (s, t) rotations of the Schur branch (rcwa1d_conical.hpp:468-485)
 __global__ void conical_schur_pq_kernel(int B, int N, const zc* __restrict__ inv_eps, const zc* __restrict__ A,
                                         const zc* __restrict__ c, const double* __restrict__ kx,
@@ -1091,8 +1136,12 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
     int* layer_fail = persist.zeros<int>(1);
     struct LayerData {
         zc *c_eps = nullptr, *einv = nullptr, *cmat = nullptr;
+        bool herm = false;       // real permittivities: the Hermitian eigensolver
+        zc* einv_h = nullptr;    // Hermitian part of [[eps]]^{-1}
+        zc *Lchol = nullptr, *Linv = nullptr, *LinvH = nullptr;  // [[1/eps]] = L L^H
     };
     std::vector<LayerData> ld(L);
+    const bool try_herm = hermitian_path_enabled(opt);
     for (int k : grating) {
         const rcwa_layer1d& Ly = *layers[k];
         std::vector<double> edges(Ly.edges, Ly.edges + Ly.n_segments + 1);
@@ -1106,6 +1155,9 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                                          layer_fail);
         zc* c_inv = layer_coefficients(st, persist, edges, inv, stack.period, M, Ly.fourier_method, Ly.fft_samples,
                                        layer_fail);
+        ld[k].herm = try_herm && make_hermitian_coefficients(st, ld[k].c_eps, M) &&
+                     make_hermitian_coefficients(st, c_inv, M) &&
+                     toeplitz_cholesky_inverse(st, c_inv, M, persist, ld[k].Lchol, ld[k].Linv, ld[k].LinvH);
         zc* E = persist.get<zc>(NN);
         zc* Ci = persist.get<zc>(NN);
         LAUNCH(toeplitz_kernel, nblocks(NN), kTpb, st, M, ld[k].c_eps, E);
@@ -1114,7 +1166,14 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
         ld[k].cmat = persist.get<zc>(NN);
         launch_lu_solve(st, N, N, 1, E, NN, E, NN, RHS_IDENTITY, nullptr, NN, ld[k].einv, NN, layer_fail);
         launch_lu_solve(st, N, N, 1, Ci, NN, Ci, NN, RHS_IDENTITY, nullptr, NN, ld[k].cmat, NN, layer_fail);
+        if (ld[k].herm) {
+            ld[k].einv_h = persist.get<zc>(NN);
+            LAUNCH(hermitian_part_kernel, nblocks(NN), kTpb, st, N, ld[k].einv, ld[k].einv_h);
+        }
     }
+    bool all_herm = !grating.empty();
+    for (int k : grating) all_herm = all_herm && ld[k].herm;
+    const bool reduced = reduced_seams_enabled();
     const int base_solves = 2 * static_cast<int>(grating.size());
 
     long long per_sample = 16LL * (nn * 16 + NN * 12 * (long long)grating.size() + (long long)n * 8 * (L + 2)) +
@@ -1184,16 +1243,31 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                 zc* AB = ABall + 2 * ndN * gi;
                 LAUNCH(assemble_te_kernel, nblocks(ndN), kTpb, st, B, M, ld[k].c_eps, kx, AB);
                 zc* Bm = mem.get<zc>(ndN);
-                LAUNCH(conical_b_kernel, nblocks(ndN), kTpb, st, B, N, ld[k].einv, kx, Bm);
-                launch_zgemm(st, N, N, N, B, Bm, N, NN, ld[k].cmat, N, 0, nullptr, 0, AB + ndN, N, NN, 1.0, 0.0);
+                LAUNCH(conical_b_kernel, nblocks(ndN), kTpb, st, B, N, all_herm ? ld[k].einv_h : ld[k].einv, kx, Bm);
+                if (all_herm) {
+                    // B C x = lambda x with C = [[1/eps]]^{-1} = (L L^H)^{-1} is the Hermitian-definite pencil
+                    // (B, L L^H): L^{-1} B L^{-H} z = lambda z, x = L z
+                    zc* t = mem.get<zc>(ndN);
+                    launch_zgemm(st, N, N, N, B, Bm, N, NN, ld[k].LinvH, N, 0, nullptr, 0, t, N, NN, 1.0, 0.0, nullptr, 1,
+                                 TRI_B_UPPER);
+                    launch_zgemm(st, N, N, N, B, ld[k].Linv, N, 0, t, N, NN, nullptr, 0, AB + ndN, N, NN, 1.0, 0.0, nullptr,
+                                 1, TRI_A_LOWER);
+                    mem.free(t);
+                } else {
+                    launch_zgemm(st, N, N, N, B, Bm, N, NN, ld[k].cmat, N, 0, nullptr, 0, AB + ndN, N, NN, 1.0, 0.0);
+                }
                 mem.free(Bm);
                 LAUNCH(finite_check_kernel, nblocks(ndN), kTpb, st, B, NN, AB, c.fail);
                 LAUNCH(finite_check_kernel, nblocks(ndN), kTpb, st, B, NN, AB + ndN, c.fail);
             }
             {
                 zc* ws = mem.get<zc>((size_t)(eig_workspace_bytes(N, 2 * B * n_gr) / sizeof(zc)) + 1);
-                launch_eig(st, N, 2 * B * n_gr, ABall, NN, lamall, vecall, infoall, nullptr, ws, opt.eps, opt.max_iter,
-                           opt.eig_group);
+                if (all_herm)
+                    launch_eig_herm(st, N, 2 * B * n_gr, ABall, NN, lamall, vecall, infoall, ws, opt.eps, opt.max_iter,
+                                    opt.eig_group);
+                else
+                    launch_eig(st, N, 2 * B * n_gr, ABall, NN, lamall, vecall, infoall, nullptr, ws, opt.eps, opt.max_iter,
+                               opt.eig_group);
                 mem.free(ws);
             }
             for (int gi = 0; gi < n_gr; ++gi) {
@@ -1210,7 +1284,18 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                 LAUNCH(conical_lambda_kernel, warp_blocks(B), 128, st, B, N, lam, info, P.ky, min_abs, R.schur, any_flag);
                 // general region (every sample not switched to the Schur basis)
                 zc* cw = mem.get<zc>(ndN);
-                launch_zgemm(st, N, N, N, B, ld[k].cmat, N, 0, vec + ndN, N, NN, nullptr, 0, cw, N, NN, 1.0, 0.0);
+                if (all_herm) {
+                    // x = L z and C x = L^{-H} z (the pencil's vectors; the region normalises each mode itself)
+                    zc* x = mem.get<zc>(ndN);
+                    launch_zgemm(st, N, N, N, B, ld[k].Lchol, N, 0, vec + ndN, N, NN, nullptr, 0, x, N, NN, 1.0, 0.0,
+                                 nullptr, 1, TRI_A_LOWER);
+                    launch_zgemm(st, N, N, N, B, ld[k].LinvH, N, 0, vec + ndN, N, NN, nullptr, 0, cw, N, NN, 1.0, 0.0,
+                                 nullptr, 1, TRI_A_UPPER);
+                    RCWA_CUDA(cudaMemcpyAsync(vec + ndN, x, ndN * sizeof(zc), cudaMemcpyDeviceToDevice, st));
+                    mem.free(x);
+                } else {
+                    launch_zgemm(st, N, N, N, B, ld[k].cmat, N, 0, vec + ndN, N, NN, nullptr, 0, cw, N, NN, 1.0, 0.0);
+                }
                 zc* sc = mem.get<zc>(ndN);
                 LAUNCH(conical_scale_kykx_kernel, nblocks(ndN), kTpb, st, B, N, cw, kx, P.ky, sc);
                 zc* coupling = mem.get<zc>(ndN);
@@ -1295,6 +1380,15 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
         DOp r;
         for (int b = block_count - 1; b >= 1; --b) {
             const int j = b / 2;
+            if (b % 2 == 0 && reduced && !(modes[j].analytic && modes[j + 1].analytic)) {
+                zc *tp, *tm;
+                interface_matching(c, modes[j], modes[j + 1], tp, tm);
+                Seam seam = reduced_seam(c, tp, tm, r);
+                if (r.kind != KZero) mem.free(r.p);
+                g[b] = seam.g;
+                r = seam.r;
+                continue;
+            }
             if (b % 2 == 0) {
                 DSBlock blk = interface_block(c, modes[j], modes[j + 1]);
                 if (blk.Tdd.kind == KDiag && r.kind != KDense) {
@@ -1356,49 +1450,81 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
         // ---- 3. top interface, columns M and N + M (rcwa1d_conical.hpp:891-919)
         zc* tdd = mem.get<zc>(2 * nv);
         zc* rud = mem.get<zc>(2 * nv);
-        DOp topRdu, topTuu;
-        if (modes[0].analytic && modes[1].analytic) {
-            zc* Tdd = c.vec();
-            zc* Rdu = c.vec();
-            zc* Rud = c.vec();
-            zc* Tuu = c.vec();
-            LAUNCH(conical_diag_interface_kernel, nblocks(nv), kTpb, st, nv, modes[0].w, modes[0].v, modes[1].w,
-                   modes[1].v, Tdd, Rdu, Rud, Tuu);
-            LAUNCH(conical_top_diag_kernel, nblocks(2 * nv), kTpb, st, B, n, M, Tdd, Rud, tdd, rud);
-            topRdu = {KDiag, Rdu};
-            topTuu = {KDiag, Tuu};
+        zc* down = nullptr;
+        if (reduced && modes[0].analytic && !modes[1].analytic && r.kind == KDense) {
+            // With the incident medium's diagonal field factors w, v: w (d_a + u_a) = W (I + r) d_b and
+            // v (d_a - u_a) = V (I - r) d_b, so (v W + w V + (v W - w V) r) d_b = 2 w v d_a -- one GEMM and one LU
+            // with the two incident columns for the reference's three LUs with 2N right-hand sides and one with
+            // two; R from whichever relation has the larger coefficient in each row, so no division by a
+            // vanishing w or v (an order grazing in the incident medium).
+            zc* Pm = c.dense();
+            zc* Qm = c.dense();
+            LAUNCH(conical_top_pq_kernel, nblocks(nd), kTpb, st, B, n, modes[1].W, modes[1].V, modes[0].w, modes[0].v, Pm,
+                   Qm);
+            gemm(c, Qm, nn, r.p, Pm, 1.0, 1.0, Pm);
+            mem.free(Qm);
+            zc* rhs = mem.get<zc>(2 * nv);
+            LAUNCH(conical_top_rhs_kernel, nblocks(2 * nv), kTpb, st, B, n, N, M, modes[0].w, modes[0].v, rhs);
+            down = solve(c, Pm, true, RHS_DENSE, rhs, 2);
+            c.n_solve += 3;
+            mem.free(Pm);
+            mem.free(rhs);
+            zc* t1 = mem.get<zc>(2 * nv);
+            zc* t2 = mem.get<zc>(2 * nv);
+            LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 2, r.p, down, down, t1, 1.0, 1.0);
+            LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 2, r.p, down, down, t2, -1.0, 1.0);
+            zc* X = mem.get<zc>(2 * nv);
+            zc* Y = mem.get<zc>(2 * nv);
+            LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 2, modes[1].W, t1, nullptr, X, 1.0, 0.0);
+            LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 2, modes[1].V, t2, nullptr, Y, 1.0, 0.0);
+            LAUNCH(conical_top_reflection_kernel, nblocks(2 * nv), kTpb, st, B, n, N, M, modes[0].w, modes[0].v, X, Y, rud);
+            for (zc* ptr : {t1, t2, X, Y}) mem.free(ptr);
         } else {
-            zc *tp, *tm;
-            interface_matching(c, modes[0], modes[1], tp, tm);
-            zc* tpi = solve(c, tp, false, RHS_IDENTITY, nullptr);
-            zc* rdu = gemm(c, tm, nn, tpi, nullptr, 1.0, 0.0);
-            zc* tm_e = mem.get<zc>(2 * nv);
-            LAUNCH(col_extract_kernel, nblocks(nv), kTpb, st, B, n, tm, M, tm_e, 2, 0);
-            LAUNCH(col_extract_kernel, nblocks(nv), kTpb, st, B, n, tm, N + M, tm_e, 2, 1);
-            LAUNCH(col_extract_kernel, nblocks(nv), kTpb, st, B, n, tp, M, tdd, 2, 0);
-            LAUNCH(col_extract_kernel, nblocks(nv), kTpb, st, B, n, tp, N + M, tdd, 2, 1);
-            LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 2, rdu, tm_e, tdd, tdd, -1.0, 1.0);
-            LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 2, tpi, tm_e, nullptr, rud, -1.0, 0.0);
-            mem.free(tp);
-            mem.free(tm);
-            topRdu = {KDense, rdu};
-            topTuu = {KDense, tpi};
+            DOp topRdu, topTuu;
+            if (modes[0].analytic && modes[1].analytic) {
+                zc* Tdd = c.vec();
+                zc* Rdu = c.vec();
+                zc* Rud = c.vec();
+                zc* Tuu = c.vec();
+                LAUNCH(conical_diag_interface_kernel, nblocks(nv), kTpb, st, nv, modes[0].w, modes[0].v, modes[1].w,
+                       modes[1].v, Tdd, Rdu, Rud, Tuu);
+                LAUNCH(conical_top_diag_kernel, nblocks(2 * nv), kTpb, st, B, n, M, Tdd, Rud, tdd, rud);
+                topRdu = {KDiag, Rdu};
+                topTuu = {KDiag, Tuu};
+            } else {
+                zc *tp, *tm;
+                interface_matching(c, modes[0], modes[1], tp, tm);
+                zc* tpi = solve(c, tp, false, RHS_IDENTITY, nullptr);
+                zc* rdu = gemm(c, tm, nn, tpi, nullptr, 1.0, 0.0);
+                zc* tm_e = mem.get<zc>(2 * nv);
+                LAUNCH(col_extract_kernel, nblocks(nv), kTpb, st, B, n, tm, M, tm_e, 2, 0);
+                LAUNCH(col_extract_kernel, nblocks(nv), kTpb, st, B, n, tm, N + M, tm_e, 2, 1);
+                LAUNCH(col_extract_kernel, nblocks(nv), kTpb, st, B, n, tp, M, tdd, 2, 0);
+                LAUNCH(col_extract_kernel, nblocks(nv), kTpb, st, B, n, tp, N + M, tdd, 2, 1);
+                LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 2, rdu, tm_e, tdd, tdd, -1.0, 1.0);
+                LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 2, tpi, tm_e, nullptr, rud, -1.0, 0.0);
+                mem.free(tp);
+                mem.free(tm);
+                topRdu = {KDense, rdu};
+                topTuu = {KDense, tpi};
+            }
+            DOp k = op_mul(c, topRdu, r);
+            down = tdd;
+            if (k.kind == KDiag) {
+                LAUNCH(vec_div_one_minus_kernel, nblocks(2 * nv), kTpb, st, B, n, 2, down, k.p);
+            } else if (k.kind == KDense) {
+                LAUNCH(identity_minus_kernel, nblocks(nd), kTpb, st, B, n, k.p, nullptr, 1);
+                down = solve(c, k.p, true, RHS_DENSE, tdd, 2);
+            }
+            zc* rdn = mem.get<zc>(2 * nv);
+            LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 2, (int)r.kind, r.p, nullptr, nullptr, down, rdn);
+            zc* back = mem.get<zc>(2 * nv);
+            LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 2, (int)topTuu.kind, topTuu.p, nullptr, nullptr, rdn, back);
+            LAUNCH(vec_add_kernel, nblocks(2 * nv), kTpb, st, 2 * nv, back, rud);
         }
-        DOp k = op_mul(c, topRdu, r);
-        zc* down = tdd;
-        if (k.kind == KDiag) {
-            LAUNCH(vec_div_one_minus_kernel, nblocks(2 * nv), kTpb, st, B, n, 2, down, k.p);
-        } else if (k.kind == KDense) {
-            LAUNCH(identity_minus_kernel, nblocks(nd), kTpb, st, B, n, k.p, nullptr, 1);
-            down = solve(c, k.p, true, RHS_DENSE, tdd, 2);
-        }
-        zc* rdn = mem.get<zc>(2 * nv);
-        LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 2, (int)r.kind, r.p, nullptr, nullptr, down, rdn);
-        zc* back = mem.get<zc>(2 * nv);
-        LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 2, (int)topTuu.kind, topTuu.p, nullptr, nullptr, rdn, back);
-        LAUNCH(vec_add_kernel, nblocks(2 * nv), kTpb, st, 2 * nv, back, rud);
         zc* cur = down;
         zc* nxt = mem.get<zc>(2 * nv);
+        zc* seam_t = mem.get<zc>(2 * nv);
         for (int b = 1; b < block_count; ++b) {
             const int j = b / 2;
             if (fields && b % 2 != 0) {  // amplitudes at the layer's top (rcwa1d_conical.hpp:921-925)
@@ -1407,8 +1533,11 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                 if (pure_films)
                     LAUNCH(conical_clear_unexcited_kernel, nblocks(2 * nv), kTpb, st, 2 * nv, n, N, M, cap.a_plus[j]);
             }
-            LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 2, (int)g[b].kind, g[b].p, g[b].alt, g[b].alt_flag, cur,
-                   nxt);
+            if (g[b].kind == KSeam)
+                apply_seam(c, g[b], 2, cur, seam_t, nxt);
+            else
+                LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 2, (int)g[b].kind, g[b].p, g[b].alt, g[b].alt_flag,
+                       cur, nxt);
             std::swap(cur, nxt);
             if (fields && b % 2 != 0) {  // the reflection below applied at the layer's bottom (:926-931)
                 zc* bottom = cur;

@@ -143,31 +143,6 @@ DSBlock interface_block(Batch& c, const DModes& up, const DModes& low) {
     return s;
 }
 
-// The seam of a dense region over an analytic one with a diagonal (or zero) reflection r below it. The
-// reference stacks the interface block (Tdd, Rdu, Rud, Tuu from tp^-1; rcwa1d.hpp:694-712) on r
-// (:794-808). Across the interface the amplitudes obey d_b = tp d_a + tm u_a and u_b = tm d_a + tp u_a (b
-// below, a above); with u_b = r d_b the same seam is
-//     r' = (tp - r tm)^-1 (r tp - tm),    g = tp + tm r',
-// one LU with n right-hand sides instead of two LUs and four products; g is only ever applied to vectors,
-// so it stays as its factors (KSeam). tp - r tm = (I - r Rdu) tp is singular exactly when the reference's tp
-// or I - Rdu r is (Sylvester's determinant identity), so the samples that fail are the same ones.
-Seam dense_on_analytic_seam(Batch& c, const DModes& up, const DModes& low, const DOp& r) {
-    zc *tp, *tm;
-    interface_matching(c, up, low, tp, tm);
-    zc* lhs = c.dense();
-    zc* rhs = c.dense();
-    LAUNCH(seam_system_kernel, nblocks((long long)c.B * c.nn()), kTpb, c.st, c.B, c.n, tp, tm,
-           r.kind == KDiag ? r.p : nullptr, lhs, rhs);
-    zc* rp = solve(c, lhs, true, RHS_DENSE, rhs);
-    if (r.kind == KDiag) ++c.n_solve;  // the reference's (I - Rdu r)^-1 Tdd
-    c.mem->free(lhs);
-    c.mem->free(rhs);
-    Seam out;
-    out.g = {KSeam, tp, tm, nullptr, rp};
-    out.r = {KDense, rp};
-    return out;
-}
-
 }  // namespace
 
 // ---------------------------------------------------------------- validation
@@ -545,9 +520,11 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
                 r = {KDiag, rv};
                 continue;
             }
-            if (b % 2 == 0 && reduced && !modes[j].analytic && modes[j + 1].analytic && r.kind != KDense) {
-                Seam seam = dense_on_analytic_seam(c, modes[j], modes[j + 1], r);
-                if (r.kind == KDiag) mem.free(r.p);
+            if (b % 2 == 0 && reduced && !(modes[j].analytic && modes[j + 1].analytic)) {
+                zc *tp, *tm;
+                interface_matching(c, modes[j], modes[j + 1], tp, tm);
+                Seam seam = reduced_seam(c, tp, tm, r);
+                if (r.kind != KZero) mem.free(r.p);
                 g[b] = seam.g;
                 r = seam.r;
                 continue;
@@ -701,10 +678,8 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
                 RCWA_CUDA(cudaMemcpyAsync(a_plus[j], cur, nv * sizeof(zc), cudaMemcpyDeviceToDevice, st));
                 if (pure_films) LAUNCH(clear_unexcited_kernel, nblocks(nv), kTpb, st, B, n, M, a_plus[j]);
             }
-            if (g[b].kind == KSeam) {  // nxt = tp cur + tm (r' cur)
-                LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 1, g[b].rp, cur, nullptr, seam_t, 1.0, 0.0);
-                LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 1, g[b].alt, seam_t, nullptr, nxt, 1.0, 0.0);
-                LAUNCH(matvec_kernel, warp_blocks(B), 128, st, B, n, 1, g[b].p, cur, nxt, nxt, 1.0, 1.0);
+            if (g[b].kind == KSeam) {
+                apply_seam(c, g[b], 1, cur, seam_t, nxt);
             } else {
                 LAUNCH(apply_g_kernel, warp_blocks(B), 128, st, B, n, 1, (int)g[b].kind, g[b].p, g[b].alt, g[b].alt_flag,
                        cur, nxt);

@@ -305,6 +305,42 @@ Seam stack_on(Batch& c, DSBlock&& s, const DOp& r) {
 }
 
 
+// The reduced form of an interface block with a dense side stacked on the reflection r below it. With the
+// interface relations d_b = tp d_a + tm u_a, u_b = tm d_a + tp u_a (b below, a above; tp, tm from
+// interface_matching) and u_b = r d_b:
+//     r' = (tp - r tm)^-1 (r tp - tm),    g = tp + tm r',
+// one LU with n right-hand sides (and two products when r is dense) in place of the reference's tp^-1,
+// three products, the stacking solve and two more products (rcwa1d.hpp:694-712, :794-808). g is only ever
+// applied to vectors, so it stays as its factors (KSeam). tp - r tm = (I - r Rdu) tp is singular exactly
+// when tp or I - Rdu r is (Sylvester's determinant identity), so the failing samples are the same;
+// n_solve keeps the reference's count.
+Seam reduced_seam(Batch& c, zc* tp, zc* tm, const DOp& r) {
+    const long long nd = (long long)c.B * c.nn();
+    zc* lhs = c.dense();
+    zc* rhs = c.dense();
+    if (r.kind == KDense) {
+        gemm(c, r.p, c.nn(), tm, tp, -1.0, 1.0, lhs);  // tp - r tm
+        gemm(c, r.p, c.nn(), tp, tm, 1.0, -1.0, rhs);  // r tp - tm
+    } else {
+        LAUNCH(seam_system_kernel, nblocks(nd), kTpb, c.st, c.B, c.n, tp, tm, r.kind == KDiag ? r.p : nullptr, lhs, rhs);
+    }
+    zc* rp = solve(c, lhs, true, RHS_DENSE, rhs);
+    if (r.kind != KZero) ++c.n_solve;  // the reference's stacking solve (I - Rdu r)^-1 Tdd
+    c.mem->free(lhs);
+    c.mem->free(rhs);
+    Seam out;
+    out.g = {KSeam, tp, tm, nullptr, rp};
+    out.r = {KDense, rp};
+    return out;
+}
+
+// y = g x for a KSeam g = tp + tm r' (cols right-hand sides); t is scratch of the size of x
+inline void apply_seam(Batch& c, const DOp& g, int cols, const zc* x, zc* t, zc* y) {
+    LAUNCH(matvec_kernel, warp_blocks(c.B), 128, c.st, c.B, c.n, cols, g.rp, x, nullptr, t, 1.0, 0.0);
+    LAUNCH(matvec_kernel, warp_blocks(c.B), 128, c.st, c.B, c.n, cols, g.alt, t, nullptr, y, 1.0, 0.0);
+    LAUNCH(matvec_kernel, warp_blocks(c.B), 128, c.st, c.B, c.n, cols, g.p, x, y, y, 1.0, 1.0);
+}
+
 // ---------------------------------------------------------------- Fourier coefficients (host)
 
 using cd = std::complex<double>;
