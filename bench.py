@@ -648,10 +648,11 @@ def run_serve(args):
     return 0
 
 
-def run_eig_only(n, batch, group):
-    """Profiling case for the eigensolver alone: `batch` lossy layer matrices of order n in the
-    benchmark's form (Toeplitz of a binary grating, index 1.46+0.01i, fill 0.4, plus Kx^2 with
-    sin(theta) in 0.75..0.95, lambda/period 0.61), eigensolved twice on device."""
+def run_eig_only(n, batch, group, hermitian=False):
+    """Profiling case for the eigensolver alone: `batch` layer matrices of order n in the benchmark's
+    form (Toeplitz of a binary grating, index 1.46+0.01i, fill 0.4, plus Kx^2 with sin(theta) in
+    0.75..0.95, lambda/period 0.61), eigensolved twice on device by the general solver; with
+    `hermitian`, the lossless index 1.46 and the Hermitian solver."""
     import torch
     from stablercwa_gb300.engine import Engine
     if group:
@@ -659,7 +660,7 @@ def run_eig_only(n, batch, group):
     rng = np.random.default_rng(1)
     M = n // 2
     h = np.subtract.outer(np.arange(n), np.arange(n))
-    e1 = complex(1.46, 0.01) ** 2
+    e1 = complex(1.46, 0.0 if hermitian else 0.01) ** 2
     with np.errstate(invalid="ignore", divide="ignore"):
         eps = np.where(h == 0, 0.4 * e1 + 0.6, (e1 - 1) * np.sin(np.pi * h * 0.4) / (np.pi * h))
     mats = []
@@ -674,10 +675,14 @@ def run_eig_only(n, batch, group):
     dI = torch.empty(batch, dtype=torch.int32, device="cuda")
     eng = Engine()
     for _ in range(2):
-        eng.eig_batch_device(n, batch, dA.data_ptr(), dW.data_ptr(), dV.data_ptr(), dI.data_ptr())
+        if hermitian:
+            eng.eig_hermitian_batch_device(n, batch, dA.data_ptr(), dW.data_ptr(), dV.data_ptr(), dI.data_ptr())
+        else:
+            eng.eig_batch_device(n, batch, dA.data_ptr(), dW.data_ptr(), dV.data_ptr(), dI.data_ptr())
         eng.synchronize()
     bad = int((dI != 0).sum().item())
-    print(json.dumps({"eig_only": {"n": n, "batch": batch, "group": group, "not_converged": bad}}))
+    print(json.dumps({"eig_only": {"n": n, "batch": batch, "group": group, "hermitian": hermitian,
+                                   "not_converged": bad}}))
     return 0 if bad == 0 else 1
 
 
@@ -697,11 +702,12 @@ def main():
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[0.5, 1.0])
     ap.add_argument("--workload", choices=["c2", "c3", "c4", "plain", "serve"], default="c2",
                     help="c2 (default, the headline line), c3 conical, c4 2-D, plain one-point-per-call")
+    ap.add_argument("--hermitian", action="store_true", help="--eig-only: lossless matrices, Hermitian solver")
     ap.add_argument("--eig-only", nargs=2, type=int, metavar=("N", "BATCH"), default=None,
                     help="profiling case: the eigensolver alone on BATCH layer matrices of order N")
     args = ap.parse_args()
     if args.eig_only:
-        return run_eig_only(args.eig_only[0], args.eig_only[1], args.eig_group)
+        return run_eig_only(args.eig_only[0], args.eig_only[1], args.eig_group, args.hermitian)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "serve":

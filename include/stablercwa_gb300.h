@@ -385,6 +385,17 @@ int rcwa_gpu_eig_batch_dev(rcwa_gpu_ctx* ctx, int n, int batch, const rcwa_compl
                            int max_iter, rcwa_complex* d_values, rcwa_complex* d_vectors, int* d_info,
                            int* d_sweeps);
 
+/* Batched Hermitian eigensolver. No counterpart in the reference: the solver the engine uses for layers
+ * with real permittivities (Householder tridiagonalisation, implicit QL with Wilkinson shifts, eigenvectors
+ * accumulated). It solves the Hermitian part (a + a^H) / 2 of each of the batch n x n matrices in a (a itself
+ * when a is Hermitian). values[batch*n] are real (imaginary parts 0) in the order the QL iteration leaves
+ * them, not sorted; vectors[batch*n*n] have orthonormal columns; info[batch] is 0 or the 1-based index of
+ * the eigenvalue that hit max_iter. eps and max_iter as in rcwa_gpu_eig_batch. */
+int rcwa_gpu_eig_hermitian_batch(rcwa_gpu_ctx* ctx, int n, int batch, const rcwa_complex* a, double eps, int max_iter,
+                                 rcwa_complex* values, rcwa_complex* vectors, int* info);
+int rcwa_gpu_eig_hermitian_batch_dev(rcwa_gpu_ctx* ctx, int n, int batch, const rcwa_complex* d_a, double eps,
+                                     int max_iter, rcwa_complex* d_values, rcwa_complex* d_vectors, int* d_info);
+
 /* Batched eigensolver that allocates nothing. No counterpart in the reference: it is the
  * rcwa_gpu_eig_batch_dev computation (same kernel and default lanes per matrix, so the same results) for callers
  * that may not allocate device memory -- a host whose own caching allocator holds the HBM, or a

@@ -620,6 +620,58 @@ int rcwa_gpu_eig_batch_dev(rcwa_gpu_ctx* ctx, int n, int batch, const rcwa_compl
     });
 }
 
+namespace {
+void check_eig_args(int n, int batch, double eps, int max_iter) {
+    if (n < 0 || batch < 0) throw EngineError{RCWA_EINVAL, "eig: negative size"};
+    if (max_iter < 1) throw EngineError{RCWA_EINVAL, "eig_qr: max_iter must be >= 1"};
+    if (!(eps >= 0.0) || !std::isfinite(eps)) throw EngineError{RCWA_EINVAL, "eig_qr: eps must be finite and >= 0"};
+}
+int eig_group_from_env() {
+    const char* g = std::getenv("RCWA_GB300_EIG_GROUP");
+    return g ? std::atoi(g) : 0;
+}
+}  // namespace
+
+int rcwa_gpu_eig_hermitian_batch_dev(rcwa_gpu_ctx* ctx, int n, int batch, const rcwa_complex* d_a, double eps,
+                                     int max_iter, rcwa_complex* d_values, rcwa_complex* d_vectors, int* d_info) {
+    return guarded(ctx, [&] {
+        check_eig_args(n, batch, eps, max_iter);
+        if (n == 0 || batch == 0) return;
+        if (!d_a || !d_values || !d_vectors || !d_info) throw EngineError{RCWA_EINVAL, "eig: null argument"};
+        DeviceScratch mem(ctx->stream);
+        zc* ws = mem.get<zc>((size_t)(eig_workspace_bytes(n, batch) / sizeof(zc)) + 1);
+        launch_eig_herm(ctx->stream, n, batch, reinterpret_cast<const zc*>(d_a), (long long)n * n,
+                        reinterpret_cast<zc*>(d_values), reinterpret_cast<zc*>(d_vectors), d_info, ws, eps, max_iter,
+                        eig_group_from_env());
+    });
+}
+
+int rcwa_gpu_eig_hermitian_batch(rcwa_gpu_ctx* ctx, int n, int batch, const rcwa_complex* a, double eps, int max_iter,
+                                 rcwa_complex* values, rcwa_complex* vectors, int* info) {
+    return guarded(ctx, [&] {
+        check_eig_args(n, batch, eps, max_iter);
+        if (n == 0 || batch == 0) return;
+        if (!a || !values || !vectors || !info) throw EngineError{RCWA_EINVAL, "eig: null argument"};
+        const size_t nn = (size_t)n * n * batch;
+        for (size_t k = 0; k < nn; ++k)
+            if (!std::isfinite(a[k].re) || !std::isfinite(a[k].im))
+                throw EngineError{RCWA_EINVAL, "eig_qr: matrix has non-finite entries"};
+        const cudaStream_t st = ctx->stream;
+        DeviceScratch mem(st);
+        zc* da = mem.get<zc>(nn);
+        zc* dw = mem.get<zc>((size_t)n * batch);
+        zc* dv = mem.get<zc>(nn);
+        int* di = mem.get<int>(batch);
+        zc* ws = mem.get<zc>((size_t)(eig_workspace_bytes(n, batch) / sizeof(zc)) + 1);
+        RCWA_CUDA(cudaMemcpyAsync(da, a, nn * sizeof(zc), cudaMemcpyHostToDevice, st));
+        launch_eig_herm(st, n, batch, da, (long long)n * n, dw, dv, di, ws, eps, max_iter, eig_group_from_env());
+        RCWA_CUDA(cudaMemcpyAsync(values, dw, (size_t)n * batch * sizeof(zc), cudaMemcpyDeviceToHost, st));
+        RCWA_CUDA(cudaMemcpyAsync(vectors, dv, nn * sizeof(zc), cudaMemcpyDeviceToHost, st));
+        RCWA_CUDA(cudaMemcpyAsync(info, di, batch * sizeof(int), cudaMemcpyDeviceToHost, st));
+        RCWA_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
 int rcwa_gpu_eig_batch(rcwa_gpu_ctx* ctx, int n, int batch, const rcwa_complex* a, double eps, int max_iter,
                        rcwa_complex* values, rcwa_complex* vectors, int* info, int* sweeps) {
     return guarded(ctx, [&] {

@@ -897,6 +897,110 @@ struct Region {
     int* schur = nullptr;                         // per-sample Schur flag (nullptr: none)
 };
 
+// One grating's flagged samples awaiting the Schur basis: H = P Q of the full 2N operator and Q, both in the
+// chunk's layout and meaningful where the region's schur flag is set
+struct SchurJob {
+    int layer;
+    zc* H;
+    zc* Q;
+};
+
+// the flagged samples' matrices gathered from the per-grating buffers into one compact batch, and back:
+// compact matrix t is sample map[t].y of grating job map[t].x
+__global__ void gather_flagged_kernel(int total, long long per, const zc* const* __restrict__ src,
+                                      const int2* __restrict__ map, zc* __restrict__ dst) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)total * per) return;
+    const long long t = idx / per, e = idx - t * per;
+    const int2 m = map[t];
+    dst[idx] = src[m.x][(long long)m.y * per + e];
+}
+__global__ void scatter_flagged_kernel(int total, long long per, zc* const* __restrict__ dst,
+                                       const int2* __restrict__ map, const zc* __restrict__ src) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)total * per) return;
+    const long long t = idx / per, e = idx - t * per;
+    const int2 m = map[t];
+    dst[m.x][(long long)m.y * per + e] = src[idx];
+}
+__global__ void scatter_flagged_info_kernel(int total, int* const* __restrict__ dst, const int2* __restrict__ map,
+                                            const int* __restrict__ src) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    dst[map[t].x][map[t].y] = src[t];
+}
+
+// The Schur basis of every flagged sample of every grating (rcwa1d_conical.hpp:466-502). A grating has a
+// few such samples and each eigensolve of order 2N runs on one SM, so the gratings' H matrices are gathered
+// into one batch and solved in one launch, side by side rather than one grating after another. Then per
+// grating: the principal square root G of the Schur form T, W = Z, V from V G = Q Z, q = diag(G).
+void conical_schur_modes(Batch& c, const std::vector<SchurJob>& jobs, std::vector<Region>& modes, int* eig_info,
+                         int* schur_count, int eig_group) {
+    const cudaStream_t st = c.st;
+    DeviceScratch& mem = *c.mem;
+    const int B = c.B, n = c.n, J = (int)jobs.size();
+    const long long nn = c.nn(), nd = (long long)B * nn;
+    std::vector<int> flags((size_t)J * B);
+    for (int q = 0; q < J; ++q)
+        RCWA_CUDA(cudaMemcpyAsync(flags.data() + (size_t)q * B, modes[jobs[q].layer + 1].schur, B * sizeof(int),
+                                  cudaMemcpyDeviceToHost, st));
+    RCWA_CUDA(cudaStreamSynchronize(st));
+    std::vector<int2> map;
+    for (int q = 0; q < J; ++q)
+        for (int b = 0; b < B; ++b)
+            if (flags[(size_t)q * B + b]) map.push_back(make_int2(q, b));
+    const int total = (int)map.size();
+    std::vector<zc*> ptrs(3 * (size_t)J);  // H sources, Z and T destinations
+    std::vector<int*> infos(J);
+    for (int q = 0; q < J; ++q) {
+        ptrs[q] = jobs[q].H;
+        ptrs[J + q] = c.dense();
+        ptrs[2 * J + q] = c.dense();
+        infos[q] = mem.zeros<int>(B);
+    }
+    if (total > 0) {
+        int2* dmap = mem.get<int2>(total);
+        zc** dptrs = mem.get<zc*>(3 * (size_t)J);
+        int** dinfos = mem.get<int*>(J);
+        RCWA_CUDA(cudaMemcpyAsync(dmap, map.data(), total * sizeof(int2), cudaMemcpyHostToDevice, st));
+        RCWA_CUDA(cudaMemcpyAsync(dptrs, ptrs.data(), ptrs.size() * sizeof(zc*), cudaMemcpyHostToDevice, st));
+        RCWA_CUDA(cudaMemcpyAsync(dinfos, infos.data(), infos.size() * sizeof(int*), cudaMemcpyHostToDevice, st));
+        const long long per = (long long)total * nn;
+        zc* Hc = mem.get<zc>((size_t)per);
+        LAUNCH(gather_flagged_kernel, nblocks(per), kTpb, st, total, nn, dptrs, dmap, Hc);
+        zc* wc = mem.get<zc>((size_t)total * n);
+        zc* Zc = mem.get<zc>((size_t)per);
+        zc* Tc = mem.get<zc>((size_t)per);
+        int* infoc = mem.zeros<int>(total);
+        zc* wsc = mem.get<zc>((size_t)(eig_workspace_bytes(n, total) / sizeof(zc)) + 1);
+        const int group = eig_group ? eig_group : eig_default_group(n, total);
+        launch_eig(st, n, total, Hc, nn, wc, Zc, infoc, nullptr, wsc, 2.220446049250313e-16, 100, group, nullptr, 0, Tc);
+        LAUNCH(scatter_flagged_kernel, nblocks(per), kTpb, st, total, nn, dptrs + J, dmap, Zc);
+        LAUNCH(scatter_flagged_kernel, nblocks(per), kTpb, st, total, nn, dptrs + 2 * J, dmap, Tc);
+        LAUNCH(scatter_flagged_info_kernel, nblocks(total), kTpb, st, total, dinfos, dmap, infoc);
+        for (zc* ptr : {Hc, wc, Zc, Tc, wsc}) mem.free(ptr);
+        mem.free(infoc);
+        mem.free(dmap);
+        mem.free(dptrs);
+        mem.free(dinfos);
+    }
+    for (int q = 0; q < J; ++q) {
+        Region& R = modes[jobs[q].layer + 1];
+        zc* Z = ptrs[J + q];
+        zc* Tm = ptrs[2 * J + q];
+        LAUNCH(schur_info_kernel, nblocks(B), kTpb, st, B, infos[q], R.schur, eig_info, c.fail);
+        R.G = c.dense();
+        zc* gg = c.dense();
+        LAUNCH(triangular_root_kernel, warp_blocks(B), 128, st, B, n, Tm, R.G, gg, R.schur, c.fail);
+        LAUNCH(copy_masked_kernel, nblocks(nd), kTpb, st, B, nn, Z, R.W, R.schur);
+        gemm(c, jobs[q].Q, nn, Z, nullptr, 1.0, 0.0, R.V, R.schur, 0);
+        LAUNCH(right_triangular_solve_kernel, warp_blocks(B), 128, st, B, n, R.V, R.G, R.q, R.schur, c.fail);
+        LAUNCH(add_flag_kernel, nblocks(B), kTpb, st, B, R.schur, schur_count);
+        for (zc* ptr : {gg, Tm, Z, jobs[q].H, jobs[q].Q}) mem.free(ptr);
+        mem.free(infos[q]);
+    }
+}
+
 void interface_matching(Batch& c, const Region& up, const Region& low, zc*& tp, zc*& tm) {
     const long long nd = (long long)c.B * c.nn();
     tp = c.dense();
@@ -1270,6 +1374,7 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                                opt.eig_group);
                 mem.free(ws);
             }
+            std::vector<SchurJob> schur_jobs;
             for (int gi = 0; gi < n_gr; ++gi) {
                 const int k = grating[gi];
                 zc* AB = ABall + 2 * ndN * gi;
@@ -1312,7 +1417,8 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                 RCWA_CUDA(cudaMemcpyAsync(&any, any_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
                 RCWA_CUDA(cudaStreamSynchronize(st));
                 if (any) {
-                    // Schur basis of the full 2N operator for the flagged samples (rcwa1d_conical.hpp:466-502)
+                    // Schur basis of the full 2N operator for the flagged samples (rcwa1d_conical.hpp:466-502): H here,
+                    // its eigensolve below together with the other gratings' flagged samples
                     zc* Pm = c.dense();
                     zc* Qm = c.dense();
                     zc* RE = c.dense();
@@ -1325,29 +1431,12 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                     gemm(c, t1, nn, RE, nullptr, 1.0, 0.0, Qm, R.schur, 0);
                     zc* H = gemm(c, Pm, nn, Qm, nullptr, 1.0, 0.0, t1, R.schur, 0);
                     LAUNCH(finite_check_masked_kernel, nblocks(nd), kTpb, st, B, nn, H, R.schur, c.fail);
-                    zc* ws2 = mem.get<zc>((size_t)(eig_workspace_bytes(n, B) / sizeof(zc)) + 1);
-                    zc* w2 = c.vec();
-                    zc* Z = c.dense();
-                    zc* Tm = c.dense();
-                    int* info2 = mem.zeros<int>(B);
-                    // few flagged samples: size the lanes per matrix by their number, not by the chunk
-                    const int schur_group = opt.eig_group ? opt.eig_group : eig_default_group(n, any);
-                    launch_eig(st, n, B, H, nn, w2, Z, info2, nullptr, ws2, 2.220446049250313e-16, 100, schur_group,
-                               R.schur, 0, Tm);
-                    mem.free(ws2);
-                    LAUNCH(schur_info_kernel, nblocks(B), kTpb, st, B, info2, R.schur, eig_info, c.fail);
-                    R.G = c.dense();
-                    zc* gg = c.dense();
-                    LAUNCH(triangular_root_kernel, warp_blocks(B), 128, st, B, n, Tm, R.G, gg, R.schur, c.fail);
-                    // W = Z; V = Q Z, then V G = Q Z solved for V; q = diag(G)
-                    LAUNCH(copy_masked_kernel, nblocks(nd), kTpb, st, B, nn, Z, R.W, R.schur);
-                    gemm(c, Qm, nn, Z, nullptr, 1.0, 0.0, R.V, R.schur, 0);
-                    LAUNCH(right_triangular_solve_kernel, warp_blocks(B), 128, st, B, n, R.V, R.G, R.q, R.schur, c.fail);
-                    LAUNCH(add_flag_kernel, nblocks(B), kTpb, st, B, R.schur, schur_count);
-                    for (zc* ptr : {gg, Tm, Z, w2, Pm, Qm, RE, RV, t1}) mem.free(ptr);
-                    mem.free(info2);
+                    for (zc* ptr : {Pm, RE, RV}) mem.free(ptr);
+                    schur_jobs.push_back(SchurJob{k, H, Qm});
                 }
             }
+            if (!schur_jobs.empty())
+                conical_schur_modes(c, schur_jobs, modes, eig_info, schur_count, opt.eig_group);
             for (void* p : {(void*)ABall, (void*)lamall, (void*)vecall, (void*)infoall}) mem.free(p);
         }
         ConicalCapture cap;

@@ -1,4 +1,6 @@
 // eig.cu -- launchers of the batched eigensolver (kernel in eig.cuh).
+#include <algorithm>
+
 #include "eig.cuh"
 #include "engine.h"
 
@@ -75,63 +77,98 @@ long long take_rotation_count() {
     return (long long)h;
 }
 
-// Hermitian matrices: the reduction with G lanes per matrix, the QL iteration one lane per matrix, the
-// rotations applied row-parallel, and the fused kernel for any matrix whose rotation log overflowed.
+// Hermitian matrices: the tridiagonalisation with G lanes per matrix, the QL iteration one lane per matrix,
+// the rotations applied row-parallel, and the fused kernel for any matrix whose rotation log overflowed.
+// While a row of the real rotation product fits in shared memory (n <= 887) the rotations go to a real
+// identity Y and the eigenvectors are Q Y; otherwise they are applied to the complex Q in place.
+namespace {
+template <int G>
+void herm_reduce_launch(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* q, zc* ws) {
+    if constexpr (G > 32) {
+        herm_reduce_block_kernel<G><<<(unsigned)batch, G, 0, st>>>(n, batch, a, a_stride, q, ws);
+    } else {
+        const int tpb = 128;
+        const unsigned blocks = (unsigned)(((long long)batch * G + tpb - 1) / tpb);
+        herm_reduce_batch_kernel<G><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, q, ws);
+    }
+}
+void herm_reduce_dispatch(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* q, zc* ws, int group) {
+    switch (group) {
+        case 4: herm_reduce_launch<4>(st, n, batch, a, a_stride, q, ws); break;
+        case 8: herm_reduce_launch<8>(st, n, batch, a, a_stride, q, ws); break;
+        case 16: herm_reduce_launch<16>(st, n, batch, a, a_stride, q, ws); break;
+        case 32: herm_reduce_launch<32>(st, n, batch, a, a_stride, q, ws); break;
+        case 64: herm_reduce_launch<64>(st, n, batch, a, a_stride, q, ws); break;
+        case 128: herm_reduce_launch<128>(st, n, batch, a, a_stride, q, ws); break;
+        case 256: herm_reduce_launch<256>(st, n, batch, a, a_stride, q, ws); break;
+        default: throw EngineError{RCWA_EINVAL, "eig: group must be 4, 8, 16, 32, 64, 128 or 256"};
+    }
+    RCWA_CUDA(cudaGetLastError());
+}
+void herm_fused_dispatch(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info,
+                         zc* ws, double eps, int max_iter, int group, const int* only) {
+    const int tpb = 128;
+    const unsigned blocks = (unsigned)(((long long)batch * std::min(group, 32) + tpb - 1) / tpb);
+    unsigned long long* rot = rotation_counter();
+    switch (group) {
+        case 4: herm_batch_kernel<4><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rot, only); break;
+        case 8: herm_batch_kernel<8><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rot, only); break;
+        case 16: herm_batch_kernel<16><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rot, only); break;
+        case 32: herm_batch_kernel<32><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rot, only); break;
+        case 64: herm_block_kernel<64><<<(unsigned)batch, 64, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rot, only); break;
+        case 128: herm_block_kernel<128><<<(unsigned)batch, 128, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rot, only); break;
+        case 256: herm_block_kernel<256><<<(unsigned)batch, 256, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rot, only); break;
+        default: throw EngineError{RCWA_EINVAL, "eig: group must be 4, 8, 16, 32, 64, 128 or 256"};
+    }
+    RCWA_CUDA(cudaGetLastError());
+}
+}  // namespace
+
 void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info, zc* ws,
                      double eps, int max_iter, int group) {
     if (batch <= 0 || n <= 0) return;
     if (group <= 0) group = eig_default_group(n, batch);
     TimedLaunch timed(TK_EIG, st);
-    if (group > 32) {
-        switch (group) {
-            case 64: herm_reduce_block_kernel<64><<<(unsigned)batch, 64, 0, st>>>(n, batch, a, a_stride, v, ws); break;
-            case 128: herm_reduce_block_kernel<128><<<(unsigned)batch, 128, 0, st>>>(n, batch, a, a_stride, v, ws); break;
-            case 256: herm_reduce_block_kernel<256><<<(unsigned)batch, 256, 0, st>>>(n, batch, a, a_stride, v, ws); break;
-            default: throw EngineError{RCWA_EINVAL, "eig: group must be 4, 8, 16, 32, 64, 128 or 256"};
-        }
-    } else {
-        const int tpb = 128;
-        const unsigned blocks = (unsigned)(((long long)batch * group + tpb - 1) / tpb);
-        switch (group) {
-            case 4: herm_reduce_batch_kernel<4><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, v, ws); break;
-            case 8: herm_reduce_batch_kernel<8><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, v, ws); break;
-            case 16: herm_reduce_batch_kernel<16><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, v, ws); break;
-            case 32: herm_reduce_batch_kernel<32><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, v, ws); break;
-            default: throw EngineError{RCWA_EINVAL, "eig: group must be 4, 8, 16, 32, 64, 128 or 256"};
-        }
+    const size_t ysm = (size_t)n * kHermRows * sizeof(double);
+    const bool real_form = ysm <= 227 * 1024;
+    zc* q = v;
+    double* y = nullptr;
+    if (real_form) {
+        RCWA_CUDA(cudaMallocAsync(&q, (size_t)batch * n * n * sizeof(zc), st));
+        RCWA_CUDA(cudaMallocAsync(&y, (size_t)batch * n * n * sizeof(double), st));
     }
-    RCWA_CUDA(cudaGetLastError());
+    herm_reduce_dispatch(st, n, batch, a, a_stride, q, ws, group);
     herm_ql_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, st>>>(n, batch, w, info, ws, eps, max_iter, rotation_counter());
     RCWA_CUDA(cudaGetLastError());
-    herm_apply_kernel<<<(unsigned)(((long long)batch * n + 127) / 128), 128, 0, st>>>(n, batch, v, ws, info);
-    RCWA_CUDA(cudaGetLastError());
-    // matrices whose log overflowed: the fused kernel, masked to them
-    int* only = nullptr;
+    int* only = nullptr;  // matrices whose log overflowed: the fused kernel, masked to them
     RCWA_CUDA(cudaMallocAsync(&only, (size_t)batch * sizeof(int), st));
     herm_overflow_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, st>>>(n, batch, ws, only);
     RCWA_CUDA(cudaGetLastError());
-    launch_count() += 4;
-    if (group > 32) {
-        switch (group) {
-            case 64: herm_block_kernel<64><<<(unsigned)batch, 64, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rotation_counter(), only); break;
-            case 128: herm_block_kernel<128><<<(unsigned)batch, 128, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rotation_counter(), only); break;
-            case 256: herm_block_kernel<256><<<(unsigned)batch, 256, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rotation_counter(), only); break;
-            default: throw EngineError{RCWA_EINVAL, "eig: group must be 4, 8, 16, 32, 64, 128 or 256"};
+    if (real_form) {
+        if (ysm > 48 * 1024) {
+            static int opted = 0;  // the largest opt-in requested so far (the attribute is per function)
+            if ((int)ysm > opted) {
+                RCWA_CUDA(cudaFuncSetAttribute(herm_apply_real_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)ysm));
+                opted = (int)ysm;
+            }
         }
+        const dim3 grid((unsigned)batch, (unsigned)((n + kHermRows - 1) / kHermRows));
+        herm_apply_real_kernel<<<grid, kHermRows, ysm, st>>>(n, batch, y, ws, info);
+        RCWA_CUDA(cudaGetLastError());
+        launch_zdgemm(st, n, n, n, batch, q, n, (long long)n * n, y, n, (long long)n * n, v, n, (long long)n * n, only, 1);
+        launch_count() += 5;
     } else {
-        const int tpb = 128;
-        const unsigned blocks = (unsigned)(((long long)batch * group + tpb - 1) / tpb);
-        switch (group) {
-            case 4: herm_batch_kernel<4><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rotation_counter(), only); break;
-            case 8: herm_batch_kernel<8><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rotation_counter(), only); break;
-            case 16: herm_batch_kernel<16><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rotation_counter(), only); break;
-            case 32: herm_batch_kernel<32><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, info, ws, eps, max_iter, rotation_counter(), only); break;
-            default: throw EngineError{RCWA_EINVAL, "eig: group must be 4, 8, 16, 32, 64, 128 or 256"};
-        }
+        herm_apply_kernel<<<(unsigned)(((long long)batch * n + 127) / 128), 128, 0, st>>>(n, batch, v, ws, info);
+        RCWA_CUDA(cudaGetLastError());
+        launch_count() += 4;
     }
-    ++launch_count();
-    RCWA_CUDA(cudaGetLastError());
+    herm_fused_dispatch(st, n, batch, a, a_stride, w, v, info, ws, eps, max_iter, group, only);
     RCWA_CUDA(cudaFreeAsync(only, st));
+    if (real_form) {
+        RCWA_CUDA(cudaFreeAsync(q, st));
+        RCWA_CUDA(cudaFreeAsync(y, st));
+    }
 }
 
 }  // namespace rcwa_gb300

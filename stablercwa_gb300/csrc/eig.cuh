@@ -670,7 +670,7 @@ __global__ void __launch_bounds__(G) herm_block_kernel(int n, int batch, const z
 __host__ __device__ inline long long herm_log_capacity(int n) { return 2LL * n * n; }
 __host__ __device__ inline long long herm_table_capacity(int n) { return 2LL * ((long long)n * n - n); }
 
-// Householder tridiagonalisation of a Hermitian A (only used through A = A^H): T = Q^H A Q with T real
+// Householder tridiagonalisation of the Hermitian part of A: T = Q^H A Q with T real
 // symmetric tridiagonal, Q = H_0 H_1 ... H_{n-2}, H_k = I - tau_k v_k v_k^H acting on indices k+1..n-1 and
 // chosen so that H_k^H x = beta_k e_1 with beta_k real (Golub and Van Loan, Matrix Computations, 4th ed.,
 // sections 5.1 and 8.3.1). The trailing block is updated as A - v w^H - w v^H with y = A v,
@@ -690,7 +690,12 @@ __device__ void herm_tridiag_one(int n, const zc* __restrict__ A0, zc* __restric
     double* __restrict__ e = d + n;
     zc* __restrict__ ww = ws + 3LL * n * n;  // y, then w, of the current step (n)
     zc* __restrict__ taus = ww + n;          // tau_k (n)
-    for (long long idx = g; idx < (long long)n * n; idx += G) A[idx] = A0[idx];
+    // the Hermitian part (A0 + A0^H) / 2, which is A0 itself (to the bit) for an exactly Hermitian input
+    for (long long idx = g; idx < (long long)n * n; idx += G) {
+        const int j = (int)(idx / n), i = (int)(idx - (long long)j * n);
+        const zc a = A0[idx], b = A0[(long long)i * n + j];
+        A[idx] = zc{0.5 * (a.re + b.re), 0.5 * (a.im - b.im)};
+    }
     grp.sync();
     for (int k = 0; k + 1 < n; ++k) {
         zc* __restrict__ col = A + (long long)k * n;  // rows k+2.. become v_k (v_{k+1} = 1 implied)
@@ -943,6 +948,45 @@ static __global__ void __launch_bounds__(128) herm_apply_kernel(int n, int batch
         }
         z[(long long)fl.x * n] = cur;
     }
+}
+
+// (3, real form) the logged rotations applied to a real identity instead of to the complex Q: Y = R_1 R_2 ...
+// is real orthogonal and the eigenvectors are Q Y, a complex-by-real product (zdgemm_kernel). One thread
+// per (matrix, row), kHermRows rows per CTA, each row kept in shared memory (row t of the CTA at element
+// i * kHermRows + t) until every sweep has passed: half the FP64 work of rotating Q, and Y meets HBM only
+// once. A matrix that overflowed its log or did not converge gets Y = I.
+constexpr int kHermRows = 32;
+static __global__ void __launch_bounds__(kHermRows) herm_apply_real_kernel(int n, int batch, double* __restrict__ y_out,
+                                                                           const zc* __restrict__ ws,
+                                                                           const int* __restrict__ info) {
+    extern __shared__ double ysm[];
+    const long long gid = blockIdx.x;
+    const int t = threadIdx.x;
+    const int r = blockIdx.y * kHermRows + t;
+    if (gid >= batch || r >= n) return;
+    double* y = ysm + t;
+    for (int i = 0; i < n; ++i) y[i * kHermRows] = i == r ? 1.0 : 0.0;
+    const zc* base = ws + gid * eig_workspace_elems(n);
+    const int* tail = reinterpret_cast<const int*>(base + 3LL * n * n);
+    if (!tail[1] && !info[gid]) {
+        const int2* table = reinterpret_cast<const int2*>(reinterpret_cast<const double*>(base) + 2 * n);
+        const double* log = reinterpret_cast<const double*>(base + (long long)n * n);
+        const int sweeps = tail[0];
+        long long pos = 0;
+        for (int k = 0; k < sweeps; ++k) {
+            const int2 fl = table[k];
+            double cur = y[(fl.y + 1) * kHermRows];
+            for (int i = fl.y; i >= fl.x; --i, ++pos) {
+                const double c = log[2 * pos], s = log[2 * pos + 1];
+                const double yi = y[i * kHermRows];
+                y[(i + 1) * kHermRows] = s * yi + c * cur;
+                cur = c * yi - s * cur;
+            }
+            y[fl.x * kHermRows] = cur;
+        }
+    }
+    double* yo = y_out + gid * (long long)n * n + r;
+    for (int i = 0; i < n; ++i) yo[(long long)i * n] = y[i * kHermRows];
 }
 
 // 1 where the matrix overflowed its log (the fused kernel redoes it)

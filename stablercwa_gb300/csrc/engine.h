@@ -80,6 +80,10 @@ void launch_lu_solve(cudaStream_t st, int n, int nrhs, int batch, const zc* a, l
 void launch_zgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride, const zc* B,
                   int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc, long long c_stride,
                   double s_ab, double s_c, const int* skip = nullptr, int skip_value = 1, int tri = 0);
+// C = A B with A complex, B real (C does not alias A or B)
+void launch_zdgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride,
+                   const double* B, int ldb, long long b_stride, zc* C, int ldc, long long c_stride,
+                   const int* skip = nullptr, int skip_value = 1);
 // tri: a triangular factor whose zero part the product skips (TRI_*, common.cuh)
 // group: lanes per matrix (0 = choose)
 // skip: optional per-matrix flags, a matrix whose flag equals skip_value is left untouched.

@@ -185,4 +185,16 @@ void launch_zgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A, 
     RCWA_CUDA(cudaGetLastError());
 }
 
+void launch_zdgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride,
+                   const double* B, int ldb, long long b_stride, zc* C, int ldc, long long c_stride, const int* skip,
+                   int skip_value) {
+    if (batch <= 0 || m <= 0 || n <= 0) return;
+    const long long warps = (long long)batch * ((m + 31) / 32) * ((n + 7) / 8);
+    const unsigned blocks = (unsigned)((warps * 32 + 127) / 128);
+    zdgemm_kernel<<<blocks, 128, 0, st>>>(m, n, k, batch, A, lda, a_stride, B, ldb, b_stride, C, ldc, c_stride, skip,
+                                          skip_value);
+    ++launch_count();
+    RCWA_CUDA(cudaGetLastError());
+}
+
 }  // namespace rcwa_gb300

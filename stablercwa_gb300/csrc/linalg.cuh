@@ -380,4 +380,44 @@ __global__ void __launch_bounds__(128) zgemm_kernel(int m, int n, int k, int bat
     }
 }
 
+// C = A B with A complex and B real (the eigenvectors Q Y of the Hermitian solver), zgemm_kernel's tiling:
+// one warp per 32 x 8 tile of C, two fused multiply-adds per term.
+__global__ void __launch_bounds__(128) zdgemm_kernel(int m, int n, int k, int batch, const zc* __restrict__ A, int lda,
+                                                     long long a_stride, const double* __restrict__ B, int ldb,
+                                                     long long b_stride, zc* __restrict__ C, int ldc, long long c_stride,
+                                                     const int* __restrict__ skip, int skip_value) {
+    const int tiles_m = (m + 31) / 32, tiles_n = (n + 7) / 8;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long per = (long long)tiles_m * tiles_n;
+    const long long sys = warp / per;
+    if (sys >= batch) return;
+    if (skip && skip[sys] == skip_value) return;
+    const int t = (int)(warp - sys * per);
+    const int tm = t % tiles_m, tn = t / tiles_m;
+    const int row = tm * 32 + (threadIdx.x & 31);
+    const int c0 = tn * 8;
+    const int cols = min(8, n - c0);
+    if (row >= m) return;
+    const zc* As = A + sys * a_stride;
+    const double* Bs = B + sys * b_stride;
+    double ar[8], ai[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) ar[j] = ai[j] = 0.0;
+    for (int p = 0; p < k; ++p) {
+        const zc av = As[(long long)p * lda + row];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (j < cols) {
+                const double bv = Bs[(long long)(c0 + j) * ldb + p];
+                ar[j] = fma(av.re, bv, ar[j]);
+                ai[j] = fma(av.im, bv, ai[j]);
+            }
+        }
+    }
+    zc* Cs = C + sys * c_stride;
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if (j < cols) Cs[(long long)(c0 + j) * ldc + row] = zc{ar[j], ai[j]};
+}
+
 }  // namespace rcwa_gb300

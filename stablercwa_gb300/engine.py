@@ -90,6 +90,8 @@ def load_library(build_if_missing=True):
     L.rcwa_gpu_fourier_coefficients.argtypes = [vp, vp, vp, ci, cd, ci, ci, ci, vp]
     L.rcwa_gpu_eig_batch.argtypes = [vp, ci, ci, vp, cd, ci, vp, vp, vp, vp]
     L.rcwa_gpu_eig_batch_dev.argtypes = [vp, ci, ci, vp, cd, ci, vp, vp, vp, vp]
+    L.rcwa_gpu_eig_hermitian_batch.argtypes = [vp, ci, ci, vp, cd, ci, vp, vp, vp]
+    L.rcwa_gpu_eig_hermitian_batch_dev.argtypes = [vp, ci, ci, vp, cd, ci, vp, vp, vp]
     L.rcwa_gpu_solve_batch.argtypes = [vp, ci, ci, ci, vp, vp, vp, vp]
     L.rcwa_gpu_multiply_batch.argtypes = [vp, ci, ci, ci, ci, vp, vp, vp]
     _lib = L
@@ -427,6 +429,23 @@ class Engine:
     def eig_batch_device(self, n, batch, d_a, d_w, d_v, d_info, d_sweeps=None, eps=float(np.finfo(np.float64).eps),
                          max_iter=30):
         self._check(self.L.rcwa_gpu_eig_batch_dev(self.h, n, batch, d_a, eps, max_iter, d_w, d_v, d_info, d_sweeps))
+
+    def eig_hermitian_batch(self, a, eps=float(np.finfo(np.float64).eps), max_iter=30):
+        """Hermitian part of a: (batch, n, n). Returns values (batch, n) real, unsorted; vectors (batch, n, n)
+        with orthonormal columns; info (batch,)."""
+        a = np.asarray(a, dtype=np.complex128)
+        batch, n = a.shape[0], a.shape[1]
+        cm = _colmajor(a)
+        w = np.empty((batch, n), np.complex128)
+        v = np.empty((batch, n, n), np.complex128)
+        info = np.empty(batch, np.int32)
+        self._check(self.L.rcwa_gpu_eig_hermitian_batch(self.h, n, batch, cm.ctypes.data, eps, max_iter, w.ctypes.data,
+                                                        v.ctypes.data, info.ctypes.data))
+        return w.real.copy(), v.transpose(0, 2, 1), info
+
+    def eig_hermitian_batch_device(self, n, batch, d_a, d_w, d_v, d_info, eps=float(np.finfo(np.float64).eps),
+                                   max_iter=30):
+        self._check(self.L.rcwa_gpu_eig_hermitian_batch_dev(self.h, n, batch, d_a, eps, max_iter, d_w, d_v, d_info))
 
     def solve_batch(self, a, b):
         """Solve a[k] x[k] = b[k]; a: (batch, n, n), b: (batch, n, nrhs). Returns x, singular."""

@@ -121,3 +121,40 @@ def test_blocked_lu(eng, n, nrhs):
         c = eng.multiply_batch(a, b)
         for q in range(3):
             assert np.max(np.abs(c[q] - oracle.multiply(a[q], b[q]))) <= 1e-12 * max(1.0, k)
+
+
+@pytest.mark.parametrize("group", ["4", "16", "32", "128"])
+@pytest.mark.parametrize("n", [1, 2, 3, 17, 81, 121])
+def test_eig_hermitian_batch(eng, n, group, monkeypatch):
+    """rcwa_gpu_eig_hermitian_batch: random Hermitian matrices, the Toeplitz-plus-Kx^2 layer matrices of a
+    lossless grating (with exactly repeated eigenvalues at normal incidence) and a diagonal one; eigenvalues
+    against numpy's eigh to 1e-13 of the spectral radius, residual <= 1e-13, orthonormal columns to 1e-13.
+    A non-Hermitian input is solved through its Hermitian part."""
+    monkeypatch.setenv("RCWA_GB300_EIG_GROUP", group)
+    rng = np.random.default_rng(n)
+    mats = []
+    for _ in range(5):
+        x = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+        mats.append(x + x.conj().T)
+    M = n // 2
+    h = np.subtract.outer(np.arange(n), np.arange(n))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        eps = np.where(h == 0, 0.4 * 1.46 ** 2 + 0.6, (1.46 ** 2 - 1) * np.sin(np.pi * h * 0.4) / (np.pi * h))
+    for kx0 in (0.0, 0.31):
+        kx = kx0 + (np.arange(n) - M) * 0.61
+        mats.append((np.diag(kx * kx) - eps).astype(np.complex128))
+    mats.append(np.diag(rng.standard_normal(n)).astype(np.complex128))
+    a = np.array(mats)
+    w, v, info = eng.eig_hermitian_batch(a)
+    assert (info == 0).all()
+    for k in range(len(a)):
+        ref = np.linalg.eigvalsh(a[k])
+        scale = max(1.0, np.max(np.abs(ref)))
+        assert np.max(np.abs(np.sort(w[k]) - ref)) <= 1e-13 * scale * max(1, n) ** 0.5, k
+        assert residual(a[k], w[k], v[k]) <= 1e-13, k
+        assert np.max(np.abs(v[k].conj().T @ v[k] - np.eye(n))) <= 1e-13 * max(1, n) ** 0.5, k
+    # a general matrix: the solver works on (a + a^H) / 2
+    g = rng.standard_normal((1, n, n)) + 1j * rng.standard_normal((1, n, n))
+    w2, v2, info2 = eng.eig_hermitian_batch(g)
+    hpart = (g[0] + g[0].conj().T) / 2
+    assert info2[0] == 0 and residual(hpart, w2[0], v2[0]) <= 1e-13
