@@ -566,18 +566,26 @@ __global__ void conical_diag_interface_kernel(long long total, const zc* __restr
 // lower side analytic: mm = rows of W scaled by 1/w, nn = rows of V by 1/v; tp, tm = (mm +- nn)/2;
 // a zero w or v fails the sample (rcwa1d_conical.hpp:539-547)
 __global__ void conical_tp_tm_low_kernel(int B, int n, const zc* __restrict__ W, const zc* __restrict__ V,
-                                         const zc* __restrict__ w, const zc* __restrict__ v, zc* __restrict__ tp,
-                                         zc* __restrict__ tm, int* __restrict__ fail) {
+                                         const zc* __restrict__ inv_w, const zc* __restrict__ inv_v, zc* __restrict__ tp,
+                                         zc* __restrict__ tm) {
     const long long nn = (long long)n * n;
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)B * nn) return;
     const int b = (int)(idx / nn);
-    const int i = (int)((idx - (long long)b * nn) % n);
-    const zc wi = w[(long long)b * n + i], vi = v[(long long)b * n + i];
-    if (is_zero(wi) || is_zero(vi)) fail[b] = 1;
-    const zc mm = W[idx] * zinv(wi), nv = V[idx] * zinv(vi);
+    const long long bi = (long long)b * n + (idx - (long long)b * nn) % n;
+    const zc mm = W[idx] * inv_w[bi], nv = V[idx] * inv_v[bi];
     tp[idx] = 0.5 * (mm + nv);
     tm[idx] = 0.5 * (mm - nv);
+}
+// 1/w and 1/v of an analytic region's diagonal field factors; a zero factor fails the sample
+__global__ void conical_inv_wv_kernel(int B, int n, const zc* __restrict__ w, const zc* __restrict__ v,
+                                      zc* __restrict__ inv_w, zc* __restrict__ inv_v, int* __restrict__ fail) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * n) return;
+    const zc wi = w[idx], vi = v[idx];
+    if (is_zero(wi) || is_zero(vi)) fail[idx / n] = 1;
+    inv_w[idx] = zinv(wi);
+    inv_v[idx] = zinv(vi);
 }
 
 // top block of two analytic regions: columns M and N + M of Tdd and Rud (rcwa1d_conical.hpp:600-609)
@@ -1006,7 +1014,12 @@ void interface_matching(Batch& c, const Region& up, const Region& low, zc*& tp, 
     tp = c.dense();
     tm = c.dense();
     if (low.analytic) {
-        LAUNCH(conical_tp_tm_low_kernel, nblocks(nd), kTpb, c.st, c.B, c.n, up.W, up.V, low.w, low.v, tp, tm, c.fail);
+        zc* inv_w = c.vec();
+        zc* inv_v = c.vec();
+        LAUNCH(conical_inv_wv_kernel, nblocks((long long)c.B * c.n), kTpb, c.st, c.B, c.n, low.w, low.v, inv_w, inv_v, c.fail);
+        LAUNCH(conical_tp_tm_low_kernel, nblocks(nd), kTpb, c.st, c.B, c.n, up.W, up.V, inv_w, inv_v, tp, tm);
+        c.mem->free(inv_w);
+        c.mem->free(inv_v);
         return;
     }
     zc *mm, *nn;

@@ -101,7 +101,10 @@ void interface_matching(Batch& c, const DModes& up, const DModes& low, zc*& tp, 
     tp = c.dense();
     tm = c.dense();
     if (low.analytic) {
-        LAUNCH(tp_tm_kernel, nblocks(nd), kTpb, c.st, c.B, c.n, up.W, up.V, low.p, tp, tm);
+        zc* inv_p = c.vec();
+        LAUNCH(reciprocal_kernel, nblocks((long long)c.B * c.n), kTpb, c.st, (long long)c.B * c.n, low.p, inv_p);
+        LAUNCH(tp_tm_kernel, nblocks(nd), kTpb, c.st, c.B, c.n, up.W, up.V, inv_p, tp, tm);
+        c.mem->free(inv_p);
         return;
     }
     zc *mm, *nn;

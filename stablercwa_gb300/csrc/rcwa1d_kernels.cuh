@@ -138,22 +138,27 @@ __global__ void scale_both_kernel(int B, int n, const zc* __restrict__ src, cons
     dst[idx] = dl[(long long)b * n + i] * (src[idx] * dr[(long long)b * n + j]);
 }
 
-// tp = (mm + nn)/2, tm = (mm - nn)/2 with nn = rows of V scaled by 1/p_low (the lower side analytic)
-// or nn given (include/stablercwa/rcwa1d.hpp:664-692).
+// tp = (mm + nn)/2, tm = (mm - nn)/2 with nn = rows of V scaled by 1/p_low (the lower side analytic; the
+// reciprocals precomputed) or nn given (include/stablercwa/rcwa1d.hpp:664-692).
 __global__ void tp_tm_kernel(int B, int n, const zc* __restrict__ mm, const zc* __restrict__ nn_or_v,
-                             const zc* __restrict__ p_low, zc* __restrict__ tp, zc* __restrict__ tm) {
+                             const zc* __restrict__ inv_p_low, zc* __restrict__ tp, zc* __restrict__ tm) {
     const long long nn = (long long)n * n;
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)B * nn) return;
     zc v = nn_or_v[idx];
-    if (p_low) {
+    if (inv_p_low) {
         const int b = (int)(idx / nn);
         const int i = (int)((idx - (long long)b * nn) % n);
-        v = v * zinv(p_low[(long long)b * n + i]);
+        v = v * inv_p_low[(long long)b * n + i];
     }
     const zc m = mm[idx];
     tp[idx] = 0.5 * (m + v);
     tm[idx] = 0.5 * (m - v);
+}
+// out = 1 / p elementwise (Smith's reciprocal, the value the per-element form would compute)
+__global__ void reciprocal_kernel(long long total, const zc* __restrict__ p, zc* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < total) out[idx] = zinv(p[idx]);
 }
 
 // lhs = tp - r tm, rhs = r tp - tm with r diagonal (r = null: zero), for the seam of a dense region
