@@ -54,6 +54,31 @@ def workload(seed=SEED, n_points=N_POINTS):
     return stack, pts, {"fill": float(fill), "depth": float(depth)}
 
 
+# DRAM bytes per matrix of the Hermitian eigensolve stage at n = 121 (tridiagonalisation 54.3 MB, real
+# rotations 1.2 MB, Q Y 0.6 MB), from one ncu --set full capture of 2432 matrices
+# (profiles/herm_eigensolver_n121.md); the QL kernel's bytes are not included
+HERM_STAGE_DRAM_BYTES_PER_MATRIX_N121 = 56.1e6
+
+
+HERM_STAGE_KERNELS = ("eigensolve stage: herm_reduce_batch_kernel + herm_ql_kernel + herm_apply_real_kernel + "
+                      "zdgemm_kernel")
+
+
+def herm_flops_text(n, rotations_per_matrix):
+    return (f"Hermitian path at order {n}: tridiagonalisation with Q {herm_reduction_flops(n)} flops per matrix, "
+            f"6 n per QL rotation applied to a real identity ({rotations_per_matrix:.0f} rotations per matrix "
+            f"measured), Q Y 4 n^3")
+
+
+def herm_eig_flops(n, rotations_per_matrix):
+    """Flops of one Hermitian eigensolve as the engine runs it: the tridiagonalisation, then (n <= 887) the
+    QL rotations applied to a real identity (6 n each) and the complex-by-real product Q Y (4 n^3), or the
+    rotations applied to the complex Q in place (12 n each)."""
+    if n <= 887:
+        return herm_reduction_flops(n) + 6 * n * rotations_per_matrix + 4 * n ** 3
+    return herm_reduction_flops(n) + 12 * n * rotations_per_matrix
+
+
 def herm_reduction_flops(n):
     """Real flops of the Householder tridiagonalisation with the reflectors accumulated, as the eigensolver
     performs it: per step with a trailing block of order m, the product A v (8 m^2), the rank-2 update of
@@ -64,18 +89,18 @@ def herm_reduction_flops(n):
 def engine_flops_per_solve(n, pol, rotations_per_matrix, reduced=True):
     """FP64 flops of one solve of this stack (a grating over films) as the engine performs it: LU factor
     8/3 n^3, triangular solves 8 n^2 per right-hand side, GEMM 8 n^3.
-    eigensolve   Hermitian (rotations_per_matrix > 0): the reduction plus 12 n per QL rotation;
+    eigensolve   Hermitian (rotations_per_matrix > 0): herm_eig_flops;
                  general: 105 n^3.
-    seams        reduced: grating over the first film, one LU with n right-hand sides and one GEMM; top
-                 interface, one GEMM and one single-column LU. The reference's sequence: 5 LUs with n
+    seams        reduced: grating over the first film, one LU with n right-hand sides (g is kept as its
+                 factors and applied to vectors); top interface, one GEMM and one single-column LU. The reference's sequence: 5 LUs with n
                  right-hand sides, 1 single-column LU, 6 GEMMs.
     TM           general: the layer matrix [[1/eps]]^-1 B and V = [[1/eps]] W q, 2 GEMMs; Hermitian:
                  L^-1 B L^-H, L^-H Y and L Y, 4 products with a triangular factor (4 n^3 each)."""
     lu, tri, mm = (8 / 3) * n ** 3, 8 * n ** 3, 8 * n ** 3
     herm = rotations_per_matrix > 0
-    eig = herm_reduction_flops(n) + 12 * n * rotations_per_matrix if herm else 105 * n ** 3
+    eig = herm_eig_flops(n, rotations_per_matrix) if herm else 105 * n ** 3
     if reduced:
-        seams = (lu + tri + mm) + (mm + lu + 8 * n ** 2)
+        seams = (lu + tri) + (mm + lu + 8 * n ** 2)
     else:
         seams = 6 * lu + 5 * tri + 8 * n ** 2 + 6 * mm
     tm = 0 if pol == 0 else (4 * mm / 2 if herm else 2 * mm)
@@ -322,7 +347,7 @@ def run_ours(args):
     rot_per_matrix = rotations / max(1, eig_launches * P)
     reduced = os.environ.get("RCWA_GB300_SEAMS", "") != "reference"
     if herm:
-        eig_flops_launch = P * (herm_reduction_flops(n) + 12 * n * rot_per_matrix)
+        eig_flops_launch = P * herm_eig_flops(n, rot_per_matrix)
     else:
         eig_flops_launch = P * 105 * n ** 3
     total_flops = P * sum(engine_flops_per_solve(n, pol, rot_per_matrix, reduced) for pol in (0, 1))
@@ -342,13 +367,14 @@ def run_ours(args):
                 "clocks": clocks,
                 "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "gpu_launches": launches,
-                "roofline": {"bound": "fp64", "kernel": ("eigensolve stage: herm_reduce_batch_kernel + herm_ql_kernel + herm_apply_kernel"
-                                        if herm else "eig_batch_kernel"),
-                             "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
-                             "flops_model": ("Hermitian path: reduction + accumulation " + str(herm_reduction_flops(n)) +
-                                             " flops per matrix plus 12 n per QL rotation, "
-                                             f"{rotations / max(1, eig_launches * P):.0f} rotations per matrix measured")
-                             if herm else "general QR: 105 n^3 per matrix",
+                "roofline": {"bound": "fp64", "kernel": (HERM_STAGE_KERNELS if herm else "eig_batch_kernel"),
+                             "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                             "traffic": (HERM_STAGE_DRAM_BYTES_PER_MATRIX_N121 * P if herm and n == 121 else None),
+                             "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's "
+                                                "kernels per matrix (2432-matrix capture) x matrices per launch; "
+                                                "QL kernel not included" if herm and n == 121 else None),
+                             "flops_model": (herm_flops_text(n, rotations / max(1, eig_launches * P)) if herm
+                                             else "general QR: 105 n^3 per matrix"),
                              "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (torch.matmul float64), best of 5",
                              "flops_per_launch": eig_flops_launch, "avg_launch_ms": eig_avg_ms,
                              "launches": eig_launches, "busy_ms": eig_busy_ms,
@@ -499,10 +525,9 @@ def run_secondary(args):
         # Schur-basis eigensolves of order 2N inside the same timer are not counted)
         mats, order = herm_model
         rot = rotations / (mats * args.steps)
-        eig_flops = mats * (herm_reduction_flops(order) + 12 * order * rot)
-        roof_kernel = "eigensolve stage: herm_reduce_batch_kernel + herm_ql_kernel + herm_apply_kernel"
-        flops_model = (f"Hermitian path: tridiagonalisation {herm_reduction_flops(order)} flops per matrix of order "
-                       f"{order} plus 12 n per QL rotation, {rot:.0f} rotations per matrix measured")
+        eig_flops = mats * herm_eig_flops(order, rot)
+        roof_kernel = HERM_STAGE_KERNELS
+        flops_model = herm_flops_text(order, rot)
     eig_ms, _ = eng.kernel_time("eig")
     lu_ms, _ = eng.kernel_time("lu")
     gemm_ms, _ = eng.kernel_time("gemm")
