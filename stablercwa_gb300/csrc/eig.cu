@@ -138,7 +138,21 @@ void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a
         RCWA_CUDA(cudaMallocAsync(&y, (size_t)batch * n * n * sizeof(double), st));
     }
     herm_reduce_dispatch(st, n, batch, a, a_stride, q, ws, group);
-    herm_ql_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, st>>>(n, batch, w, info, ws, eps, max_iter, rotation_counter());
+    const size_t qsm = (size_t)2 * n * kHermQlThreads * sizeof(double);
+    if (qsm <= 227 * 1024) {
+        if (qsm > 48 * 1024) {
+            static int opted = 0;  // the largest opt-in requested so far
+            if ((int)qsm > opted) {
+                RCWA_CUDA(cudaFuncSetAttribute(herm_ql_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm));
+                opted = (int)qsm;
+            }
+        }
+        herm_ql_kernel<true><<<(unsigned)((batch + kHermQlThreads - 1) / kHermQlThreads), kHermQlThreads, qsm, st>>>(
+            n, batch, w, info, ws, eps, max_iter, rotation_counter());
+    } else {
+        herm_ql_kernel<false><<<(unsigned)((batch + 127) / 128), 128, 0, st>>>(n, batch, w, info, ws, eps, max_iter,
+                                                                               rotation_counter());
+    }
     RCWA_CUDA(cudaGetLastError());
     int* only = nullptr;  // matrices whose log overflowed: the fused kernel, masked to them
     RCWA_CUDA(cudaMallocAsync(&only, (size_t)batch * sizeof(int), st));

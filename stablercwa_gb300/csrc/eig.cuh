@@ -833,18 +833,35 @@ __global__ void __launch_bounds__(G) herm_reduce_block_kernel(int n, int batch, 
     herm_tridiag_one<G>(n, a + gid * a_stride, v + gid * (long long)n * n, ws + gid * eig_workspace_elems(n), red, ired);
 }
 
-// (2) implicit symmetric QL with Wilkinson's shift on (d, e), one thread per matrix; rotations logged
-static __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, zc* __restrict__ w, int* __restrict__ info,
+// (2) implicit symmetric QL with Wilkinson's shift on (d, e), one thread per matrix; rotations logged. The
+// rotation chain is the whole cost, so with SMEM the thread's d and e live in shared memory (kHermQlThreads
+// threads per CTA, 16 n bytes each) rather than in the workspace, whose loads would sit on the chain.
+constexpr int kHermQlThreads = 32;
+template <bool SMEM>
+__global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, zc* __restrict__ w, int* __restrict__ info,
                                                       zc* __restrict__ ws, double eps, int max_iter,
                                                       unsigned long long* rotations) {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= batch) return;
     zc* base = ws + gid * eig_workspace_elems(n);
-    double* d = reinterpret_cast<double*>(base);
-    double* e = d + n;
+    // d and e: this thread's column of the CTA's shared array (SMEM), else the H block of the workspace
+    double* d;
+    int sd;
+    if constexpr (SMEM) {
+        extern __shared__ double de_sm[];
+        d = de_sm + threadIdx.x;
+        sd = kHermQlThreads;
+    } else {
+        d = reinterpret_cast<double*>(base);
+        sd = 1;
+    }
+    double* e = d + (long long)n * sd;
     const double* src = reinterpret_cast<const double*>(base + 2LL * n * n);  // written by the reduction
-    for (int k = 0; k < 2 * n; ++k) d[k] = src[k];
-    int2* table = reinterpret_cast<int2*>(e + n);
+    for (int k = 0; k < n; ++k) {
+        d[(k) * sd] = src[k];
+        e[(k) * sd] = src[n + k];
+    }
+    int2* table = reinterpret_cast<int2*>(reinterpret_cast<double*>(base) + 2 * n);
     double* log = reinterpret_cast<double*>(base + (long long)n * n);
     int* tail = reinterpret_cast<int*>(base + 3LL * n * n);  // [0] sweeps, [1] overflow
     const long long log_cap = herm_log_capacity(n), table_cap = herm_table_capacity(n);
@@ -854,8 +871,8 @@ static __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, z
         for (int its = 0;; ++its) {
             int m = l;
             for (; m < n - 1; ++m) {
-                const double dd = fabs(d[m]) + fabs(d[m + 1]);
-                if (fabs(e[m]) <= eps * dd || fabs(e[m]) <= DBL_MIN) break;
+                const double dd = fabs(d[(m) * sd]) + fabs(d[(m + 1) * sd]);
+                if (fabs(e[(m) * sd]) <= eps * dd || fabs(e[(m) * sd]) <= DBL_MIN) break;
             }
             if (m == l) break;
             if (its >= max_iter) {
@@ -866,14 +883,14 @@ static __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, z
                 overflow = 1;
                 break;
             }
-            double gg = (d[l + 1] - d[l]) / (2.0 * e[l]);
+            double gg = (d[(l + 1) * sd] - d[(l) * sd]) / (2.0 * e[(l) * sd]);
             double r = hypot(gg, 1.0);
-            gg = d[m] - d[l] + e[l] / (gg + copysign(r, gg));
+            gg = d[(m) * sd] - d[(l) * sd] + e[(l) * sd] / (gg + copysign(r, gg));
             double s = 1.0, c = 1.0, p = 0.0;
             bool split = false;
             int i = m - 1;
             for (; i >= l; --i) {
-                const double f = s * e[i], b = c * e[i];
+                const double f = s * e[(i) * sd], b = c * e[(i) * sd];
                 // r = |(f, g)| and 1/r from one reciprocal square root: the rotation chain is the whole cost
                 // of this one-thread-per-matrix kernel; hypot and a division where f^2 + g^2 could under- or
                 // overflow
@@ -886,19 +903,19 @@ static __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, z
                     r = hypot(f, gg);
                     inv = r == 0.0 ? 0.0 : 1.0 / r;
                 }
-                e[i + 1] = r;
+                e[(i + 1) * sd] = r;
                 if (r == 0.0) {
-                    d[i + 1] -= p;
-                    e[m] = 0.0;
+                    d[(i + 1) * sd] -= p;
+                    e[(m) * sd] = 0.0;
                     split = true;
                     break;
                 }
                 s = f * inv;
                 c = gg * inv;
-                gg = d[i + 1] - p;
-                r = (d[i] - gg) * s + 2.0 * c * b;
+                gg = d[(i + 1) * sd] - p;
+                r = (d[(i) * sd] - gg) * s + 2.0 * c * b;
                 p = s * r;
-                d[i + 1] = gg + p;
+                d[(i + 1) * sd] = gg + p;
                 gg = c * r - b;
                 log[2 * pos] = c;
                 log[2 * pos + 1] = s;
@@ -906,9 +923,9 @@ static __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, z
             }
             const int first = split ? i + 1 : l;
             if (!split) {
-                d[l] -= p;
-                e[l] = gg;
-                e[m] = 0.0;
+                d[(l) * sd] -= p;
+                e[(l) * sd] = gg;
+                e[(m) * sd] = 0.0;
             }
             if (m - 1 >= first) table[sweeps++] = make_int2(first, m - 1);
         }
@@ -917,7 +934,7 @@ static __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, z
     tail[1] = overflow;
     info[gid] = overflow ? 0 : status;
     if (!overflow) {
-        for (int k = 0; k < n; ++k) w[gid * n + k] = zc{d[k], 0.0};
+        for (int k = 0; k < n; ++k) w[gid * n + k] = zc{d[(k) * sd], 0.0};
         if (rotations) atomicAdd(rotations, (unsigned long long)pos);
     }
 }
