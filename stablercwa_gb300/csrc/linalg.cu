@@ -112,10 +112,16 @@ void lu_solve_blocked(cudaStream_t st, int n, int nrhs, int batch, const zc* a, 
                                                                    rhs_stride, x, x_stride, skip, skip_value);
     ++launch_count();
     RCWA_CUDA(cudaGetLastError());
+    // a warp per system once the batch gives every SM sub-partition a system of moderate order
+    const bool warp_panels = n <= 256 && batch >= 608;
     for (int k0 = 0; k0 < n; k0 += kPanel) {
         const int kend = std::min(k0 + kPanel, n);
-        lu_panel_kernel<<<(unsigned)batch, 256, 0, st>>>(n, nrhs, batch, lu, lu_stride, x, x_stride, k0, kPanel, sing_local,
-                                                         skip, skip_value);
+        if (warp_panels)
+            lu_panel_warp_kernel<<<(unsigned)(((long long)batch * 32 + 127) / 128), 128, 0, st>>>(
+                n, nrhs, batch, lu, lu_stride, x, x_stride, k0, kPanel, sing_local, skip, skip_value);
+        else
+            lu_panel_kernel<<<(unsigned)batch, 256, 0, st>>>(n, nrhs, batch, lu, lu_stride, x, x_stride, k0, kPanel,
+                                                             sing_local, skip, skip_value);
         ++launch_count();
         RCWA_CUDA(cudaGetLastError());
         const long long tcols = (long long)batch * (n + nrhs - kend);

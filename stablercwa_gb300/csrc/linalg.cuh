@@ -189,6 +189,71 @@ __global__ void lu_init_kernel(int n, int nrhs, int batch, const zc* a, long lon
     }
 }
 
+// The same panel factorisation with one warp per system (rows strided over the lanes, warp shuffles for
+// the pivot search, no block barriers): the form for many systems of moderate order, where a CTA per
+// system spends most of its time in barriers. Same pivot rule and the same arithmetic per element as
+// lu_panel_kernel, so the factors are identical.
+__global__ void __launch_bounds__(128) lu_panel_warp_kernel(int n, int nrhs, int batch, zc* lu, long long lu_stride, zc* x,
+                                                            long long x_stride, int k0, int nb, int* __restrict__ sing_local,
+                                                            const int* __restrict__ skip, int skip_value) {
+    const long long sys = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (sys >= batch) return;
+    if (skip && skip[sys] == skip_value) return;
+    const int lane = threadIdx.x & 31;
+    zc* L = lu + sys * lu_stride;
+    zc* X = x + sys * x_stride;
+    const int kend = min(k0 + nb, n);
+    for (int j = k0; j < kend; ++j) {
+        zc* col = L + (long long)j * n;
+        double best = -1.0;
+        int bi = n;
+        for (int i = j + lane; i < n; i += 32) {
+            const double v = zabs(col[i]);
+            if (v > best) {
+                best = v;
+                bi = i;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > best || (ov == best && oi < bi)) {
+                best = ov;
+                bi = oi;
+            }
+        }
+        const int p = (best < 0.0 || bi >= n) ? j : bi;  // all-NaN column: keep the diagonal
+        if (p != j) {
+            for (int c = lane; c < n + nrhs; c += 32) {
+                zc* cc = aug_col(L, X, n, c);
+                const zc t = cc[j];
+                cc[j] = cc[p];
+                cc[p] = t;
+            }
+            __syncwarp();
+        }
+        const zc piv = col[j];
+        if (is_zero(piv)) {
+            if (lane == 0) sing_local[sys] = 1;
+            for (int i = j + 1 + lane; i < n; i += 32) col[i] = zc{0.0, 0.0};
+            __syncwarp();
+            continue;
+        }
+        const zc inv = zinv(piv);
+        const bool inv_ok = zfinite(inv);
+        for (int i = j + 1 + lane; i < n; i += 32) col[i] = inv_ok ? col[i] * inv : zdiv(col[i], piv);
+        // each lane updates the rows whose multipliers it just wrote; row j of the panel's columns was
+        // settled by the swap above
+        for (int c = j + 1; c < kend; ++c) {
+            zc* cc = L + (long long)c * n;
+            const zc u = cc[j];
+            for (int i = j + 1 + lane; i < n; i += 32) cc[i] = zfms(col[i], u, cc[i]);
+        }
+        __syncwarp();
+    }
+}
+
 // Factor columns k0 .. k0+nb-1 (all rows below the diagonal), one 256-thread CTA per system.
 __global__ void __launch_bounds__(256) lu_panel_kernel(int n, int nrhs, int batch, zc* lu, long long lu_stride, zc* x,
                                                        long long x_stride, int k0, int nb, int* __restrict__ sing_local,
