@@ -713,15 +713,21 @@ def run_eig_only(n, batch, group, hermitian=False):
     dV = torch.empty((batch, n, n, 2), dtype=torch.float64, device="cuda")
     dI = torch.empty(batch, dtype=torch.int32, device="cuda")
     eng = Engine()
+    est = torch.cuda.ExternalStream(eng.stream())
+    ms = []
     for _ in range(2):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(est)
         if hermitian:
             eng.eig_hermitian_batch_device(n, batch, dA.data_ptr(), dW.data_ptr(), dV.data_ptr(), dI.data_ptr())
         else:
             eng.eig_batch_device(n, batch, dA.data_ptr(), dW.data_ptr(), dV.data_ptr(), dI.data_ptr())
-        eng.synchronize()
+        e1.record(est)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
     bad = int((dI != 0).sum().item())
     print(json.dumps({"eig_only": {"n": n, "batch": batch, "group": group, "hermitian": hermitian,
-                                   "not_converged": bad}}))
+                                   "not_converged": bad, "ms_second_call": ms[1]}}))
     return 0 if bad == 0 else 1
 
 
