@@ -342,88 +342,107 @@ __global__ void conical_schur_pq_kernel(int B, int N, const zc* __restrict__ inv
     }
 }
 
-__device__ double warp_norm1_upper(const zc* a, int n, int lane) {
+// The Schur-branch kernels below run one CTA of kSchurThreads per flagged sample (the launches span the
+// chunk and unflagged samples return at once): a chunk has few flagged samples, so the work of each must
+// spread over many threads.
+constexpr int kSchurThreads = 256;
+
+// max_j sum_{i <= j} |a_ij| of one sample's upper triangle (the 1-norm of an upper triangular matrix),
+// one column per thread then a block maximum (fmax: a NaN column sum is passed over; the callers test the
+// entries' finiteness themselves); every thread gets the result
+__device__ double block_norm1_upper(const zc* a, int n, double* red) {
     double best = 0.0;
-    for (int j = 0; j < n; ++j) {
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
         double s = 0.0;
-        for (int i = lane; i < n; i += 32) s += zabs(a[(long long)j * n + i]);
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        for (int i = 0; i <= j; ++i) s += zabs(a[(long long)j * n + i]);
         best = fmax(best, s);
     }
-    return best;
+    for (int o = 16; o > 0; o >>= 1) best = fmax(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = best;
+    __syncthreads();
+    double out = red[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) out = fmax(out, red[w]);
+    __syncthreads();
+    return out;
 }
 
-// Principal square root of the Schur form T, diagonal by diagonal, and the residual check
-// ||G G - T||_1 <= 1e-10 ||T||_1 (rcwa1d_conical.hpp:415-437). Warp per sample; gg holds G G.
-__global__ void triangular_root_kernel(int B, int n, const zc* __restrict__ T, zc* __restrict__ G, zc* __restrict__ gg,
-                                       const int* __restrict__ schur, int* __restrict__ fail) {
-    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// Principal square root G of the Schur form T, diagonal by diagonal (rcwa1d_conical.hpp:415-437); the
+// residual G G - T is checked by schur_root_check_kernel after a batched product
+__global__ void __launch_bounds__(kSchurThreads) triangular_root_kernel(int B, int n, const zc* __restrict__ T,
+                                                                       zc* __restrict__ G, const int* __restrict__ schur,
+                                                                       int* __restrict__ fail) {
+    const long long b = blockIdx.x;
     if (b >= B || !schur[b]) return;
-    const int lane = threadIdx.x & 31;
     const long long nn = (long long)n * n;
     const zc* t = T + b * nn;
     zc* g = G + b * nn;
-    bool bad = false;
-    for (long long k = lane; k < nn; k += 32) {
-        if (!zfinite(t[k])) bad = true;
+    int bad = 0;
+    for (long long k = threadIdx.x; k < nn; k += blockDim.x) {
+        if (!zfinite(t[k])) bad = 1;
         g[k] = zc{0.0, 0.0};
     }
-    __syncwarp();
-    for (int i = lane; i < n; i += 32) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const zc r = branch(zsqrt(t[(long long)i * n + i]));
-        if (is_zero(r) || !zfinite(r)) bad = true;
+        if (is_zero(r) || !zfinite(r)) bad = 1;
         g[(long long)i * n + i] = r;
     }
-    __syncwarp();
+    __syncthreads();
     for (int gap = 1; gap < n; ++gap) {
-        for (int i = lane; i + gap < n; i += 32) {
+        for (int i = threadIdx.x; i + gap < n; i += blockDim.x) {
             const int j = i + gap;
             zc v = t[(long long)j * n + i];
             for (int k = i + 1; k < j; ++k) v = v - g[(long long)k * n + i] * g[(long long)j * n + k];
             const zc den = g[(long long)i * n + i] + g[(long long)j * n + j];
-            if (is_zero(den)) bad = true;
+            if (is_zero(den)) bad = 1;
             g[(long long)j * n + i] = zdiv(v, den);
         }
-        __syncwarp();
+        __syncthreads();
     }
-    // residual G G - T
-    zc* rr = gg + b * nn;
-    for (long long k = lane; k < nn; k += 32) {
-        const int j = (int)(k / n), i = (int)(k - (long long)j * n);
-        zc acc = zc{0.0, 0.0};
-        for (int q = 0; q < n; ++q) acc = zfma(g[(long long)q * n + i], g[(long long)j * n + q], acc);
-        if (!zfinite(g[k])) bad = true;
-        rr[k] = acc - t[k];
-    }
-    __syncwarp();
-    const double scale = warp_norm1_upper(t, n, lane), error = warp_norm1_upper(rr, n, lane);
-    if (!isfinite(scale) || !isfinite(error) || error > 1e-10 * fmax(scale, 2.2250738585072014e-308)) bad = true;
-    bad = __any_sync(0xffffffffu, bad);
-    if (bad && lane == 0) fail[b] = 1;
+    for (long long k = threadIdx.x; k < nn; k += blockDim.x)
+        if (!zfinite(g[k])) bad = 1;
+    if (__syncthreads_or(bad) && threadIdx.x == 0) fail[b] = 1;
 }
 
-// V G = Q Z solved for V by rows (rcwa1d_conical.hpp:494-500); q = diag(G).
+// ||G G - T||_1 <= 1e-10 ||T||_1 (rcwa1d_conical.hpp:430-436), with gg = G G from a batched product
+__global__ void __launch_bounds__(kSchurThreads) schur_root_check_kernel(int B, int n, const zc* __restrict__ T,
+                                                                        zc* __restrict__ gg, const int* __restrict__ schur,
+                                                                        int* __restrict__ fail) {
+    __shared__ double red[kSchurThreads / 32];
+    const long long b = blockIdx.x;
+    if (b >= B || !schur[b]) return;
+    const long long nn = (long long)n * n;
+    const zc* t = T + b * nn;
+    zc* rr = gg + b * nn;
+    for (long long k = threadIdx.x; k < nn; k += blockDim.x) rr[k] = rr[k] - t[k];
+    __syncthreads();
+    const double scale = block_norm1_upper(t, n, red), error = block_norm1_upper(rr, n, red);
+    if (threadIdx.x == 0 &&
+        (!isfinite(scale) || !isfinite(error) || error > 1e-10 * fmax(scale, 2.2250738585072014e-308)))
+        fail[b] = 1;
+}
+
+// V G = Q Z solved for V by rows (rcwa1d_conical.hpp:494-500), one thread per (sample, row); q = diag(G)
 __global__ void right_triangular_solve_kernel(int B, int n, zc* __restrict__ Vm, const zc* __restrict__ G,
                                               zc* __restrict__ q, const int* __restrict__ schur, int* __restrict__ fail) {
-    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (b >= B || !schur[b]) return;
-    const int lane = threadIdx.x & 31;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * n) return;
+    const long long b = idx / n;
+    if (!schur[b]) return;
+    const int i = (int)(idx - b * n);
     const long long nn = (long long)n * n;
     zc* v = Vm + b * nn;
     const zc* g = G + b * nn;
     bool bad = false;
-    for (int i = lane; i < n; i += 32) {
-        for (int j = 0; j < n; ++j) {
-            zc x = v[(long long)j * n + i];
-            for (int k = 0; k < j; ++k) x = x - v[(long long)k * n + i] * g[(long long)j * n + k];
-            x = zdiv(x, g[(long long)j * n + j]);
-            if (!zfinite(x)) bad = true;
-            v[(long long)j * n + i] = x;
-        }
-        q[b * n + i] = g[(long long)i * n + i];
+    for (int j = 0; j < n; ++j) {
+        zc x = v[(long long)j * n + i];
+        for (int k = 0; k < j; ++k) x = x - v[(long long)k * n + i] * g[(long long)j * n + k];
+        x = zdiv(x, g[(long long)j * n + j]);
+        if (!zfinite(x)) bad = true;
+        v[(long long)j * n + i] = x;
     }
-    bad = __any_sync(0xffffffffu, bad);
-    if (bad && lane == 0) fail[b] = 1;
+    q[b * n + i] = g[(long long)i * n + i];
+    if (bad) fail[b] = 1;
 }
 
 // exp(-k0 d G) for the Schur samples by scaling and squaring (rcwa1d_conical.hpp:439-464), with the
@@ -433,14 +452,16 @@ __global__ void right_triangular_solve_kernel(int B, int n, zc* __restrict__ Vm,
 // terms until every sample has converged (at most 40), then the squarings. Per sample, work holds
 // a = -k0 d G, bm = a 2^-s, term and tmp; iter[b] is 1 while sample b sums Taylor terms, done[b]
 // is 1 once its sum has converged.
-__global__ void texp_prep_kernel(int B, int n, const zc* __restrict__ G, const double* __restrict__ k0, double d,
-                                 zc* __restrict__ E, zc* __restrict__ work, const int* __restrict__ schur,
-                                 int* __restrict__ iter, int* __restrict__ done, int* __restrict__ scal,
-                                 int* __restrict__ max_scal, int* __restrict__ fail) {
-    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void __launch_bounds__(kSchurThreads) texp_prep_kernel(int B, int n, const zc* __restrict__ G,
+                                                                  const double* __restrict__ k0, double d,
+                                                                  zc* __restrict__ E, zc* __restrict__ work,
+                                                                  const int* __restrict__ schur, int* __restrict__ iter,
+                                                                  int* __restrict__ done, int* __restrict__ scal,
+                                                                  int* __restrict__ max_scal, int* __restrict__ fail) {
+    __shared__ double red[kSchurThreads / 32];
+    const long long b = blockIdx.x;
     if (b >= B) return;
-    const int lane = threadIdx.x & 31;
-    if (lane == 0) {
+    if (threadIdx.x == 0) {
         iter[b] = 0;
         done[b] = 0;
         scal[b] = 0;
@@ -453,24 +474,22 @@ __global__ void texp_prep_kernel(int B, int n, const zc* __restrict__ G, const d
     zc* term = bm + nn;
     zc* e = E + b * nn;
     const zc* g = G + b * nn;
-    for (long long k = lane; k < nn; k += 32) a[k] = zc{f * g[k].re, f * g[k].im};
-    __syncwarp();
-    const double size = warp_norm1_upper(a, n, lane);
-    bool bad = !isfinite(size);
-    const int scaling = size > .25 ? max(0, (int)ceil(log2(size) + 2.)) : 0;
-    if (scaling > 1020) bad = true;
-    if (bad) {
-        if (lane == 0) fail[b] = 1;
+    for (long long k = threadIdx.x; k < nn; k += blockDim.x) a[k] = zc{f * g[k].re, f * g[k].im};
+    __syncthreads();
+    const double size = block_norm1_upper(a, n, red);
+    const int scaling = isfinite(size) && size > .25 ? max(0, (int)ceil(log2(size) + 2.)) : 0;
+    if (!isfinite(size) || scaling > 1020) {
+        if (threadIdx.x == 0) fail[b] = 1;
         return;
     }
     const double sf = ldexp(1., -scaling);
-    for (long long k = lane; k < nn; k += 32) {
+    for (long long k = threadIdx.x; k < nn; k += blockDim.x) {
         const int j = (int)(k / n), i = (int)(k - (long long)j * n);
         bm[k] = zc{a[k].re * sf, a[k].im * sf};
         e[k] = zc{i == j ? 1.0 : 0.0, 0.0};
         term[k] = e[k];
     }
-    if (lane == 0) {
+    if (threadIdx.x == 0) {
         if (n == 0) done[b] = 1;
         else iter[b] = 1;
         scal[b] = scaling;
@@ -479,27 +498,31 @@ __global__ void texp_prep_kernel(int B, int n, const zc* __restrict__ G, const d
 }
 
 // term = tmp / kk, e += term, then the convergence test ||term||_1 <= eps max(1, ||e||_1)
-__global__ void texp_term_kernel(int B, int n, int kk, zc* __restrict__ E, zc* __restrict__ work, int* __restrict__ iter,
-                                 int* __restrict__ done, int* __restrict__ any_iter, int* __restrict__ fail) {
-    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void __launch_bounds__(kSchurThreads) texp_term_kernel(int B, int n, int kk, zc* __restrict__ E,
+                                                                  zc* __restrict__ work, int* __restrict__ iter,
+                                                                  int* __restrict__ done, int* __restrict__ any_iter,
+                                                                  int* __restrict__ fail) {
+    __shared__ double red[kSchurThreads / 32];
+    const long long b = blockIdx.x;
     if (b >= B || !iter[b]) return;
-    const int lane = threadIdx.x & 31;
     const long long nn = (long long)n * n;
     zc* term = work + b * 4 * nn + 2 * nn;
     const zc* tmp = term + nn;
     zc* e = E + b * nn;
     const double inv = 1. / kk;
-    bool bad = false;
-    for (long long k = lane; k < nn; k += 32) {
+    int bad = 0;
+    for (long long k = threadIdx.x; k < nn; k += blockDim.x) {
         term[k] = tmp[k] * zc{inv, 0.0};
         e[k] = e[k] + term[k];
-        if (!zfinite(e[k]) || !zfinite(term[k])) bad = true;
+        if (!zfinite(e[k]) || !zfinite(term[k])) bad = 1;
     }
-    __syncwarp();
-    bad = __any_sync(0xffffffffu, bad);
+    bad = __syncthreads_or(bad);
     bool converged = false;
-    if (!bad) converged = warp_norm1_upper(term, n, lane) <= 2.220446049250313e-16 * fmax(1., warp_norm1_upper(e, n, lane));
-    if (lane == 0) {
+    if (!bad) {
+        const double nt = block_norm1_upper(term, n, red), ne = block_norm1_upper(e, n, red);
+        converged = nt <= 2.220446049250313e-16 * fmax(1., ne);
+    }
+    if (threadIdx.x == 0) {
         if (bad || (!converged && kk == 40)) {
             fail[b] = 1;
             iter[b] = 0;
@@ -514,32 +537,31 @@ __global__ void texp_term_kernel(int B, int n, int kk, zc* __restrict__ E, zc* _
 
 // e_ii = exp(a_ii 2^(k+1-s)): after the Taylor sum (mode 0, k = -1), or after squaring k (mode 1,
 // which first copies the product in), for converged samples with k < s
-__global__ void texp_fix_kernel(int B, int n, int k, int mode, zc* __restrict__ E, const zc* __restrict__ work,
-                                const int* __restrict__ done, const int* __restrict__ scal, int* __restrict__ fail) {
-    const long long b = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void __launch_bounds__(kSchurThreads) texp_fix_kernel(int B, int n, int k, int mode, zc* __restrict__ E,
+                                                                 const zc* __restrict__ work, const int* __restrict__ done,
+                                                                 const int* __restrict__ scal, int* __restrict__ fail) {
+    const long long b = blockIdx.x;
     if (b >= B || !done[b]) return;
     const int s_ = scal[b];
     if (mode == 1 && k >= s_) return;
-    const int lane = threadIdx.x & 31;
     const long long nn = (long long)n * n;
     const zc* a = work + b * 4 * nn;
     const zc* tmp = a + 3 * nn;
     zc* e = E + b * nn;
-    bool bad = false;
+    int bad = 0;
     if (mode == 1) {
-        for (long long q = lane; q < nn; q += 32) {
+        for (long long q = threadIdx.x; q < nn; q += blockDim.x) {
             e[q] = tmp[q];
-            if (!zfinite(e[q])) bad = true;
+            if (!zfinite(e[q])) bad = 1;
         }
-        __syncwarp();
+        __syncthreads();
     }
     const double s2 = ldexp(1., k + 1 - s_);
-    for (int i = lane; i < n; i += 32) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const zc ai = a[(long long)i * n + i];
         e[(long long)i * n + i] = zexp(zc{ai.re * s2, ai.im * s2});
     }
-    bad = __any_sync(0xffffffffu, bad);
-    if (bad && lane == 0) fail[b] = 1;
+    if (__syncthreads_or(bad) && threadIdx.x == 0) fail[b] = 1;
 }
 
 // 1 where sample b squares at step k
@@ -715,26 +737,27 @@ void batched_triangular_exp(Batch& c, int n, const zc* G, const double* k0, doub
     int* scal = c.mem->zeros<int>(B);
     int* mask = c.mem->zeros<int>(B);
     int* flags = c.mem->zeros<int>(2);  // [0] largest scaling, [1] any sample still summing terms
-    LAUNCH(texp_prep_kernel, warp_blocks(B), 128, st, B, n, G, k0, d, E, work, schur, iter, done, scal, flags, c.fail);
+    LAUNCH(texp_prep_kernel, (unsigned)B, kSchurThreads, st, B, n, G, k0, d, E, work, schur, iter, done, scal, flags,
+           c.fail);
     for (int kk = 1; kk <= 40; ++kk) {
         // tmp = term bm for the samples still summing
         launch_zgemm(st, n, n, n, B, work + 2 * nn, n, 4 * nn, work + nn, n, 4 * nn, nullptr, 0, work + 3 * nn, n, 4 * nn,
                      1.0, 0.0, iter, 0);
         RCWA_CUDA(cudaMemsetAsync(flags + 1, 0, sizeof(int), st));
-        LAUNCH(texp_term_kernel, warp_blocks(B), 128, st, B, n, kk, E, work, iter, done, flags + 1, c.fail);
+        LAUNCH(texp_term_kernel, (unsigned)B, kSchurThreads, st, B, n, kk, E, work, iter, done, flags + 1, c.fail);
         int any = 0;
         RCWA_CUDA(cudaMemcpyAsync(&any, flags + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
         RCWA_CUDA(cudaStreamSynchronize(st));
         if (!any) break;
     }
-    LAUNCH(texp_fix_kernel, warp_blocks(B), 128, st, B, n, -1, 0, E, work, done, scal, c.fail);
+    LAUNCH(texp_fix_kernel, (unsigned)B, kSchurThreads, st, B, n, -1, 0, E, work, done, scal, c.fail);
     int max_scal = 0;
     RCWA_CUDA(cudaMemcpyAsync(&max_scal, flags, sizeof(int), cudaMemcpyDeviceToHost, st));
     RCWA_CUDA(cudaStreamSynchronize(st));
     for (int k = 0; k < max_scal; ++k) {
         LAUNCH(texp_square_mask_kernel, nblocks(B), kTpb, st, B, k, done, scal, mask);
         launch_zgemm(st, n, n, n, B, E, n, nn, E, n, nn, nullptr, 0, work + 3 * nn, n, 4 * nn, 1.0, 0.0, mask, 0);
-        LAUNCH(texp_fix_kernel, warp_blocks(B), 128, st, B, n, k, 1, E, work, done, scal, c.fail);
+        LAUNCH(texp_fix_kernel, (unsigned)B, kSchurThreads, st, B, n, k, 1, E, work, done, scal, c.fail);
     }
     for (int* p : {iter, done, scal, mask, flags}) c.mem->free(p);
 }
@@ -999,10 +1022,12 @@ void conical_schur_modes(Batch& c, const std::vector<SchurJob>& jobs, std::vecto
         LAUNCH(schur_info_kernel, nblocks(B), kTpb, st, B, infos[q], R.schur, eig_info, c.fail);
         R.G = c.dense();
         zc* gg = c.dense();
-        LAUNCH(triangular_root_kernel, warp_blocks(B), 128, st, B, n, Tm, R.G, gg, R.schur, c.fail);
+        LAUNCH(triangular_root_kernel, (unsigned)B, kSchurThreads, st, B, n, Tm, R.G, R.schur, c.fail);
+        gemm(c, R.G, nn, R.G, nullptr, 1.0, 0.0, gg, R.schur, 0);
+        LAUNCH(schur_root_check_kernel, (unsigned)B, kSchurThreads, st, B, n, Tm, gg, R.schur, c.fail);
         LAUNCH(copy_masked_kernel, nblocks(nd), kTpb, st, B, nn, Z, R.W, R.schur);
         gemm(c, jobs[q].Q, nn, Z, nullptr, 1.0, 0.0, R.V, R.schur, 0);
-        LAUNCH(right_triangular_solve_kernel, warp_blocks(B), 128, st, B, n, R.V, R.G, R.q, R.schur, c.fail);
+        LAUNCH(right_triangular_solve_kernel, nblocks((long long)B * n), kTpb, st, B, n, R.V, R.G, R.q, R.schur, c.fail);
         LAUNCH(add_flag_kernel, nblocks(B), kTpb, st, B, R.schur, schur_count);
         for (zc* ptr : {gg, Tm, Z, jobs[q].H, jobs[q].Q}) mem.free(ptr);
         mem.free(infos[q]);
