@@ -1507,6 +1507,14 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
         DOp r;
         for (int b = block_count - 1; b >= 1; --b) {
             const int j = b / 2;
+            if (b % 2 == 0 && reduced && modes[j].analytic && !modes[j + 1].analytic && r.kind == KDense) {
+                // a film over a grating
+                Seam seam = analytic_over_dense_seam(c, modes[j + 1].W, modes[j + 1].V, modes[j].w, modes[j].v, r);
+                mem.free(r.p);
+                g[b] = seam.g;
+                r = seam.r;
+                continue;
+            }
             if (b % 2 == 0 && reduced && !(modes[j].analytic && modes[j + 1].analytic)) {
                 zc *tp, *tm;
                 interface_matching(c, modes[j], modes[j + 1], tp, tm);

@@ -163,7 +163,9 @@ void launch_lu_solve(cudaStream_t st, int n, int nrhs, int batch, const zc* a, l
                      long long lu_stride, int rhs_kind, const zc* rhs, long long rhs_stride, zc* x, long long x_stride,
                      int* singular, const int* skip, int skip_value) {
     if (batch <= 0 || n <= 0) return;
-    if (n >= lu_blocked_min_n() && nrhs > 0) {
+    // blocked from n = 100, and for a handful of systems of moderate order (the per-layer inverses),
+    // where one warp per system would leave the GPU idle
+    if ((n >= lu_blocked_min_n() || (batch < 152 && n >= 32)) && nrhs > 0) {
         TimedLaunch timed(TK_LU, st);
         lu_solve_blocked(st, n, nrhs, batch, a, a_stride, lu, lu_stride, rhs_kind, rhs, rhs_stride, x, x_stride, singular,
                          skip, skip_value);

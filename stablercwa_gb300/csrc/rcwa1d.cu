@@ -523,6 +523,14 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
                 r = {KDiag, rv};
                 continue;
             }
+            if (b % 2 == 0 && reduced && modes[j].analytic && !modes[j + 1].analytic && r.kind == KDense) {
+                // a film (or the incident medium's counterpart) over a grating
+                Seam seam = analytic_over_dense_seam(c, modes[j + 1].W, modes[j + 1].V, nullptr, modes[j].p, r);
+                mem.free(r.p);
+                g[b] = seam.g;
+                r = seam.r;
+                continue;
+            }
             if (b % 2 == 0 && reduced && !(modes[j].analytic && modes[j + 1].analytic)) {
                 zc *tp, *tm;
                 interface_matching(c, modes[j], modes[j + 1], tp, tm);

@@ -205,6 +205,66 @@ __global__ void sub_incident_kernel(int B, int n, int M, zc* __restrict__ R) {
     R[b * n + M].re -= 1.0;
 }
 
+// An analytic medium (diagonal field factors w, v; w = null: 1, the planar form) over a dense region (W, V):
+// the row-scaled combinations of the tangential relations w (d_a + u_a) = W (I + r) d_b and
+// v (d_a - u_a) = V (I - r) d_b. Row i uses the E relation when |w_i| >= |v_i| (always when w is null).
+__device__ __forceinline__ bool e_row(const zc* w, const zc* v, long long bi) {
+    return !w || zabs(w[bi]) >= zabs(v[bi]);
+}
+// P = v W + w V, Q = v W - w V
+__global__ void analytic_pq_kernel(int B, int n, const zc* __restrict__ W, const zc* __restrict__ V,
+                                   const zc* __restrict__ w, const zc* __restrict__ v, zc* __restrict__ P,
+                                   zc* __restrict__ Q) {
+    const long long nn = (long long)n * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * nn) return;
+    const long long b = idx / nn;
+    const long long bi = b * n + (idx - b * nn) % n;
+    const zc a = v[bi] * W[idx], c = w ? w[bi] * V[idx] : V[idx];
+    P[idx] = a + c;
+    Q[idx] = a - c;
+}
+// out = 2 w v per (sample, order)
+__global__ void two_wv_kernel(long long total, const zc* __restrict__ w, const zc* __restrict__ v, zc* __restrict__ out) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < total) out[idx] = 2.0 * (w ? w[idx] * v[idx] : v[idx]);
+}
+// Z0 + Z1 r is W (I + r) in E rows and V (I - r) in H rows: Z0 = W or V, Z1 = W or -V by row
+__global__ void z_rows_kernel(int B, int n, const zc* __restrict__ W, const zc* __restrict__ V, const zc* __restrict__ w,
+                              const zc* __restrict__ v, zc* __restrict__ Z0, zc* __restrict__ Z1) {
+    const long long nn = (long long)n * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * nn) return;
+    const long long b = idx / nn;
+    const long long bi = b * n + (idx - b * nn) % n;
+    if (e_row(w, v, bi)) {
+        Z0[idx] = W[idx];
+        Z1[idx] = W[idx];
+    } else {
+        Z0[idx] = V[idx];
+        Z1[idx] = zc{-V[idx].re, -V[idx].im};
+    }
+}
+// r' from Zg = Z g in place: E rows Zg / w - I, H rows I - Zg / v
+__global__ void seam_reflection_kernel(int B, int n, zc* __restrict__ Zg, const zc* __restrict__ w,
+                                       const zc* __restrict__ v) {
+    const long long nn = (long long)n * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * nn) return;
+    const long long b = idx / nn;
+    const long long rem = idx - b * nn;
+    const int j = (int)(rem / n), i = (int)(rem - (long long)j * n);
+    const long long bi = b * n + i;
+    const double d = i == j ? 1.0 : 0.0;
+    if (e_row(w, v, bi)) {
+        const zc x = w ? zdiv(Zg[idx], w[bi]) : Zg[idx];
+        Zg[idx] = zc{x.re - d, x.im};
+    } else {
+        const zc y = zdiv(Zg[idx], v[bi]);
+        Zg[idx] = zc{d - y.re, -y.im};
+    }
+}
+
 // I - m in place (include/stablercwa/rcwa1d.hpp:623-629)
 __global__ void identity_minus_kernel(int B, int n, zc* __restrict__ m, const int* __restrict__ skip, int skip_value) {
     const long long nn = (long long)n * n;

@@ -334,6 +334,38 @@ Seam reduced_seam(Batch& c, zc* tp, zc* tm, const DOp& r) {
     return out;
 }
 
+// An analytic medium above (diagonal field factors w, v; w = null for the planar form, where w = 1) and a
+// dense region below (W, V) with the dense reflection r under the interface. With
+// w (d_a + u_a) = W (I + r) d_b and v (d_a - u_a) = V (I - r) d_b:
+//     (v W + w V + (v W - w V) r) d_b = 2 w v d_a,  so g = (P + Q r)^-1 diag(2 w v),
+// and u_a from the E relation (rows with |w| >= |v|; every row of the planar form) or the H relation:
+//     r' = diag(1/w) Z g - I  or  I - diag(1/v) Z g,  Z = W (I + r) or V (I - r) row by row,
+// so nothing is divided by a vanishing factor. Three GEMMs and one LU with n right-hand sides for the
+// reference's interface matching (two LUs), interface block (one LU, three GEMMs) and stacking (one LU,
+// three GEMMs): 35 n^3 instead of 69 n^3 flops. n_solve keeps the reference's count.
+Seam analytic_over_dense_seam(Batch& c, const zc* W, const zc* V, const zc* w, const zc* v, const DOp& r) {
+    const long long nd = (long long)c.B * c.nn(), nv = (long long)c.B * c.n;
+    zc* P = c.dense();
+    zc* Q = c.dense();
+    LAUNCH(analytic_pq_kernel, nblocks(nd), kTpb, c.st, c.B, c.n, W, V, w, v, P, Q);
+    gemm(c, Q, c.nn(), r.p, P, 1.0, 1.0, P);
+    zc* dv = c.vec();
+    LAUNCH(two_wv_kernel, nblocks(nv), kTpb, c.st, nv, w, v, dv);
+    zc* g = solve(c, P, true, RHS_DIAG, dv);
+    c.n_solve += 3;  // the reference: W^-1 and V^-1 of the matching, tp^-1, the stacking solve
+    c.mem->free(dv);
+    LAUNCH(z_rows_kernel, nblocks(nd), kTpb, c.st, c.B, c.n, W, V, w, v, P, Q);  // P, Q reused as Z0, Z1
+    gemm(c, Q, c.nn(), r.p, P, 1.0, 1.0, P);                                     // Z = Z0 + Z1 r
+    zc* rp = gemm(c, P, c.nn(), g, nullptr, 1.0, 0.0);
+    LAUNCH(seam_reflection_kernel, nblocks(nd), kTpb, c.st, c.B, c.n, rp, w, v);
+    c.mem->free(P);
+    c.mem->free(Q);
+    Seam out;
+    out.g = {KDense, g};
+    out.r = {KDense, rp};
+    return out;
+}
+
 // y = g x for a KSeam g = tp + tm r' (cols right-hand sides); t is scratch of the size of x
 inline void apply_seam(Batch& c, const DOp& g, int cols, const zc* x, zc* t, zc* y) {
     LAUNCH(matvec_kernel, warp_blocks(c.B), 128, c.st, c.B, c.n, cols, g.rp, x, nullptr, t, 1.0, 0.0);
