@@ -95,7 +95,8 @@ def engine_flops_per_solve(n, pol, rotations_per_matrix, reduced=True):
                  factors and applied to vectors); top interface, one GEMM and one single-column LU. The reference's sequence: 5 LUs with n
                  right-hand sides, 1 single-column LU, 6 GEMMs.
     TM           general: the layer matrix [[1/eps]]^-1 B and V = [[1/eps]] W q, 2 GEMMs; Hermitian:
-                 L^-1 B L^-H, L^-H Y and L Y, 4 products with a triangular factor (4 n^3 each)."""
+                 L^-1 B L^-H from the layer's constant parts (O(n^2)), then L^-H Y and L Y, 2 products with a
+                 triangular factor (4 n^3 each)."""
     lu, tri, mm = (8 / 3) * n ** 3, 8 * n ** 3, 8 * n ** 3
     herm = rotations_per_matrix > 0
     eig = herm_eig_flops(n, rotations_per_matrix) if herm else 105 * n ** 3
@@ -103,7 +104,7 @@ def engine_flops_per_solve(n, pol, rotations_per_matrix, reduced=True):
         seams = (lu + tri) + (mm + lu + 8 * n ** 2)
     else:
         seams = 6 * lu + 5 * tri + 8 * n ** 2 + 6 * mm
-    tm = 0 if pol == 0 else (4 * mm / 2 if herm else 2 * mm)
+    tm = 0 if pol == 0 else (2 * mm / 2 if herm else 2 * mm)
     return eig + seams + tm
 
 

@@ -1281,6 +1281,7 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
         bool herm = false;       // real permittivities: the Hermitian eigensolver
         zc* einv_h = nullptr;    // Hermitian part of [[eps]]^{-1}
         zc *Lchol = nullptr, *Linv = nullptr, *LinvH = nullptr;  // [[1/eps]] = L L^H
+        zc* pencil[4] = {nullptr, nullptr, nullptr, nullptr};    // constant parts of L^-1 B L^-H
     };
     std::vector<LayerData> ld(L);
     const bool try_herm = hermitian_path_enabled(opt);
@@ -1311,6 +1312,7 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
         if (ld[k].herm) {
             ld[k].einv_h = persist.get<zc>(NN);
             LAUNCH(hermitian_part_kernel, nblocks(NN), kTpb, st, N, ld[k].einv, ld[k].einv_h);
+            pencil_parts(st, persist, M, ld[k].einv_h, ld[k].Linv, ld[k].LinvH, ld[k].pencil);
         }
     }
     bool all_herm = !grating.empty();
@@ -1384,21 +1386,18 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                 const int k = grating[gi];
                 zc* AB = ABall + 2 * ndN * gi;
                 LAUNCH(assemble_te_kernel, nblocks(ndN), kTpb, st, B, M, ld[k].c_eps, kx, AB);
-                zc* Bm = mem.get<zc>(ndN);
-                LAUNCH(conical_b_kernel, nblocks(ndN), kTpb, st, B, N, all_herm ? ld[k].einv_h : ld[k].einv, kx, Bm);
                 if (all_herm) {
                     // B C x = lambda x with C = [[1/eps]]^{-1} = (L L^H)^{-1} is the Hermitian-definite pencil
-                    // (B, L L^H): L^{-1} B L^{-H} z = lambda z, x = L z
-                    zc* t = mem.get<zc>(ndN);
-                    launch_zgemm(st, N, N, N, B, Bm, N, NN, ld[k].LinvH, N, 0, nullptr, 0, t, N, NN, 1.0, 0.0, nullptr, 1,
-                                 TRI_B_UPPER);
-                    launch_zgemm(st, N, N, N, B, ld[k].Linv, N, 0, t, N, NN, nullptr, 0, AB + ndN, N, NN, 1.0, 0.0, nullptr,
-                                 1, TRI_A_LOWER);
-                    mem.free(t);
+                    // (B, L L^H): L^{-1} B L^{-H} z = lambda z, x = L z; L^{-1} B L^{-H} from the layer's constant
+                    // parts (kx_j = s cos(phi) - (j - M) lambda / period)
+                    LAUNCH(pencil_combine_kernel, nblocks(ndN), kTpb, st, B, N, ld[k].pencil[0], ld[k].pencil[1],
+                           ld[k].pencil[2], ld[k].pencil[3], P.s_cphi, P.wl, stack.period, AB + ndN);
                 } else {
+                    zc* Bm = mem.get<zc>(ndN);
+                    LAUNCH(conical_b_kernel, nblocks(ndN), kTpb, st, B, N, ld[k].einv, kx, Bm);
                     launch_zgemm(st, N, N, N, B, Bm, N, NN, ld[k].cmat, N, 0, nullptr, 0, AB + ndN, N, NN, 1.0, 0.0);
+                    mem.free(Bm);
                 }
-                mem.free(Bm);
                 LAUNCH(finite_check_kernel, nblocks(ndN), kTpb, st, B, NN, AB, c.fail);
                 LAUNCH(finite_check_kernel, nblocks(ndN), kTpb, st, B, NN, AB + ndN, c.fail);
             }

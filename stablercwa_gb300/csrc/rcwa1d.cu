@@ -329,6 +329,7 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
         bool herm = false;       // Hermitian operators: the Hermitian eigensolver path
         zc* einv_h = nullptr;    // Hermitian part of [[eps]]^{-1} (TM, herm)
         zc *Lchol = nullptr, *Linv = nullptr, *LinvH = nullptr;  // L, L^{-1}, L^{-H} of [[1/eps]] = L L^H (TM, herm)
+        zc* pencil[4] = {nullptr, nullptr, nullptr, nullptr};    // constant parts of L^-1 (Kx E Kx - I) L^-H
     };
     const bool try_herm = hermitian_path_enabled(opt);
     std::vector<LayerData> ld(L);
@@ -363,6 +364,7 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
             if (ld[k].herm) {
                 ld[k].einv_h = persist.get<zc>(nn);
                 LAUNCH(hermitian_part_kernel, nblocks(nn), kTpb, st, n, ld[k].einv, ld[k].einv_h);
+                pencil_parts(st, persist, M, ld[k].einv_h, ld[k].Linv, ld[k].LinvH, ld[k].pencil);
             }
         }
     }
@@ -419,17 +421,18 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
                 if (pol == RCWA_TE) {
                     LAUNCH(assemble_te_kernel, nblocks(nd), kTpb, st, B, M, ld[k].c_eps, kx, A);
                 } else {
-                    mid = c.dense();
-                    LAUNCH(tm_middle_kernel, nblocks(nd), kTpb, st, B, n, herm ? ld[k].einv_h : ld[k].einv, kx, mid);
                     if (herm) {
-                        // the pencil (mid, [[1/eps]]) as the Hermitian L^{-1} mid L^{-H}
-                        zc* t = c.dense();
-                        launch_zgemm(st, n, n, n, B, mid, n, nn, ld[k].LinvH, n, 0, nullptr, 0, t, n, nn, 1.0, 0.0,
-                                     nullptr, 1, TRI_B_UPPER);
-                        launch_zgemm(st, n, n, n, B, ld[k].Linv, n, 0, t, n, nn, nullptr, 0, A, n, nn, 1.0, 0.0,
-                                     nullptr, 1, TRI_A_LOWER);
-                        mem.free(t);
+                        // the pencil (Kx E Kx - I, [[1/eps]]) as the Hermitian L^{-1} (Kx E Kx - I) L^{-H}, from the
+                        // layer's constant parts
+                        LAUNCH(pencil_combine_kernel, nblocks(nd), kTpb, st, B, n, ld[k].pencil[0], ld[k].pencil[1],
+                               ld[k].pencil[2], ld[k].pencil[3], d_s + p0, d_wl + p0, stack.period, A);
+                        if (opt.diagnostics) {  // the residual is taken on [[1/eps]]^{-1} mid, the reference's A
+                            mid = c.dense();
+                            LAUNCH(tm_middle_kernel, nblocks(nd), kTpb, st, B, n, ld[k].einv_h, kx, mid);
+                        }
                     } else {
+                        mid = c.dense();
+                        LAUNCH(tm_middle_kernel, nblocks(nd), kTpb, st, B, n, ld[k].einv, kx, mid);
                         gemm(c, ld[k].cinv, 0, mid, nullptr, 1.0, 0.0, A);
                     }
                     c.n_solve += 2;  // the reference forms A with two dense solves per sample

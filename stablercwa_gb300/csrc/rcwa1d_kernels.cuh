@@ -82,6 +82,32 @@ __global__ void tm_middle_kernel(int B, int n, const zc* __restrict__ einv, cons
     out[idx] = v;
 }
 
+// The parts of Kx E Kx for kx_j = a + b m_j, m_j = j - M (every sample's kx has this form):
+// Kx E Kx = a^2 E + a b X1 + b^2 X2 with X1_ij = (m_i + m_j) E_ij, X2_ij = m_i m_j E_ij (one n x n matrix)
+__global__ void pencil_parts_kernel(int n, int M, const zc* __restrict__ E, zc* __restrict__ X1, zc* __restrict__ X2) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n * n) return;
+    const int j = idx / n, i = idx - j * n;
+    const double mi = (double)(i - M), mj = (double)(j - M);
+    const zc e = E[idx];
+    X1[idx] = (mi + mj) * e;
+    X2[idx] = (mi * mj) * e;
+}
+// A = a^2 S0 + a b S1 + b^2 S2 - C per sample, a = a_s[b] (the order-0 kx), b = -wl[b] / period: the pencil's
+// Hermitian matrix L^-1 (Kx E Kx - I) L^-H from the layer's four constant parts
+__global__ void pencil_combine_kernel(int B, int n, const zc* __restrict__ S0, const zc* __restrict__ S1,
+                                      const zc* __restrict__ S2, const zc* __restrict__ C, const double* __restrict__ a_s,
+                                      const double* __restrict__ wl, double period, zc* __restrict__ A) {
+    const long long nn = (long long)n * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * nn) return;
+    const long long b = idx / nn, e = idx - b * nn;
+    const double a = a_s[b], bb = -wl[b] / period;
+    const double c0 = a * a, c1 = a * bb, c2 = bb * bb;
+    const zc s0 = S0[e], s1 = S1[e], s2 = S2[e], cc = C[e];
+    A[idx] = zc{c0 * s0.re + c1 * s1.re + c2 * s2.re - cc.re, c0 * s0.im + c1 * s1.im + c2 * s2.im - cc.im};
+}
+
 // Modes of an eigen-decomposed layer (include/stablercwa/rcwa1d.hpp:949-958):
 // q = branch(sqrt(lambda)) with Re q >= 0 and Im q <= 0 when Re q < 1e-10; basis q = 1 where q == 0.
 __device__ __forceinline__ zc branch(zc q) {
