@@ -869,11 +869,26 @@ __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, zc* __re
     int status = 0, overflow = 0;
     for (int l = 0; l < n && status == 0 && !overflow; ++l) {
         for (int its = 0;; ++its) {
+            // first m >= l with a negligible e[m]; four tests per pass, independent of one another
             int m = l;
+            for (; m + 3 < n - 1; m += 4) {
+                bool hit[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const double dd = fabs(d[(m + u) * sd]) + fabs(d[(m + u + 1) * sd]);
+                    const double em = fabs(e[(m + u) * sd]);
+                    hit[u] = em <= eps * dd || em <= DBL_MIN;
+                }
+                if (hit[0] || hit[1] || hit[2] || hit[3]) {
+                    m += hit[0] ? 0 : hit[1] ? 1 : hit[2] ? 2 : 3;
+                    goto found;
+                }
+            }
             for (; m < n - 1; ++m) {
                 const double dd = fabs(d[(m) * sd]) + fabs(d[(m + 1) * sd]);
                 if (fabs(e[(m) * sd]) <= eps * dd || fabs(e[(m) * sd]) <= DBL_MIN) break;
             }
+        found:
             if (m == l) break;
             if (its >= max_iter) {
                 status = l + 1;
