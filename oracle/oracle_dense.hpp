@@ -1,6 +1,6 @@
 // oracle_dense.hpp -- CPU restatement of StableRCWA's dense kernels (TEST INFRASTRUCTURE ONLY).
 //
-// This is the checker, not the product: only tests/, __graft_entry__.smoke() and bench.py's CPU
+// This is the oracle, not the product: only tests/, __graft_entry__.smoke() and bench.py's CPU
 // baseline may build, load or call anything under oracle/. It restates, in plain C++17, the
 // reference's complex dense numerics on the RCWA hot path:
 //   * the column-major complex matrix            (include/stablercwa/matrix.hpp:34-114)

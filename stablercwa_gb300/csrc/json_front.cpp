@@ -950,7 +950,7 @@ void write_npy(const std::filesystem::path& path, const char* dtype, const std::
     if (!out) throw std::runtime_error("NPY: cannot create output file");
     out.write(reinterpret_cast<const char*>(prefix), sizeof prefix);
     out.write(header.data(), static_cast<std::streamsize>(header.size()));
-    out.write(static_cast<const char*>(data), static_cast<std::streamsize>(bytes));  // this build's hosts are little-endian
+    out.write(static_cast<const char*>(data), static_cast<std::streamsize>(bytes));  // the supported hosts (x86-64, aarch64) are little-endian
     out.close();
     if (!out) throw std::runtime_error("NPY: writing output failed");
 }

@@ -32,7 +32,7 @@ def masked(text):
     return NUMBER.sub("#", text)
 
 
-# per-key bounds: efficiencies as the benchmark spec's 1e-10; amplitudes 1e-9; kinematics to rounding
+# per-key bounds: efficiencies within the parity bound 1e-10; amplitudes 1e-9; kinematics to rounding
 EFF = {"DEr", "DEt", "R_total", "T_total", "DEr_channels", "DEt_channels", "DEr_s", "DEr_p", "DEt_s", "DEt_p"}
 AMP = {"R", "T", "Jr", "Jt", "Rs", "Rp", "Ts", "Tp", "Ex_r", "Ey_r", "Ez_r", "Ex_t", "Ey_t", "Ez_t", "flux_unitarity",
        "jones_in"}
