@@ -1,7 +1,7 @@
 // oracle_capi.cpp -- C entry points of the CPU oracle (TEST INFRASTRUCTURE ONLY).
 //
 // Built into oracle/_build/liboracle.so by oracle/build.py. Loaded by tests/ (as the parity
-// checker), by __graft_entry__.smoke() and by bench.py's CPU-baseline leg; never by the engine.
+// reference), by __graft_entry__.smoke() and by bench.py's CPU-baseline leg; never by the engine.
 // The structs are the engine's public C ABI (include/stablercwa_gb300.h), so both sides read the
 // same inputs.
 #include <atomic>
