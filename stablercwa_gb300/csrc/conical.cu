@@ -242,20 +242,6 @@ __global__ void conical_scale_kykx_kernel(int B, int N, const zc* __restrict__ c
     out[idx] = (ky[b] * kx[(long long)b * N + m]) * cw[idx];
 }
 
-// Top interface in the reduced form: P = v W + w V, Q = v W - w V (rows scaled by the incident medium's
-// diagonal field factors w, v)
-__global__ void conical_top_pq_kernel(int B, int n, const zc* __restrict__ W, const zc* __restrict__ V,
-                                      const zc* __restrict__ w, const zc* __restrict__ v, zc* __restrict__ P,
-                                      zc* __restrict__ Q) {
-    const long long nn = (long long)n * n;
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long long)B * nn) return;
-    const long long b = idx / nn;
-    const long long bi = b * n + (idx - b * nn) % n;
-    const zc a = v[bi] * W[idx], c = w[bi] * V[idx];
-    P[idx] = a + c;
-    Q[idx] = a - c;
-}
 // right-hand sides 2 w_j v_j e_j for the incident orders j = M (s input) and N + M (p input)
 __global__ void conical_top_rhs_kernel(int B, int n, int N, int M, const zc* __restrict__ w, const zc* __restrict__ v,
                                        zc* __restrict__ rhs) {
@@ -1593,8 +1579,7 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
             // vanishing w or v (an order grazing in the incident medium).
             zc* Pm = c.dense();
             zc* Qm = c.dense();
-            LAUNCH(conical_top_pq_kernel, nblocks(nd), kTpb, st, B, n, modes[1].W, modes[1].V, modes[0].w, modes[0].v, Pm,
-                   Qm);
+            LAUNCH(analytic_pq_kernel, nblocks(nd), kTpb, st, B, n, modes[1].W, modes[1].V, modes[0].w, modes[0].v, Pm, Qm);
             gemm(c, Qm, nn, r.p, Pm, 1.0, 1.0, Pm);
             mem.free(Qm);
             zc* rhs = mem.get<zc>(2 * nv);

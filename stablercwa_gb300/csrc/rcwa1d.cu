@@ -621,7 +621,7 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
             // with a single column; no division by p0, so an order grazing in the incident medium is fine.
             zc* P = c.dense();
             zc* Q = c.dense();
-            LAUNCH(top_pq_kernel, nblocks(nd), kTpb, st, B, n, modes[1].W, modes[1].V, modes[0].p, P, Q);
+            LAUNCH(analytic_pq_kernel, nblocks(nd), kTpb, st, B, n, modes[1].W, modes[1].V, nullptr, modes[0].p, P, Q);
             gemm(c, Q, nn, r.p, P, 1.0, 1.0, P);
             mem.free(Q);
             zc* rhs = c.vec();

@@ -205,17 +205,6 @@ __global__ void seam_system_kernel(int B, int n, const zc* __restrict__ tp, cons
     lhs[idx] = a - ri * m;
     rhs[idx] = ri * a - m;
 }
-// P = p0 W + V, Q = p0 W - V (rows of W scaled by the incident medium's p0), for the top interface
-__global__ void top_pq_kernel(int B, int n, const zc* __restrict__ W, const zc* __restrict__ V, const zc* __restrict__ p0,
-                              zc* __restrict__ P, zc* __restrict__ Q) {
-    const long long nn = (long long)n * n;
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long long)B * nn) return;
-    const long long b = idx / nn;
-    const zc pw = p0[b * n + (idx - b * nn) % n] * W[idx], v = V[idx];
-    P[idx] = pw + v;
-    Q[idx] = pw - v;
-}
 // rhs = 2 p0_M e_M per sample
 __global__ void top_rhs_kernel(int B, int n, int M, const zc* __restrict__ p0, zc* __restrict__ rhs) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
