@@ -238,6 +238,18 @@ def fp64_peak_tflops(torch):
     return 2 * n ** 3 / (best * 1e-3) / 1e12
 
 
+def replica_rate(world, units_per_rank, seconds, device="cpu"):
+    """Whole-job rate of `world` replicas (one per rank, weak scaling): every rank's units over the slowest
+    rank's time, the maximum taken over the ranks with one all-reduce (the replicas exchange no data)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        seconds = float(t.item())
+    return world * units_per_rank / seconds
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -314,13 +326,11 @@ def run_ours(args):
     gemm_ms, gemm_launches = eng.kernel_time("gemm")
     eng.set_kernel_timing(False)
     eig_rotations()
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-        dist.barrier()
     solves_per_step = 2 * P
-    value = world * solves_per_step * args.steps / (total_ms * 1e-3)
+    value = replica_rate(world, solves_per_step * args.steps, total_ms * 1e-3, device="cuda")
+    total_ms = 1e3 * world * solves_per_step * args.steps / value  # the slowest rank's time
+    if world > 1:
+        dist.barrier()
 
     # ---- end to end through the host-buffer entry point
     e2e_times = []
@@ -330,7 +340,7 @@ def run_ours(args):
         both = eng.solve1d_arrays(stack, pts, M, 2)
         e2e_times.append(time.perf_counter() - t0)
     host = [{k: v[:P] for k, v in both.items()}, {k: v[P:] for k, v in both.items()}]
-    e2e_value = world * solves_per_step / (sum(e2e_times) / len(e2e_times))
+    e2e_value = replica_rate(world, solves_per_step, sum(e2e_times) / len(e2e_times), device="cuda")
     h2d = P * 16  # s and wavelength per point, once for both polarizations
     d2h = 2 * (P * n * (16 + 16 + 8 + 8) + P * 4 * 4)
 
