@@ -9,6 +9,11 @@
 #include <math.h>
 #include <stdint.h>
 
+// A kernel's dynamically sized shared array (a host emulation of the kernels for tests predefines it)
+#ifndef RCWA_DYN_SMEM
+#define RCWA_DYN_SMEM(T, name) extern __shared__ T name[]
+#endif
+
 namespace rcwa_gb300 {
 
 struct __align__(16) zc {

@@ -848,7 +848,7 @@ __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, zc* __re
     double* d;
     int sd;
     if constexpr (SMEM) {
-        extern __shared__ double de_sm[];
+        RCWA_DYN_SMEM(double, de_sm);
         d = de_sm + threadIdx.x;
         sd = kHermQlThreads;
     } else {
@@ -991,7 +991,7 @@ constexpr int kHermRows = 32;
 static __global__ void __launch_bounds__(kHermRows) herm_apply_real_kernel(int n, int batch, double* __restrict__ y_out,
                                                                            const zc* __restrict__ ws,
                                                                            const int* __restrict__ info) {
-    extern __shared__ double ysm[];
+    RCWA_DYN_SMEM(double, ysm);
     const long long gid = blockIdx.x;
     const int t = threadIdx.x;
     const int r = blockIdx.y * kHermRows + t;

@@ -1,0 +1,166 @@
+// Runs the Hermitian eigensolver's kernels (stablercwa_gb300/csrc/eig.cuh: herm_tridiag_one, herm_ql_kernel,
+// herm_apply_real_kernel, herm_apply_kernel) on the CPU through tests/emu/cuda_runtime.h and checks the
+// eigenpairs: residual ||A v - lambda v|| / (||A||_F ||v||) <= 1e-13 and orthonormal columns. The group of G
+// lanes is G std::threads; the QL and rotation kernels run one emulated thread at a time. Exit status 0 and
+// a final "OK" line when every case passes. Test infrastructure only.
+#include <barrier>
+#include <cmath>
+#include <cstdio>
+#include <random>
+#include <thread>
+#include <vector>
+
+#include "cuda_runtime.h"
+
+thread_local dim3e threadIdx;
+static std::barrier<>* bar;
+static int group_size;
+static double dslot[256];
+static int islot[256];
+void emu_sync() { bar->arrive_and_wait(); }
+double emu_shfl_xor(double v, int o) {
+    const int l = threadIdx.x;
+    dslot[l] = v;
+    bar->arrive_and_wait();
+    const double r = dslot[l ^ o];
+    bar->arrive_and_wait();
+    return r;
+}
+int emu_shfl_xor_i(int v, int o) {
+    const int l = threadIdx.x;
+    islot[l] = v;
+    bar->arrive_and_wait();
+    const int r = islot[l ^ o];
+    bar->arrive_and_wait();
+    return r;
+}
+unsigned emu_ballot(int p) {
+    const int l = threadIdx.x;
+    islot[l] = p;
+    bar->arrive_and_wait();
+    unsigned b = 0;
+    const int w0 = (l / 32) * 32;
+    for (int k = w0; k < group_size && k < w0 + 32; ++k)
+        if (islot[k]) b |= 1u << (k - w0);
+    bar->arrive_and_wait();
+    return b;
+}
+
+#include "../../stablercwa_gb300/csrc/eig.cuh"
+
+using namespace rcwa_gb300;
+
+static int failures = 0;
+
+template <int G>
+void run(int n, const std::vector<zc>& a, const char* tag, bool real_form, bool smem_ql) {
+    group_size = G;
+    std::barrier<> b(G);
+    bar = &b;
+    std::vector<zc> V((size_t)n * n), W(n), ws(eig_workspace_elems(n));
+    int info = -7;
+    std::vector<std::thread> th;
+    for (int l = 0; l < G; ++l)
+        th.emplace_back([&, l] {
+            threadIdx.x = l;
+            herm_tridiag_one<G>(n, a.data(), V.data(), ws.data(), nullptr, nullptr);
+        });
+    for (auto& t : th) t.join();
+    unsigned long long rot = 0;
+    threadIdx.x = 0;
+    blockIdx.x = 0;
+    blockIdx.y = 0;
+    blockDim.x = smem_ql ? kHermQlThreads : 128;
+    if (smem_ql)
+        herm_ql_kernel<true>(n, 1, W.data(), &info, ws.data(), 2.220446049250313e-16, 30, &rot);
+    else
+        herm_ql_kernel<false>(n, 1, W.data(), &info, ws.data(), 2.220446049250313e-16, 30, &rot);
+    const int* tail = reinterpret_cast<const int*>(ws.data() + 3LL * n * n);
+    if (info != 0 || tail[1] != 0) {
+        std::printf("FAIL %s n=%d: info %d overflow %d\n", tag, n, info, tail[1]);
+        ++failures;
+        return;
+    }
+    if (real_form) {
+        std::vector<double> Y((size_t)n * n);
+        for (int r = 0; r < n; ++r) {
+            blockIdx.x = 0;
+            blockIdx.y = r / kHermRows;
+            threadIdx.x = r % kHermRows;
+            herm_apply_real_kernel(n, 1, Y.data(), ws.data(), &info);
+        }
+        std::vector<zc> Q = V;  // Z = Q Y, the product zdgemm_kernel forms on the device
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i) {
+                zc acc{0.0, 0.0};
+                for (int k = 0; k < n; ++k) acc = acc + Q[(size_t)k * n + i] * Y[(size_t)j * n + k];
+                V[(size_t)j * n + i] = acc;
+            }
+    } else {
+        blockDim.x = 128;
+        for (int r = 0; r < n; ++r) {
+            blockIdx.x = 0;
+            threadIdx.x = r;
+            herm_apply_kernel(n, 1, V.data(), ws.data(), &info);
+        }
+    }
+    blockIdx.y = 0;
+    double fro = 0.0;
+    for (const zc& z : a) fro += norm2(z);
+    fro = std::sqrt(fro);
+    double worst = 0.0, orth = 0.0;
+    for (int j = 0; j < n; ++j) {
+        double dn = 0.0, vn = 0.0;
+        for (int i = 0; i < n; ++i) {
+            zc acc{0.0, 0.0};
+            for (int k = 0; k < n; ++k) acc = acc + a[(size_t)k * n + i] * V[(size_t)j * n + k];
+            dn += norm2(acc - W[j] * V[(size_t)j * n + i]);
+            vn += norm2(V[(size_t)j * n + i]);
+        }
+        worst = std::fmax(worst, std::sqrt(dn) / (std::fmax(fro, 1e-300) * std::sqrt(vn)));
+        for (int k = 0; k < n; ++k) {
+            zc dot{0.0, 0.0};
+            for (int i = 0; i < n; ++i) dot = dot + conj(V[(size_t)j * n + i]) * V[(size_t)k * n + i];
+            orth = std::fmax(orth, zabs(dot - zc{j == k ? 1.0 : 0.0, 0.0}));
+        }
+    }
+    const bool ok = worst <= 1e-13 && orth <= 1e-13 * std::sqrt((double)std::max(n, 1));
+    std::printf("%s %s G=%d n=%d rotations %llu residual %.2e orth %.2e%s\n", ok ? "pass" : "FAIL", tag, G, n, rot, worst,
+                orth, real_form ? "" : " (complex rotations)");
+    if (!ok) ++failures;
+}
+
+int main() {
+    std::setvbuf(stdout, nullptr, _IONBF, 0);
+    std::mt19937_64 rng(11);
+    std::normal_distribution<double> nd;
+    for (int n : {1, 2, 3, 9, 33, 61}) {
+        std::vector<zc> r((size_t)n * n), t((size_t)n * n), d((size_t)n * n, zc{0.0, 0.0});
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i <= j; ++i) {
+                const zc v{nd(rng), i == j ? 0.0 : nd(rng)};
+                r[(size_t)j * n + i] = v;
+                r[(size_t)i * n + j] = conj(v);
+            }
+        // a lossless grating's TE layer matrix Kx^2 - [[eps]] (repeated eigenvalues at kx0 = 0)
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i) {
+                const int h = i - j;
+                const double kx = (i - n / 2) * 0.61;
+                const zc c = h == 0 ? zc{2.2, 0.0} : zc{0.6 * std::sin(0.9 * h) / h, 0.6 * (1 - std::cos(0.9 * h)) / h};
+                t[(size_t)j * n + i] = (i == j ? zc{kx * kx, 0.0} : zc{0.0, 0.0}) - c;
+            }
+        for (int i = 0; i < n; ++i) d[(size_t)i * n + i] = zc{(double)(i % 3), 0.0};  // repeated, already diagonal
+        run<4>(n, r, "random", true, true);
+        run<16>(n, r, "random", true, false);
+        run<32>(n, t, "toeplitz", true, true);
+        run<8>(n, t, "toeplitz", false, true);
+        run<4>(n, d, "diagonal", true, true);
+    }
+    if (failures) {
+        std::printf("%d FAILED\n", failures);
+        return 1;
+    }
+    std::printf("OK\n");
+    return 0;
+}
