@@ -1,8 +1,9 @@
 // Runs the Hermitian eigensolver's kernels (stablercwa_gb300/csrc/eig.cuh: herm_tridiag_one, herm_ql_kernel,
-// herm_apply_real_kernel, herm_apply_kernel) on the CPU through tests/emu/cuda_runtime.h and checks the
-// eigenpairs: residual ||A v - lambda v|| / (||A||_F ||v||) <= 1e-13 and orthonormal columns. The group of G
-// lanes is G std::threads; the QL and rotation kernels run one emulated thread at a time. Exit status 0 and
-// a final "OK" line when every case passes. Test infrastructure only.
+// herm_apply_real_kernel, herm_apply_kernel) and the general solver's eig_one on the CPU through
+// tests/emu/cuda_runtime.h and checks the eigenpairs: residual ||A v - lambda v|| / (||A||_F ||v||) <= 1e-13,
+// and orthonormal columns for the Hermitian solver. The group of G lanes is G std::threads; the QL and
+// rotation kernels run one emulated thread at a time. Exit status 0 and a final "OK" line when every case
+// passes. Test infrastructure only.
 #include <barrier>
 #include <cmath>
 #include <cstdio>
@@ -130,6 +131,43 @@ void run(int n, const std::vector<zc>& a, const char* tag, bool real_form, bool 
     if (!ok) ++failures;
 }
 
+// the general solver (CORTH + COMQR2, eig_one) with G lanes or a CTA of G threads per matrix
+template <int G>
+void run_general(int n, const std::vector<zc>& a, const char* tag) {
+    group_size = G;
+    std::barrier<> b(G);
+    bar = &b;
+    std::vector<zc> V((size_t)n * n), W(n), ws(eig_workspace_elems(n));
+    int info = -7, sweeps = 0;
+    static double red[8];
+    static int ired[8];
+    std::vector<std::thread> th;
+    for (int l = 0; l < G; ++l)
+        th.emplace_back([&, l] {
+            threadIdx.x = l;
+            eig_one<G>(n, a.data(), W.data(), V.data(), &info, &sweeps, ws.data(), 2.220446049250313e-16, 30, nullptr, red,
+                       ired);
+        });
+    for (auto& t : th) t.join();
+    double fro = 0.0;
+    for (const zc& z : a) fro += norm2(z);
+    fro = std::sqrt(fro);
+    double worst = 0.0;
+    for (int j = 0; j < n; ++j) {
+        double dn = 0.0, vn = 0.0;
+        for (int i = 0; i < n; ++i) {
+            zc acc{0.0, 0.0};
+            for (int k = 0; k < n; ++k) acc = acc + a[(size_t)k * n + i] * V[(size_t)j * n + k];
+            dn += norm2(acc - W[j] * V[(size_t)j * n + i]);
+            vn += norm2(V[(size_t)j * n + i]);
+        }
+        worst = std::fmax(worst, std::sqrt(dn) / (std::fmax(fro, 1e-300) * std::sqrt(vn)));
+    }
+    const bool ok = info == 0 && worst <= 1e-13;
+    std::printf("%s general %s G=%d n=%d sweeps %d residual %.2e\n", ok ? "pass" : "FAIL", tag, G, n, sweeps, worst);
+    if (!ok) ++failures;
+}
+
 int main() {
     std::setvbuf(stdout, nullptr, _IONBF, 0);
     std::mt19937_64 rng(11);
@@ -156,6 +194,13 @@ int main() {
         run<32>(n, t, "toeplitz", true, true);
         run<8>(n, t, "toeplitz", false, true);
         run<4>(n, d, "diagonal", true, true);
+    }
+    for (int n : {1, 2, 5, 17, 30}) {
+        std::vector<zc> g((size_t)n * n);
+        for (auto& z : g) z = zc{nd(rng), nd(rng)};
+        run_general<4>(n, g, "random");
+        run_general<32>(n, g, "random");
+        run_general<64>(n, g, "random");
     }
     if (failures) {
         std::printf("%d FAILED\n", failures);
