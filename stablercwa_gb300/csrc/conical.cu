@@ -1284,9 +1284,12 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                                          layer_fail);
         zc* c_inv = layer_coefficients(st, persist, edges, inv, stack.period, M, Ly.fourier_method, Ly.fft_samples,
                                        layer_fail);
-        ld[k].herm = try_herm && make_hermitian_coefficients(st, ld[k].c_eps, M) &&
-                     make_hermitian_coefficients(st, c_inv, M) &&
-                     toeplitz_cholesky_inverse(st, c_inv, M, persist, ld[k].Lchol, ld[k].Linv, ld[k].LinvH);
+        ld[k].herm = try_herm && real_profile(eps) && real_profile(inv);
+        if (ld[k].herm) {
+            make_hermitian_coefficients(st, ld[k].c_eps, M);
+            make_hermitian_coefficients(st, c_inv, M);
+            toeplitz_cholesky_inverse(st, c_inv, M, persist, layer_fail, ld[k].Lchol, ld[k].Linv, ld[k].LinvH);
+        }
         zc* E = persist.get<zc>(NN);
         zc* Ci = persist.get<zc>(NN);
         LAUNCH(toeplitz_kernel, nblocks(NN), kTpb, st, M, ld[k].c_eps, E);

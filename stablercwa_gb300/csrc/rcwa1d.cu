@@ -344,13 +344,15 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
         }
         ld[k].c_eps = layer_coefficients(st, persist, edges, eps, stack.period, M, Ly.fourier_method, Ly.fft_samples,
                                          layer_fail);
-        ld[k].herm = try_herm && make_hermitian_coefficients(st, ld[k].c_eps, M);
+        ld[k].herm = try_herm && real_profile(eps) && real_profile(inv);
+        if (ld[k].herm) make_hermitian_coefficients(st, ld[k].c_eps, M);
         if (pol == RCWA_TM) {
             zc* c_inv = layer_coefficients(st, persist, edges, inv, stack.period, M, Ly.fourier_method, Ly.fft_samples,
                                            layer_fail);
-            if (ld[k].herm)
-                ld[k].herm = make_hermitian_coefficients(st, c_inv, M) &&
-                             toeplitz_cholesky_inverse(st, c_inv, M, persist, ld[k].Lchol, ld[k].Linv, ld[k].LinvH);
+            if (ld[k].herm) {
+                make_hermitian_coefficients(st, c_inv, M);
+                toeplitz_cholesky_inverse(st, c_inv, M, persist, layer_fail, ld[k].Lchol, ld[k].Linv, ld[k].LinvH);
+            }
             zc* E = persist.get<zc>(nn);
             ld[k].inv_eps = persist.get<zc>(nn);
             LAUNCH(toeplitz_kernel, nblocks(nn), kTpb, st, M, ld[k].c_eps, E);
@@ -801,13 +803,9 @@ void fourier_coefficients_api(cudaStream_t st, const double* edges, const rcwa_c
             throw EngineError{RCWA_EINVAL, "rcwa: FFT material values must be finite"};
         v[j] = cd{values[j].re, values[j].im};
     }
-    if (method == 0) {
-        const std::vector<cd> c = fourier_coefficients(e, v, period, hmax);
-        std::memcpy(out, c.data(), c.size() * sizeof(cd));
-        return;
-    }
     DeviceScratch mem(st);
-    zc* d = fft_coefficients_dev(st, mem, e, v, period, hmax, samples);
+    zc* d = method == 0 ? closed_form_coefficients(st, mem, e, v, period, hmax)
+                        : fft_coefficients_dev(st, mem, e, v, period, hmax, samples);
     RCWA_CUDA(cudaMemcpyAsync(out, d, (2 * (size_t)hmax + 1) * sizeof(zc), cudaMemcpyDeviceToHost, st));
     RCWA_CUDA(cudaStreamSynchronize(st));
 }

@@ -29,16 +29,15 @@ namespace {
 
 // ============================================================== host: geometry and Fourier data
 
-struct HostProfile {
-    std::vector<double> edges;
-    std::vector<cd> n;
-};
+// A layer's geometry as host vectors (strip k spans y_edges[k]..y_edges[k+1] and holds the x profile
+// strip_edges[k] / strip_n[k]).
 struct HostLayer {
     double d = 0.0;
     bool homog = true;
     cd n{1.0, 0.0};
     std::vector<double> y_edges;
-    std::vector<HostProfile> rows;
+    std::vector<std::vector<double>> strip_edges;
+    std::vector<std::vector<cd>> strip_n;
 };
 
 inline cd to_cd(const rcwa_complex& z) { return cd{z.re, z.im}; }
@@ -52,137 +51,18 @@ HostLayer host_layer(const rcwa_layer2d& L) {
         h.y_edges.assign(L.y_edges, L.y_edges + L.n_strips + 1);
         for (int k = 0; k < L.n_strips; ++k) {
             const rcwa_xprofile2d& p = L.x_profiles[k];
-            HostProfile r;
-            r.edges.assign(p.edges, p.edges + p.n_segments + 1);
-            for (int s = 0; s < p.n_segments; ++s) r.n.push_back(to_cd(p.n_values[s]));
-            h.rows.push_back(std::move(r));
+            h.strip_edges.emplace_back(p.edges, p.edges + p.n_segments + 1);
+            std::vector<cd> nv(p.n_segments);
+            for (int s = 0; s < p.n_segments; ++s) nv[s] = to_cd(p.n_values[s]);
+            h.strip_n.push_back(std::move(nv));
         }
     }
     return h;
 }
 
-// exp(-i 2 pi h x_k / P), argument evaluated as the reference (rcwa2d_operators.hpp:86-95)
-std::vector<cd> edge_phases(const std::vector<double>& edges, int h, double period) {
-    std::vector<cd> phase(edges.size());
-    for (size_t k = 0; k < edges.size(); ++k) {
-        const double arg = (-2.0 * kPiD * (static_cast<double>(h) * edges[k])) / period;
-        phase[k] = cd{std::cos(arg), std::sin(arg)};
-    }
-    return phase;
-}
-
-// c[h + hmax] of a piecewise-constant profile (fourier_1d, rcwa2d_operators.hpp:97-117)
-std::vector<cd> fourier_1d(const std::vector<double>& edges, const std::vector<cd>& values, double period, int hmax) {
-    std::vector<cd> c(2 * hmax + 1);
-    cd mean{};
-    for (size_t j = 0; j < values.size(); ++j) mean += values[j] * (edges[j + 1] - edges[j]);
-    c[hmax] = mean / period;
-    for (int h = -hmax; h <= hmax; ++h) {
-        if (h == 0) continue;
-        const std::vector<cd> phase = edge_phases(edges, h, period);
-        cd sum{};
-        for (size_t j = 0; j < values.size(); ++j) sum += values[j] * (phase[j + 1] - phase[j]);
-        const double w = -2.0 * kPiD * static_cast<double>(h);
-        c[h + hmax] = cd{sum.imag() / w, -sum.real() / w};
-    }
-    return c;
-}
-
-// segment weights, K x (2 hmax + 1) row-major (seg_fourier, rcwa2d_operators.hpp:121-140)
-std::vector<cd> seg_fourier(const std::vector<double>& edges, int hmax, double period) {
-    const int K = static_cast<int>(edges.size()) - 1, H = 2 * hmax + 1;
-    std::vector<cd> out((size_t)K * H);
-    for (int k = 0; k < K; ++k) out[(size_t)k * H + hmax] = cd{(edges[k + 1] - edges[k]) / period, 0.0};
-    for (int h = -hmax; h <= hmax; ++h) {
-        if (h == 0) continue;
-        const std::vector<cd> phase = edge_phases(edges, h, period);
-        const double w = -2.0 * kPiD * static_cast<double>(h);
-        for (int k = 0; k < K; ++k) {
-            const cd d = phase[k + 1] - phase[k];
-            out[(size_t)k * H + h + hmax] = cd{d.imag() / w, -d.real() / w};
-        }
-    }
-    return out;
-}
-
-// Python's float % (rcwa2d_operators.hpp:144-154)
-double floor_mod(double a, double b) {
-    double mod = std::fmod(a, b);
-    if (mod != 0.0) {
-        if ((b < 0.0) != (mod < 0.0)) mod += b;
-    } else {
-        mod = std::copysign(0.0, b);
-    }
-    return mod;
-}
-
-void sort_unique(std::vector<double>& v) {
-    std::sort(v.begin(), v.end());
-    v.erase(std::unique(v.begin(), v.end()), v.end());
-}
-
-// epsilon = n^2 of a profile at x, wrapped by the period (eps_at, rcwa2d_operators.hpp:162-171)
-cd eps_at(const HostProfile& p, double x, double Lx) {
-    const double xx = p.edges[0] + floor_mod(x - p.edges[0], Lx);
-    long k = (long)(std::upper_bound(p.edges.begin(), p.edges.end(), xx) - p.edges.begin()) - 1;
-    const long last = (long)p.n.size() - 1;
-    k = std::min(std::max(k, 0L), last);
-    return p.n[(size_t)k] * p.n[(size_t)k];
-}
-
-// x cuts of all profiles merged (merge_x_cuts, rcwa2d_operators.hpp:178-192)
-std::vector<double> merge_x_cuts(const std::vector<HostProfile>& rows, double Lx) {
-    std::vector<double> cuts;
-    for (const HostProfile& p : rows)
-        for (double e : p.edges) cuts.push_back(floor_mod(e, Lx));
-    cuts.push_back(0.0);
-    cuts.push_back(Lx);
-    sort_unique(cuts);
-    for (double& c : cuts) c = std::rint(c * 1e12) / 1e12;
-    sort_unique(cuts);
-    cuts.erase(std::remove_if(cuts.begin(), cuts.end(), [&](double c) { return !(c >= -1e-12 && c <= Lx + 1e-12); }),
-               cuts.end());
-    if (cuts.empty() || cuts.front() > 1e-12) cuts.insert(cuts.begin(), 0.0);
-    if (cuts.back() < Lx - 1e-12) cuts.push_back(Lx);
-    return cuts;
-}
-
-// Everything of layer_operators (rcwa2d_operators.hpp:325-429) that is O(K M) work: the Fourier
-// coefficients of each strip and of each x-cut column, and the segment weights.
-struct LayerFourier {
-    int K = 0, Kx = 0;
-    std::vector<cd> wy, ce, ci, wx, cyc;
-};
-
-LayerFourier layer_fourier(const HostLayer& L, double Lx, double Ly, int M1, int M2, bool li) {
-    LayerFourier F;
-    F.K = (int)L.rows.size();
-    F.wy = seg_fourier(L.y_edges, 2 * M2, Ly);
-    for (const HostProfile& p : L.rows) {
-        std::vector<cd> sq(p.n.size());
-        for (size_t j = 0; j < p.n.size(); ++j) sq[j] = p.n[j] * p.n[j];
-        const std::vector<cd> c = fourier_1d(p.edges, sq, Lx, 2 * M1);
-        F.ce.insert(F.ce.end(), c.begin(), c.end());
-        if (li) {
-            std::vector<cd> inv(sq.size());
-            for (size_t j = 0; j < sq.size(); ++j) inv[j] = cd{1.0, 0.0} / sq[j];
-            const std::vector<cd> ci = fourier_1d(p.edges, inv, Lx, 2 * M1);
-            F.ci.insert(F.ci.end(), ci.begin(), ci.end());
-        }
-    }
-    if (li) {
-        const std::vector<double> xcuts = merge_x_cuts(L.rows, Lx);
-        F.Kx = (int)xcuts.size() - 1;
-        F.wx = seg_fourier(xcuts, 2 * M1, Lx);
-        for (int j = 0; j < F.Kx; ++j) {
-            const double xm = 0.5 * (xcuts[j] + xcuts[j + 1]);
-            std::vector<cd> inv_col(F.K);
-            for (int k = 0; k < F.K; ++k) inv_col[k] = cd{1.0, 0.0} / eps_at(L.rows[k], xm, Lx);
-            const std::vector<cd> c = fourier_1d(L.y_edges, inv_col, Ly, 2 * M2);
-            F.cyc.insert(F.cyc.end(), c.begin(), c.end());
-        }
-    }
-    return F;
+LayerFourier2D layer_fourier(cudaStream_t st, DeviceScratch& mem, const HostLayer& L, double Lx, double Ly, int M1,
+                             int M2, bool li) {
+    return layer_fourier2d(st, mem, L.y_edges, L.strip_edges, L.strip_n, Lx, Ly, M1, M2, li);
 }
 
 zc* upload(DeviceScratch& mem, cudaStream_t st, const std::vector<cd>& v) {
@@ -201,48 +81,40 @@ struct DevOps {
     zc *eps = nullptr, *cx = nullptr, *cy = nullptr;
 };
 
-// Eps, Cx, Cy of one patterned layer on the device; a singular inverse-rule Toeplitz matrix or a
-// non-finite operator sets *d_flag.
-DevOps device_operators(cudaStream_t st, DeviceScratch& mem, const LayerFourier& F, int M1, int M2, bool li, int* d_flag) {
+// Eps, Cx, Cy of one patterned layer on the device from its device Fourier data (consumed and freed);
+// a singular inverse-rule Toeplitz matrix or a non-finite operator sets *d_flag.
+DevOps device_operators(cudaStream_t st, DeviceScratch& mem, LayerFourier2D F, int M1, int M2, bool li, int* d_flag) {
     const int n1 = 2 * M1 + 1, n2 = 2 * M2 + 1, N = n1 * n2;
     const long long NN = (long long)N * N;
     DevOps o;
-    zc* wy = upload(mem, st, F.wy);
-    zc* ce = upload(mem, st, F.ce);
     o.eps = mem.get<zc>(NN);
-    LAUNCH(op_eps_kernel, nblocks(NN), kTpb, st, M1, M2, F.K, wy, ce, o.eps);
+    LAUNCH(op_eps_kernel, nblocks(NN), kTpb, st, M1, M2, F.K, F.wy, F.ce, o.eps);
     if (!li) {
         o.cx = o.eps;
         o.cy = o.eps;
     } else {
-        zc* ci = upload(mem, st, F.ci);
         zc* tx = mem.get<zc>((size_t)F.K * n1 * n1);
         zc* invx = mem.get<zc>((size_t)F.K * n1 * n1);
         int* sing = mem.zeros<int>(F.K);
-        LAUNCH(toeplitz_batch_kernel, nblocks((long long)F.K * n1 * n1), kTpb, st, F.K, M1, ci, tx);
+        LAUNCH(toeplitz_batch_kernel, nblocks((long long)F.K * n1 * n1), kTpb, st, F.K, M1, F.ci, tx);
         launch_lu_solve(st, n1, n1, F.K, tx, (long long)n1 * n1, tx, (long long)n1 * n1, RHS_IDENTITY, nullptr, 0, invx,
                         (long long)n1 * n1, sing);
         LAUNCH(any_set_kernel, nblocks(F.K), kTpb, st, F.K, sing, d_flag);
         o.cx = mem.get<zc>(NN);
-        LAUNCH(op_cx_kernel, nblocks(NN), kTpb, st, M1, M2, F.K, wy, invx, o.cx);
+        LAUNCH(op_cx_kernel, nblocks(NN), kTpb, st, M1, M2, F.K, F.wy, invx, o.cx);
 
-        zc* wx = upload(mem, st, F.wx);
-        zc* cyc = upload(mem, st, F.cyc);
         zc* ty = mem.get<zc>((size_t)F.Kx * n2 * n2);
         zc* invy = mem.get<zc>((size_t)F.Kx * n2 * n2);
         int* sing_y = mem.zeros<int>(F.Kx);
-        LAUNCH(toeplitz_batch_kernel, nblocks((long long)F.Kx * n2 * n2), kTpb, st, F.Kx, M2, cyc, ty);
+        LAUNCH(toeplitz_batch_kernel, nblocks((long long)F.Kx * n2 * n2), kTpb, st, F.Kx, M2, F.cyc, ty);
         launch_lu_solve(st, n2, n2, F.Kx, ty, (long long)n2 * n2, ty, (long long)n2 * n2, RHS_IDENTITY, nullptr, 0, invy,
                         (long long)n2 * n2, sing_y);
         LAUNCH(any_set_kernel, nblocks(F.Kx), kTpb, st, F.Kx, sing_y, d_flag);
         o.cy = mem.get<zc>(NN);
-        LAUNCH(op_cy_kernel, nblocks(NN), kTpb, st, M1, M2, F.Kx, wx, invy, o.cy);
-        for (void* p : {(void*)ci, (void*)tx, (void*)invx, (void*)sing, (void*)wx, (void*)cyc, (void*)ty, (void*)invy,
-                        (void*)sing_y})
-            mem.free(p);
+        LAUNCH(op_cy_kernel, nblocks(NN), kTpb, st, M1, M2, F.Kx, F.wx, invy, o.cy);
+        for (void* p : {(void*)tx, (void*)invx, (void*)sing, (void*)ty, (void*)invy, (void*)sing_y}) mem.free(p);
     }
-    mem.free(wy);
-    mem.free(ce);
+    free_layer_fourier2d(mem, F);
     for (zc* m : {o.eps, o.cx, o.cy}) LAUNCH(any_nonfinite_kernel, nblocks(NN), kTpb, st, NN, m, d_flag);
     return o;
 }
@@ -493,7 +365,7 @@ void layer_operators2d(cudaStream_t st, const rcwa_layer2d& layer, double Lx, do
     DeviceScratch mem(st);
     const bool li = factorization == RCWA_FACTORIZATION_LI;
     int* flag = mem.zeros<int>(1);
-    const DevOps o = device_operators(st, mem, layer_fourier(host_layer(layer), Lx, Ly, M1, M2, li), M1, M2, li, flag);
+    const DevOps o = device_operators(st, mem, layer_fourier(st, mem, host_layer(layer), Lx, Ly, M1, M2, li), M1, M2, li, flag);
     if (eps) RCWA_CUDA(cudaMemcpyAsync(eps, o.eps, NN * sizeof(zc), cudaMemcpyDeviceToHost, st));
     if (cx) RCWA_CUDA(cudaMemcpyAsync(cx, o.cx, NN * sizeof(zc), cudaMemcpyDeviceToHost, st));
     if (cy) RCWA_CUDA(cudaMemcpyAsync(cy, o.cy, NN * sizeof(zc), cudaMemcpyDeviceToHost, st));
@@ -600,7 +472,8 @@ void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d
     std::vector<zc*> Ei(P);
     for (int k = 0; k < P; ++k) {
         const HostLayer& hl = layers[patterned[k]];
-        ops[k] = device_operators(st, call_mem, layer_fourier(hl, stack.Lx, stack.Ly, M1, M2, li), M1, M2, li, op_flag);
+        ops[k] = device_operators(st, call_mem, layer_fourier(st, call_mem, hl, stack.Lx, stack.Ly, M1, M2, li), M1, M2, li,
+                                  op_flag);
         int* sing = call_mem.zeros<int>(1);
         Ei[k] = call_mem.get<zc>(NN);
         zc* tmp = call_mem.get<zc>(NN);

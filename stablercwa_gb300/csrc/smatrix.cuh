@@ -15,23 +15,12 @@
 #include <vector>
 
 #include "engine.h"
+#include "fourier.cuh"
+#include "launch.cuh"
 #include "rcwa1d_kernels.cuh"
 
 namespace rcwa_gb300 {
 namespace {
-
-constexpr int kTpb = 256;
-inline unsigned nblocks(long long total, int tpb = kTpb) {
-    return static_cast<unsigned>((total + tpb - 1) / tpb > 0 ? (total + tpb - 1) / tpb : 1);
-}
-inline unsigned warp_blocks(long long warps) { return static_cast<unsigned>((warps * 32 + 127) / 128); }
-
-#define LAUNCH(kernel, grid, block, st, ...)                      \
-    do {                                                         \
-        kernel<<<(grid), (block), 0, (st)>>>(__VA_ARGS__);       \
-        ++launch_count();                                        \
-        RCWA_CUDA(cudaGetLastError());                           \
-    } while (0)
 
 // ---------------------------------------------------------------- small per-sample vector kernels
 
@@ -378,32 +367,6 @@ inline void apply_seam(Batch& c, const DOp& g, int cols, const zc* x, zc* t, zc*
 using cd = std::complex<double>;
 constexpr double kPiD = 3.141592653589793238462643383279502884;
 
-// c_h, h = -hmax..hmax, of a piecewise-constant profile (include/stablercwa/rcwa1d.hpp:366-388)
-std::vector<cd> fourier_coefficients(const std::vector<double>& edges, const std::vector<cd>& values, double period,
-                                     int hmax) {
-    std::vector<cd> c(2 * hmax + 1);
-    const size_t segments = values.size();
-    std::vector<cd> phase(edges.size());
-    for (int h = -hmax; h <= hmax; ++h) {
-        cd sum{};
-        if (h == 0) {
-            for (size_t j = 0; j < segments; ++j) sum += values[j] * (edges[j + 1] - edges[j]) / period;
-        } else {
-            for (size_t k = 0; k < edges.size(); ++k) {
-                const double arg = -2.0 * kPiD * h * edges[k] / period;
-                phase[k] = cd{std::cos(arg), std::sin(arg)};
-            }
-            const double w = -2.0 * kPiD * h;
-            for (size_t j = 0; j < segments; ++j) {
-                const cd t = values[j] * (phase[j + 1] - phase[j]);
-                sum += cd{t.imag() / w, -t.real() / w};
-            }
-        }
-        c[h + hmax] = sum;
-    }
-    return c;
-}
-
 // ---------------------------------------------------------------- FFT-sampled coefficients
 
 // The reference's FFT alternative (include/stablercwa/fourier.hpp:26-83): the profile is sampled at
@@ -511,12 +474,7 @@ inline zc* fft_coefficients_dev(cudaStream_t st, DeviceScratch& mem, const std::
 // value with the FFT method is the reference's numerical failure (rcwa1d.hpp:392-397): *fail is set.
 inline zc* layer_coefficients(cudaStream_t st, DeviceScratch& mem, const std::vector<double>& edges,
                               const std::vector<cd>& values, double period, int M, int method, int samples, int* fail) {
-    if (method != 1) {
-        zc* d = mem.get<zc>(4 * M + 1);
-        const std::vector<cd> c = fourier_coefficients(edges, values, period, 2 * M);
-        RCWA_CUDA(cudaMemcpyAsync(d, c.data(), c.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
-        return d;
-    }
+    if (method != 1) return closed_form_coefficients(st, mem, edges, values, period, 2 * M);
     for (const cd& v : values)
         if (!std::isfinite(v.real()) || !std::isfinite(v.imag())) {
             zc* d = mem.zeros<zc>(4 * M + 1);
@@ -550,84 +508,102 @@ inline bool hermitian_path_enabled(const Options& opt) {
     return opt.eps == 2.220446049250313e-16 && opt.max_iter == 30;
 }
 
-// c[h + 2M], h = -2M..2M, on the device: true when c_{-h} = conj(c_h) to 8 eps max|c|, and then c is made
-// exactly Hermitian (the average of the two, imaginary part of c_0 dropped).
-inline bool make_hermitian_coefficients(cudaStream_t st, zc* c, int M) {
-    const int K = 4 * M + 1;
-    std::vector<zc> h(K);
-    RCWA_CUDA(cudaMemcpyAsync(h.data(), c, K * sizeof(zc), cudaMemcpyDeviceToHost, st));
-    RCWA_CUDA(cudaStreamSynchronize(st));
-    double big = 0.0;
-    for (const zc& z : h) {
-        if (!std::isfinite(z.re) || !std::isfinite(z.im)) return false;
-        big = std::max(big, std::hypot(z.re, z.im));
+// True when a grating layer's operators are Hermitian: every segment value (eps, or 1/eps) real, finite and
+// nonzero, with a spread of magnitudes below 1e10 so that the Toeplitz matrix of 1/eps stays numerically
+// positive definite (its eigenvalues lie between the smallest and largest value; the Cholesky factorisation
+// keeps its pivots positive while that ratio is far above n eps). A decision on the inputs alone, taken
+// on the host without reading anything back from the device.
+inline bool real_profile(const std::vector<std::complex<double>>& values) {
+    double lo = INFINITY, hi = 0.0;
+    for (const std::complex<double>& v : values) {
+        if (v.imag() != 0.0 || !std::isfinite(v.real()) || v.real() == 0.0) return false;
+        lo = std::min(lo, std::fabs(v.real()));
+        hi = std::max(hi, std::fabs(v.real()));
     }
-    const double tol = 8.0 * 2.220446049250313e-16 * big;
-    if (std::fabs(h[2 * M].im) > tol) return false;
-    for (int k = 1; k <= 2 * M; ++k) {
-        const zc a = h[2 * M + k], b = h[2 * M - k];
-        if (std::hypot(a.re - b.re, a.im + b.im) > tol) return false;
-    }
-    h[2 * M].im = 0.0;
-    for (int k = 1; k <= 2 * M; ++k) {
-        const zc a = h[2 * M + k], b = h[2 * M - k];
-        const zc avg{0.5 * (a.re + b.re), 0.5 * (a.im - b.im)};
-        h[2 * M + k] = avg;
-        h[2 * M - k] = zc{avg.re, -avg.im};
-    }
-    RCWA_CUDA(cudaMemcpyAsync(c, h.data(), K * sizeof(zc), cudaMemcpyHostToDevice, st));
-    RCWA_CUDA(cudaStreamSynchronize(st));
-    return true;
+    return !values.empty() && hi <= 1e10 * lo;
 }
 
-// Cholesky factor T = L L^H of the Hermitian Toeplitz matrix of the device coefficients c (host arithmetic,
-// once per layer), then Linv = L^{-1} and LinvH = L^{-H} on the device (column-major n x n). False when T
-// is not positive definite.
-inline bool toeplitz_cholesky_inverse(cudaStream_t st, const zc* c, int M, DeviceScratch& mem, zc*& Lfac, zc*& Linv,
-                                      zc*& LinvH) {
-    const int n = 2 * M + 1, K = 4 * M + 1;
-    std::vector<zc> h(K);
-    RCWA_CUDA(cudaMemcpyAsync(h.data(), c, K * sizeof(zc), cudaMemcpyDeviceToHost, st));
-    RCWA_CUDA(cudaStreamSynchronize(st));
-    std::vector<cd> L((size_t)n * n, cd{0.0, 0.0});  // column-major, lower triangle
-    const auto T = [&](int i, int j) { const zc z = h[i - j + 2 * M]; return cd{z.re, z.im}; };
-    for (int j = 0; j < n; ++j) {
-        double dj = T(j, j).real();
-        for (int k = 0; k < j; ++k) dj -= std::norm(L[(size_t)k * n + j]);
-        if (!(dj > 0.0) || !std::isfinite(dj)) return false;
-        const double ljj = std::sqrt(dj);
-        L[(size_t)j * n + j] = ljj;
-        for (int i = j + 1; i < n; ++i) {
-            cd s = T(i, j);
-            for (int k = 0; k < j; ++k) s -= L[(size_t)k * n + i] * std::conj(L[(size_t)k * n + j]);
-            L[(size_t)j * n + i] = s / ljj;
-        }
+// Coefficients of a real profile made exactly conjugate-symmetric on the device (the closed form already is;
+// the FFT-sampled form is to rounding).
+inline void make_hermitian_coefficients(cudaStream_t st, zc* c, int M) {
+    LAUNCH(hermitian_coeff_kernel, nblocks(2 * M + 1), kTpb, st, 2 * M, c);
+}
+
+// Cholesky factor T = L L^H of the Hermitian Toeplitz matrix T(i, j) = c[i - j + 2M] (n = 2M + 1), one CTA,
+// right-looking: at step j the pivot is the updated T(j, j), column j below it is divided by its square
+// root and the trailing lower triangle takes the rank-one update. L is column-major, zero above the
+// diagonal, held in global memory (the CTA's barriers order it). A pivot that is not positive and finite
+// sets *fail and leaves L incomplete.
+__global__ void __launch_bounds__(1024) toeplitz_cholesky_kernel(int M, const zc* __restrict__ c, zc* __restrict__ L,
+                                                                 int* __restrict__ fail) {
+    const int n = 2 * M + 1, tid = threadIdx.x, nt = blockDim.x;
+    __shared__ double s_piv;
+    __shared__ int s_bad;
+    for (long long idx = tid; idx < (long long)n * n; idx += nt) {
+        const int j = (int)(idx / n), i = (int)(idx - (long long)j * n);
+        L[idx] = i >= j ? c[i - j + 2 * M] : zc{0.0, 0.0};
     }
-    std::vector<cd> X((size_t)n * n, cd{0.0, 0.0});  // X = L^{-1}, lower triangular, column by column
+    __syncthreads();
     for (int j = 0; j < n; ++j) {
-        X[(size_t)j * n + j] = 1.0 / L[(size_t)j * n + j];
-        for (int i = j + 1; i < n; ++i) {
-            cd s{0.0, 0.0};
-            for (int k = j; k < i; ++k) s += L[(size_t)k * n + i] * X[(size_t)j * n + k];
-            X[(size_t)j * n + i] = -s / L[(size_t)i * n + i];
+        zc* colj = L + (long long)j * n;
+        if (tid == 0) {
+            const double d = colj[j].re;
+            const int bad = !(d > 0.0) || !isfinite(d);
+            s_bad = bad;
+            s_piv = bad ? 1.0 : sqrt(d);
+            if (bad) atomicOr(fail, 1);
         }
+        __syncthreads();
+        if (s_bad) return;  // uniform: every thread read the same flag after the barrier
+        const double piv = s_piv, rpiv = 1.0 / piv;
+        for (int i = j + tid; i < n; i += nt) colj[i] = i == j ? zc{piv, 0.0} : colj[i] * rpiv;
+        __syncthreads();
+        const int m = n - j - 1;
+        for (long long idx = tid; idx < (long long)m * m; idx += nt) {
+            const int kk = (int)(idx / m), ii = (int)(idx - (long long)kk * m);
+            if (ii < kk) continue;
+            const int k = j + 1 + kk, i = j + 1 + ii;
+            L[(long long)k * n + i] = zfms(colj[i], conj(colj[k]), L[(long long)k * n + i]);
+        }
+        __syncthreads();
     }
-    std::vector<zc> lf((size_t)n * n), xi((size_t)n * n), xh((size_t)n * n);
-    for (int j = 0; j < n; ++j)
-        for (int i = 0; i < n; ++i) {
-            const cd v = X[(size_t)j * n + i], l = L[(size_t)j * n + i];
-            lf[(size_t)j * n + i] = zc{l.real(), l.imag()};
-            xi[(size_t)j * n + i] = zc{v.real(), v.imag()};
-            xh[(size_t)i * n + j] = zc{v.real(), -v.imag()};
+}
+
+// X = L^{-1} of a lower-triangular L with a real positive diagonal (column-major), one warp per column of X:
+// forward substitution down the column, each row's dot product split over the lanes. XH = X^H as well.
+__global__ void lower_inverse_kernel(int n, const zc* __restrict__ L, zc* __restrict__ X, zc* __restrict__ XH) {
+    const long long j = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (j >= n) return;
+    const int lane = threadIdx.x & 31;
+    zc* x = X + j * n;
+    for (int i = lane; i < n; i += 32) x[i] = zc{0.0, 0.0};
+    __syncwarp();
+    if (lane == 0) x[j] = zc{1.0 / L[j * n + j].re, 0.0};
+    __syncwarp();
+    for (int i = (int)j + 1; i < n; ++i) {
+        zc s{0.0, 0.0};
+        for (int k = (int)j + lane; k < i; k += 32) s = zfma(L[(long long)k * n + i], x[k], s);
+        for (int o = 16; o > 0; o >>= 1) {
+            s.re += __shfl_xor_sync(0xffffffffu, s.re, o);
+            s.im += __shfl_xor_sync(0xffffffffu, s.im, o);
         }
+        if (lane == 0) x[i] = s * (-1.0 / L[(long long)i * n + i].re);
+        __syncwarp();
+    }
+    for (int i = lane; i < n; i += 32) XH[(long long)i * n + j] = conj(x[i]);
+}
+
+// L, L^{-1} and L^{-H} of [[1/eps]] = L L^H for a layer's device coefficients c, all on the device and
+// stream-ordered (nothing read back). A failed factorisation sets *fail (the layer's samples then fail);
+// real_profile keeps it from happening for the profiles this is called with.
+inline void toeplitz_cholesky_inverse(cudaStream_t st, const zc* c, int M, DeviceScratch& mem, int* fail, zc*& Lfac,
+                                      zc*& Linv, zc*& LinvH) {
+    const int n = 2 * M + 1;
     Lfac = mem.get<zc>((size_t)n * n);
     Linv = mem.get<zc>((size_t)n * n);
     LinvH = mem.get<zc>((size_t)n * n);
-    RCWA_CUDA(cudaMemcpyAsync(Lfac, lf.data(), lf.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
-    RCWA_CUDA(cudaMemcpyAsync(Linv, xi.data(), xi.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
-    RCWA_CUDA(cudaMemcpyAsync(LinvH, xh.data(), xh.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
-    RCWA_CUDA(cudaStreamSynchronize(st));
-    return true;
+    LAUNCH(toeplitz_cholesky_kernel, 1, 1024, st, M, c, Lfac, fail);
+    LAUNCH(lower_inverse_kernel, warp_blocks(n), 128, st, n, Lfac, Linv, LinvH);
 }
 
 // The four constant parts of a Hermitian-definite pencil layer (E Hermitian, [[1/eps]] = L L^H):
