@@ -36,9 +36,14 @@ def build_oracle(force=False):
     return LIB
 
 
-def build_reference(reference="/root/reference", force=False):
+def reference_root():
+    """The StableRCWA checkout: $STABLERCWA_REFERENCE, else /root/reference."""
+    return os.environ.get("STABLERCWA_REFERENCE", "/root/reference")
+
+
+def build_reference(reference=None, force=False):
     """Compile the reference's own solve in place (ref_solve1d.cpp includes its headers)."""
-    inc = os.path.join(reference, "include")
+    inc = os.path.join(reference or reference_root(), "include")
     if not os.path.isdir(inc):
         return None
     os.makedirs(REF_OUT, exist_ok=True)

@@ -14,8 +14,11 @@
 
 #include <cstdio>
 #include <cstdlib>
+#include <fstream>
 #include <random>
+#include <stdexcept>
 #include <string>
+#include <thread>
 
 namespace {
 
@@ -488,14 +491,92 @@ void export_generated(std::FILE* f, const Case& c) {
     std::fprintf(f, "}\n");
 }
 
+// ---- cases described in a text file (the seeded benchmark structures, written by make_golden.py):
+//   case <name> <wavelength> <theta> <phi> <M1> <M2> <Es re> <Es im> <Ep re> <Ep im> <laurent>
+//   stack <nI> <nII re> <nII im> <Lx> <Ly>
+//   uniform <d> <n re> <n im>
+//   patterned <d> <K> <y_0> ... <y_K>        followed by K lines
+//   profile <S> <x_0> ... <x_S> <n_0 re> <n_0 im> ... <n_{S-1} re> <n_{S-1} im>
+//   end
+std::vector<Case> read_cases(const char* path) {
+    std::vector<Case> out;
+    std::ifstream in(path);
+    std::string word;
+    auto num = [&] { std::string t; in >> t; return std::strtod(t.c_str(), nullptr); };
+    while (in >> word) {
+        if (word != "case") throw std::runtime_error("case expected");
+        Case c;
+        c.source = "benchmark";
+        in >> c.name;
+        c.wavelength = num(); c.theta = num(); c.phi = num();
+        in >> c.M1 >> c.M2;
+        const double a = num(), b = num(), d = num(), e = num();
+        c.jones = {cplx{a, b}, cplx{d, e}};
+        int laurent = 0;
+        in >> laurent;
+        c.laurent = laurent != 0;
+        in >> word;
+        c.stack.nI = num();
+        const double r = num(), i = num();
+        c.stack.nII = cplx{r, i};
+        c.stack.Lx = num(); c.stack.Ly = num();
+        while (in >> word && word != "end") {
+            if (word == "uniform") {
+                const double th = num(), nr = num(), ni = num();
+                c.stack.layers.push_back(rcwa::Layer2D::uniform(th, cplx{nr, ni}));
+            } else {
+                const double th = num();
+                int K = 0;
+                in >> K;
+                std::vector<double> ye(K + 1);
+                for (double& y : ye) y = num();
+                std::vector<rcwa::XProfile2D> rows;
+                for (int k = 0; k < K; ++k) {
+                    in >> word;
+                    int S = 0;
+                    in >> S;
+                    std::vector<double> xe(S + 1);
+                    for (double& x : xe) x = num();
+                    std::vector<cplx> nv(S);
+                    for (cplx& v : nv) { const double vr = num(), vi = num(); v = cplx{vr, vi}; }
+                    rows.push_back(rcwa::XProfile2D{xe, nv});
+                }
+                c.stack.layers.push_back(rcwa::Layer2D::patterned(th, ye, rows));
+            }
+        }
+        out.push_back(c);
+    }
+    return out;
+}
+
+// every case solved by the reference on its own thread (solve2d is reentrant), written in input order
+void export_listed(std::FILE* f, const std::vector<Case>& cases) {
+    std::vector<rcwa::Result2D> res(cases.size());
+    std::vector<std::thread> th;
+    for (std::size_t k = 0; k < cases.size(); ++k) th.emplace_back([&, k] { res[k] = run(cases[k]); });
+    for (std::thread& t : th) t.join();
+    for (std::size_t k = 0; k < cases.size(); ++k) {
+        put_head(f, cases[k]);
+        std::fprintf(f, "\"operators\":[],");
+        put_rayleigh(f, cases[k].stack, res[k]);
+        std::fputc(',', f);
+        put_result(f, res[k], false);
+        std::fprintf(f, "}\n");
+    }
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
     std::FILE* f = argc > 1 ? std::fopen(argv[1], "w") : stdout;
     if (!f) return 2;
-    for (int i = 0; i < kRcwa2dRefCaseCount; ++i) export_reference_case(f, kRcwa2dRefCases[i]);
-    for (int i = 0; i < kCoreRefCaseCount; ++i) export_core_case(f, kCoreRefCases[i]);
-    for (const Case& c : generated_cases()) export_generated(f, c);
+    if (argc > 3 && std::string(argv[2]) == "--cases") {
+        export_listed(f, read_cases(argv[3]));
+    } else {
+        for (int i = 0; i < kRcwa2dRefCaseCount; ++i) export_reference_case(f, kRcwa2dRefCases[i]);
+        for (int i = 0; i < kCoreRefCaseCount; ++i) export_core_case(f, kCoreRefCases[i]);
+        for (const Case& c : generated_cases()) export_generated(f, c);
+    }
     if (f != stdout) std::fclose(f);
     return 0;
 }
