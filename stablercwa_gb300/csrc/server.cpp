@@ -279,7 +279,8 @@ struct rcwa_gpu_server {
     std::vector<rcwa_gpu_ctx*> ctxs;
     std::vector<std::thread> workers;
     std::mutex m;
-    std::condition_variable cv_work, cv_done;
+    std::condition_variable cv_work, cv_done, cv_idle;
+    int waiters = 0;  // threads inside rcwa_gpu_server_wait (destroy lets them leave before freeing)
     std::map<int, std::deque<Job*>> buckets;
     std::map<unsigned long long, std::unique_ptr<Job>> jobs;
     double budget = 0, in_use = 0;
@@ -396,12 +397,24 @@ int rcwa_gpu_server_create(const rcwa_server_config* config, rcwa_gpu_server** o
 void rcwa_gpu_server_destroy(rcwa_gpu_server* s) {
     if (!s) return;
     {
+        // requests still queued are cancelled: their waiters wake with RCWA_ECANCELLED
         std::lock_guard<std::mutex> lk(s->m);
         s->stop = true;
-        for (auto& kv : s->buckets) kv.second.clear();
+        for (auto& kv : s->buckets)
+            for (Job* j : kv.second) {
+                j->code = RCWA_ECANCELLED;
+                j->done = true;
+            }
+        s->buckets.clear();
     }
     s->cv_work.notify_all();
-    for (std::thread& t : s->workers) t.join();
+    s->cv_done.notify_all();
+    for (std::thread& t : s->workers) t.join();  // requests already running finish and wake their waiters
+    {
+        std::unique_lock<std::mutex> lk(s->m);
+        s->cv_done.notify_all();
+        s->cv_idle.wait(lk, [&] { return s->waiters == 0; });
+    }
     for (rcwa_gpu_ctx* c : s->ctxs) rcwa_gpu_destroy(c);
     delete s;
 }
@@ -435,6 +448,7 @@ int rcwa_gpu_server_submit(rcwa_gpu_server* s, const rcwa_request* r, unsigned l
     j->footprint = footprint_of(*j);
     {
         std::lock_guard<std::mutex> lk(s->m);
+        if (s->stop) return RCWA_ECANCELLED;
         j->ticket = s->next_ticket++;
         j->submitted = Clock::now();
         j->submit_s = s->now_s();
@@ -454,13 +468,14 @@ int rcwa_gpu_server_wait(rcwa_gpu_server* s, unsigned long long ticket, int time
         auto it = s->jobs.find(ticket);
         if (it == s->jobs.end()) return RCWA_EINVAL;
         Job* p = it->second.get();
-        if (timeout_ms < 0) {
-            s->cv_done.wait(lk, [&] { return p->done; });
-        } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return p->done; })) {
-            return RCWA_ETIMEOUT;
-        }
-        j = std::move(it->second);
-        s->jobs.erase(it);
+        ++s->waiters;
+        bool finished = true;
+        if (timeout_ms < 0) s->cv_done.wait(lk, [&] { return p->done; });
+        else finished = s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return p->done; });
+        if (--s->waiters == 0 && s->stop) s->cv_idle.notify_all();
+        if (!finished) return RCWA_ETIMEOUT;
+        j = std::move(s->jobs[ticket]);
+        s->jobs.erase(ticket);
     }
     if (resp) *resp = rcwa_response{j->code, j->slot, j->submit_s, j->start_s, j->finish_s, j->footprint};
     if (result) {
@@ -468,7 +483,7 @@ int rcwa_gpu_server_wait(rcwa_gpu_server* s, unsigned long long ticket, int time
         else if (j->req.kind == RCWA_REQ_CONICAL) j->rc.out(static_cast<rcwa_result_conical*>(result));
         else j->r2.out(static_cast<rcwa_result2d*>(result));
     }
-    return RCWA_OK;
+    return j->code == RCWA_ECANCELLED ? RCWA_ECANCELLED : RCWA_OK;
 }
 
 }  // extern "C"

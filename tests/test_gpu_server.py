@@ -104,3 +104,94 @@ def test_wait_timeout(cases2d):
         assert np.max(np.abs(r["DEr"] - np.array([float(x) for x in c["ref"]["DEr"]]))) <= 1e-10
     finally:
         srv.close()
+
+
+def _pillars(cases2d):
+    return next(c for c in cases2d if c["name"] == "pillars_films_m6")
+
+
+def _submit_pillars(srv, c, dl=0.0):
+    return srv.submit_2d(stack2d_from_json(c["stack"]), c["wavelength"] + dl, c["theta"], c["phi"], c["M1"], c["M2"],
+                         (complex(*c["jones"][0]), complex(*c["jones"][1])))
+
+
+def _footprints(cases1d, cases2d):
+    """The admission charge of one large (2-D, N = 169) and one small (1-D) request."""
+    from stablercwa_gb300.engine import Server
+    srv = Server(slots=1)
+    try:
+        big = srv.wait(_submit_pillars(srv, _pillars(cases2d)))[0]["footprint_bytes"]
+        c = cases1d[0]
+        small = srv.wait(srv.submit_1d(stack_from_json(c["stack"]), c["wavelength"], c["theta"], c["M"]))[0]
+    finally:
+        srv.close()
+    return big, small["footprint_bytes"]
+
+
+def test_admission_budget_and_bypass(cases1d, cases2d):
+    """A budget that holds one large request and a few small ones: the second large request waits for
+    the first to finish, and small requests submitted behind it start inside the bypass window."""
+    from stablercwa_gb300.engine import Server
+    big, small = _footprints(cases1d, cases2d)
+    assert big > 8 * small
+    c1 = cases1d[0]
+    stack1 = stack_from_json(c1["stack"])
+    srv = Server(slots=4, hbm_budget=int(big + 4 * small), max_bypass_ms=60000)
+    try:
+        a = _submit_pillars(srv, _pillars(cases2d))
+        b = _submit_pillars(srv, _pillars(cases2d), 0.01)
+        smalls = [srv.submit_1d(stack1, c1["wavelength"] + 0.01 * k, c1["theta"], c1["M"]) for k in range(3)]
+        ia, ib = srv.wait(a)[0], srv.wait(b)[0]
+        iss = [srv.wait(t)[0] for t in smalls]
+    finally:
+        srv.close()
+    assert ia["code"] == ib["code"] == 0 and all(i["code"] == 0 for i in iss)
+    assert ib["start_s"] >= ia["finish_s"]            # never both large requests at once
+    assert all(i["start_s"] < ib["start_s"] for i in iss)  # the small ones bypassed the waiting large one
+
+
+def test_admission_no_bypass_after_window(cases1d, cases2d):
+    """With a bypass window of 1 ms, small requests queued behind a waiting large one keep their order."""
+    import time
+    from stablercwa_gb300.engine import Server
+    big, small = _footprints(cases1d, cases2d)
+    c1 = cases1d[0]
+    stack1 = stack_from_json(c1["stack"])
+    srv = Server(slots=4, hbm_budget=int(big + 4 * small), max_bypass_ms=1)
+    try:
+        a = _submit_pillars(srv, _pillars(cases2d))
+        b = _submit_pillars(srv, _pillars(cases2d), 0.01)
+        time.sleep(0.02)  # b has waited longer than the bypass window
+        smalls = [srv.submit_1d(stack1, c1["wavelength"] + 0.01 * k, c1["theta"], c1["M"]) for k in range(3)]
+        ia, ib = srv.wait(a)[0], srv.wait(b)[0]
+        iss = [srv.wait(t)[0] for t in smalls]
+    finally:
+        srv.close()
+    if ib["submit_s"] + 0.001 >= ia["finish_s"]:
+        pytest.skip("the first request finished before the window closed")
+    assert all(i["start_s"] >= ib["start_s"] for i in iss)
+
+
+def test_destroy_wakes_waiters(cases2d):
+    """Destroying the server while a thread waits (without a timeout) on a queued request wakes that
+    thread with RCWA_ECANCELLED (or the result, if the request got to run) instead of leaving it blocked."""
+    import threading
+    import time
+    from stablercwa_gb300 import abi
+    from stablercwa_gb300.engine import Server
+    c = _pillars(cases2d)
+    srv = Server(slots=1)
+    tickets = [_submit_pillars(srv, c, 0.01 * k) for k in range(4)]
+    got = {}
+
+    def waiter():
+        got["r"] = srv.wait(tickets[-1])
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    time.sleep(0.5)  # the waiter is inside rcwa_gpu_server_wait before destroy begins
+    srv.close()
+    th.join(timeout=120)
+    assert not th.is_alive()
+    info, _ = got["r"]
+    assert info["code"] in (0, abi.RCWA_ECANCELLED)
