@@ -9,11 +9,16 @@
 // in the file-scope array below, the caller passes device inputs and outputs, and the call
 // allocates nothing.
 //
-// Set-up is once per device: the first call made with a device current looks up the array's
-// address with cudaGetSymbolAddress and loads the kernel variants. Make that first call before
-// any stream capture begins on the device. Every call uses the same array, so calls that overlap in
-// time on one device (issued on different streams, or from several host threads without ordering)
-// race on it; calls on one stream are ordered and safe.
+// Set-up is once per device context: the first call made with a device current looks up the array's
+// address with cudaGetSymbolAddress and loads the kernel variants. Make that first call before any
+// stream capture begins on the device. The address is cached together with the id of the CUDA context
+// it belongs to; a call under another context (after cudaDeviceReset, or with a context of the
+// caller's own) repeats the set-up instead of using a stale address. Every call uses the same array,
+// so calls that overlap in time on one device (issued on different streams, or from several host
+// threads without ordering) race on it; calls on one stream are ordered and safe. The lanes per
+// matrix are chosen exactly as rcwa_gpu_eig_batch_dev chooses them (RCWA_GB300_EIG_GROUP included),
+// so both entry points run the same kernel on the same inputs.
+#include <cstdlib>
 #include <mutex>
 
 #include "eig.cuh"
@@ -32,7 +37,11 @@ static __device__ __align__(256) unsigned char eig_static_scratch[kScratchBytes]
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_lock;
-zc* g_scratch[kMaxDevices] = {};
+struct DeviceSetup {
+    unsigned long long ctx_id = 0;
+    zc* scratch = nullptr;
+};
+DeviceSetup g_setup[kMaxDevices];
 
 template <int G>
 cudaError_t load_kernel() {
@@ -41,21 +50,49 @@ cudaError_t load_kernel() {
     else return cudaFuncGetAttributes(&attr, rcwa_gb300::eig_batch_kernel<G>);
 }
 
-// Address of this device's copy of the array; looked up on the device's first call.
-int scratch_for_current_device(zc** out) {
+// Id of the calling thread's current CUDA context, through the driver's own entry points (resolved by
+// the runtime, so the library needs no link-time driver dependency); 0 when none is current.
+unsigned long long current_context_id() {
+    using GetCurrent = int (*)(void**);
+    using GetId = int (*)(void*, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(f);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+    });
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
+// Address of the array in the current device context; set up on the context's first call.
+int scratch_for_current_context(zc** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return RCWA_ECUDA;
     if (dev < 0 || dev >= kMaxDevices) return RCWA_EUNSUPPORTED;
     std::lock_guard<std::mutex> guard(g_setup_lock);
-    if (!g_scratch[dev]) {
+    DeviceSetup& d = g_setup[dev];
+    const unsigned long long id = current_context_id();
+    if (!d.scratch || id == 0 || id != d.ctx_id) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, eig_static_scratch) != cudaSuccess || !p) return RCWA_ECUDA;
         if (load_kernel<4>() != cudaSuccess || load_kernel<8>() != cudaSuccess || load_kernel<16>() != cudaSuccess ||
-            load_kernel<32>() != cudaSuccess || load_kernel<128>() != cudaSuccess || load_kernel<256>() != cudaSuccess)
+            load_kernel<32>() != cudaSuccess || load_kernel<64>() != cudaSuccess || load_kernel<128>() != cudaSuccess ||
+            load_kernel<256>() != cudaSuccess)
             return RCWA_ECUDA;
-        g_scratch[dev] = static_cast<zc*>(p);
+        d.scratch = static_cast<zc*>(p);
+        d.ctx_id = current_context_id();  // the symbol lookup made the device's context current
     }
-    *out = g_scratch[dev];
+    *out = d.scratch;
     return RCWA_OK;
 }
 
@@ -72,25 +109,17 @@ extern "C" int rcwa_gpu_eig_batch_static(void* stream, int n, int batch, const r
     if (per_matrix > kScratchBytes || (unsigned long long)batch > kScratchBytes / per_matrix) return RCWA_ESCRATCH;
 
     zc* ws = nullptr;
-    const int rc = scratch_for_current_device(&ws);
+    const int rc = scratch_for_current_context(&ws);
     if (rc != RCWA_OK) return rc;
 
-    const cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int group = eig_default_group(n, batch);
-    const int tpb = 128;
-    const unsigned blocks = (unsigned)(((long long)batch * group + tpb - 1) / tpb);
-    const zc* a = reinterpret_cast<const zc*>(d_a);
-    zc* w = reinterpret_cast<zc*>(d_values);
-    zc* v = reinterpret_cast<zc*>(d_vectors);
-    const long long a_stride = (long long)n * n;
-    switch (group) {
-        case 4: eig_batch_kernel<4><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, d_info, d_sweeps, ws, eps, max_iter, nullptr, 1, nullptr); break;
-        case 8: eig_batch_kernel<8><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, d_info, d_sweeps, ws, eps, max_iter, nullptr, 1, nullptr); break;
-        case 16: eig_batch_kernel<16><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, d_info, d_sweeps, ws, eps, max_iter, nullptr, 1, nullptr); break;
-        case 128: eig_block_kernel<128><<<(unsigned)batch, 128, 0, st>>>(n, batch, a, a_stride, w, v, d_info, d_sweeps, ws, eps, max_iter, nullptr, 1, nullptr); break;
-        case 256: eig_block_kernel<256><<<(unsigned)batch, 256, 0, st>>>(n, batch, a, a_stride, w, v, d_info, d_sweeps, ws, eps, max_iter, nullptr, 1, nullptr); break;
-        default: eig_batch_kernel<32><<<blocks, tpb, 0, st>>>(n, batch, a, a_stride, w, v, d_info, d_sweeps, ws, eps, max_iter, nullptr, 1, nullptr); break;
+    int group = 0;
+    if (const char* g = std::getenv("RCWA_GB300_EIG_GROUP")) group = std::atoi(g);
+    try {
+        launch_eig(static_cast<cudaStream_t>(stream), n, batch, reinterpret_cast<const zc*>(d_a), (long long)n * n,
+                   reinterpret_cast<zc*>(d_values), reinterpret_cast<zc*>(d_vectors), d_info, d_sweeps, ws, eps,
+                   max_iter, group);
+    } catch (const EngineError& e) {
+        return e.code;
     }
-    ++launch_count();
-    return cudaGetLastError() == cudaSuccess ? RCWA_OK : RCWA_ECUDA;
+    return RCWA_OK;
 }

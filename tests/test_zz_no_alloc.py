@@ -1,7 +1,9 @@
 """rcwa_gpu_eig_batch_static, the eigensolver entry point that allocates nothing, against
 rcwa_gpu_eig_batch_dev on the same device inputs: two calls in a row (different sizes, the second
-close to the fixed workspace's limit), the oversize rejection, and no change in free device memory
-across a call once the device is set up. Named to be collected last; it also passes alone."""
+close to the fixed workspace's limit), every lane-group form the fixed workspace can reach, the
+RCWA_GB300_EIG_GROUP override honoured by both entry points alike, the oversize rejection, and no
+change in free device memory across a call once the device is set up. Named to be collected last; it
+also passes alone."""
 import ctypes as C
 
 import numpy as np
@@ -138,3 +140,54 @@ def test_static_rejects_oversize(env):
     assert workspace_bytes(n_big) > SCRATCH_BYTES
     rc = f(torch.cuda.current_stream().cuda_stream, n_big, 1, p, float(np.finfo(np.float64).eps), 30, p, p, p, None)
     assert rc == RCWA_ESCRATCH
+
+
+def default_group(n, batch):
+    """The lanes per matrix both entry points choose (eig_default_group in csrc/eig.cu)."""
+    lanes_wanted = 152 * 4 * 32 * 2
+    for g in (4, 8, 16):
+        if batch * g >= lanes_wanted and n >= 4 * g:
+            return g
+    if batch * 16 >= lanes_wanted:
+        return 16
+    if n < 64:
+        return 32
+    if n >= 384:
+        if batch <= 152:
+            return 256
+        return 128 if batch * 32 < 2 * lanes_wanted else 32
+    return 32 if batch * 32 * 4 >= lanes_wanted else 128
+
+
+# one case per kernel form the 64 MiB workspace can hold (groups 4 and 8 need more matrices than fit):
+# lane groups of 16 and 32, a CTA of 128 and of 256 threads per matrix, and one cluster per matrix (-1),
+# which a few matrices of order >= 384 take by default
+GROUP_CASES = [(8, 4096, 16, None), (40, 64, 32, None), (121, 94, 128, None), (400, 4, 256, "256"),
+               (400, 4, -1, None)]
+
+
+@pytest.mark.parametrize("n,batch,group,forced", GROUP_CASES)
+def test_static_matches_existing_per_group(env, monkeypatch, n, batch, group, forced):
+    torch, eng, f = env
+    if forced:
+        monkeypatch.setenv("RCWA_GB300_EIG_GROUP", forced)  # both entry points read it at call time
+    elif group > 0:
+        assert default_group(n, batch) == group
+    assert batch * workspace_bytes(n) <= SCRATCH_BYTES
+    a, d_a = device_problem(torch, n, batch, 10 + group)
+    ref = run_existing(torch, eng, n, batch, d_a)
+    out = outputs(torch, n, batch)
+    assert run_static(torch, f, n, batch, d_a, out) == RCWA_OK
+    check_same(a, [t.cpu().numpy() for t in out], ref)
+
+
+def test_static_honours_group_override(env, monkeypatch):
+    torch, eng, f = env
+    n, batch = 121, 20
+    assert default_group(n, batch) == 128
+    monkeypatch.setenv("RCWA_GB300_EIG_GROUP", "32")  # both entry points read it at call time
+    a, d_a = device_problem(torch, n, batch, 7)
+    ref = run_existing(torch, eng, n, batch, d_a)
+    out = outputs(torch, n, batch)
+    assert run_static(torch, f, n, batch, d_a, out) == RCWA_OK
+    check_same(a, [t.cpu().numpy() for t in out], ref)
