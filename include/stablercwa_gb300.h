@@ -39,6 +39,7 @@ extern "C" {
 #define RCWA_ESCRATCH (-5)     /* problem larger than rcwa_gpu_eig_batch_static's fixed workspace */
 #define RCWA_ETIMEOUT (-6)     /* rcwa_gpu_server_wait: the request has not finished yet */
 #define RCWA_ENUMERIC (-7)     /* non-finite result where the reference throws std::runtime_error */
+#define RCWA_ECANCELLED (-8)   /* rcwa_gpu_server_wait: the server was destroyed before the request started */
 
 /* per-sample status word */
 #define RCWA_SAMPLE_OK 0
@@ -426,6 +427,27 @@ int rcwa_gpu_solve_batch(rcwa_gpu_ctx* ctx, int n, int nrhs, int batch, const rc
 int rcwa_gpu_multiply_batch(rcwa_gpu_ctx* ctx, int m, int k, int n, int batch, const rcwa_complex* a,
                             const rcwa_complex* b, rcwa_complex* c);
 
+/* Host-only argument checks of the three solves, the checks rcwa::solve, rcwa::solve_conical and
+ * rcwa::solve2d make before any work (include/stablercwa/rcwa1d.hpp:191-229, rcwa1d_conical.hpp:688-689,
+ * rcwa2d.hpp:1042-1070): RCWA_OK, or RCWA_EINVAL with the reference's std::invalid_argument message
+ * copied into message (size bytes, NUL-terminated). No device is needed; the batched solves make the
+ * same checks themselves. */
+int rcwa_validate_solve1d(const rcwa_stack1d* stack, const rcwa_point1d* points, int n_points, int M, int polarization,
+                          char* message, size_t size);
+int rcwa_validate_solve_conical(const rcwa_stack1d* stack, const rcwa_point_conical* points, int n_points, int M,
+                                char* message, size_t size);
+int rcwa_validate_solve2d(const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points, int M1, int M2,
+                          int factorization, char* message, size_t size);
+
+/* No reference counterpart: how the engine forms its complex products. Products whose three orders are
+ * all >= 32 run on the tensor cores (tcgen05, bf16 digit slices of each FP64 operand, exact FP32
+ * accumulation of the slice products, FP64 sums: accurate to about k 2^-53 of the largest entries of
+ * the row and column, like an FP64 GEMM) unless RCWA_GB300_GEMM=fp64 is set, in which case every product
+ * runs on the FP64 pipe. *tensor_cores: 1 when the tensor-core path is on; *slices: digits per operand
+ * (RCWA_GB300_TC_SLICES, default 7); *stuck: nonzero once a tensor-core product kernel gave up on a
+ * wait that never completed (its output was then not written). Any pointer may be NULL. */
+int rcwa_gpu_gemm_info(int* tensor_cores, int* slices, int* stuck);
+
 /* ---- Serving: a request loop over worker slots -------------------------------------------- */
 
 /* No reference counterpart: the reference serves one solve per call (rcwa_json.hpp:1287-1312,
@@ -473,12 +495,16 @@ typedef struct rcwa_response {
 
 typedef struct rcwa_gpu_server rcwa_gpu_server;
 int rcwa_gpu_server_create(const rcwa_server_config* config, rcwa_gpu_server** server);
+/* Stops the server: requests still queued are cancelled (their waiters return RCWA_ECANCELLED),
+ * requests already running finish, and the call returns once every thread blocked in
+ * rcwa_gpu_server_wait has left it. No call may use the server after destroy has begun. */
 void rcwa_gpu_server_destroy(rcwa_gpu_server* server);
 /* Validates the request's shape (the solve itself validates the physics) and queues it. */
 int rcwa_gpu_server_submit(rcwa_gpu_server* server, const rcwa_request* request, unsigned long long* ticket);
 /* Waits up to timeout_ms (< 0: forever) for the request, then copies its result into result (an
  * rcwa_result1d*, rcwa_result_conical* or rcwa_result2d* of host arrays sized for one point, by
- * kind; may be NULL) and releases it. Returns RCWA_OK, or RCWA_ETIMEOUT if it has not finished. */
+ * kind; may be NULL) and releases it. Returns RCWA_OK, RCWA_ETIMEOUT if it has not finished, or
+ * RCWA_ECANCELLED if the server was destroyed before the request started. */
 int rcwa_gpu_server_wait(rcwa_gpu_server* server, unsigned long long ticket, int timeout_ms, rcwa_response* response,
                          void* result);
 /* ---- JSON front end ------------------------------------------------------------------------- */

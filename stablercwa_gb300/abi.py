@@ -307,6 +307,7 @@ def result2d_views(n_points, N, n_layers):
 
 RCWA_ETIMEOUT = -6
 RCWA_ENUMERIC = -7
+RCWA_ECANCELLED = -8
 RCWA_SLICE_XZ, RCWA_SLICE_YZ = 0, 1
 RCWA_PHASE_ABSOLUTE, RCWA_PHASE_INCIDENT, RCWA_PHASE_CUSTOM = 0, 1, 2
 RCWA_UNWRAP_NONE, RCWA_UNWRAP_X, RCWA_UNWRAP_Z, RCWA_UNWRAP_BOTH = 0, 1, 2, 3

@@ -8,6 +8,7 @@
 #include <complex>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <exception>
 #include <mutex>
 #include <string>
@@ -724,6 +725,59 @@ int rcwa_gpu_solve_batch(rcwa_gpu_ctx* ctx, int n, int nrhs, int batch, const rc
         copy_back(singular, ds, batch, st);
         RCWA_CUDA(cudaStreamSynchronize(st));
     });
+}
+
+namespace {
+int validated(char* message, size_t size, const std::function<void()>& check) {
+    try {
+        check();
+        if (message && size) message[0] = '\0';
+        return RCWA_OK;
+    } catch (const EngineError& e) {
+        if (message && size) {
+            std::strncpy(message, e.message.c_str(), size - 1);
+            message[size - 1] = '\0';
+        }
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        return RCWA_ENOMEM;
+    }
+}
+}  // namespace
+
+int rcwa_validate_solve1d(const rcwa_stack1d* stack, const rcwa_point1d* points, int n_points, int M, int polarization,
+                          char* message, size_t size) {
+    return validated(message, size, [&] {
+        if (!stack || (n_points > 0 && !points) || n_points < 0) throw EngineError{RCWA_EINVAL, "rcwa: null argument"};
+        validate1d(*stack, points, n_points, M, polarization);
+    });
+}
+
+int rcwa_validate_solve_conical(const rcwa_stack1d* stack, const rcwa_point_conical* points, int n_points, int M,
+                                char* message, size_t size) {
+    return validated(message, size, [&] {
+        if (!stack || (n_points > 0 && !points) || n_points < 0) throw EngineError{RCWA_EINVAL, "rcwa: null argument"};
+        validate_conical(*stack, points, n_points, M);
+    });
+}
+
+int rcwa_validate_solve2d(const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points, int M1, int M2,
+                          int factorization, char* message, size_t size) {
+    return validated(message, size, [&] {
+        if (!stack || (n_points > 0 && !points) || n_points < 0) throw EngineError{RCWA_EINVAL, "rcwa2d: null argument"};
+        validate2d(*stack, points, n_points, M1, M2, factorization);
+    });
+}
+
+int rcwa_gpu_gemm_info(int* tensor_cores, int* slices, int* stuck) {
+    try {
+        if (tensor_cores) *tensor_cores = tc_gemm_enabled() ? 1 : 0;
+        if (slices) *slices = tc_gemm_slices();
+        if (stuck) *stuck = tc_gemm_error();
+        return RCWA_OK;
+    } catch (const EngineError& e) {
+        return e.code;
+    }
 }
 
 int rcwa_gpu_multiply_batch(rcwa_gpu_ctx* ctx, int m, int k, int n, int batch, const rcwa_complex* a,

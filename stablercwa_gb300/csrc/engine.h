@@ -80,6 +80,30 @@ void launch_lu_solve(cudaStream_t st, int n, int nrhs, int batch, const zc* a, l
 void launch_zgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride, const zc* B,
                   int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc, long long c_stride,
                   double s_ab, double s_c, const int* skip = nullptr, int skip_value = 1, int tri = 0);
+// One matrix per thread-block cluster (eig_cluster.cu) for a few large matrices: the same algorithm as
+// launch_eig's kernels, spread over 8 or 16 SMs. launch_eig takes it by itself (eig_cluster_wanted).
+bool eig_cluster_wanted(int n, int batch);
+void launch_eig_cluster(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info,
+                        int* sweeps, zc* ws, double eps, int max_iter, const int* skip, int skip_value, zc* t_out);
+// The same product on the tensor cores (gemm_tc.cu: Ozaki-split bf16 tcgen05 products, FP64-accurate);
+// launch_zgemm takes it for products of order >= 32 unless RCWA_GB300_GEMM=fp64. The triangular hint
+// does not apply (the full product is formed; zero entries contribute exact zeros).
+void launch_zgemm_tc(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride,
+                     const zc* B, int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc,
+                     long long c_stride, double s_ab, double s_c, const int* skip = nullptr, int skip_value = 1);
+bool tc_gemm_enabled();
+// Products launched by this host thread while a guard lives stay on the FP64 pipe (the 2-D solve: its
+// operands span many decades within a row or column, where an FP64 product's error, relative to the
+// terms it sums, is smaller than the slice products', relative to the row and column maxima).
+struct Fp64ProductsGuard {
+    Fp64ProductsGuard();
+    ~Fp64ProductsGuard();
+    Fp64ProductsGuard(const Fp64ProductsGuard&) = delete;
+    Fp64ProductsGuard& operator=(const Fp64ProductsGuard&) = delete;
+    static bool active();
+};
+int tc_gemm_slices();
+int tc_gemm_error();  // nonzero once a tensor-core product kernel gave up on a stuck wait (synchronous read)
 // C = A B with A complex, B real (C does not alias A or B)
 void launch_zdgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride,
                    const double* B, int ldb, long long b_stride, zc* C, int ldc, long long c_stride,

@@ -1,0 +1,581 @@
+// gemm_tc.cu -- batched complex FP64 GEMM on the tensor cores (tcgen05, sm_103a), accurate to FP64.
+//
+// C = s_ab A B + s_c C0 with A m x k, B k x n complex double, any batch. The product is emulated with
+// the Ozaki scheme (Ozaki, Ogita, Oishi and Rump, "Error-free transformations of matrix
+// multiplication by using fast routines of matrix multiplication", Numer. Algorithms 59, 2012) on
+// bf16 tensor-core products:
+//   * the complex product is one real product of twice the size: rows 2i and 2i+1 of A^ are
+//     [Re A(i,:), -Im A(i,:)] and [Im A(i,:), Re A(i,:)], and B^ = [Re B; Im B], so (A^ B^)(2i, j) and
+//     (A^ B^)(2i+1, j) are the real and imaginary parts of C(i, j);
+//   * every row of A^ is scaled by a power of two 2^ea(i) taken from its largest entry, every column of
+//     B^ by 2^eb(j), and each scaled entry y in (-1, 1) is split into S signed integer digits,
+//     y = 2^-7 (d_1 + 2^-8 d_2 + ... + 2^-8(S-1) d_S), |d_s| <= 128: each digit is exact in bf16;
+//   * the digit products d_s e_t are exact (<= 2^14) and a tensor-core sum of up to 1024 of them stays
+//     an integer below 2^24, exact in the FP32 accumulator. Digit pairs (s, t) with s + t <= S + 1 are
+//     kept (the dropped ones lie below 2^-8S of the product's scale); pairs of one diagonal s + t share
+//     a scale factor 2^(-14 - 8 (s + t - 2)), so up to 1024 / K of them accumulate in one exact FP32
+//     tensor-memory accumulator (a "group") before it is added into FP64.
+// Per element the result is exact up to the digit truncation (relative 2^-8S of max|A(i,:)| max|B(:,j)|
+// times k) and the FP64 additions of the group sums: FP64-level accuracy with S = 7.
+//
+// Kernels. The split kernels write the digit planes in HBM as bf16 rows with K contiguous (K-major for
+// both operands). The product kernel gives each CTA one 128 x 128 tile of C^ of one matrix: one warp
+// issues TMA loads (128-byte swizzle, boxes of 128 rows x 64 K) into a 4-stage shared-memory ring; one
+// thread issues tcgen05.mma (M = 128, N = 128, K = 16, bf16 in, FP32 out) into one of two 128-column
+// tensor-memory accumulators; eight warps read each finished group out of tensor memory (tcgen05.ld),
+// scale it and add it into FP64 registers while the next group accumulates in the other buffer, then
+// apply 2^(ea + eb), pair the real and imaginary rows and write C. Every mbarrier wait is bounded: on
+// expiry the kernel records an error, drains its own copies and products, frees its tensor memory and
+// returns without writing C.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "engine.h"
+
+namespace rcwa_gb300 {
+namespace {
+
+constexpr int kTileM = 128, kTileN = 128, kTileK = 64;  // K per stage: 64 bf16 = one 128-byte swizzle row
+constexpr int kStages = 4;
+constexpr int kStageBytes = (kTileM + kTileN) * kTileK * 2;  // 32 KB
+constexpr int kTmemCols = 256;                                // two accumulators of 128 columns
+constexpr int kThreads = 320;                                 // producer, MMA, 8 epilogue warps
+constexpr int kMaxGroups = 160;
+constexpr int kMaxSlices = 8;
+constexpr unsigned kWaitLimit = 1u << 22;  // try_wait rounds before a wait is declared stuck
+
+// One accumulation group: digit pairs (i, d - i) for i in [i0, i0 + ni), K blocks [kb0, kb0 + nkb).
+struct Plan {
+    int n_groups;
+    int S;
+    unsigned g[kMaxGroups];  // d | i0 << 4 | ni << 8 | kb0 << 12 | nkb << 22
+};
+__host__ __device__ inline int g_d(unsigned v) { return v & 15; }
+__host__ __device__ inline int g_i0(unsigned v) { return (v >> 4) & 15; }
+__host__ __device__ inline int g_ni(unsigned v) { return (v >> 8) & 15; }
+__host__ __device__ inline int g_kb0(unsigned v) { return (v >> 12) & 1023; }
+__host__ __device__ inline int g_nkb(unsigned v) { return (v >> 22) & 1023; }
+
+// ---------------------------------------------------------------- PTX wrappers
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for phase `parity` of bar: false when the CTA is aborting or the wait ran out (which
+// starts the abort and records it in *err).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, int* err) {
+    for (unsigned it = 0;; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 63u) == 63u && *abort_flag) return false;
+        if (it >= kWaitLimit) {
+            *abort_flag = 1;
+            atomicOr(err, 1);
+            return false;
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// shared-memory matrix descriptor of a K-major tile written by TMA with the 128-byte swizzle: rows of
+// 128 bytes, 8-row atoms 1024 bytes apart (stride byte offset), descriptor version 1 (bits 46-48)
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) |
+           ((uint64_t)2 << 61);
+}
+
+// instruction descriptor: D f32, A and B bf16, both K-major, N = 128, M = 128
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTileN >> 3) << 17) | ((uint32_t)(kTileM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// ---------------------------------------------------------------- digit split
+
+// exponent e with max = f 2^e, f in [0.5, 1); 0 for 0 or a non-finite max (the digits then carry it)
+__device__ __forceinline__ int scale_exponent(double mx) {
+    if (!(mx > 0.0) || !isfinite(mx)) return 0;
+    int e;
+    frexp(mx, &e);
+    return e;
+}
+
+// the S digits of y in (-1, 1): bf16 bit patterns of exact small integers
+__device__ __forceinline__ void store_digits(double y, int S, uint16_t* out, long long plane_stride) {
+    double t = y * 128.0;
+#pragma unroll 1
+    for (int s = 0; s < S; ++s) {
+        const double d = rint(t);
+        out[s * plane_stride] = (uint16_t)(__float_as_uint((float)d) >> 16);
+        t = (t - d) * 256.0;
+    }
+}
+
+// A (m x k, column-major, lda) of matrix blockIdx.y -> S planes of A^ (2m rows x Kp, K contiguous) and
+// ea[i]; one CTA per 32 rows of A
+__global__ void __launch_bounds__(256) tc_split_a_kernel(int m, int k, int Kp, int S, const zc* __restrict__ A, int lda,
+                                                         long long a_stride, uint16_t* __restrict__ out,
+                                                         int* __restrict__ ea) {
+    const long long b = blockIdx.y;
+    const int i0 = blockIdx.x * 32, t = threadIdx.x, il = t & 31, w = t >> 5;
+    const zc* As = A + b * a_stride;
+    __shared__ double smax[8][32];
+    __shared__ int sexp[32];
+    double mx = 0.0;
+    if (i0 + il < m)
+        for (int kk = w; kk < k; kk += 8) {
+            const zc v = As[(long long)kk * lda + i0 + il];
+            mx = fmax(mx, fmax(fabs(v.re), fabs(v.im)));
+        }
+    smax[w][il] = mx;
+    __syncthreads();
+    if (w == 0) {
+        for (int q = 1; q < 8; ++q) mx = fmax(mx, smax[q][il]);
+        sexp[il] = scale_exponent(mx);
+        if (i0 + il < m) ea[b * m + i0 + il] = sexp[il];
+    }
+    __syncthreads();
+    const long long rows = 2LL * m, plane = rows * Kp;
+    uint16_t* o = out + b * S * plane;
+    for (int idx = t; idx < 64 * Kp; idx += 256) {
+        const int rr = idx / Kp, kk = idx - rr * Kp;
+        const int i = i0 + (rr >> 1), part = rr & 1;
+        if (i >= m) continue;
+        double x = 0.0;
+        if (kk < k) {
+            const zc v = As[(long long)kk * lda + i];
+            x = part ? v.im : v.re;
+        } else if (kk < 2 * k) {
+            const zc v = As[(long long)(kk - k) * lda + i];
+            x = part ? v.re : -v.im;
+        }
+        store_digits(ldexp(x, -sexp[rr >> 1]), S, o + (2LL * i + part) * Kp + kk, plane);
+    }
+}
+
+// B (k x n, column-major, ldb) -> S planes of B^t (n rows x Kp: [Re B(:, j); Im B(:, j)]) and eb[j];
+// one warp per column
+__global__ void __launch_bounds__(128) tc_split_b_kernel(int n, int k, int Kp, int S, int batch, const zc* __restrict__ B,
+                                                         int ldb, long long b_stride, uint16_t* __restrict__ out,
+                                                         int* __restrict__ eb) {
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (gw >= (long long)batch * n) return;
+    const long long b = gw / n;
+    const int j = (int)(gw - b * n), lane = threadIdx.x & 31;
+    const zc* col = B + b * b_stride + (long long)j * ldb;
+    double mx = 0.0;
+    for (int kk = lane; kk < k; kk += 32) mx = fmax(mx, fmax(fabs(col[kk].re), fabs(col[kk].im)));
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    const int e = scale_exponent(mx);
+    if (lane == 0) eb[b * n + j] = e;
+    const long long plane = (long long)n * Kp;
+    uint16_t* o = out + b * S * plane + (long long)j * Kp;
+    for (int kk = lane; kk < Kp; kk += 32) {
+        const double x = kk < k ? col[kk].re : (kk < 2 * k ? col[kk - k].im : 0.0);
+        store_digits(ldexp(x, -e), S, o + kk, plane);
+    }
+}
+
+// ---------------------------------------------------------------- the product
+
+struct SharedState {
+    uint64_t full[kStages], empty[kStages], tfull[2], tempty[2], drain;
+    uint32_t tmem_base;
+    int abort_flag;
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, const __grid_constant__ Plan plan,
+                   int m, int n, int batch0, int a_bcast, int b_bcast, const int* __restrict__ ea, const int* __restrict__ eb,
+                   const zc* C0, long long c0_stride, zc* C, int ldc, long long c_stride, double s_ab, double s_c,
+                   const int* __restrict__ skip, int skip_value, int* __restrict__ err) {
+    const int lb = blockIdx.z;  // matrix within this chunk
+    if (skip && skip[batch0 + lb] == skip_value) return;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    SharedState* ss = reinterpret_cast<SharedState*>(smem + kStages * kStageBytes);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.y * kTileM, n0 = blockIdx.x * kTileN;
+    const int S = plan.S;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&ss->full[s], 1);
+            mbar_init(&ss->empty[s], 1);
+        }
+        for (int s = 0; s < 2; ++s) {
+            mbar_init(&ss->tfull[s], 1);
+            mbar_init(&ss->tempty[s], 8);
+        }
+        mbar_init(&ss->drain, 1);
+        ss->abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&ss->tmem_base)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        tc_fence_before();
+    }
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = ss->tmem_base;
+    volatile int* abort_flag = &ss->abort_flag;
+    const int za = a_bcast ? 0 : lb, zb = b_bcast ? 0 : lb;
+
+    if (warp == 0) {
+        // ---- TMA producer
+        if (lane == 0) {
+            int it = 0;
+            int issued[kStages];
+            for (int s = 0; s < kStages; ++s) issued[s] = -1;
+            bool ok = true;
+            for (int gi = 0; gi < plan.n_groups && ok; ++gi) {
+                const unsigned g = plan.g[gi];
+                const int d = g_d(g);
+                for (int p = 0; p < g_ni(g) && ok; ++p) {
+                    const int i = g_i0(g) + p, j = d - i;
+                    for (int kb = g_kb0(g); kb < g_kb0(g) + g_nkb(g); ++kb, ++it) {
+                        const int st = it % kStages, ph = (it / kStages) & 1;
+                        if (!mbar_wait(&ss->empty[st], ph ^ 1, abort_flag, err)) {
+                            ok = false;
+                            break;
+                        }
+                        unsigned char* sa = smem + st * kStageBytes;
+                        mbar_expect_tx(&ss->full[st], kStageBytes);
+                        tma_load_3d(sa, &map_a, kb * kTileK, m0, za * S + i - 1, &ss->full[st]);
+                        tma_load_3d(sa + kTileM * kTileK * 2, &map_b, kb * kTileK, n0, zb * S + j - 1, &ss->full[st]);
+                        issued[st] = it;
+                    }
+                }
+            }
+            if (!ok) {
+                // drain: wait (bounded) for the copies this thread started into each stage
+                for (int s = 0; s < kStages; ++s) {
+                    if (issued[s] < 0) continue;
+                    const int ph = (issued[s] / kStages) & 1;
+                    for (unsigned r = 0; r < kWaitLimit && !mbar_try_wait(&ss->full[s], ph); ++r) {
+                    }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        // ---- MMA issuer
+        if (lane == 0) {
+            int it = 0;
+            bool ok = true;
+            bool any = false;
+            for (int gi = 0; gi < plan.n_groups && ok; ++gi) {
+                const unsigned g = plan.g[gi];
+                const int buf = gi & 1;
+                if (!mbar_wait(&ss->tempty[buf], ((gi >> 1) & 1) ^ 1, abort_flag, err)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d_tmem = tmem + buf * kTileN;
+                uint32_t acc = 0;
+                for (int p = 0; p < g_ni(g) && ok; ++p) {
+                    for (int kb = 0; kb < g_nkb(g); ++kb, ++it) {
+                        const int st = it % kStages, ph = (it / kStages) & 1;
+                        if (!mbar_wait(&ss->full[st], ph, abort_flag, err)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t a_addr = smem_u32(smem + st * kStageBytes);
+                        const uint32_t b_addr = a_addr + kTileM * kTileK * 2;
+#pragma unroll
+                        for (int kk = 0; kk < kTileK / 16; ++kk) {
+                            mma_bf16(d_tmem, smem_desc_sw128(a_addr + kk * 32), smem_desc_sw128(b_addr + kk * 32), acc);
+                            acc = 1;
+                        }
+                        any = true;
+                        mma_commit(&ss->empty[st]);  // the stage is free once these products have read it
+                    }
+                }
+                if (ok) mma_commit(&ss->tfull[buf]);
+            }
+            if (!ok && any) {
+                // drain: every product issued so far completes before the accumulators are freed
+                mma_commit(&ss->drain);
+                for (unsigned r = 0; r < kWaitLimit && !mbar_try_wait(&ss->drain, 0); ++r) {
+                }
+            }
+        }
+    } else {
+        // ---- epilogue: warps 2..9; lane quarter q of tensor memory, column half h
+        const int q = warp & 3, h = (warp - 2) >> 2;
+        double acc[64];
+#pragma unroll
+        for (int c = 0; c < 64; ++c) acc[c] = 0.0;
+        bool ok = true;
+        for (int gi = 0; gi < plan.n_groups; ++gi) {
+            const int buf = gi & 1;
+            ok = mbar_wait(&ss->tfull[buf], (gi >> 1) & 1, abort_flag, err);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) break;
+            tc_fence_after();
+            const int d = g_d(plan.g[gi]);
+            const double scale = ldexp(1.0, -14 - 8 * (d - 2));
+            const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + buf * kTileN + h * 64;
+#pragma unroll
+            for (int c16 = 0; c16 < 4; ++c16) {
+                float v[16];
+                tmem_ld16(base + c16 * 16, v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) acc[c16 * 16 + j] = fma((double)v[j], scale, acc[c16 * 16 + j]);
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&ss->tempty[buf]);
+        }
+        if (ok && !*abort_flag) {
+            const int r = m0 + q * 32 + lane;  // row of A^
+            const int i = r >> 1;
+            const int er = (i < m) ? ea[(long long)(a_bcast ? 0 : batch0 + lb) * m + i] : 0;
+            const bool writer = ((lane & 1) == 0) && i < m;
+            const int* ebs = eb + (long long)(b_bcast ? 0 : batch0 + lb) * n;
+            zc* Cs = C + (long long)(batch0 + lb) * c_stride;
+            const zc* C0s = C0 ? C0 + (long long)(batch0 + lb) * c0_stride : nullptr;
+#pragma unroll
+            for (int c = 0; c < 64; ++c) {
+                const int col = n0 + h * 64 + c;
+                const int e = col < n ? er + ebs[col] : 0;
+                const double v = ldexp(acc[c], e);
+                const double im = __shfl_down_sync(0xffffffffu, v, 1);
+                if (writer && col < n) {
+                    zc out{s_ab * v, s_ab * im};
+                    const long long off = (long long)col * ldc + i;
+                    if (C0s && s_c != 0.0) {
+                        const zc c0 = C0s[off];
+                        out = zc{s_c * c0.re + out.re, s_c * c0.im + out.im};
+                    }
+                    Cs[off] = out;
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    }
+}
+
+// ---------------------------------------------------------------- host side
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+    static EncodeTiled fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(f);
+    });
+    if (!fn) throw EngineError{RCWA_ECUDA, "tensor-core GEMM: cuTensorMapEncodeTiled is not available"};
+    return fn;
+}
+
+// digit planes (planes x rows x Kp bf16, K contiguous) as a 3-D tensor map with 64 x 128 boxes
+CUtensorMap plane_map(const uint16_t* base, long long rows, int Kp, long long planes) {
+    CUtensorMap map;
+    const cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)planes};
+    const cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)rows * Kp * 2};
+    const cuuint32_t box[3] = {(cuuint32_t)kTileK, (cuuint32_t)kTileM, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<uint16_t*>(base), dims, strides,
+                                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw EngineError{RCWA_ECUDA, "tensor-core GEMM: tensor map encoding failed"};
+    return map;
+}
+
+// The groups, smallest contributions first: diagonal d = S + 1 down to 2, K in chunks of at most 1024,
+// at most 1024 / (chunk length) digit pairs per group so every group's sum is exact in FP32.
+Plan make_plan(int S, int kblocks) {
+    Plan p{};
+    p.S = S;
+    const int chunk_kb = 1024 / kTileK;
+    for (int d = S + 1; d >= 2; --d) {
+        const int lo = std::max(1, d - S), hi = std::min(S, d - 1);
+        for (int kb0 = 0; kb0 < kblocks; kb0 += chunk_kb) {
+            const int nkb = std::min(chunk_kb, kblocks - kb0);
+            const int per = std::max(1, 1024 / (nkb * kTileK));
+            for (int i0 = lo; i0 <= hi; i0 += per) {
+                if (p.n_groups >= kMaxGroups) throw EngineError{RCWA_EUNSUPPORTED, "tensor-core GEMM: K too large"};
+                const int ni = std::min(per, hi - i0 + 1);
+                p.g[p.n_groups++] = (unsigned)d | (unsigned)i0 << 4 | (unsigned)ni << 8 | (unsigned)kb0 << 12 |
+                                    (unsigned)nkb << 22;
+            }
+        }
+    }
+    return p;
+}
+
+int* error_flag() {
+    static int* d = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        if (cudaMalloc(&d, sizeof(int)) != cudaSuccess || cudaMemset(d, 0, sizeof(int)) != cudaSuccess) d = nullptr;
+    });
+    if (!d) throw EngineError{RCWA_ECUDA, "tensor-core GEMM: no error flag"};
+    return d;
+}
+
+}  // namespace
+
+int tc_gemm_slices() {
+    static const int s = [] {
+        const char* e = std::getenv("RCWA_GB300_TC_SLICES");
+        const int v = e ? std::atoi(e) : 7;
+        return std::min(kMaxSlices, std::max(2, v));
+    }();
+    return s;
+}
+
+bool tc_gemm_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("RCWA_GB300_GEMM");
+        return !(e && std::strcmp(e, "fp64") == 0);
+    }();
+    return on;
+}
+
+namespace {
+thread_local int g_fp64_guards = 0;
+}
+Fp64ProductsGuard::Fp64ProductsGuard() { ++g_fp64_guards; }
+Fp64ProductsGuard::~Fp64ProductsGuard() { --g_fp64_guards; }
+bool Fp64ProductsGuard::active() { return g_fp64_guards > 0; }
+
+int tc_gemm_error() {
+    int h = 0;
+    RCWA_CUDA(cudaMemcpy(&h, error_flag(), sizeof(int), cudaMemcpyDeviceToHost));
+    return h;
+}
+
+void launch_zgemm_tc(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride,
+                     const zc* B, int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc,
+                     long long c_stride, double s_ab, double s_c, const int* skip, int skip_value) {
+    if (batch <= 0 || m <= 0 || n <= 0) return;
+    const int smem_bytes = kStages * kStageBytes + 1024 + (int)sizeof(SharedState) + 64;
+    static std::once_flag attr_once;
+    static cudaError_t attr_rc = cudaSuccess;
+    std::call_once(attr_once, [&] {
+        attr_rc = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    });
+    RCWA_CUDA(attr_rc);
+    const int S = tc_gemm_slices();
+    const int Kp = ((2 * k + kTileK - 1) / kTileK) * kTileK;
+    const Plan plan = make_plan(S, Kp / kTileK);
+    const bool a_bcast = a_stride == 0, b_bcast = b_stride == 0;
+    const long long a_bytes = (long long)S * 2 * m * Kp * 2, b_bytes = (long long)S * n * Kp * 2;
+    // matrices per pass: digit planes of at most ~1 GiB
+    const long long per = (a_bcast ? 0 : a_bytes) + (b_bcast ? 0 : b_bytes) + 1;
+    const int chunk = (int)std::max(1LL, std::min<long long>(batch, (1LL << 30) / per));
+    int* err = error_flag();
+
+    uint16_t *pa = nullptr, *pb = nullptr;
+    int *dea = nullptr, *deb = nullptr;
+    const int na = a_bcast ? 1 : chunk, nb = b_bcast ? 1 : chunk;
+    RCWA_CUDA(cudaMallocAsync(&pa, (size_t)a_bytes * na, st));
+    RCWA_CUDA(cudaMallocAsync(&pb, (size_t)b_bytes * nb, st));
+    RCWA_CUDA(cudaMallocAsync(&dea, sizeof(int) * (size_t)m * (a_bcast ? 1 : batch), st));
+    RCWA_CUDA(cudaMallocAsync(&deb, sizeof(int) * (size_t)n * (b_bcast ? 1 : batch), st));
+    const CUtensorMap map_a = plane_map(pa, 2LL * m, Kp, (long long)na * S);
+    const CUtensorMap map_b = plane_map(pb, n, Kp, (long long)nb * S);
+    if (a_bcast) {
+        tc_split_a_kernel<<<dim3((m + 31) / 32, 1), 256, 0, st>>>(m, k, Kp, S, A, lda, 0, pa, dea);
+        ++launch_count();
+    }
+    if (b_bcast) {
+        tc_split_b_kernel<<<(unsigned)((n * 32LL + 127) / 128), 128, 0, st>>>(n, k, Kp, S, 1, B, ldb, 0, pb, deb);
+        ++launch_count();
+    }
+    for (int b0 = 0; b0 < batch; b0 += chunk) {
+        const int cb = std::min(chunk, batch - b0);
+        if (!a_bcast) {
+            tc_split_a_kernel<<<dim3((m + 31) / 32, cb), 256, 0, st>>>(m, k, Kp, S, A + (long long)b0 * a_stride, lda,
+                                                                        a_stride, pa, dea + (long long)b0 * m);
+            ++launch_count();
+        }
+        if (!b_bcast) {
+            tc_split_b_kernel<<<(unsigned)((cb * (long long)n * 32 + 127) / 128), 128, 0, st>>>(
+                n, k, Kp, S, cb, B + (long long)b0 * b_stride, ldb, b_stride, pb, deb + (long long)b0 * n);
+            ++launch_count();
+        }
+        const dim3 grid((n + kTileN - 1) / kTileN, (2 * m + kTileM - 1) / kTileM, cb);
+        tc_gemm_kernel<<<grid, kThreads, smem_bytes, st>>>(map_a, map_b, plan, m, n, b0, a_bcast, b_bcast, dea, deb, C0,
+                                                           c0_stride, C, ldc, c_stride, s_ab, s_c, skip, skip_value, err);
+        ++launch_count();
+        RCWA_CUDA(cudaGetLastError());
+    }
+    RCWA_CUDA(cudaFreeAsync(pa, st));
+    RCWA_CUDA(cudaFreeAsync(pb, st));
+    RCWA_CUDA(cudaFreeAsync(dea, st));
+    RCWA_CUDA(cudaFreeAsync(deb, st));
+}
+
+}  // namespace rcwa_gb300

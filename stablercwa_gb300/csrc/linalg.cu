@@ -184,9 +184,14 @@ void launch_zgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A, 
                   int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc, long long c_stride,
                   double s_ab, double s_c, const int* skip, int skip_value, int tri) {
     if (batch <= 0 || m <= 0 || n <= 0) return;
+    TimedLaunch timed(TK_GEMM, st);
+    if (k >= 32 && m >= 32 && n >= 32 && tc_gemm_enabled() && !Fp64ProductsGuard::active()) {
+        launch_zgemm_tc(st, m, n, k, batch, A, lda, a_stride, B, ldb, b_stride, C0, c0_stride, C, ldc, c_stride, s_ab, s_c,
+                        skip, skip_value);
+        return;
+    }
     const long long warps = (long long)batch * ((m + 31) / 32) * ((n + 7) / 8);
     const unsigned blocks = (unsigned)((warps * 32 + 127) / 128);
-    TimedLaunch timed(TK_GEMM, st);
     zgemm_kernel<<<blocks, 128, 0, st>>>(m, n, k, batch, A, lda, a_stride, B, ldb, b_stride, C0, c0_stride, C, ldc,
                                          c_stride, s_ab, s_c, skip, skip_value, tri);
     ++launch_count();

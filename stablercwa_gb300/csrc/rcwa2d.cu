@@ -380,6 +380,7 @@ void layer_operators2d(cudaStream_t st, const rcwa_layer2d& layer, double Lx, do
 void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d* points, int n_points, int M1, int M2,
                   int factorization, const Options& opt, const rcwa_result2d& out, size_t chunk_bytes,
                   const FieldSpec* fields) {
+    const Fp64ProductsGuard fp64_products;
     const int n1 = 2 * M1 + 1, n2 = 2 * M2 + 1, N = n1 * n2, n = 2 * N;
     const long long NN = (long long)N * N, nn = (long long)n * n;
     const int L = stack.n_layers;

@@ -94,6 +94,7 @@ def load_library(build_if_missing=True):
     L.rcwa_gpu_eig_hermitian_batch_dev.argtypes = [vp, ci, ci, vp, cd, ci, vp, vp, vp]
     L.rcwa_gpu_solve_batch.argtypes = [vp, ci, ci, ci, vp, vp, vp, vp]
     L.rcwa_gpu_multiply_batch.argtypes = [vp, ci, ci, ci, ci, vp, vp, vp]
+    L.rcwa_gpu_gemm_info.argtypes = [vp, vp, vp]
     _lib = L
     return L
 
@@ -470,6 +471,16 @@ class Engine:
         return c.transpose(0, 2, 1)
 
 
+def gemm_info():
+    """(tensor_cores, slices, stuck) of the engine's complex products (rcwa_gpu_gemm_info)."""
+    L = load_library()
+    t, sl, st = C.c_int(), C.c_int(), C.c_int()
+    rc = L.rcwa_gpu_gemm_info(C.byref(t), C.byref(sl), C.byref(st))
+    if rc != 0:
+        raise EngineError(rc, "rcwa_gpu_gemm_info failed")
+    return bool(t.value), sl.value, st.value
+
+
 def _json_call(fn, handle, request, indent):
     L = load_library()
     out = C.c_void_p()
@@ -590,6 +601,9 @@ class Server:
         rc = self.L.rcwa_gpu_server_wait(self.h, ticket, timeout_ms, C.byref(resp), C.cast(C.byref(res), C.c_void_p))
         if rc == abi.RCWA_ETIMEOUT:
             return None
+        if rc == abi.RCWA_ECANCELLED:
+            del self.meta[ticket]
+            return {"code": rc, "kind": kind}, None
         if rc != 0:
             raise ValueError(f"rcwa_gpu_server_wait: error {rc}")
         del self.meta[ticket]
