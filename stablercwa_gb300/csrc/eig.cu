@@ -31,6 +31,11 @@ int eig_default_group(int n, int batch) {
 void launch_eig(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info, int* sweeps,
                 zc* ws, double eps, int max_iter, int group, const int* skip, int skip_value, zc* t_out) {
     if (batch <= 0 || n <= 0) return;
+    if (group == -1 || (group == 0 && eig_cluster_wanted(n, batch))) {
+        TimedLaunch timed(TK_EIG, st);
+        launch_eig_cluster(st, n, batch, a, a_stride, w, v, info, sweeps, ws, eps, max_iter, skip, skip_value, t_out);
+        return;
+    }
     if (group <= 0) group = eig_default_group(n, batch);
     TimedLaunch timed(TK_EIG, st);
     if (group > 32) {
