@@ -41,11 +41,16 @@ WORKLOAD = ("config 2: batched 1-D TE+TM sweep, M=60 (N=121), binary grating on 
             "4096 seeded (lambda, theta) points x 2 polarizations per step")
 
 
-def workload(seed=SEED, n_points=N_POINTS):
+# the absorbing variant of the grating (the general Hessenberg + shifted QR eigensolver instead of the
+# Hermitian one): index 1.46 + 0.01i
+LOSSY_RIDGE = complex(1.46, 0.01)
+
+
+def workload(seed=SEED, n_points=N_POINTS, ridge=1.46):
     from stablercwa_gb300 import Layer, Stack
     rng = np.random.default_rng(seed)
     fill, depth = rng.uniform(0.3, 0.5), rng.uniform(0.3, 0.5)
-    layers = [Layer.grating(depth, [0.0, fill * PERIOD, PERIOD], [1.46, 1.0])]
+    layers = [Layer.grating(depth, [0.0, fill * PERIOD, PERIOD], [ridge, 1.0])]
     for _ in range(10):
         layers.append(Layer.uniform(1.053 / (4 * 2.1), 2.1))
         layers.append(Layer.uniform(1.053 / (4 * 1.46), 1.46))
@@ -55,8 +60,8 @@ def workload(seed=SEED, n_points=N_POINTS):
 
 
 # DRAM bytes per matrix of the Hermitian eigensolve stage at n = 121 (tridiagonalisation 54.3 MB, real
-# rotations 1.2 MB, Q Y 0.6 MB), from one ncu --set full capture of 2432 matrices
-# (profiles/herm_eigensolver_n121.md); the QL kernel's bytes are not included
+# rotations 1.2 MB, Q Y 0.6 MB), from one ncu --set full capture of 2432 matrices of this order; the QL
+# kernel's bytes are not included
 HERM_STAGE_DRAM_BYTES_PER_MATRIX_N121 = 56.1e6
 
 
@@ -344,8 +349,14 @@ def run_ours(args):
     h2d = P * 16  # s and wavelength per point, once for both polarizations
     d2h = 2 * (P * n * (16 + 16 + 8 + 8) + P * 4 * 4)
 
-    # ---- accuracy and CPU baseline (rank 0): the oracle on a bounded sample of the same points
+    # ---- the plain path and the lossy variant (rank 0, after the timed region)
     line_extra = {}
+    if rank == 0 and args.plain_points > 0:
+        line_extra["plain"] = plain_rate(eng, stack, pts, args.plain_points, value)
+    if rank == 0 and args.lossy_steps > 0:
+        line_extra["lossy_c2"] = lossy_rate(eng, torch, est, flush, args, peak)
+
+    # ---- accuracy and CPU baseline (rank 0): the oracle on a bounded sample of the same points
     if rank == 0:
         threads = os.cpu_count() or 1
         sample_idx = np.linspace(0, P - 1, args.cpu_points).astype(int)
@@ -416,6 +427,81 @@ def run_ours(args):
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def plain_rate(eng, stack, pts, count, batched_value):
+    """The plain path: `count` of the points, each solved alone through the host-buffer entry point, TE
+    then TM (one solve per call), all FP64; solves/s and the batched value over it."""
+    sel = pts[np.linspace(0, len(pts) - 1, count).astype(int)]
+    eng.solve1d_arrays(stack, sel[:1], M, 0)  # warm
+    t0 = time.perf_counter()
+    for pol in (0, 1):
+        for k in range(len(sel)):
+            eng.solve1d_arrays(stack, sel[k:k + 1], M, pol)
+    dt = time.perf_counter() - t0
+    rate = 2 * len(sel) / dt
+    return {"value": rate, "unit": "solves/s", "solves": 2 * len(sel), "seconds": dt,
+            "batched_over_plain": batched_value / rate,
+            "how": "one point and one polarization per call (rcwa_gpu_solve1d_batch with n_points = 1), host buffers"}
+
+
+def lossy_rate(eng, torch, est, flush, args, peak):
+    """The same C2 sweep with an absorbing grating (n = 1.46 + 0.01i): the general Hessenberg + shifted
+    complex QR eigensolver on every grating matrix. Device-resident points, CUDA events, L2 flushed;
+    accuracy against the oracle on a sample."""
+    from stablercwa_gb300.engine import launch_count
+    stack, pts, geo = workload(n_points=args.points, ridge=LOSSY_RIDGE)
+    n, P = 2 * M + 1, len(pts)
+    d_pts = torch.tensor(pts, dtype=torch.float64, device="cuda")
+    out = {"R": torch.empty((2 * P, n, 2), dtype=torch.float64, device="cuda"),
+           "T": torch.empty((2 * P, n, 2), dtype=torch.float64, device="cuda"),
+           "DEr": torch.empty((2 * P, n), dtype=torch.float64, device="cuda"),
+           "DEt": torch.empty((2 * P, n), dtype=torch.float64, device="cuda"),
+           "status": torch.empty(2 * P, dtype=torch.int32, device="cuda")}
+    ptrs = {k: v.data_ptr() for k, v in out.items()}
+
+    def step():
+        eng.solve1d_device(stack, d_pts.data_ptr(), P, M, 2, ptrs)
+    step()
+    eng.synchronize()
+    total = 0.0
+    l0 = launch_count()
+    for _ in range(args.lossy_steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(est)
+        step()
+        e1.record(est)
+        e1.synchronize()
+        total += e0.elapsed_time(e1)
+    launches = launch_count() - l0
+    eng.set_kernel_timing(True)
+    flush.fill_(1.0)
+    torch.cuda.synchronize()
+    step()
+    eng.synchronize()
+    eig_busy = eng.kernel_busy("eig")
+    eig_ms, eig_launches = eng.kernel_time("eig")
+    eng.set_kernel_timing(False)
+    value = 2 * P * args.lossy_steps / (total * 1e-3)
+    achieved = eig_launches * P * 105 * n ** 3 / (eig_busy * 1e-3) / 1e12 if eig_busy > 0 else None
+    from oracle import oracle
+    idx = np.linspace(0, P - 1, max(2, args.cpu_points // 4)).astype(int)
+    host = {k: v.cpu().numpy() for k, v in out.items() if k in ("DEr", "DEt", "status")}
+    err = 0.0
+    for pol in (0, 1):
+        ref = oracle.solve1d_batch(stack, pts[idx], M, pol, threads=os.cpu_count() or 1)
+        for key in ("DEr", "DEt"):
+            err = max(err, float(np.max(np.abs(host[key][pol * P + idx] - ref[key]))))
+    return {"value": value, "unit": "solves/s", "steps": args.lossy_steps, "ms_per_step": total / args.lossy_steps,
+            "gpu_launches": launches, "ridge_index": [LOSSY_RIDGE.real, LOSSY_RIDGE.imag],
+            "eigensolver": "general: Hessenberg reduction + shifted complex QR + back substitution (eig_batch_kernel)",
+            "eig_ms_per_step": eig_ms, "eig_busy_ms_per_step": eig_busy,
+            "eig_roofline": {"achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                             "frac": achieved / peak if achieved else None, "flops_model": "105 n^3 per matrix"},
+            "accuracy": {"max_abs_dDE_vs_oracle": err, "sample_solves": 2 * len(idx),
+                         "all_status_ok": bool((host["status"] == 0).all())}}
 
 
 # ------------------------------------------------------------------------------------- other configurations
@@ -753,6 +839,10 @@ def main():
     ap.add_argument("--points", type=int, default=N_POINTS,
                     help="C2 points per step (the headline is 4096; fewer only for small profiling captures)")
     ap.add_argument("--ref-points", type=int, default=128)
+    ap.add_argument("--plain-points", type=int, default=32,
+                    help="points of the plain one-solve-per-call line in the headline run (0: skip)")
+    ap.add_argument("--lossy-steps", type=int, default=1,
+                    help="timed steps of the absorbing-grating C2 line in the headline run (0: skip)")
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-slots", type=int, default=48)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[0.5, 1.0])
