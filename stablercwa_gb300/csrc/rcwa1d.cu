@@ -398,17 +398,28 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
         std::vector<DModes> modes(L + 2);
         std::vector<zc*> cap_W(L, nullptr), cap_V(L, nullptr);  // retained W, V of grating layers (fields)
         std::vector<DOp> r_below(L);                             // reflection below each layer (fields)
-        const auto analytic = [&](DModes& m, rcwa_complex idx, int fzb) {
-            m.analytic = true;
-            m.fzb = fzb != 0;
-            m.q = c.vec();
-            m.p = c.vec();
-            LAUNCH(analytic_modes_kernel, nblocks(nv), kTpb, st, B, n, kx, zc{idx.re, idx.im}, pol, fzb, m.q, m.p, nullptr);
-        };
-        analytic(modes[0], stack.nI, 0);
-        analytic(modes[L + 1], stack.nII, 0);
-        for (int k = 0; k < L; ++k)
-            if (stack.layers[k].homogeneous) analytic(modes[k + 1], stack.layers[k].n, 1);
+        // the analytic modes of every homogeneous region in one launch, region r at offset r * B * n
+        zc* aq = mem.get<zc>((size_t)(L + 2) * nv);
+        zc* ap = mem.get<zc>((size_t)(L + 2) * nv);
+        {
+            std::vector<AnalyticRegion> regs(L + 2);
+            regs[0] = {zc{stack.nI.re, stack.nI.im}, 0, 1};
+            regs[L + 1] = {nII, 0, 1};
+            for (int k = 0; k < L; ++k) {
+                const rcwa_layer1d& Ly = stack.layers[k];
+                regs[k + 1] = Ly.homogeneous ? AnalyticRegion{zc{Ly.n.re, Ly.n.im}, 1, 1} : AnalyticRegion{zc{0.0, 0.0}, 0, 0};
+            }
+            AnalyticRegion* d_regs = mem.get<AnalyticRegion>(regs.size());
+            RCWA_CUDA(cudaMemcpyAsync(d_regs, regs.data(), regs.size() * sizeof(AnalyticRegion), cudaMemcpyHostToDevice, st));
+            LAUNCH(analytic_modes_all_kernel, nblocks((long long)(L + 2) * nv), kTpb, st, L + 2, B, n, kx, d_regs, pol, aq, ap);
+            for (int r = 0; r < L + 2; ++r)
+                if (regs[r].active) {
+                    modes[r].analytic = true;
+                    modes[r].fzb = regs[r].fzb != 0;
+                    modes[r].q = aq + (long long)r * nv;
+                    modes[r].p = ap + (long long)r * nv;
+                }
+        }
 
         if (!grating.empty()) {
             zc* ws = mem.get<zc>((size_t)(eig_workspace_bytes(n, B) / sizeof(zc)) + 1);
@@ -510,7 +521,35 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
         const int block_count = 2 * L + 1;
         std::vector<DOp> g(block_count);
         DOp r;  // Zero: nothing comes up from the exit medium
-        for (int b = block_count - 1; b >= 1; --b) {
+        // The run of homogeneous regions at the bottom (every block diagonal) in one launch when no fields are
+        // captured: blocks [b_stop, block_count) (film_run_kernel), their g kept for one downward launch.
+        int b_stop = block_count;
+        zc* g_run = nullptr;
+        if (!fields) {
+            int b = block_count - 1;
+            while (b >= 1) {
+                const int j = b / 2;
+                if (!(b % 2 == 0 ? (modes[j].analytic && modes[j + 1].analytic) : modes[j + 1].analytic)) break;
+                --b;
+            }
+            if (block_count - 1 - b >= 2) b_stop = b + 1;
+        }
+        if (b_stop < block_count) {
+            const int nblk = block_count - b_stop;
+            std::vector<FilmBlock> fb(nblk);
+            for (int t = 0; t < nblk; ++t) {
+                const int bb = block_count - 1 - t, j = bb / 2;
+                fb[t] = bb % 2 == 0 ? FilmBlock{0, j, j + 1, 0, 0.0}
+                                    : FilmBlock{1, j + 1, 0, modes[j + 1].fzb ? 1 : 0, stack.layers[j].d};
+            }
+            FilmBlock* d_fb = mem.get<FilmBlock>(nblk);
+            RCWA_CUDA(cudaMemcpyAsync(d_fb, fb.data(), nblk * sizeof(FilmBlock), cudaMemcpyHostToDevice, st));
+            g_run = mem.get<zc>((size_t)nblk * nv);
+            zc* rv = c.vec();
+            LAUNCH(film_run_kernel, nblocks(nv), kTpb, st, B, n, nblk, d_fb, aq, ap, k0, g_run, rv, c.fail);
+            r = {KDiag, rv};
+        }
+        for (int b = b_stop - 1; b >= 1; --b) {
             const int j = b / 2;
             if (b % 2 == 0 && modes[j].analytic && modes[j + 1].analytic && r.kind != KDense) {
                 // Fresnel block between two analytic regions stacked on a diagonal (or zero) reflection
@@ -689,6 +728,11 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
         std::vector<zc*> a_plus(L, nullptr), a_minus(L, nullptr);
         for (int b = 1; b < block_count; ++b) {
             const int j = b / 2;
+            if (b == b_stop) {  // the fused bottom run: all of its blocks in one launch
+                LAUNCH(film_push_kernel, nblocks(nv), kTpb, st, nv, block_count - b_stop, g_run, cur, nxt);
+                std::swap(cur, nxt);
+                break;
+            }
             if (fields && b % 2 != 0) {  // amplitude at the layer's top (rcwa1d.hpp:1008-1012)
                 a_plus[j] = c.vec();
                 RCWA_CUDA(cudaMemcpyAsync(a_plus[j], cur, nv * sizeof(zc), cudaMemcpyDeviceToDevice, st));

@@ -26,22 +26,127 @@ __global__ void kx_kernel(int B, int M, const double* __restrict__ s, const doub
 // Analytic modes of a homogeneous region of index nidx (include/stablercwa/rcwa1d.hpp:522-544):
 // kz = sqrt(n^2 - kx^2) with Im kz >= 0 (Re >= 0 when Im ~ 0), q = -i kz, p = q (TE) or q/n^2 (TM);
 // with finite_zero_basis an exact q == 0 uses the auxiliary basis q = 1 in p.
-__global__ void analytic_modes_kernel(int B, int n, const double* __restrict__ kx, zc nidx, int pol, int fzb,
-                                      zc* __restrict__ q, zc* __restrict__ p, int* __restrict__ zero_flag) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long long)B * n) return;
-    const double k = kx[idx];
+__device__ __forceinline__ bool analytic_mode(double k, zc nidx, int pol, int fzb, zc& q, zc& p) {
     const zc n2 = zc{__dsub_rn(__dmul_rn(nidx.re, nidx.re), __dmul_rn(nidx.im, nidx.im)),
                      __dadd_rn(__dmul_rn(nidx.re, nidx.im), __dmul_rn(nidx.im, nidx.re))};
     zc kz = zsqrt(zc{__dsub_rn(n2.re, __dmul_rn(k, k)), n2.im});
     if (kz.im < 0.0) kz = -kz;
     if (fabs(kz.im) < 1e-12 && kz.re < 0.0) kz = -kz;
     const zc qq = zc{kz.im, -kz.re};
-    q[idx] = qq;
+    q = qq;
     const bool zero = is_zero(qq);
     const zc bq = (fzb && zero) ? zc{1.0, 0.0} : qq;
-    p[idx] = pol == 0 ? bq : zdiv(bq, n2);
+    p = pol == 0 ? bq : zdiv(bq, n2);
+    return zero;
+}
+
+__global__ void analytic_modes_kernel(int B, int n, const double* __restrict__ kx, zc nidx, int pol, int fzb,
+                                      zc* __restrict__ q, zc* __restrict__ p, int* __restrict__ zero_flag) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * n) return;
+    zc qq, pp;
+    const bool zero = analytic_mode(kx[idx], nidx, pol, fzb, qq, pp);
+    q[idx] = qq;
+    p[idx] = pp;
     if (zero_flag && fzb && zero) zero_flag[idx / n] = 1;
+}
+
+// The analytic modes of several homogeneous regions in one launch: region r (index n_r, exact-zero basis
+// flag fzb_r) writes q and p at offset r * B * n; inactive regions (gratings) are skipped.
+struct AnalyticRegion {
+    zc n;
+    int fzb;
+    int active;
+};
+__global__ void analytic_modes_all_kernel(int R, int B, int n, const double* __restrict__ kx,
+                                          const AnalyticRegion* __restrict__ regions, int pol, zc* __restrict__ q,
+                                          zc* __restrict__ p) {
+    const long long nv = (long long)B * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)R * nv) return;
+    const int r = (int)(idx / nv);
+    const AnalyticRegion reg = regions[r];
+    if (!reg.active) return;
+    const long long e = idx - (long long)r * nv;
+    zc qq, pp;
+    analytic_mode(kx[e], reg.n, pol, reg.fzb, qq, pp);
+    q[idx] = qq;
+    p[idx] = pp;
+}
+
+// The run of homogeneous regions at the bottom of a stack, every block diagonal: one thread per (sample,
+// order) carries the reflection r up through the run, block by block from the exit medium, with the
+// Fresnel interface (diagonal_interface_kernel's formulas), the propagation factor of each film
+// (propagation_kernel's, exact q == 0 included) and the diagonal stack_on step (stack_on_diag_kernel's),
+// and stores each block's g for the downward pass; the final r is the run's reflection. The same
+// arithmetic in the same order as the per-block launches (include/stablercwa/rcwa1d.hpp:644-661,
+// :751-808), in one launch.
+struct FilmBlock {
+    int propagate;  // 1: through the film of region `up`, thickness d; 0: interface between `up` and `low`
+    int up, low;
+    int fzb;
+    double d;
+};
+__global__ void film_run_kernel(int B, int n, int nblk, const FilmBlock* __restrict__ blk, const zc* __restrict__ aq,
+                                const zc* __restrict__ ap, const double* __restrict__ k0, zc* __restrict__ g_out,
+                                zc* __restrict__ r_out, int* __restrict__ fail) {
+    const long long nv = (long long)B * n;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nv) return;
+    const int b = (int)(idx / n);
+    bool rzero = true;
+    zc r{0.0, 0.0};
+    for (int t = 0; t < nblk; ++t) {
+        const FilmBlock fb = blk[t];
+        zc tdd, rdu, rud, tuu;
+        if (!fb.propagate) {
+            const zc a = ap[(long long)fb.up * nv + idx], c = ap[(long long)fb.low * nv + idx];
+            const zc inv = zinv(a + c);
+            tdd = (2.0 * a) * inv;
+            rdu = (c - a) * inv;
+            rud = (a - c) * inv;
+            tuu = (2.0 * c) * inv;
+        } else {
+            const zc qq = aq[(long long)fb.up * nv + idx];
+            const double kd = k0[b];
+            if (fb.fzb && is_zero(qq)) {
+                const double h = kd * fb.d;
+                if (!isfinite(h)) fail[b] = 1;
+                const double den = 1.0 + 0.5 * h;
+                tdd = zc{1.0 / den, 0.0};
+                rdu = zc{(0.5 * h) / den, 0.0};
+            } else {
+                const double f = -kd * fb.d;
+                tdd = zexp(zc{f * qq.re, f * qq.im});
+                rdu = zc{0.0, 0.0};
+            }
+            rud = rdu;
+            tuu = tdd;
+        }
+        zc gv;
+        if (!rzero) {
+            const zc k = rdu * r;
+            const zc f = zinv(zc{1.0, 0.0} - k);
+            gv = f * tdd;
+            r = rud + tuu * (r * gv);
+        } else {
+            gv = tdd;
+            r = rud;
+            rzero = false;
+        }
+        g_out[(long long)t * nv + idx] = gv;
+    }
+    r_out[idx] = r;
+}
+
+// y = g_0 (g_1 (... (g_{nblk-1} x))) elementwise: the downward pass through the run, top block first
+__global__ void film_push_kernel(long long nv, int nblk, const zc* __restrict__ g, const zc* __restrict__ x,
+                                 zc* __restrict__ y) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nv) return;
+    zc v = x[idx];
+    for (int t = nblk - 1; t >= 0; --t) v = g[(long long)t * nv + idx] * v;
+    y[idx] = v;
 }
 
 // TE layer matrix A = Kx^2 - [[eps]] from the Toeplitz coefficients c_h, h = -2M..2M
