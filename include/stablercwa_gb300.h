@@ -439,6 +439,23 @@ int rcwa_validate_solve_conical(const rcwa_stack1d* stack, const rcwa_point_coni
 int rcwa_validate_solve2d(const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points, int M1, int M2,
                           int factorization, char* message, size_t size);
 
+/* No reference counterpart: the autotuner of the eigensolvers' kernel form. The batched eigensolvers run
+ * a matrix on G = 4..32 lanes of a warp, on a CTA of 64, 128 or 256 threads, or (general solver, order
+ * >= 384) on a thread-block cluster; a fixed rule picks one unless a tuned form is recorded for the key
+ * (solver, order, batch size rounded down to a power of two). rcwa_gpu_autotune_eig times every
+ * applicable form on batch device matrices d_a (column-major, n x n each) on the context's stream, keeps
+ * only forms that converge where the rule's form does, records the fastest for the key and returns it in
+ * *form (-1 = cluster, else threads per matrix) with its time in *milliseconds. hermitian selects the
+ * Hermitian solver (lossless layers) instead of the general one. rcwa_gpu_autotune_set records a form
+ * directly (a table saved earlier); rcwa_gpu_autotune_table writes the table as text lines
+ * "<general|hermitian> <order> <batch bucket> <form>" and returns its length. The table is process-wide.
+ * RCWA_GB300_AUTOTUNE=0 makes the solves ignore it; =auto also tunes each new key (at least 64 matrices)
+ * on the first call that meets it, on that call's own matrices. */
+int rcwa_gpu_autotune_eig(rcwa_gpu_ctx* ctx, int hermitian, int n, int batch, const rcwa_complex* d_a, int* form,
+                          double* milliseconds);
+int rcwa_gpu_autotune_set(int hermitian, int n, int batch, int form);
+int rcwa_gpu_autotune_table(char* buffer, size_t size);
+
 /* No reference counterpart: how the engine forms its complex products. Products whose three orders are
  * all >= 32 run on the tensor cores (tcgen05, bf16 digit slices of each FP64 operand, exact FP32
  * accumulation of the slice products, FP64 sums: accurate to about k 2^-53 of the largest entries of

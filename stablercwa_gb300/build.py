@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libstablercwa_gb300.so")
-SOURCES = ["capi.cu", "rcwa1d.cu", "conical.cu", "rcwa2d.cu", "eig.cu", "eig_cluster.cu", "eig_static.cu", "fields_post.cu", "linalg.cu", "gemm_tc.cu", "server.cpp", "json_text.cpp", "json_front.cpp"]
+SOURCES = ["capi.cu", "rcwa1d.cu", "conical.cu", "rcwa2d.cu", "eig.cu", "autotune.cu", "eig_cluster.cu", "eig_static.cu", "fields_post.cu", "linalg.cu", "gemm_tc.cu", "server.cpp", "json_text.cpp", "json_front.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-diag-suppress", "177"]
 

@@ -1,0 +1,165 @@
+// autotune.cu -- the eigensolver's kernel form per (kind, order, batch size), picked by timing.
+//
+// The batched eigensolvers come in several forms: G = 4..32 lanes of a warp per matrix, a CTA of 64, 128
+// or 256 threads per matrix, and (general solver, order >= 384) a thread-block cluster per matrix. Which
+// is fastest depends on the order, the batch and the device; the built-in rule (eig_default_group) is a
+// fixed heuristic. The tuner runs every applicable form on a batch of real matrices (each form twice, the
+// second run timed with CUDA events on the caller's stream), keeps only forms whose results agree with
+// the heuristic's form on convergence (info), and records the fastest for the key (solver kind, order,
+// batch size rounded down to a power of two). The launchers consult the table whenever no form is forced.
+// Tuning happens when asked (rcwa_gpu_autotune_eig) or, with RCWA_GB300_AUTOTUNE=auto, the first time a
+// launcher meets a key with at least 64 matrices, on that call's own matrices; RCWA_GB300_AUTOTUNE=0
+// ignores the table.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "eig.cuh"
+#include "engine.h"
+
+namespace rcwa_gb300 {
+namespace {
+
+struct Key {
+    int kind, n, bucket;
+    bool operator<(const Key& o) const { return std::tie(kind, n, bucket) < std::tie(o.kind, o.n, o.bucket); }
+};
+
+std::mutex g_lock;                 // the table
+std::recursive_mutex g_tune_lock;  // one tuning at a time (a tuning run calls the launchers itself)
+std::map<Key, int> g_table;
+thread_local int g_tuning = 0;     // this thread is inside a tuning run: launchers use the form they are given
+
+int bucket_of(int batch) {
+    int b = 0;
+    while ((2LL << b) <= batch) ++b;
+    return b;
+}
+
+int mode() {
+    static const int m = [] {
+        const char* e = std::getenv("RCWA_GB300_AUTOTUNE");
+        if (!e) return 1;                         // consult the table
+        if (std::strcmp(e, "auto") == 0) return 2;  // and tune unseen keys
+        return std::atoi(e) != 0 ? 1 : 0;
+    }();
+    return m;
+}
+
+std::vector<int> candidates(int kind, int n, int batch) {
+    std::vector<int> c;
+    for (int g : {4, 8, 16, 32})
+        if (g == 32 || n >= 4 * g) c.push_back(g);
+    if (n >= 32)
+        for (int g : {64, 128, 256}) c.push_back(g);
+    if (kind == 0 && eig_cluster_wanted(n, batch)) c.push_back(-1);
+    return c;
+}
+
+void run_form(cudaStream_t st, int kind, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info,
+              zc* ws, int form) {
+    if (kind == 0) launch_eig(st, n, batch, a, a_stride, w, v, info, nullptr, ws, 2.220446049250313e-16, 30, form);
+    else launch_eig_herm(st, n, batch, a, a_stride, w, v, info, ws, 2.220446049250313e-16, 30, form);
+}
+
+}  // namespace
+
+int tuned_eig_form(int kind, int n, int batch) {
+    if (g_tuning || mode() == 0) return 0;
+    std::lock_guard<std::mutex> g(g_lock);
+    const auto it = g_table.find(Key{kind, n, bucket_of(batch)});
+    return it == g_table.end() ? 0 : it->second;
+}
+
+bool autotune_wanted(int kind, int n, int batch) {
+    if (g_tuning || mode() != 2 || batch < 64) return false;
+    std::lock_guard<std::mutex> g(g_lock);
+    return g_table.find(Key{kind, n, bucket_of(batch)}) == g_table.end();
+}
+
+void set_tuned_eig_form(int kind, int n, int batch, int form) {
+    std::lock_guard<std::mutex> g(g_lock);
+    g_table[Key{kind, n, bucket_of(batch)}] = form;
+}
+
+int autotune_eig(cudaStream_t st, int kind, int n, int batch, const zc* a, long long a_stride, double* best_ms) {
+    std::lock_guard<std::recursive_mutex> tune(g_tune_lock);
+    {
+        std::lock_guard<std::mutex> g(g_lock);
+        const auto it = g_table.find(Key{kind, n, bucket_of(batch)});
+        if (it != g_table.end() && !best_ms) return it->second;  // another thread tuned it meanwhile
+    }
+    ++g_tuning;
+    zc *w = nullptr, *v = nullptr, *ws = nullptr;
+    int *info = nullptr, *info0 = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int best = 0;
+    double best_t = 0.0;
+    try {
+        RCWA_CUDA(cudaMallocAsync(&w, (size_t)batch * n * sizeof(zc), st));
+        RCWA_CUDA(cudaMallocAsync(&v, (size_t)batch * n * n * sizeof(zc), st));
+        RCWA_CUDA(cudaMallocAsync(&ws, (size_t)eig_workspace_bytes(n, batch) + sizeof(zc), st));
+        RCWA_CUDA(cudaMallocAsync(&info, (size_t)batch * sizeof(int), st));
+        RCWA_CUDA(cudaMallocAsync(&info0, (size_t)batch * sizeof(int), st));
+        RCWA_CUDA(cudaEventCreate(&e0));
+        RCWA_CUDA(cudaEventCreate(&e1));
+        // the heuristic's form first: its convergence pattern is the reference for the others
+        const int base = kind == 0 && eig_cluster_wanted(n, batch) ? -1 : eig_default_group(n, batch);
+        run_form(st, kind, n, batch, a, a_stride, w, v, info0, ws, base);
+        std::vector<int> h0(batch), h1(batch);
+        RCWA_CUDA(cudaMemcpyAsync(h0.data(), info0, batch * sizeof(int), cudaMemcpyDeviceToHost, st));
+        RCWA_CUDA(cudaStreamSynchronize(st));
+        for (int form : candidates(kind, n, batch)) {
+            run_form(st, kind, n, batch, a, a_stride, w, v, info, ws, form);  // warm: modules loaded, caches settled
+            RCWA_CUDA(cudaEventRecord(e0, st));
+            run_form(st, kind, n, batch, a, a_stride, w, v, info, ws, form);
+            RCWA_CUDA(cudaEventRecord(e1, st));
+            RCWA_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            RCWA_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            RCWA_CUDA(cudaMemcpy(h1.data(), info, batch * sizeof(int), cudaMemcpyDeviceToHost));
+            bool same = true;
+            for (int k = 0; k < batch && same; ++k) same = (h0[k] == 0) == (h1[k] == 0);
+            if (same && (best == 0 || ms < best_t)) {
+                best = form;
+                best_t = ms;
+            }
+        }
+    } catch (...) {
+        --g_tuning;
+        for (void* p : {(void*)w, (void*)v, (void*)ws, (void*)info, (void*)info0})
+            if (p) cudaFreeAsync(p, st);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        throw;
+    }
+    --g_tuning;
+    for (void* p : {(void*)w, (void*)v, (void*)ws, (void*)info, (void*)info0}) RCWA_CUDA(cudaFreeAsync(p, st));
+    RCWA_CUDA(cudaEventDestroy(e0));
+    RCWA_CUDA(cudaEventDestroy(e1));
+    if (best != 0) set_tuned_eig_form(kind, n, batch, best);
+    if (best_ms) *best_ms = best_t;
+    return best;
+}
+
+std::string autotune_table_text() {
+    std::lock_guard<std::mutex> g(g_lock);
+    std::string out;
+    char buf[160];
+    for (const auto& kv : g_table) {
+        std::snprintf(buf, sizeof buf, "%s %d %d %d\n", kv.first.kind == 0 ? "general" : "hermitian", kv.first.n,
+                      1 << kv.first.bucket, kv.second);
+        out += buf;
+    }
+    return out;
+}
+
+}  // namespace rcwa_gb300

@@ -769,6 +769,39 @@ int rcwa_validate_solve2d(const rcwa_stack2d* stack, const rcwa_point2d* points,
     });
 }
 
+int rcwa_gpu_autotune_eig(rcwa_gpu_ctx* ctx, int hermitian, int n, int batch, const rcwa_complex* d_a, int* form,
+                          double* milliseconds) {
+    return guarded(ctx, [&] {
+        if (n < 1 || batch < 1 || !d_a) throw EngineError{RCWA_EINVAL, "autotune: positive order and batch and a matrix array"};
+        double ms = 0.0;
+        const int f = autotune_eig(ctx->stream, hermitian ? 1 : 0, n, batch, reinterpret_cast<const zc*>(d_a),
+                                   (long long)n * n, &ms);
+        if (form) *form = f;
+        if (milliseconds) *milliseconds = ms;
+    });
+}
+
+int rcwa_gpu_autotune_set(int hermitian, int n, int batch, int form) {
+    const bool ok_form = form == -1 || form == 4 || form == 8 || form == 16 || form == 32 || form == 64 || form == 128 ||
+                         form == 256;
+    if (n < 1 || batch < 1 || !ok_form || (form == -1 && hermitian)) return RCWA_EINVAL;
+    set_tuned_eig_form(hermitian ? 1 : 0, n, batch, form);
+    return RCWA_OK;
+}
+
+int rcwa_gpu_autotune_table(char* buffer, size_t size) {
+    try {
+        const std::string t = autotune_table_text();
+        if (buffer && size) {
+            std::strncpy(buffer, t.c_str(), size - 1);
+            buffer[size - 1] = '\0';
+        }
+        return (int)t.size();
+    } catch (...) {
+        return RCWA_ENOMEM;
+    }
+}
+
 int rcwa_gpu_gemm_info(int* tensor_cores, int* slices, int* stuck) {
     try {
         if (tensor_cores) *tensor_cores = tc_gemm_enabled() ? 1 : 0;

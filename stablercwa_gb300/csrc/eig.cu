@@ -31,6 +31,10 @@ int eig_default_group(int n, int batch) {
 void launch_eig(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info, int* sweeps,
                 zc* ws, double eps, int max_iter, int group, const int* skip, int skip_value, zc* t_out) {
     if (batch <= 0 || n <= 0) return;
+    if (group == 0 && !skip && !t_out) {
+        if (autotune_wanted(0, n, batch)) autotune_eig(st, 0, n, batch, a, a_stride, nullptr);
+        group = tuned_eig_form(0, n, batch);
+    }
     if (group == -1 || (group == 0 && eig_cluster_wanted(n, batch))) {
         TimedLaunch timed(TK_EIG, st);
         launch_eig_cluster(st, n, batch, a, a_stride, w, v, info, sweeps, ws, eps, max_iter, skip, skip_value, t_out);
@@ -132,6 +136,10 @@ void herm_fused_dispatch(cudaStream_t st, int n, int batch, const zc* a, long lo
 void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info, zc* ws,
                      double eps, int max_iter, int group) {
     if (batch <= 0 || n <= 0) return;
+    if (group == 0) {
+        if (autotune_wanted(1, n, batch)) autotune_eig(st, 1, n, batch, a, a_stride, nullptr);
+        group = tuned_eig_form(1, n, batch);
+    }
     if (group <= 0) group = eig_default_group(n, batch);
     TimedLaunch timed(TK_EIG, st);
     const size_t ysm = (size_t)n * kHermRows * sizeof(double);

@@ -80,6 +80,14 @@ void launch_lu_solve(cudaStream_t st, int n, int nrhs, int batch, const zc* a, l
 void launch_zgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride, const zc* B,
                   int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc, long long c_stride,
                   double s_ab, double s_c, const int* skip = nullptr, int skip_value = 1, int tri = 0);
+// The eigensolver's form per (kind 0 general / 1 Hermitian, order, batch) from timing (autotune.cu): the
+// tuned form, 0 when none is recorded; autotune_eig times every applicable form on the given matrices and
+// records the fastest (returns it; best_ms its time if non-null).
+int tuned_eig_form(int kind, int n, int batch);
+bool autotune_wanted(int kind, int n, int batch);
+int autotune_eig(cudaStream_t st, int kind, int n, int batch, const zc* a, long long a_stride, double* best_ms);
+void set_tuned_eig_form(int kind, int n, int batch, int form);
+std::string autotune_table_text();
 // One matrix per thread-block cluster (eig_cluster.cu) for a few large matrices: the same algorithm as
 // launch_eig's kernels, spread over 8 or 16 SMs. launch_eig takes it by itself (eig_cluster_wanted).
 bool eig_cluster_wanted(int n, int batch);

@@ -95,6 +95,9 @@ def load_library(build_if_missing=True):
     L.rcwa_gpu_solve_batch.argtypes = [vp, ci, ci, ci, vp, vp, vp, vp]
     L.rcwa_gpu_multiply_batch.argtypes = [vp, ci, ci, ci, ci, vp, vp, vp]
     L.rcwa_gpu_gemm_info.argtypes = [vp, vp, vp]
+    L.rcwa_gpu_autotune_eig.argtypes = [vp, ci, ci, ci, vp, vp, vp]
+    L.rcwa_gpu_autotune_set.argtypes = [ci, ci, ci, ci]
+    L.rcwa_gpu_autotune_table.argtypes = [vp, C.c_size_t]
     _lib = L
     return L
 
@@ -431,6 +434,13 @@ class Engine:
                          max_iter=30):
         self._check(self.L.rcwa_gpu_eig_batch_dev(self.h, n, batch, d_a, eps, max_iter, d_w, d_v, d_info, d_sweeps))
 
+    def autotune_eig(self, n, batch, d_a, hermitian=False):
+        """Time every eigensolver form on `batch` device matrices at d_a and record the fastest
+        (rcwa_gpu_autotune_eig): (form, milliseconds)."""
+        form, ms = C.c_int(), C.c_double()
+        self._check(self.L.rcwa_gpu_autotune_eig(self.h, 1 if hermitian else 0, n, batch, d_a, C.byref(form), C.byref(ms)))
+        return form.value, ms.value
+
     def eig_hermitian_batch(self, a, eps=float(np.finfo(np.float64).eps), max_iter=30):
         """Hermitian part of a: (batch, n, n). Returns values (batch, n) real, unsorted; vectors (batch, n, n)
         with orthonormal columns; info (batch,)."""
@@ -469,6 +479,20 @@ class Engine:
         c = np.empty((batch, n, m), np.complex128)
         self._check(self.L.rcwa_gpu_multiply_batch(self.h, m, k, n, batch, ca.ctypes.data, cb.ctypes.data, c.ctypes.data))
         return c.transpose(0, 2, 1)
+
+
+def autotune_set(hermitian, n, batch, form):
+    """Record an eigensolver form for (solver, order, batch bucket) (rcwa_gpu_autotune_set); returns the code."""
+    return load_library().rcwa_gpu_autotune_set(1 if hermitian else 0, n, batch, form)
+
+
+def autotune_table():
+    """The autotuner's table as text lines "<general|hermitian> <order> <batch bucket> <form>"."""
+    L = load_library()
+    size = L.rcwa_gpu_autotune_table(None, 0)
+    buf = C.create_string_buffer(max(1, size + 1))
+    L.rcwa_gpu_autotune_table(buf, len(buf))
+    return buf.value.decode()
 
 
 def gemm_info():

@@ -70,3 +70,11 @@ def test_server_create_without_device_reports_error():
     from stablercwa_gb300.engine import Server
     with pytest.raises(EngineError):
         Server(slots=1)
+
+
+def test_autotune_set_validates_forms():
+    from stablercwa_gb300.engine import autotune_set, autotune_table
+    assert autotune_set(False, 77, 1000, 12) == -1      # not a kernel form
+    assert autotune_set(True, 77, 1000, -1) == -1       # no cluster form for the Hermitian solver
+    assert autotune_set(False, 77, 1000, 16) == 0
+    assert "general 77 512 16" in autotune_table()      # batch 1000 falls in the bucket of 512
