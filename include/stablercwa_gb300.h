@@ -113,8 +113,11 @@ typedef struct rcwa_result1d {
     int* status;               /* RCWA_SAMPLE_* */
     int* eig_info;             /* optional */
     int* n_eig;                /* optional */
-    int* n_dense_solve;        /* optional */
+    int* n_dense_solve;        /* optional: the reference's count of dense solves for the point */
     double* max_eig_residual;  /* optional, filled when options.diagnostics */
+    int* n_lu;                 /* optional: dense LU factorisations the engine itself ran for the point
+                                  (reduced seams need fewer than n_dense_solve; per-layer factorisations
+                                  shared by every point of the call are not counted) */
 } rcwa_result1d;
 
 /* One conical sweep point (include/stablercwa/rcwa1d_conical.hpp:186). */
@@ -136,7 +139,7 @@ typedef struct rcwa_result_conical {
     int* status;                   /* RCWA_SAMPLE_* */
     int* eig_info;                 /* optional */
     int* n_eig;                    /* optional */
-    int* n_dense_solve;            /* optional */
+    int* n_dense_solve;            /* optional: the reference's count */
     int* n_schur;                  /* optional: layers switched to Schur propagation */
     double* min_abs_lambda;        /* optional */
     int* degenerate_mode_warning;  /* optional */
@@ -144,6 +147,8 @@ typedef struct rcwa_result_conical {
     double* ky;                    /* optional, n_points */
     double* flux_r;                /* optional, n_points * n */
     double* flux_t;                /* optional, n_points * n */
+    int* n_lu;                     /* optional: dense LU factorisations the engine ran for the point (as in
+                                      rcwa_result1d) */
 } rcwa_result_conical;
 
 /* ---- 2-D crossed gratings ------------------------------------------------------------------ */

@@ -76,6 +76,7 @@ class rcwa_result1d(C.Structure):
         ("n_eig", C.c_void_p),
         ("n_dense_solve", C.c_void_p),
         ("max_eig_residual", C.c_void_p),
+        ("n_lu", C.c_void_p),
     ]
 
 
@@ -86,7 +87,7 @@ class rcwa_point_conical(C.Structure):
 class rcwa_result_conical(C.Structure):
     _fields_ = [(name, C.c_void_p) for name in (
         "Jr", "Jt", "DEr", "DEt", "status", "eig_info", "n_eig", "n_dense_solve", "n_schur", "min_abs_lambda",
-        "degenerate_mode_warning", "kx", "ky", "flux_r", "flux_t")]
+        "degenerate_mode_warning", "kx", "ky", "flux_r", "flux_t", "n_lu")]
 
 
 class rcwa_gpu_config(C.Structure):
@@ -148,6 +149,7 @@ def result_views(n_points, M, with_diag=True):
         "n_eig": np.empty(n_points, np.int32),
         "n_dense_solve": np.empty(n_points, np.int32),
         "max_eig_residual": np.zeros(n_points, np.float64),
+        "n_lu": np.empty(n_points, np.int32),
     }
     res = rcwa_result1d()
     for name, arr in arrays.items():
@@ -174,6 +176,7 @@ def conical_views(n_points, M):
         "ky": np.empty(n_points, np.float64),
         "flux_r": np.empty((n_points, n), np.float64),
         "flux_t": np.empty((n_points, n), np.float64),
+        "n_lu": np.empty(n_points, np.int32),
     }
     res = rcwa_result_conical()
     for name, arr in arrays.items():

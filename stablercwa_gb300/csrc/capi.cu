@@ -124,6 +124,7 @@ void solve_both(rcwa_gpu_ctx* ctx, const rcwa_stack1d& stack, const double* ds, 
     tm.eig_info = d_out.eig_info ? d_out.eig_info + n_points : nullptr;
     tm.n_eig = d_out.n_eig ? d_out.n_eig + n_points : nullptr;
     tm.n_dense_solve = d_out.n_dense_solve ? d_out.n_dense_solve + n_points : nullptr;
+    tm.n_lu = d_out.n_lu ? d_out.n_lu + n_points : nullptr;
     tm.max_eig_residual = d_out.max_eig_residual ? d_out.max_eig_residual + n_points : nullptr;
     const size_t cb = chunk_bytes(ctx) / 2;
     std::exception_ptr tm_error;
@@ -327,6 +328,7 @@ int rcwa_gpu_solve1d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const r
         d.n_eig = mem.get<int>(np);
         d.n_dense_solve = mem.get<int>(np);
         d.max_eig_residual = opt.diagnostics ? mem.zeros<double>(np) : nullptr;
+        d.n_lu = out->n_lu ? mem.get<int>(np) : nullptr;
         if (both) solve_both(ctx, *stack, ds, dw, n_points, M, opt, d);
         else solve1d_device(st, *stack, ds, dw, n_points, M, polarization, opt, d, chunk_bytes(ctx));
         copy_back(out->R, d.R, nv, st);
@@ -337,6 +339,7 @@ int rcwa_gpu_solve1d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const r
         copy_back(out->eig_info, d.eig_info, np, st);
         copy_back(out->n_eig, d.n_eig, np, st);
         copy_back(out->n_dense_solve, d.n_dense_solve, np, st);
+        if (out->n_lu) copy_back(out->n_lu, d.n_lu, np, st);
         if (opt.diagnostics) copy_back(out->max_eig_residual, d.max_eig_residual, np, st);
         RCWA_CUDA(cudaStreamSynchronize(st));
     });
@@ -446,6 +449,7 @@ void conical_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_poin
     d.eig_info = mem.get<int>(n_points);
     d.n_eig = mem.get<int>(n_points);
     d.n_dense_solve = mem.get<int>(n_points);
+    d.n_lu = out->n_lu ? mem.get<int>(n_points) : nullptr;
     d.n_schur = mem.get<int>(n_points);
     d.min_abs_lambda = mem.get<double>(n_points);
     d.degenerate_mode_warning = mem.get<int>(n_points);
@@ -473,6 +477,7 @@ void conical_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_poin
     copy_back(out->eig_info, d.eig_info, n_points, st);
     copy_back(out->n_eig, d.n_eig, n_points, st);
     copy_back(out->n_dense_solve, d.n_dense_solve, n_points, st);
+    if (out->n_lu) copy_back(out->n_lu, d.n_lu, n_points, st);
     copy_back(out->n_schur, d.n_schur, n_points, st);
     copy_back(out->min_abs_lambda, d.min_abs_lambda, n_points, st);
     copy_back(out->degenerate_mode_warning, d.degenerate_mode_warning, n_points, st);
@@ -558,6 +563,7 @@ int rcwa_gpu_solve1d_fields(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const 
         d.eig_info = mem.get<int>(n_points);
         d.n_eig = mem.get<int>(n_points);
         d.n_dense_solve = mem.get<int>(n_points);
+        d.n_lu = out->n_lu ? mem.get<int>(n_points) : nullptr;
         FieldSpec fs;
         fs.zs.assign(zs, zs + nz);
         fs.out = nz > 0 ? mem.get<zc>(nf) : nullptr;
@@ -574,6 +580,7 @@ int rcwa_gpu_solve1d_fields(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const 
         copy_back(out->eig_info, d.eig_info, n_points, st);
         copy_back(out->n_eig, d.n_eig, n_points, st);
         copy_back(out->n_dense_solve, d.n_dense_solve, n_points, st);
+        if (out->n_lu) copy_back(out->n_lu, d.n_lu, n_points, st);
         if (nz > 0) copy_back(reinterpret_cast<zc*>(fields), fs.out, nf, st);
         RCWA_CUDA(cudaStreamSynchronize(st));
     });

@@ -655,15 +655,16 @@ __global__ void conical_finalize_kernel(int B, int N, int M, int pure_films, con
 
 __global__ void conical_status_kernel(int B, const int* __restrict__ fail, const int* __restrict__ eig_info,
                                       int base_eig, const int* __restrict__ schur_count, int base_solves,
-                                      const double* __restrict__ min_abs, const double* __restrict__ ky, int* status,
-                                      int* info_out, int* n_eig, int* n_solve, int* n_schur, double* min_abs_out,
-                                      int* warning) {
+                                      int base_lu, const double* __restrict__ min_abs, const double* __restrict__ ky,
+                                      int* status, int* info_out, int* n_eig, int* n_solve, int* n_lu, int* n_schur,
+                                      double* min_abs_out, int* warning) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
     if (status) status[b] = fail[b] ? (eig_info[b] ? RCWA_SAMPLE_EIG_NOCONV : RCWA_SAMPLE_NUMERICAL) : RCWA_SAMPLE_OK;
     if (info_out) info_out[b] = eig_info[b];
     if (n_eig) n_eig[b] = base_eig + schur_count[b];
     if (n_solve) n_solve[b] = base_solves;
+    if (n_lu) n_lu[b] = base_lu;
     if (n_schur) n_schur[b] = schur_count[b];
     if (min_abs_out) min_abs_out[b] = min_abs[b];
     if (warning) {
@@ -1685,9 +1686,10 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                reinterpret_cast<zc*>(d_out.Jt) + (long long)p0 * N * 4, d_out.DEr + (long long)p0 * N * 4,
                d_out.DEt + (long long)p0 * N * 4);
         LAUNCH(conical_status_kernel, nblocks(B), kTpb, st, B, c.fail, eig_info, 2 * (int)grating.size(), schur_count,
-               c.n_solve, min_abs, P.ky, d_out.status ? d_out.status + p0 : nullptr,
+               c.n_solve, c.n_lu, min_abs, P.ky, d_out.status ? d_out.status + p0 : nullptr,
                d_out.eig_info ? d_out.eig_info + p0 : nullptr, d_out.n_eig ? d_out.n_eig + p0 : nullptr,
-               d_out.n_dense_solve ? d_out.n_dense_solve + p0 : nullptr, d_out.n_schur ? d_out.n_schur + p0 : nullptr,
+               d_out.n_dense_solve ? d_out.n_dense_solve + p0 : nullptr, d_out.n_lu ? d_out.n_lu + p0 : nullptr,
+               d_out.n_schur ? d_out.n_schur + p0 : nullptr,
                d_out.min_abs_lambda ? d_out.min_abs_lambda + p0 : nullptr,
                d_out.degenerate_mode_warning ? d_out.degenerate_mode_warning + p0 : nullptr);
         if (fields) {

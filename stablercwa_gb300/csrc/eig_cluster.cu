@@ -14,7 +14,8 @@
 //     cluster barriers per column;
 //   * the reflectors are accumulated into Z column by column by each column's owner (no barrier);
 //   * each QR sweep: the leader CTA runs the rotation chain on the active window only (one CTA barrier
-//     per rotation; a rotation needs just the column it zeroes), logging the rotations in its shared
+//     per rotation; a rotation needs just the column it zeroes; each thread carries its columns' current
+//     row in registers and loads the next one a step ahead), logging the rotations in its shared
 //     memory; then every CTA reads the log (DSMEM) and applies it to its share of the work that does not
 //     feed the chain: H's rows 0..en from the right, the columns right of the window from the left, and
 //     all rows of Z; two cluster barriers per sweep;
@@ -37,6 +38,7 @@ namespace {
 
 constexpr int kCT = 512;  // threads per CTA
 constexpr int kWarps = kCT / 32;
+constexpr int kMaxCarry = 4;  // window columns per thread in the leader's chain: orders up to 4 kCT
 
 __device__ __forceinline__ unsigned cl_rank() {
     unsigned r;
@@ -366,9 +368,23 @@ __global__ void __launch_bounds__(kCT, 1)
                     *p = *p - s;
                 }
                 __syncthreads();
-                // the chain: rotation i from column i - 1, applied to window columns i..en; the owner of
-                // column i forms rotation i + 1 as soon as rotation i has reached it
-                if (t == l % kCT) {
+                // the chain: rotation i from column i - 1, applied to window columns i..en. Thread t owns the
+                // window columns c = l + 1 + t + k kCT; each keeps its column's current row i - 1 (cy) and the
+                // next row i (cz, loaded one step ahead) in registers, so a step stores one entry per column
+                // and reads none; the owner of column i forms rotation i + 1 from its carried row and the
+                // subdiagonal entry it loaded a step ahead (csub).
+                const int c_first = l + 1;
+                zc cy[kMaxCarry], cz[kMaxCarry];
+                double csub = 0.0;
+#pragma unroll
+                for (int k = 0; k < kMaxCarry; ++k) {
+                    const int c = c_first + t + k * kCT;
+                    if (c <= en) {
+                        cy[k] = H[(long long)c * n + l];
+                        cz[k] = H[(long long)c * n + l + 1];
+                    }
+                }
+                if (t == 0) {
                     zc* cp = H + (long long)l * n;
                     zc top;
                     const Rot q = make_rotation(cp[l], cp[l + 1].re, top);
@@ -377,25 +393,35 @@ __global__ void __launch_bounds__(kCT, 1)
                     rcr[l + 1] = q.cr;
                     rci[l + 1] = q.ci;
                     rs[l + 1] = q.s;
+                    if (c_first < en) csub = H[(long long)c_first * n + c_first + 1].re;
                 }
                 __syncthreads();
                 for (int i = l + 1; i <= en; ++i) {
                     const double cr = rcr[i], ci = rci[i], sn = rs[i];
-                    for (int c = i + ((t - i) % kCT + kCT) % kCT; c <= en; c += kCT) {
+#pragma unroll
+                    for (int k = 0; k < kMaxCarry; ++k) {
+                        const int c = c_first + t + k * kCT;
+                        if (c < i || c > en) continue;
                         zc* col = H + (long long)c * n;
-                        zc y = col[i - 1], z = col[i];
+                        zc y = cy[k], z = cz[k];
                         rot_left(cr, ci, sn, y, z);
                         col[i - 1] = y;
-                        if (c == i && i < en) {
-                            zc top;
-                            const Rot q = make_rotation(z, col[i + 1].re, top);
-                            col[i] = top;
-                            col[i + 1] = zc{0.0, 0.0};
-                            rcr[i + 1] = q.cr;
-                            rci[i + 1] = q.ci;
-                            rs[i + 1] = q.s;
+                        if (c == i) {
+                            if (i < en) {
+                                zc top;
+                                const Rot q = make_rotation(z, csub, top);
+                                col[i] = top;
+                                col[i + 1] = zc{0.0, 0.0};
+                                rcr[i + 1] = q.cr;
+                                rci[i + 1] = q.ci;
+                                rs[i + 1] = q.s;
+                            } else {
+                                col[i] = z;
+                            }
                         } else {
-                            col[i] = z;
+                            cy[k] = z;
+                            cz[k] = col[i + 1];
+                            if (c == i + 1 && i + 1 < en) csub = col[i + 2].re;
                         }
                     }
                     __syncthreads();
@@ -579,7 +605,7 @@ int cluster_size_for(int n) {
     if (n == cached_n) return cached_c;
     const size_t smem = eig_cluster_smem_bytes(n);
     int c = 0;
-    if (smem <= 200 * 1024 &&
+    if (smem <= 200 * 1024 && n <= kMaxCarry * kCT &&
         cudaFuncSetAttribute(eig_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess &&
         cudaFuncSetAttribute(eig_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
         for (int want : {16, 8}) {

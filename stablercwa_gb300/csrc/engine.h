@@ -99,6 +99,9 @@ void launch_eig_cluster(cudaStream_t st, int n, int batch, const zc* a, long lon
 void launch_zgemm_tc(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride,
                      const zc* B, int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc,
                      long long c_stride, double s_ab, double s_c, const int* skip = nullptr, int skip_value = 1);
+void launch_zdgemm_tc(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride,
+                      const double* B, int ldb, long long b_stride, zc* C, int ldc, long long c_stride,
+                      const int* skip = nullptr, int skip_value = 1);
 bool tc_gemm_enabled();
 // Products launched by this host thread while a guard lives stay on the FP64 pipe (the 2-D solve: its
 // operands span many decades within a row or column, where an FP64 product's error, relative to the

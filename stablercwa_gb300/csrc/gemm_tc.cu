@@ -14,17 +14,18 @@
 //     an integer below 2^24, exact in the FP32 accumulator. Digit pairs (s, t) with s + t <= S + 1 are
 //     kept (the dropped ones lie below 2^-8S of the product's scale); pairs of one diagonal s + t share
 //     a scale factor 2^(-14 - 8 (s + t - 2)), so up to 1024 / K of them accumulate in one exact FP32
-//     tensor-memory accumulator (a "group") before it is added into FP64.
+//     tensor-memory accumulator (a "group") before it is added, exactly, into an int64 per element.
 // Per element the result is exact up to the digit truncation (relative 2^-8S of max|A(i,:)| max|B(:,j)|
-// times k) and the FP64 additions of the group sums: FP64-level accuracy with S = 7.
+// times k) and one final rounding: FP64-level accuracy with S = 7.
 //
 // Kernels. The split kernels write the digit planes in HBM as bf16 rows with K contiguous (K-major for
 // both operands). The product kernel gives each CTA one 128 x 128 tile of C^ of one matrix: one warp
 // issues TMA loads (128-byte swizzle, boxes of 128 rows x 64 K) into a 4-stage shared-memory ring; one
 // thread issues tcgen05.mma (M = 128, N = 128, K = 16, bf16 in, FP32 out) into one of two 128-column
-// tensor-memory accumulators; eight warps read each finished group out of tensor memory (tcgen05.ld),
-// scale it and add it into FP64 registers while the next group accumulates in the other buffer, then
-// apply 2^(ea + eb), pair the real and imaginary rows and write C. Every mbarrier wait is bounded: on
+// tensor-memory accumulators; eight warps read each finished group out of tensor memory (tcgen05.ld) and
+// add it, as an integer at its diagonal's weight, into one int64 per element while the next group
+// accumulates in the other buffer, then convert once, apply 2^(ea + eb), pair the real and imaginary rows
+// and write C. Every mbarrier wait is bounded: on
 // expiry the kernel records an error, drains its own copies and products, frees its tensor memory and
 // returns without writing C.
 #include <cuda.h>
@@ -55,6 +56,7 @@ constexpr unsigned kWaitLimit = 1u << 22;  // try_wait rounds before a wait is d
 struct Plan {
     int n_groups;
     int S;
+    int s0;  // the int64 accumulator holds the product in units of 2^(-14 - s0) (diagonal d enters times 2^(s0 - 8 (d - 2)))
     unsigned g[kMaxGroups];  // d | i0 << 4 | ni << 8 | kb0 << 12 | nkb << 22
 };
 __host__ __device__ inline int g_d(unsigned v) { return v & 15; }
@@ -146,39 +148,66 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 // ---------------------------------------------------------------- digit split
 
 // exponent e with max = f 2^e, f in [0.5, 1); 0 for 0 or a non-finite max (the digits then carry it)
+// A row of A or column of B holding a non-finite entry gets this exponent: its digits come out zero and
+// the epilogue writes NaN for every element of C it touches (any such product is non-finite in FP64 too).
+constexpr int kNonFinite = 1 << 20;
+
+// the scale exponent of a row or column from its largest magnitude (+inf when it holds a non-finite entry)
 __device__ __forceinline__ int scale_exponent(double mx) {
-    if (!(mx > 0.0) || !isfinite(mx)) return 0;
+    if (!isfinite(mx)) return kNonFinite;
+    if (!(mx > 0.0)) return 0;
     int e;
     frexp(mx, &e);
     return e;
 }
 
-// the S digits of y in (-1, 1): bf16 bit patterns of exact small integers
-__device__ __forceinline__ void store_digits(double y, int S, uint16_t* out, long long plane_stride) {
-    double t = y * 128.0;
+// bf16 bit pattern of a small integer (exact: |d| <= 256)
+__device__ __forceinline__ uint16_t bf16_int(long long d) { return (uint16_t)(__float_as_uint((float)d) >> 16); }
+
+// The S digits of x 2^-e (|x 2^-e| < 1), integer arithmetic: Y = x 2^(62 - e) is the value to 62 fractional
+// bits (an int64 below 2^62, so adding the rounding half never overflows); digit s (from 0) is Y rounded at
+// bit 55 - 8 s and taken out of Y before the next, so each lies in [-128, 128] and carries weight
+// 2^(-7 - 8 s); an eighth digit is the remainder itself, in units of 2^-63. A non-finite x (whose row or
+// column then carries kNonFinite) gives zero digits.
+__device__ __forceinline__ void store_digits(double x, int e, int S, uint16_t* out, long long plane_stride) {
+    if (!isfinite(x) || e == kNonFinite) {
+        for (int s = 0; s < S; ++s) out[s * plane_stride] = 0;
+        return;
+    }
+    long long Y = __double2ll_rn(ldexp(x, 62 - e));
 #pragma unroll 1
     for (int s = 0; s < S; ++s) {
-        const double d = rint(t);
-        out[s * plane_stride] = (uint16_t)(__float_as_uint((float)d) >> 16);
-        t = (t - d) * 256.0;
+        const int sh = 55 - 8 * s;
+        long long d;
+        if (sh > 0) {
+            d = (Y + (1LL << (sh - 1))) >> sh;
+            Y -= d * (1LL << sh);
+        } else {
+            d = Y * (1LL << -sh);
+            Y = 0;
+        }
+        out[s * plane_stride] = bf16_int(d);
     }
 }
 
 // A (m x k, column-major, lda) of matrix blockIdx.y -> S planes of A^ (2m rows x Kp, K contiguous) and
-// ea[i]; one CTA per 32 rows of A
-__global__ void __launch_bounds__(256) tc_split_a_kernel(int m, int k, int Kp, int S, const zc* __restrict__ A, int lda,
-                                                         long long a_stride, uint16_t* __restrict__ out,
+// ea[i]; one CTA per 32 rows of A. Complex B (real_b = 0): rows 2i, 2i+1 = [Re A(i,:), -Im A(i,:)] and
+// [Im A(i,:), Re A(i,:)] over K = 2k; real B (real_b = 1): rows [Re A(i,:)] and [Im A(i,:)] over K = k.
+// A is read through a shared-memory tile (coalesced along the rows) and written row by row.
+__global__ void __launch_bounds__(256) tc_split_a_kernel(int m, int k, int Kp, int S, int real_b, const zc* __restrict__ A,
+                                                         int lda, long long a_stride, uint16_t* __restrict__ out,
                                                          int* __restrict__ ea) {
     const long long b = blockIdx.y;
     const int i0 = blockIdx.x * 32, t = threadIdx.x, il = t & 31, w = t >> 5;
     const zc* As = A + b * a_stride;
     __shared__ double smax[8][32];
     __shared__ int sexp[32];
+    __shared__ zc tile[32][33];
     double mx = 0.0;
     if (i0 + il < m)
         for (int kk = w; kk < k; kk += 8) {
             const zc v = As[(long long)kk * lda + i0 + il];
-            mx = fmax(mx, fmax(fabs(v.re), fabs(v.im)));
+            mx = (isfinite(v.re) && isfinite(v.im)) ? fmax(mx, fmax(fabs(v.re), fabs(v.im))) : INFINITY;
         }
     smax[w][il] = mx;
     __syncthreads();
@@ -190,42 +219,66 @@ __global__ void __launch_bounds__(256) tc_split_a_kernel(int m, int k, int Kp, i
     __syncthreads();
     const long long rows = 2LL * m, plane = rows * Kp;
     uint16_t* o = out + b * S * plane;
-    for (int idx = t; idx < 64 * Kp; idx += 256) {
-        const int rr = idx / Kp, kk = idx - rr * Kp;
+    const int kin = real_b ? k : 2 * k;  // K of the product before padding
+    for (int kc = 0; kc < k; kc += 32) {
+        for (int q = w; q < 32; q += 8) {
+            const int kk = kc + q, i = i0 + il;
+            tile[il][q] = (kk < k && i < m) ? As[(long long)kk * lda + i] : zc{0.0, 0.0};
+        }
+        __syncthreads();
+        for (int idx = t; idx < 64 * 32; idx += 256) {
+            const int rr = idx >> 5, c = idx & 31, kk = kc + c;
+            const int i = i0 + (rr >> 1), part = rr & 1;
+            if (i >= m || kk >= k) continue;
+            const zc v = tile[rr >> 1][c];
+            const int e = sexp[rr >> 1];
+            uint16_t* row = o + (2LL * i + part) * Kp;
+            store_digits(part ? v.im : v.re, e, S, row + kk, plane);
+            if (!real_b) store_digits(part ? v.re : -v.im, e, S, row + k + kk, plane);
+        }
+        __syncthreads();
+    }
+    for (int idx = t; idx < 64 * (Kp - kin); idx += 256) {  // zero padding of K
+        const int rr = idx / (Kp - kin), kk = kin + idx - rr * (Kp - kin);
         const int i = i0 + (rr >> 1), part = rr & 1;
         if (i >= m) continue;
-        double x = 0.0;
-        if (kk < k) {
-            const zc v = As[(long long)kk * lda + i];
-            x = part ? v.im : v.re;
-        } else if (kk < 2 * k) {
-            const zc v = As[(long long)(kk - k) * lda + i];
-            x = part ? v.re : -v.im;
-        }
-        store_digits(ldexp(x, -sexp[rr >> 1]), S, o + (2LL * i + part) * Kp + kk, plane);
+        uint16_t* cell = o + (2LL * i + part) * Kp + kk;
+        for (int s2 = 0; s2 < S; ++s2) cell[s2 * plane] = 0;
     }
 }
 
-// B (k x n, column-major, ldb) -> S planes of B^t (n rows x Kp: [Re B(:, j); Im B(:, j)]) and eb[j];
-// one warp per column
+// B (k x n, column-major, ldb) -> S planes of B^t (n rows x Kp) and eb[j]; one warp per column. Complex B:
+// [Re B(:, j); Im B(:, j)]; real B (Br, double): B(:, j).
 __global__ void __launch_bounds__(128) tc_split_b_kernel(int n, int k, int Kp, int S, int batch, const zc* __restrict__ B,
-                                                         int ldb, long long b_stride, uint16_t* __restrict__ out,
-                                                         int* __restrict__ eb) {
+                                                         const double* __restrict__ Br, int ldb, long long b_stride,
+                                                         uint16_t* __restrict__ out, int* __restrict__ eb) {
     const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (gw >= (long long)batch * n) return;
     const long long b = gw / n;
     const int j = (int)(gw - b * n), lane = threadIdx.x & 31;
-    const zc* col = B + b * b_stride + (long long)j * ldb;
     double mx = 0.0;
-    for (int kk = lane; kk < k; kk += 32) mx = fmax(mx, fmax(fabs(col[kk].re), fabs(col[kk].im)));
+    if (Br) {
+        const double* col = Br + b * b_stride + (long long)j * ldb;
+        for (int kk = lane; kk < k; kk += 32) mx = isfinite(col[kk]) ? fmax(mx, fabs(col[kk])) : INFINITY;
+    } else {
+        const zc* col = B + b * b_stride + (long long)j * ldb;
+        for (int kk = lane; kk < k; kk += 32)
+            mx = (isfinite(col[kk].re) && isfinite(col[kk].im)) ? fmax(mx, fmax(fabs(col[kk].re), fabs(col[kk].im))) : INFINITY;
+    }
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     const int e = scale_exponent(mx);
     if (lane == 0) eb[b * n + j] = e;
     const long long plane = (long long)n * Kp;
     uint16_t* o = out + b * S * plane + (long long)j * Kp;
     for (int kk = lane; kk < Kp; kk += 32) {
-        const double x = kk < k ? col[kk].re : (kk < 2 * k ? col[kk - k].im : 0.0);
-        store_digits(ldexp(x, -e), S, o + kk, plane);
+        double x;
+        if (Br) {
+            x = kk < k ? Br[b * b_stride + (long long)j * ldb + kk] : 0.0;
+        } else {
+            const zc* col = B + b * b_stride + (long long)j * ldb;
+            x = kk < k ? col[kk].re : (kk < 2 * k ? col[kk - k].im : 0.0);
+        }
+        store_digits(x, e, S, o + kk, plane);
     }
 }
 
@@ -360,9 +413,15 @@ __global__ void __launch_bounds__(kThreads, 1)
     } else {
         // ---- epilogue: warps 2..9; lane quarter q of tensor memory, column half h
         const int q = warp & 3, h = (warp - 2) >> 2;
-        double acc[64];
+        // Every group sum is an integer below 2^24 (exact in the FP32 accumulator). They are added into one
+        // int64 per element in units of 2^(-14 - s0): diagonal d enters times 2^(s0 - 8 (d - 2)), exactly
+        // while that shift is >= 0, else rounded right (half a unit per group at most); s0 = 47 - log2(Kp)
+        // keeps the whole sum below 2^62, so the unit is 2^-53 of the row-and-column scale for K = 256.
+        // Integer sums are exact in any order; the element is then (double) acc 2^(ea + eb - 14 - s0), one
+        // rounding.
+        long long acc[64];
 #pragma unroll
-        for (int c = 0; c < 64; ++c) acc[c] = 0.0;
+        for (int c = 0; c < 64; ++c) acc[c] = 0;
         bool ok = true;
         for (int gi = 0; gi < plan.n_groups; ++gi) {
             const int buf = gi & 1;
@@ -371,14 +430,20 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (!ok) break;
             tc_fence_after();
             const int d = g_d(plan.g[gi]);
-            const double scale = ldexp(1.0, -14 - 8 * (d - 2));
+            const int sh = plan.s0 - 8 * (d - 2);
+            const long long mul = sh >= 0 ? (1LL << sh) : 1LL;
+            const int rsh = sh >= 0 ? 0 : -sh;
+            const long long half = rsh ? (1LL << (rsh - 1)) : 0LL;
             const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + buf * kTileN + h * 64;
 #pragma unroll
             for (int c16 = 0; c16 < 4; ++c16) {
                 float v[16];
                 tmem_ld16(base + c16 * 16, v);
 #pragma unroll
-                for (int j = 0; j < 16; ++j) acc[c16 * 16 + j] = fma((double)v[j], scale, acc[c16 * 16 + j]);
+                for (int j = 0; j < 16; ++j) {
+                    const long long gv = (long long)__float2int_rn(v[j]);
+                    acc[c16 * 16 + j] += (gv * mul + half) >> rsh;  // mul = 1 or half = rsh = 0
+                }
             }
             tc_fence_before();
             __syncwarp();
@@ -396,7 +461,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int c = 0; c < 64; ++c) {
                 const int col = n0 + h * 64 + c;
                 const int e = col < n ? er + ebs[col] : 0;
-                const double v = ldexp(acc[c], e);
+                const double v = e >= kNonFinite / 2 ? __longlong_as_double(0x7FF8000000000000LL)
+                                                     : ldexp((double)acc[c], e - 14 - plan.s0);
                 const double im = __shfl_down_sync(0xffffffffu, v, 1);
                 if (writer && col < n) {
                     zc out{s_ab * v, s_ab * im};
@@ -457,6 +523,9 @@ CUtensorMap plane_map(const uint16_t* base, long long rows, int Kp, long long pl
 Plan make_plan(int S, int kblocks) {
     Plan p{};
     p.S = S;
+    int lg = 0;
+    while ((1 << lg) < kblocks * kTileK) ++lg;
+    p.s0 = 47 - lg;
     const int chunk_kb = 1024 / kTileK;
     for (int d = S + 1; d >= 2; --d) {
         const int lo = std::max(1, d - S), hi = std::min(S, d - 1);
@@ -516,9 +585,12 @@ int tc_gemm_error() {
     return h;
 }
 
-void launch_zgemm_tc(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride,
-                     const zc* B, int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc,
-                     long long c_stride, double s_ab, double s_c, const int* skip, int skip_value) {
+namespace {
+
+// C = s_ab A B + s_c C0 with B complex (B) or real (Br)
+void tc_product(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride, const zc* B,
+                const double* Br, int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc,
+                long long c_stride, double s_ab, double s_c, const int* skip, int skip_value) {
     if (batch <= 0 || m <= 0 || n <= 0) return;
     const int smem_bytes = kStages * kStageBytes + 1024 + (int)sizeof(SharedState) + 64;
     static std::once_flag attr_once;
@@ -527,8 +599,10 @@ void launch_zgemm_tc(cudaStream_t st, int m, int n, int k, int batch, const zc* 
         attr_rc = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
     });
     RCWA_CUDA(attr_rc);
+    const int real_b = Br != nullptr;
     const int S = tc_gemm_slices();
-    const int Kp = ((2 * k + kTileK - 1) / kTileK) * kTileK;
+    const int kin = real_b ? k : 2 * k;
+    const int Kp = ((kin + kTileK - 1) / kTileK) * kTileK;
     const Plan plan = make_plan(S, Kp / kTileK);
     const bool a_bcast = a_stride == 0, b_bcast = b_stride == 0;
     const long long a_bytes = (long long)S * 2 * m * Kp * 2, b_bytes = (long long)S * n * Kp * 2;
@@ -547,23 +621,24 @@ void launch_zgemm_tc(cudaStream_t st, int m, int n, int k, int batch, const zc* 
     const CUtensorMap map_a = plane_map(pa, 2LL * m, Kp, (long long)na * S);
     const CUtensorMap map_b = plane_map(pb, n, Kp, (long long)nb * S);
     if (a_bcast) {
-        tc_split_a_kernel<<<dim3((m + 31) / 32, 1), 256, 0, st>>>(m, k, Kp, S, A, lda, 0, pa, dea);
+        tc_split_a_kernel<<<dim3((m + 31) / 32, 1), 256, 0, st>>>(m, k, Kp, S, real_b, A, lda, 0, pa, dea);
         ++launch_count();
     }
     if (b_bcast) {
-        tc_split_b_kernel<<<(unsigned)((n * 32LL + 127) / 128), 128, 0, st>>>(n, k, Kp, S, 1, B, ldb, 0, pb, deb);
+        tc_split_b_kernel<<<(unsigned)((n * 32LL + 127) / 128), 128, 0, st>>>(n, k, Kp, S, 1, B, Br, ldb, 0, pb, deb);
         ++launch_count();
     }
     for (int b0 = 0; b0 < batch; b0 += chunk) {
         const int cb = std::min(chunk, batch - b0);
         if (!a_bcast) {
-            tc_split_a_kernel<<<dim3((m + 31) / 32, cb), 256, 0, st>>>(m, k, Kp, S, A + (long long)b0 * a_stride, lda,
+            tc_split_a_kernel<<<dim3((m + 31) / 32, cb), 256, 0, st>>>(m, k, Kp, S, real_b, A + (long long)b0 * a_stride, lda,
                                                                         a_stride, pa, dea + (long long)b0 * m);
             ++launch_count();
         }
         if (!b_bcast) {
             tc_split_b_kernel<<<(unsigned)((cb * (long long)n * 32 + 127) / 128), 128, 0, st>>>(
-                n, k, Kp, S, cb, B + (long long)b0 * b_stride, ldb, b_stride, pb, deb + (long long)b0 * n);
+                n, k, Kp, S, cb, B ? B + (long long)b0 * b_stride : nullptr, Br ? Br + (long long)b0 * b_stride : nullptr,
+                ldb, b_stride, pb, deb + (long long)b0 * n);
             ++launch_count();
         }
         const dim3 grid((n + kTileN - 1) / kTileN, (2 * m + kTileM - 1) / kTileM, cb);
@@ -576,6 +651,22 @@ void launch_zgemm_tc(cudaStream_t st, int m, int n, int k, int batch, const zc* 
     RCWA_CUDA(cudaFreeAsync(pb, st));
     RCWA_CUDA(cudaFreeAsync(dea, st));
     RCWA_CUDA(cudaFreeAsync(deb, st));
+}
+
+}  // namespace
+
+void launch_zgemm_tc(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride,
+                     const zc* B, int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc,
+                     long long c_stride, double s_ab, double s_c, const int* skip, int skip_value) {
+    tc_product(st, m, n, k, batch, A, lda, a_stride, B, nullptr, ldb, b_stride, C0, c0_stride, C, ldc, c_stride, s_ab, s_c,
+               skip, skip_value);
+}
+
+void launch_zdgemm_tc(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride,
+                      const double* B, int ldb, long long b_stride, zc* C, int ldc, long long c_stride, const int* skip,
+                      int skip_value) {
+    tc_product(st, m, n, k, batch, A, lda, a_stride, nullptr, B, ldb, b_stride, nullptr, 0, C, ldc, c_stride, 1.0, 0.0,
+               skip, skip_value);
 }
 
 }  // namespace rcwa_gb300

@@ -93,6 +93,11 @@ constexpr int kPanel = 32;
 void zgemm_raw(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride, const zc* B,
                int ldb, long long b_stride, zc* C, int ldc, long long c_stride, double s_ab, const int* skip, int skip_value) {
     if (batch <= 0 || m <= 0 || n <= 0 || k <= 0) return;
+    if (k >= 32 && m >= 32 && n >= 32 && tc_gemm_enabled() && !Fp64ProductsGuard::active()) {
+        launch_zgemm_tc(st, m, n, k, batch, A, lda, a_stride, B, ldb, b_stride, C, c_stride, C, ldc, c_stride, s_ab, 1.0,
+                        skip, skip_value);
+        return;
+    }
     const long long warps = (long long)batch * ((m + 31) / 32) * ((n + 7) / 8);
     const unsigned blocks = (unsigned)((warps * 32 + 127) / 128);
     zgemm_kernel<<<blocks, 128, 0, st>>>(m, n, k, batch, A, lda, a_stride, B, ldb, b_stride, C, c_stride, C, ldc,
@@ -202,6 +207,10 @@ void launch_zdgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A,
                    const double* B, int ldb, long long b_stride, zc* C, int ldc, long long c_stride, const int* skip,
                    int skip_value) {
     if (batch <= 0 || m <= 0 || n <= 0) return;
+    if (k >= 32 && m >= 32 && n >= 32 && tc_gemm_enabled() && !Fp64ProductsGuard::active()) {
+        launch_zdgemm_tc(st, m, n, k, batch, A, lda, a_stride, B, ldb, b_stride, C, ldc, c_stride, skip, skip_value);
+        return;
+    }
     const long long warps = (long long)batch * ((m + 31) / 32) * ((n + 7) / 8);
     const unsigned blocks = (unsigned)((warps * 32 + 127) / 128);
     zdgemm_kernel<<<blocks, 128, 0, st>>>(m, n, k, batch, A, lda, a_stride, B, ldb, b_stride, C, ldc, c_stride, skip,

@@ -75,14 +75,16 @@ __global__ void finalize_kernel(int B, int n, int M, int pol, int pure_films, co
 }
 
 __global__ void status_kernel(int B, const int* __restrict__ fail, const int* __restrict__ eig_info, int base_solves,
-                              const int* __restrict__ extra_solves, int n_eig, int* __restrict__ status,
-                              int* __restrict__ info_out, int* __restrict__ n_eig_out, int* __restrict__ n_solve_out) {
+                              int base_lu, const int* __restrict__ extra_solves, int n_eig, int* __restrict__ status,
+                              int* __restrict__ info_out, int* __restrict__ n_eig_out, int* __restrict__ n_solve_out,
+                              int* __restrict__ n_lu_out) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
     if (status) status[b] = fail[b] ? (eig_info[b] ? RCWA_SAMPLE_EIG_NOCONV : RCWA_SAMPLE_NUMERICAL) : RCWA_SAMPLE_OK;
     if (info_out) info_out[b] = eig_info[b];
     if (n_eig_out) n_eig_out[b] = n_eig;
     if (n_solve_out) n_solve_out[b] = base_solves + extra_solves[b];
+    if (n_lu_out) n_lu_out[b] = base_lu + extra_solves[b];  // the flagged samples' extra solve is an LU here too
 }
 
 struct DModes {
@@ -768,9 +770,10 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
                modes[L + 1].q, k0, nI, nII, c.fail, reinterpret_cast<zc*>(d_out.R) + (long long)p0 * n,
                reinterpret_cast<zc*>(d_out.T) + (long long)p0 * n, d_out.DEr + (long long)p0 * n,
                d_out.DEt + (long long)p0 * n);
-        LAUNCH(status_kernel, nblocks(B), kTpb, st, B, c.fail, eig_info, c.n_solve, c.extra_solves, (int)grating.size(),
-               d_out.status ? d_out.status + p0 : nullptr, d_out.eig_info ? d_out.eig_info + p0 : nullptr,
-               d_out.n_eig ? d_out.n_eig + p0 : nullptr, d_out.n_dense_solve ? d_out.n_dense_solve + p0 : nullptr);
+        LAUNCH(status_kernel, nblocks(B), kTpb, st, B, c.fail, eig_info, c.n_solve, c.n_lu, c.extra_solves,
+               (int)grating.size(), d_out.status ? d_out.status + p0 : nullptr,
+               d_out.eig_info ? d_out.eig_info + p0 : nullptr, d_out.n_eig ? d_out.n_eig + p0 : nullptr,
+               d_out.n_dense_solve ? d_out.n_dense_solve + p0 : nullptr, d_out.n_lu ? d_out.n_lu + p0 : nullptr);
         if (fields && fields->layer_info)
             for (int k = 0; k < L; ++k)
                 LAUNCH(zero_q_count_kernel, nblocks(B), kTpb, st, B, n, modes[k + 1].q, fields->layer_info + (size_t)p0 * L + k, L);

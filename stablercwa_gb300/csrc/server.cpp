@@ -118,14 +118,14 @@ void put1(T* dst, T v) {
 struct Res1D {
     std::vector<rcwa_complex> R, T;
     std::vector<double> DEr, DEt;
-    int status = 0, eig_info = 0, n_eig = 0, n_dense = 0;
+    int status = 0, eig_info = 0, n_eig = 0, n_dense = 0, n_lu = 0;
     double resid = 0;
     rcwa_result1d view(int n) {
         R.resize(n);
         T.resize(n);
         DEr.resize(n);
         DEt.resize(n);
-        return rcwa_result1d{R.data(), T.data(), DEr.data(), DEt.data(), &status, &eig_info, &n_eig, &n_dense, &resid};
+        return rcwa_result1d{R.data(), T.data(), DEr.data(), DEt.data(), &status, &eig_info, &n_eig, &n_dense, &resid, &n_lu};
     }
     void out(rcwa_result1d* o) const {
         put(o->R, R);
@@ -137,13 +137,14 @@ struct Res1D {
         put1(o->n_eig, n_eig);
         put1(o->n_dense_solve, n_dense);
         put1(o->max_eig_residual, resid);
+        put1(o->n_lu, n_lu);
     }
 };
 
 struct ResConical {
     std::vector<rcwa_complex> Jr, Jt;
     std::vector<double> DEr, DEt, kx, flux_r, flux_t;
-    int status = 0, eig_info = 0, n_eig = 0, n_dense = 0, n_schur = 0, warn = 0;
+    int status = 0, eig_info = 0, n_eig = 0, n_dense = 0, n_schur = 0, warn = 0, n_lu = 0;
     double min_abs = 0, ky = 0;
     rcwa_result_conical view(int n) {
         Jr.resize(4 * n);
@@ -154,7 +155,7 @@ struct ResConical {
         flux_r.resize(n);
         flux_t.resize(n);
         return rcwa_result_conical{Jr.data(), Jt.data(), DEr.data(), DEt.data(), &status, &eig_info, &n_eig, &n_dense,
-                                   &n_schur, &min_abs, &warn, kx.data(), &ky, flux_r.data(), flux_t.data()};
+                                   &n_schur, &min_abs, &warn, kx.data(), &ky, flux_r.data(), flux_t.data(), &n_lu};
     }
     void out(rcwa_result_conical* o) const {
         put(o->Jr, Jr);
@@ -168,6 +169,7 @@ struct ResConical {
         put1(o->n_schur, n_schur);
         put1(o->min_abs_lambda, min_abs);
         put1(o->degenerate_mode_warning, warn);
+        put1(o->n_lu, n_lu);
         put(o->kx, kx);
         put1(o->ky, ky);
         put(o->flux_r, flux_r);

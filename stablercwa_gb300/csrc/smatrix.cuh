@@ -180,7 +180,8 @@ struct Batch {
     int B, n, M;
     int* fail;
     int* extra_solves;
-    int n_solve = 0;
+    int n_solve = 0;  // the reference's dense solves per sample (rcwa1d.hpp's count)
+    int n_lu = 0;     // the LU factorisations per sample this engine runs
     long long nn() const { return (long long)n * n; }
     zc* dense() { return mem->get<zc>((size_t)B * nn()); }
     zc* vec() { return mem->get<zc>((size_t)B * n); }
@@ -189,6 +190,7 @@ struct Batch {
 // linear_solve (include/stablercwa/rcwa1d.hpp:248-281): a zero pivot fails the sample.
 zc* solve(Batch& c, zc* a, bool consume_a, int rhs_kind, const zc* rhs, int nrhs = -1) {
     ++c.n_solve;
+    ++c.n_lu;
     if (nrhs < 0) nrhs = c.n;
     zc* x = c.mem->get<zc>((size_t)c.B * c.n * nrhs);
     zc* lu = consume_a ? a : c.dense();

@@ -170,7 +170,8 @@ class Engine:
 
     def solve1d_arrays(self, stack, points, M, pol, options=None):
         """Batched solve with host buffers; returns a dict of numpy arrays (R, T, DEr, DEt, status,
-        eig_info, n_eig, n_dense_solve, max_eig_residual). pol = 2 (RCWA_TE_TM): both polarizations,
+        eig_info, n_eig, n_dense_solve (the reference's count), max_eig_residual, n_lu (the engine's own LU
+        factorisations per point)). pol = 2 (RCWA_TE_TM): both polarizations,
         every array holding the TE rows then the TM rows (2 x points)."""
         st, keep = abi.marshal_stack1d(stack)
         pts = abi.points_array(points)
@@ -268,7 +269,7 @@ class Engine:
         pol = 2 (RCWA_TE_TM) solves both polarizations: every array holds TE results then TM results."""
         st, keep = abi.marshal_stack1d(stack)
         res = abi.rcwa_result1d()
-        for k in ("R", "T", "DEr", "DEt", "status", "eig_info", "n_eig", "n_dense_solve", "max_eig_residual"):
+        for k in ("R", "T", "DEr", "DEt", "status", "eig_info", "n_eig", "n_dense_solve", "max_eig_residual", "n_lu"):
             setattr(res, k, d_out.get(k))
         o = _options(options)
         self._check(self.L.rcwa_gpu_solve1d_batch_dev(self.h, C.byref(st), d_points, n_points, M, pol, C.byref(o),
@@ -304,7 +305,8 @@ class Engine:
         return [Result(orders=orders, R=a["R"][p], T=a["T"][p], DEr=a["DEr"][p], DEt=a["DEt"][p],
                        eig_info=int(a["eig_info"][p]), n_eig=int(a["n_eig"][p]),
                        n_dense_solve=int(a["n_dense_solve"][p]), status=int(a["status"][p]),
-                       max_eig_residual=float(a["max_eig_residual"][p])) for p in range(len(a["status"]))]
+                       max_eig_residual=float(a["max_eig_residual"][p]), n_lu=int(a["n_lu"][p]))
+                for p in range(len(a["status"]))]
 
     def solve(self, stack, wavelength, theta_deg, M, pol=0, options=None):
         return self.sweep(stack, [(wavelength, theta_deg)], M, pol, options)[0]
@@ -314,7 +316,7 @@ class Engine:
     def solve_conical_arrays(self, stack, points, M, options=None):
         """rcwa::sweep_conical over (wavelength, theta, phi) points: dict of numpy arrays with Jr, Jt
         (P, 2M+1, 4 complex: ss, sp, ps, pp), DEr, DEt (P, 2M+1, 4), status, eig_info, n_eig,
-        n_dense_solve, n_schur, min_abs_lambda, degenerate_mode_warning, kx, ky, flux_r, flux_t."""
+        n_dense_solve, n_schur, min_abs_lambda, degenerate_mode_warning, kx, ky, flux_r, flux_t, n_lu."""
         st, keep = abi.marshal_stack1d(stack)
         pts = abi.conical_points_array(points)
         res, arrays = abi.conical_views(len(pts), M)

@@ -60,9 +60,10 @@ class Result:
     DEt: np.ndarray
     eig_info: int = 0
     n_eig: int = 0
-    n_dense_solve: int = 0
+    n_dense_solve: int = 0  # the reference's count of dense solves
     status: int = 0
     max_eig_residual: float = 0.0
+    n_lu: int = 0  # LU factorisations the engine ran for this point (fewer than n_dense_solve with reduced seams)
 
     def reflectance(self):
         return float(np.sum(self.DEr))

@@ -1,5 +1,5 @@
 """The tensor-core complex product (csrc/gemm_tc.cu: Ozaki bf16 digit slices on tcgen05.mma, exact FP32
-group sums, FP64 accumulation) through rcwa_gpu_multiply_batch, the engine behind the reference's
+group sums, exact int64 accumulation) through rcwa_gpu_multiply_batch, the engine behind the reference's
 Options::custom_multiply hook (include/stablercwa/rcwa1d.hpp:125-129), against numpy's FP64 product:
 square and ragged shapes, K above one exact-accumulation chunk (2k > 1024), rows and columns scaled
 over hundreds of decades, zero rows, and non-finite entries, which must stay non-finite."""
