@@ -355,6 +355,8 @@ def run_ours(args):
         line_extra["plain"] = plain_rate(eng, stack, pts, args.plain_points, value)
     if rank == 0 and args.lossy_steps > 0:
         line_extra["lossy_c2"] = lossy_rate(eng, torch, est, flush, args, peak)
+    if rank == 0 and args.serve_sample > 0:
+        line_extra["serving"] = serving_sample(args)
 
     # ---- accuracy and CPU baseline (rank 0): the oracle on a bounded sample of the same points
     if rank == 0:
@@ -754,6 +756,23 @@ def serve_run(reqs, slots, rate=None, seed=0):
     return makespan, lat, kinds, ok
 
 
+def serving_sample(args):
+    """A bounded sample of the serving mix for the headline line: its first `serve_sample` requests
+    submitted at once to the serving loop (served solves/s, p50 / p99 of completion - submission), then
+    the same requests one at a time on one slot (the plain one-request-per-launch path)."""
+    reqs = serve_requests(SEED + 5, args.serve_sample)
+    mk, lat, kinds, ok = serve_run(reqs, args.serve_slots)
+    mk1, lat1, _, ok1 = serve_run(reqs, 1)
+    return {"value": len(reqs) / mk, "unit": "solves/s", "requests": len(reqs),
+            "kinds": {k: len(v) for k, v in kinds.items()}, "slots": args.serve_slots,
+            "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)), "makespan_s": mk,
+            "plain_one_slot": {"value": len(reqs) / mk1, "makespan_s": mk1, "p50_s": float(np.percentile(lat1, 50)),
+                               "p99_s": float(np.percentile(lat1, 99))},
+            "served_over_plain": mk1 / mk, "all_ok": bool(ok and ok1),
+            "how": "the first requests of the seeded serving mix (70 % 1-D, 20 % conical, 10 % 2-D), all submitted "
+                   "at once; the full mix with Poisson arrivals is --workload serve"}
+
+
 def run_serve(args):
     reqs = serve_requests(SEED + 5, args.serve_requests)
     stats = {}
@@ -828,6 +847,32 @@ def run_eig_only(n, batch, group, hermitian=False):
     return 0 if bad == 0 else 1
 
 
+def run_gemm_only(batch, m, k, n):
+    """Profiling case for the complex product alone: `batch` products of seeded normal complex m x k and
+    k x n matrices through rcwa_gpu_multiply_batch (the tensor-core path unless RCWA_GB300_GEMM=fp64),
+    three times; the device time of the third (digit splits + product kernel, CUDA events on the engine's
+    stream) and its FP64-equivalent rate 8 m n k / time."""
+    from stablercwa_gb300.engine import Engine
+    rng = np.random.default_rng(2)
+    a = rng.normal(size=(batch, m, k)) + 1j * rng.normal(size=(batch, m, k))
+    b = rng.normal(size=(batch, k, n)) + 1j * rng.normal(size=(batch, k, n))
+    eng = Engine()
+    eng.multiply_batch(a, b)
+    eng.set_kernel_timing(True)
+    ms = []
+    for _ in range(2):
+        eng.kernel_time("gemm")
+        c = eng.multiply_batch(a, b)
+        ms.append(eng.kernel_time("gemm")[0])
+    eng.set_kernel_timing(False)
+    eng.close()
+    err = float(np.max(np.abs(c[:2] - a[:2] @ b[:2])))
+    print(json.dumps({"gemm_only": {"batch": batch, "m": m, "k": k, "n": n, "ms": ms[-1],
+                                    "tflops_fp64_equivalent": 8.0 * batch * m * n * k / (ms[-1] * 1e-3) / 1e12,
+                                    "max_abs_err_first_two": err}}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -845,13 +890,19 @@ def main():
                     help="timed steps of the absorbing-grating C2 line in the headline run (0: skip)")
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-slots", type=int, default=48)
+    ap.add_argument("--serve-sample", type=int, default=40,
+                    help="requests of the serving mix run in the headline line (0: skip)")
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[0.5, 1.0])
     ap.add_argument("--workload", choices=["c2", "c3", "c4", "plain", "serve"], default="c2",
                     help="c2 (default, the headline line), c3 conical, c4 2-D, plain one-point-per-call")
     ap.add_argument("--hermitian", action="store_true", help="--eig-only: lossless matrices, Hermitian solver")
     ap.add_argument("--eig-only", nargs=2, type=int, metavar=("N", "BATCH"), default=None,
                     help="profiling case: the eigensolver alone on BATCH layer matrices of order N")
+    ap.add_argument("--gemm-only", nargs=4, type=int, metavar=("BATCH", "M", "K", "N"), default=None,
+                    help="profiling case: BATCH complex products of m x k by k x n, digit splits and product kernel")
     args = ap.parse_args()
+    if args.gemm_only:
+        return run_gemm_only(*args.gemm_only)
     if args.eig_only:
         return run_eig_only(args.eig_only[0], args.eig_only[1], args.eig_group, args.hermitian)
     if args.impl == "reference":

@@ -116,7 +116,7 @@ int autotune_eig(cudaStream_t st, int kind, int n, int batch, const zc* a, long 
         run_form(st, kind, n, batch, a, a_stride, w, v, info0, ws, base);
         std::vector<int> h0(batch), h1(batch);
         RCWA_CUDA(cudaMemcpyAsync(h0.data(), info0, batch * sizeof(int), cudaMemcpyDeviceToHost, st));
-        RCWA_CUDA(cudaStreamSynchronize(st));
+        RCWA_CUDA(stream_wait(st));
         for (int form : candidates(kind, n, batch)) {
             run_form(st, kind, n, batch, a, a_stride, w, v, info, ws, form);  // warm: modules loaded, caches settled
             RCWA_CUDA(cudaEventRecord(e0, st));

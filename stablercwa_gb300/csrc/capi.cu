@@ -210,11 +210,15 @@ int rcwa_gpu_create(const rcwa_gpu_config* config, rcwa_gpu_ctx** out) {
         delete ctx;
         return RCWA_ECUDA;
     }
-    // keep stream-ordered allocations cached in the device pool between calls
+    // keep stream-ordered allocations cached in the device pool between calls, and never let the pool hand
+    // one stream memory that another stream freed with work still pending (it would make the second stream
+    // wait for the first: contexts on separate streams, as the serving loop's slots are, would serialise)
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
         uint64_t threshold = UINT64_MAX;
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+        int no = 0;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no);
     }
     *out = ctx;
     return RCWA_OK;
@@ -225,10 +229,10 @@ void rcwa_gpu_destroy(rcwa_gpu_ctx* ctx) {
     {
         std::lock_guard<std::mutex> hold(ctx->lock);
         cudaSetDevice(ctx->device);
-        cudaStreamSynchronize(ctx->stream);
+        stream_wait(ctx->stream);
         cudaStreamDestroy(ctx->stream);
         if (ctx->stream2) {
-            cudaStreamSynchronize(ctx->stream2);
+            stream_wait(ctx->stream2);
             cudaStreamDestroy(ctx->stream2);
         }
         if (ctx->fork) cudaEventDestroy(ctx->fork);
@@ -289,7 +293,7 @@ int rcwa_gpu_kernel_time(rcwa_gpu_ctx* ctx, const char* kind, double* millisecon
 }
 
 int rcwa_gpu_synchronize(rcwa_gpu_ctx* ctx) {
-    return guarded(ctx, [&] { RCWA_CUDA(cudaStreamSynchronize(ctx->stream)); });
+    return guarded(ctx, [&] { RCWA_CUDA(stream_wait(ctx->stream)); });
 }
 
 int rcwa_gpu_solve1d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_point1d* points, int n_points, int M,
@@ -341,7 +345,7 @@ int rcwa_gpu_solve1d_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const r
         copy_back(out->n_dense_solve, d.n_dense_solve, np, st);
         if (out->n_lu) copy_back(out->n_lu, d.n_lu, np, st);
         if (opt.diagnostics) copy_back(out->max_eig_residual, d.max_eig_residual, np, st);
-        RCWA_CUDA(cudaStreamSynchronize(st));
+        RCWA_CUDA(stream_wait(st));
     });
 }
 
@@ -485,7 +489,7 @@ void conical_batch(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const rcwa_poin
     copy_back(out->ky, d.ky, n_points, st);
     copy_back(out->flux_r, d.flux_r, nv, st);
     copy_back(out->flux_t, d.flux_t, nv, st);
-    RCWA_CUDA(cudaStreamSynchronize(st));
+    RCWA_CUDA(stream_wait(st));
 }
 }  // namespace
 
@@ -582,7 +586,7 @@ int rcwa_gpu_solve1d_fields(rcwa_gpu_ctx* ctx, const rcwa_stack1d* stack, const 
         copy_back(out->n_dense_solve, d.n_dense_solve, n_points, st);
         if (out->n_lu) copy_back(out->n_lu, d.n_lu, n_points, st);
         if (nz > 0) copy_back(reinterpret_cast<zc*>(fields), fs.out, nf, st);
-        RCWA_CUDA(cudaStreamSynchronize(st));
+        RCWA_CUDA(stream_wait(st));
     });
 }
 
@@ -676,7 +680,7 @@ int rcwa_gpu_eig_hermitian_batch(rcwa_gpu_ctx* ctx, int n, int batch, const rcwa
         RCWA_CUDA(cudaMemcpyAsync(values, dw, (size_t)n * batch * sizeof(zc), cudaMemcpyDeviceToHost, st));
         RCWA_CUDA(cudaMemcpyAsync(vectors, dv, nn * sizeof(zc), cudaMemcpyDeviceToHost, st));
         RCWA_CUDA(cudaMemcpyAsync(info, di, batch * sizeof(int), cudaMemcpyDeviceToHost, st));
-        RCWA_CUDA(cudaStreamSynchronize(st));
+        RCWA_CUDA(stream_wait(st));
     });
 }
 
@@ -708,7 +712,7 @@ int rcwa_gpu_eig_batch(rcwa_gpu_ctx* ctx, int n, int batch, const rcwa_complex* 
         copy_back(reinterpret_cast<zc*>(vectors), dv, nn, st);
         copy_back(info, di, batch, st);
         copy_back(sweeps, dsw, batch, st);
-        RCWA_CUDA(cudaStreamSynchronize(st));
+        RCWA_CUDA(stream_wait(st));
     });
 }
 
@@ -730,7 +734,7 @@ int rcwa_gpu_solve_batch(rcwa_gpu_ctx* ctx, int n, int nrhs, int batch, const rc
                         db, (long long)n * nrhs, ds);
         copy_back(reinterpret_cast<zc*>(x), db, nb, st);
         copy_back(singular, ds, batch, st);
-        RCWA_CUDA(cudaStreamSynchronize(st));
+        RCWA_CUDA(stream_wait(st));
     });
 }
 
@@ -837,7 +841,7 @@ int rcwa_gpu_multiply_batch(rcwa_gpu_ctx* ctx, int m, int k, int n, int batch, c
         launch_zgemm(st, m, n, k, batch, da, m, (long long)m * k, db, k, (long long)k * n, nullptr, 0, dc, m,
                      (long long)m * n, 1.0, 0.0);
         copy_back(reinterpret_cast<zc*>(c), dc, nc, st);
-        RCWA_CUDA(cudaStreamSynchronize(st));
+        RCWA_CUDA(stream_wait(st));
     });
 }
 

@@ -734,13 +734,13 @@ void batched_triangular_exp(Batch& c, int n, const zc* G, const double* k0, doub
         LAUNCH(texp_term_kernel, (unsigned)B, kSchurThreads, st, B, n, kk, E, work, iter, done, flags + 1, c.fail);
         int any = 0;
         RCWA_CUDA(cudaMemcpyAsync(&any, flags + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-        RCWA_CUDA(cudaStreamSynchronize(st));
+        RCWA_CUDA(stream_wait(st));
         if (!any) break;
     }
     LAUNCH(texp_fix_kernel, (unsigned)B, kSchurThreads, st, B, n, -1, 0, E, work, done, scal, c.fail);
     int max_scal = 0;
     RCWA_CUDA(cudaMemcpyAsync(&max_scal, flags, sizeof(int), cudaMemcpyDeviceToHost, st));
-    RCWA_CUDA(cudaStreamSynchronize(st));
+    RCWA_CUDA(stream_wait(st));
     for (int k = 0; k < max_scal; ++k) {
         LAUNCH(texp_square_mask_kernel, nblocks(B), kTpb, st, B, k, done, scal, mask);
         launch_zgemm(st, n, n, n, B, E, n, nn, E, n, nn, nullptr, 0, work + 3 * nn, n, 4 * nn, 1.0, 0.0, mask, 0);
@@ -962,7 +962,7 @@ void conical_schur_modes(Batch& c, const std::vector<SchurJob>& jobs, std::vecto
     for (int q = 0; q < J; ++q)
         RCWA_CUDA(cudaMemcpyAsync(flags.data() + (size_t)q * B, modes[jobs[q].layer + 1].schur, B * sizeof(int),
                                   cudaMemcpyDeviceToHost, st));
-    RCWA_CUDA(cudaStreamSynchronize(st));
+    RCWA_CUDA(stream_wait(st));
     std::vector<int2> map;
     for (int q = 0; q < J; ++q)
         for (int b = 0; b < B; ++b)
@@ -1208,13 +1208,13 @@ void sample_conical_fields(Batch& c, const FieldSpec& f, const std::vector<const
             launch_zgemm(st, N, cnt, N, B, einv, N, 0, ez, N, (long long)N * cnt, nullptr, 0, ez2, N, (long long)N * cnt, 1.0,
                          0.0);
             LAUNCH(ez_out_kernel, nblocks(totN), kTpb, st, B, N, cnt, nz, d_cols, ez2, nullptr, out);
-            RCWA_CUDA(cudaStreamSynchronize(st));
+            RCWA_CUDA(stream_wait(st));
             mem.free(ez2);
         } else {
             const zc hs{ie.real(), ie.imag()};
             RCWA_CUDA(cudaMemcpyAsync(scale, &hs, sizeof(zc), cudaMemcpyHostToDevice, st));
             LAUNCH(ez_out_kernel, nblocks(totN), kTpb, st, B, N, cnt, nz, d_cols, ez, scale, out);
-            RCWA_CUDA(cudaStreamSynchronize(st));  // the host values of this group end here
+            RCWA_CUDA(stream_wait(st));  // the host values of this group end here
         }
         for (void* p : {(void*)F, (void*)G, (void*)ez, (void*)d_z, (void*)d_cols}) mem.free(p);
     }
@@ -1332,7 +1332,7 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
         {
             std::vector<double> inf(B, INFINITY);
             RCWA_CUDA(cudaMemcpyAsync(min_abs, inf.data(), B * sizeof(double), cudaMemcpyHostToDevice, st));
-            RCWA_CUDA(cudaStreamSynchronize(st));
+            RCWA_CUDA(stream_wait(st));
         }
         const long long nvN = (long long)B * N, nv = (long long)B * n, nd = (long long)B * nn, ndN = (long long)B * NN;
         ConicalPointsDev P{pts.s_cphi + p0, pts.ky + p0, pts.cphi + p0, pts.sphi + p0, pts.ctheta + p0, pts.wl + p0};
@@ -1442,7 +1442,7 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
                 mem.free(coupling);
                 int any = 0;
                 RCWA_CUDA(cudaMemcpyAsync(&any, any_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
-                RCWA_CUDA(cudaStreamSynchronize(st));
+                RCWA_CUDA(stream_wait(st));
                 if (any) {
                     // Schur basis of the full 2N operator for the flagged samples (rcwa1d_conical.hpp:466-502): H here,
                     // its eigensolve below together with the other gratings' flagged samples
@@ -1715,7 +1715,7 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
     }
     int lf = 0;
     RCWA_CUDA(cudaMemcpyAsync(&lf, layer_fail, sizeof(int), cudaMemcpyDeviceToHost, st));
-    RCWA_CUDA(cudaStreamSynchronize(st));
+    RCWA_CUDA(stream_wait(st));
     if (lf) {
         const double nan = std::nan("");
         const size_t cnt = (size_t)n_points * N * 4;
@@ -1732,9 +1732,9 @@ void solve_conical_device(cudaStream_t st, const rcwa_stack1d& stack, const Coni
             const size_t cf = (size_t)n_points * 6 * N * fields->zs.size();
             std::vector<double> fn(cf * 2, nan);
             RCWA_CUDA(cudaMemcpyAsync(fields->out, fn.data(), cf * sizeof(zc), cudaMemcpyHostToDevice, st));
-            RCWA_CUDA(cudaStreamSynchronize(st));
+            RCWA_CUDA(stream_wait(st));
         }
-        RCWA_CUDA(cudaStreamSynchronize(st));
+        RCWA_CUDA(stream_wait(st));
     }
 }
 

@@ -114,6 +114,73 @@ void herm_reduce_dispatch(cudaStream_t st, int n, int batch, const zc* a, long l
     }
     RCWA_CUDA(cudaGetLastError());
 }
+template <int G>
+void herm_panel_launch(cudaStream_t st, int n, int batch, int k0, const zc* a, long long a_stride, zc* ws, zc* pan,
+                       zc* vall, zc* mall, int pnb) {
+    const int tpb = 128;
+    const unsigned blocks = (unsigned)(((long long)batch * G + tpb - 1) / tpb);
+    herm_panel_batch_kernel<G><<<blocks, tpb, 0, st>>>(n, batch, k0, a, a_stride, ws, pan, vall, mall, pnb);
+    ++launch_count();
+    RCWA_CUDA(cudaGetLastError());
+}
+
+// The blocked tridiagonalisation (eig.cuh herm_panel_one): per panel one kernel over all matrices, then the
+// trailing block's rank-2 nb update A -= V W^H + W V^H as two batched products (the tensor cores for
+// orders >= 32). vall receives the reflectors, mall the panels' T V^H.
+void herm_blocked_reduce(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* ws, zc* pan, zc* vall,
+                         zc* mall, int group) {
+    const int nb = kHermNb, P = herm_panel_count(n), pnb = P * nb;
+    const long long ws_stride = eig_workspace_elems(n), pan_stride = herm_panel_elems(n);
+    for (int b = 0; b < P; ++b) {
+        const int k0 = b * nb;
+        switch (group) {
+            case 4: herm_panel_launch<4>(st, n, batch, k0, a, a_stride, ws, pan, vall, mall, pnb); break;
+            case 8: herm_panel_launch<8>(st, n, batch, k0, a, a_stride, ws, pan, vall, mall, pnb); break;
+            case 16: herm_panel_launch<16>(st, n, batch, k0, a, a_stride, ws, pan, vall, mall, pnb); break;
+            case 32: herm_panel_launch<32>(st, n, batch, k0, a, a_stride, ws, pan, vall, mall, pnb); break;
+            default: throw EngineError{RCWA_EINVAL, "eig: the blocked Hermitian reduction takes 4, 8, 16 or 32 lanes"};
+        }
+        if (k0 + nb < n - 1) {  // another panel follows: bring its trailing block up to date
+            // as two products, V W^H and W V^H: the tensor-core product scales each row and column by its
+            // largest entry, and a row of [V W] mixes V's entries (order 1) with W's (order |A|)
+            const int t0 = k0 + nb, m2 = n - t0;
+            zc* blk = ws + (long long)t0 * n + t0;
+            const zc* bt = pan + 2LL * nb * n + (long long)t0 * 2 * nb;
+            launch_zgemm_untimed(st, m2, m2, nb, batch, pan + t0, n, pan_stride, bt, 2 * nb, pan_stride, blk, ws_stride, blk,
+                                 n, ws_stride, -1.0, 1.0);
+            launch_zgemm_untimed(st, m2, m2, nb, batch, pan + (long long)nb * n + t0, n, pan_stride, bt + nb, 2 * nb,
+                                 pan_stride, blk, ws_stride, blk, n, ws_stride, -1.0, 1.0);
+        }
+    }
+}
+
+// X (the eigenvectors, in place) = Q Y = Q_0 (Q_1 (.. (Q_last Y))) with Q_b = I - V_b T_b V_b^H, applied
+// as X(k0+1:, :) -= V_b (M_b X(k0+1:, :)) with M_b = T_b V_b^H; u is nb x n scratch per matrix.
+void herm_blocked_back(cudaStream_t st, int n, int batch, zc* x, const zc* vall, const zc* mall, zc* u, const int* skip) {
+    const int nb = kHermNb, P = herm_panel_count(n), pnb = P * nb;
+    const long long nn = (long long)n * n;
+    for (int b = P - 1; b >= 0; --b) {
+        const int k0 = b * nb, nbp = std::min(nb, n - 1 - k0), r0 = k0 + 1, mr = n - r0;
+        launch_zgemm_untimed(st, nbp, n, mr, batch, mall + b * nb + (long long)r0 * pnb, pnb, (long long)pnb * n, x + r0, n,
+                             nn, nullptr, 0, u, nb, (long long)nb * n, 1.0, 0.0, skip, 1);
+        launch_zgemm_untimed(st, mr, n, nbp, batch, vall + (long long)k0 * n + r0, n, nn, u, nb, (long long)nb * n, x + r0,
+                             nn, x + r0, n, nn, -1.0, 1.0, skip, 1);
+    }
+}
+
+__global__ void real_to_complex_kernel(long long count, const double* __restrict__ y, zc* __restrict__ x) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) x[i] = zc{y[i], 0.0};
+}
+
+// the blocked reduction replaces the unblocked one for batched groups of lanes where the products run on the
+// tensor cores; RCWA_GB300_HERM_BLOCKED=0 keeps the unblocked kernel
+bool herm_blocked_wanted(int n, int group) {
+    const char* env = std::getenv("RCWA_GB300_HERM_BLOCKED");
+    if (env && env[0] == '0') return false;
+    return group <= 32 && n >= 64 && tc_gemm_enabled() && !Fp64ProductsGuard::active();
+}
+
 void herm_fused_dispatch(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info,
                          zc* ws, double eps, int max_iter, int group, const int* only) {
     const int tpb = 128;
@@ -146,11 +213,21 @@ void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a
     const bool real_form = ysm <= 227 * 1024;
     zc* q = v;
     double* y = nullptr;
+    const bool blocked = real_form && herm_blocked_wanted(n, group);
+    zc *pan = nullptr, *mall = nullptr, *u = nullptr;
     if (real_form) {
-        RCWA_CUDA(cudaMallocAsync(&q, (size_t)batch * n * n * sizeof(zc), st));
+        RCWA_CUDA(cudaMallocAsync(&q, (size_t)batch * n * n * sizeof(zc), st));  // Q, or the reflectors when blocked
         RCWA_CUDA(cudaMallocAsync(&y, (size_t)batch * n * n * sizeof(double), st));
     }
-    herm_reduce_dispatch(st, n, batch, a, a_stride, q, ws, group);
+    if (blocked) {
+        const size_t pnb = (size_t)herm_panel_count(n) * kHermNb;
+        RCWA_CUDA(cudaMallocAsync(&pan, (size_t)batch * herm_panel_elems(n) * sizeof(zc), st));
+        RCWA_CUDA(cudaMallocAsync(&mall, (size_t)batch * pnb * n * sizeof(zc), st));
+        RCWA_CUDA(cudaMallocAsync(&u, (size_t)batch * kHermNb * n * sizeof(zc), st));
+        herm_blocked_reduce(st, n, batch, a, a_stride, ws, pan, q, mall, group);
+    } else {
+        herm_reduce_dispatch(st, n, batch, a, a_stride, q, ws, group);
+    }
     const size_t qsm = (size_t)2 * n * kHermQlThreads * sizeof(double);
     if (qsm <= 227 * 1024) {
         if (qsm > 48 * 1024) {
@@ -183,7 +260,14 @@ void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a
         const dim3 grid((unsigned)batch, (unsigned)((n + kHermRows - 1) / kHermRows));
         herm_apply_real_kernel<<<grid, kHermRows, ysm, st>>>(n, batch, y, ws, info);
         RCWA_CUDA(cudaGetLastError());
-        launch_zdgemm(st, n, n, n, batch, q, n, (long long)n * n, y, n, (long long)n * n, v, n, (long long)n * n, only, 1);
+        if (blocked) {
+            const long long cnt = (long long)batch * n * n;
+            real_to_complex_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, st>>>(cnt, y, v);
+            RCWA_CUDA(cudaGetLastError());
+            herm_blocked_back(st, n, batch, v, q, mall, u, only);
+        } else {
+            launch_zdgemm(st, n, n, n, batch, q, n, (long long)n * n, y, n, (long long)n * n, v, n, (long long)n * n, only, 1);
+        }
         launch_count() += 5;
     } else {
         herm_apply_kernel<<<(unsigned)(((long long)batch * n + 127) / 128), 128, 0, st>>>(n, batch, v, ws, info);
@@ -195,6 +279,11 @@ void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a
     if (real_form) {
         RCWA_CUDA(cudaFreeAsync(q, st));
         RCWA_CUDA(cudaFreeAsync(y, st));
+    }
+    if (blocked) {
+        RCWA_CUDA(cudaFreeAsync(pan, st));
+        RCWA_CUDA(cudaFreeAsync(mall, st));
+        RCWA_CUDA(cudaFreeAsync(u, st));
     }
 }
 

@@ -833,6 +833,203 @@ __global__ void __launch_bounds__(G) herm_reduce_block_kernel(int n, int batch, 
     herm_tridiag_one<G>(n, a + gid * a_stride, v + gid * (long long)n * n, ws + gid * eig_workspace_elems(n), red, ired);
 }
 
+// ---------------------------------------------------------------- (1') the blocked tridiagonalisation
+//
+// The same reduction T = Q^H A Q (same reflectors H_k = I - tau_k v_k v_k^H, same d and e) in panels of
+// kHermNb columns, after LAPACK's zhetrd / zlatrd (Dongarra, Hammarling and Sorensen, "Block reduction of
+// matrices to condensed forms for eigenvalue computations", J. Comput. Appl. Math. 27, 1989). Within a
+// panel the trailing matrix is left as it was at the panel's start, A0; after i reflectors of the panel
+// the reduced matrix is A0 - V W^H - W V^H with V = [v_0 .. v_{i-1}] and W = [w_0 .. w_{i-1}], so
+//   * column j = k0 + i is first brought up to date: A(:, j) -= V W(j, :)^H + W V(j, :)^H (rows >= j);
+//   * its reflector is formed as in herm_tridiag_one;
+//   * y = A0 v - V (W^H v) - W (V^H v) (the product with A0 reads the trailing block once and writes
+//     nothing), w = tau y - (|tau|^2 (v^H y) / 2) v.
+// After the panel the whole trailing block takes A -= V W^H + W V^H as two complex products of inner
+// dimension kHermNb (the tensor cores), launched by the host between panel launches.
+// The reflectors are also kept for the back-transformation instead of forming Q: the panel's
+// H_{k0} .. H_{k0+nb-1} = I - V T V^H with T upper triangular (LAPACK's zlarft, forward and columnwise:
+// T(i, i) = tau_i, T(0:i, i) = -tau_i T(0:i, 0:i) (V^H v_i), and V^H v_i is the t2 the panel computes
+// anyway), and the panel stores M = T V^H, so Q Y = Q_0 (Q_1 (.. (Q_last Y))) is applied as
+// X -= V (M X), two products per panel.
+//
+// Per-matrix panel scratch (herm_panel_elems(n) zc): [V | W] (n x 2 nb, column-major), Bt = [W | V]^H
+// (2 nb x n, column-major: the second operand of the trailing update), T (nb x nb), t2 (nb). The reflectors
+// go to vall (n x n: column k is v_k, zero above row k + 1, one at k + 1) and M to mall (rows
+// b nb .. b nb + nb - 1 of a pnb x n column-major matrix for panel b). d, e, tau and the work matrix keep
+// herm_tridiag_one's places in ws.
+constexpr int kHermNb = 32;
+__host__ __device__ inline long long herm_panel_elems(int n) { return 4LL * kHermNb * n + kHermNb * kHermNb + kHermNb; }
+__host__ __device__ inline int herm_panel_count(int n) { return n > 1 ? (n - 2) / kHermNb + 1 : 0; }
+
+template <int G>
+__device__ void herm_panel_one(int n, int k0, const zc* __restrict__ A0, zc* __restrict__ ws, zc* __restrict__ pan,
+                               zc* __restrict__ vall, zc* __restrict__ mall, int pnb) {
+    constexpr int nb = kHermNb;
+    const int g = threadIdx.x & (G - 1);
+    const Grp<G> grp(nullptr, nullptr);
+    zc* __restrict__ A = ws;
+    double* __restrict__ d = reinterpret_cast<double*>(ws + 2LL * n * n);
+    double* __restrict__ e = d + n;
+    zc* __restrict__ ww = ws + 3LL * n * n;  // y, then w, of the current column (n)
+    zc* __restrict__ taus = ww + n;
+    zc* __restrict__ VW = pan;                 // V(r, p) = VW[p n + r], W(r, p) = VW[(nb + p) n + r]
+    zc* __restrict__ Bt = pan + 2LL * nb * n;  // Bt(q, r) = Bt[r 2 nb + q]
+    zc* __restrict__ T = Bt + 2LL * nb * n;    // T(p, q) = T[q nb + p]
+    zc* __restrict__ t2 = T + nb * nb;         // V^H v of the current column
+    const int nbp = min(nb, n - 1 - k0);       // reflectors in this panel
+    const zc one{1.0, 0.0}, zero{0.0, 0.0};
+    if (k0 == 0) {  // the Hermitian part (A0 + A0^H) / 2, as herm_tridiag_one starts
+        for (long long idx = g; idx < (long long)n * n; idx += G) {
+            const int j = (int)(idx / n), i = (int)(idx - (long long)j * n);
+            const zc a = A0[idx], b = A0[(long long)i * n + j];
+            A[idx] = zc{0.5 * (a.re + b.re), 0.5 * (a.im - b.im)};
+        }
+    }
+    for (int c = 0; c < 2 * nb; ++c)
+        for (int r = g; r < n; r += G) VW[(long long)c * n + r] = zero;
+    for (int idx = g; idx < nb * nb; idx += G) T[idx] = zero;
+    grp.sync();
+    for (int i = 0; i < nbp; ++i) {
+        const int j = k0 + i;
+        zc* __restrict__ col = A + (long long)j * n;
+        if (i > 0) {  // column j as the panel's earlier reflectors leave it (rows >= j)
+            for (int r = first_owned<G>(j, g); r < n; r += G) {
+                zc acc = col[r];
+                for (int p = 0; p < i; ++p) {
+                    acc = zfms(VW[(long long)p * n + r], conj(VW[(long long)(nb + p) * n + j]), acc);
+                    acc = zfms(VW[(long long)(nb + p) * n + r], conj(VW[(long long)p * n + j]), acc);
+                }
+                col[r] = acc;
+            }
+            grp.sync();
+        }
+        if (g == 0) d[j] = col[j].re;
+        const zc alpha = col[j + 1];
+        const int r2 = first_owned<G>(j + 2, g), r1 = first_owned<G>(j + 1, g);
+        double xs = 0.0;
+        for (int r = r2; r < n; r += G) xs += norm2(col[r]);
+        xs = grp.sum(xs);
+        zc tau{0.0, 0.0};
+        double beta = alpha.re;
+        if (xs != 0.0 || alpha.im != 0.0) {
+            const double nrm = hypot(hypot(alpha.re, alpha.im), sqrt(xs));
+            beta = alpha.re >= 0.0 ? -nrm : nrm;
+            tau = zc{(beta - alpha.re) / beta, -alpha.im / beta};
+            const zc scal = zinv(alpha - zc{beta, 0.0});
+            for (int r = r2; r < n; r += G) col[r] = col[r] * scal;
+        }
+        if (g == 0) {
+            e[j] = beta;
+            taus[j] = tau;
+        }
+        zc* __restrict__ vcol = vall + (long long)j * n;
+        for (int r = g; r < n; r += G) {
+            const zc vr = r <= j ? zero : (r == j + 1 ? one : col[r]);
+            vcol[r] = vr;
+            VW[(long long)i * n + r] = vr;
+        }
+        if (is_zero(tau)) {  // H_j = I: w = 0 and T's column is zero (both already)
+            grp.sync();
+            continue;
+        }
+        grp.sync();  // v is complete
+        // y = A0 v over the trailing block, owned rows, four rows per pass
+        for (int i0 = r1; i0 < n; i0 += 4 * G) {
+            zc acc[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int r = i0 + u * G;
+                acc[u] = r < n ? A[(long long)(j + 1) * n + r] : zero;
+            }
+            for (int c = j + 2; c < n; ++c) {
+                const zc vc = col[c];
+                const zc* ac = A + (long long)c * n;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int r = i0 + u * G;
+                    if (r < n) acc[u] = zmac(ac[r], vc, acc[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int r = i0 + u * G;
+                if (r < n) ww[r] = acc[u];
+            }
+        }
+        // y -= V (W^H v) + W (V^H v), one earlier reflector at a time
+        for (int p = 0; p < i; ++p) {
+            const zc* vp = VW + (long long)p * n;
+            const zc* wp = VW + (long long)(nb + p) * n;
+            zc a1 = zero, a2 = zero;
+            for (int r = r1; r < n; r += G) {
+                const zc vr = r == j + 1 ? one : col[r];
+                a1 = zmacc(wp[r], vr, a1);
+                a2 = zmacc(vp[r], vr, a2);
+            }
+            const zc s1{grp.sum(a1.re), grp.sum(a1.im)}, s2{grp.sum(a2.re), grp.sum(a2.im)};
+            for (int r = r1; r < n; r += G) ww[r] = zfms(wp[r], s2, zfms(vp[r], s1, ww[r]));
+            if (g == 0) t2[p] = s2;
+        }
+        double mr = 0.0;
+        for (int r = r1; r < n; r += G) {
+            const zc vr = r == j + 1 ? one : col[r];
+            mr += vr.re * ww[r].re + vr.im * ww[r].im;  // Re(conj(v_r) y_r)
+        }
+        const double half = 0.5 * norm2(tau) * grp.sum(mr);
+        zc* __restrict__ wi = VW + (long long)(nb + i) * n;
+        for (int r = r1; r < n; r += G) {
+            const zc vr = r == j + 1 ? one : col[r];
+            wi[r] = tau * ww[r] - zc{half * vr.re, half * vr.im};
+        }
+        grp.sync();  // t2 is complete
+        // T(0:i, i) = -tau T(0:i, 0:i) t2, T(i, i) = tau
+        for (int p = g; p < i; p += G) {
+            zc z = zero;
+            for (int q = p; q < i; ++q) z = zmac(T[q * nb + p], t2[q], z);
+            T[i * nb + p] = zc{0.0, 0.0} - tau * z;
+        }
+        if (g == 0) T[i * nb + i] = tau;
+        grp.sync();  // w and T's column are complete
+    }
+    if (k0 + nbp == n - 1 && g == 0) {  // the last panel: the last diagonal entry takes its updates too
+        zc a = A[(long long)(n - 1) * n + n - 1];
+        for (int p = 0; p < nbp; ++p) {
+            a = zfms(VW[(long long)p * n + n - 1], conj(VW[(long long)(nb + p) * n + n - 1]), a);
+            a = zfms(VW[(long long)(nb + p) * n + n - 1], conj(VW[(long long)p * n + n - 1]), a);
+        }
+        d[n - 1] = a.re;
+        e[n - 1] = 0.0;
+    }
+    // the trailing update's second operand, and M = T V^H (rows of V above k0 + 1 are zero)
+    for (int r = g; r < n; r += G) {
+        zc* bt = Bt + (long long)r * 2 * nb;
+        for (int q = 0; q < nb; ++q) {
+            bt[q] = conj(VW[(long long)(nb + q) * n + r]);
+            bt[nb + q] = conj(VW[(long long)q * n + r]);
+        }
+    }
+    const int b = k0 / nb;
+    for (int r = first_owned<G>(k0 + 1, g); r < n; r += G) {
+        zc* m = mall + (long long)r * pnb + b * nb;
+        for (int p = 0; p < nbp; ++p) {
+            zc acc = zero;
+            for (int q = p; q < nbp; ++q) acc = zmac(T[q * nb + p], conj(VW[(long long)q * n + r]), acc);
+            m[p] = acc;
+        }
+    }
+}
+
+template <int G>
+__global__ void __launch_bounds__(128) herm_panel_batch_kernel(int n, int batch, int k0, const zc* __restrict__ a,
+                                                               long long a_stride, zc* __restrict__ ws,
+                                                               zc* __restrict__ pan, zc* __restrict__ vall,
+                                                               zc* __restrict__ mall, int pnb) {
+    const long long gid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    if (gid >= batch) return;
+    herm_panel_one<G>(n, k0, a + gid * a_stride, ws + gid * eig_workspace_elems(n), pan + gid * herm_panel_elems(n),
+                      vall + gid * (long long)n * n, mall + gid * (long long)pnb * n, pnb);
+}
+
 // (2) implicit symmetric QL with Wilkinson's shift on (d, e), one thread per matrix; rotations logged. The
 // rotation chain is the whole cost, so with SMEM the thread's d and e live in shared memory (kHermQlThreads
 // threads per CTA, 16 n bytes each) rather than in the workspace, whose loads would sit on the chain.

@@ -635,6 +635,12 @@ int cluster_size_for(int n) {
 
 }  // namespace
 
+void preload_eig_cluster_kernel() {
+    cudaFuncAttributes attr;
+    cudaFuncGetAttributes(&attr, eig_cluster_kernel);  // loads the kernel under lazy module loading
+    cudaGetLastError();
+}
+
 bool eig_cluster_wanted(int n, int batch) {
     static const int mode = [] {
         const char* e = std::getenv("RCWA_GB300_EIG_CLUSTER");

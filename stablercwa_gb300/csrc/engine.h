@@ -80,6 +80,14 @@ void launch_lu_solve(cudaStream_t st, int n, int nrhs, int batch, const zc* a, l
 void launch_zgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride, const zc* B,
                   int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc, long long c_stride,
                   double s_ab, double s_c, const int* skip = nullptr, int skip_value = 1, int tri = 0);
+// Waits for the work queued on st like cudaStreamSynchronize, but sleeping (an event with blocking sync)
+// instead of spinning: the serving loop's slot threads wait on their own streams while others launch.
+cudaError_t stream_wait(cudaStream_t st);
+// the same without the per-kind kernel timer (products inside another timed stage, e.g. the eigensolver's)
+void launch_zgemm_untimed(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride,
+                          const zc* B, int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc,
+                          long long c_stride, double s_ab, double s_c, const int* skip = nullptr, int skip_value = 1,
+                          int tri = 0);
 // The eigensolver's form per (kind 0 general / 1 Hermitian, order, batch) from timing (autotune.cu): the
 // tuned form, 0 when none is recorded; autotune_eig times every applicable form on the given matrices and
 // records the fastest (returns it; best_ms its time if non-null).
@@ -91,6 +99,7 @@ std::string autotune_table_text();
 // One matrix per thread-block cluster (eig_cluster.cu) for a few large matrices: the same algorithm as
 // launch_eig's kernels, spread over 8 or 16 SMs. launch_eig takes it by itself (eig_cluster_wanted).
 bool eig_cluster_wanted(int n, int batch);
+void preload_eig_cluster_kernel();
 void launch_eig_cluster(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info,
                         int* sweeps, zc* ws, double eps, int max_iter, const int* skip, int skip_value, zc* t_out);
 // The same product on the tensor cores (gemm_tc.cu: Ozaki-split bf16 tcgen05 products, FP64-accurate);

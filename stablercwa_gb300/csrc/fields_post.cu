@@ -163,7 +163,7 @@ void field_slice_api(cudaStream_t st, const rcwa_complex* harmonics, int n, int 
     int hb[2] = {0, 0};
     RCWA_CUDA(cudaMemcpyAsync(hb, bad, sizeof hb, cudaMemcpyDeviceToHost, st));
     RCWA_CUDA(cudaMemcpyAsync(out, O, no * sizeof(zc), cudaMemcpyDeviceToHost, st));
-    RCWA_CUDA(cudaStreamSynchronize(st));
+    RCWA_CUDA(stream_wait(st));
     if (hb[0]) throw EngineError{RCWA_ENUMERIC, "rcwa: field carrier produced nonfinite values"};
     if (hb[1]) throw EngineError{RCWA_ENUMERIC, "rcwa: field reconstruction produced nonfinite values"};
 }
@@ -215,7 +215,7 @@ void phase_data_api(cudaStream_t st, const rcwa_complex* field, int nt, int nz, 
            bad);
     int hbad = 0;
     RCWA_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
-    RCWA_CUDA(cudaStreamSynchronize(st));
+    RCWA_CUDA(stream_wait(st));
     if (hbad) throw EngineError{RCWA_EINVAL, "rcwa: incident reference coordinates must be finite and representable"};
     LAUNCH(phase_mask_kernel, nblocks(size), kTpb, st, size, f, amp, ref, phase_floor, peak, mk);
     if (unwrap == RCWA_UNWRAP_X || unwrap == RCWA_UNWRAP_BOTH) LAUNCH(unwrap_rows_kernel, nblocks(nz, 128), 128, st, nt, nz, ph, mk);
@@ -225,7 +225,7 @@ void phase_data_api(cudaStream_t st, const rcwa_complex* field, int nt, int nz, 
     RCWA_CUDA(cudaMemcpyAsync(amplitude, amp, size * sizeof(double), cudaMemcpyDeviceToHost, st));
     RCWA_CUDA(cudaMemcpyAsync(mask, mk, size, cudaMemcpyDeviceToHost, st));
     if (reference_out && ref) RCWA_CUDA(cudaMemcpyAsync(reference_out, ref, size * sizeof(zc), cudaMemcpyDeviceToHost, st));
-    RCWA_CUDA(cudaStreamSynchronize(st));
+    RCWA_CUDA(stream_wait(st));
 }
 
 }  // namespace rcwa_gb300

@@ -147,22 +147,120 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 
 // ---------------------------------------------------------------- digit split
 
-// exponent e with max = f 2^e, f in [0.5, 1); 0 for 0 or a non-finite max (the digits then carry it)
 // A row of A or column of B holding a non-finite entry gets this exponent: its digits come out zero and
 // the epilogue writes NaN for every element of C it touches (any such product is non-finite in FP64 too).
 constexpr int kNonFinite = 1 << 20;
 
-// the scale exponent of a row or column from its largest magnitude (+inf when it holds a non-finite entry)
-__device__ __forceinline__ int scale_exponent(double mx) {
-    if (!isfinite(mx)) return kNonFinite;
-    if (!(mx > 0.0)) return 0;
-    int e;
-    frexp(mx, &e);
-    return e;
+// The split kernels use no FP64 arithmetic: the FP64 pipe of this GPU runs 1/32 of the FP32 rate, and
+// conversions between FP64 and 64-bit integers run there too. Magnitudes are compared as the bit patterns
+// of |x| (ordered like the values), and a value is brought to fixed point from its exponent and mantissa.
+constexpr unsigned long long kMagInf = 0x7FF0000000000000ull;
+// |x| as a comparable bit pattern; kMagInf for inf and NaN
+__device__ __forceinline__ unsigned long long mag_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+    return b >= kMagInf ? kMagInf : b;
 }
 
-// bf16 bit pattern of a small integer (exact: |d| <= 256)
-__device__ __forceinline__ uint16_t bf16_int(long long d) { return (uint16_t)(__float_as_uint((float)d) >> 16); }
+// the scale exponent of a row or column from its largest magnitude's bits: max = f 2^e with f in [0.5, 1);
+// kNonFinite when the row or column holds a non-finite entry, 0 when it is zero
+__device__ __forceinline__ int scale_exponent(unsigned long long mb) {
+    if (mb >= kMagInf) return kNonFinite;
+    if (mb == 0) return 0;
+    const int be = (int)(mb >> 52);
+    if (be == 0) {  // a subnormal maximum (the FP64 path: rare)
+        int e;
+        frexp(__longlong_as_double((long long)mb), &e);
+        return e;
+    }
+    return be - 1022;
+}
+
+// Y = x 2^(62 - e) rounded to the nearest integer (ties to even), for |x| < 2^e: |Y| < 2^62
+__device__ __forceinline__ long long fixed62(double x, int e) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int be = (int)((b >> 52) & 0x7FF);
+    if (be == 0) {
+        if ((b << 1) == 0) return 0;
+        return __double2ll_rn(ldexp(x, 62 - e));  // subnormal: the FP64 path
+    }
+    const unsigned long long mant = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = be - 1075 + 62 - e;  // |Y| = mant 2^sh; |x| < 2^e keeps sh <= 9
+    unsigned long long m = 0;
+    if (sh >= 0) {
+        m = mant << sh;
+    } else if (sh > -64) {
+        const int r = -sh;
+        const unsigned long long rem = mant & ((1ull << r) - 1ull), half = 1ull << (r - 1);
+        m = mant >> r;
+        if (rem > half || (rem == half && (m & 1ull))) ++m;
+    }
+    return (b >> 63) ? -(long long)m : (long long)m;
+}
+
+// x 2^e2 as the nearest double (ties to even), for |x| < 2^63, from integer operations only: the FP64 pipe
+// of this GPU runs 1/32 of the FP32 rate, so the epilogue's conversions would otherwise dominate the tile.
+// False when the result is not a normal double (the caller converts in FP64 then).
+__device__ __forceinline__ bool i64_ldexp_bits(long long x, int e2, unsigned long long& bits) {
+    if (x == 0) {
+        bits = 0;
+        return true;
+    }
+    const unsigned long long sign = x < 0 ? 0x8000000000000000ull : 0ull;
+    const unsigned long long u = x < 0 ? 0ull - (unsigned long long)x : (unsigned long long)x;
+    const int msb = 63 - __clzll((long long)u);
+    int ex = msb + e2;
+    unsigned long long mant;
+    if (msb > 52) {
+        const int r = msb - 52;
+        const unsigned long long rem = u & ((1ull << r) - 1ull), half = 1ull << (r - 1);
+        mant = u >> r;
+        if (rem > half || (rem == half && (mant & 1ull))) ++mant;
+        if (mant >> 53) {
+            mant >>= 1;
+            ++ex;
+        }
+    } else {
+        mant = u << (52 - msb);
+    }
+    if (ex < -1022 || ex > 1023) return false;
+    bits = sign | ((unsigned long long)(ex + 1023) << 52) | (mant & 0xFFFFFFFFFFFFFull);
+    return true;
+}
+
+// c as an integer count of 2^e2 units (nearest, ties to even), for adding C0 into the accumulator; false when
+// c is subnormal, not finite, or at least 2^61 units (the caller adds in FP64 then)
+__device__ __forceinline__ bool double_to_units(double c, int e2, long long& t) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(c);
+    const int be = (int)((b >> 52) & 0x7FF);
+    if (be == 0) {
+        t = 0;
+        return (b << 1) == 0;
+    }
+    if (be == 0x7FF) return false;
+    const unsigned long long mant = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = (be - 1075) - e2;  // c = mant 2^(be - 1075)
+    unsigned long long m = 0;
+    if (sh >= 0) {
+        if (sh > 8) return false;
+        m = mant << sh;
+    } else if (sh > -64) {
+        const int r = -sh;
+        const unsigned long long rem = mant & ((1ull << r) - 1ull), half = 1ull << (r - 1);
+        m = mant >> r;
+        if (rem > half || (rem == half && (m & 1ull))) ++m;
+    }
+    t = (b >> 63) ? -(long long)m : (long long)m;
+    return true;
+}
+
+// bf16 bit pattern of a small integer (exact for |d| <= 256), from integer operations
+__device__ __forceinline__ uint16_t bf16_int(long long d) {
+    if (d == 0) return 0;
+    const unsigned sign = d < 0 ? 0x8000u : 0u;
+    const unsigned a = (unsigned)(d < 0 ? -d : d);
+    const int p = 31 - __clz((int)a);  // a = 1.f 2^p
+    return (uint16_t)(sign | ((unsigned)(p + 127) << 7) | ((a << (7 - p)) & 0x7Fu));
+}
 
 // The S digits of x 2^-e (|x 2^-e| < 1), integer arithmetic: Y = x 2^(62 - e) is the value to 62 fractional
 // bits (an int64 below 2^62, so adding the rounding half never overflows); digit s (from 0) is Y rounded at
@@ -170,11 +268,11 @@ __device__ __forceinline__ uint16_t bf16_int(long long d) { return (uint16_t)(__
 // 2^(-7 - 8 s); an eighth digit is the remainder itself, in units of 2^-63. A non-finite x (whose row or
 // column then carries kNonFinite) gives zero digits.
 __device__ __forceinline__ void store_digits(double x, int e, int S, uint16_t* out, long long plane_stride) {
-    if (!isfinite(x) || e == kNonFinite) {
+    if (mag_bits(x) >= kMagInf || e == kNonFinite) {
         for (int s = 0; s < S; ++s) out[s * plane_stride] = 0;
         return;
     }
-    long long Y = __double2ll_rn(ldexp(x, 62 - e));
+    long long Y = fixed62(x, e);
 #pragma unroll 1
     for (int s = 0; s < S; ++s) {
         const int sh = 55 - 8 * s;
@@ -200,19 +298,19 @@ __global__ void __launch_bounds__(256) tc_split_a_kernel(int m, int k, int Kp, i
     const long long b = blockIdx.y;
     const int i0 = blockIdx.x * 32, t = threadIdx.x, il = t & 31, w = t >> 5;
     const zc* As = A + b * a_stride;
-    __shared__ double smax[8][32];
+    __shared__ unsigned long long smax[8][32];
     __shared__ int sexp[32];
     __shared__ zc tile[32][33];
-    double mx = 0.0;
+    unsigned long long mx = 0;
     if (i0 + il < m)
         for (int kk = w; kk < k; kk += 8) {
             const zc v = As[(long long)kk * lda + i0 + il];
-            mx = (isfinite(v.re) && isfinite(v.im)) ? fmax(mx, fmax(fabs(v.re), fabs(v.im))) : INFINITY;
+            mx = max(mx, max(mag_bits(v.re), mag_bits(v.im)));
         }
     smax[w][il] = mx;
     __syncthreads();
     if (w == 0) {
-        for (int q = 1; q < 8; ++q) mx = fmax(mx, smax[q][il]);
+        for (int q = 1; q < 8; ++q) mx = max(mx, smax[q][il]);
         sexp[il] = scale_exponent(mx);
         if (i0 + il < m) ea[b * m + i0 + il] = sexp[il];
     }
@@ -256,16 +354,15 @@ __global__ void __launch_bounds__(128) tc_split_b_kernel(int n, int k, int Kp, i
     if (gw >= (long long)batch * n) return;
     const long long b = gw / n;
     const int j = (int)(gw - b * n), lane = threadIdx.x & 31;
-    double mx = 0.0;
+    unsigned long long mx = 0;
     if (Br) {
         const double* col = Br + b * b_stride + (long long)j * ldb;
-        for (int kk = lane; kk < k; kk += 32) mx = isfinite(col[kk]) ? fmax(mx, fabs(col[kk])) : INFINITY;
+        for (int kk = lane; kk < k; kk += 32) mx = max(mx, mag_bits(col[kk]));
     } else {
         const zc* col = B + b * b_stride + (long long)j * ldb;
-        for (int kk = lane; kk < k; kk += 32)
-            mx = (isfinite(col[kk].re) && isfinite(col[kk].im)) ? fmax(mx, fmax(fabs(col[kk].re), fabs(col[kk].im))) : INFINITY;
+        for (int kk = lane; kk < k; kk += 32) mx = max(mx, max(mag_bits(col[kk].re), mag_bits(col[kk].im)));
     }
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     const int e = scale_exponent(mx);
     if (lane == 0) eb[b * n + j] = e;
     const long long plane = (long long)n * Kp;
@@ -431,47 +528,72 @@ __global__ void __launch_bounds__(kThreads, 1)
             tc_fence_after();
             const int d = g_d(plan.g[gi]);
             const int sh = plan.s0 - 8 * (d - 2);
-            const long long mul = sh >= 0 ? (1LL << sh) : 1LL;
-            const int rsh = sh >= 0 ? 0 : -sh;
-            const long long half = rsh ? (1LL << (rsh - 1)) : 0LL;
             const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + buf * kTileN + h * 64;
+            const int lsh = sh >= 0 ? sh : 0, rsh = sh >= 0 ? 0 : -sh;  // one of them is zero
+            const long long half = rsh ? (1LL << (rsh - 1)) : 0LL;
 #pragma unroll
             for (int c16 = 0; c16 < 4; ++c16) {
                 float v[16];
                 tmem_ld16(base + c16 * 16, v);
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const long long gv = (long long)__float2int_rn(v[j]);
-                    acc[c16 * 16 + j] += (gv * mul + half) >> rsh;  // mul = 1 or half = rsh = 0
-                }
+                for (int j = 0; j < 16; ++j)
+                    acc[c16 * 16 + j] += (((long long)__float2int_rn(v[j]) << lsh) + half) >> rsh;
             }
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&ss->tempty[buf]);
         }
         if (ok && !*abort_flag) {
+            // Each lane writes its own row's part of C: row r of C^ is the real (r even) or imaginary part of
+            // row r / 2 of C, so a warp's 32 lanes store 32 consecutive doubles of a column. With s_ab = +-1
+            // and s_c in {0, 1} (every product of the solves) the element is formed without FP64 arithmetic:
+            // C0's part joins the accumulator as an integer count of the same unit, and the sum is rounded
+            // once to a double by integer operations; anything else takes the FP64 path.
             const int r = m0 + q * 32 + lane;  // row of A^
-            const int i = r >> 1;
+            const int i = r >> 1, part = r & 1;
             const int er = (i < m) ? ea[(long long)(a_bcast ? 0 : batch0 + lb) * m + i] : 0;
-            const bool writer = ((lane & 1) == 0) && i < m;
             const int* ebs = eb + (long long)(b_bcast ? 0 : batch0 + lb) * n;
-            zc* Cs = C + (long long)(batch0 + lb) * c_stride;
-            const zc* C0s = C0 ? C0 + (long long)(batch0 + lb) * c0_stride : nullptr;
+            double* Cd = reinterpret_cast<double*>(C + (long long)(batch0 + lb) * c_stride);
+            const double* C0d = C0 && s_c != 0.0 ? reinterpret_cast<const double*>(C0 + (long long)(batch0 + lb) * c0_stride)
+                                                 : nullptr;
+            const bool unit_scales = (s_ab == 1.0 || s_ab == -1.0) && (C0d == nullptr || s_c == 1.0);
+            const bool neg = s_ab < 0.0;
+            // The accumulators go to shared memory first (the stage ring is idle once the last group has
+            // landed; column-major by thread, so a warp's accesses are conflict-free), which keeps the
+            // conversion loop below out of the registers that hold them.
+            long long* sacc = reinterpret_cast<long long*>(smem);
+            const int et = threadIdx.x - 64;
 #pragma unroll
-            for (int c = 0; c < 64; ++c) {
-                const int col = n0 + h * 64 + c;
-                const int e = col < n ? er + ebs[col] : 0;
-                const double v = e >= kNonFinite / 2 ? __longlong_as_double(0x7FF8000000000000LL)
-                                                     : ldexp((double)acc[c], e - 14 - plan.s0);
-                const double im = __shfl_down_sync(0xffffffffu, v, 1);
-                if (writer && col < n) {
-                    zc out{s_ab * v, s_ab * im};
-                    const long long off = (long long)col * ldc + i;
-                    if (C0s && s_c != 0.0) {
-                        const zc c0 = C0s[off];
-                        out = zc{s_c * c0.re + out.re, s_c * c0.im + out.im};
+            for (int c = 0; c < 64; ++c) sacc[c * 256 + et] = acc[c];
+            if (i < m) {
+#pragma unroll 2
+                for (int c = 0; c < 64; ++c) {
+                    const int col = n0 + h * 64 + c;
+                    if (col >= n) break;
+                    const long long ac = sacc[c * 256 + et];
+                    const int e = er + ebs[col];
+                    const long long off2 = 2 * ((long long)col * ldc + i) + part;
+                    double out;
+                    if (e >= kNonFinite / 2) {
+                        out = __longlong_as_double(0x7FF8000000000000LL);
+                    } else {
+                        const int e2 = e - 14 - plan.s0;
+                        long long a = neg ? -ac : ac;
+                        bool fast = unit_scales;
+                        if (fast && C0d) {
+                            long long t;
+                            fast = double_to_units(C0d[off2], e2, t);
+                            a += t;
+                        }
+                        unsigned long long bits;
+                        if (fast && i64_ldexp_bits(a, e2, bits)) {
+                            out = __longlong_as_double((long long)bits);
+                        } else {
+                            out = s_ab * ldexp((double)ac, e2);
+                            if (C0d) out = fma(s_c, C0d[off2], out);
+                        }
                     }
-                    Cs[off] = out;
+                    Cd[off2] = out;
                 }
             }
         }

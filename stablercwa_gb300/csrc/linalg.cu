@@ -185,11 +185,43 @@ void launch_lu_solve(cudaStream_t st, int n, int nrhs, int batch, const zc* a, l
     RCWA_CUDA(cudaGetLastError());
 }
 
+cudaError_t stream_wait(cudaStream_t st) {
+    struct Ev {
+        cudaEvent_t e = nullptr;
+        int device = -1;
+        ~Ev() {
+            if (e) cudaEventDestroy(e);
+        }
+    };
+    thread_local Ev ev;
+    int dev = 0;
+    cudaError_t r = cudaGetDevice(&dev);
+    if (r != cudaSuccess) return r;
+    if (!ev.e || ev.device != dev) {
+        if (ev.e) cudaEventDestroy(ev.e);
+        ev.e = nullptr;
+        r = cudaEventCreateWithFlags(&ev.e, cudaEventBlockingSync | cudaEventDisableTiming);
+        if (r != cudaSuccess) return r;
+        ev.device = dev;
+    }
+    r = cudaEventRecord(ev.e, st);
+    if (r != cudaSuccess) return r;
+    return cudaEventSynchronize(ev.e);
+}
+
 void launch_zgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride, const zc* B,
                   int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc, long long c_stride,
                   double s_ab, double s_c, const int* skip, int skip_value, int tri) {
     if (batch <= 0 || m <= 0 || n <= 0) return;
     TimedLaunch timed(TK_GEMM, st);
+    launch_zgemm_untimed(st, m, n, k, batch, A, lda, a_stride, B, ldb, b_stride, C0, c0_stride, C, ldc, c_stride, s_ab, s_c,
+                         skip, skip_value, tri);
+}
+
+void launch_zgemm_untimed(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride,
+                          const zc* B, int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc,
+                          long long c_stride, double s_ab, double s_c, const int* skip, int skip_value, int tri) {
+    if (batch <= 0 || m <= 0 || n <= 0) return;
     if (k >= 32 && m >= 32 && n >= 32 && tc_gemm_enabled() && !Fp64ProductsGuard::active()) {
         launch_zgemm_tc(st, m, n, k, batch, A, lda, a_stride, B, ldb, b_stride, C0, c0_stride, C, ldc, c_stride, s_ab, s_c,
                         skip, skip_value);

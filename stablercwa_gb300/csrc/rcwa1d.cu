@@ -297,7 +297,7 @@ void sample_fields(Batch& c, const FieldSpec& f, const rcwa_stack1d& stack, int 
             }
         }
         LAUNCH(field_out_kernel, nblocks(tot), kTpb, st, B, n, cnt, nz, d_cols, pol, kx, S, U, Ez, out);
-        RCWA_CUDA(cudaStreamSynchronize(st));  // the host vectors of this group end here
+        RCWA_CUDA(stream_wait(st));  // the host vectors of this group end here
         for (void* p : {(void*)S, (void*)U, (void*)Ez, (void*)d_z, (void*)d_cols})
             if (p) mem.free(p);
     }
@@ -629,7 +629,7 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
                 RCWA_CUDA(cudaMemsetAsync(zero_any, 0, sizeof(int), st));
                 LAUNCH(any_flag_kernel, rb, kTpb, st, B, hz, zero_any);
                 RCWA_CUDA(cudaMemcpyAsync(&any, zero_any, sizeof(int), cudaMemcpyDeviceToHost, st));
-                RCWA_CUDA(cudaStreamSynchronize(st));
+                RCWA_CUDA(stream_wait(st));
                 if (any) {
                     zc* k = c.dense();
                     LAUNCH(scale_rows_kernel, nblocks(nd), kTpb, st, B, n, r.p, refl, k, hz, 0);
@@ -785,7 +785,7 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
     // A singular [[eps]] or [[1/eps]] (TM) fails every sample; checked once at the end.
     int lf = 0;
     RCWA_CUDA(cudaMemcpyAsync(&lf, layer_fail, sizeof(int), cudaMemcpyDeviceToHost, st));
-    RCWA_CUDA(cudaStreamSynchronize(st));
+    RCWA_CUDA(stream_wait(st));
     if (lf) {
         // reference: the TM assembly solve throws NumericalFailure for every point
         const double nan = std::nan("");
@@ -798,7 +798,7 @@ void solve1d_device(cudaStream_t st, const rcwa_stack1d& stack, const double* d_
             std::vector<int> s(n_points, RCWA_SAMPLE_NUMERICAL);
             RCWA_CUDA(cudaMemcpyAsync(d_out.status, s.data(), n_points * sizeof(int), cudaMemcpyHostToDevice, st));
         }
-        RCWA_CUDA(cudaStreamSynchronize(st));
+        RCWA_CUDA(stream_wait(st));
     }
 }
 
@@ -823,7 +823,7 @@ bool prepare_points_device(cudaStream_t st, const rcwa_point1d* d_points, int n_
     LAUNCH(prepare_points_kernel, nblocks(n_points), kTpb, st, n_points, d_points, nI, d_s, d_wl, bad);
     int h = 0;
     RCWA_CUDA(cudaMemcpyAsync(&h, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
-    RCWA_CUDA(cudaStreamSynchronize(st));
+    RCWA_CUDA(stream_wait(st));
     return h == 0;
 }
 
@@ -854,7 +854,7 @@ void fourier_coefficients_api(cudaStream_t st, const double* edges, const rcwa_c
     zc* d = method == 0 ? closed_form_coefficients(st, mem, e, v, period, hmax)
                         : fft_coefficients_dev(st, mem, e, v, period, hmax, samples);
     RCWA_CUDA(cudaMemcpyAsync(out, d, (2 * (size_t)hmax + 1) * sizeof(zc), cudaMemcpyDeviceToHost, st));
-    RCWA_CUDA(cudaStreamSynchronize(st));
+    RCWA_CUDA(stream_wait(st));
 }
 
 }  // namespace rcwa_gb300

@@ -268,13 +268,13 @@ void sample_fields2d(Batch& c, const std::vector<double>& zs, const std::vector<
             zc* e = mem.get<zc>(totN);
             launch_zgemm(st, N, cnt, N, B, ei, N, 0, t, N, (long long)N * cnt, nullptr, 0, e, N, (long long)N * cnt, 1.0, 0.0);
             LAUNCH(fields2d_ez_kernel, nblocks(totN), kTpb, st, B, N, cnt, nz, d_cols, e, nullptr, out);
-            RCWA_CUDA(cudaStreamSynchronize(st));
+            RCWA_CUDA(stream_wait(st));
             mem.free(e);
         } else {
             const zc hs{ie.real(), ie.imag()};
             RCWA_CUDA(cudaMemcpyAsync(scale, &hs, sizeof(zc), cudaMemcpyHostToDevice, st));
             LAUNCH(fields2d_ez_kernel, nblocks(totN), kTpb, st, B, N, cnt, nz, d_cols, t, scale, out);
-            RCWA_CUDA(cudaStreamSynchronize(st));  // the host values of this group end here
+            RCWA_CUDA(stream_wait(st));  // the host values of this group end here
         }
         for (void* p : {(void*)F, (void*)G, (void*)t, (void*)d_z, (void*)d_cols}) mem.free(p);
     }
@@ -371,7 +371,7 @@ void layer_operators2d(cudaStream_t st, const rcwa_layer2d& layer, double Lx, do
     if (cy) RCWA_CUDA(cudaMemcpyAsync(cy, o.cy, NN * sizeof(zc), cudaMemcpyDeviceToHost, st));
     int h_flag = 0;
     RCWA_CUDA(cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
-    RCWA_CUDA(cudaStreamSynchronize(st));
+    RCWA_CUDA(stream_wait(st));
     if (singular) *singular = h_flag;
 }
 
@@ -486,7 +486,7 @@ void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d
     }
     int h_op_flag = 0;
     RCWA_CUDA(cudaMemcpyAsync(&h_op_flag, op_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
-    RCWA_CUDA(cudaStreamSynchronize(st));
+    RCWA_CUDA(stream_wait(st));
     if (h_op_flag) {  // operators or Ei singular / non-finite: every point fails (rcwa2d.hpp:412-418, :1394-1403)
         for (int p : valid) {
             out.status[p] = RCWA_SAMPLE_NUMERICAL;
@@ -894,7 +894,7 @@ void solve2d_host(cudaStream_t st, const rcwa_stack2d& stack, const rcwa_point2d
         RCWA_CUDA(cudaMemcpyAsync(hfail.data(), fail, B * sizeof(int), cudaMemcpyDeviceToHost, st));
         RCWA_CUDA(cudaMemcpyAsync(hinfo.data(), eig_info, B * sizeof(int), cudaMemcpyDeviceToHost, st));
         RCWA_CUDA(cudaMemcpyAsync(hres.data(), resid, B * sizeof(double), cudaMemcpyDeviceToHost, st));
-        RCWA_CUDA(cudaStreamSynchronize(st));
+        RCWA_CUDA(stream_wait(st));
         rcwa_complex* dst[10] = {out.Ex_r, out.Ey_r, out.Ez_r, out.Ex_t, out.Ey_t, out.Ez_t, out.Rs, out.Rp, out.Ts, out.Tp};
         const int n_solve = P + c.n_solve;  // Ei per layer (rcwa2d.hpp:420) plus the chunk's dense solves
         for (int b = 0; b < B; ++b) {

@@ -24,6 +24,10 @@
 
 #include "../../include/stablercwa_gb300.h"
 
+namespace rcwa_gb300 {
+void preload_eig_cluster_kernel();  // eig_cluster.cu
+}
+
 namespace {
 
 using Clock = std::chrono::steady_clock;
@@ -274,6 +278,65 @@ int bucket_of(int order) {
     return b;
 }
 
+// With lazy module loading (the CUDA default) a kernel is loaded at its first launch, and a load may
+// synchronise the context: on a busy server it then waits for every running solve, however long, and
+// each slot whose request meets a kernel for the first time stalls behind the longest one. Small solves of
+// each kind on one context before the slots start load the kernels the requests use (once per process);
+// the cluster eigensolver, which only orders >= 384 reach, is loaded directly.
+void warm_up(rcwa_gpu_ctx* ctx) {
+    static std::once_flag once;
+    std::call_once(once, [ctx] {
+        const double e1[3] = {0.0, 0.3, 1.0}, e2[3] = {0.0, 0.55, 1.0};
+        const rcwa_complex v1[2] = {{1.5, 0.0}, {1.0, 0.0}}, v2[2] = {{1.6, 0.01}, {1.0, 0.0}};
+        rcwa_layer1d L[3] = {};
+        L[0].d = 0.2;
+        L[0].n_segments = 2;
+        L[0].edges = e1;
+        L[0].n_values = v1;
+        L[1].d = 0.1;
+        L[1].homogeneous = 1;
+        L[1].n = {2.0, 0.0};
+        L[2] = L[0];
+        L[2].edges = e2;
+        L[2].n_values = v2;
+        for (int lossy = 0; lossy < 2; ++lossy) {
+            const rcwa_stack1d st{{1.0, 0.0}, {1.46, 0.0}, 1.0, lossy ? 3 : 2, L};
+            for (int M : {20, 60}) {
+                Res1D r;
+                rcwa_result1d v = r.view(2 * M + 1);
+                const rcwa_point1d p{0.7, 10.0};
+                for (int pol = 0; pol < 2; ++pol) rcwa_gpu_solve1d_batch(ctx, &st, &p, 1, M, pol, nullptr, &v);
+            }
+            for (int M : {10, 40}) {
+                ResConical r;
+                rcwa_result_conical v = r.view(2 * M + 1);
+                const rcwa_point_conical p{0.7, 10.0, 20.0};
+                rcwa_gpu_solve_conical_batch(ctx, &st, &p, 1, M, nullptr, &v);
+            }
+        }
+        const double ye[4] = {0.0, 0.3, 0.7, 1.0}, xe0[2] = {0.0, 1.0}, xe1[3] = {0.0, 0.4, 1.0};
+        const rcwa_complex xv0[1] = {{1.0, 0.0}}, xv1[2] = {{2.0, 0.0}, {1.0, 0.0}};
+        const rcwa_xprofile2d rows[3] = {{1, xe0, xv0}, {2, xe1, xv1}, {1, xe0, xv0}};
+        rcwa_layer2d L2[2] = {};
+        L2[0].d = 0.2;
+        L2[0].n_strips = 3;
+        L2[0].y_edges = ye;
+        L2[0].x_profiles = rows;
+        L2[1].d = 0.1;
+        L2[1].homogeneous = 1;
+        L2[1].n = {1.8, 0.0};
+        const rcwa_stack2d st2{1.0, {1.5, 0.0}, 1.0, 1.0, 2, L2};
+        for (int M : {2, 5}) {
+            const int N = (2 * M + 1) * (2 * M + 1);
+            Res2D r;
+            rcwa_result2d v = r.view(N, 2);
+            const rcwa_point2d p{0.7, 10.0, 20.0, {1.0, 0.0}, {0.0, 0.0}};
+            rcwa_gpu_solve2d_batch(ctx, &st2, &p, 1, M, M, 0, nullptr, &v);
+        }
+        rcwa_gb300::preload_eig_cluster_kernel();
+    });
+}
+
 }  // namespace
 
 struct rcwa_gpu_server {
@@ -391,6 +454,7 @@ int rcwa_gpu_server_create(const rcwa_server_config* config, rcwa_gpu_server** o
         cudaSetDevice(s->device);
         s->budget = cudaMemGetInfo(&free_b, &total) == cudaSuccess ? 0.8 * (double)free_b : 8.0 * (1 << 30);
     }
+    warm_up(s->ctxs[0]);
     for (int k = 0; k < slots; ++k) s->workers.emplace_back(&rcwa_gpu_server::worker, s.get(), k);
     *out = s.release();
     return RCWA_OK;

@@ -464,7 +464,7 @@ inline zc* fft_coefficients_dev(cudaStream_t st, DeviceScratch& mem, const std::
     RCWA_CUDA(cudaMemcpyAsync(d_vals, values.data(), values.size() * sizeof(zc), cudaMemcpyHostToDevice, st));
     RCWA_CUDA(cudaMemcpyAsync(d_phase, phase.data(), H * sizeof(zc), cudaMemcpyHostToDevice, st));
     LAUNCH(fft_coeff_kernel, nblocks(H), kTpb, st, hmax, (int)values.size(), (long long)S, d_start, d_vals, d_phase, d);
-    RCWA_CUDA(cudaStreamSynchronize(st));  // the host staging vectors end with this function
+    RCWA_CUDA(stream_wait(st));  // the host staging vectors end with this function
     mem.free(d_start);
     mem.free(d_vals);
     mem.free(d_phase);

@@ -131,6 +131,101 @@ void run(int n, const std::vector<zc>& a, const char* tag, bool real_form, bool 
     if (!ok) ++failures;
 }
 
+// The blocked reduction (herm_panel_one per panel, the trailing update and the back-transformation as
+// plain host products, standing in for the device's batched products), then the same QL and rotation
+// kernels as run(), and X = Q Y applied panel by panel from the stored reflectors and T V^H.
+template <int G>
+void run_blocked(int n, const std::vector<zc>& a, const char* tag) {
+    group_size = G;
+    std::barrier<> b(G);
+    bar = &b;
+    const int nb = kHermNb, P = herm_panel_count(n), pnb = P * nb;
+    std::vector<zc> V((size_t)n * n), W(n), ws(eig_workspace_elems(n)), pan(herm_panel_elems(n)), vall((size_t)n * n),
+        mall((size_t)pnb * n);
+    for (int p = 0; p < P; ++p) {
+        const int k0 = p * nb;
+        std::vector<std::thread> th;
+        for (int l = 0; l < G; ++l)
+            th.emplace_back([&, l] {
+                threadIdx.x = l;
+                herm_panel_one<G>(n, k0, a.data(), ws.data(), pan.data(), vall.data(), mall.data(), pnb);
+            });
+        for (auto& t : th) t.join();
+        if (k0 + nb < n - 1) {  // A(t0:, t0:) -= [V W](t0:, :) Bt(:, t0:)
+            const int t0 = k0 + nb;
+            const zc* VW = pan.data();
+            const zc* Bt = pan.data() + 2LL * nb * n;
+            for (int c = t0; c < n; ++c)
+                for (int r = t0; r < n; ++r) {
+                    zc acc{0.0, 0.0};
+                    for (int q = 0; q < 2 * nb; ++q) acc = acc + VW[(size_t)q * n + r] * Bt[(size_t)c * 2 * nb + q];
+                    ws[(size_t)c * n + r] = ws[(size_t)c * n + r] - acc;
+                }
+        }
+    }
+    int info = -7;
+    unsigned long long rot = 0;
+    threadIdx.x = 0;
+    blockIdx.x = 0;
+    blockIdx.y = 0;
+    blockDim.x = kHermQlThreads;
+    herm_ql_kernel<true>(n, 1, W.data(), &info, ws.data(), 2.220446049250313e-16, 30, &rot);
+    const int* tail = reinterpret_cast<const int*>(ws.data() + 3LL * n * n);
+    if (info != 0 || tail[1] != 0) {
+        std::printf("FAIL blocked %s n=%d: info %d overflow %d\n", tag, n, info, tail[1]);
+        ++failures;
+        return;
+    }
+    std::vector<double> Y((size_t)n * n);
+    for (int r = 0; r < n; ++r) {
+        blockIdx.x = 0;
+        blockIdx.y = r / kHermRows;
+        threadIdx.x = r % kHermRows;
+        herm_apply_real_kernel(n, 1, Y.data(), ws.data(), &info);
+    }
+    blockIdx.y = 0;
+    for (size_t i = 0; i < Y.size(); ++i) V[i] = zc{Y[i], 0.0};
+    for (int p = P - 1; p >= 0; --p) {  // X(r0:, :) -= V_p (M_p X(r0:, :))
+        const int k0 = p * nb, nbp = std::min(nb, n - 1 - k0), r0 = k0 + 1;
+        std::vector<zc> U((size_t)nb * n, zc{0.0, 0.0});
+        for (int c = 0; c < n; ++c)
+            for (int q = 0; q < nbp; ++q) {
+                zc acc{0.0, 0.0};
+                for (int r = r0; r < n; ++r) acc = acc + mall[(size_t)r * pnb + k0 + q] * V[(size_t)c * n + r];
+                U[(size_t)c * nb + q] = acc;
+            }
+        for (int c = 0; c < n; ++c)
+            for (int r = r0; r < n; ++r) {
+                zc acc{0.0, 0.0};
+                for (int q = 0; q < nbp; ++q) acc = acc + vall[(size_t)(k0 + q) * n + r] * U[(size_t)c * nb + q];
+                V[(size_t)c * n + r] = V[(size_t)c * n + r] - acc;
+            }
+    }
+    double fro = 0.0;
+    for (const zc& z : a) fro += norm2(z);
+    fro = std::sqrt(fro);
+    double worst = 0.0, orth = 0.0;
+    for (int j = 0; j < n; ++j) {
+        double dn = 0.0, vn = 0.0;
+        for (int i = 0; i < n; ++i) {
+            zc acc{0.0, 0.0};
+            for (int k = 0; k < n; ++k) acc = acc + a[(size_t)k * n + i] * V[(size_t)j * n + k];
+            dn += norm2(acc - W[j] * V[(size_t)j * n + i]);
+            vn += norm2(V[(size_t)j * n + i]);
+        }
+        worst = std::fmax(worst, std::sqrt(dn) / (std::fmax(fro, 1e-300) * std::sqrt(vn)));
+        for (int k = 0; k < n; ++k) {
+            zc dot{0.0, 0.0};
+            for (int i = 0; i < n; ++i) dot = dot + conj(V[(size_t)j * n + i]) * V[(size_t)k * n + i];
+            orth = std::fmax(orth, zabs(dot - zc{j == k ? 1.0 : 0.0, 0.0}));
+        }
+    }
+    const bool ok = worst <= 1e-13 && orth <= 1e-13 * std::sqrt((double)std::max(n, 1));
+    std::printf("%s blocked %s G=%d n=%d panels %d rotations %llu residual %.2e orth %.2e\n", ok ? "pass" : "FAIL", tag, G,
+                n, P, rot, worst, orth);
+    if (!ok) ++failures;
+}
+
 // the general solver (CORTH + COMQR2, eig_one) with G lanes or a CTA of G threads per matrix
 template <int G>
 void run_general(int n, const std::vector<zc>& a, const char* tag) {
@@ -194,6 +289,24 @@ int main() {
         run<32>(n, t, "toeplitz", true, true);
         run<8>(n, t, "toeplitz", false, true);
         run<4>(n, d, "diagonal", true, true);
+    }
+    for (int n : {64, 65, 97, 121}) {  // the blocked form: full and partial last panels
+        std::vector<zc> r((size_t)n * n), t((size_t)n * n);
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i <= j; ++i) {
+                const zc v{nd(rng), i == j ? 0.0 : nd(rng)};
+                r[(size_t)j * n + i] = v;
+                r[(size_t)i * n + j] = conj(v);
+            }
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i) {
+                const int h = i - j;
+                const double kx = (i - n / 2) * 0.61;
+                const zc c = h == 0 ? zc{2.2, 0.0} : zc{0.6 * std::sin(0.9 * h) / h, 0.6 * (1 - std::cos(0.9 * h)) / h};
+                t[(size_t)j * n + i] = (i == j ? zc{kx * kx, 0.0} : zc{0.0, 0.0}) - c;
+            }
+        run_blocked<16>(n, r, "random");
+        run_blocked<8>(n, t, "toeplitz");
     }
     for (int n : {1, 2, 5, 17, 30}) {
         std::vector<zc> g((size_t)n * n);

@@ -74,3 +74,15 @@ def test_non_finite_propagates(eng):
     ok[0, 3, :] = False
     ok[1, :, 6] = False
     assert np.all(np.isfinite(c[ok]))
+
+
+def test_exact_integer_products_are_bit_exact(eng):
+    """Integer entries up to 2^20 with k = 64: every product and sum is an integer below 2^53, exact in FP64, so
+    the slice product (exact digit products, exact integer accumulation, one final rounding) must return
+    numpy's result bit for bit."""
+    rng = np.random.default_rng(11)
+    batch, m, k, n = 3, 70, 64, 90
+    a = rng.integers(-(1 << 20), 1 << 20, size=(batch, m, k)) + 1j * rng.integers(-(1 << 20), 1 << 20, size=(batch, m, k))
+    b = rng.integers(-(1 << 20), 1 << 20, size=(batch, k, n)) + 1j * rng.integers(-(1 << 20), 1 << 20, size=(batch, k, n))
+    c = eng.multiply_batch(a, b)
+    assert np.array_equal(c, a @ b)
