@@ -59,36 +59,32 @@ def workload(seed=SEED, n_points=N_POINTS, ridge=1.46):
     return stack, pts, {"fill": float(fill), "depth": float(depth)}
 
 
-# DRAM bytes per matrix of the Hermitian eigensolve stage at n = 121 (tridiagonalisation 54.3 MB, real
-# rotations 1.2 MB, Q Y 0.6 MB), from one ncu --set full capture of 2432 matrices of this order; the QL
-# kernel's bytes are not included
-HERM_STAGE_DRAM_BYTES_PER_MATRIX_N121 = 56.1e6
+# DRAM bytes per matrix of the Hermitian eigensolve stage at n = 121 (blocked tridiagonalisation 22.0 MB,
+# its tensor-core trailing updates and the back-transformation with their digit splits 8.5 MB, QL 0.3 MB,
+# rotations on the real identity 1.2 MB, the rest 1.0 MB), from one ncu capture of every launch of one
+# 4096-matrix eigensolve of this order
+HERM_STAGE_DRAM_BYTES_PER_MATRIX_N121 = 33.0e6
 
 
-HERM_STAGE_KERNELS = ("eigensolve stage: herm_reduce_batch_kernel + herm_ql_kernel + herm_apply_real_kernel + "
-                      "zdgemm_kernel")
+HERM_STAGE_KERNELS = ("eigensolve stage: herm_panel_batch_kernel (blocked tridiagonalisation, FP64) + tensor-core "
+                      "trailing updates + herm_ql_kernel + herm_apply_real_kernel (QL and its rotations on a real "
+                      "identity, FP64) + tensor-core back-transformation")
 
 
 def herm_flops_text(n, rotations_per_matrix):
-    return (f"Hermitian path at order {n}: tridiagonalisation with Q {herm_reduction_flops(n)} flops per matrix, "
-            f"6 n per QL rotation applied to a real identity ({rotations_per_matrix:.0f} rotations per matrix "
-            f"measured), Q Y 4 n^3")
+    vec = (f"QL rotations 6 n each ({rotations_per_matrix:.0f} per matrix measured)" if rotations_per_matrix > 0
+           else "divide and conquer 8/3 n^3")
+    return (f"Hermitian eigensolve at order {n}: tridiagonalisation 16/3 n^3, tridiagonal eigenvectors by {vec}, "
+            f"back-transformation Q Y 4 n^3 (real flops per matrix)")
 
 
 def herm_eig_flops(n, rotations_per_matrix):
-    """Flops of one Hermitian eigensolve as the engine runs it: the tridiagonalisation, then (n <= 887) the
-    QL rotations applied to a real identity (6 n each) and the complex-by-real product Q Y (4 n^3), or the
-    rotations applied to the complex Q in place (12 n each)."""
-    if n <= 887:
-        return herm_reduction_flops(n) + 6 * n * rotations_per_matrix + 4 * n ** 3
-    return herm_reduction_flops(n) + 12 * n * rotations_per_matrix
-
-
-def herm_reduction_flops(n):
-    """Real flops of the Householder tridiagonalisation with the reflectors accumulated, as the eigensolver
-    performs it: per step with a trailing block of order m, the product A v (8 m^2), the rank-2 update of
-    the whole block (16 m^2) and the accumulation of the reflector into Q (16 m^2)."""
-    return 40 * sum(m * m for m in range(1, n))
+    """Algorithmic real flops of one Hermitian eigensolve with eigenvectors: the Householder tridiagonalisation
+    (16/3 n^3, LAPACK's zhetrd count), the tridiagonal eigenvectors (divide and conquer: about 8/3 n^3 for the
+    merge products without deflation; or, when the QL iteration runs, 6 n per measured rotation), and the
+    back-transformation of the real eigenvectors by Q (4 n^3)."""
+    vec = 6 * n * rotations_per_matrix if rotations_per_matrix > 0 else (8 / 3) * n ** 3
+    return (16 / 3) * n ** 3 + vec + 4 * n ** 3
 
 
 def engine_flops_per_solve(n, pol, rotations_per_matrix, reduced=True):
@@ -103,7 +99,7 @@ def engine_flops_per_solve(n, pol, rotations_per_matrix, reduced=True):
                  L^-1 B L^-H from the layer's constant parts (O(n^2)), then L^-H Y and L Y, 2 products with a
                  triangular factor (4 n^3 each)."""
     lu, tri, mm = (8 / 3) * n ** 3, 8 * n ** 3, 8 * n ** 3
-    herm = rotations_per_matrix > 0
+    herm = not os.environ.get("RCWA_GB300_HERMITIAN", "").startswith("0")
     eig = herm_eig_flops(n, rotations_per_matrix) if herm else 105 * n ** 3
     if reduced:
         seams = (lu + tri) + (mm + lu + 8 * n ** 2)
@@ -376,7 +372,8 @@ def run_ours(args):
                                   "all_status_ok": bool(ok), "max_energy_defect_all_points": energy}
 
     eig_avg_ms = eig_ms / max(1, eig_launches)
-    herm = rotations > 0  # the grating's real permittivities take the Hermitian eigensolver
+    # the grating's real permittivities take the Hermitian eigensolver unless it is switched off
+    herm = not os.environ.get("RCWA_GB300_HERMITIAN", "").startswith("0")
     rot_per_matrix = rotations / (args.steps * 2 * P)  # the timed steps' TE and TM matrices
     reduced = os.environ.get("RCWA_GB300_SEAMS", "") != "reference"
     if herm:
@@ -402,10 +399,12 @@ def run_ours(args):
                 "gpu_launches": launches,
                 "roofline": {"bound": "fp64", "kernel": (HERM_STAGE_KERNELS if herm else "eig_batch_kernel"),
                              "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                             "traffic": (HERM_STAGE_DRAM_BYTES_PER_MATRIX_N121 * P if herm and n == 121 else None),
-                             "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's "
-                                                "kernels per matrix (2432-matrix capture) x matrices per launch; "
-                                                "QL kernel not included" if herm and n == 121 else None),
+                             "traffic": (HERM_STAGE_DRAM_BYTES_PER_MATRIX_N121 * P
+                                         if herm and n == 121 and HERM_STAGE_DRAM_BYTES_PER_MATRIX_N121 else None),
+                             "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of every launch of "
+                                                "one eigensolve call per matrix (4096-matrix capture) x matrices per "
+                                                "launch" if herm and n == 121 and HERM_STAGE_DRAM_BYTES_PER_MATRIX_N121
+                                                else None),
                              "flops_model": (herm_flops_text(n, rot_per_matrix) if herm
                                              else "general QR: 105 n^3 per matrix"),
                              "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (torch.matmul float64), best of 5",
@@ -633,7 +632,7 @@ def run_secondary(args):
     eng.set_kernel_timing(True)
     step()
     roof_kernel, flops_model = "eig_batch_kernel", "general QR: 105 n^3 per matrix"
-    if herm_model and rotations > 0:
+    if herm_model and not os.environ.get("RCWA_GB300_HERMITIAN", "").startswith("0"):
         # lossless layers: the Hermitian eigensolver; the model counts its matrices only (the few conical
         # Schur-basis eigensolves of order 2N inside the same timer are not counted)
         mats, order = herm_model
@@ -681,15 +680,17 @@ def run_secondary(args):
 
 # ------------------------------------------------------------------------------------- serving
 
-def serve_requests(seed, count):
+def serve_requests(seed, count, repeat=1):
     """The serving mix: 70 % 1-D (M 20..150, 1..30 layers, each a grating with p 0.3 and at least one,
     K 2..5 random edges, n 1.0..2.5 + i 0..0.05, films likewise, period 0.5..1.5, lambda 0.4..1.6,
     theta 0..70, TE/TM), 20 % conical (M 20..60, built like config 3), 10 % 2-D (Mx = My 5..12,
-    built like config 4). Returns (kind, stack, args) tuples."""
+    built like config 4). Returns (kind, stack, args) tuples. With repeat > 1 every drawn request is
+    followed by repeat - 1 more of the same structure and truncation at new seeded points (a client
+    scanning wavelengths and angles of one design)."""
     from stablercwa_gb300 import Layer, Stack
     rng = np.random.default_rng(seed)
     out = []
-    for _ in range(count):
+    for _ in range((count + repeat - 1) // repeat):
         u = rng.uniform()
         if u < 0.7:
             period = rng.uniform(0.5, 1.5)
@@ -718,7 +719,14 @@ def serve_requests(seed, count):
             stack, pts, _ = workload_c4(int(rng.integers(0, 1 << 30)))
             Mx = int(rng.integers(5, 13))
             out.append(("2d", stack, dict(wavelength=rng.uniform(0.4, 1.2), M1=Mx, M2=Mx, jones=(pts[0][3], pts[0][4]))))
-    return out
+        kind, stack, a = out[-1]
+        for _ in range(repeat - 1):  # the same design at other points
+            b = dict(a)
+            b["wavelength"] = a["wavelength"] * rng.uniform(0.9, 1.1)
+            if "theta" in b:
+                b["theta"] = min(70.0, a["theta"] + rng.uniform(0.0, 5.0))
+            out.append((kind, stack, b))
+    return out[:count]
 
 
 def serve_submit(srv, req):
@@ -730,11 +738,11 @@ def serve_submit(srv, req):
     return srv.submit_2d(stack, a["wavelength"], 0.0, 0.0, a["M1"], a["M2"], a["jones"])
 
 
-def serve_run(reqs, slots, rate=None, seed=0):
+def serve_run(reqs, slots, rate=None, seed=0, max_batch=0):
     """Submit reqs (all at once, or with Poisson arrivals at `rate` per second) to a server with
     `slots` worker slots; returns (makespan s, latencies s, per-kind latencies, statuses)."""
     from stablercwa_gb300.engine import Server
-    srv = Server(slots=slots)
+    srv = Server(slots=slots, max_batch=max_batch)
     rng = np.random.default_rng(seed)
     arrivals = np.zeros(len(reqs)) if rate is None else np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
     t0 = time.perf_counter()
@@ -762,7 +770,7 @@ def serving_sample(args):
     the same requests one at a time on one slot (the plain one-request-per-launch path)."""
     reqs = serve_requests(SEED + 5, args.serve_sample)
     mk, lat, kinds, ok = serve_run(reqs, args.serve_slots)
-    mk1, lat1, _, ok1 = serve_run(reqs, 1)
+    mk1, lat1, _, ok1 = serve_run(reqs, 1, max_batch=1)
     return {"value": len(reqs) / mk, "unit": "solves/s", "requests": len(reqs),
             "kinds": {k: len(v) for k, v in kinds.items()}, "slots": args.serve_slots,
             "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)), "makespan_s": mk,
@@ -789,9 +797,18 @@ def run_serve(args):
         stats[f"poisson_{frac:g}x"] = {"offered_per_s": frac * capacity, "solves_per_s": len(reqs) / mk, **summary(lat),
                                         "all_ok": ok,
                                         "by_kind": {k: {**summary(np.array(v)), "count": len(v)} for k, v in kinds.items()}}
-    mk, lat, kinds, ok = serve_run(reqs, 1)
+    mk, lat, kinds, ok = serve_run(reqs, 1, max_batch=1)
     stats["plain_one_slot"] = {"solves_per_s": len(reqs) / mk, "makespan_s": mk, **summary(lat), "all_ok": ok,
                                "by_kind": {k: {**summary(np.array(v)), "count": len(v)} for k, v in kinds.items()}}
+    if args.serve_repeat > 1:
+        # the same mix where each design is requested at several points: same-structure requests share calls
+        rreqs = serve_requests(SEED + 5, args.serve_requests, args.serve_repeat)
+        mk, lat, kinds, ok = serve_run(rreqs, args.serve_slots)
+        mk1, lat1, _, ok1 = serve_run(rreqs, 1, max_batch=1)
+        stats[f"repeat_{args.serve_repeat}"] = {
+            "solves_per_s": len(rreqs) / mk, "makespan_s": mk, **summary(lat), "all_ok": ok and ok1,
+            "plain_one_slot_solves_per_s": len(rreqs) / mk1, "served_over_plain": mk1 / mk,
+            "by_kind": {k: {**summary(np.array(v)), "count": len(v)} for k, v in kinds.items()}}
     head = stats.get("poisson_1x", stats["saturated"])
     line = {"metric": "served solves/s and p50/p99 latency, mixed 1-D / conical / 2-D requests (70/20/10)",
             "value": head["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
@@ -890,6 +907,8 @@ def main():
                     help="timed steps of the absorbing-grating C2 line in the headline run (0: skip)")
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-slots", type=int, default=48)
+    ap.add_argument("--serve-repeat", type=int, default=8,
+                    help="--workload serve: also run the mix with each design requested at this many points (1: skip)")
     ap.add_argument("--serve-sample", type=int, default=40,
                     help="requests of the serving mix run in the headline line (0: skip)")
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[0.5, 1.0])

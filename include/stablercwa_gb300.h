@@ -489,6 +489,7 @@ typedef struct rcwa_server_config {
     int slots;              /* concurrent requests on the device (worker slots); 0 = 32 */
     size_t hbm_budget;      /* bytes the admitted requests may hold together; 0 = 80 % of free memory */
     int max_bypass_ms;      /* how long backfilling may pass over the oldest request; 0 = 2000 */
+    int max_batch;          /* queued requests of one structure solved together in one call; 0 = 256, 1 = never */
 } rcwa_server_config;
 
 typedef struct rcwa_request {
@@ -513,6 +514,7 @@ typedef struct rcwa_response {
     double start_s;
     double finish_s;
     double footprint_bytes;  /* device footprint the admission charged */
+    int batch;               /* requests solved in the same call as this one (1: alone) */
 } rcwa_response;
 
 typedef struct rcwa_gpu_server rcwa_gpu_server;

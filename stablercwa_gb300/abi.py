@@ -320,7 +320,8 @@ RCWA_REQ_2D = 2
 
 
 class rcwa_server_config(C.Structure):
-    _fields_ = [("device", C.c_int), ("slots", C.c_int), ("hbm_budget", C.c_size_t), ("max_bypass_ms", C.c_int)]
+    _fields_ = [("device", C.c_int), ("slots", C.c_int), ("hbm_budget", C.c_size_t), ("max_bypass_ms", C.c_int),
+                ("max_batch", C.c_int)]
 
 
 class rcwa_request(C.Structure):
@@ -344,4 +345,4 @@ class rcwa_request(C.Structure):
 
 class rcwa_response(C.Structure):
     _fields_ = [("code", C.c_int), ("slot", C.c_int), ("submit_s", C.c_double), ("start_s", C.c_double),
-                ("finish_s", C.c_double), ("footprint_bytes", C.c_double)]
+                ("finish_s", C.c_double), ("footprint_bytes", C.c_double), ("batch", C.c_int)]

@@ -173,6 +173,23 @@ __global__ void real_to_complex_kernel(long long count, const double* __restrict
     if (i < count) x[i] = zc{y[i], 0.0};
 }
 
+template <int G>
+void herm_dc_launch(cudaStream_t st, int n, int batch, zc* ws, double* y, zc* w, int* info, double eps, int max_iter) {
+    const int tpb = 128;
+    const unsigned blocks = (unsigned)(((long long)batch * G + tpb - 1) / tpb);
+    herm_dc_batch_kernel<G><<<blocks, tpb, 0, st>>>(n, batch, ws, y, w, info, eps, max_iter);
+    ++launch_count();
+    RCWA_CUDA(cudaGetLastError());
+}
+
+// divide and conquer (eig.cuh herm_dc_one) in place of the QL iteration and its rotations, for batched groups
+// of lanes, when RCWA_GB300_HERM_DC=1. Off by default: on this GPU it is FP64-bound with about half of
+// each warp's lanes active (4096 matrices of order 121: 244 ms against 203 ms for QL and the rotations).
+bool herm_dc_wanted(int group) {
+    const char* env = std::getenv("RCWA_GB300_HERM_DC");
+    return env && env[0] == '1' && group <= 32;
+}
+
 // the blocked reduction replaces the unblocked one for batched groups of lanes where the products run on the
 // tensor cores; RCWA_GB300_HERM_BLOCKED=0 keeps the unblocked kernel
 bool herm_blocked_wanted(int n, int group) {
@@ -228,8 +245,16 @@ void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a
     } else {
         herm_reduce_dispatch(st, n, batch, a, a_stride, q, ws, group);
     }
+    const bool dc = real_form && herm_dc_wanted(group);
     const size_t qsm = (size_t)2 * n * kHermQlThreads * sizeof(double);
-    if (qsm <= 227 * 1024) {
+    if (dc) {
+        switch (group) {
+            case 4: herm_dc_launch<4>(st, n, batch, ws, y, w, info, eps, max_iter); break;
+            case 8: herm_dc_launch<8>(st, n, batch, ws, y, w, info, eps, max_iter); break;
+            case 16: herm_dc_launch<16>(st, n, batch, ws, y, w, info, eps, max_iter); break;
+            default: herm_dc_launch<32>(st, n, batch, ws, y, w, info, eps, max_iter); break;
+        }
+    } else if (qsm <= 227 * 1024) {
         if (qsm > 48 * 1024) {
             static int opted = 0;  // the largest opt-in requested so far
             if ((int)qsm > opted) {
@@ -257,9 +282,11 @@ void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a
                 opted = (int)ysm;
             }
         }
-        const dim3 grid((unsigned)batch, (unsigned)((n + kHermRows - 1) / kHermRows));
-        herm_apply_real_kernel<<<grid, kHermRows, ysm, st>>>(n, batch, y, ws, info);
-        RCWA_CUDA(cudaGetLastError());
+        if (!dc) {  // divide and conquer has left Y in y already
+            const dim3 grid((unsigned)batch, (unsigned)((n + kHermRows - 1) / kHermRows));
+            herm_apply_real_kernel<<<grid, kHermRows, ysm, st>>>(n, batch, y, ws, info);
+            RCWA_CUDA(cudaGetLastError());
+        }
         if (blocked) {
             const long long cnt = (long long)batch * n * n;
             real_to_complex_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, st>>>(cnt, y, v);
@@ -268,7 +295,7 @@ void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a
         } else {
             launch_zdgemm(st, n, n, n, batch, q, n, (long long)n * n, y, n, (long long)n * n, v, n, (long long)n * n, only, 1);
         }
-        launch_count() += 5;
+        launch_count() += dc ? 3 : 5;  // the overflow flags, the fused redo, and the reduction or r2c; QL and rotations
     } else {
         herm_apply_kernel<<<(unsigned)(((long long)batch * n + 127) / 128), 128, 0, st>>>(n, batch, v, ws, info);
         RCWA_CUDA(cudaGetLastError());

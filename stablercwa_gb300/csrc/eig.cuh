@@ -1151,6 +1151,415 @@ __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, zc* __re
     }
 }
 
+// ---------------------------------------------------------------- (2') divide and conquer on (d, e)
+//
+// The eigenvectors Y of the real tridiagonal T = tridiag(e, d, e) by Cuppen's divide and conquer with the
+// Gu-Eisenstat eigenvectors (Gu and Eisenstat, "A divide-and-conquer algorithm for the symmetric tridiagonal
+// eigenproblem", SIAM J. Matrix Anal. Appl. 16, 1995; the merge and deflation steps of LAPACK's dstedc /
+// dlaed0-dlaed4, restated), as the replacement of the QL iteration plus its rotations applied to a real
+// identity: T is torn at the boundaries of 2^L leaves of at most kDcLeaf rows (T = diag(T_1, T_2) +
+// |beta| u u^T with u = e_b + sign(beta) e_{b+1}, the two touching diagonal entries lowered by |beta|), each
+// leaf is solved by the QL iteration with its rotations applied directly, and neighbouring blocks are merged
+// level by level: with Q = diag(Q_1, Q_2), D their eigenvalues and z = Q^T u, the merged problem is
+// D + rho z z^T. Entries with rho |z_i| below tol and pairs of nearly equal d_i (a rotation of theirs whose
+// coupling is below tol) deflate; the k others give the secular equation 1 + rho sum z_i^2 / (d_i - lambda)
+// = 0 with one root in each gap, found from the nearer pole (the differences d_i - lambda kept exact) by a
+// two-pole rational model (Bunch, Nielsen and Sorensen 1978) safeguarded by bisection; z is then recomputed
+// from the roots by Loewner's formula, so the eigenvectors (z_i / (d_i - lambda_j), normalised) are
+// orthogonal to working accuracy, and Y's block takes Y U. Work per matrix: the products Y U (about m^3 for
+// a merge of order m) and O(k^2) per merge for the roots, against 6 n flops for each of the ~n^2 QL
+// rotations; the roots and the products are spread over the group's lanes instead of one thread's chain.
+constexpr int kDcLeaf = 8;
+
+// QL with Wilkinson shifts on a leaf: d[0..m), e[0..m-1), eigenvectors into the m x m block y (leading
+// dimension ld), which it sets to the identity first. 0, or l + 1 when eigenvalue l did not converge.
+__device__ inline int dc_leaf(int m, double* d, double* e, double* y, int ld, double eps, int max_iter) {
+    for (int j = 0; j < m; ++j)
+        for (int i = 0; i < m; ++i) y[(long long)j * ld + i] = i == j ? 1.0 : 0.0;
+    if (m <= 1) return 0;
+    e[m - 1] = 0.0;
+    for (int l = 0; l < m; ++l) {
+        for (int its = 0;; ++its) {
+            int mm = l;
+            for (; mm < m - 1; ++mm) {
+                const double dd = fabs(d[mm]) + fabs(d[mm + 1]);
+                if (fabs(e[mm]) <= eps * dd || fabs(e[mm]) <= DBL_MIN) break;
+            }
+            if (mm == l) break;
+            if (its >= max_iter) return l + 1;
+            double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+            double r = hypot(g, 1.0);
+            g = d[mm] - d[l] + e[l] / (g + copysign(r, g));
+            double s = 1.0, c = 1.0, p = 0.0;
+            bool split = false;
+            for (int i = mm - 1; i >= l; --i) {
+                const double f = s * e[i], b = c * e[i];
+                r = hypot(f, g);
+                e[i + 1] = r;
+                if (r == 0.0) {
+                    d[i + 1] -= p;
+                    e[mm] = 0.0;
+                    split = true;
+                    break;
+                }
+                s = f / r;
+                c = g / r;
+                g = d[i + 1] - p;
+                r = (d[i] - g) * s + 2.0 * c * b;
+                p = s * r;
+                d[i + 1] = g + p;
+                g = c * r - b;
+                double* yi = y + (long long)i * ld;
+                double* yj = yi + ld;
+                for (int q = 0; q < m; ++q) {
+                    const double a0 = yi[q], a1 = yj[q];
+                    yj[q] = s * a0 + c * a1;
+                    yi[q] = c * a0 - s * a1;
+                }
+            }
+            if (!split) {
+                d[l] -= p;
+                e[l] = g;
+                e[mm] = 0.0;
+            }
+        }
+    }
+    return 0;
+}
+
+// Root j of 1 + sum_i w_i / (d_i - lambda) = 0 (d ascending, w_i = rho z_i^2 > 0): lambda in (d_j, d_{j+1}),
+// or in (d_{k-1}, d_{k-1} + sum w) for j = k - 1. Returns the pole o it is measured from and tau = lambda -
+// d_o; every d_i - lambda is then formed as (d_i - d_o) - tau.
+__device__ inline void dc_root(int k, int j, const double* d, const double* w, double wsum, double eps, int& o,
+                               double& tau) {
+    double lo, hi;
+    if (j < k - 1) {
+        const double mid = 0.5 * (d[j + 1] - d[j]);
+        double f = 1.0;
+        for (int i = 0; i < k; ++i) f += w[i] / ((d[i] - d[j]) - mid);
+        if (f > 0.0) {  // f rises through each gap: the root lies left of the middle
+            o = j;
+            lo = 0.0;
+            hi = mid;
+        } else {
+            o = j + 1;
+            lo = -mid;
+            hi = 0.0;
+        }
+    } else {
+        o = j;
+        lo = 0.0;
+        hi = wsum;
+    }
+    const double dl = d[j] - d[o], dr = j < k - 1 ? d[j + 1] - d[o] : 0.0;  // the two poles, shifted
+    tau = 0.5 * (lo + hi);
+    for (int it = 0; it < 200; ++it) {
+        double psi = 0.0, dpsi = 0.0, phi = 0.0, dphi = 0.0;
+        for (int i = 0; i < k; ++i) {
+            const double r = 1.0 / ((d[i] - d[o]) - tau);
+            const double v = w[i] * r;
+            if (i <= j) {
+                psi += v;
+                dpsi += v * r;
+            } else {
+                phi += v;
+                dphi += v * r;
+            }
+        }
+        const double f = 1.0 + psi + phi;
+        if (f == 0.0) return;
+        if (f > 0.0) hi = tau;
+        else lo = tau;
+        if (hi - lo <= 2.0 * eps * fmax(fabs(lo), fabs(hi))) break;
+        // two-pole model c + s1 / (DL - eta) + s2 / (DR - eta) = 0 (one pole for the last root)
+        const double DL = dl - tau, s1 = DL * DL * dpsi;
+        double next;
+        if (j < k - 1) {
+            const double DR = dr - tau, s2 = DR * DR * dphi;
+            const double c = f - DL * dpsi - DR * dphi;
+            const double B = c * (DL + DR) + s1 + s2, C = c * DL * DR + s1 * DR + s2 * DL;
+            double eta;
+            if (c == 0.0) {
+                eta = C / B;
+            } else {
+                const double disc = sqrt(fmax(0.0, B * B - 4.0 * c * C));
+                const double q = B >= 0.0 ? B + disc : B - disc;
+                const double r1 = q / (2.0 * c), r2 = q != 0.0 ? 2.0 * C / q : r1;
+                eta = (r1 > DL && r1 < DR) ? r1 : r2;
+            }
+            next = tau + eta;
+        } else {
+            const double c = f - DL * dpsi;
+            next = c > 0.0 ? tau + DL + s1 / c : 0.5 * (lo + hi);
+        }
+        if (!(next > lo && next < hi)) next = 0.5 * (lo + hi);
+        const bool done = fabs(next - tau) <= 4.0 * eps * fabs(next);
+        tau = next;
+        if (done) break;
+    }
+}
+
+// an unsigned integer that orders finite doubles as their values (the sign-magnitude bits mapped to a
+// monotone range), so comparisons run on the integer pipe
+__device__ __forceinline__ unsigned long long dc_order_key(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// Merge of the block [o, o + m) of y (its halves [o, o + n1) and [o + n1, o + m) already diagonalised, their
+// eigenvalues in lam) across the tear beta. Scratch from sc: 8 m doubles, 3 m ints, 2 m^2 doubles.
+template <int G>
+__device__ void dc_merge(int n, int o, int n1, int m, double beta, double* y, double* lam, double* sc, double eps,
+                         const Grp<G>& grp) {
+    const int g = threadIdx.x & (G - 1);
+    double* D = sc;            // unsorted eigenvalues of the halves
+    double* Z = D + m;         // z
+    double* ds = Z + m;        // sorted d, rotated by deflation
+    double* zs = ds + m;       // sorted z
+    double* dk = zs + m;       // the k secular poles
+    double* wk = dk + m;       // rho z^2 of the poles
+    double* tk = wk + m;       // roots: tau
+    double* zh = tk + m;       // Loewner z
+    int* perm = reinterpret_cast<int*>(zh + m);  // sorted position -> block column
+    int* nd = perm + m;                          // secular pole -> sorted position
+    int* ok = nd + m;                            // root -> its origin pole; [m] k, [m+1] rotations
+    double* U = reinterpret_cast<double*>(ok + m + 2 + ((m + 2) & 1));  // k x k (column-major)
+    double* tmp = U + (long long)m * m;          // m x k
+    const double sg = beta >= 0.0 ? 1.0 : -1.0;
+    double zz = 0.0;
+    for (int i = g; i < m; i += G) {
+        D[i] = lam[o + i];
+        Z[i] = i < n1 ? y[(long long)(o + i) * n + o + n1 - 1] : sg * y[(long long)(o + i) * n + o + n1];
+        zz += Z[i] * Z[i];
+    }
+    zz = grp.sum(zz);
+    const double rho = fabs(beta) * zz, zscale = 1.0 / sqrt(zz);
+    grp.sync();
+    for (int i = g; i < m; i += G) {  // rank sort, ties by index; doubles compared as ordered integer keys
+        const double di = D[i];
+        const unsigned long long ki = dc_order_key(di);
+        int r = 0;
+        for (int q = 0; q < m; ++q) {
+            const unsigned long long kq = dc_order_key(D[q]);
+            r += (kq < ki || (kq == ki && q < i)) ? 1 : 0;
+        }
+        perm[r] = i;
+        ds[r] = di;
+        zs[r] = Z[i] * zscale;
+    }
+    grp.sync();
+    double dmax = 0.0, zmax = 0.0;
+    for (int i = g; i < m; i += G) {
+        dmax = fmax(dmax, fabs(ds[i]));
+        zmax = fmax(zmax, fabs(zs[i]));
+    }
+    dmax = grp.max(dmax);
+    zmax = grp.max(zmax);
+    const double tol = 8.0 * eps * fmax(dmax, rho * zmax);
+    // deflation scan (one lane): small rho z_i, then nearly equal poles rotated together; the rotations are
+    // kept (in tk, zh, nd as c, s, pair) and applied to y's columns afterwards in order
+    if (g == 0) {
+        int nrot = 0, pj = -1;
+        for (int j = 0; j < m; ++j) {
+            if (rho * fabs(zs[j]) <= tol) continue;  // deflated: eigenpair (ds[j], column perm[j])
+            if (pj >= 0) {
+                const double c0 = zs[j], s0 = zs[pj], t = hypot(c0, s0);
+                const double c = c0 / t, s = -s0 / t;
+                if (fabs((ds[j] - ds[pj]) * c * s) <= tol) {
+                    zs[j] = t;
+                    zs[pj] = 0.0;
+                    const double dp = ds[pj] * c * c + ds[j] * s * s;
+                    ds[j] = ds[pj] * s * s + ds[j] * c * c;
+                    ds[pj] = dp;
+                    tk[nrot] = c;
+                    zh[nrot] = s;
+                    ok[nrot] = pj;  // the pair (pj, j), stashed below
+                    nd[nrot] = j;
+                    ++nrot;
+                }
+            }
+            pj = j;
+        }
+        ok[m] = nrot;
+        // rotations are applied below before nd / ok are rebuilt: stash them in U's space
+        for (int r = 0; r < nrot; ++r) {
+            U[4 * r] = tk[r];
+            U[4 * r + 1] = zh[r];
+            U[4 * r + 2] = (double)ok[r];
+            U[4 * r + 3] = (double)nd[r];
+        }
+        int q = 0;
+        for (int j = 0; j < m; ++j)
+            if (zs[j] != 0.0 && rho * fabs(zs[j]) > tol) nd[q++] = j;
+        ok[m + 1] = q;
+    }
+    grp.sync();
+    const int nrot = ok[m], k = ok[m + 1];
+    // the deflation rotations on y's columns (rows of the block), in order: col_p' = c col_p + s col_j,
+    // col_j' = c col_j - s col_p
+    for (int r = 0; r < nrot; ++r) {
+        const double c = U[4 * r], s = U[4 * r + 1];
+        double* yp = y + (long long)(o + perm[(int)U[4 * r + 2]]) * n + o;
+        double* yj = y + (long long)(o + perm[(int)U[4 * r + 3]]) * n + o;
+        for (int i = g; i < m; i += G) {
+            const double a = yp[i], b = yj[i];
+            yp[i] = c * a + s * b;
+            yj[i] = c * b - s * a;
+        }
+    }
+    grp.sync();
+    for (int i = g; i < k; i += G) {
+        dk[i] = ds[nd[i]];
+        wk[i] = rho * zs[nd[i]] * zs[nd[i]];
+    }
+    double wsum = 0.0;
+    for (int i = g; i < k; i += G) wsum += rho * zs[nd[i]] * zs[nd[i]];
+    wsum = grp.sum(wsum);
+    grp.sync();
+    for (int j = g; j < k; j += G) {
+        int oj;
+        double t;
+        dc_root(k, j, dk, wk, wsum, eps, oj, t);
+        ok[j] = oj;
+        tk[j] = t;
+    }
+    grp.sync();
+    // Loewner: zh_i^2 = prod_j (lambda_j - d_i) / (rho prod_{j != i} (d_j - d_i)), each root paired with a
+    // neighbouring pole so the partial products stay near one
+    for (int i = g; i < k; i += G) {
+        double p = -((dk[i] - dk[ok[k - 1]]) - tk[k - 1]) / rho;  // lambda_{k-1} - d_i
+        for (int j = 0; j < k - 1; ++j) {
+            const double lj = -((dk[i] - dk[ok[j]]) - tk[j]);  // lambda_j - d_i
+            p *= j < i ? lj / (dk[j] - dk[i]) : lj / (dk[j + 1] - dk[i]);
+        }
+        const double zi = zs[nd[i]];
+        zh[i] = copysign(sqrt(fabs(p)), zi);
+    }
+    grp.sync();
+    for (int j = g; j < k; j += G) {  // the merged eigenvectors, normalised
+        double* u = U + (long long)j * k;
+        double nrm = 0.0;
+        for (int i = 0; i < k; ++i) {
+            const double v = zh[i] / ((dk[i] - dk[ok[j]]) - tk[j]);
+            u[i] = v;
+            nrm += v * v;
+        }
+        const double inv = 1.0 / sqrt(nrm);
+        for (int i = 0; i < k; ++i) u[i] *= inv;
+    }
+    grp.sync();
+    // y's columns of the poles <- (those columns) U; lam <- roots and deflated values. tmp holds the k
+    // columns (m rows, column-major), so the lanes' row accesses are consecutive
+    for (int l = 0; l < k; ++l) {
+        const double* yc = y + (long long)(o + perm[nd[l]]) * n + o;
+        for (int i = g; i < m; i += G) tmp[(long long)l * m + i] = yc[i];
+    }
+    grp.sync();
+    for (int j0 = 0; j0 < k; j0 += 4) {  // four output columns per pass over tmp
+        const int nj = min(4, k - j0);
+        const double* u0 = U + (long long)j0 * k;
+        const double* u1 = nj > 1 ? u0 + k : u0;
+        const double* u2 = nj > 2 ? u0 + 2 * k : u0;
+        const double* u3 = nj > 3 ? u0 + 3 * k : u0;
+        for (int i = g; i < m; i += G) {
+            double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+            for (int l = 0; l < k; ++l) {
+                const double t = tmp[(long long)l * m + i];
+                a0 = fma(t, u0[l], a0);
+                a1 = fma(t, u1[l], a1);
+                a2 = fma(t, u2[l], a2);
+                a3 = fma(t, u3[l], a3);
+            }
+            y[(long long)(o + perm[nd[j0]]) * n + o + i] = a0;
+            if (nj > 1) y[(long long)(o + perm[nd[j0 + 1]]) * n + o + i] = a1;
+            if (nj > 2) y[(long long)(o + perm[nd[j0 + 2]]) * n + o + i] = a2;
+            if (nj > 3) y[(long long)(o + perm[nd[j0 + 3]]) * n + o + i] = a3;
+        }
+    }
+    for (int q = g; q < m; q += G) lam[o + perm[q]] = ds[q];  // deflated values (the poles' are replaced below)
+    grp.sync();
+    for (int j = g; j < k; j += G) lam[o + perm[nd[j]]] = dk[ok[j]] + tk[j];
+    grp.sync();
+}
+
+// The whole solve for one matrix: d, e at ws + 2 n^2 (as the reductions leave them), eigenvalues to w,
+// eigenvectors to y (n x n, column-major), info 0 or the failing leaf's QL index; scratch in ws [0, 2 n^2)
+// doubles and ws + n^2 onwards.
+template <int G>
+__device__ void herm_dc_one(int n, zc* __restrict__ ws, double* __restrict__ y, zc* __restrict__ w, int* info, double eps,
+                            int max_iter) {
+    const int g = threadIdx.x & (G - 1);
+    const Grp<G> grp(nullptr, nullptr);
+    const double* src = reinterpret_cast<const double*>(ws + 2LL * n * n);
+    double* d = reinterpret_cast<double*>(ws + 3LL * n * n + 2LL * n);  // own copies: d, e, lam, the tears
+    double* e = d + n;
+    double* lam = e + n;
+    double* sc = reinterpret_cast<double*>(ws);  // merge scratch: 2 n^2 + 11 n doubles fit in [0, 2 n^2 + ...)
+    int L = 0;
+    while ((n >> L) > kDcLeaf) ++L;
+    const int leaves = 1 << L;
+    for (int i = g; i < n; i += G) {
+        d[i] = src[i];
+        e[i] = i < n - 1 ? src[n + i] : 0.0;
+    }
+    grp.sync();
+    // tears at every leaf boundary b (between rows b - 1 and b); beta stays in e[b - 1]
+    if (g == 0)
+        for (int q = 1; q < leaves; ++q) {
+            const int b = (int)(((long long)q * n) >> L);
+            const double a = fabs(e[b - 1]);
+            d[b - 1] -= a;
+            d[b] -= a;
+        }
+    grp.sync();
+    int bad = 0;
+    for (int q = g; q < leaves; q += G) {
+        const int b0 = (int)(((long long)q * n) >> L), b1 = (int)(((long long)(q + 1) * n) >> L);
+        double* dl = lam + b0;
+        double el[kDcLeaf + 1];
+        for (int i = b0; i < b1; ++i) {
+            dl[i - b0] = d[i];
+            el[i - b0] = i < b1 - 1 ? e[i] : 0.0;
+        }
+        const int r = dc_leaf(b1 - b0, dl, el, y + (long long)b0 * n + b0, n, eps, max_iter);
+        if (r && !bad) bad = b0 + r;
+    }
+    // zero the off-diagonal blocks of y
+    for (long long idx = g; idx < (long long)n * n; idx += G) {
+        const int col = (int)(idx / n), row = (int)(idx - (long long)col * n);
+        const int qc = (int)((((long long)col + 1) << L) - 1) / n, qr = (int)((((long long)row + 1) << L) - 1) / n;
+        if (qc != qr) y[idx] = 0.0;
+    }
+    bad = (int)grp.max((double)bad);
+    grp.sync();
+    for (int lev = L - 1; lev >= 0; --lev) {
+        const int blocks = 1 << lev;
+        for (int q = 0; q < blocks; ++q) {
+            const int o = (int)(((long long)q * n) >> lev), mid = (int)(((long long)(2 * q + 1) * n) >> (lev + 1));
+            const int end = (int)(((long long)(q + 1) * n) >> lev);
+            const double beta = e[mid - 1];
+            if (beta != 0.0) dc_merge<G>(n, o, mid - o, end - o, beta, y, lam, sc, eps, grp);
+        }
+    }
+    for (int i = g; i < n; i += G) w[i] = zc{lam[i], 0.0};
+    if (g == 0) {
+        *info = bad;
+        int* tail = reinterpret_cast<int*>(ws + 3LL * n * n);  // no rotation log: nothing overflowed
+        tail[0] = 0;
+        tail[1] = 0;
+    }
+}
+
+template <int G>
+__global__ void __launch_bounds__(128) herm_dc_batch_kernel(int n, int batch, zc* __restrict__ ws, double* __restrict__ y,
+                                                            zc* __restrict__ w, int* __restrict__ info, double eps,
+                                                            int max_iter) {
+    const long long gid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    if (gid >= batch) return;
+    herm_dc_one<G>(n, ws + gid * eig_workspace_elems(n), y + gid * (long long)n * n, w + gid * n, info + gid, eps,
+                   max_iter);
+}
+
 // (3) the logged rotations applied to Z (in v), thread per (matrix, row)
 static __global__ void __launch_bounds__(128) herm_apply_kernel(int n, int batch, zc* __restrict__ v, const zc* __restrict__ ws,
                                                          const int* __restrict__ info) {

@@ -112,6 +112,7 @@ void launch_zdgemm_tc(cudaStream_t st, int m, int n, int k, int batch, const zc*
                       const double* B, int ldb, long long b_stride, zc* C, int ldc, long long c_stride,
                       const int* skip = nullptr, int skip_value = 1);
 bool tc_gemm_enabled();
+bool tc_gemm_wanted(int m, int n, int k);  // this product goes to the tensor cores (linalg.cu)
 // Products launched by this host thread while a guard lives stay on the FP64 pipe (the 2-D solve: its
 // operands span many decades within a row or column, where an FP64 product's error, relative to the
 // terms it sums, is smaller than the slice products', relative to the row and column maxima).

@@ -267,6 +267,27 @@ __device__ __forceinline__ uint16_t bf16_int(long long d) {
 // bit 55 - 8 s and taken out of Y before the next, so each lies in [-128, 128] and carries weight
 // 2^(-7 - 8 s); an eighth digit is the remainder itself, in units of 2^-63. A non-finite x (whose row or
 // column then carries kNonFinite) gives zero digits.
+__device__ __forceinline__ void split_digits(double x, int e, int S, uint16_t* dg) {
+    if (mag_bits(x) >= kMagInf || e == kNonFinite) {
+        for (int s = 0; s < S; ++s) dg[s] = 0;
+        return;
+    }
+    long long Y = fixed62(x, e);
+#pragma unroll 1
+    for (int s = 0; s < S; ++s) {
+        const int sh = 55 - 8 * s;
+        long long d;
+        if (sh > 0) {
+            d = (Y + (1LL << (sh - 1))) >> sh;
+            Y -= d * (1LL << sh);
+        } else {
+            d = Y * (1LL << -sh);
+            Y = 0;
+        }
+        dg[s] = bf16_int(d);
+    }
+}
+
 __device__ __forceinline__ void store_digits(double x, int e, int S, uint16_t* out, long long plane_stride) {
     if (mag_bits(x) >= kMagInf || e == kNonFinite) {
         for (int s = 0; s < S; ++s) out[s * plane_stride] = 0;
@@ -324,15 +345,22 @@ __global__ void __launch_bounds__(256) tc_split_a_kernel(int m, int k, int Kp, i
             tile[il][q] = (kk < k && i < m) ? As[(long long)kk * lda + i] : zc{0.0, 0.0};
         }
         __syncthreads();
+        // each value is split once: Re A(i, kk) goes to row 2i at kk and row 2i+1 at k + kk, Im A(i, kk) to row
+        // 2i+1 at kk and, negated digit by digit (the negated digits sum exactly to -Im A), to row 2i at k + kk
         for (int idx = t; idx < 64 * 32; idx += 256) {
-            const int rr = idx >> 5, c = idx & 31, kk = kc + c;
-            const int i = i0 + (rr >> 1), part = rr & 1;
+            const int vi = idx >> 5, c = idx & 31, kk = kc + c;
+            const int il2 = vi >> 1, im_part = vi & 1, i = i0 + il2;
             if (i >= m || kk >= k) continue;
-            const zc v = tile[rr >> 1][c];
-            const int e = sexp[rr >> 1];
-            uint16_t* row = o + (2LL * i + part) * Kp;
-            store_digits(part ? v.im : v.re, e, S, row + kk, plane);
-            if (!real_b) store_digits(part ? v.re : -v.im, e, S, row + k + kk, plane);
+            const zc v = tile[il2][c];
+            uint16_t dg[kMaxSlices];
+            split_digits(im_part ? v.im : v.re, sexp[il2], S, dg);
+            uint16_t* first = o + (2LL * i + im_part) * Kp + kk;
+            for (int s2 = 0; s2 < S; ++s2) first[s2 * plane] = dg[s2];
+            if (!real_b) {
+                uint16_t* second = o + (2LL * i + (1 - im_part)) * Kp + k + kk;
+                for (int s2 = 0; s2 < S; ++s2)
+                    second[s2 * plane] = im_part && dg[s2] ? (uint16_t)(dg[s2] ^ 0x8000u) : dg[s2];
+            }
         }
         __syncthreads();
     }
@@ -380,6 +408,27 @@ __global__ void __launch_bounds__(128) tc_split_b_kernel(int n, int k, int Kp, i
 }
 
 // ---------------------------------------------------------------- the product
+
+// One element of C from its int64 accumulator ac (units of 2^(e - 14 - s0)), e = ea + eb: s_ab = +-1 and
+// s_c in {0, 1} (unit_scales) without FP64 arithmetic (C0's part joins as an integer count of the same unit,
+// one rounding to double by integer operations), anything else in FP64; NaN for a non-finite row or column.
+__device__ __forceinline__ double finish_element(long long ac, int e, int s0, bool neg, bool unit_scales, const double* C0d,
+                                                 long long off2, double s_ab, double s_c) {
+    if (e >= kNonFinite / 2) return __longlong_as_double(0x7FF8000000000000LL);
+    const int e2 = e - 14 - s0;
+    long long a = neg ? -ac : ac;
+    bool fast = unit_scales;
+    if (fast && C0d) {
+        long long t;
+        fast = double_to_units(C0d[off2], e2, t);
+        a += t;
+    }
+    unsigned long long bits;
+    if (fast && i64_ldexp_bits(a, e2, bits)) return __longlong_as_double((long long)bits);
+    double out = s_ab * ldexp((double)ac, e2);
+    if (C0d) out = fma(s_c, C0d[off2], out);
+    return out;
+}
 
 struct SharedState {
     uint64_t full[kStages], empty[kStages], tfull[2], tempty[2], drain;
@@ -573,27 +622,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const long long ac = sacc[c * 256 + et];
                     const int e = er + ebs[col];
                     const long long off2 = 2 * ((long long)col * ldc + i) + part;
-                    double out;
-                    if (e >= kNonFinite / 2) {
-                        out = __longlong_as_double(0x7FF8000000000000LL);
-                    } else {
-                        const int e2 = e - 14 - plan.s0;
-                        long long a = neg ? -ac : ac;
-                        bool fast = unit_scales;
-                        if (fast && C0d) {
-                            long long t;
-                            fast = double_to_units(C0d[off2], e2, t);
-                            a += t;
-                        }
-                        unsigned long long bits;
-                        if (fast && i64_ldexp_bits(a, e2, bits)) {
-                            out = __longlong_as_double((long long)bits);
-                        } else {
-                            out = s_ab * ldexp((double)ac, e2);
-                            if (C0d) out = fma(s_c, C0d[off2], out);
-                        }
-                    }
-                    Cd[off2] = out;
+                    Cd[off2] = finish_element(ac, e, plan.s0, neg, unit_scales, C0d, off2, s_ab, s_c);
                 }
             }
         }
@@ -603,6 +632,246 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (warp == 1) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    }
+}
+
+// ---------------------------------------------------------------- the slice-resident product
+//
+// The same product with each operand tile loaded once per K block instead of once per digit pair: a CTA
+// computes a 128 x 64 tile of C^; per K block of 64 the producer loads the S slices of B's 64 rows (one B
+// stage, S x 8 KB, double-buffered) and then the S slices of A's 128 rows one after another (a 4-deep
+// ring of 16 KB), and A slice s meets every B slice t with s + t <= S - 1 (0-based) while it is resident:
+// 4 MMAs (M 128, N 64, K 16) per pair into the tensor-memory accumulator of its diagonal s + t (S
+// accumulators of 64 columns). 168 KB of operand tiles feed 28 pairs per K block for S = 7, against 32 KB
+// per pair in the kernel above: about 2.7x fewer bytes per MMA. Every accumulator sums at most S pairs over
+// K chunks of 128 (S x 128 x 2^14 <= 2^24, exact in FP32); after each chunk the eight epilogue warps add
+// the S accumulators into their int64 registers at each diagonal's weight (the same units as above) while
+// the MMA warp waits for them, then the last chunk's sums are converted as above.
+constexpr int kTileNr = 64;                                   // columns of C^ per CTA
+constexpr int kBStage = kMaxSlices * kTileNr * kTileK * 2;     // one K block of every B slice: 64 KB
+constexpr int kATile = kTileM * kTileK * 2;                    // one A slice tile: 16 KB
+constexpr int kARing = 4;
+constexpr int kChunkKb = 2;                                    // K blocks per exact accumulation chunk
+constexpr uint32_t kIdescN64 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTileNr >> 3) << 17) |
+                               ((uint32_t)(kTileM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16_n64(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdescN64), "r"(accumulate)
+        : "memory");
+}
+
+struct SharedStateR {
+    uint64_t afull[kARing], aempty[kARing], bfull[2], bempty[2], tfull, tempty, drain;
+    uint32_t tmem_base;
+    int abort_flag;
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_gemm_resident_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int S,
+                            int s0, int kblocks, int m, int n, int batch0, int a_bcast, int b_bcast,
+                            const int* __restrict__ ea, const int* __restrict__ eb, const zc* C0, long long c0_stride,
+                            zc* C, int ldc, long long c_stride, double s_ab, double s_c, const int* __restrict__ skip,
+                            int skip_value, int* __restrict__ err) {
+    const int lb = blockIdx.z;
+    if (skip && skip[batch0 + lb] == skip_value) return;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    unsigned char* bst = smem;                    // 2 B stages
+    unsigned char* ast = smem + 2 * kBStage;      // the A ring
+    SharedStateR* ss = reinterpret_cast<SharedStateR*>(ast + kARing * kATile);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.y * kTileM, n0 = blockIdx.x * kTileNr;
+    const int nchunks = (kblocks + kChunkKb - 1) / kChunkKb;
+
+    if (threadIdx.x == 0) {
+        for (int r = 0; r < kARing; ++r) {
+            mbar_init(&ss->afull[r], 1);
+            mbar_init(&ss->aempty[r], 1);
+        }
+        for (int r = 0; r < 2; ++r) {
+            mbar_init(&ss->bfull[r], 1);
+            mbar_init(&ss->bempty[r], 1);
+        }
+        mbar_init(&ss->tfull, 1);
+        mbar_init(&ss->tempty, 8);
+        mbar_init(&ss->drain, 1);
+        ss->abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&ss->tmem_base)),
+                     "r"(512)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        tc_fence_before();
+    }
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = ss->tmem_base;
+    volatile int* abort_flag = &ss->abort_flag;
+    const int za = a_bcast ? 0 : lb, zb = b_bcast ? 0 : lb;
+
+    if (warp == 0) {
+        // ---- TMA producer: per K block one B stage (all slices), then the A slices through the ring
+        if (lane == 0) {
+            bool ok = true;
+            int ai = 0, bi = 0;
+            int aissued[kARing], bissued[2];
+            for (int r = 0; r < kARing; ++r) aissued[r] = -1;
+            bissued[0] = bissued[1] = -1;
+            for (int kb = 0; kb < kblocks && ok; ++kb) {
+                const int b = bi & 1, bph = (bi >> 1) & 1;
+                if (!mbar_wait(&ss->bempty[b], bph ^ 1, abort_flag, err)) {
+                    ok = false;
+                    break;
+                }
+                mbar_expect_tx(&ss->bfull[b], (uint32_t)(S * kTileNr * kTileK * 2));
+                for (int t = 0; t < S; ++t)
+                    tma_load_3d(bst + b * kBStage + t * (kTileNr * kTileK * 2), &map_b, kb * kTileK, n0, zb * S + t,
+                                &ss->bfull[b]);
+                bissued[b] = bi;
+                ++bi;
+                for (int sl = 0; sl < S; ++sl, ++ai) {
+                    const int r = ai % kARing, aph = (ai / kARing) & 1;
+                    if (!mbar_wait(&ss->aempty[r], aph ^ 1, abort_flag, err)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_expect_tx(&ss->afull[r], (uint32_t)kATile);
+                    tma_load_3d(ast + r * kATile, &map_a, kb * kTileK, m0, za * S + sl, &ss->afull[r]);
+                    aissued[r] = ai;
+                }
+            }
+            if (!ok) {  // drain: wait (bounded) for the copies this thread started
+                for (int r = 0; r < kARing; ++r) {
+                    if (aissued[r] < 0) continue;
+                    const int ph = (aissued[r] / kARing) & 1;
+                    for (unsigned it = 0; it < kWaitLimit && !mbar_try_wait(&ss->afull[r], ph); ++it) {
+                    }
+                }
+                for (int r = 0; r < 2; ++r) {
+                    if (bissued[r] < 0) continue;
+                    const int ph = (bissued[r] >> 1) & 1;
+                    for (unsigned it = 0; it < kWaitLimit && !mbar_try_wait(&ss->bfull[r], ph); ++it) {
+                    }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        // ---- MMA issuer
+        if (lane == 0) {
+            bool ok = true, any = false;
+            int ai = 0, bi = 0;
+            for (int c = 0; c < nchunks && ok; ++c) {
+                if (!mbar_wait(&ss->tempty, (c & 1) ^ 1, abort_flag, err)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const int kb0 = c * kChunkKb, kb1 = min(kblocks, kb0 + kChunkKb);
+                for (int kb = kb0; kb < kb1 && ok; ++kb) {
+                    const int b = bi & 1, bph = (bi >> 1) & 1;
+                    if (!mbar_wait(&ss->bfull[b], bph, abort_flag, err)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t b_base = smem_u32(bst + b * kBStage);
+                    for (int sl = 0; sl < S; ++sl, ++ai) {
+                        const int r = ai % kARing, aph = (ai / kARing) & 1;
+                        if (!mbar_wait(&ss->afull[r], aph, abort_flag, err)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t a_addr = smem_u32(ast + r * kATile);
+                        for (int t = 0; t + sl < S; ++t) {
+                            const uint32_t b_addr = b_base + t * (kTileNr * kTileK * 2);
+                            const uint32_t d_tmem = tmem + (uint32_t)((sl + t) * kTileNr);
+#pragma unroll
+                            for (int kk = 0; kk < kTileK / 16; ++kk) {
+                                const uint32_t acc = (kb == kb0 && sl == 0 && kk == 0) ? 0u : 1u;
+                                mma_bf16_n64(d_tmem, smem_desc_sw128(a_addr + kk * 32), smem_desc_sw128(b_addr + kk * 32),
+                                             acc);
+                            }
+                        }
+                        any = true;
+                        mma_commit(&ss->aempty[r]);  // the A tile is free once these products have read it
+                    }
+                    if (!ok) break;
+                    mma_commit(&ss->bempty[b]);
+                    ++bi;
+                }
+                if (ok) mma_commit(&ss->tfull);
+            }
+            if (!ok && any) {
+                mma_commit(&ss->drain);
+                for (unsigned it = 0; it < kWaitLimit && !mbar_try_wait(&ss->drain, 0); ++it) {
+                }
+            }
+        }
+    } else {
+        // ---- epilogue: warps 2..9; lane quarter q of tensor memory, column half h (32 of the 64 columns)
+        const int q = warp & 3, h = (warp - 2) >> 2;
+        long long acc[32];
+#pragma unroll
+        for (int cc = 0; cc < 32; ++cc) acc[cc] = 0;
+        bool ok = true;
+        for (int c = 0; c < nchunks; ++c) {
+            ok = mbar_wait(&ss->tfull, c & 1, abort_flag, err);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) break;
+            tc_fence_after();
+            for (int dg = 0; dg < S; ++dg) {  // diagonal dg = s + t enters at 2^(s0 - 8 dg)
+                const int sh = s0 - 8 * dg;
+                const int lsh = sh >= 0 ? sh : 0, rsh = sh >= 0 ? 0 : -sh;
+                const long long half = rsh ? (1LL << (rsh - 1)) : 0LL;
+                const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(dg * kTileNr + h * 32);
+#pragma unroll
+                for (int c16 = 0; c16 < 2; ++c16) {
+                    float v[16];
+                    tmem_ld16(base + c16 * 16, v);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        acc[c16 * 16 + j] += (((long long)__float2int_rn(v[j]) << lsh) + half) >> rsh;
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&ss->tempty);
+        }
+        if (ok && !*abort_flag) {
+            const int r = m0 + q * 32 + lane;  // row of A^
+            const int i = r >> 1, part = r & 1;
+            const int er = (i < m) ? ea[(long long)(a_bcast ? 0 : batch0 + lb) * m + i] : 0;
+            const int* ebs = eb + (long long)(b_bcast ? 0 : batch0 + lb) * n;
+            double* Cd = reinterpret_cast<double*>(C + (long long)(batch0 + lb) * c_stride);
+            const double* C0d = C0 && s_c != 0.0 ? reinterpret_cast<const double*>(C0 + (long long)(batch0 + lb) * c0_stride)
+                                                 : nullptr;
+            const bool unit_scales = (s_ab == 1.0 || s_ab == -1.0) && (C0d == nullptr || s_c == 1.0);
+            const bool neg = s_ab < 0.0;
+            long long* sacc = reinterpret_cast<long long*>(ast);  // the A ring is idle after the last chunk
+            const int et = threadIdx.x - 64;
+#pragma unroll
+            for (int cc = 0; cc < 32; ++cc) sacc[cc * 256 + et] = acc[cc];
+            if (i < m) {
+#pragma unroll 2
+                for (int cc = 0; cc < 32; ++cc) {
+                    const int col = n0 + h * 32 + cc;
+                    if (col >= n) break;
+                    const long long off2 = 2 * ((long long)col * ldc + i) + part;
+                    Cd[off2] = finish_element(sacc[cc * 256 + et], er + ebs[col], s0, neg, unit_scales, C0d, off2, s_ab, s_c);
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
     }
 }
 
@@ -626,12 +895,12 @@ EncodeTiled encode_fn() {
     return fn;
 }
 
-// digit planes (planes x rows x Kp bf16, K contiguous) as a 3-D tensor map with 64 x 128 boxes
-CUtensorMap plane_map(const uint16_t* base, long long rows, int Kp, long long planes) {
+// digit planes (planes x rows x Kp bf16, K contiguous) as a 3-D tensor map with 64 x box_rows boxes
+CUtensorMap plane_map(const uint16_t* base, long long rows, int Kp, long long planes, int box_rows = kTileM) {
     CUtensorMap map;
     const cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)planes};
     const cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)rows * Kp * 2};
-    const cuuint32_t box[3] = {(cuuint32_t)kTileK, (cuuint32_t)kTileM, 1};
+    const cuuint32_t box[3] = {(cuuint32_t)kTileK, (cuuint32_t)box_rows, 1};
     const cuuint32_t estr[3] = {1, 1, 1};
     const CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<uint16_t*>(base), dims, strides,
                                    box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -677,6 +946,19 @@ int* error_flag() {
 
 }  // namespace
 
+// the slice-resident kernel when RCWA_GB300_TC_KERNEL=resident. Not the default: it moves 2.7x fewer bytes
+// from L2 per MMA but measured slower (4096 products of order 121: 9.8 ms against 8.8 ms; tensor pipe 17 %
+// against 22 %): its tiles are half as wide, so twice the CTAs pay the per-tile setup and epilogue, and its
+// single set of accumulators makes the MMAs wait for every chunk's drain. A persistent form that overlaps
+// one tile's epilogue with the next tile's products is what it needs.
+bool tc_gemm_resident() {
+    static const bool on = [] {
+        const char* e = std::getenv("RCWA_GB300_TC_KERNEL");
+        return e && std::strcmp(e, "resident") == 0;
+    }();
+    return on;
+}
+
 int tc_gemm_slices() {
     static const int s = [] {
         const char* e = std::getenv("RCWA_GB300_TC_SLICES");
@@ -714,11 +996,17 @@ void tc_product(cudaStream_t st, int m, int n, int k, int batch, const zc* A, in
                 const double* Br, int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc,
                 long long c_stride, double s_ab, double s_c, const int* skip, int skip_value) {
     if (batch <= 0 || m <= 0 || n <= 0) return;
-    const int smem_bytes = kStages * kStageBytes + 1024 + (int)sizeof(SharedState) + 64;
+    const bool resident = tc_gemm_resident();
+    const int smem_bytes = resident ? 2 * kBStage + kARing * kATile + 1024 + (int)sizeof(SharedStateR) + 64
+                                    : kStages * kStageBytes + 1024 + (int)sizeof(SharedState) + 64;
     static std::once_flag attr_once;
     static cudaError_t attr_rc = cudaSuccess;
     std::call_once(attr_once, [&] {
-        attr_rc = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+        attr_rc = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       kStages * kStageBytes + 1024 + (int)sizeof(SharedState) + 64);
+        if (attr_rc == cudaSuccess)
+            attr_rc = cudaFuncSetAttribute(tc_gemm_resident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           2 * kBStage + kARing * kATile + 1024 + (int)sizeof(SharedStateR) + 64);
     });
     RCWA_CUDA(attr_rc);
     const int real_b = Br != nullptr;
@@ -741,7 +1029,7 @@ void tc_product(cudaStream_t st, int m, int n, int k, int batch, const zc* A, in
     RCWA_CUDA(cudaMallocAsync(&dea, sizeof(int) * (size_t)m * (a_bcast ? 1 : batch), st));
     RCWA_CUDA(cudaMallocAsync(&deb, sizeof(int) * (size_t)n * (b_bcast ? 1 : batch), st));
     const CUtensorMap map_a = plane_map(pa, 2LL * m, Kp, (long long)na * S);
-    const CUtensorMap map_b = plane_map(pb, n, Kp, (long long)nb * S);
+    const CUtensorMap map_b = plane_map(pb, n, Kp, (long long)nb * S, resident ? kTileNr : kTileN);
     if (a_bcast) {
         tc_split_a_kernel<<<dim3((m + 31) / 32, 1), 256, 0, st>>>(m, k, Kp, S, real_b, A, lda, 0, pa, dea);
         ++launch_count();
@@ -763,9 +1051,16 @@ void tc_product(cudaStream_t st, int m, int n, int k, int batch, const zc* A, in
                 ldb, b_stride, pb, deb + (long long)b0 * n);
             ++launch_count();
         }
-        const dim3 grid((n + kTileN - 1) / kTileN, (2 * m + kTileM - 1) / kTileM, cb);
-        tc_gemm_kernel<<<grid, kThreads, smem_bytes, st>>>(map_a, map_b, plan, m, n, b0, a_bcast, b_bcast, dea, deb, C0,
-                                                           c0_stride, C, ldc, c_stride, s_ab, s_c, skip, skip_value, err);
+        if (resident) {
+            const dim3 grid((n + kTileNr - 1) / kTileNr, (2 * m + kTileM - 1) / kTileM, cb);
+            tc_gemm_resident_kernel<<<grid, kThreads, smem_bytes, st>>>(map_a, map_b, S, plan.s0, Kp / kTileK, m, n, b0,
+                                                                        a_bcast, b_bcast, dea, deb, C0, c0_stride, C, ldc,
+                                                                        c_stride, s_ab, s_c, skip, skip_value, err);
+        } else {
+            const dim3 grid((n + kTileN - 1) / kTileN, (2 * m + kTileM - 1) / kTileM, cb);
+            tc_gemm_kernel<<<grid, kThreads, smem_bytes, st>>>(map_a, map_b, plan, m, n, b0, a_bcast, b_bcast, dea, deb, C0,
+                                                               c0_stride, C, ldc, c_stride, s_ab, s_c, skip, skip_value, err);
+        }
         ++launch_count();
         RCWA_CUDA(cudaGetLastError());
     }

@@ -93,7 +93,7 @@ constexpr int kPanel = 32;
 void zgemm_raw(cudaStream_t st, int m, int n, int k, int batch, const zc* A, int lda, long long a_stride, const zc* B,
                int ldb, long long b_stride, zc* C, int ldc, long long c_stride, double s_ab, const int* skip, int skip_value) {
     if (batch <= 0 || m <= 0 || n <= 0 || k <= 0) return;
-    if (k >= 32 && m >= 32 && n >= 32 && tc_gemm_enabled() && !Fp64ProductsGuard::active()) {
+    if (tc_gemm_wanted(m, n, k)) {
         launch_zgemm_tc(st, m, n, k, batch, A, lda, a_stride, B, ldb, b_stride, C, c_stride, C, ldc, c_stride, s_ab, 1.0,
                         skip, skip_value);
         return;
@@ -185,6 +185,16 @@ void launch_lu_solve(cudaStream_t st, int n, int nrhs, int batch, const zc* a, l
     RCWA_CUDA(cudaGetLastError());
 }
 
+// The tensor-core product costs about the same per tile of the real-ified product whatever m and n fill of
+// it, and its digit planes are padded to 64 in K; the FP64 kernel costs 8 m n k flops at 1.1 TFLOP/s. A
+// product goes to the tensor cores when every dimension is at least 16 and m n k >= 2^15 (a 57 x 57 x 32
+// trailing update or a 24 x 121 x 120 back-transformation panel does; an order-25 trailing update of
+// 25 x 25 x 32, or a one-column solve, does not).
+bool tc_gemm_wanted(int m, int n, int k) {
+    return k >= 16 && m >= 16 && n >= 16 && (long long)m * n * k >= (1LL << 15) && tc_gemm_enabled() &&
+           !Fp64ProductsGuard::active();
+}
+
 cudaError_t stream_wait(cudaStream_t st) {
     struct Ev {
         cudaEvent_t e = nullptr;
@@ -222,7 +232,7 @@ void launch_zgemm_untimed(cudaStream_t st, int m, int n, int k, int batch, const
                           const zc* B, int ldb, long long b_stride, const zc* C0, long long c0_stride, zc* C, int ldc,
                           long long c_stride, double s_ab, double s_c, const int* skip, int skip_value, int tri) {
     if (batch <= 0 || m <= 0 || n <= 0) return;
-    if (k >= 32 && m >= 32 && n >= 32 && tc_gemm_enabled() && !Fp64ProductsGuard::active()) {
+    if (tc_gemm_wanted(m, n, k)) {
         launch_zgemm_tc(st, m, n, k, batch, A, lda, a_stride, B, ldb, b_stride, C0, c0_stride, C, ldc, c_stride, s_ab, s_c,
                         skip, skip_value);
         return;
@@ -239,7 +249,7 @@ void launch_zdgemm(cudaStream_t st, int m, int n, int k, int batch, const zc* A,
                    const double* B, int ldb, long long b_stride, zc* C, int ldc, long long c_stride, const int* skip,
                    int skip_value) {
     if (batch <= 0 || m <= 0 || n <= 0) return;
-    if (k >= 32 && m >= 32 && n >= 32 && tc_gemm_enabled() && !Fp64ProductsGuard::active()) {
+    if (tc_gemm_wanted(m, n, k)) {
         launch_zdgemm_tc(st, m, n, k, batch, A, lda, a_stride, B, ldb, b_stride, C, ldc, c_stride, skip, skip_value);
         return;
     }

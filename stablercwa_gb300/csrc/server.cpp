@@ -6,7 +6,10 @@
 // fits, otherwise the oldest request of another bucket that fits (backfilling), unless the oldest
 // request has already waited longer than max_bypass_ms, in which case the slot waits for memory to
 // be released. A request alone on the device is always admitted. Requests on different slots run
-// concurrently, so work arriving while others are on the device overlaps with them.
+// concurrently, so work arriving while others are on the device overlaps with them. A slot that takes a
+// request also takes the queued requests that differ from it only in the point (same kind, stack, orders,
+// polarization or factorization, and options: the same structure at other wavelengths, angles or Jones
+// vectors), up to max_batch of them while they fit the budget, and solves them in one batched call.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -16,6 +19,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <string>
 #include <new>
 #include <thread>
 #include <vector>
@@ -231,6 +235,8 @@ struct Res2D {
 struct Job {
     unsigned long long ticket = 0;
     rcwa_request req{};
+    std::string key;  // everything but the point: requests with equal keys can share one batched call
+    int batch = 1;    // requests in the call that solved this one
     Owned1D s1;
     Owned2D s2;
     int order = 0;
@@ -264,6 +270,72 @@ double footprint_of(const Job& j) {
             return z * n * n * (5.0 * j.s2.patterned + 3.0 * (j.s2.stack.n_layers + 1) + 8.0) + (1 << 20);
         }
     }
+}
+
+// The batching key: kind, orders, polarization / factorization, options and the stack's contents, as bytes
+// (field by field, so no padding enters).
+template <class T>
+void add_bytes(std::string& k, const T& v) {
+    k.append(reinterpret_cast<const char*>(&v), sizeof v);
+}
+template <class T>
+void add_array(std::string& k, const T* p, size_t n) {
+    if (p && n) k.append(reinterpret_cast<const char*>(p), n * sizeof(T));
+}
+std::string key_of(const Job& j) {
+    std::string k;
+    const rcwa_request& r = j.req;
+    add_bytes(k, r.kind);
+    add_bytes(k, r.M);
+    add_bytes(k, r.polarization);
+    add_bytes(k, r.M1);
+    add_bytes(k, r.M2);
+    add_bytes(k, r.factorization);
+    add_bytes(k, r.options.eig_method);
+    add_bytes(k, r.options.linear_solver);
+    add_bytes(k, r.options.homogeneous_fast_path);
+    add_bytes(k, r.options.diagnostics);
+    add_bytes(k, r.options.eig_max_iter);
+    add_bytes(k, r.options.eig_eps);
+    if (r.kind == RCWA_REQ_2D) {
+        const rcwa_stack2d& s = j.s2.stack;
+        add_bytes(k, s.nI);
+        add_bytes(k, s.nII);
+        add_bytes(k, s.Lx);
+        add_bytes(k, s.Ly);
+        add_bytes(k, s.n_layers);
+        for (int l = 0; l < s.n_layers; ++l) {
+            const rcwa_layer2d& L = j.s2.layers[l];
+            add_bytes(k, L.d);
+            add_bytes(k, L.homogeneous);
+            add_bytes(k, L.n);
+            add_bytes(k, L.n_strips);
+            add_array(k, j.s2.y_edges[l].data(), j.s2.y_edges[l].size());
+            for (size_t q = 0; q < j.s2.rows[l].size(); ++q) {
+                add_bytes(k, j.s2.rows[l][q].n_segments);
+                add_array(k, j.s2.x_edges[l][q].data(), j.s2.x_edges[l][q].size());
+                add_array(k, j.s2.n_values[l][q].data(), j.s2.n_values[l][q].size());
+            }
+        }
+    } else {
+        const rcwa_stack1d& s = j.s1.stack;
+        add_bytes(k, s.nI);
+        add_bytes(k, s.nII);
+        add_bytes(k, s.period);
+        add_bytes(k, s.n_layers);
+        for (int l = 0; l < s.n_layers; ++l) {
+            const rcwa_layer1d& L = j.s1.layers[l];
+            add_bytes(k, L.d);
+            add_bytes(k, L.homogeneous);
+            add_bytes(k, L.n);
+            add_bytes(k, L.n_segments);
+            add_bytes(k, L.fourier_method);
+            add_bytes(k, L.fft_samples);
+            add_array(k, j.s1.edges[l].data(), j.s1.edges[l].size());
+            add_array(k, j.s1.values[l].data(), j.s1.values[l].size());
+        }
+    }
+    return k;
 }
 
 int order_of(const rcwa_request& r) {
@@ -351,11 +423,35 @@ struct rcwa_gpu_server {
     double budget = 0, in_use = 0;
     int running = 0;
     std::chrono::milliseconds max_bypass{2000};
+    int max_batch = 256;
     bool stop = false;
     unsigned long long next_ticket = 1;
     Clock::time_point t0 = Clock::now();
 
     double now_s() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+
+    // under the lock: the next request a free slot may start and the queued requests that can share its
+    // call (equal keys, while they fit the budget), or an empty batch
+    std::vector<Job*> pick_batch() {
+        std::vector<Job*> batch;
+        Job* lead = pick();
+        if (!lead) return batch;
+        batch.push_back(lead);
+        double room = budget - in_use - lead->footprint;
+        if (max_batch > 1) {
+            std::deque<Job*>& q = buckets[lead->bucket];
+            for (auto it = q.begin(); it != q.end() && (int)batch.size() < max_batch;) {
+                if ((*it)->key == lead->key && (*it)->footprint <= room) {
+                    room -= (*it)->footprint;
+                    batch.push_back(*it);
+                    it = q.erase(it);
+                } else {
+                    ++it;
+                }
+            }
+        }
+        return batch;
+    }
 
     // under the lock: the next request a free slot may start, or null
     Job* pick() {
@@ -395,26 +491,153 @@ struct rcwa_gpu_server {
         }
     }
 
+    // Several requests of one key in one call: the points side by side, the results copied back to each.
+    void run_batch(std::vector<Job*>& b, rcwa_gpu_ctx* ctx) {
+        const int P = (int)b.size();
+        const rcwa_request& r0 = b[0]->req;
+        rcwa_options o = r0.options;
+        int code = RCWA_OK;
+        if (r0.kind == RCWA_REQ_1D) {
+            const int n = 2 * r0.M + 1;
+            std::vector<rcwa_point1d> pts(P);
+            std::vector<rcwa_complex> R((size_t)P * n), T((size_t)P * n);
+            std::vector<double> DEr((size_t)P * n), DEt((size_t)P * n), resid(P);
+            std::vector<int> st(P), info(P), neig(P), nds(P), nlu(P);
+            for (int p = 0; p < P; ++p) pts[p] = rcwa_point1d{b[p]->req.wavelength, b[p]->req.theta_deg};
+            rcwa_result1d v{R.data(), T.data(), DEr.data(), DEt.data(), st.data(), info.data(), neig.data(), nds.data(),
+                            resid.data(), nlu.data()};
+            code = rcwa_gpu_solve1d_batch(ctx, &b[0]->s1.stack, pts.data(), P, r0.M, r0.polarization, &o, &v);
+            for (int p = 0; p < P; ++p) {
+                Res1D& h = b[p]->r1;
+                h.view(n);
+                std::copy_n(R.begin() + (size_t)p * n, n, h.R.begin());
+                std::copy_n(T.begin() + (size_t)p * n, n, h.T.begin());
+                std::copy_n(DEr.begin() + (size_t)p * n, n, h.DEr.begin());
+                std::copy_n(DEt.begin() + (size_t)p * n, n, h.DEt.begin());
+                h.status = st[p];
+                h.eig_info = info[p];
+                h.n_eig = neig[p];
+                h.n_dense = nds[p];
+                h.n_lu = nlu[p];
+                h.resid = resid[p];
+            }
+        } else if (r0.kind == RCWA_REQ_CONICAL) {
+            const int n = 2 * r0.M + 1;
+            std::vector<rcwa_point_conical> pts(P);
+            std::vector<rcwa_complex> Jr((size_t)P * n * 4), Jt((size_t)P * n * 4);
+            std::vector<double> DEr((size_t)P * n * 4), DEt((size_t)P * n * 4), kx((size_t)P * n), fr((size_t)P * n),
+                ft((size_t)P * n), ky(P), minl(P);
+            std::vector<int> st(P), info(P), neig(P), nds(P), nsch(P), warn(P), nlu(P);
+            for (int p = 0; p < P; ++p)
+                pts[p] = rcwa_point_conical{b[p]->req.wavelength, b[p]->req.theta_deg, b[p]->req.phi_deg};
+            rcwa_result_conical v{Jr.data(), Jt.data(), DEr.data(), DEt.data(), st.data(), info.data(), neig.data(),
+                                  nds.data(), nsch.data(), minl.data(), warn.data(), kx.data(), ky.data(), fr.data(),
+                                  ft.data(), nlu.data()};
+            code = rcwa_gpu_solve_conical_batch(ctx, &b[0]->s1.stack, pts.data(), P, r0.M, &o, &v);
+            for (int p = 0; p < P; ++p) {
+                ResConical& h = b[p]->rc;
+                h.view(n);
+                std::copy_n(Jr.begin() + (size_t)p * n * 4, n * 4, h.Jr.begin());
+                std::copy_n(Jt.begin() + (size_t)p * n * 4, n * 4, h.Jt.begin());
+                std::copy_n(DEr.begin() + (size_t)p * n * 4, n * 4, h.DEr.begin());
+                std::copy_n(DEt.begin() + (size_t)p * n * 4, n * 4, h.DEt.begin());
+                std::copy_n(kx.begin() + (size_t)p * n, n, h.kx.begin());
+                std::copy_n(fr.begin() + (size_t)p * n, n, h.flux_r.begin());
+                std::copy_n(ft.begin() + (size_t)p * n, n, h.flux_t.begin());
+                h.status = st[p];
+                h.eig_info = info[p];
+                h.n_eig = neig[p];
+                h.n_dense = nds[p];
+                h.n_schur = nsch[p];
+                h.warn = warn[p];
+                h.n_lu = nlu[p];
+                h.min_abs = minl[p];
+                h.ky = ky[p];
+            }
+        } else {
+            const int N = (2 * r0.M1 + 1) * (2 * r0.M2 + 1), L = b[0]->s2.stack.n_layers;
+            std::vector<rcwa_point2d> pts(P);
+            std::vector<double> Kx((size_t)P * N), Ky((size_t)P * N), DEr((size_t)P * N), DEt((size_t)P * N), resid(P);
+            std::vector<rcwa_complex> c[12];
+            for (auto& x : c) x.resize((size_t)P * N);
+            std::vector<unsigned char> pr((size_t)P * N), pt((size_t)P * N), reg((size_t)P * (L + 2));
+            std::vector<int> st(P), info(P), neig(P), nds(P);
+            for (int p = 0; p < P; ++p)
+                pts[p] = rcwa_point2d{b[p]->req.wavelength, b[p]->req.theta_deg, b[p]->req.phi_deg, b[p]->req.Es, b[p]->req.Ep};
+            rcwa_result2d v{};
+            v.Kx = Kx.data();
+            v.Ky = Ky.data();
+            rcwa_complex** z[12] = {&v.kzI, &v.kzII, &v.Ex_r, &v.Ey_r, &v.Ez_r, &v.Ex_t, &v.Ey_t, &v.Ez_t, &v.Rs, &v.Rp, &v.Ts, &v.Tp};
+            for (int q = 0; q < 12; ++q) *z[q] = c[q].data();
+            v.DEr = DEr.data();
+            v.DEt = DEt.data();
+            v.prop_r = pr.data();
+            v.prop_t = pt.data();
+            v.status = st.data();
+            v.eig_info = info.data();
+            v.n_eig = neig.data();
+            v.n_dense_solve = nds.data();
+            v.max_eig_residual = resid.data();
+            v.rayleigh_regions = reg.data();
+            code = rcwa_gpu_solve2d_batch(ctx, &b[0]->s2.stack, pts.data(), P, r0.M1, r0.M2, r0.factorization, &o, &v);
+            for (int p = 0; p < P; ++p) {
+                Res2D& h = b[p]->r2;
+                h.view(N, L);
+                std::copy_n(Kx.begin() + (size_t)p * N, N, h.Kx.begin());
+                std::copy_n(Ky.begin() + (size_t)p * N, N, h.Ky.begin());
+                std::copy_n(DEr.begin() + (size_t)p * N, N, h.DEr.begin());
+                std::copy_n(DEt.begin() + (size_t)p * N, N, h.DEt.begin());
+                for (int q = 0; q < 12; ++q) std::copy_n(c[q].begin() + (size_t)p * N, N, h.c[q].begin());
+                std::copy_n(pr.begin() + (size_t)p * N, N, h.prop_r.begin());
+                std::copy_n(pt.begin() + (size_t)p * N, N, h.prop_t.begin());
+                std::copy_n(reg.begin() + (size_t)p * (L + 2), L + 2, h.regions.begin());
+                h.status = st[p];
+                h.eig_info = info[p];
+                h.n_eig = neig[p];
+                h.n_dense = nds[p];
+                h.resid = resid[p];
+            }
+        }
+        for (Job* j : b) {
+            j->code = code;
+            j->batch = P;
+        }
+    }
+
     void worker(int slot) {
         cudaSetDevice(device);
         for (;;) {
-            Job* j = nullptr;
+            std::vector<Job*> b;
             {
                 std::unique_lock<std::mutex> lk(m);
-                cv_work.wait(lk, [&] { return stop || (j = pick()) != nullptr; });
-                if (!j) return;
-                in_use += j->footprint;
+                cv_work.wait(lk, [&] { return stop || !(b = pick_batch()).empty(); });
+                if (b.empty()) return;
+                const double t = now_s();
+                for (Job* j : b) {
+                    in_use += j->footprint;
+                    j->slot = slot;
+                    j->start_s = t;
+                }
                 ++running;
-                j->slot = slot;
-                j->start_s = now_s();
             }
-            run(*j, ctxs[slot]);
+            if (b.size() == 1) {
+                run(*b[0], ctxs[slot]);
+            } else {
+                try {
+                    run_batch(b, ctxs[slot]);
+                } catch (const std::bad_alloc&) {
+                    for (Job* j : b) j->code = RCWA_ENOMEM;
+                }
+            }
             {
                 std::lock_guard<std::mutex> lk(m);
-                in_use -= j->footprint;
+                const double t = now_s();
+                for (Job* j : b) {
+                    in_use -= j->footprint;
+                    j->finish_s = t;
+                    j->done = true;
+                }
                 --running;
-                j->finish_s = now_s();
-                j->done = true;
             }
             cv_done.notify_all();
             cv_work.notify_all();
@@ -437,6 +660,7 @@ int rcwa_gpu_server_create(const rcwa_server_config* config, rcwa_gpu_server** o
     }
     s->device = config ? config->device : 0;
     if (config && config->max_bypass_ms > 0) s->max_bypass = std::chrono::milliseconds(config->max_bypass_ms);
+    if (config && config->max_batch > 0) s->max_batch = config->max_batch;
     for (int k = 0; k < slots; ++k) {
         rcwa_gpu_config c{s->device, 0};
         rcwa_gpu_ctx* ctx = nullptr;
@@ -512,6 +736,11 @@ int rcwa_gpu_server_submit(rcwa_gpu_server* s, const rcwa_request* r, unsigned l
     j->order = order_of(j->req);
     j->bucket = bucket_of(j->order);
     j->footprint = footprint_of(*j);
+    try {
+        j->key = key_of(*j);
+    } catch (const std::bad_alloc&) {
+        return RCWA_ENOMEM;
+    }
     {
         std::lock_guard<std::mutex> lk(s->m);
         if (s->stop) return RCWA_ECANCELLED;
@@ -543,7 +772,7 @@ int rcwa_gpu_server_wait(rcwa_gpu_server* s, unsigned long long ticket, int time
         j = std::move(s->jobs[ticket]);
         s->jobs.erase(ticket);
     }
-    if (resp) *resp = rcwa_response{j->code, j->slot, j->submit_s, j->start_s, j->finish_s, j->footprint};
+    if (resp) *resp = rcwa_response{j->code, j->slot, j->submit_s, j->start_s, j->finish_s, j->footprint, j->batch};
     if (result) {
         if (j->req.kind == RCWA_REQ_1D) j->r1.out(static_cast<rcwa_result1d*>(result));
         else if (j->req.kind == RCWA_REQ_CONICAL) j->rc.out(static_cast<rcwa_result_conical*>(result));

@@ -559,11 +559,13 @@ def rayleigh_message(stack, r, M1, M2):
 
 class Server:
     """The serving request loop (rcwa_gpu_server_*): submit single solves of any kind, collect them
-    with wait(). Requests run concurrently on `slots` worker slots, admitted by device footprint."""
+    with wait(). Requests run concurrently on `slots` worker slots, admitted by device footprint; queued
+    requests of one structure (differing only in the point) share one batched call, up to `max_batch`
+    (0: 256, 1: never)."""
 
-    def __init__(self, device=0, slots=32, hbm_budget=0, max_bypass_ms=0):
+    def __init__(self, device=0, slots=32, hbm_budget=0, max_bypass_ms=0, max_batch=0):
         self.L = load_library()
-        cfg = abi.rcwa_server_config(device, slots, hbm_budget, max_bypass_ms)
+        cfg = abi.rcwa_server_config(device, slots, hbm_budget, max_bypass_ms, max_batch)
         h = C.c_void_p()
         rc = self.L.rcwa_gpu_server_create(C.byref(cfg), C.byref(h))
         if rc != 0:
@@ -635,5 +637,5 @@ class Server:
         del self.meta[ticket]
         r = {k: v[0] for k, v in arrays.items()}
         info = {"code": resp.code, "slot": resp.slot, "submit_s": resp.submit_s, "start_s": resp.start_s,
-                "finish_s": resp.finish_s, "footprint_bytes": resp.footprint_bytes, "kind": kind}
+                "finish_s": resp.finish_s, "footprint_bytes": resp.footprint_bytes, "batch": resp.batch, "kind": kind}
         return info, r

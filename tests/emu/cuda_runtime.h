@@ -38,6 +38,11 @@ inline double __longlong_as_double(long long v) {
     std::memcpy(&d, &v, 8);
     return d;
 }
+inline long long __double_as_longlong(double d) {
+    long long v;
+    std::memcpy(&v, &d, 8);
+    return v;
+}
 
 void emu_sync();
 double emu_shfl_xor(double v, int o);

@@ -131,6 +131,70 @@ void run(int n, const std::vector<zc>& a, const char* tag, bool real_form, bool 
     if (!ok) ++failures;
 }
 
+// The tridiagonalisation (herm_tridiag_one), then divide and conquer on (d, e) (herm_dc_one) for Y and the
+// eigenvalues, and X = Q Y on the host; residual and orthonormality as run().
+template <int G>
+void run_dc(int n, const std::vector<zc>& a, const char* tag) {
+    group_size = G;
+    std::barrier<> b(G);
+    bar = &b;
+    std::vector<zc> Q((size_t)n * n), W(n), ws(eig_workspace_elems(n));
+    std::vector<double> Y((size_t)n * n, -7.0);
+    int info = -7;
+    {
+        std::vector<std::thread> th;
+        for (int l = 0; l < G; ++l)
+            th.emplace_back([&, l] {
+                threadIdx.x = l;
+                herm_tridiag_one<G>(n, a.data(), Q.data(), ws.data(), nullptr, nullptr);
+            });
+        for (auto& t : th) t.join();
+    }
+    {
+        std::vector<std::thread> th;
+        for (int l = 0; l < G; ++l)
+            th.emplace_back([&, l] {
+                threadIdx.x = l;
+                herm_dc_one<G>(n, ws.data(), Y.data(), W.data(), &info, 2.220446049250313e-16, 30);
+            });
+        for (auto& t : th) t.join();
+    }
+    if (info != 0) {
+        std::printf("FAIL dc %s n=%d: info %d\n", tag, n, info);
+        ++failures;
+        return;
+    }
+    std::vector<zc> V((size_t)n * n);
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+            zc acc{0.0, 0.0};
+            for (int k = 0; k < n; ++k) acc = acc + Q[(size_t)k * n + i] * Y[(size_t)j * n + k];
+            V[(size_t)j * n + i] = acc;
+        }
+    double fro = 0.0;
+    for (const zc& z : a) fro += norm2(z);
+    fro = std::sqrt(fro);
+    double worst = 0.0, orth = 0.0;
+    for (int j = 0; j < n; ++j) {
+        double dn = 0.0, vn = 0.0;
+        for (int i = 0; i < n; ++i) {
+            zc acc{0.0, 0.0};
+            for (int k = 0; k < n; ++k) acc = acc + a[(size_t)k * n + i] * V[(size_t)j * n + k];
+            dn += norm2(acc - W[j] * V[(size_t)j * n + i]);
+            vn += norm2(V[(size_t)j * n + i]);
+        }
+        worst = std::fmax(worst, std::sqrt(dn) / (std::fmax(fro, 1e-300) * std::sqrt(vn)));
+        for (int k = 0; k < n; ++k) {
+            zc dot{0.0, 0.0};
+            for (int i = 0; i < n; ++i) dot = dot + conj(V[(size_t)j * n + i]) * V[(size_t)k * n + i];
+            orth = std::fmax(orth, zabs(dot - zc{j == k ? 1.0 : 0.0, 0.0}));
+        }
+    }
+    const bool ok = worst <= 1e-13 && orth <= 1e-13 * std::sqrt((double)std::max(n, 1));
+    std::printf("%s dc %s G=%d n=%d residual %.2e orth %.2e\n", ok ? "pass" : "FAIL", tag, G, n, worst, orth);
+    if (!ok) ++failures;
+}
+
 // The blocked reduction (herm_panel_one per panel, the trailing update and the back-transformation as
 // plain host products, standing in for the device's batched products), then the same QL and rotation
 // kernels as run(), and X = Q Y applied panel by panel from the stored reflectors and T V^H.
@@ -289,6 +353,43 @@ int main() {
         run<32>(n, t, "toeplitz", true, true);
         run<8>(n, t, "toeplitz", false, true);
         run<4>(n, d, "diagonal", true, true);
+    }
+    for (int n : {1, 2, 5, 9, 16, 17, 33, 61, 121, 162}) {  // divide and conquer, incl. repeated eigenvalues
+        std::vector<zc> r((size_t)n * n), t((size_t)n * n), d((size_t)n * n, zc{0.0, 0.0}), t0((size_t)n * n);
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i <= j; ++i) {
+                const zc v{nd(rng), i == j ? 0.0 : nd(rng)};
+                r[(size_t)j * n + i] = v;
+                r[(size_t)i * n + j] = conj(v);
+            }
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i) {
+                const int h = i - j;
+                const double kx = (i - n / 2) * 0.61, kx0 = (i - n / 2) * 0.61 + 0.3;
+                const zc c = h == 0 ? zc{2.2, 0.0} : zc{0.6 * std::sin(0.9 * h) / h, 0.6 * (1 - std::cos(0.9 * h)) / h};
+                const zc c0 = h == 0 ? zc{2.2, 0.0} : zc{0.6 * std::sin(0.9 * h) / h, 0.0};  // symmetric: degenerate at kx0
+                t[(size_t)j * n + i] = (i == j ? zc{kx0 * kx0, 0.0} : zc{0.0, 0.0}) - c;
+                t0[(size_t)j * n + i] = (i == j ? zc{kx * kx, 0.0} : zc{0.0, 0.0}) - c0;
+            }
+        for (int i = 0; i < n; ++i) d[(size_t)i * n + i] = zc{(double)(i % 3), 0.0};
+        // Wilkinson's W+ (pairs of eigenvalues equal to many digits) and glued copies of one small
+        // tridiagonal (clusters of nearly equal eigenvalues)
+        std::vector<zc> wk((size_t)n * n, zc{0.0, 0.0}), gl((size_t)n * n, zc{0.0, 0.0});
+        for (int i = 0; i < n; ++i) {
+            wk[(size_t)i * n + i] = zc{std::fabs(i - (n - 1) / 2.0), 0.0};
+            gl[(size_t)i * n + i] = zc{1.0 + 0.5 * std::sin((double)(i % 6)), 0.0};
+            if (i + 1 < n) {
+                wk[(size_t)(i + 1) * n + i] = wk[(size_t)i * n + i + 1] = zc{1.0, 0.0};
+                const double off = (i % 6 == 5) ? 1e-10 : 0.7;
+                gl[(size_t)(i + 1) * n + i] = gl[(size_t)i * n + i + 1] = zc{off, 0.0};
+            }
+        }
+        run_dc<16>(n, r, "random");
+        run_dc<8>(n, t, "toeplitz");
+        run_dc<32>(n, t0, "toeplitz-symmetric");
+        run_dc<4>(n, d, "diagonal");
+        run_dc<16>(n, wk, "wilkinson");
+        run_dc<16>(n, gl, "glued");
     }
     for (int n : {64, 65, 97, 121}) {  // the blocked form: full and partial last panels
         std::vector<zc> r((size_t)n * n), t((size_t)n * n);

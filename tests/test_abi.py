@@ -39,6 +39,8 @@ def test_struct_layouts_match_header():
     assert C.sizeof(abi.rcwa_options) == 24 + 8
     assert C.sizeof(abi.rcwa_result1d) == 10 * 8
     assert C.sizeof(abi.rcwa_result_conical) == 16 * 8
+    assert C.sizeof(abi.rcwa_server_config) == 4 + 4 + 8 + 4 + 4
+    assert C.sizeof(abi.rcwa_response) == 4 + 4 + 4 * 8 + 8
     assert C.sizeof(abi.rcwa_xprofile2d) == 8 + 8 + 8
     assert C.sizeof(abi.rcwa_layer2d) == 8 + 8 + 16 + 8 + 8 + 8
     assert C.sizeof(abi.rcwa_stack2d) == 8 + 16 + 8 + 8 + 8 + 8

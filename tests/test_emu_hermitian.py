@@ -4,7 +4,10 @@ through a thread-level emulation of the CUDA primitives they use (tests/emu/): t
 applied to a real identity or to the complex Q, on random Hermitian, Toeplitz-plus-Kx^2 and diagonal
 (repeated-eigenvalue) matrices of orders 1..61; the blocked reduction (herm_panel_one, panels of 32
 reflectors, the trailing update and the back-transformation X = Q Y from the stored reflectors and T V^H as
-host products) at orders 64, 65, 97 and 121 (partial and full last panels); and the general solver (eig_one, 4 and 32 lanes and a
+host products) at orders 64, 65, 97 and 121 (partial and full last panels); the divide-and-conquer
+tridiagonal eigensolver (herm_dc_one) at orders 1..162 on random, Toeplitz-plus-Kx^2, diagonal (massive
+deflation), Wilkinson W+ (eigenvalue pairs equal to many digits) and glued (clusters) matrices; and the
+general solver (eig_one, 4 and 32 lanes and a
 64-thread CTA) on random complex matrices of orders 1..30. Eigenpair residuals <= 1e-13, orthonormal
 columns for the Hermitian solver. This checks the kernels' arithmetic and index logic without a GPU; the
 device runs are the -m gpu tests."""
@@ -27,4 +30,4 @@ def test_hermitian_kernels_in_emulation(tmp_path):
     assert build.returncode == 0, build.stderr[-2000:]
     run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     assert run.returncode == 0 and run.stdout.strip().endswith("OK"), run.stdout[-3000:]
-    assert run.stdout.count("pass ") == 53
+    assert run.stdout.count("pass ") == 113

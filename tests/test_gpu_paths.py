@@ -1,7 +1,8 @@
 """The engine's own forms of the solve against the reference's sequence on the same inputs, through the C
 ABI: the Hermitian eigensolver of lossless grating layers against the general QR (RCWA_GB300_HERMITIAN=0),
 and the reduced seam algebra against the reference's interface blocks and stacking solves
-(RCWA_GB300_SEAMS=reference), each alone and both together. Seeded random stacks cover several gratings
+(RCWA_GB300_SEAMS=reference), each alone and both together, and the tridiagonal eigenvectors by divide and
+conquer (RCWA_GB300_HERM_DC=1) instead of the QL iteration. Seeded random stacks cover several gratings
 in a row (grating under grating), films between them, a grating directly on the substrate and directly
 under the incident medium, lossless and absorbing gratings; 1-D TE and TM, and conical incidence.
 Per-order efficiencies agree within 1e-10 and the amplitudes within 1e-9 (1 + |b|); status, n_eig and
@@ -21,7 +22,8 @@ pytestmark = pytest.mark.gpu
 PERIOD = 0.7
 VARIANTS = {"hermitian": {"RCWA_GB300_SEAMS": "reference"},
             "seams": {"RCWA_GB300_HERMITIAN": "0"},
-            "both": {}}
+            "both": {},
+            "divide-and-conquer": {"RCWA_GB300_HERM_DC": "1"}}
 BASE = {"RCWA_GB300_HERMITIAN": "0", "RCWA_GB300_SEAMS": "reference"}
 
 
@@ -35,7 +37,7 @@ def eng():
 
 @contextlib.contextmanager
 def env(values):
-    keys = ("RCWA_GB300_HERMITIAN", "RCWA_GB300_SEAMS")
+    keys = ("RCWA_GB300_HERMITIAN", "RCWA_GB300_SEAMS", "RCWA_GB300_HERM_DC")
     old = {k: os.environ.get(k) for k in keys}
     try:
         for k in keys:
@@ -93,7 +95,7 @@ def test_1d_forms_agree(eng, lossless):
                 assert np.array_equal(got["n_eig"], ref["n_eig"]), where
                 assert np.array_equal(got["n_dense_solve"], ref["n_dense_solve"]), where
                 assert np.all(got["n_lu"] <= ref["n_lu"]) and np.all(ref["n_lu"] <= ref["n_dense_solve"]), where
-                if name != "hermitian":  # every shape has a reduced seam (the top or a film over a grating)
+                if name not in ("hermitian",):  # every shape has a reduced seam (the top or a film over a grating)
                     assert np.all(got["n_lu"] < ref["n_lu"]), where
                 for key in ("DEr", "DEt"):
                     assert np.max(np.abs(got[key] - ref[key])) <= 1e-10, (where, key)

@@ -1,6 +1,8 @@
 """The serving loop (rcwa_gpu_server_*): a mix of 1-D, conical and 2-D requests submitted together
 gives, for every request, the result the same request gives alone through the direct entry points;
-a budget too small for two requests runs them one at a time; wait() honours its timeout."""
+requests that differ only in the point share one batched call and match their lone results within the
+parity tolerances; a budget too small for two requests runs them one at a time; wait() honours its
+timeout."""
 import numpy as np
 import pytest
 
@@ -58,7 +60,7 @@ def test_mix_equals_alone(eng, cases1d, conical_cases, cases2d):
     reqs = mix(cases1d, conical_cases, cases2d)
     assert len({k for k, _, _ in reqs}) == 3
     ref = [alone(eng, k, s, c) for k, s, c in reqs]
-    srv = Server(slots=8)
+    srv = Server(slots=8, max_batch=1)  # each request in its own call: results bit for bit
     try:
         tickets = [submit(srv, k, s, c) for k, s, c in reqs]
         out = [srv.wait(t) for t in tickets]
@@ -73,6 +75,57 @@ def test_mix_equals_alone(eng, cases1d, conical_cases, cases2d):
         assert info["submit_s"] <= info["start_s"] <= info["finish_s"]
         slots.add(info["slot"])
     assert len(slots) > 1  # the requests really ran on several slots
+
+
+def test_same_structure_requests_share_a_call(eng, cases1d, conical_cases, cases2d):
+    """Requests of one structure queued together (1-D, conical and 2-D, each at several points) run as one
+    batched call per structure (the response reports the batch size), and each result equals the request
+    solved alone within 1e-10 on the efficiencies and 1e-9 (1 + |b|) on the amplitudes, with the same
+    status; with max_batch = 1 every request runs alone."""
+    from stablercwa_gb300.engine import Server
+    c1, cc, cp = cases1d[0], conical_cases[0], _pillars(cases2d)
+    s1, sc, s2 = stack_from_json(c1["stack"]), stack_from_json(cc["stack"]), stack2d_from_json(cp["stack"])
+    jones = (complex(*cp["jones"][0]), complex(*cp["jones"][1]))
+    pol = 0 if c1["pol"] == "TE" else 1
+    reqs = [("1d", (c1["wavelength"] + 0.011 * k, c1["theta"] + 0.5 * k)) for k in range(10)]
+    reqs += [("conical", (cc["wavelength"] + 0.009 * k, cc["theta"] + 0.4 * k, cc["phi"] + 1.0 * k)) for k in range(6)]
+    reqs += [("2d", (cp["wavelength"] + 0.007 * k, cp["theta"], cp["phi"])) for k in range(4)]
+
+    def go(srv, kind, p):
+        if kind == "1d":
+            return srv.submit_1d(s1, p[0], p[1], c1["M"], pol)
+        if kind == "conical":
+            return srv.submit_conical(sc, p[0], p[1], p[2], cc["M"])
+        return srv.submit_2d(s2, p[0], p[1], p[2], cp["M1"], cp["M2"], jones)
+
+    for max_batch in (0, 1):
+        srv = Server(slots=1, max_batch=max_batch)
+        try:
+            # another structure (one order less) keeps the one slot busy while the rest queue
+            first = srv.submit_2d(s2, cp["wavelength"], cp["theta"], cp["phi"], cp["M1"] - 1, cp["M2"] - 1, jones)
+            tickets = [go(srv, kind, p) for kind, p in reqs]
+            srv.wait(first)
+            out = [srv.wait(t) for t in tickets]
+        finally:
+            srv.close()
+        batches = {kind: max(info["batch"] for (k2, _), (info, _) in zip(reqs, out) if k2 == kind) for kind in KEYS}
+        if max_batch == 1:
+            assert all(b == 1 for b in batches.values()), batches
+            continue
+        assert batches == {"1d": 10, "conical": 6, "2d": 4}, batches
+        for (kind, p), (info, r) in zip(reqs, out):
+            assert info["code"] == 0
+            if kind == "1d":
+                r0 = {k: v[0] for k, v in eng.solve1d_arrays(s1, [p], c1["M"], pol).items()}
+            elif kind == "conical":
+                r0 = eng.solve_conical(sc, p[0], p[1], p[2], cc["M"])
+            else:
+                r0 = eng.solve2d(s2, p[0], p[1], p[2], cp["M1"], cp["M2"], jones)
+            assert r["status"] == r0["status"], (kind, p)
+            for key in KEYS[kind]:
+                a, b = np.asarray(r[key]), np.asarray(r0[key])
+                tol = 1e-10 if key.startswith("DE") else 1e-9
+                assert np.max(np.abs(a - b) / (1.0 if key.startswith("DE") else 1.0 + np.abs(b))) <= tol, (kind, key)
 
 
 def test_small_budget_serialises(cases1d):
