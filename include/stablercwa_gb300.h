@@ -479,7 +479,12 @@ int rcwa_gpu_gemm_info(int* tensor_cores, int* slices, int* stuck);
  * footprint fits what remains of hbm_budget, else the oldest smaller one (backfilling, bounded so
  * the oldest is never passed over for longer than max_bypass_ms). Requests on different slots run
  * concurrently on the device. Each request is one solve: 1-D (rcwa::solve), conical
- * (rcwa::solve_conical) or 2-D (rcwa::solve2d). */
+ * (rcwa::solve_conical) or 2-D (rcwa::solve2d). A slot that takes a request also takes up to
+ * max_batch - 1 queued requests that differ from it only in the point (wavelength, angles, Jones
+ * vector) and solves them in one batched call; their results equal the lone ones within the parity
+ * tolerances (1e-10 on efficiencies), and rcwa_response.batch reports the call's size. Creating a
+ * server runs a few small solves on one context first, so that CUDA has loaded the engine's kernels
+ * before the slots start. */
 #define RCWA_REQ_1D 0
 #define RCWA_REQ_CONICAL 1
 #define RCWA_REQ_2D 2
