@@ -60,7 +60,7 @@ std::vector<int> candidates(int kind, int n, int batch) {
         if (g == 32 || n >= 4 * g) c.push_back(g);
     if (n >= 32)
         for (int g : {64, 128, 256}) c.push_back(g);
-    if (kind == 0 && eig_cluster_wanted(n, batch)) c.push_back(-1);
+    if (kind == 0 && eig_cluster_possible(n, batch)) c.push_back(-1);
     return c;
 }
 

@@ -641,12 +641,26 @@ void preload_eig_cluster_kernel() {
     cudaGetLastError();
 }
 
-bool eig_cluster_wanted(int n, int batch) {
+namespace {
+int cluster_mode() {
     static const int mode = [] {
         const char* e = std::getenv("RCWA_GB300_EIG_CLUSTER");
         return e ? std::atoi(e) : 1;
     }();
-    return mode != 0 && n >= 384 && batch <= 64 && cluster_size_for(n) > 0;
+    return mode;
+}
+}  // namespace
+
+// The built-in rule: orders >= 384, up to 64 matrices. Measured on GB300 (one second call, RCWA-type
+// matrices): a lone matrix of order 121 takes 63 ms on a 16-CTA cluster against 97 on one CTA, 2 of order
+// 162 111 against 201, 4 of order 242 266 against 481, 8 of order 301 791 against 905, but 8 of order 162
+// 221 against 203 and 8 of order 121 125 against 97 (eight 16-CTA clusters fill the GPU and share it).
+// Below 384 the rule leaves the choice to the autotuner, which times the cluster form whenever it applies.
+bool eig_cluster_wanted(int n, int batch) { return cluster_mode() != 0 && n >= 384 && batch <= 64 && cluster_size_for(n) > 0; }
+
+// the cluster form can run this key (the autotuner's candidates)
+bool eig_cluster_possible(int n, int batch) {
+    return cluster_mode() != 0 && n >= 96 && batch <= 64 && cluster_size_for(n) > 0;
 }
 
 void launch_eig_cluster(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info,

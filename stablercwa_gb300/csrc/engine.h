@@ -99,6 +99,7 @@ std::string autotune_table_text();
 // One matrix per thread-block cluster (eig_cluster.cu) for a few large matrices: the same algorithm as
 // launch_eig's kernels, spread over 8 or 16 SMs. launch_eig takes it by itself (eig_cluster_wanted).
 bool eig_cluster_wanted(int n, int batch);
+bool eig_cluster_possible(int n, int batch);
 void preload_eig_cluster_kernel();
 void launch_eig_cluster(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info,
                         int* sweeps, zc* ws, double eps, int max_iter, const int* skip, int skip_value, zc* t_out);

@@ -24,11 +24,11 @@ def layer_matrices(n, batch, seed):
     return out
 
 
-@pytest.mark.parametrize("hermitian", [False, True])
-def test_tuned_form_is_used(monkeypatch, hermitian):
+@pytest.mark.parametrize("hermitian,n,batch", [(False, 45, 300), (True, 45, 300), (False, 121, 2)])
+def test_tuned_form_is_used(monkeypatch, hermitian, n, batch):
+    """(121, 2): a key where the thread-block cluster form is among the timed candidates."""
     import torch
     from stablercwa_gb300.engine import Engine, autotune_table
-    n, batch = 45, 300
     a = layer_matrices(n, batch, 3)
     if hermitian:
         a = 0.5 * (a + a.conj().transpose(0, 2, 1))
@@ -37,7 +37,8 @@ def test_tuned_form_is_used(monkeypatch, hermitian):
     try:
         form, ms = eng.autotune_eig(n, batch, d_a.data_ptr(), hermitian=hermitian)
         assert form in FORMS and ms > 0
-        line = f"{'hermitian' if hermitian else 'general'} {n} 256 {form}"
+        bucket = 1 << (batch.bit_length() - 1)
+        line = f"{'hermitian' if hermitian else 'general'} {n} {bucket} {form}"
         assert line in autotune_table()
         solve = eng.eig_hermitian_batch if hermitian else eng.eig_batch
         monkeypatch.delenv("RCWA_GB300_EIG_GROUP", raising=False)
