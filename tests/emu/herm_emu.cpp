@@ -384,6 +384,9 @@ int main() {
                 gl[(size_t)(i + 1) * n + i] = gl[(size_t)i * n + i + 1] = zc{off, 0.0};
             }
         }
+        run<32>(n, t0, "toeplitz-symmetric", true, true);  // the QL kernel on the clustered spectra too
+        run<16>(n, wk, "wilkinson", true, true);
+        run<16>(n, gl, "glued", true, false);
         run_dc<16>(n, r, "random");
         run_dc<8>(n, t, "toeplitz");
         run_dc<32>(n, t0, "toeplitz-symmetric");
