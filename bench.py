@@ -67,8 +67,8 @@ HERM_STAGE_DRAM_BYTES_PER_MATRIX_N121 = 33.0e6
 
 
 HERM_STAGE_KERNELS = ("eigensolve stage: herm_panel_batch_kernel (blocked tridiagonalisation, FP64) + tensor-core "
-                      "trailing updates + herm_ql_kernel + herm_apply_real_kernel (QL and its rotations on a real "
-                      "identity, FP64) + tensor-core back-transformation")
+                      "trailing updates + herm_ql_kernel + herm_apply_real_kernel (QL, FP64; its rotations on a real "
+                      "identity in 64-bit fixed point on the integer pipes) + tensor-core back-transformation")
 
 
 def herm_flops_text(n, rotations_per_matrix):
@@ -81,7 +81,8 @@ def herm_flops_text(n, rotations_per_matrix):
 def herm_eig_flops(n, rotations_per_matrix):
     """Algorithmic real flops of one Hermitian eigensolve with eigenvectors: the Householder tridiagonalisation
     (16/3 n^3, LAPACK's zhetrd count), the tridiagonal eigenvectors (divide and conquer: about 8/3 n^3 for the
-    merge products without deflation; or, when the QL iteration runs, 6 n per measured rotation), and the
+    merge products without deflation; or, when the QL iteration runs, 6 n per measured rotation, which the
+    engine applies in fixed point on the integer pipes and counts at its FP64 equivalent), and the
     back-transformation of the real eigenvectors by Q (4 n^3)."""
     vec = 6 * n * rotations_per_matrix if rotations_per_matrix > 0 else (8 / 3) * n ** 3
     return (16 / 3) * n ** 3 + vec + 4 * n ** 3

@@ -88,8 +88,9 @@ long long take_rotation_count() {
 
 // Hermitian matrices: the tridiagonalisation with G lanes per matrix, the QL iteration one lane per matrix,
 // the rotations applied row-parallel, and the fused kernel for any matrix whose rotation log overflowed.
-// While a row of the real rotation product fits in shared memory (n <= 887) the rotations go to a real
-// identity Y and the eigenvectors are Q Y; otherwise they are applied to the complex Q in place.
+// While 32 rows of the real rotation product fit in shared memory (n <= 904) the rotations go to a real
+// identity Y, in fixed point on the integer pipes, and the eigenvectors are Q Y; otherwise they are applied
+// to the complex Q in place in FP64.
 namespace {
 template <int G>
 void herm_reduce_launch(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* q, zc* ws) {
@@ -227,7 +228,7 @@ void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a
     if (group <= 0) group = eig_default_group(n, batch);
     TimedLaunch timed(TK_EIG, st);
     const size_t ysm = (size_t)n * kHermRows * sizeof(double);
-    const bool real_form = ysm <= 227 * 1024;
+    const bool real_form = ysm + kHermApplyStaticSmem <= 227 * 1024;
     zc* q = v;
     double* y = nullptr;
     const bool blocked = real_form && herm_blocked_wanted(n, group);
@@ -258,15 +259,20 @@ void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a
         if (qsm > 48 * 1024) {
             static int opted = 0;  // the largest opt-in requested so far
             if ((int)qsm > opted) {
-                RCWA_CUDA(cudaFuncSetAttribute(herm_ql_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm));
+                RCWA_CUDA(cudaFuncSetAttribute(herm_ql_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)qsm));
                 opted = (int)qsm;
             }
         }
-        herm_ql_kernel<true><<<(unsigned)((batch + kHermQlThreads - 1) / kHermQlThreads), kHermQlThreads, qsm, st>>>(
+        // the real form's log is fixed point (herm_apply_real_kernel); the shared-memory form implies it
+        herm_ql_kernel<true, true><<<(unsigned)((batch + kHermQlThreads - 1) / kHermQlThreads), kHermQlThreads, qsm, st>>>(
             n, batch, w, info, ws, eps, max_iter, rotation_counter());
+    } else if (real_form) {
+        herm_ql_kernel<false, true><<<(unsigned)((batch + 127) / 128), 128, 0, st>>>(n, batch, w, info, ws, eps,
+                                                                                     max_iter, rotation_counter());
     } else {
-        herm_ql_kernel<false><<<(unsigned)((batch + 127) / 128), 128, 0, st>>>(n, batch, w, info, ws, eps, max_iter,
-                                                                               rotation_counter());
+        herm_ql_kernel<false, false><<<(unsigned)((batch + 127) / 128), 128, 0, st>>>(n, batch, w, info, ws, eps,
+                                                                                      max_iter, rotation_counter());
     }
     RCWA_CUDA(cudaGetLastError());
     int* only = nullptr;  // matrices whose log overflowed: the fused kernel, masked to them

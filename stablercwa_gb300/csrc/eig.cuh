@@ -1030,11 +1030,29 @@ __global__ void __launch_bounds__(128) herm_panel_batch_kernel(int n, int batch,
                       vall + gid * (long long)n * n, mall + gid * (long long)pnb * n, pnb);
 }
 
+// round(x 2^63) for |x| <= 1, saturated to +-(2^63 - 1), with integer operations only: the QL kernel runs
+// one thread per matrix and is bound by its warp's FP64 instructions, so converting each rotation's
+// (c, s) to fixed point there must not add any.
+__device__ inline long long herm_q63(double x) {
+    const long long b = __double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff);                          // x = +-m 2^(e - 1075)
+    const long long m = (b & 0xfffffffffffffLL) | 0x10000000000000LL;  // 2^52 <= m < 2^53
+    const int sh = 1012 - e;                                          // x 2^63 = m 2^-sh
+    long long v;
+    if (e >= 1023) v = 0x7fffffffffffffffLL;  // |x| >= 1 (c or s one ulp above 1 included)
+    else if (sh <= 0) v = m << -sh;           // 2^-11 <= |x| < 1: exact
+    else if (sh < 64) v = (m + (1LL << (sh - 1))) >> sh;
+    else v = 0;
+    return b < 0 ? -v : v;
+}
+
 // (2) implicit symmetric QL with Wilkinson's shift on (d, e), one thread per matrix; rotations logged. The
 // rotation chain is the whole cost, so with SMEM the thread's d and e live in shared memory (kHermQlThreads
 // threads per CTA, 16 n bytes each) rather than in the workspace, whose loads would sit on the chain.
+// FIXED logs each rotation as (round(-c 2^63), round(s 2^63)), the fixed-point form herm_apply_real_kernel
+// applies on the integer pipes; else as the doubles (c, s) herm_apply_kernel applies to the complex Q.
 constexpr int kHermQlThreads = 32;
-template <bool SMEM>
+template <bool SMEM, bool FIXED>
 __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, zc* __restrict__ w, int* __restrict__ info,
                                                       zc* __restrict__ ws, double eps, int max_iter,
                                                       unsigned long long* rotations) {
@@ -1129,8 +1147,14 @@ __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, zc* __re
                 p = s * r;
                 d[(i + 1) * sd] = gg + p;
                 gg = c * r - b;
-                log[2 * pos] = c;
-                log[2 * pos + 1] = s;
+                if constexpr (FIXED) {
+                    long long* q63 = reinterpret_cast<long long*>(log);
+                    q63[2 * pos] = herm_q63(-c);
+                    q63[2 * pos + 1] = herm_q63(s);
+                } else {
+                    log[2 * pos] = c;
+                    log[2 * pos + 1] = s;
+                }
                 ++pos;
             }
             const int first = split ? i + 1 : l;
@@ -1589,42 +1613,79 @@ static __global__ void __launch_bounds__(128) herm_apply_kernel(int n, int batch
 }
 
 // (3, real form) the logged rotations applied to a real identity instead of to the complex Q: Y = R_1 R_2 ...
-// is real orthogonal and the eigenvectors are Q Y, a complex-by-real product (zdgemm_kernel). One thread
-// per (matrix, row), kHermRows rows per CTA, each row kept in shared memory (row t of the CTA at element
-// i * kHermRows + t) until every sweep has passed: half the FP64 work of rotating Q, and Y meets HBM only
-// once. A matrix that overflowed its log or did not converge gets Y = I.
+// is real orthogonal and the eigenvectors are Q Y, a complex-by-real product. One thread per (matrix, row),
+// kHermRows rows per CTA, each row kept in shared memory (row t of the CTA at element i * kHermRows + t)
+// until every sweep has passed, so Y meets HBM only once. A matrix that overflowed its log or did not
+// converge gets Y = I.
+//
+// The arithmetic is 64-bit fixed point on the integer pipes, not FP64: this GPU issues FP64 at 2 lanes a
+// cycle per SM and 32-bit integer multiply-adds at 64, and every quantity here lies in [-1, 1] (the rotation
+// coefficients, and the entries of an orthogonal Y). Y is held as round(y 2^62) (Q1.62) and the log as
+// C' = round(-c 2^63), S = round(s 2^63) (Q0.63), so a product's high 64 bits, hi(S Y) = floor(s y 2^61),
+// doubled is back in Q1.62:
+//   y_{i+1} <- 2 (hi(S y_i) - hi(C' y_{i+1})),   y_i <- 2 (-hi(C' y_i) - hi(S y_{i+1})),
+// each output the difference of a floor and a negated floor, so the truncations (-1/2 unit on average
+// each) cancel instead of drifting over the ~2 n rotations an entry takes. Resolution 2^-61 absolute per
+// product against FP64's 2^-53 relative: as accurate for entries near 1/sqrt(n), more so near 1. The entries
+// leave as doubles.
+//
+// A rotation then costs tens of cycles, less than a load of its log entry from L2 or HBM, so the log is
+// streamed through shared memory: the CTA's one warp holds 32 entries in stage[b], has the next 32 in flight
+// in registers (one entry a lane, loaded 32 rotations before use) and swaps at each chunk boundary. The
+// reads run to the log's capacity at most, inside the workspace; entries past the last rotation are never
+// used.
 constexpr int kHermRows = 32;
+constexpr int kHermApplyStaticSmem = 2 * kHermRows * (int)sizeof(longlong2);  // stage
 static __global__ void __launch_bounds__(kHermRows) herm_apply_real_kernel(int n, int batch, double* __restrict__ y_out,
                                                                            const zc* __restrict__ ws,
                                                                            const int* __restrict__ info) {
-    RCWA_DYN_SMEM(double, ysm);
+    RCWA_DYN_SMEM(long long, yfix_sm);
     const long long gid = blockIdx.x;
     const int t = threadIdx.x;
-    const int r = blockIdx.y * kHermRows + t;
-    if (gid >= batch || r >= n) return;
-    double* y = ysm + t;
-    for (int i = 0; i < n; ++i) y[i * kHermRows] = i == r ? 1.0 : 0.0;
+    const int r = blockIdx.y * kHermRows + t;  // lanes past the last row stage log entries and rotate zeros
+    if (gid >= batch) return;
+    long long* y = yfix_sm + t;
+    const long long one = 1LL << 62;
+    for (int i = 0; i < n; ++i) y[i * kHermRows] = i == r ? one : 0;
     const zc* base = ws + gid * eig_workspace_elems(n);
     const int* tail = reinterpret_cast<const int*>(base + 3LL * n * n);
-    if (!tail[1] && !info[gid]) {
+    __shared__ longlong2 stage[2][kHermRows];
+    const bool applied = !tail[1] && !info[gid];
+    if (applied) {
         const int2* table = reinterpret_cast<const int2*>(reinterpret_cast<const double*>(base) + 2 * n);
-        const double* log = reinterpret_cast<const double*>(base + (long long)n * n);
+        const longlong2* log = reinterpret_cast<const longlong2*>(base + (long long)n * n);  // (C', S)
+        const long long cap = herm_log_capacity(n);
         const int sweeps = tail[0];
+        // entries [cb, cb + 32) in stage[b], [cb + 32, cb + 64) in next
+        long long cb = 0;
+        int b = 0;
+        stage[0][t] = t < cap ? log[t] : longlong2{0, 0};
+        longlong2 next = kHermRows + t < cap ? log[kHermRows + t] : longlong2{0, 0};
+        __syncwarp();
         long long pos = 0;
         for (int k = 0; k < sweeps; ++k) {
             const int2 fl = table[k];
-            double cur = y[(fl.y + 1) * kHermRows];
+            long long cur = y[(fl.y + 1) * kHermRows];
             for (int i = fl.y; i >= fl.x; --i, ++pos) {
-                const double c = log[2 * pos], s = log[2 * pos + 1];
-                const double yi = y[i * kHermRows];
-                y[(i + 1) * kHermRows] = s * yi + c * cur;
-                cur = c * yi - s * cur;
+                if (pos == cb + kHermRows) {  // the next chunk: stage it, start loading the one after
+                    stage[b ^ 1][t] = next;
+                    b ^= 1;
+                    cb += kHermRows;
+                    const long long q = cb + kHermRows + t;
+                    next = q < cap ? log[q] : longlong2{0, 0};
+                    __syncwarp();
+                }
+                const longlong2 cs = stage[b][pos - cb];
+                const long long yi = y[i * kHermRows];
+                y[(i + 1) * kHermRows] = 2 * (__mul64hi(cs.y, yi) - __mul64hi(cs.x, cur));
+                cur = 2 * (-__mul64hi(cs.x, yi) - __mul64hi(cs.y, cur));
             }
             y[fl.x * kHermRows] = cur;
         }
     }
+    if (r >= n) return;
     double* yo = y_out + gid * (long long)n * n + r;
-    for (int i = 0; i < n; ++i) yo[(long long)i * n] = y[i * kHermRows];
+    for (int i = 0; i < n; ++i) yo[(long long)i * n] = (double)y[i * kHermRows] * 0x1p-62;
 }
 
 // 1 where the matrix overflowed its log (the fused kernel redoes it)

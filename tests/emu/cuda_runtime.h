@@ -31,6 +31,10 @@ struct int2 {
 struct double2 {
     double x, y;
 };
+struct longlong2 {
+    long long x, y;
+};
+inline long long __mul64hi(long long a, long long b) { return (long long)(((__int128)a * b) >> 64); }
 inline double2 make_double2(double a, double b) { return {a, b}; }
 inline int2 make_int2(int a, int b) { return {a, b}; }
 inline double __longlong_as_double(long long v) {

@@ -1,9 +1,9 @@
 // Runs the Hermitian eigensolver's kernels (stablercwa_gb300/csrc/eig.cuh: herm_tridiag_one, herm_ql_kernel,
 // herm_apply_real_kernel, herm_apply_kernel) and the general solver's eig_one on the CPU through
 // tests/emu/cuda_runtime.h and checks the eigenpairs: residual ||A v - lambda v|| / (||A||_F ||v||) <= 1e-13,
-// and orthonormal columns for the Hermitian solver. The group of G lanes is G std::threads; the QL and
-// rotation kernels run one emulated thread at a time. Exit status 0 and a final "OK" line when every case
-// passes. Test infrastructure only.
+// and orthonormal columns for the Hermitian solver. The group of G lanes is G std::threads, and so is each
+// 32-row CTA of herm_apply_real_kernel; the QL and complex rotation kernels run one emulated thread at a
+// time. Exit status 0 and a final "OK" line when every case passes. Test infrastructure only.
 #include <barrier>
 #include <cmath>
 #include <cstdio>
@@ -53,6 +53,26 @@ using namespace rcwa_gb300;
 
 static int failures = 0;
 
+// herm_apply_real_kernel for one matrix: each CTA (32 rows) as 32 threads meeting at one barrier, since the
+// warp stages the rotation log through shared memory
+static void apply_real(int n, double* Y, const zc* ws, const int* info) {
+    for (int by = 0; by * kHermRows < n; ++by) {
+        blockIdx.x = 0;
+        blockIdx.y = by;
+        group_size = kHermRows;
+        std::barrier<> b(kHermRows);
+        bar = &b;
+        std::vector<std::thread> th;
+        for (int l = 0; l < kHermRows; ++l)
+            th.emplace_back([&, l] {
+                threadIdx.x = l;
+                herm_apply_real_kernel(n, 1, Y, ws, info);
+            });
+        for (auto& x : th) x.join();
+    }
+    blockIdx.y = 0;
+}
+
 template <int G>
 void run(int n, const std::vector<zc>& a, const char* tag, bool real_form, bool smem_ql) {
     group_size = G;
@@ -72,10 +92,15 @@ void run(int n, const std::vector<zc>& a, const char* tag, bool real_form, bool 
     blockIdx.x = 0;
     blockIdx.y = 0;
     blockDim.x = smem_ql ? kHermQlThreads : 128;
-    if (smem_ql)
-        herm_ql_kernel<true>(n, 1, W.data(), &info, ws.data(), 2.220446049250313e-16, 30, &rot);
+    // the real form's log is fixed point, the complex form's doubles
+    if (smem_ql && real_form)
+        herm_ql_kernel<true, true>(n, 1, W.data(), &info, ws.data(), 2.220446049250313e-16, 30, &rot);
+    else if (smem_ql)
+        herm_ql_kernel<true, false>(n, 1, W.data(), &info, ws.data(), 2.220446049250313e-16, 30, &rot);
+    else if (real_form)
+        herm_ql_kernel<false, true>(n, 1, W.data(), &info, ws.data(), 2.220446049250313e-16, 30, &rot);
     else
-        herm_ql_kernel<false>(n, 1, W.data(), &info, ws.data(), 2.220446049250313e-16, 30, &rot);
+        herm_ql_kernel<false, false>(n, 1, W.data(), &info, ws.data(), 2.220446049250313e-16, 30, &rot);
     const int* tail = reinterpret_cast<const int*>(ws.data() + 3LL * n * n);
     if (info != 0 || tail[1] != 0) {
         std::printf("FAIL %s n=%d: info %d overflow %d\n", tag, n, info, tail[1]);
@@ -84,12 +109,7 @@ void run(int n, const std::vector<zc>& a, const char* tag, bool real_form, bool 
     }
     if (real_form) {
         std::vector<double> Y((size_t)n * n);
-        for (int r = 0; r < n; ++r) {
-            blockIdx.x = 0;
-            blockIdx.y = r / kHermRows;
-            threadIdx.x = r % kHermRows;
-            herm_apply_real_kernel(n, 1, Y.data(), ws.data(), &info);
-        }
+        apply_real(n, Y.data(), ws.data(), &info);
         std::vector<zc> Q = V;  // Z = Q Y, the product zdgemm_kernel forms on the device
         for (int j = 0; j < n; ++j)
             for (int i = 0; i < n; ++i) {
@@ -233,7 +253,7 @@ void run_blocked(int n, const std::vector<zc>& a, const char* tag) {
     blockIdx.x = 0;
     blockIdx.y = 0;
     blockDim.x = kHermQlThreads;
-    herm_ql_kernel<true>(n, 1, W.data(), &info, ws.data(), 2.220446049250313e-16, 30, &rot);
+    herm_ql_kernel<true, true>(n, 1, W.data(), &info, ws.data(), 2.220446049250313e-16, 30, &rot);
     const int* tail = reinterpret_cast<const int*>(ws.data() + 3LL * n * n);
     if (info != 0 || tail[1] != 0) {
         std::printf("FAIL blocked %s n=%d: info %d overflow %d\n", tag, n, info, tail[1]);
@@ -241,13 +261,7 @@ void run_blocked(int n, const std::vector<zc>& a, const char* tag) {
         return;
     }
     std::vector<double> Y((size_t)n * n);
-    for (int r = 0; r < n; ++r) {
-        blockIdx.x = 0;
-        blockIdx.y = r / kHermRows;
-        threadIdx.x = r % kHermRows;
-        herm_apply_real_kernel(n, 1, Y.data(), ws.data(), &info);
-    }
-    blockIdx.y = 0;
+    apply_real(n, Y.data(), ws.data(), &info);
     for (size_t i = 0; i < Y.size(); ++i) V[i] = zc{Y[i], 0.0};
     for (int p = P - 1; p >= 0; --p) {  // X(r0:, :) -= V_p (M_p X(r0:, :))
         const int k0 = p * nb, nbp = std::min(nb, n - 1 - k0), r0 = k0 + 1;
