@@ -1030,27 +1030,33 @@ __global__ void __launch_bounds__(128) herm_panel_batch_kernel(int n, int batch,
                       vall + gid * (long long)n * n, mall + gid * (long long)pnb * n, pnb);
 }
 
-// round(x 2^63) for |x| <= 1, saturated to +-(2^63 - 1), with integer operations only: the QL kernel runs
+// round(x 2^62) for |x| <= 1, saturated to +-(2^62 - 1), with integer operations only: the QL kernel runs
 // one thread per matrix and is bound by its warp's FP64 instructions, so converting each rotation's
 // (c, s) to fixed point there must not add any.
-__device__ inline long long herm_q63(double x) {
+__device__ inline long long herm_q62(double x) {
     const long long b = __double_as_longlong(x);
     const int e = (int)((b >> 52) & 0x7ff);                          // x = +-m 2^(e - 1075)
     const long long m = (b & 0xfffffffffffffLL) | 0x10000000000000LL;  // 2^52 <= m < 2^53
-    const int sh = 1012 - e;                                          // x 2^63 = m 2^-sh
+    const int sh = 1013 - e;                                          // x 2^62 = m 2^-sh
     long long v;
-    if (e >= 1023) v = 0x7fffffffffffffffLL;  // |x| >= 1 (c or s one ulp above 1 included)
-    else if (sh <= 0) v = m << -sh;           // 2^-11 <= |x| < 1: exact
+    if (e >= 1023) v = 0x3fffffffffffffffLL;  // |x| >= 1 (c or s one ulp above 1 included)
+    else if (sh <= 0) v = m << -sh;           // 2^-10 <= |x| < 1: exact
     else if (sh < 64) v = (m + (1LL << (sh - 1))) >> sh;
     else v = 0;
     return b < 0 ? -v : v;
+}
+// The fixed-point log entry of a rotation: S = herm_q62(s) and M = herm_q62(-c) as 31-bit limbs,
+// (S >> 31, S & (2^31 - 1), M >> 31, M & (2^31 - 1)); the high limbs are signed, the low ones in [0, 2^31).
+__device__ inline int4 herm_fixed_entry(double c, double s) {
+    const long long sq = herm_q62(s), mq = herm_q62(-c);
+    return make_int4((int)(sq >> 31), (int)(sq & 0x7fffffff), (int)(mq >> 31), (int)(mq & 0x7fffffff));
 }
 
 // (2) implicit symmetric QL with Wilkinson's shift on (d, e), one thread per matrix; rotations logged. The
 // rotation chain is the whole cost, so with SMEM the thread's d and e live in shared memory (kHermQlThreads
 // threads per CTA, 16 n bytes each) rather than in the workspace, whose loads would sit on the chain.
-// FIXED logs each rotation as (round(-c 2^63), round(s 2^63)), the fixed-point form herm_apply_real_kernel
-// applies on the integer pipes; else as the doubles (c, s) herm_apply_kernel applies to the complex Q.
+// FIXED logs each rotation as herm_fixed_entry(c, s), the fixed-point form herm_apply_real_kernel applies
+// on the integer pipes; else as the doubles (c, s) herm_apply_kernel applies to the complex Q.
 constexpr int kHermQlThreads = 32;
 template <bool SMEM, bool FIXED>
 __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, zc* __restrict__ w, int* __restrict__ info,
@@ -1148,9 +1154,7 @@ __global__ void __launch_bounds__(128) herm_ql_kernel(int n, int batch, zc* __re
                 d[(i + 1) * sd] = gg + p;
                 gg = c * r - b;
                 if constexpr (FIXED) {
-                    long long* q63 = reinterpret_cast<long long*>(log);
-                    q63[2 * pos] = herm_q63(-c);
-                    q63[2 * pos + 1] = herm_q63(s);
+                    reinterpret_cast<int4*>(log)[pos] = herm_fixed_entry(c, s);
                 } else {
                     log[2 * pos] = c;
                     log[2 * pos + 1] = s;
@@ -1620,14 +1624,19 @@ static __global__ void __launch_bounds__(128) herm_apply_kernel(int n, int batch
 //
 // The arithmetic is 64-bit fixed point on the integer pipes, not FP64: this GPU issues FP64 at 2 lanes a
 // cycle per SM and 32-bit integer multiply-adds at 64, and every quantity here lies in [-1, 1] (the rotation
-// coefficients, and the entries of an orthogonal Y). Y is held as round(y 2^62) (Q1.62) and the log as
-// C' = round(-c 2^63), S = round(s 2^63) (Q0.63), so a product's high 64 bits, hi(S Y) = floor(s y 2^61),
-// doubled is back in Q1.62:
-//   y_{i+1} <- 2 (hi(S y_i) - hi(C' y_{i+1})),   y_i <- 2 (-hi(C' y_i) - hi(S y_{i+1})),
-// each output the difference of a floor and a negated floor, so the truncations (-1/2 unit on average
-// each) cancel instead of drifting over the ~2 n rotations an entry takes. Resolution 2^-61 absolute per
-// product against FP64's 2^-53 relative: as accurate for entries near 1/sqrt(n), more so near 1. The entries
-// leave as doubles.
+// coefficients, and the entries of an orthogonal Y). Y is held as Y = round(y 2^60) and the coefficients as
+// S = round(s 2^62), M = round(-c 2^62), all three split into 31-bit limbs (X = X1 2^31 + X0, X0 in
+// [0, 2^31)). A product of coefficient and entry in Y's scale, C Y 2^-62, is then
+//   R(C, Y) = C1 Y1 + (C1 Y0 + C0 Y1) 2^-31   (+ C0 Y0 2^-62, below one unit, dropped)
+// -- three 32 x 32 -> 64 multiply-adds -- and the rotation y_{i+1} <- s y_i + c y_{i+1}, y_i <- c y_i -
+// s y_{i+1} is
+//   y_{i+1} = R(S, y_i) - R(M, y_{i+1}),   y_i = -R(M, y_i) - R(S, y_{i+1}),
+// each the sum of four limb products (signs carried by the entry limbs), the four 2^-31 terms gathered in one
+// 64-bit accumulator and rounded to nearest once. Each output is the difference of two products that drop
+// the same kind of term, so those errors (under a unit each) cancel on average instead of drifting over the
+// ~2 n rotations an entry takes. Resolution 2^-60 absolute against FP64's 2^-53 relative: as accurate for
+// entries near 1/sqrt(n), more so near 1. No intermediate overflows: |Y| <= 2^60 and s^2 + c^2 = 1 keep the
+// accumulator below 2^63. The entries leave as doubles.
 //
 // A rotation then costs tens of cycles, less than a load of its log entry from L2 or HBM, so the log is
 // streamed through shared memory: the CTA's one warp holds 32 entries in stage[b], has the next 32 in flight
@@ -1635,7 +1644,7 @@ static __global__ void __launch_bounds__(128) herm_apply_kernel(int n, int batch
 // reads run to the log's capacity at most, inside the workspace; entries past the last rotation are never
 // used.
 constexpr int kHermRows = 32;
-constexpr int kHermApplyStaticSmem = 2 * kHermRows * (int)sizeof(longlong2);  // stage
+constexpr int kHermApplyStaticSmem = 2 * kHermRows * (int)sizeof(int4);  // stage
 static __global__ void __launch_bounds__(kHermRows) herm_apply_real_kernel(int n, int batch, double* __restrict__ y_out,
                                                                            const zc* __restrict__ ws,
                                                                            const int* __restrict__ info) {
@@ -1645,22 +1654,23 @@ static __global__ void __launch_bounds__(kHermRows) herm_apply_real_kernel(int n
     const int r = blockIdx.y * kHermRows + t;  // lanes past the last row stage log entries and rotate zeros
     if (gid >= batch) return;
     long long* y = yfix_sm + t;
-    const long long one = 1LL << 62;
+    const long long one = 1LL << 60;
     for (int i = 0; i < n; ++i) y[i * kHermRows] = i == r ? one : 0;
     const zc* base = ws + gid * eig_workspace_elems(n);
     const int* tail = reinterpret_cast<const int*>(base + 3LL * n * n);
-    __shared__ longlong2 stage[2][kHermRows];
+    __shared__ int4 stage[2][kHermRows];
     const bool applied = !tail[1] && !info[gid];
     if (applied) {
         const int2* table = reinterpret_cast<const int2*>(reinterpret_cast<const double*>(base) + 2 * n);
-        const longlong2* log = reinterpret_cast<const longlong2*>(base + (long long)n * n);  // (C', S)
+        const int4* log = reinterpret_cast<const int4*>(base + (long long)n * n);  // (S1, S0, M1, M0)
         const long long cap = herm_log_capacity(n);
         const int sweeps = tail[0];
+        const int4 zero4 = make_int4(0, 0, 0, 0);
         // entries [cb, cb + 32) in stage[b], [cb + 32, cb + 64) in next
         long long cb = 0;
         int b = 0;
-        stage[0][t] = t < cap ? log[t] : longlong2{0, 0};
-        longlong2 next = kHermRows + t < cap ? log[kHermRows + t] : longlong2{0, 0};
+        stage[0][t] = t < cap ? log[t] : zero4;
+        int4 next = kHermRows + t < cap ? log[kHermRows + t] : zero4;
         __syncwarp();
         long long pos = 0;
         for (int k = 0; k < sweeps; ++k) {
@@ -1672,20 +1682,28 @@ static __global__ void __launch_bounds__(kHermRows) herm_apply_real_kernel(int n
                     b ^= 1;
                     cb += kHermRows;
                     const long long q = cb + kHermRows + t;
-                    next = q < cap ? log[q] : longlong2{0, 0};
+                    next = q < cap ? log[q] : zero4;
                     __syncwarp();
                 }
-                const longlong2 cs = stage[b][pos - cb];
+                const int4 e = stage[b][pos - cb];
                 const long long yi = y[i * kHermRows];
-                y[(i + 1) * kHermRows] = 2 * (__mul64hi(cs.y, yi) - __mul64hi(cs.x, cur));
-                cur = 2 * (-__mul64hi(cs.x, yi) - __mul64hi(cs.y, cur));
+                const int a1 = (int)(yi >> 31), a0 = (int)(yi & 0x7fffffff);
+                const int b1 = (int)(cur >> 31), b0 = (int)(cur & 0x7fffffff);
+                // the y_i terms first: they do not wait for the previous rotation's output
+                long long u1 = (long long)e.x * a0 + (long long)e.y * a1 + (1LL << 30);
+                long long u2 = (long long)e.z * -a0 + (long long)e.w * -a1 + (1LL << 30);
+                const long long v1 = (long long)e.x * a1, v2 = (long long)e.z * -a1;
+                u1 += (long long)e.z * -b0 + (long long)e.w * -b1;
+                u2 += (long long)e.x * -b0 + (long long)e.y * -b1;
+                y[(i + 1) * kHermRows] = v1 + (long long)e.z * -b1 + (u1 >> 31);
+                cur = v2 + (long long)e.x * -b1 + (u2 >> 31);
             }
             y[fl.x * kHermRows] = cur;
         }
     }
     if (r >= n) return;
     double* yo = y_out + gid * (long long)n * n + r;
-    for (int i = 0; i < n; ++i) yo[(long long)i * n] = (double)y[i * kHermRows] * 0x1p-62;
+    for (int i = 0; i < n; ++i) yo[(long long)i * n] = (double)y[i * kHermRows] * 0x1p-60;
 }
 
 // 1 where the matrix overflowed its log (the fused kernel redoes it)

@@ -31,10 +31,10 @@ struct int2 {
 struct double2 {
     double x, y;
 };
-struct longlong2 {
-    long long x, y;
+struct int4 {
+    int x, y, z, w;
 };
-inline long long __mul64hi(long long a, long long b) { return (long long)(((__int128)a * b) >> 64); }
+inline int4 make_int4(int a, int b, int c, int d) { return {a, b, c, d}; }
 inline double2 make_double2(double a, double b) { return {a, b}; }
 inline int2 make_int2(int a, int b) { return {a, b}; }
 inline double __longlong_as_double(long long v) {
