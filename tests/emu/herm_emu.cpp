@@ -151,6 +151,75 @@ void run(int n, const std::vector<zc>& a, const char* tag, bool real_form, bool 
     if (!ok) ++failures;
 }
 
+// herm_apply_real_kernel alone on synthetic sweeps of ~1.05 n^2 random rotations (c = +-1 and s = +-1
+// among them), logged with herm_fixed_entry as the QL kernel logs them, against the same rotations applied
+// in long double: max |Y - exact| <= 2e-16 and orthogonality <= 4e-16 n^(1/2) (the entries leave rounded to
+// doubles).
+void run_rotations(int n, unsigned seed) {
+    std::mt19937_64 rng(seed);
+    std::uniform_real_distribution<double> ang(-3.14159, 3.14159);
+    std::vector<zc> ws(eig_workspace_elems(n));
+    zc* base = ws.data();
+    int2* table = reinterpret_cast<int2*>(reinterpret_cast<double*>(base) + 2 * n);
+    int4* log = reinterpret_cast<int4*>(base + (long long)n * n);
+    int* tail = reinterpret_cast<int*>(base + 3LL * n * n);
+    std::vector<double> cs;
+    std::vector<int2> sweeps;
+    long long pos = 0;
+    const long long target = (long long)(1.05 * n * n);
+    while (n > 1) {
+        int l = (int)(rng() % n), m = (int)(rng() % n);
+        if (l > m) std::swap(l, m);
+        if (m == l) continue;
+        if (pos + (m - l) > target) break;
+        sweeps.push_back(make_int2(l, m - 1));
+        for (int i = m - 1; i >= l; --i) {
+            const double th = ang(rng);
+            double c = std::cos(th), s = std::sin(th);
+            switch (rng() % 50) {
+                case 0: c = 1.0, s = 0.0; break;
+                case 1: c = -1.0, s = 0.0; break;
+                case 2: c = 0.0, s = 1.0; break;
+                case 3: c = 0.0, s = -1.0; break;
+                default: break;
+            }
+            cs.push_back(c);
+            cs.push_back(s);
+            log[pos++] = herm_fixed_entry(c, s);
+        }
+    }
+    for (size_t k = 0; k < sweeps.size(); ++k) table[k] = sweeps[k];
+    tail[0] = (int)sweeps.size();
+    tail[1] = 0;
+    int info = 0;
+    std::vector<double> Y((size_t)n * n);
+    apply_real(n, Y.data(), ws.data(), &info);
+    std::vector<long double> X((size_t)n * n, 0.0L);  // column-major, as Y
+    for (int i = 0; i < n; ++i) X[(size_t)i * n + i] = 1.0L;
+    size_t p = 0;
+    for (const int2& f : sweeps)
+        for (int i = f.y; i >= f.x; --i, p += 2) {
+            const long double c = cs[p], s = cs[p + 1];
+            for (int r = 0; r < n; ++r) {
+                const long double a = X[(size_t)i * n + r], b = X[(size_t)(i + 1) * n + r];
+                X[(size_t)(i + 1) * n + r] = s * a + c * b;
+                X[(size_t)i * n + r] = c * a - s * b;
+            }
+        }
+    double err = 0.0, orth = 0.0;
+    for (size_t k = 0; k < Y.size(); ++k) err = std::fmax(err, (double)std::fabs((long double)Y[k] - X[k]));
+    for (int a = 0; a < n; ++a)
+        for (int b = 0; b < n; ++b) {
+            long double d = 0.0L;
+            for (int r = 0; r < n; ++r) d += (long double)Y[(size_t)a * n + r] * Y[(size_t)b * n + r];
+            orth = std::fmax(orth, (double)std::fabs(d - (a == b ? 1.0L : 0.0L)));
+        }
+    const bool ok = err <= 2e-16 && orth <= 4e-16 * std::sqrt((double)n);
+    std::printf("%s rotations n=%d count %zu max |Y - exact| %.2e orth %.2e\n", ok ? "pass" : "FAIL", n, cs.size() / 2,
+                err, orth);
+    if (!ok) ++failures;
+}
+
 // The tridiagonalisation (herm_tridiag_one), then divide and conquer on (d, e) (herm_dc_one) for Y and the
 // eigenvalues, and X = Q Y on the host; residual and orthonormality as run().
 template <int G>
@@ -345,6 +414,7 @@ int main() {
     std::setvbuf(stdout, nullptr, _IONBF, 0);
     std::mt19937_64 rng(11);
     std::normal_distribution<double> nd;
+    for (int n : {2, 8, 121, 301}) run_rotations(n, 5u + (unsigned)n);  // the fixed-point rotation product alone
     for (int n : {1, 2, 3, 9, 33, 61}) {
         std::vector<zc> r((size_t)n * n), t((size_t)n * n), d((size_t)n * n, zc{0.0, 0.0});
         for (int j = 0; j < n; ++j)
