@@ -240,7 +240,9 @@ void rcwa_options_default(rcwa_options* options);
 long long rcwa_gpu_launch_count(void);
 /* QL rotations applied by the Hermitian eigensolver (the solve path for layers of real permittivity) on the
  * current device since the previous call; reading resets the count and synchronises the device. For work
- * accounting: each rotation is 12 n real flops on the eigenvector matrix. -1 on a device error. */
+ * accounting: each rotation is 6 n real operations on the real eigenvector factor Y (orders up to 904,
+ * carried out in 64-bit fixed point on the integer pipes), or 12 n real flops on the complex eigenvector
+ * matrix above that order. -1 on a device error. */
 long long rcwa_gpu_eig_rotations(void);
 
 /* Context lifetime. No reference counterpart: the reference keeps no state between calls
