@@ -151,6 +151,37 @@ void run(int n, const std::vector<zc>& a, const char* tag, bool real_form, bool 
     if (!ok) ++failures;
 }
 
+// herm_q62 (a rotation coefficient to round(x 2^62), integer operations only) against long-double rounding
+// on random values of every magnitude and on the edges: +-0, subnormals, values below 2^-63, ties, +-1 and
+// one ulp above 1 (saturated to 2^62 - 1), and the limbs of herm_fixed_entry recombined.
+void check_q62() {
+    std::mt19937_64 rng(3);
+    std::uniform_real_distribution<double> u(-1.0, 1.0);
+    std::uniform_int_distribution<int> ex(-80, 0);
+    std::vector<double> xs = {0.0, -0.0, 5e-324, -5e-324, 2.2e-308, 1e-300, 0x1p-63, 0x1p-64, 0x1.8p-63, -0x1.8p-63,
+                              0x1p-62, 0x1.4p-62, 0.5, -0.5, 0.75, 1.0, -1.0, std::nextafter(1.0, 2.0),
+                              -std::nextafter(1.0, 2.0), std::nextafter(1.0, 0.0), -std::nextafter(1.0, 0.0)};
+    for (int k = 0; k < 200000; ++k) xs.push_back(std::ldexp(u(rng), ex(rng)));
+    int bad = 0;
+    for (double x : xs) {
+        const long double lim = 4611686018427387903.0L;  // 2^62 - 1
+        long double want = std::fabs((long double)x) * 4611686018427387904.0L;  // |x| 2^62
+        want = want >= lim ? lim : std::floor(want + 0.5L);                  // half away from zero
+        if (x < 0) want = -want;
+        const long long got = herm_q62(x);
+        if ((long double)got != want) {
+            if (++bad <= 3) std::printf("herm_q62(%a) = %lld, want %.0Lf\n", x, got, want);
+        }
+        const int4 e = herm_fixed_entry(-x, x);  // S = q62(x), M = q62(x)
+        const long long s = (long long)e.x * 2147483648LL + e.y, m = (long long)e.z * 2147483648LL + e.w;
+        if (s != got || m != got || e.y < 0 || e.w < 0) {
+            if (++bad <= 3) std::printf("herm_fixed_entry limbs of %a do not recombine\n", x);
+        }
+    }
+    std::printf("%s q62 conversions %zu mismatches %d\n", bad ? "FAIL" : "pass", xs.size(), bad);
+    if (bad) ++failures;
+}
+
 // herm_apply_real_kernel alone on synthetic sweeps of ~1.05 n^2 random rotations (c = +-1 and s = +-1
 // among them), logged with herm_fixed_entry as the QL kernel logs them, against the same rotations applied
 // in long double: max |Y - exact| <= 2e-16 and orthogonality <= 4e-16 n^(1/2) (the entries leave rounded to
@@ -414,6 +445,7 @@ int main() {
     std::setvbuf(stdout, nullptr, _IONBF, 0);
     std::mt19937_64 rng(11);
     std::normal_distribution<double> nd;
+    check_q62();
     for (int n : {2, 8, 121, 301}) run_rotations(n, 5u + (unsigned)n);  // the fixed-point rotation product alone
     for (int n : {1, 2, 3, 9, 33, 61}) {
         std::vector<zc> r((size_t)n * n), t((size_t)n * n), d((size_t)n * n, zc{0.0, 0.0});

@@ -4,7 +4,8 @@ through a thread-level emulation of the CUDA primitives they use (tests/emu/): t
 applied to a real identity or to the complex Q, on random Hermitian, Toeplitz-plus-Kx^2 and diagonal
 (repeated-eigenvalue) matrices of orders 1..61 and on symmetric-Toeplitz, Wilkinson W+ and glued matrices
 (clustered spectra) of orders 1..162; the fixed-point rotation product alone on synthetic sweeps of
-orders 2..301 against long-double arithmetic (max |Y - exact| <= 2e-16); the blocked reduction (herm_panel_one, panels of 32
+orders 2..301 against long-double arithmetic (max |Y - exact| <= 2e-16), and the conversion of rotation
+coefficients to that fixed point on 200,000 values and its edge cases; the blocked reduction (herm_panel_one, panels of 32
 reflectors, the trailing update and the back-transformation X = Q Y from the stored reflectors and T V^H as
 host products) at orders 64, 65, 97 and 121 (partial and full last panels); the divide-and-conquer
 tridiagonal eigensolver (herm_dc_one) at orders 1..162 on random, Toeplitz-plus-Kx^2, diagonal (massive
@@ -32,4 +33,4 @@ def test_hermitian_kernels_in_emulation(tmp_path):
     assert build.returncode == 0, build.stderr[-2000:]
     run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     assert run.returncode == 0 and run.stdout.strip().endswith("OK"), run.stdout[-3000:]
-    assert run.stdout.count("pass ") == 147
+    assert run.stdout.count("pass ") == 148
