@@ -16,7 +16,8 @@ BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(BUILD, "liboracle.so")
 SOURCES = ["oracle_capi.cpp"]
-HEADERS = ["oracle_dense.hpp", "oracle_rcwa1d.hpp", "oracle_conical.hpp", "../include/stablercwa_gb300.h"]
+HEADERS = ["oracle_dense.hpp", "oracle_rcwa1d.hpp", "oracle_conical.hpp", "oracle_rcwa2d.hpp",
+           "../include/stablercwa_gb300.h"]
 
 
 def _stale(target, deps):

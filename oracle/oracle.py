@@ -35,6 +35,12 @@ def lib():
         L.oracle_eig_residual.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_layer_matrix.argtypes = [C.POINTER(abi.rcwa_layer1d), C.c_double, C.c_double, C.c_double,
                                           C.c_double, C.c_int, C.c_int, C.c_void_p]
+        L.oracle_layer_operators2d.restype = C.c_int
+        L.oracle_layer_operators2d.argtypes = [C.POINTER(abi.rcwa_layer2d), C.c_double, C.c_double, C.c_int, C.c_int,
+                                               C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_solve2d_batch.restype = C.c_int
+        L.oracle_solve2d_batch.argtypes = [C.POINTER(abi.rcwa_stack2d), C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                           C.POINTER(abi.rcwa_result2d), C.c_int, C.c_char_p, C.c_size_t]
         _lib = L
     return _lib
 
@@ -128,3 +134,30 @@ def layer_matrix(layer, period, wavelength, nI, theta_deg, M, pol):
     if rc != 0:
         raise ArithmeticError("singular permittivity matrix")
     return a
+
+
+def layer_operators2d(layer, Lx, Ly, M1, M2, laurent=False):
+    """(Eps, Cx, Cy) of one 2-D layer as N x N arrays, and a singular flag (rcwa2d_operators.hpp:325-429)."""
+    N = (2 * M1 + 1) * (2 * M2 + 1)
+    keep = []
+    L = abi.rcwa_layer2d()
+    abi.marshal_layer2d(layer, L, keep)
+    out = [np.zeros((N, N), np.complex128) for _ in range(3)]
+    rc = lib().oracle_layer_operators2d(C.byref(L), Lx, Ly, M1, M2, 1 if laurent else 0,
+                                        *[o.ctypes.data for o in out])
+    return out[0], out[1], out[2], rc != 0
+
+
+def solve2d_batch(stack, points, M1, M2, laurent=False, threads=1):
+    """rcwa::solve2d per point on the CPU: dict of numpy arrays shaped (P, N) as abi.result2d_views gives
+    (n_dense_solve is not restated). points: (wavelength, theta_deg, phi_deg, Es, Ep) tuples."""
+    st, keep = abi.marshal_stack2d(stack)
+    pts = abi.points2d_array(points)
+    N = (2 * M1 + 1) * (2 * M2 + 1)
+    res, arrays = abi.result2d_views(len(points), N, len(stack.layers))
+    err = C.create_string_buffer(512)
+    rc = lib().oracle_solve2d_batch(C.byref(st), C.cast(pts, C.c_void_p), len(points), M1, M2, 1 if laurent else 0,
+                                    C.byref(res), threads, err, 512)
+    if rc != 0:
+        raise OracleInvalidArgument(err.value.decode())
+    return arrays

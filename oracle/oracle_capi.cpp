@@ -13,6 +13,7 @@
 
 #include "../include/stablercwa_gb300.h"
 #include "oracle_conical.hpp"
+#include "oracle_rcwa2d.hpp"
 
 using namespace oracle;
 
@@ -47,6 +48,29 @@ Stack1D to_stack(const rcwa_stack1d* s) {
         out.layers.push_back(std::move(l));
     }
     return out;
+}
+
+r2d::Layer to_layer2d(const rcwa_layer2d& L) {
+    r2d::Layer l;
+    l.d = L.d;
+    l.homogeneous = L.homogeneous != 0;
+    l.n = C(L.n);
+    if (!l.homogeneous) {
+        for (int k = 0; k <= L.n_strips; ++k) l.y_edges.push_back(L.y_edges[k]);
+        for (int k = 0; k < L.n_strips; ++k) {
+            const rcwa_xprofile2d& xp = L.x_profiles[k];
+            r2d::XProfile p;
+            for (int j = 0; j <= xp.n_segments; ++j) p.edges.push_back(xp.edges[j]);
+            for (int j = 0; j < xp.n_segments; ++j) p.n.push_back(C(xp.n_values[j]));
+            l.strips.push_back(std::move(p));
+        }
+    }
+    return l;
+}
+
+void put_mat(const Mat& m, rcwa_complex* out) {  // row-major, as the engine's operator export
+    for (int i = 0; i < m.rows; ++i)
+        for (int j = 0; j < m.cols; ++j) out[static_cast<std::size_t>(i) * m.cols + j] = R(m(i, j));
 }
 
 Mat to_mat(const rcwa_complex* p, int rows, int cols) {
@@ -243,6 +267,94 @@ int oracle_layer_matrix(const rcwa_layer1d* layer, double period, double wavelen
         for (std::size_t k = 0; k < op.a.a.size(); ++k) a[k] = R(op.a.a[k]);
     } catch (const r1::NumericalFailure&) {
         return -1;
+    }
+    return 0;
+}
+
+// Eps, Cx, Cy of one 2-D layer (include/stablercwa/rcwa2d_operators.hpp:325-429), N x N row-major each.
+// factorization: RCWA_FACTORIZATION_LI or _LAURENT. Returns 0, or 1 where an inverse-rule block is singular.
+int oracle_layer_operators2d(const rcwa_layer2d* layer, double Lx, double Ly, int M1, int M2, int factorization,
+                             rcwa_complex* eps, rcwa_complex* cx, rcwa_complex* cy) {
+    try {
+        const r2d::Operators op = r2d::layer_operators(to_layer2d(*layer), Lx, Ly, M1, M2,
+                                                       factorization == RCWA_FACTORIZATION_LAURENT);
+        put_mat(op.eps, eps);
+        put_mat(op.cx, cx);
+        put_mat(op.cy, cy);
+    } catch (const Singular&) {
+        return 1;
+    }
+    return 0;
+}
+
+// Batched 2-D solve on the CPU: rcwa::solve2d per point (include/stablercwa/rcwa2d.hpp:1359), the operators
+// formed once per stack, points split over n_threads std::threads. out's arrays as rcwa_result2d documents;
+// n_dense_solve is not restated (left untouched). Returns 0, or -1 with a message.
+int oracle_solve2d_batch(const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points, int M1, int M2,
+                         int factorization, rcwa_result2d* out, int n_threads, char* err, size_t err_len) {
+    r2d::Stack st;
+    st.nI = stack->nI;
+    st.nII = C(stack->nII);
+    st.Lx = stack->Lx;
+    st.Ly = stack->Ly;
+    for (int k = 0; k < stack->n_layers; ++k) st.layers.push_back(to_layer2d(stack->layers[k]));
+    const int L = static_cast<int>(st.layers.size());
+    std::vector<r2d::Operators> ops(static_cast<std::size_t>(L));
+    bool singular = false;
+    for (int k = 0; k < L; ++k) {
+        if (st.layers[k].homogeneous) continue;
+        try {
+            ops[k] = r2d::layer_operators(st.layers[k], st.Lx, st.Ly, M1, M2, factorization == RCWA_FACTORIZATION_LAURENT);
+        } catch (const Singular&) {
+            singular = true;
+        }
+    }
+    if (singular) {
+        put_error(err, err_len, "oracle: an inverse-rule Toeplitz block is singular");
+        return -1;
+    }
+    const int N = (2 * M1 + 1) * (2 * M2 + 1);
+    std::atomic<int> next{0};
+    const auto worker = [&]() {
+        for (;;) {
+            const int p = next.fetch_add(1);
+            if (p >= n_points) return;
+            const rcwa_point2d& pt = points[p];
+            const r2d::Result r = r2d::solve2d(st, ops, pt.wavelength, pt.theta_deg, pt.phi_deg, M1, M2, C(pt.Es), C(pt.Ep));
+            const std::size_t o = static_cast<std::size_t>(p) * N;
+            for (int i = 0; i < N; ++i) {
+                out->Kx[o + i] = r.Kx[i];
+                out->Ky[o + i] = r.Ky[i];
+                out->kzI[o + i] = R(r.kzI[i]);
+                out->kzII[o + i] = R(r.kzII[i]);
+                out->Ex_r[o + i] = R(r.Ex_r[i]);
+                out->Ey_r[o + i] = R(r.Ey_r[i]);
+                out->Ez_r[o + i] = R(r.Ez_r[i]);
+                out->Ex_t[o + i] = R(r.Ex_t[i]);
+                out->Ey_t[o + i] = R(r.Ey_t[i]);
+                out->Ez_t[o + i] = R(r.Ez_t[i]);
+                out->Rs[o + i] = R(r.Rs[i]);
+                out->Rp[o + i] = R(r.Rp[i]);
+                out->Ts[o + i] = R(r.Ts[i]);
+                out->Tp[o + i] = R(r.Tp[i]);
+                out->DEr[o + i] = r.DEr[i];
+                out->DEt[o + i] = r.DEt[i];
+                out->prop_r[o + i] = r.prop_r[i];
+                out->prop_t[o + i] = r.prop_t[i];
+            }
+            out->status[p] = r.status;
+            if (out->eig_info) out->eig_info[p] = r.eig_info;
+            if (out->n_eig) out->n_eig[p] = r.n_eig;
+            if (out->rayleigh_regions)
+                for (int k = 0; k < L + 2; ++k) out->rayleigh_regions[static_cast<std::size_t>(p) * (L + 2) + k] = r.rayleigh[k];
+        }
+    };
+    if (n_threads <= 1) {
+        worker();
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < n_threads; ++t) pool.emplace_back(worker);
+        for (std::thread& t : pool) t.join();
     }
     return 0;
 }
