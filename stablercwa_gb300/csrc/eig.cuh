@@ -1631,8 +1631,8 @@ static __global__ void __launch_bounds__(128) herm_apply_kernel(int n, int batch
 // -- three 32 x 32 -> 64 multiply-adds -- and the rotation y_{i+1} <- s y_i + c y_{i+1}, y_i <- c y_i -
 // s y_{i+1} is
 //   y_{i+1} = R(S, y_i) - R(M, y_{i+1}),   y_i = -R(M, y_i) - R(S, y_{i+1}),
-// each the sum of four limb products (signs carried by the entry limbs), the four 2^-31 terms gathered in one
-// 64-bit accumulator and rounded to nearest once. Each output is the difference of two products that drop
+// six limb products an output (signs carried by the entry limbs): the two high-by-high terms added whole, the
+// four cross terms gathered in one 64-bit accumulator and rounded to nearest once. Each output is the difference of two products that drop
 // the same kind of term, so those errors (under a unit each) cancel on average instead of drifting over the
 // ~2 n rotations an entry takes. Resolution 2^-60 absolute against FP64's 2^-53 relative: as accurate for
 // entries near 1/sqrt(n), more so near 1. No intermediate overflows: |Y| <= 2^60 and s^2 + c^2 = 1 keep the
