@@ -38,6 +38,10 @@ def lib():
         L.oracle_layer_operators2d.restype = C.c_int
         L.oracle_layer_operators2d.argtypes = [C.POINTER(abi.rcwa_layer2d), C.c_double, C.c_double, C.c_int, C.c_int,
                                                C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_solve2d_fields.restype = C.c_int
+        L.oracle_solve2d_fields.argtypes = [C.POINTER(abi.rcwa_stack2d), C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                            C.c_void_p, C.c_int, C.POINTER(abi.rcwa_result2d), C.c_void_p, C.c_int,
+                                            C.c_char_p, C.c_size_t]
         L.oracle_solve2d_batch.restype = C.c_int
         L.oracle_solve2d_batch.argtypes = [C.POINTER(abi.rcwa_stack2d), C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                            C.POINTER(abi.rcwa_result2d), C.c_int, C.c_char_p, C.c_size_t]
@@ -161,3 +165,20 @@ def solve2d_batch(stack, points, M1, M2, laurent=False, threads=1):
     if rc != 0:
         raise OracleInvalidArgument(err.value.decode())
     return arrays
+
+
+def solve2d_fields(stack, points, M1, M2, zs, laurent=False, threads=1):
+    """solve2d_batch plus the near-field harmonics at depths zs (include/stablercwa/rcwa2d_fields.hpp): returns
+    (arrays, fields) with fields shaped (P, 6, N, len(zs)), components Ex, Ey, Ez, Hx, Hy, Hz."""
+    st, keep = abi.marshal_stack2d(stack)
+    pts = abi.points2d_array(points)
+    N = (2 * M1 + 1) * (2 * M2 + 1)
+    res, arrays = abi.result2d_views(len(points), N, len(stack.layers))
+    z = np.ascontiguousarray(zs, np.float64)
+    fields = np.zeros((len(points), 6, N, len(z)), np.complex128)
+    err = C.create_string_buffer(512)
+    rc = lib().oracle_solve2d_fields(C.byref(st), C.cast(pts, C.c_void_p), len(points), M1, M2, 1 if laurent else 0,
+                                     z.ctypes.data, len(z), C.byref(res), fields.ctypes.data, threads, err, 512)
+    if rc != 0:
+        raise OracleInvalidArgument(err.value.decode())
+    return arrays, fields

@@ -287,11 +287,13 @@ int oracle_layer_operators2d(const rcwa_layer2d* layer, double Lx, double Ly, in
     return 0;
 }
 
-// Batched 2-D solve on the CPU: rcwa::solve2d per point (include/stablercwa/rcwa2d.hpp:1359), the operators
-// formed once per stack, points split over n_threads std::threads. out's arrays as rcwa_result2d documents;
-// n_dense_solve is not restated (left untouched). Returns 0, or -1 with a message.
-int oracle_solve2d_batch(const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points, int M1, int M2,
-                         int factorization, rcwa_result2d* out, int n_threads, char* err, size_t err_len) {
+}  // extern "C"
+
+namespace {
+
+int solve2d_points(const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points, int M1, int M2,
+                   int factorization, const double* zs, int nz, rcwa_complex* fields, rcwa_result2d* out,
+                   int n_threads, char* err, size_t err_len) {
     r2d::Stack st;
     st.nI = stack->nI;
     st.nII = C(stack->nII);
@@ -320,7 +322,12 @@ int oracle_solve2d_batch(const rcwa_stack2d* stack, const rcwa_point2d* points, 
             const int p = next.fetch_add(1);
             if (p >= n_points) return;
             const rcwa_point2d& pt = points[p];
-            const r2d::Result r = r2d::solve2d(st, ops, pt.wavelength, pt.theta_deg, pt.phi_deg, M1, M2, C(pt.Es), C(pt.Ep));
+            std::vector<double> depths(zs, zs + (fields ? nz : 0));
+            CVec f;
+            const r2d::Result r = r2d::solve2d(st, ops, pt.wavelength, pt.theta_deg, pt.phi_deg, M1, M2, C(pt.Es), C(pt.Ep),
+                                               fields ? &depths : nullptr, fields ? &f : nullptr);
+            if (fields)
+                for (std::size_t k = 0; k < f.size(); ++k) fields[static_cast<std::size_t>(p) * f.size() + k] = R(f[k]);
             const std::size_t o = static_cast<std::size_t>(p) * N;
             for (int i = 0; i < N; ++i) {
                 out->Kx[o + i] = r.Kx[i];
@@ -357,6 +364,27 @@ int oracle_solve2d_batch(const rcwa_stack2d* stack, const rcwa_point2d* points, 
         for (std::thread& t : pool) t.join();
     }
     return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Batched 2-D solve on the CPU: rcwa::solve2d per point (include/stablercwa/rcwa2d.hpp:1359), the operators
+// formed once per stack, points split over n_threads std::threads. out's arrays as rcwa_result2d documents;
+// n_dense_solve is not restated (left untouched). Returns 0, or -1 with a message.
+int oracle_solve2d_batch(const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points, int M1, int M2,
+                         int factorization, rcwa_result2d* out, int n_threads, char* err, size_t err_len) {
+    return solve2d_points(stack, points, n_points, M1, M2, factorization, nullptr, 0, nullptr, out, n_threads, err,
+                          err_len);
+}
+
+// The same with the near-field harmonics at nz depths (include/stablercwa/rcwa2d_fields.hpp): fields holds,
+// per point, 6 components (Ex, Ey, Ez, Hx, Hy, Hz) x N orders x nz depths, the depth index fastest.
+int oracle_solve2d_fields(const rcwa_stack2d* stack, const rcwa_point2d* points, int n_points, int M1, int M2,
+                          int factorization, const double* zs, int nz, rcwa_result2d* out, rcwa_complex* fields,
+                          int n_threads, char* err, size_t err_len) {
+    return solve2d_points(stack, points, n_points, M1, M2, factorization, zs, nz, fields, out, n_threads, err, err_len);
 }
 
 }  // extern "C"

@@ -11,7 +11,10 @@
 //   * the reflection recursion from the exit medium up, with every interface in the reference's direct form
 //     (r' = A+^-1 A-, A+- = (I + r) Nn +- (I - r) Mm; rcwa2d.hpp:738-790), the propagation blocks, the top
 //     interface solved directly (K d = 2 e; rcwa2d.hpp:871-896) and the amplitudes carried back down;
-//   * the efficiencies, the z components and the s/p amplitudes (rcwa2d.hpp:1226-1262), Rayleigh checks.
+//   * the efficiencies, the z components and the s/p amplitudes (rcwa2d.hpp:1226-1262), Rayleigh checks;
+//   * the near-field harmonics at given depths (include/stablercwa/rcwa2d_fields.hpp:17-43: the layer
+//     amplitudes a+ at each layer's top and a- at its bottom, the regions' plane waves, hz and Ez from the
+//     tangential fields, H = -i h), with the reference's rule for which region a depth belongs to.
 // The reference keeps block-diagonal operators of homogeneous regions in O(N) form and switches between
 // S-block and direct forms by case; here every matrix is dense and every interface direct: the same
 // algebra, so results agree with the reference's to rounding, not bit for bit. Parity with the reference
@@ -261,6 +264,7 @@ inline cplx kz_over_k0(cplx n, double Kx, double Ky) {
 struct Modes {
     CVec q;
     Mat W, V;
+    Mat Ei;  // structured layers: Eps^-1 (the near field's Ez)
 };
 
 // A homogeneous region (rcwa2d.hpp:386-410): W = I, q = branch(-i kz) twice, V = Qb / q with
@@ -288,7 +292,8 @@ inline Modes homogeneous_modes(cplx n, const std::vector<double>& Kx, const std:
 // H = P Q, H W = W diag(lambda), q = branch(sqrt(lambda)), V = Q W / q. Returns the eigensolver's info.
 inline int structured_modes(const Operators& op, const std::vector<double>& Kx, const std::vector<double>& Ky, Modes& m) {
     const int N = static_cast<int>(Kx.size()), n = 2 * N;
-    const Mat Ei = solve(op.eps, Mat::eye(N));
+    m.Ei = solve(op.eps, Mat::eye(N));
+    const Mat& Ei = m.Ei;
     Mat P(n, n), Q(n, n);
     for (int j = 0; j < N; ++j)
         for (int i = 0; i < N; ++i) {
@@ -387,8 +392,16 @@ inline bool finite_vec(const CVec& v) {
 
 // rcwa::solve2d for one point (rcwa2d.hpp:1042-1347, :1359). ops[j] are layer j's operators (ignored for
 // homogeneous layers).
+inline void near_fields(const Stack& st, const std::vector<Modes>& modes, const std::vector<CVec>& a_plus,
+                        const std::vector<CVec>& a_minus, const CVec& inc, const CVec& R, const CVec& T,
+                        const Result& res, double k0, int i0, const std::vector<double>& zs, CVec& fields);
+
+// rcwa::solve2d for one point (rcwa2d.hpp:1042-1347, :1359). ops[j] are layer j's operators (ignored for
+// homogeneous layers). With zs, fields receives the near-field harmonics (6 components Ex, Ey, Ez, Hx, Hy, Hz
+// x N orders x zs.size() depths, last index fastest), NaN where the solve failed.
 inline Result solve2d(const Stack& st, const std::vector<Operators>& ops, double wavelength, double theta_deg,
-                      double phi_deg, int M1, int M2, cplx Es, cplx Ep) {
+                      double phi_deg, int M1, int M2, cplx Es, cplx Ep, const std::vector<double>* zs = nullptr,
+                      CVec* fields = nullptr) {
     const int n1 = 2 * M1 + 1, n2 = 2 * M2 + 1, N = n1 * n2, L = static_cast<int>(st.layers.size());
     const double nI = st.nI, k0 = 2.0 * kPi / wavelength;
     const double th = theta_deg * (kPi / 180.0), ph = phi_deg * (kPi / 180.0);
@@ -421,6 +434,7 @@ inline Result solve2d(const Stack& st, const std::vector<Operators>& ops, double
             v->assign(N, cplx{nan, nan});
         res.DEr.assign(N, nan);
         res.DEt.assign(N, nan);
+        if (fields) fields->assign(6 * static_cast<std::size_t>(N) * (zs ? zs->size() : 0), cplx{nan, nan});
         return res;
     };
     // Rayleigh anomalies: an order with kz exactly 0 in a homogeneous region (rcwa2d.hpp:1094-1112)
@@ -469,11 +483,16 @@ inline Result solve2d(const Stack& st, const std::vector<Operators>& ops, double
         // the exit medium (r = 0) up to block 1, block 0 (the top interface) solved directly
         const int blocks = 2 * L + 1;
         std::vector<Step> steps(static_cast<std::size_t>(blocks));
+        std::vector<Mat> r_below(static_cast<std::size_t>(L));  // the reflection under each layer
         Mat r(2 * N, 2 * N);
         for (int b = blocks - 1; b >= 1; --b) {
             const int j = b / 2;
-            if (b % 2 == 0) r = interface_on(modes[j], modes[j + 1], r, steps[b]);
-            else r = propagation_on(modes[j + 1].q, st.layers[j].d, k0, r, steps[b]);
+            if (b % 2 == 0) {
+                r = interface_on(modes[j], modes[j + 1], r, steps[b]);
+            } else {
+                if (fields) r_below[j] = r;
+                r = propagation_on(modes[j + 1].q, st.layers[j].d, k0, r, steps[b]);
+            }
         }
         // top: e + R = W (I + r) d, V_I (e - R) = V (I - r) d  =>  [W (I + r) + V_I^-1 V (I - r)] d = 2 e
         const Modes& low = modes[1];
@@ -485,7 +504,13 @@ inline Result solve2d(const Stack& st, const std::vector<Operators>& ops, double
         CVec down(dmat.a);
         CVec R = matvec(wp, down);
         for (int i = 0; i < 2 * N; ++i) R[i] -= inc[i];
-        for (int b = 1; b < blocks; ++b) down = carry(steps[b], down);
+        std::vector<CVec> a_plus(static_cast<std::size_t>(L)), a_minus(static_cast<std::size_t>(L));
+        for (int b = 1; b < blocks; ++b) {
+            const bool propagation = b % 2 != 0;
+            if (fields && propagation) a_plus[b / 2] = down;  // at the layer's top
+            down = carry(steps[b], down);
+            if (fields && propagation) a_minus[b / 2] = matvec(r_below[b / 2], down);  // at its bottom
+        }
         const CVec& T = down;
         if (!finite_vec(R) || !finite_vec(T)) return fail(kNumerical);
         // efficiencies and s/p amplitudes (rcwa2d.hpp:1226-1262)
@@ -525,10 +550,104 @@ inline Result solve2d(const Stack& st, const std::vector<Operators>& ops, double
             if (!std::isfinite(res.DEr[i]) || !std::isfinite(res.DEt[i]) || !finite(res.Rs[i]) || !finite(res.Rp[i]) ||
                 !finite(res.Ts[i]) || !finite(res.Tp[i]))
                 return fail(kNumerical);
+        if (fields) {
+            near_fields(st, modes, a_plus, a_minus, inc, R, T, res, k0, i0, *zs, *fields);
+            if (!finite_vec(*fields)) return fail(kNumerical);
+        }
     } catch (const Singular&) {
         return fail(kNumerical);
     }
     return res;
+}
+
+// The six near-field harmonics at each depth (include/stablercwa/rcwa2d_fields.hpp:17-43). z runs down from
+// the top surface (z = 0) to z_bot, the sum of the thicknesses. A depth belongs to the incident region when
+// z < 0, to the exit region when z > z_bot (or when there are no layers), else to the first layer with
+// z <= z_top + d + 1e-12, its distance from the layer's top clamped to [0, d]. Per region:
+//   incident:  F = inc e^(-k0 q z) + R e^(k0 q z), G = V_I (-inc e^(-k0 q z) + R e^(k0 q z)), the incident term
+//              only on the (0, 0) order's two entries (where inc is non-zero), Ei = 1 / nI^2;
+//   exit:      F = T e^(-k0 q (z - z_bot)), G = -V_II F, Ei = 1 / nII^2;
+//   layer:     F = W (a+ e^(-k0 q zl) + a- e^(-k0 q (d - zl))), G = V (-a+ ... + a- ...), Ei = Eps^-1 (1 / n^2
+//              for a homogeneous layer);
+// then Ex, Ey = F's halves, hx, hy = G's halves, hz = i (Ky Ex - Kx Ey), Ez = i Ei (Ky hx - Kx hy),
+// (Hx, Hy, Hz) = -i (hx, hy, hz).
+inline void near_fields(const Stack& st, const std::vector<Modes>& modes, const std::vector<CVec>& a_plus,
+                        const std::vector<CVec>& a_minus, const CVec& inc, const CVec& R, const CVec& T,
+                        const Result& res, double k0, int i0, const std::vector<double>& zs, CVec& fields) {
+    const int N = static_cast<int>(res.Kx.size()), L = static_cast<int>(st.layers.size());
+    const std::size_t nz = zs.size();
+    fields.assign(6 * static_cast<std::size_t>(N) * nz, cplx{});
+    std::vector<double> top(static_cast<std::size_t>(L));
+    double zbot = 0.0;
+    for (int j = 0; j < L; ++j) {
+        top[j] = zbot;
+        zbot += st.layers[j].d;
+    }
+    const cplx I{0.0, 1.0};
+    for (std::size_t iz = 0; iz < nz; ++iz) {
+        const double z = zs[iz];
+        int region = -1;  // -1 incident, L exit, else the layer
+        if (z < 0.0) region = -1;
+        else if (L == 0 || z > zbot) region = L;
+        else {
+            region = L;
+            for (int j = 0; j < L; ++j)
+                if (z <= top[j] + st.layers[j].d + 1e-12) {
+                    region = j;
+                    break;
+                }
+        }
+        CVec F(2 * static_cast<std::size_t>(N)), u(2 * static_cast<std::size_t>(N));
+        const Mat* Vm = nullptr;
+        const Mat* Eim = nullptr;
+        cplx inv_eps{};
+        if (region < 0) {
+            const Modes& m = modes[0];
+            for (int i = 0; i < 2 * N; ++i) {
+                const cplx up = R[i] * std::exp(k0 * m.q[i] * z);
+                F[i] = up;
+                u[i] = up;
+            }
+            for (int i : {i0, N + i0}) {
+                const cplx dn = inc[i] * std::exp(-k0 * m.q[i] * z);
+                F[i] += dn;
+                u[i] -= dn;
+            }
+            Vm = &m.V;
+            inv_eps = cplx{1.0, 0.0} / (cplx{st.nI, 0.0} * st.nI);
+        } else if (region == L) {
+            const Modes& m = modes[L + 1];
+            for (int i = 0; i < 2 * N; ++i) {
+                F[i] = T[i] * std::exp(-k0 * m.q[i] * (z - zbot));
+                u[i] = -F[i];
+            }
+            Vm = &m.V;
+            inv_eps = cplx{1.0, 0.0} / (st.nII * st.nII);
+        } else {
+            const Modes& m = modes[region + 1];
+            const double d = st.layers[region].d, zl = std::min(std::max(z - top[region], 0.0), d);
+            CVec w(2 * static_cast<std::size_t>(N));
+            for (int i = 0; i < 2 * N; ++i) {
+                const cplx ep = a_plus[region][i] * std::exp(-k0 * m.q[i] * zl);
+                const cplx em = a_minus[region][i] * std::exp(-k0 * m.q[i] * (d - zl));
+                w[i] = ep + em;
+                u[i] = em - ep;
+            }
+            F = matvec(m.W, w);
+            Vm = &m.V;
+            if (st.layers[region].homogeneous) inv_eps = cplx{1.0, 0.0} / (st.layers[region].n * st.layers[region].n);
+            else Eim = &m.Ei;
+        }
+        const CVec G = matvec(*Vm, u);
+        CVec t(static_cast<std::size_t>(N));
+        for (int i = 0; i < N; ++i) t[i] = res.Ky[i] * G[i] - res.Kx[i] * G[N + i];
+        const CVec ez = Eim ? matvec(*Eim, t) : t;
+        for (int i = 0; i < N; ++i) {
+            const cplx hz = I * (res.Ky[i] * F[i] - res.Kx[i] * F[N + i]);
+            const cplx vals[6] = {F[i], F[N + i], I * (Eim ? ez[i] : inv_eps * ez[i]), -I * G[i], -I * G[N + i], -I * hz};
+            for (int c = 0; c < 6; ++c) fields[(static_cast<std::size_t>(c) * N + i) * nz + iz] = vals[c];
+        }
+    }
 }
 
 }  // namespace r2d

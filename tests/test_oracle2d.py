@@ -2,8 +2,9 @@
 the reference's frozen operator tables, its amplitudes and efficiencies against the frozen tables of
 tests/rcwa2d_reference.inc and tests/rcwa2d_core_fixture.inc and against the reference's own rcwa::solve2d
 outputs (include/stablercwa/rcwa2d.hpp:1359) for every case of tests/golden/rcwa2d_cases.jsonl.gz, its
-Rayleigh statuses, and energy conservation on the lossless cases. CPU only: the oracle is the checker the
-device parity tests can use on inputs the fixtures do not hold."""
+Rayleigh statuses, energy conservation on the lossless cases, and its near-field harmonics against the
+reference's field_at. CPU only: the oracle is the checker the device parity tests can use on inputs the
+fixtures do not hold."""
 import gzip
 import json
 import os
@@ -137,3 +138,39 @@ def test_energy_conservation_lossless(oracle, cases):
         defect = abs(np.sum(r["DEr"]) + np.sum(r["DEt"]) - 1.0)
         assert defect <= 1e-11, (c["name"], defect)
     assert seen >= 20
+
+
+def test_near_fields_match_reference(oracle):
+    """The oracle's near-field harmonics against the reference's rcwa::field_at (every case of
+    tests/golden/fields2d_cases.jsonl.gz, zero-thickness and layer-less stacks included) and against the
+    frozen Python harmonics within their own tolerances."""
+    with gzip.open(os.path.join(HERE, "golden", "fields2d_cases.jsonl.gz"), "rt") as f:
+        cases = [json.loads(line) for line in f]
+    for c in cases:
+        stack = stack2d_from_json(c["stack"])
+        jones = complex(*c["jones"][0]), complex(*c["jones"][1])
+        arrays, fields = oracle.solve2d_fields(stack, [(c["wavelength"], c["theta"], c["phi"], *jones)], c["M1"], c["M2"],
+                                               c["zs"], laurent=bool(c["laurent"]))
+        assert arrays["status"][0] == 0, c["name"]
+        assert np.max(np.abs(arrays["DEr"][0] - rvec(c["DEr"]))) <= DE_TOL, c["name"]
+        want = np.array([[[complex(*z) for z in row] for row in comp] for comp in c["fields"]])  # (6, N, nz)
+        err = np.max(np.abs(fields[0] - want) / (1.0 + np.abs(want)))
+        assert err <= 1e-11, (c["name"], err)
+        if "frozen" in c:
+            fz = np.array([[[complex(*z) for z in row] for row in comp] for comp in c["frozen"]])
+            assert np.all(np.abs(fields[0] - fz) <= c["near_atol"] + c["near_rtol"] * np.abs(fz)), c["name"]
+    assert len(cases) >= 28
+
+
+def test_c4_point_against_reference(oracle):
+    """One point of the 2-D C4 workload (Mx = My = 10: N = 441, eigenproblems of order 882) through the oracle
+    against the reference's own solve2d output for it: efficiencies within 1e-10 (about a minute on one core)."""
+    with gzip.open(os.path.join(HERE, "golden", "rcwa2d_c4_cases.jsonl.gz"), "rt") as f:
+        c = json.loads(f.readline())
+    assert (c["M1"], c["M2"]) == (10, 10)
+    r = solve(oracle, {**c, "laurent": c.get("laurent", 0)})
+    ref = c["ref"]
+    assert r["status"] == 0 and ref["status"] == 0
+    for key in ("DEr", "DEt"):
+        assert np.max(np.abs(r[key] - rvec(ref[key]))) <= DE_TOL, key
+    assert r["n_eig"] == ref["n_eig"]
