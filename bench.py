@@ -37,7 +37,7 @@ N_POINTS = 4096
 M = 60
 PERIOD = 0.574
 METRIC = "solves/s, batched 1-D TE+TM sweep (M=60, N=121), per-order efficiency error <= 1e-10 vs the FP64 CPU oracle"
-WORKLOAD = ("config 2: batched 1-D TE+TM sweep, M=60 (N=121), binary grating on a 20-layer quarter-wave mirror, "
+WORKLOAD = ("batched 1-D TE+TM sweep, M=60 (N=121), binary grating on a 20-layer quarter-wave mirror, "
             "4096 seeded (lambda, theta) points x 2 polarizations per step")
 
 
@@ -448,7 +448,7 @@ def plain_rate(eng, stack, pts, count, batched_value):
 
 
 def lossy_rate(eng, torch, est, flush, args, peak):
-    """The same C2 sweep with an absorbing grating (n = 1.46 + 0.01i): the general Hessenberg + shifted
+    """The same headline sweep with an absorbing grating (n = 1.46 + 0.01i): the general Hessenberg + shifted
     complex QR eigensolver on every grating matrix. Device-resident points, CUDA events, L2 flushed;
     accuracy against the oracle on a sample."""
     from stablercwa_gb300.engine import launch_count
@@ -508,11 +508,11 @@ def lossy_rate(eng, torch, est, flush, args, peak):
 
 # ------------------------------------------------------------------------------------- other configurations
 
-C3_POINTS, C3_M = 1024, 40
-C4_POINTS, C4_M = 256, 10
+CONICAL_POINTS, CONICAL_M = 1024, 40
+CROSSED_POINTS, CROSSED_M = 256, 10
 
 
-def workload_c3(seed=SEED):
+def workload_conical(seed=SEED):
     """Batched conical incidence, M = 40 (N = 81, 2N = 162): three gratings with 2-4 random
     segments (n 1.0..2.5, d 0.05..0.3) and one absorbing film n = 1.5+U(0,.5) + i U(0,.1), period
     0.574, nI 1.0, nII 1.46; 1024 points lambda 0.5..1.6, theta 0..60, phi 0..90 degrees."""
@@ -528,12 +528,12 @@ def workload_c3(seed=SEED):
     layers.append(Layer.uniform(rng.uniform(0.05, 0.3), complex(1.5 + rng.uniform(0, 0.5), rng.uniform(0, 0.1))))
     layers.append(grating())
     stack = Stack(nI=1.0, nII=1.46, period=PERIOD, layers=layers)
-    pts = np.stack([rng.uniform(0.5, 1.6, C3_POINTS), rng.uniform(0.0, 60.0, C3_POINTS),
-                    rng.uniform(0.0, 90.0, C3_POINTS)], axis=1)
+    pts = np.stack([rng.uniform(0.5, 1.6, CONICAL_POINTS), rng.uniform(0.0, 60.0, CONICAL_POINTS),
+                    rng.uniform(0.0, 90.0, CONICAL_POINTS)], axis=1)
     return stack, pts
 
 
-def workload_c4(seed=SEED):
+def workload_crossed2d(seed=SEED):
     """Batched 2-D crossed grating, Mx = My = 10 (N = 441, 2N = 882): square lattice P 0.6..1.0,
     three patterned layers (d 0.05..0.3; a circular pillar r = 0.15..0.4 P staircased into 16 y strips
     or a w x h = 0.2..0.7 P rectangle, n = 2.0 in air) between five films (n 1.3..2.2, d 0.05..0.2),
@@ -568,12 +568,12 @@ def workload_c4(seed=SEED):
     layers = [film(), patterned(), film(), patterned(), film(), patterned(), film(), film()]
     stack = Stack2D(nI=1.0, nII=1.46, layers=layers, Lx=P, Ly=P)
     es, ep = jones_from_angles_2d(90.0)
-    pts = [(wl, 0.0, 0.0, es, ep) for wl in rng.uniform(0.4, 1.2, C4_POINTS)]
+    pts = [(wl, 0.0, 0.0, es, ep) for wl in rng.uniform(0.4, 1.2, CROSSED_POINTS)]
     return stack, pts, {"period": float(P)}
 
 
 def run_secondary(args):
-    """--workload c3 | c4 | plain: the conical and 2-D batched configurations, and the C2 structure
+    """--workload conical | crossed2d | plain: the conical and 2-D batched workloads, and the headline structure
     solved one point per call (the plain path). Measured through the host-buffer entry points (these
     paths take host arrays), so value and e2e are the same number."""
     import torch
@@ -581,26 +581,26 @@ def run_secondary(args):
     eng = Engine()
     peak = fp64_peak_tflops(torch)
     herm_model = None  # (matrices per step, order) of the eigensolves that may take the Hermitian path
-    if args.workload == "c3":
-        stack, pts = workload_c3()
+    if args.workload == "conical":
+        stack, pts = workload_conical()
         n_eig_layers = sum(1 for L in stack.layers if not L.homogeneous)
         def step():
-            return eng.solve_conical_arrays(stack, pts, C3_M)
+            return eng.solve_conical_arrays(stack, pts, CONICAL_M)
         solves = len(pts)
-        eig_flops = solves * n_eig_layers * 2 * 105 * (2 * C3_M + 1) ** 3
-        herm_model = (solves * n_eig_layers * 2, 2 * C3_M + 1)
+        eig_flops = solves * n_eig_layers * 2 * 105 * (2 * CONICAL_M + 1) ** 3
+        herm_model = (solves * n_eig_layers * 2, 2 * CONICAL_M + 1)
         metric = "solves/s, batched conical sweep (M=40, 2N=162), full Jones per order"
-        config = {"workload": workload_c3.__doc__.split(":")[0].strip() + " (config 3)", "points": len(pts), "M": C3_M,
+        config = {"workload": workload_conical.__doc__.split(":")[0].strip(), "points": len(pts), "M": CONICAL_M,
                   "seed": SEED + 3}
-    elif args.workload == "c4":
-        stack, pts, geo = workload_c4()
+    elif args.workload == "crossed2d":
+        stack, pts, geo = workload_crossed2d()
         n_pat = sum(1 for L in stack.layers if not L.homogeneous)
         def step():
-            return eng.solve2d_arrays(stack, pts, C4_M, C4_M)
+            return eng.solve2d_arrays(stack, pts, CROSSED_M, CROSSED_M)
         solves = len(pts)
-        eig_flops = solves * n_pat * 105 * (2 * (2 * C4_M + 1) ** 2) ** 3
+        eig_flops = solves * n_pat * 105 * (2 * (2 * CROSSED_M + 1) ** 2) ** 3
         metric = "solves/s, batched 2-D solve2d sweep (Mx=My=10, N=441, 2N=882)"
-        config = {"workload": "batched 2-D crossed grating (config 4)", "points": len(pts), "M1": C4_M, "M2": C4_M,
+        config = {"workload": "batched 2-D crossed grating, Mx=My=10 (N=441), 256 wavelengths", "points": len(pts), "M1": CROSSED_M, "M2": CROSSED_M,
                   "seed": SEED + 4, **geo}
     else:
         stack, all_pts, geo = workload()
@@ -610,8 +610,8 @@ def run_secondary(args):
         solves = 2 * len(pts)
         eig_flops = solves * 105 * (2 * M + 1) ** 3
         herm_model = (solves, 2 * M + 1)
-        metric = "solves/s, plain path: the C2 structure solved one point per call (M=60, N=121)"
-        config = {"workload": "config 2 structure, 64 of its points x TE+TM, one solve per call", "M": M, "seed": SEED,
+        metric = "solves/s, plain path: the grating-on-mirror structure solved one point per call (M=60, N=121)"
+        config = {"workload": "grating-on-mirror structure, 64 of its points x TE+TM, one solve per call", "M": M, "seed": SEED,
                   **geo}
     for _ in range(args.warmup):
         out = step()
@@ -659,19 +659,19 @@ def run_secondary(args):
             "kernels_ms_per_step": {"eig": eig_ms, "lu": lu_ms, "gemm": gemm_ms,
                                     "other": 1e3 * step_s - (eig_ms + lu_ms + gemm_ms),
                                     "note": "one instrumented step run after the timed ones"}}
-    if args.workload == "c3":
+    if args.workload == "conical":
         from oracle import oracle
         threads = os.cpu_count() or 1
         idx = np.linspace(0, len(pts) - 1, args.cpu_points).astype(int)
         t0 = time.perf_counter()
-        ref = oracle.solve_conical_batch(stack, pts[idx], C3_M, threads=threads)
+        ref = oracle.solve_conical_batch(stack, pts[idx], CONICAL_M, threads=threads)
         dt = time.perf_counter() - t0
         err = max(float(np.nanmax(np.abs(out[k][idx] - ref[k]))) for k in ("DEr", "DEt"))
         line["cpu_baseline"] = {"value": len(idx) / dt, "unit": "solves/s", "cores": threads, "kind": "port",
                                 "sample": f"{len(idx)} of the {len(pts)} points, {dt:.1f} s wall"}
         line["accuracy"] = {"max_abs_dDE_vs_oracle": err, "sample_solves": len(idx),
                             "all_status_ok": bool((out["status"] == 0).all())}
-    elif args.workload == "c4":
+    elif args.workload == "crossed2d":
         line["accuracy"] = {"all_status_ok": bool((out["status"] == 0).all()),
                             "max_energy_defect": float(np.max(np.abs(out["DEr"].sum(1) + out["DEt"].sum(1) - 1.0)))}
     print(json.dumps(line), flush=True)
@@ -684,8 +684,8 @@ def run_secondary(args):
 def serve_requests(seed, count, repeat=1):
     """The serving mix: 70 % 1-D (M 20..150, 1..30 layers, each a grating with p 0.3 and at least one,
     K 2..5 random edges, n 1.0..2.5 + i 0..0.05, films likewise, period 0.5..1.5, lambda 0.4..1.6,
-    theta 0..70, TE/TM), 20 % conical (M 20..60, built like config 3), 10 % 2-D (Mx = My 5..12,
-    built like config 4). Returns (kind, stack, args) tuples. With repeat > 1 every drawn request is
+    theta 0..70, TE/TM), 20 % conical (M 20..60, built like the conical workload), 10 % 2-D (Mx = My 5..12,
+    built like the 2-D workload). Returns (kind, stack, args) tuples. With repeat > 1 every drawn request is
     followed by repeat - 1 more of the same structure and truncation at new seeded points (a client
     scanning wavelengths and angles of one design)."""
     from stablercwa_gb300 import Layer, Stack
@@ -713,11 +713,11 @@ def serve_requests(seed, count, repeat=1):
             out.append(("1d", stack, dict(wavelength=rng.uniform(0.4, 1.6), theta=rng.uniform(0.0, 70.0),
                                           M=int(rng.integers(20, 151)), pol=int(rng.integers(0, 2)))))
         elif u < 0.9:
-            stack, _ = workload_c3(int(rng.integers(0, 1 << 30)))
+            stack, _ = workload_conical(int(rng.integers(0, 1 << 30)))
             out.append(("conical", stack, dict(wavelength=rng.uniform(0.5, 1.6), theta=rng.uniform(0.0, 60.0),
                                                phi=rng.uniform(0.0, 90.0), M=int(rng.integers(20, 61)))))
         else:
-            stack, pts, _ = workload_c4(int(rng.integers(0, 1 << 30)))
+            stack, pts, _ = workload_crossed2d(int(rng.integers(0, 1 << 30)))
             Mx = int(rng.integers(5, 13))
             out.append(("2d", stack, dict(wavelength=rng.uniform(0.4, 1.2), M1=Mx, M2=Mx, jones=(pts[0][3], pts[0][4]))))
         kind, stack, a = out[-1]
@@ -900,12 +900,12 @@ def main():
     ap.add_argument("--eig-group", type=int, default=0)
     ap.add_argument("--cpu-points", type=int, default=128)
     ap.add_argument("--points", type=int, default=N_POINTS,
-                    help="C2 points per step (the headline is 4096; fewer only for small profiling captures)")
+                    help="sweep points per step (the headline is 4096; fewer only for small profiling captures)")
     ap.add_argument("--ref-points", type=int, default=128)
     ap.add_argument("--plain-points", type=int, default=32,
                     help="points of the plain one-solve-per-call line in the headline run (0: skip)")
     ap.add_argument("--lossy-steps", type=int, default=1,
-                    help="timed steps of the absorbing-grating C2 line in the headline run (0: skip)")
+                    help="timed steps of the absorbing-grating sweep line in the headline run (0: skip)")
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-slots", type=int, default=48)
     ap.add_argument("--serve-repeat", type=int, default=8,
@@ -913,8 +913,9 @@ def main():
     ap.add_argument("--serve-sample", type=int, default=40,
                     help="requests of the serving mix run in the headline line (0: skip)")
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[0.5, 1.0])
-    ap.add_argument("--workload", choices=["c2", "c3", "c4", "plain", "serve"], default="c2",
-                    help="c2 (default, the headline line), c3 conical, c4 2-D, plain one-point-per-call")
+    ap.add_argument("--workload", choices=["sweep", "conical", "crossed2d", "plain", "serve"], default="sweep",
+                    help="sweep (default, the headline line), conical, crossed2d (2-D), plain one-point-per-call, "
+                         "serve (the serving mix)")
     ap.add_argument("--hermitian", action="store_true", help="--eig-only: lossless matrices, Hermitian solver")
     ap.add_argument("--eig-only", nargs=2, type=int, metavar=("N", "BATCH"), default=None,
                     help="profiling case: the eigensolver alone on BATCH layer matrices of order N")
@@ -929,7 +930,7 @@ def main():
         return run_reference(args)
     if args.workload == "serve":
         return run_serve(args)
-    if args.workload != "c2":
+    if args.workload != "sweep":
         return run_secondary(args)
     return run_ours(args)
 

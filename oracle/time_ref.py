@@ -4,7 +4,7 @@
 
 Builds oracle/_ref/ref_solve1d from the StableRCWA sources in place (oracle/build.py; needs the
 reference checkout, $STABLERCWA_REFERENCE or /root/reference), then solves the same sample of the
-benchmark's C2 points (TE and TM) with both on the same number of host threads and prints one JSON line:
+benchmark's headline sweep points (TE and TM) with both on the same number of host threads and prints one JSON line:
 each one's solves/s and the largest per-order efficiency difference between them. The benchmark host has
 no reference sources, so its CPU baseline is the port; this records how the two compare where both exist.
 """

@@ -34,12 +34,12 @@ EXPORTERS = [
 ]
 
 
-def write_c4_cases(path):
+def write_n441_cases(path):
     """The benchmark's seeded 2-D structure (Mx = My = 10, N = 441, 2N = 882) at six of its 256
     wavelengths: the first four and the two whose energy defect is largest, as text for the exporter."""
     sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
     import bench
-    stack, pts, _ = bench.workload_c4()
+    stack, pts, _ = bench.workload_crossed2d()
     wls = [p[0] for p in pts]
     picks = list(range(4))
     for target in (0.8462, 0.8656):
@@ -51,7 +51,7 @@ def write_c4_cases(path):
     with open(path, "w") as f:
         for k in picks:
             wl, th, ph, es, ep = pts[k]
-            f.write(f"case c4_point{k} {r(wl)} {r(th)} {r(ph)} {bench.C4_M} {bench.C4_M} "
+            f.write(f"case n441_point{k} {r(wl)} {r(th)} {r(ph)} {bench.CROSSED_M} {bench.CROSSED_M} "
                     f"{r(es.real)} {r(es.imag)} {r(ep.real)} {r(ep.imag)} 0\n")
             nii = complex(stack.nII)
             f.write(f"stack {r(float(stack.nI))} {r(nii.real)} {r(nii.imag)} {r(stack.Lx)} {r(stack.Ly)}\n")
@@ -68,7 +68,7 @@ def write_c4_cases(path):
 
 
 # fixtures made by an exporter in a second mode: (source, output, writer of the exporter's input)
-LISTED = [("export_rcwa2d.cpp", "rcwa2d_c4_cases.jsonl.gz", write_c4_cases)]
+LISTED = [("export_rcwa2d.cpp", "rcwa2d_n441_cases.jsonl.gz", write_n441_cases)]
 
 
 def gzip_into(plain, dest):

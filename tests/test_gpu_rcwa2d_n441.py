@@ -2,7 +2,7 @@
 per patterned layer) against the reference's own rcwa::solve2d (include/stablercwa/rcwa2d.hpp:1359) on
 six wavelengths of the seeded three-pillar, five-film structure: the first four and the two whose
 energy defect is largest (the reference itself gives 1.1e-11 and 3.4e-12 there). Fixture:
-tests/golden/rcwa2d_c4_cases.jsonl.gz, written by tests/golden/make_golden.py."""
+tests/golden/rcwa2d_n441_cases.jsonl.gz, written by tests/golden/make_golden.py."""
 import numpy as np
 import pytest
 
@@ -23,28 +23,28 @@ ILL_CONDITIONED_FACTOR = 1.5
 
 
 @pytest.fixture(scope="module")
-def c4():
-    cases = load_jsonl("rcwa2d_c4_cases.jsonl.gz")
+def crossed():
+    cases = load_jsonl("rcwa2d_n441_cases.jsonl.gz")
     assert len(cases) == 6 and all(c["M1"] == c["M2"] == 10 for c in cases)
     return cases
 
 
 @pytest.fixture(scope="module")
-def solved(c4):
+def solved(crossed):
     from stablercwa_gb300.engine import Engine
     eng = Engine()
     try:
-        stack = stack2d_from_json(c4[0]["stack"])
-        assert all(c["stack"] == c4[0]["stack"] for c in c4)  # one structure, six wavelengths: one batched call
-        pts = [(c["wavelength"], c["theta"], c["phi"], complex(*c["jones"][0]), complex(*c["jones"][1])) for c in c4]
+        stack = stack2d_from_json(crossed[0]["stack"])
+        assert all(c["stack"] == crossed[0]["stack"] for c in crossed)  # one structure, six wavelengths: one batched call
+        pts = [(c["wavelength"], c["theta"], c["phi"], complex(*c["jones"][0]), complex(*c["jones"][1])) for c in crossed]
         return eng.solve2d_arrays(stack, pts, 10, 10)
     finally:
         eng.close()
 
 
-def test_c4_efficiencies_match_reference(c4, solved):
+def test_n441_efficiencies_match_reference(crossed, solved):
     worst = 0.0
-    for k, c in enumerate(c4):
+    for k, c in enumerate(crossed):
         ref = c["ref"]
         assert solved["status"][k] == ref["status"] == 0, c["name"]
         assert solved["eig_info"][k] == ref["eig_info"], c["name"]
@@ -53,12 +53,12 @@ def test_c4_efficiencies_match_reference(c4, solved):
             d = float(np.max(np.abs(solved[key][k] - rvec(ref[key]))))
             assert d <= DE_TOL, (c["name"], key, d)
             worst = max(worst, d)
-    print(f"C4 worst |dDE| vs reference {worst:.2e}")
+    print(f"N = 441 worst |dDE| vs reference {worst:.2e}")
 
 
-def test_c4_energy_no_worse_than_reference(c4, solved):
+def test_n441_energy_no_worse_than_reference(crossed, solved):
     rows = []
-    for k, c in enumerate(c4):
+    for k, c in enumerate(crossed):
         ref = c["ref"]
         e_ref = abs(float(np.sum(rvec(ref["DEr"])) + np.sum(rvec(ref["DEt"]))) - 1.0)
         e_gpu = abs(float(np.sum(solved["DEr"][k]) + np.sum(solved["DEt"][k])) - 1.0)

@@ -162,10 +162,10 @@ def test_near_fields_match_reference(oracle):
     assert len(cases) >= 28
 
 
-def test_c4_point_against_reference(oracle):
-    """One point of the 2-D C4 workload (Mx = My = 10: N = 441, eigenproblems of order 882) through the oracle
+def test_n441_point_against_reference(oracle):
+    """One point of the benchmark's 2-D workload (Mx = My = 10: N = 441, eigenproblems of order 882) through the oracle
     against the reference's own solve2d output for it: efficiencies within 1e-10 (about a minute on one core)."""
-    with gzip.open(os.path.join(HERE, "golden", "rcwa2d_c4_cases.jsonl.gz"), "rt") as f:
+    with gzip.open(os.path.join(HERE, "golden", "rcwa2d_n441_cases.jsonl.gz"), "rt") as f:
         c = json.loads(f.readline())
     assert (c["M1"], c["M2"]) == (10, 10)
     r = solve(oracle, {**c, "laurent": c.get("laurent", 0)})
