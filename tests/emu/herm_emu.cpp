@@ -52,6 +52,9 @@ unsigned emu_ballot(int p) {
 using namespace rcwa_gb300;
 
 static int failures = 0;
+// the shared reduction slots of a CTA form (G > 32 lanes: herm_reduce_block_kernel's red and ired)
+static double cta_red[8];
+static int cta_ired[8];
 
 // herm_apply_real_kernel for one matrix: each CTA (32 rows) as 32 threads meeting at one barrier, since the
 // warp stages the rotation log through shared memory
@@ -84,7 +87,7 @@ void run(int n, const std::vector<zc>& a, const char* tag, bool real_form, bool 
     for (int l = 0; l < G; ++l)
         th.emplace_back([&, l] {
             threadIdx.x = l;
-            herm_tridiag_one<G>(n, a.data(), V.data(), ws.data(), nullptr, nullptr);
+            herm_tridiag_one<G>(n, a.data(), V.data(), ws.data(), G > 32 ? cta_red : nullptr, G > 32 ? cta_ired : nullptr);
         });
     for (auto& t : th) t.join();
     unsigned long long rot = 0;
@@ -404,6 +407,111 @@ void run_blocked(int n, const std::vector<zc>& a, const char* tag) {
     if (!ok) ++failures;
 }
 
+// Layer matrices of a lossless binary grating (ridge index nr, groove ng, ridge fill f of the period,
+// lambda / period = lp, sin(theta) = st) at order n = 2M + 1, as the engine forms them: TE the Hermitian
+// Kx^2 - [[eps]]; TM the pencil matrix L^-1 (Kx E Kx - I) L^-H with E the Hermitian part of [[eps]]^-1,
+// [[1/eps]] = L L^H and L^-1 formed explicitly; coefficients made exactly conjugate-symmetric first.
+static std::vector<zc> grating_coefficients(int M, double f, zc v_ridge, zc v_groove) {
+    const int H = 2 * M;
+    std::vector<zc> c(2 * H + 1);
+    for (int h = 0; h <= H; ++h) {
+        zc w;
+        if (h == 0) {
+            w = v_ridge * f + v_groove * (1.0 - f);
+        } else {  // (1/P) integral of the profile exp(-2 pi i h x / P): ridge on [0, f P), groove after
+            const double t = 2.0 * 3.14159265358979323846 * h;
+            const zc e{std::cos(t * f), -std::sin(t * f)};  // exp(-i t f)
+            const zc one{1.0, 0.0};
+            const zc ridge = (e - one) * zc{0.0, 1.0 / t};   // (exp(-i t f) - 1) / (-i t)
+            const zc groove = (one - e) * zc{0.0, 1.0 / t};
+            w = v_ridge * ridge + v_groove * groove;
+        }
+        c[H + h] = w;
+        c[H - h] = conj(w);
+    }
+    return c;
+}
+
+static std::vector<zc> inverse(int n, std::vector<zc> a) {  // Gauss-Jordan, partial pivoting, column-major
+    std::vector<zc> x((size_t)n * n, zc{0.0, 0.0});
+    for (int i = 0; i < n; ++i) x[(size_t)i * n + i] = zc{1.0, 0.0};
+    for (int k = 0; k < n; ++k) {
+        int p = k;
+        for (int i = k + 1; i < n; ++i)
+            if (zabs(a[(size_t)k * n + i]) > zabs(a[(size_t)k * n + p])) p = i;
+        for (int j = 0; j < n; ++j) {
+            std::swap(a[(size_t)j * n + k], a[(size_t)j * n + p]);
+            std::swap(x[(size_t)j * n + k], x[(size_t)j * n + p]);
+        }
+        const zc piv = a[(size_t)k * n + k];
+        const zc r = zinv(piv);
+        for (int j = 0; j < n; ++j) {
+            a[(size_t)j * n + k] = a[(size_t)j * n + k] * r;
+            x[(size_t)j * n + k] = x[(size_t)j * n + k] * r;
+        }
+        for (int i = 0; i < n; ++i) {
+            if (i == k) continue;
+            const zc m = a[(size_t)k * n + i];
+            if (m.re == 0.0 && m.im == 0.0) continue;
+            for (int j = 0; j < n; ++j) {
+                a[(size_t)j * n + i] = a[(size_t)j * n + i] - m * a[(size_t)j * n + k];
+                x[(size_t)j * n + i] = x[(size_t)j * n + i] - m * x[(size_t)j * n + k];
+            }
+        }
+    }
+    return x;
+}
+
+static std::vector<zc> matmul(int n, const std::vector<zc>& a, const std::vector<zc>& b) {
+    std::vector<zc> c((size_t)n * n, zc{0.0, 0.0});
+    for (int j = 0; j < n; ++j)
+        for (int k = 0; k < n; ++k) {
+            const zc bkj = b[(size_t)j * n + k];
+            for (int i = 0; i < n; ++i) c[(size_t)j * n + i] = c[(size_t)j * n + i] + a[(size_t)k * n + i] * bkj;
+        }
+    return c;
+}
+
+static std::vector<zc> grating_matrix(int M, bool tm, double nr, double ng, double f, double lp, double st) {
+    const int n = 2 * M + 1, H = 2 * M;
+    const std::vector<zc> ce = grating_coefficients(M, f, zc{nr * nr, 0.0}, zc{ng * ng, 0.0});
+    std::vector<zc> E((size_t)n * n);
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) E[(size_t)j * n + i] = ce[i - j + H];
+    std::vector<double> kx(n);
+    for (int i = 0; i < n; ++i) kx[i] = st - (i - M) * lp;
+    if (!tm) {
+        for (auto& z : E) z = zc{-z.re, -z.im};
+        for (int i = 0; i < n; ++i) E[(size_t)i * n + i].re += kx[i] * kx[i];
+        return E;
+    }
+    const std::vector<zc> ci = grating_coefficients(M, f, zc{1.0 / (nr * nr), 0.0}, zc{1.0 / (ng * ng), 0.0});
+    std::vector<zc> L((size_t)n * n, zc{0.0, 0.0});
+    for (int j = 0; j < n; ++j)
+        for (int i = j; i < n; ++i) L[(size_t)j * n + i] = ci[i - j + H];
+    for (int j = 0; j < n; ++j) {  // right-looking Cholesky, as toeplitz_cholesky_kernel
+        const double piv = std::sqrt(L[(size_t)j * n + j].re);
+        L[(size_t)j * n + j] = zc{piv, 0.0};
+        for (int i = j + 1; i < n; ++i) L[(size_t)j * n + i] = L[(size_t)j * n + i] * (1.0 / piv);
+        for (int k = j + 1; k < n; ++k)
+            for (int i = k; i < n; ++i)
+                L[(size_t)k * n + i] = L[(size_t)k * n + i] - L[(size_t)j * n + i] * conj(L[(size_t)j * n + k]);
+    }
+    const std::vector<zc> Li = inverse(n, L);
+    std::vector<zc> LiH((size_t)n * n);
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) LiH[(size_t)j * n + i] = conj(Li[(size_t)i * n + j]);
+    const std::vector<zc> Ei = inverse(n, E);
+    std::vector<zc> B((size_t)n * n);
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+            const zc a = Ei[(size_t)j * n + i], b = Ei[(size_t)i * n + j];
+            const zc h{0.5 * (a.re + b.re), 0.5 * (a.im - b.im)};
+            B[(size_t)j * n + i] = h * (kx[i] * kx[j]) - zc{i == j ? 1.0 : 0.0, 0.0};
+        }
+    return matmul(n, Li, matmul(n, B, LiH));
+}
+
 // the general solver (CORTH + COMQR2, eig_one) with G lanes or a CTA of G threads per matrix
 template <int G>
 void run_general(int n, const std::vector<zc>& a, const char* tag) {
@@ -527,6 +635,15 @@ int main() {
             }
         run_blocked<16>(n, r, "random");
         run_blocked<8>(n, t, "toeplitz");
+    }
+    {  // order 301 (M = 150), high index contrast: the CTA form a lone solve takes (128 threads), and the
+       // blocked form with a warp (a few hundred matrices) or 16 lanes (thousands) per matrix
+        const std::vector<zc> tm_si = grating_matrix(150, true, 3.48, 1.0, 0.37, 0.6, 0.5);
+        const std::vector<zc> te_si = grating_matrix(150, false, 3.48, 1.0, 0.37, 0.6, 0.5);
+        const std::vector<zc> tm_ge = grating_matrix(150, true, 4.0, 1.0, 0.5, 1.3, std::sin(85.0 * 3.14159265358979323846 / 180.0));
+        run<128>(301, tm_si, "tm-pencil-n3.48", true, true);
+        run_blocked<32>(301, te_si, "te-n3.48");
+        run_blocked<16>(301, tm_ge, "tm-pencil-n4.0-grazing");
     }
     for (int n : {1, 2, 5, 17, 30}) {
         std::vector<zc> g((size_t)n * n);
