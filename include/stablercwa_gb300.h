@@ -416,7 +416,8 @@ int rcwa_gpu_eig_hermitian_batch_dev(rcwa_gpu_ctx* ctx, int n, int batch, const 
  * The first call with a device current looks up that device's array and loads the kernels; make it
  * before any stream capture begins on the device. Calls that overlap in time on one device (on
  * different streams, or unordered host threads) share the array and race; calls on one stream are
- * ordered. Errors are reported by the return code only. */
+ * ordered. It never starts the autotuner (tuning allocates trial buffers): a form recorded for the key
+ * is used, else the built-in rule. Errors are reported by the return code only. */
 #define RCWA_GPU_EIG_STATIC_SCRATCH_BYTES (64ULL << 20)
 int rcwa_gpu_eig_batch_static(void* stream, int n, int batch, const rcwa_complex* d_a, double eps,
                               int max_iter, rcwa_complex* d_values, rcwa_complex* d_vectors, int* d_info,
@@ -464,7 +465,7 @@ int rcwa_gpu_autotune_set(int hermitian, int n, int batch, int form);
 int rcwa_gpu_autotune_table(char* buffer, size_t size);
 
 /* No reference counterpart: how the engine forms its complex products. Products whose three orders are
- * all >= 32 run on the tensor cores (tcgen05, bf16 digit slices of each FP64 operand, exact FP32
+ * all >= 16 with m n k >= 2^15 run on the tensor cores (tcgen05, bf16 digit slices of each FP64 operand, exact FP32
  * accumulation of the slice products, FP64 sums: accurate to about k 2^-53 of the largest entries of
  * the row and column, like an FP64 GEMM) unless RCWA_GB300_GEMM=fp64 is set, in which case every product
  * runs on the FP64 pipe. *tensor_cores: 1 when the tensor-core path is on; *slices: digits per operand
@@ -535,7 +536,8 @@ int rcwa_gpu_server_submit(rcwa_gpu_server* server, const rcwa_request* request,
 /* Waits up to timeout_ms (< 0: forever) for the request, then copies its result into result (an
  * rcwa_result1d*, rcwa_result_conical* or rcwa_result2d* of host arrays sized for one point, by
  * kind; may be NULL) and releases it. Returns RCWA_OK, RCWA_ETIMEOUT if it has not finished, or
- * RCWA_ECANCELLED if the server was destroyed before the request started. */
+ * RCWA_ECANCELLED if the server was destroyed before the request started. A ticket is released by the
+ * first wait that returns its result; any other wait on it, concurrent or later, returns RCWA_EINVAL. */
 int rcwa_gpu_server_wait(rcwa_gpu_server* server, unsigned long long ticket, int timeout_ms, rcwa_response* response,
                          void* result);
 /* ---- JSON front end ------------------------------------------------------------------------- */

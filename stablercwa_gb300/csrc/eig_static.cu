@@ -15,9 +15,13 @@
 // it belongs to; a call under another context (after cudaDeviceReset, or with a context of the
 // caller's own) repeats the set-up instead of using a stale address. Every call uses the same array,
 // so calls that overlap in time on one device (issued on different streams, or from several host
-// threads without ordering) race on it; calls on one stream are ordered and safe. The lanes per
-// matrix are chosen exactly as rcwa_gpu_eig_batch_dev chooses them (RCWA_GB300_EIG_GROUP included),
-// so both entry points run the same kernel on the same inputs.
+// threads without ordering) race on it; calls on one stream are ordered and safe. The kernel form
+// (lanes per matrix, a CTA or a thread-block cluster per matrix) is chosen as rcwa_gpu_eig_batch_dev
+// chooses it: RCWA_GB300_EIG_GROUP when set, else a form the autotuner has recorded for the order and
+// batch, else the built-in rule. This entry never starts the autotuner itself, because tuning allocates
+// its trial buffers; with RCWA_GB300_AUTOTUNE=auto the allocating entry may tune a key that this one
+// then leaves on the built-in rule until a table entry exists, so the two agree to rounding, not bit
+// for bit, in that case only.
 #include <cstdlib>
 #include <mutex>
 
@@ -89,6 +93,7 @@ int scratch_for_current_context(zc** out) {
             load_kernel<32>() != cudaSuccess || load_kernel<64>() != cudaSuccess || load_kernel<128>() != cudaSuccess ||
             load_kernel<256>() != cudaSuccess)
             return RCWA_ECUDA;
+        rcwa_gb300::preload_eig_cluster_kernel();  // the cluster form too (a few matrices of order >= 384)
         d.scratch = static_cast<zc*>(p);
         d.ctx_id = current_context_id();  // the symbol lookup made the device's context current
     }
@@ -114,6 +119,8 @@ extern "C" int rcwa_gpu_eig_batch_static(void* stream, int n, int batch, const r
 
     int group = 0;
     if (const char* g = std::getenv("RCWA_GB300_EIG_GROUP")) group = std::atoi(g);
+    if (group == 0) group = tuned_eig_form(0, n, batch);  // a recorded form; never a tuning run
+    if (group == 0) group = eig_cluster_wanted(n, batch) ? -1 : eig_default_group(n, batch);
     try {
         launch_eig(static_cast<cudaStream_t>(stream), n, batch, reinterpret_cast<const zc*>(d_a), (long long)n * n,
                    reinterpret_cast<zc*>(d_values), reinterpret_cast<zc*>(d_vectors), d_info, d_sweeps, ws, eps,

@@ -760,17 +760,23 @@ int rcwa_gpu_server_wait(rcwa_gpu_server* s, unsigned long long ticket, int time
     std::unique_ptr<Job> j;
     {
         std::unique_lock<std::mutex> lk(s->m);
-        auto it = s->jobs.find(ticket);
-        if (it == s->jobs.end()) return RCWA_EINVAL;
-        Job* p = it->second.get();
+        if (s->jobs.find(ticket) == s->jobs.end()) return RCWA_EINVAL;
+        // the job is looked up again on every wake-up: another thread waiting on the same ticket may have
+        // taken (and freed) it meanwhile
+        const auto ready = [&] {
+            const auto it = s->jobs.find(ticket);
+            return it == s->jobs.end() || it->second->done;
+        };
         ++s->waiters;
         bool finished = true;
-        if (timeout_ms < 0) s->cv_done.wait(lk, [&] { return p->done; });
-        else finished = s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return p->done; });
+        if (timeout_ms < 0) s->cv_done.wait(lk, ready);
+        else finished = s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready);
         if (--s->waiters == 0 && s->stop) s->cv_idle.notify_all();
         if (!finished) return RCWA_ETIMEOUT;
-        j = std::move(s->jobs[ticket]);
-        s->jobs.erase(ticket);
+        const auto it = s->jobs.find(ticket);
+        if (it == s->jobs.end()) return RCWA_EINVAL;  // released by a concurrent wait on the same ticket
+        j = std::move(it->second);
+        s->jobs.erase(it);
     }
     if (resp) *resp = rcwa_response{j->code, j->slot, j->submit_s, j->start_s, j->finish_s, j->footprint, j->batch};
     if (result) {
