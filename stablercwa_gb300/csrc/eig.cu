@@ -70,12 +70,47 @@ void launch_eig(cudaStream_t st, int n, int batch, const zc* a, long long a_stri
 // QL rotations applied by the Hermitian eigensolver since the last read (the work of its sweeps, 12 n flops
 // each, for the benchmark's roofline)
 unsigned long long* rotation_counter() {
-    static unsigned long long* d = nullptr;
-    if (!d) {
-        RCWA_CUDA(cudaMalloc(&d, sizeof(unsigned long long)));
-        RCWA_CUDA(cudaMemset(d, 0, sizeof(unsigned long long)));
+    return static_cast<unsigned long long*>(device_word(0, sizeof(unsigned long long)));
+}
+
+void* device_word(int which, size_t bytes) {
+    static std::mutex lock;
+    static std::vector<std::vector<void*>> words;  // [which][device]
+    int dev = 0;
+    RCWA_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(lock);
+    if ((int)words.size() <= which) words.resize(which + 1);
+    std::vector<void*>& per_device = words[which];
+    if ((int)per_device.size() <= dev) per_device.resize(dev + 1, nullptr);
+    if (!per_device[dev]) {
+        void* d = nullptr;
+        RCWA_CUDA(cudaMalloc(&d, bytes));
+        const cudaError_t rc = cudaMemset(d, 0, bytes);
+        if (rc != cudaSuccess) {
+            cudaFree(d);
+            RCWA_CUDA(rc);
+        }
+        per_device[dev] = d;
     }
-    return d;
+    return per_device[dev];
+}
+
+void ensure_smem_optin(const void* func, int bytes) {
+    static std::mutex lock;
+    static std::vector<std::pair<std::pair<const void*, int>, int>> done;  // ((func, device), bytes)
+    int dev = 0;
+    RCWA_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(lock);
+    for (auto& e : done)
+        if (e.first.first == func && e.first.second == dev) {
+            if (bytes > e.second) {
+                RCWA_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+                e.second = bytes;
+            }
+            return;
+        }
+    RCWA_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    done.push_back({{func, dev}, bytes});
 }
 long long take_rotation_count() {
     unsigned long long h = 0;
@@ -256,14 +291,7 @@ void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a
             default: herm_dc_launch<32>(st, n, batch, ws, y, w, info, eps, max_iter); break;
         }
     } else if (qsm <= 227 * 1024) {
-        if (qsm > 48 * 1024) {
-            static int opted = 0;  // the largest opt-in requested so far
-            if ((int)qsm > opted) {
-                RCWA_CUDA(cudaFuncSetAttribute(herm_ql_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)qsm));
-                opted = (int)qsm;
-            }
-        }
+        if (qsm > 48 * 1024) ensure_smem_optin(reinterpret_cast<const void*>(herm_ql_kernel<true, true>), (int)qsm);
         // the real form's log is fixed point (herm_apply_real_kernel); the shared-memory form implies it
         herm_ql_kernel<true, true><<<(unsigned)((batch + kHermQlThreads - 1) / kHermQlThreads), kHermQlThreads, qsm, st>>>(
             n, batch, w, info, ws, eps, max_iter, rotation_counter());
@@ -280,14 +308,7 @@ void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a
     herm_overflow_kernel<<<(unsigned)((batch + 127) / 128), 128, 0, st>>>(n, batch, ws, only);
     RCWA_CUDA(cudaGetLastError());
     if (real_form) {
-        if (ysm > 48 * 1024) {
-            static int opted = 0;  // the largest opt-in requested so far (the attribute is per function)
-            if ((int)ysm > opted) {
-                RCWA_CUDA(cudaFuncSetAttribute(herm_apply_real_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)ysm));
-                opted = (int)ysm;
-            }
-        }
+        if (ysm > 48 * 1024) ensure_smem_optin(reinterpret_cast<const void*>(herm_apply_real_kernel), (int)ysm);
         if (!dc) {  // divide and conquer has left Y in y already
             const dim3 grid((unsigned)batch, (unsigned)((n + kHermRows - 1) / kHermRows));
             herm_apply_real_kernel<<<grid, kHermRows, ysm, st>>>(n, batch, y, ws, info);

@@ -597,17 +597,28 @@ namespace rcwa_gb300 {
 namespace {
 
 // cluster size for the kernel at this shared-memory size: 16 CTAs when the device can co-schedule them,
-// else 8, else 0 (no cluster form); decided once per order
+// else 8, else 0 (no cluster form); decided once per (device, order). The kernel's dynamic shared memory
+// opt-in only ever grows (ensure_smem_optin), so a launch of one order never finds it lowered by a
+// concurrent call for a smaller order.
 int cluster_size_for(int n) {
     static std::mutex lock;
-    static int cached_n = -1, cached_c = 0;
+    static std::vector<std::pair<std::pair<int, int>, int>> sizes;  // ((device, order), cluster size)
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     std::lock_guard<std::mutex> g(lock);
-    if (n == cached_n) return cached_c;
+    for (const auto& e : sizes)
+        if (e.first.first == dev && e.first.second == n) return e.second;
     const size_t smem = eig_cluster_smem_bytes(n);
     int c = 0;
-    if (smem <= 200 * 1024 && n <= kMaxCarry * kCT &&
-        cudaFuncSetAttribute(eig_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess &&
-        cudaFuncSetAttribute(eig_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+    bool opted = false;
+    if (smem <= 200 * 1024 && n <= kMaxCarry * kCT) {
+        try {
+            ensure_smem_optin(reinterpret_cast<const void*>(eig_cluster_kernel), (int)smem);
+            opted = true;
+        } catch (const EngineError&) {
+        }
+    }
+    if (opted && cudaFuncSetAttribute(eig_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
         for (int want : {16, 8}) {
             cudaLaunchConfig_t cfg = {};
             cudaLaunchAttribute attr[1];
@@ -628,8 +639,7 @@ int cluster_size_for(int n) {
         }
     }
     cudaGetLastError();  // a refused size leaves no error behind
-    cached_n = n;
-    cached_c = c;
+    sizes.push_back({{dev, n}, c});
     return c;
 }
 

@@ -141,6 +141,12 @@ void launch_eig(cudaStream_t st, int n, int batch, const zc* a, long long a_stri
 // eigenvectors in v; info as launch_eig.
 void launch_eig_herm(cudaStream_t st, int n, int batch, const zc* a, long long a_stride, zc* w, zc* v, int* info, zc* ws,
                      double eps, int max_iter, int group);
+// Per-device launcher state, safe for several host threads and several devices in one process: a zeroed
+// device word per (use, device), allocated on its first use with that device current (which 0: the
+// rotation counter, 1: the tensor-core products' stuck-wait flag); and a dynamic shared memory opt-in of
+// func for the current device, made once per (func, device) and raised when a larger size is needed.
+void* device_word(int which, size_t bytes);
+void ensure_smem_optin(const void* func, int bytes);
 unsigned long long* rotation_counter();  // device counter the Hermitian eigensolver adds its QL rotations to
 long long take_rotation_count();         // read and reset it (synchronises the device)
 long long eig_workspace_bytes(int n, int batch);

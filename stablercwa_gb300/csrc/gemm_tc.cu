@@ -934,15 +934,7 @@ Plan make_plan(int S, int kblocks) {
     return p;
 }
 
-int* error_flag() {
-    static int* d = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        if (cudaMalloc(&d, sizeof(int)) != cudaSuccess || cudaMemset(d, 0, sizeof(int)) != cudaSuccess) d = nullptr;
-    });
-    if (!d) throw EngineError{RCWA_ECUDA, "tensor-core GEMM: no error flag"};
-    return d;
-}
+int* error_flag() { return static_cast<int*>(device_word(1, sizeof(int))); }
 
 }  // namespace
 
@@ -999,16 +991,8 @@ void tc_product(cudaStream_t st, int m, int n, int k, int batch, const zc* A, in
     const bool resident = tc_gemm_resident();
     const int smem_bytes = resident ? 2 * kBStage + kARing * kATile + 1024 + (int)sizeof(SharedStateR) + 64
                                     : kStages * kStageBytes + 1024 + (int)sizeof(SharedState) + 64;
-    static std::once_flag attr_once;
-    static cudaError_t attr_rc = cudaSuccess;
-    std::call_once(attr_once, [&] {
-        attr_rc = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       kStages * kStageBytes + 1024 + (int)sizeof(SharedState) + 64);
-        if (attr_rc == cudaSuccess)
-            attr_rc = cudaFuncSetAttribute(tc_gemm_resident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           2 * kBStage + kARing * kATile + 1024 + (int)sizeof(SharedStateR) + 64);
-    });
-    RCWA_CUDA(attr_rc);
+    if (resident) ensure_smem_optin(reinterpret_cast<const void*>(tc_gemm_resident_kernel), smem_bytes);
+    else ensure_smem_optin(reinterpret_cast<const void*>(tc_gemm_kernel), smem_bytes);
     const int real_b = Br != nullptr;
     const int S = tc_gemm_slices();
     const int kin = real_b ? k : 2 * k;
